@@ -1,0 +1,1284 @@
+// CPU oracle for the flip-graph hot path -- TEST INFRASTRUCTURE ONLY.
+//
+// Restates, operation for operation, the reference's search-path algorithms
+// (dronperminov/FlipGraphGPU; citations are path:line in that project):
+//   FlipSet                      src/entities/flip_set.cu:1-43
+//   SchemeZ2 walk algebra        src/schemes/scheme_z2.cu:3-182,531-641,982-1154
+//   Addition (ternary vector)    src/entities/addition.cu:1-232
+//   SchemeInteger walk algebra   src/schemes/scheme_integer.cu:3-147,229-269,398-571,907-1101
+//   randint / randomPermutation  src/utils/random.cuh:5-22
+//   randomWalkKernel             src/entities/flip_graph.cu:520-573
+//   minimizeKernel               src/entities/complexity_minimizer.cu:190-214
+//   AdditionsReducer / PairsCounter / runReducersKernel
+//                                src/entities/additions_reducer.cuh, pairs_counter.cuh,
+//                                src/entities/scheme_additions_reducer.cu:463-540
+// It is the checker of the CUDA library, never the thing measured or shipped.
+//
+// Draws come from a policy object: RefDraws replays a recorded cuRAND XORWOW
+// tape (curand() words and curand_uniform() floats recorded on the GPU), and
+// reproduces the reference's stream; FastDraws is the library's fast-mode
+// stream (Philox4x32-10, Salmon et al. SC'11) with cheaper draw sites:
+// multiply-high instead of modulo, integer thresholds instead of float gates,
+// and no draw for a gate whose probability is zero.  Control flow is the
+// same for both, so one implementation serves both modes.
+//
+// The reference's unbounded retry loops (scheme_z2.cu:1036, scheme_integer.cu:984,1029)
+// are bounded by kRetryCap; hitting it sets status bit 2 (the reference would hang).
+#include "fg_oracle.h"
+
+#include <algorithm>
+#include <cstdlib>
+#include <cstring>
+#include <cmath>
+#include <unordered_map>
+#include <vector>
+
+namespace {
+
+constexpr int kMaxRank = 350;   // config.cuh:10
+constexpr int kMaxPairs = 500;  // config.cuh:14
+constexpr int kRetryCap = 1 << 20;
+enum { ST_TAPE = 1, ST_RETRY = 2, ST_OVERFLOW = 4 };
+
+inline int popc64(uint64_t x) { return __builtin_popcountll(x); }
+
+// ------------------------------------------------------------ Philox4x32-10
+void philox(const uint32_t c_in[4], const uint32_t k_in[2], uint32_t out[4]) {
+    uint32_t c0 = c_in[0], c1 = c_in[1], c2 = c_in[2], c3 = c_in[3];
+    uint32_t k0 = k_in[0], k1 = k_in[1];
+    for (int r = 0; r < 10; r++) {
+        if (r > 0) { k0 += 0x9E3779B9u; k1 += 0xBB67AE85u; }
+        uint64_t p0 = (uint64_t)0xD2511F53u * c0;
+        uint64_t p1 = (uint64_t)0xCD9E8D57u * c2;
+        uint32_t n0 = (uint32_t)(p1 >> 32) ^ c1 ^ k0;
+        uint32_t n1 = (uint32_t)p1;
+        uint32_t n2 = (uint32_t)(p0 >> 32) ^ c3 ^ k1;
+        uint32_t n3 = (uint32_t)p0;
+        c0 = n0; c1 = n1; c2 = n2; c3 = n3;
+    }
+    out[0] = c0; out[1] = c1; out[2] = c2; out[3] = c3;
+}
+
+// ------------------------------------------------------------ draw policies
+struct RefDraws {
+    const uint32_t *d = nullptr;
+    const float *u = nullptr;
+    int64_t n = 0, pos = 0;
+    int32_t *status = nullptr;
+    uint32_t raw() {
+        if (pos >= n) { *status |= ST_TAPE; return 0; }
+        return d[pos++];
+    }
+    float uniform() {
+        if (pos >= n) { *status |= ST_TAPE; return 1.0f; }
+        return u[pos++];
+    }
+    uint32_t below(uint32_t k) { return raw() % k; }             // curand() % k
+    bool coin() { return raw() % 2; }                              // curand() % 2
+    // curand_uniform(&state) * maxIterations < p   (flip_graph.cu:550-562)
+    bool gate(double p, int iters) { float x = uniform(); return (double)(x * (float)iters) < p; }
+    bool tie() { return (double)uniform() < 0.01; }              // flip_graph.cu:545
+    uint64_t mask(int nn) { return (uint64_t)raw() % ((uint64_t)1 << nn); }  // scheme_z2.cu:1064
+};
+
+// Fast-mode stream: word q of walk w is Philox(ctr = (q/4 lo, q/4 hi, w, 0), key = seed)[q%4].
+struct FastDraws {
+    uint32_t key[2] = {0, 0};
+    uint32_t walk = 0;
+    int64_t pos = 0;
+    int64_t cached = -1;
+    uint32_t block[4];
+    int32_t *status = nullptr;
+    uint32_t raw() {
+        int64_t b = pos >> 2;
+        if (b != cached) {
+            uint32_t c[4] = {(uint32_t)b, (uint32_t)((uint64_t)b >> 32), walk, 0u};
+            philox(c, key, block);
+            cached = b;
+        }
+        return block[pos++ & 3];
+    }
+    float uniform() { return (float)(raw() >> 8) * (1.0f / 16777216.0f); }
+    uint32_t below(uint32_t k) { return (uint32_t)(((uint64_t)raw() * k) >> 32); }
+    bool coin() { return raw() >> 31; }
+    bool gate(double p, int iters) {
+        if (!(p > 0)) return false;  // can never fire: no draw
+        double q = p / (double)iters;
+        uint64_t t = q >= 1.0 ? ((uint64_t)1 << 32) : (uint64_t)(q * 4294967296.0);
+        return (uint64_t)raw() < t;
+    }
+    bool tie() { return raw() < 42949672u; }  // floor(0.01 * 2^32)
+    uint64_t mask(int nn) { return nn >= 32 ? (uint64_t)raw() : (uint64_t)(raw() & ((1u << nn) - 1u)); }
+};
+
+template <class R> inline int randint(int a, int b, R &r) { return a + (int)r.below((uint32_t)(b - a + 1)); }
+
+template <class R> inline void permutation(int *p, int n, R &r) {  // random.cuh:9-22
+    for (int i = 0; i < n; i++) p[i] = i;
+    for (int i = n - 1; i > 0; i--) {
+        int j = (int)r.below((uint32_t)(i + 1));
+        std::swap(p[i], p[j]);
+    }
+}
+
+// ------------------------------------------------------------ FlipSet
+struct FlipList {
+    int size = 0;
+    uint32_t pairs[kMaxPairs];
+    void clear() { size = 0; }
+    void add(uint32_t a, uint32_t b) {  // flip_set.cu:7-13: silently full at 500
+        if (size >= kMaxPairs) return;
+        pairs[size++] = (a << 16) | b;
+    }
+    void removeIndex(uint32_t idx) {  // flip_set.cu:27-31
+        for (int p = 0; p < size; p++)
+            if ((pairs[p] >> 16) == idx || (pairs[p] & 0xFFFFu) == idx) {
+                pairs[p] = pairs[--size];
+                p--;
+            }
+    }
+    int first(int p) const { return (int)(pairs[p] >> 16); }
+    int second(int p) const { return (int)(pairs[p] & 0xFFFFu); }
+};
+
+// ------------------------------------------------------------ Z2 scheme
+struct Z2 {
+    int n[3], nn[3], m;
+    uint64_t x[3][kMaxRank];
+    FlipList lists[3];
+    int32_t *status;
+
+    bool nonzero(int t) const { return x[0][t] && x[1][t] && x[2][t]; }
+
+    void initNaive(int n1, int n2, int n3) {  // scheme_z2.cu:32-55
+        n[0] = n1; n[1] = n2; n[2] = n3;
+        nn[0] = n1 * n2; nn[1] = n2 * n3; nn[2] = n3 * n1;
+        m = n1 * n2 * n3;
+        for (int i = 0; i < n1; i++)
+            for (int j = 0; j < n3; j++)
+                for (int k = 0; k < n2; k++) {
+                    int t = (i * n3 + j) * n2 + k;
+                    x[0][t] = (uint64_t)1 << (i * n2 + k);
+                    x[1][t] = (uint64_t)1 << (k * n3 + j);
+                    x[2][t] = (uint64_t)1 << (j * n1 + i);
+                }
+        rebuildLists();
+    }
+
+    void rebuildLists() {  // initFlips, scheme_z2.cu:141-150
+        for (int c = 0; c < 3; c++) {
+            lists[c].clear();
+            for (int a = 0; a < m; a++)
+                for (int b = a + 1; b < m; b++)
+                    if (x[c][a] == x[c][b]) lists[c].add(a, b);
+        }
+    }
+
+    void moveTerm(int dst, int src) { for (int c = 0; c < 3; c++) x[c][dst] = x[c][src]; }
+
+    void removeZeroes() {  // scheme_z2.cu:152-164 (no re-check of the moved term)
+        while (m > 0 && !nonzero(m - 1)) m--;
+        for (int t = 0; t < m; t++)
+            if (!nonzero(t)) { m--; moveTerm(t, m); }
+    }
+
+    void removeAt(int t) {  // scheme_z2.cu:166-175
+        m--;
+        if (t == m) return;
+        moveTerm(t, m);
+    }
+
+    void addTriplet(int i, int j, int k, uint64_t a, uint64_t b, uint64_t c) {  // scheme_z2.cu:177-182
+        if (m >= kMaxRank) { *status |= ST_OVERFLOW; return; }
+        x[i][m] = a; x[j][m] = b; x[k][m] = c;
+        m++;
+    }
+
+    void reduce(int i, int a, int b) {  // scheme_z2.cu:631-641
+        x[i][a] ^= x[i][b];
+        bool zero = !x[i][a];
+        removeAt(b);
+        if (zero) removeZeroes();
+        rebuildLists();
+    }
+
+    void flip(int i, int j, int k, int a, int b, bool checkReduce) {  // scheme_z2.cu:531-577
+        x[j][a] ^= x[j][b];
+        x[k][b] ^= x[k][a];
+        lists[j].removeIndex(a);
+        lists[k].removeIndex(b);
+        if (!x[j][a] || !x[k][b]) {
+            removeZeroes();
+            rebuildLists();
+            return;
+        }
+        for (int t = 0; t < m; t++) {
+            if (t != a && x[j][t] == x[j][a]) {
+                if (checkReduce) {
+                    if (x[i][t] == x[i][a]) { reduce(k, t, a); return; }
+                    if (x[k][t] == x[k][a]) { reduce(i, t, a); return; }
+                }
+                lists[j].add(a, t);
+            }
+            if (t != b && x[k][t] == x[k][b]) {
+                if (checkReduce) {
+                    if (x[i][t] == x[i][b]) { reduce(j, t, b); return; }
+                    if (x[j][t] == x[j][b]) { reduce(i, t, b); return; }
+                }
+                lists[k].add(b, t);
+            }
+        }
+    }
+
+    void plus(int i, int j, int k, int p, int q, int variant) {  // scheme_z2.cu:579-612
+        const uint64_t a1 = x[i][p], b1 = x[j][p], c1 = x[k][p];
+        const uint64_t a2 = x[i][q], b2 = x[j][q], c2 = x[k][q];
+        const uint64_t a = a1 ^ a2, b = b1 ^ b2, c = c1 ^ c2;
+        if (variant == 0) { x[j][p] = b; x[i][q] = a; addTriplet(i, j, k, a1, b2, c); }
+        else if (variant == 1) { x[k][p] = c; x[j][q] = b; addTriplet(i, j, k, a, b1, c2); }
+        else { x[i][p] = a; x[k][q] = c; addTriplet(i, j, k, a2, b, c1); }
+        if (!a || !b || !c) removeZeroes();
+        rebuildLists();
+    }
+
+    void split(int i, int j, int k, int t, uint64_t a1) {  // scheme_z2.cu:614-619
+        uint64_t a2 = x[i][t] ^ a1;
+        x[i][t] = a1;
+        addTriplet(i, j, k, a2, x[j][t], x[k][t]);
+        rebuildLists();
+    }
+
+    template <class R> bool tryFlip(R &r, bool checkReduce) {  // scheme_z2.cu:982-1027
+        int size = lists[0].size + lists[1].size + lists[2].size;
+        if (!size) return false;
+        int idx = (int)r.below((uint32_t)size);
+        int i, j, k, a, b;
+        if (idx < lists[0].size) { i = 0; j = 1; k = 2; a = lists[0].first(idx); b = lists[0].second(idx); }
+        else if (idx < lists[0].size + lists[1].size) {
+            idx -= lists[0].size; i = 1; j = 0; k = 2; a = lists[1].first(idx); b = lists[1].second(idx);
+        } else {
+            idx -= lists[0].size + lists[1].size; i = 2; j = 0; k = 1; a = lists[2].first(idx); b = lists[2].second(idx);
+        }
+        if (r.coin()) std::swap(j, k);
+        if (r.coin()) std::swap(a, b);
+        flip(i, j, k, a, b, checkReduce);
+        return true;
+    }
+
+    template <class R> bool tryPlus(R &r) {  // scheme_z2.cu:1029-1050
+        if (m >= kMaxRank || m >= n[0] * n[1] * n[2]) return false;
+        int a = (int)r.below(m), b = (int)r.below(m);
+        int guard = 0;
+        while (a == b || x[0][a] == x[0][b] || x[1][a] == x[1][b] || x[2][a] == x[2][b]) {
+            if (++guard > kRetryCap) { *status |= ST_RETRY; return false; }
+            a = (int)r.below(m);
+            b = (int)r.below(m);
+        }
+        int perm[3];
+        permutation(perm, 3, r);
+        int variant = (int)r.below(3);
+        plus(perm[0], perm[1], perm[2], a, b, variant);
+        return true;
+    }
+
+    template <class R> bool trySplit(R &r) {  // scheme_z2.cu:1052-1078
+        if (m >= kMaxRank || m >= n[0] * n[1] * n[2]) return false;
+        int t = (int)r.below(m);
+        int perm[3];
+        permutation(perm, 3, r);
+        int i = perm[0], j = perm[1], k = perm[2];
+        uint64_t a1 = r.mask(nn[i]);
+        const uint64_t a2 = x[i][t];
+        int loop = 0;
+        while (loop < 5 && a1 == a2) { a1 = r.mask(nn[i]); loop++; }
+        if (loop == 5) return false;
+        split(i, j, k, t, a1);
+        return true;
+    }
+
+    template <class R> bool trySplitExisted(R &r) {  // scheme_z2.cu:1080-1104
+        if (m >= kMaxRank || m >= n[0] * n[1] * n[2]) return false;
+        int perm[3];
+        permutation(perm, 3, r);
+        int i = perm[0], j = perm[1], k = perm[2];
+        int a = (int)r.below(m), b = (int)r.below(m);
+        int loop = 0;
+        while (loop < 5 && (a == b || x[i][a] == x[i][b])) { b = (int)r.below(m); loop++; }
+        if (loop == 5) return false;
+        split(i, j, k, a, x[i][b]);
+        return true;
+    }
+
+    template <class R> bool tryExpand(int count, R &r) {  // scheme_z2.cu:1106-1125
+        int maxRank = n[0] * n[1] * n[2];
+        bool result = false;
+        for (int q = 0; q < count && m < maxRank; q++) {
+            int v = (int)r.below(3);
+            if (v == 0) result |= tryPlus(r);
+            else if (v == 1) result |= trySplit(r);
+            else result |= trySplitExisted(r);
+        }
+        return result;
+    }
+
+    bool tryReduce() {  // scheme_z2.cu:1127-1154
+        for (int p = 0; p < lists[0].size; p++) {
+            int a = lists[0].first(p), b = lists[0].second(p);
+            if (x[1][a] == x[1][b]) { reduce(2, a, b); return true; }
+            if (x[2][a] == x[2][b]) { reduce(1, a, b); return true; }
+        }
+        for (int p = 0; p < lists[1].size; p++) {
+            int a = lists[1].first(p), b = lists[1].second(p);
+            if (x[2][a] == x[2][b]) { reduce(0, a, b); return true; }
+        }
+        return false;
+    }
+
+    int complexity() const {  // scheme_z2.cu:127-139
+        int count = 0;
+        for (int t = 0; t < m; t++)
+            for (int c = 0; c < 3; c++) count += popc64(x[c][t]);
+        return count - 2 * m - nn[2];
+    }
+};
+
+// ------------------------------------------------------------ ternary vector
+struct Tern {  // addition.cuh:8-13 (n is implied by the slot)
+    uint64_t v = 0, s = 0;
+    bool ok = true;
+    bool operator==(const Tern &o) const { return v == o.v && s == o.s; }
+    explicit operator bool() const { return v != 0; }
+    int at(int idx) const { int r = (int)((v >> idx) & 1); return ((s >> idx) & 1) ? -r : r; }
+    Tern add(const Tern &o) const {  // addition.cu:112-119
+        Tern r;
+        r.v = v ^ o.v;
+        r.s = ((s & v) | (o.s & o.v)) & r.v;
+        r.ok = !(v & o.v & ~(s ^ o.s));
+        return r;
+    }
+    Tern sub(const Tern &o) const {  // addition.cu:121-128
+        Tern r;
+        r.v = v ^ o.v;
+        r.s = ((s & v) | (~o.s & o.v)) & r.v;
+        r.ok = !(v & o.v & (s ^ o.s));
+        return r;
+    }
+    void addIn(const Tern &o) {  // addition.cu:138-146
+        uint64_t sv1 = s & v, sv2 = o.s & o.v;
+        ok = !(v & o.v & ~(s ^ o.s));
+        v ^= o.v;
+        s = (sv1 | sv2) & v;
+    }
+    void subIn(const Tern &o) {  // addition.cu:148-156
+        uint64_t sv1 = s & v, sv2 = ~o.s & o.v;
+        ok = !(v & o.v & (s ^ o.s));
+        v ^= o.v;
+        s = (sv1 | sv2) & v;
+    }
+    void negate() { s = ~s & v; }  // inverse(), addition.cu:62-64
+    int compare(const Tern &o) const {  // addition.cu:82-93
+        if (v != o.v) return 0;
+        if (s == o.s) return 1;
+        if (s == (~o.s & o.v)) return -1;
+        return 0;
+    }
+    static bool firstPositive(uint64_t vv, uint64_t ss) { return vv == 0 || (vv & ~(vv & (vv - 1)) & ~ss); }
+    bool positiveFirstNonZero() const { return firstPositive(v, s); }
+    bool limit(bool fp) const { if (!ok) return false; return fp ? firstPositive(v, s) : true; }
+    bool limitSum(const Tern &o, bool fp) const {  // addition.cu:172-186
+        if (v & o.v & ~(s ^ o.s)) return false;
+        if (fp) { uint64_t sv = v ^ o.v; return firstPositive(sv, ((s & v) | (o.s & o.v)) & sv); }
+        return true;
+    }
+    bool limitSub(const Tern &o, bool fp) const {  // addition.cu:188-202
+        if (v & o.v & (s ^ o.s)) return false;
+        if (fp) { uint64_t sv = v ^ o.v; return firstPositive(sv, ((s & v) | (~o.s & o.v)) & sv); }
+        return true;
+    }
+    bool positiveFirstNonZeroSub(const Tern &o) const {
+        uint64_t sv = v ^ o.v;
+        return firstPositive(sv, ((s & v) | (~o.s & o.v)) & sv);
+    }
+};
+
+// Addition::random (addition.cu:66-80): the reference shifts a uint16 promoted
+// to int, so chunk 16 is sign-extended into bits 32..63 and chunks >= 32 shift
+// out to zero (PTX shl.b32 clamps its shift amount); both are reproduced.
+template <class R> Tern randomTern(int n, R &r) {
+    Tern a;
+    for (int i = 0; i < n; i += 16) {
+        uint32_t sb = r.raw() & 0xFFFF;
+        uint32_t vb = r.raw() & 0xFFFF;
+        int32_t vs = i >= 32 ? 0 : (int32_t)(vb << i);
+        int32_t ss = i >= 32 ? 0 : (int32_t)(sb << i);
+        a.v |= (uint64_t)(int64_t)vs;
+        a.s |= (uint64_t)(int64_t)ss;
+    }
+    a.s &= a.v;
+    a.ok = true;
+    return a;
+}
+
+// ------------------------------------------------------------ ZT scheme
+struct ZT {
+    int n[3], nn[3], m;
+    Tern x[3][kMaxRank];
+    FlipList lists[3];
+    int32_t *status;
+
+    bool nonzero(int t) const { return x[0][t].v && x[1][t].v && x[2][t].v; }
+
+    void initNaive(int n1, int n2, int n3) {  // scheme_integer.cu:41-64
+        n[0] = n1; n[1] = n2; n[2] = n3;
+        nn[0] = n1 * n2; nn[1] = n2 * n3; nn[2] = n3 * n1;
+        m = n1 * n2 * n3;
+        for (int i = 0; i < n1; i++)
+            for (int j = 0; j < n3; j++)
+                for (int k = 0; k < n2; k++) {
+                    int t = (i * n3 + j) * n2 + k;
+                    x[0][t] = Tern{(uint64_t)1 << (i * n2 + k), 0, true};
+                    x[1][t] = Tern{(uint64_t)1 << (k * n3 + j), 0, true};
+                    x[2][t] = Tern{(uint64_t)1 << (j * n1 + i), 0, true};
+                }
+        rebuildLists();
+    }
+
+    void rebuildLists() {  // scheme_integer.cu:229-238
+        for (int c = 0; c < 3; c++) {
+            lists[c].clear();
+            for (int a = 0; a < m; a++)
+                for (int b = a + 1; b < m; b++)
+                    if (x[c][a] == x[c][b]) lists[c].add(a, b);
+        }
+    }
+
+    void moveTerm(int dst, int src) { for (int c = 0; c < 3; c++) x[c][dst] = x[c][src]; }
+
+    void removeZeroes() {  // scheme_integer.cu:240-251 (re-checks the moved term)
+        for (int t = 0; t < m; t++) {
+            if (nonzero(t)) continue;
+            m--;
+            moveTerm(t, m);
+            t--;
+        }
+    }
+
+    void removeAt(int t) {
+        m--;
+        if (t == m) return;
+        moveTerm(t, m);
+    }
+
+    void addTriplet(int i, int j, int k, const Tern &a, const Tern &b, const Tern &c) {
+        if (m >= kMaxRank) { *status |= ST_OVERFLOW; return; }
+        x[i][m] = a; x[j][m] = b; x[k][m] = c;
+        m++;
+    }
+
+    bool fixSigns() {  // scheme_integer.cu:398-425
+        bool changed = false;
+        for (int t = 0; t < m; t++) {
+            bool pi = x[0][t].positiveFirstNonZero(), pj = x[1][t].positiveFirstNonZero();
+            if (pi && pj) continue;
+            if (!pi && !pj) { x[0][t].negate(); x[1][t].negate(); }
+            else if (!pi) { x[0][t].negate(); x[2][t].negate(); }
+            else { x[1][t].negate(); x[2][t].negate(); }
+            changed = true;
+        }
+        return changed;
+    }
+
+    void reduceAdd(int i, int a, int b) {  // scheme_integer.cu:549-559
+        x[i][a].addIn(x[i][b]);
+        bool zero = !x[i][a].v;
+        removeAt(b);
+        if (zero) removeZeroes();
+        rebuildLists();
+    }
+
+    void reduceSub(int i, int a, int b) {  // scheme_integer.cu:561-571
+        x[i][a].subIn(x[i][b]);
+        bool zero = !x[i][a].v;
+        removeAt(b);
+        if (zero) removeZeroes();
+        rebuildLists();
+    }
+
+    bool tryReduce() {  // scheme_integer.cu:1062-1101
+        for (int p = 0; p < lists[0].size; p++) {
+            int a = lists[0].first(p), b = lists[0].second(p);
+            if (x[1][a] == x[1][b] && x[2][a].limitSum(x[2][b], false)) { reduceAdd(2, a, b); return true; }
+            int cmp2 = x[2][a].compare(x[2][b]);
+            if (cmp2 == 1 && x[1][a].limitSum(x[1][b], true)) { reduceAdd(1, a, b); return true; }
+            if (cmp2 == -1 && x[1][a].limitSub(x[1][b], true)) { reduceSub(1, a, b); return true; }
+        }
+        for (int p = 0; p < lists[1].size; p++) {
+            int a = lists[1].first(p), b = lists[1].second(p);
+            int cmp2 = x[2][a].compare(x[2][b]);
+            if (cmp2 == 1 && x[0][a].limitSum(x[0][b], true)) { reduceAdd(0, a, b); return true; }
+            if (cmp2 == -1 && x[0][a].limitSub(x[0][b], true)) { reduceSub(0, a, b); return true; }
+        }
+        return false;
+    }
+
+    void flip(int i, int j, int k, int a, int b, bool checkReduce) {  // scheme_integer.cu:428-501
+        x[j][a].addIn(x[j][b]);
+        x[k][b].subIn(x[k][a]);
+        lists[j].removeIndex(a);
+        lists[k].removeIndex(b);
+        if (!x[j][a].v || !x[k][b].v) {
+            removeZeroes();
+            rebuildLists();
+            int guard = 0;
+            while (tryReduce())
+                if (++guard > kRetryCap) { *status |= ST_RETRY; break; }
+            return;
+        }
+        for (int t = 0; t < m; t++) {
+            if (t != a && x[j][t] == x[j][a]) {
+                if (checkReduce) {
+                    int cmpI = x[i][t].compare(x[i][a]);
+                    if (cmpI == 1 && x[k][t].limitSum(x[k][a], k != 2)) { reduceAdd(k, t, a); return; }
+                    if (i == 2 && cmpI == -1 && x[k][t].limitSub(x[k][a], true)) { reduceSub(k, t, a); return; }
+                    int cmpK = x[k][t].compare(x[k][a]);
+                    if (cmpK == 1 && x[i][t].limitSum(x[i][a], i != 2)) { reduceAdd(i, t, a); return; }
+                    if (k == 2 && cmpK == -1 && x[i][t].limitSub(x[i][a], true)) { reduceSub(i, t, a); return; }
+                }
+                lists[j].add(a, t);
+            }
+            if (t != b && x[k][t] == x[k][b]) {
+                if (checkReduce) {
+                    int cmpI = x[i][t].compare(x[i][b]);
+                    if (cmpI == 1 && x[j][t].limitSum(x[j][b], j != 2)) { reduceAdd(j, t, b); return; }
+                    if (i == 2 && cmpI == -1 && x[j][t].limitSub(x[j][b], true)) { reduceSub(j, t, b); return; }
+                    int cmpJ = x[j][t].compare(x[j][b]);
+                    if (cmpJ == 1 && x[i][t].limitSum(x[i][b], i != 2)) { reduceAdd(i, t, b); return; }
+                    if (j == 2 && cmpJ == -1 && x[i][t].limitSub(x[i][b], true)) { reduceSub(i, t, b); return; }
+                }
+                lists[k].add(b, t);
+            }
+        }
+    }
+
+    void plus(int i, int j, int k, int p, int q, int variant) {  // scheme_integer.cu:503-539
+        const Tern a1 = x[i][p], b1 = x[j][p], c1 = x[k][p];
+        const Tern a2 = x[i][q], b2 = x[j][q], c2 = x[k][q];
+        const Tern aAdd = a1.add(a2), bAdd = b1.add(b2), cAdd = c1.add(c2);
+        const Tern aSub = a2.sub(a1), bSub = b2.sub(b1), cSub = c2.sub(c1);
+        if (variant == 0 && aSub.limit(i != 2) && bAdd.limit(j != 2) && cSub.limit(k != 2)) {
+            x[j][p] = bAdd; x[i][q] = aSub; addTriplet(i, j, k, a1, b2, cSub);
+        } else if (variant == 1 && aSub.limit(i != 2) && bSub.limit(j != 2) && cAdd.limit(k != 2)) {
+            x[k][p] = cAdd; x[j][q] = bSub; addTriplet(i, j, k, aSub, b1, c2);
+        } else if (aAdd.limit(i != 2) && bSub.limit(j != 2) && cSub.limit(k != 2)) {
+            x[i][p] = aAdd; x[k][q] = cSub; addTriplet(i, j, k, a2, bSub, c1);
+        }
+        removeZeroes();
+        fixSigns();
+        rebuildLists();
+    }
+
+    void split(int i, int j, int k, int t, const Tern &a) {  // scheme_integer.cu:541-547
+        Tern rest = x[i][t].sub(a);
+        Tern bj = x[j][t], bk = x[k][t];
+        addTriplet(i, j, k, rest, bj, bk);
+        x[i][t] = a;
+        fixSigns();
+        rebuildLists();
+    }
+
+    template <class R> bool tryFlip(R &r, bool checkReduce) {  // scheme_integer.cu:907-975
+        int size = lists[0].size + lists[1].size + lists[2].size;
+        std::vector<int> order(size > 0 ? size : 1);
+        permutation(order.data(), size, r);
+        for (int p = 0; p < size; p++) {
+            int idx = order[p];
+            int i, j, k, a, b;
+            if (idx < lists[0].size) { i = 0; j = 1; k = 2; a = lists[0].first(idx); b = lists[0].second(idx); }
+            else if (idx < lists[0].size + lists[1].size) {
+                idx -= lists[0].size; i = 1; j = 0; k = 2; a = lists[1].first(idx); b = lists[1].second(idx);
+            } else {
+                idx -= lists[0].size + lists[1].size; i = 2; j = 0; k = 1; a = lists[2].first(idx); b = lists[2].second(idx);
+            }
+            if (r.coin()) std::swap(j, k);
+            if (r.coin()) std::swap(a, b);
+            if (x[j][a].limitSum(x[j][b], j != 2) && x[k][b].limitSub(x[k][a], false)) {
+                if (k == 2 || x[k][b].positiveFirstNonZeroSub(x[k][a])) flip(i, j, k, a, b, checkReduce);
+                else flip(i, j, k, b, a, checkReduce);
+                return true;
+            }
+            if (x[k][a].limitSum(x[k][b], k != 2) && x[j][b].limitSub(x[j][a], false)) {
+                if (j == 2 || x[j][b].positiveFirstNonZeroSub(x[j][a])) flip(i, k, j, a, b, checkReduce);
+                else flip(i, k, j, b, a, checkReduce);
+                return true;
+            }
+        }
+        return false;
+    }
+
+    template <class R> bool tryPlus(R &r) {  // scheme_integer.cu:977-998
+        if (m >= kMaxRank || m >= n[0] * n[1] * n[2]) return false;
+        int a = (int)r.below(m), b = (int)r.below(m);
+        int guard = 0;
+        while (a == b || x[0][a] == x[0][b] || x[1][a] == x[1][b] || x[2][a] == x[2][b]) {
+            if (++guard > kRetryCap) { *status |= ST_RETRY; return false; }
+            a = (int)r.below(m);
+            b = (int)r.below(m);
+        }
+        int perm[3];
+        permutation(perm, 3, r);
+        int variant = (int)r.below(3);
+        plus(perm[0], perm[1], perm[2], a, b, variant);
+        return true;
+    }
+
+    template <class R> bool trySplit(R &r) {  // scheme_integer.cu:1000-1020
+        if (m >= kMaxRank || m >= n[0] * n[1] * n[2]) return false;
+        int t = (int)r.below(m);
+        int perm[3];
+        permutation(perm, 3, r);
+        int i = perm[0], j = perm[1], k = perm[2];
+        Tern a = randomTern(nn[i], r);
+        if (!x[i][t].limitSub(a, i != 2)) return false;
+        split(i, j, k, t, a);
+        return true;
+    }
+
+    template <class R> bool trySplitExisted(R &r) {  // scheme_integer.cu:1022-1043
+        if (m >= kMaxRank || m >= n[0] * n[1] * n[2]) return false;
+        int a, b, i;
+        int guard = 0;
+        do {
+            if (++guard > kRetryCap) { *status |= ST_RETRY; return false; }
+            a = (int)r.below(m);
+            b = (int)r.below(m);
+            i = (int)r.below(3);
+        } while (a == b || x[i][a] == x[i][b]);
+        if (!x[i][a].limitSub(x[i][b], i != 2)) return false;
+        Tern xb = x[i][b];
+        split(i, (i + 1) % 3, (i + 2) % 3, a, xb);
+        return true;
+    }
+
+    template <class R> bool tryExpand(int count, R &r) {  // scheme_integer.cu:1045-1060
+        bool result = false;
+        for (int q = 0; q < count && m < kMaxRank; q++) {
+            int v = (int)r.below(3);
+            if (v == 0) result |= tryPlus(r);
+            else if (v == 1) result |= trySplit(r);
+            else result |= trySplitExisted(r);
+        }
+        return result;
+    }
+
+    int complexity() const {  // scheme_integer.cu:139-147
+        int count = 0;
+        for (int t = 0; t < m; t++)
+            for (int c = 0; c < 3; c++) count += popc64(x[c][t].v);
+        return count - 2 * m - nn[2];
+    }
+};
+
+// ------------------------------------------------------------ record <-> scheme
+inline size_t facIndex(int w, int c, int t, int cap) { return ((size_t)w * 3 + c) * cap + t; }
+
+void loadZ2(Z2 &s, const fgo_batch *b, int w, int cap) {
+    for (int c = 0; c < 3; c++) s.n[c] = b->n[w * 3 + c];
+    for (int c = 0; c < 3; c++) s.nn[c] = s.n[c] * s.n[(c + 1) % 3];
+    s.m = b->m[w];
+    for (int c = 0; c < 3; c++)
+        for (int t = 0; t < s.m; t++) s.x[c][t] = b->fac[facIndex(w, c, t, cap)];
+    for (int c = 0; c < 3; c++) {
+        s.lists[c].size = b->list_size[w * 3 + c];
+        std::memcpy(s.lists[c].pairs, b->list_pairs + ((size_t)w * 3 + c) * kMaxPairs, sizeof(uint32_t) * s.lists[c].size);
+    }
+}
+
+void storeZ2(const Z2 &s, fgo_batch *b, int w, int cap) {
+    if (s.m > cap) { b->status[w] |= ST_OVERFLOW; return; }
+    b->m[w] = s.m;
+    for (int c = 0; c < 3; c++) b->n[w * 3 + c] = s.n[c];
+    for (int c = 0; c < 3; c++)
+        for (int t = 0; t < cap; t++) b->fac[facIndex(w, c, t, cap)] = t < s.m ? s.x[c][t] : 0;
+    for (int c = 0; c < 3; c++) {
+        b->list_size[w * 3 + c] = s.lists[c].size;
+        uint32_t *dst = b->list_pairs + ((size_t)w * 3 + c) * kMaxPairs;
+        std::memset(dst, 0, sizeof(uint32_t) * kMaxPairs);
+        std::memcpy(dst, s.lists[c].pairs, sizeof(uint32_t) * s.lists[c].size);
+    }
+}
+
+void loadZT(ZT &s, const fgo_batch *b, int w, int cap) {
+    for (int c = 0; c < 3; c++) s.n[c] = b->n[w * 3 + c];
+    for (int c = 0; c < 3; c++) s.nn[c] = s.n[c] * s.n[(c + 1) % 3];
+    s.m = b->m[w];
+    for (int c = 0; c < 3; c++)
+        for (int t = 0; t < s.m; t++) {
+            size_t q = facIndex(w, c, t, cap);
+            s.x[c][t] = Tern{b->fac[q], b->sgn[q], b->valid[q] != 0};
+        }
+    for (int c = 0; c < 3; c++) {
+        s.lists[c].size = b->list_size[w * 3 + c];
+        std::memcpy(s.lists[c].pairs, b->list_pairs + ((size_t)w * 3 + c) * kMaxPairs, sizeof(uint32_t) * s.lists[c].size);
+    }
+}
+
+void storeZT(const ZT &s, fgo_batch *b, int w, int cap) {
+    if (s.m > cap) { b->status[w] |= ST_OVERFLOW; return; }
+    b->m[w] = s.m;
+    for (int c = 0; c < 3; c++) b->n[w * 3 + c] = s.n[c];
+    for (int c = 0; c < 3; c++)
+        for (int t = 0; t < cap; t++) {
+            size_t q = facIndex(w, c, t, cap);
+            b->fac[q] = t < s.m ? s.x[c][t].v : 0;
+            b->sgn[q] = t < s.m ? s.x[c][t].s : 0;
+            b->valid[q] = t < s.m ? (uint8_t)s.x[c][t].ok : 0;
+        }
+    for (int c = 0; c < 3; c++) {
+        b->list_size[w * 3 + c] = s.lists[c].size;
+        uint32_t *dst = b->list_pairs + ((size_t)w * 3 + c) * kMaxPairs;
+        std::memset(dst, 0, sizeof(uint32_t) * kMaxPairs);
+        std::memcpy(dst, s.lists[c].pairs, sizeof(uint32_t) * s.lists[c].size);
+    }
+}
+
+// best := current without lists (copyTo(target, false))
+void storeBestZ2(const Z2 &s, fgo_batch *b, int w, int cap) {
+    if (s.m > cap) { b->status[w] |= ST_OVERFLOW; return; }
+    b->best_m[w] = s.m;
+    for (int c = 0; c < 3; c++)
+        for (int t = 0; t < cap; t++) b->best_fac[facIndex(w, c, t, cap)] = t < s.m ? s.x[c][t] : 0;
+}
+
+void storeBestZT(const ZT &s, fgo_batch *b, int w, int cap) {
+    if (s.m > cap) { b->status[w] |= ST_OVERFLOW; return; }
+    b->best_m[w] = s.m;
+    for (int c = 0; c < 3; c++)
+        for (int t = 0; t < cap; t++) {
+            size_t q = facIndex(w, c, t, cap);
+            b->best_fac[q] = t < s.m ? s.x[c][t].v : 0;
+            b->best_sgn[q] = t < s.m ? s.x[c][t].s : 0;
+            b->best_valid[q] = t < s.m ? (uint8_t)s.x[c][t].ok : 0;
+        }
+}
+
+inline void storeBest(const Z2 &s, fgo_batch *b, int w, int cap) { storeBestZ2(s, b, w, cap); }
+inline void storeBest(const ZT &s, fgo_batch *b, int w, int cap) { storeBestZT(s, b, w, cap); }
+
+// randomWalkKernel body (flip_graph.cu:526-569) with randomIterations=false and
+// sandwiching / basis probabilities 0: their gate draws are still consumed
+// (RefDraws) exactly as the reference does.
+template <class Scheme, class R>
+void walkLaunch(Scheme &s, R &r, const fgo_walk_cfg *cfg, fgo_batch *b, int w) {
+    int cap = cfg->cap;
+    int flipsCount = b->flips[w];
+    int bestRank = b->best_rank[w];
+    int bestM = b->best_m[w];
+    const int iters = cfg->iterations;
+    for (int it = 0; it < iters; it++) {
+        int rank = s.m;
+        if (!s.tryFlip(r, true)) {
+            s.tryExpand(randint(1, 2, r), r);
+            continue;
+        }
+        if (s.m < rank) flipsCount = 0;
+        flipsCount++;
+        if (s.m < bestRank || (s.m == bestRank && r.tie())) {
+            bestRank = s.m;
+            storeBest(s, b, w, cap);
+            bestM = s.m;
+        }
+        if (r.gate(cfg->reduce_p, iters)) s.tryReduce();
+        if (r.gate(cfg->expand_p, iters) && s.m <= bestM + 2) {
+            if (s.tryExpand(randint(1, 2, r), r)) flipsCount = 0;
+        }
+        r.gate(0.0, iters);  // sandwiching gate (probability 0)
+        r.gate(0.0, iters);  // basis gate (probability 0)
+        if (flipsCount >= cfg->plus_iterations && s.tryPlus(r)) flipsCount = 0;
+        if (b->status[w]) break;
+    }
+    b->flips[w] = flipsCount;
+    b->best_rank[w] = bestRank;
+}
+
+template <class Scheme> void loadScheme(Scheme &s, const fgo_batch *b, int w, int cap);
+template <> void loadScheme<Z2>(Z2 &s, const fgo_batch *b, int w, int cap) { loadZ2(s, b, w, cap); }
+template <> void loadScheme<ZT>(ZT &s, const fgo_batch *b, int w, int cap) { loadZT(s, b, w, cap); }
+inline void storeScheme(const Z2 &s, fgo_batch *b, int w, int cap) { storeZ2(s, b, w, cap); }
+inline void storeScheme(const ZT &s, fgo_batch *b, int w, int cap) { storeZT(s, b, w, cap); }
+
+template <class Scheme>
+void runWalks(const fgo_walk_cfg *cfg, int S, fgo_batch *b, const fgo_tape *tape) {
+    Scheme *s = new Scheme;
+    for (int w = 0; w < S; w++) {
+        loadScheme(*s, b, w, cfg->cap);
+        s->status = &b->status[w];
+        if (cfg->rng == FGO_RNG_TAPE) {
+            RefDraws r;
+            r.d = tape->draws + tape->offsets[w];
+            r.u = tape->uniforms + tape->offsets[w];
+            r.n = tape->offsets[w + 1] - tape->offsets[w];
+            r.pos = b->rng_pos[w];
+            r.status = &b->status[w];
+            for (int L = 0; L < cfg->launches && !b->status[w]; L++) walkLaunch(*s, r, cfg, b, w);
+            b->rng_pos[w] = r.pos;
+        } else {
+            FastDraws r;
+            r.key[0] = (uint32_t)cfg->seed;
+            r.key[1] = (uint32_t)(cfg->seed >> 32);
+            r.walk = (uint32_t)w;
+            r.pos = b->rng_pos[w];
+            r.status = &b->status[w];
+            for (int L = 0; L < cfg->launches && !b->status[w]; L++) walkLaunch(*s, r, cfg, b, w);
+            b->rng_pos[w] = r.pos;
+        }
+        storeScheme(*s, b, w, cfg->cap);
+    }
+    delete s;
+}
+
+// minimizeKernel body (complexity_minimizer.cu:245-263).
+template <class Scheme, class R>
+void minimizeLaunch(Scheme &s, R &r, const fgo_walk_cfg *cfg, fgo_batch *b, int w, int32_t *bestC) {
+    int best = bestC[w];
+    for (int it = 0; it < cfg->iterations; it++) {
+        if (!s.tryFlip(r, false)) break;
+        int c = s.complexity();
+        if (c < best) {
+            best = c;
+            storeBest(s, b, w, cfg->cap);
+        }
+        if (b->status[w]) break;
+    }
+    bestC[w] = best;
+}
+
+template <class Scheme>
+void runMinimize(const fgo_walk_cfg *cfg, int S, fgo_batch *b, const fgo_tape *tape, int32_t *bestC) {
+    Scheme *s = new Scheme;
+    for (int w = 0; w < S; w++) {
+        loadScheme(*s, b, w, cfg->cap);  // lists keep their persisted order
+        s->status = &b->status[w];
+        if (cfg->rng == FGO_RNG_TAPE) {
+            RefDraws r;
+            r.d = tape->draws + tape->offsets[w];
+            r.u = tape->uniforms + tape->offsets[w];
+            r.n = tape->offsets[w + 1] - tape->offsets[w];
+            r.pos = b->rng_pos[w];
+            r.status = &b->status[w];
+            minimizeLaunch(*s, r, cfg, b, w, bestC);
+            b->rng_pos[w] = r.pos;
+        } else {
+            FastDraws r;
+            r.key[0] = (uint32_t)cfg->seed;
+            r.key[1] = (uint32_t)(cfg->seed >> 32);
+            r.walk = (uint32_t)w;
+            r.pos = b->rng_pos[w];
+            r.status = &b->status[w];
+            minimizeLaunch(*s, r, cfg, b, w, bestC);
+            b->rng_pos[w] = r.pos;
+        }
+        storeScheme(*s, b, w, cfg->cap);
+    }
+    delete s;
+}
+
+}  // namespace
+
+// ============================================================ additions reducer
+namespace {
+
+enum { GREEDY = 0, GREEDY_ALT = 1, GREEDY_RANDOM = 2, GREEDY_INTER = 3, WEIGHTED_RANDOM = 4, MIX = 5, RANDOM = 6 };
+
+struct Pair { int i, j, count; };
+
+// PairsCounter (pairs_counter.cuh): pairs kept in first-insertion order with
+// counts; the open-addressing table only locates them, so an ordinary map
+// gives the same order.  Pairs beyond maxPairs are dropped (pairs_counter.cuh:242).
+struct PairCounter {
+    int maxPairs;
+    std::vector<Pair> pairs;
+    int topSize = 0, maxCount = 0;
+    std::unordered_map<uint64_t, int> where;
+    void clear() { pairs.clear(); where.clear(); topSize = 0; maxCount = 0; }
+    void insert(int i, int j) {
+        if (std::abs(i) > std::abs(j)) std::swap(i, j);  // canonizePair
+        if (i < 0) { i = -i; j = -j; }
+        uint64_t key = ((uint64_t)(uint32_t)i << 32) | (uint32_t)j;
+        auto it = where.find(key);
+        int idx;
+        if (it == where.end()) {
+            if ((int)pairs.size() >= maxPairs) return;
+            idx = (int)pairs.size();
+            pairs.push_back({i, j, 0});
+            where[key] = idx;
+        } else {
+            idx = it->second;
+        }
+        if (++pairs[idx].count > maxCount) maxCount = pairs[idx].count;
+    }
+    void sort() {  // pairs_counter.cuh:73-101
+        int size = (int)pairs.size();
+        if (maxCount < 2) { topSize = size; return; }
+        topSize = 0;
+        for (int i = 0; i < size; i++) {
+            if (pairs[i].count != maxCount) continue;
+            if (i != topSize) std::swap(pairs[i], pairs[topSize]);
+            topSize++;
+        }
+        int j = topSize;
+        for (int i = topSize; i < size; i++)
+            if (pairs[i].count > 1) pairs[j++] = pairs[i];
+        pairs.resize(j);
+    }
+    bool any() const { return !pairs.empty() && maxCount > 1; }
+};
+
+bool intersects(const Pair &a, const Pair &b) {
+    return a.i == b.i || a.i == std::abs(b.j) || std::abs(a.j) == b.i || std::abs(a.j) == std::abs(b.j);
+}
+
+// Whether nvcc's default floating-point contraction (--fmad=true) fused the
+// multiply-adds of getGreedyIntersections (pairs_counter.cuh:163,167) in the
+// reference build; pinned by the golden reducer fixtures.
+int g_fuse_float = 1;
+int g_fuse_double = 1;
+
+struct Reducer {  // AdditionsReducer<maxExpr, maxFresh, maxLen, maxSub>
+    int maxFresh, maxLen;
+    std::vector<std::vector<int>> expr;
+    std::vector<std::pair<int, int>> vars;
+    PairCounter sub;
+    int realVariables = 0, freshVariables = 0, naiveAdditions = 0, mode = GREEDY;
+    float scale = -1;
+
+    void clear() { expr.clear(); vars.clear(); realVariables = freshVariables = naiveAdditions = 0; }
+    void setMode(int md) { mode = md; scale = -1; }
+
+    bool addExpression(const int *values, int count) {  // additions_reducer.cuh:67-86
+        std::vector<int> e;
+        for (int i = 0; i < count; i++) {
+            if (values[i] == 1) e.push_back(i + 1);
+            else if (values[i] == -1) e.push_back(-(i + 1));
+            else if (values[i] != 0) return false;
+        }
+        if (count > realVariables) realVariables = count;
+        naiveAdditions += (int)e.size() - 1;
+        expr.push_back(e);
+        return true;
+    }
+
+    int additions() const {
+        int a = freshVariables;
+        for (auto &e : expr) a += (int)e.size() - 1;
+        return a;
+    }
+
+    static int search(const std::vector<int> &e, int value, int start) {  // additions_reducer.cuh:247-269
+        int lo = start, hi = (int)e.size() - 1, va = std::abs(value);
+        while (lo <= hi) {
+            int mid = lo + (hi - lo) / 2;
+            int ma = std::abs(e[mid]);
+            if (ma < va) lo = mid + 1;
+            else if (ma > va) hi = mid - 1;
+            else return mid;
+        }
+        return -1;
+    }
+
+    void replace(int pi, int pj) {  // additions_reducer.cuh:218-245,291-301
+        int var = realVariables + freshVariables + 1;
+        for (auto &e : expr) {
+            if (e.size() < 2) continue;
+            int i = search(e, pi, 0);
+            if (i == -1) continue;
+            int j = search(e, pj, i + 1);
+            if (j == -1) continue;
+            int v;
+            if (e[i] == pi && e[j] == pj) v = var;
+            else if (e[i] == -pi && e[j] == -pj) v = -var;
+            else continue;
+            std::vector<int> out;
+            for (int q = 0; q < (int)e.size(); q++)
+                if (q != i && q != j) out.push_back(e[q]);
+            out.push_back(v);
+            e.swap(out);
+        }
+        vars.push_back({pi, pj});
+        freshVariables++;
+    }
+
+    void update() {  // additions_reducer.cuh:207-216
+        sub.clear();
+        for (auto &e : expr)
+            for (size_t i = 0; i < e.size(); i++)
+                for (size_t j = i + 1; j < e.size(); j++) sub.insert(e[i], e[j]);
+        sub.sort();
+    }
+
+    template <class R> Pair select(int md, R &r) {  // additions_reducer.cuh:272-289
+        auto &p = sub.pairs;
+        int size = (int)p.size();
+        if (md == GREEDY) return p[0];
+        if (md == GREEDY_ALT) return p[r.raw() % (uint32_t)sub.topSize];
+        if (md == GREEDY_RANDOM) {
+            if (r.uniform() < scale) return p[r.raw() % (uint32_t)size];
+            return p[r.raw() % (uint32_t)sub.topSize];
+        }
+        if (md == GREEDY_INTER) {  // pairs_counter.cuh:148-176
+            int imax = 0;
+            float maxScore = 0;
+            for (int i = 0; i < size; i++) {
+                float inter = 0;
+                for (int j = 0; j < size; j++) {
+                    if (i == j) continue;
+                    if (!intersects(p[i], p[j])) {
+                        inter += (float)(p[j].count - 1);
+                    } else {
+                        bool skip = r.raw() % 2;
+                        if (!skip) {
+                            double add = g_fuse_double ? std::fma(0.69, (double)p[j].count, (double)inter)
+                                                       : (double)inter + 0.69 * (double)p[j].count;
+                            inter = (float)add;
+                        }
+                    }
+                }
+                float score = g_fuse_float ? std::fmaf(scale, inter, (float)(p[i].count - 1))
+                                           : (float)(p[i].count - 1) + scale * inter;
+                if (score > maxScore) { maxScore = score; imax = i; }
+            }
+            return p[imax];
+        }
+        if (md == WEIGHTED_RANDOM) {  // pairs_counter.cuh:178-196
+            float total = 0;
+            for (int i = 0; i < size; i++) total += (float)p[i].count;
+            float x = r.uniform() * total;
+            float sum = 0;
+            for (int i = 0; i < size; i++) {
+                sum += (float)p[i].count;
+                if (x <= sum) return p[i];
+            }
+            return p[size - 1];
+        }
+        return p[r.raw() % (uint32_t)size];
+    }
+
+    template <class R> void reduce(R &r) {  // additions_reducer.cuh:89-103
+        if (scale < 0) scale = r.uniform() / 2;
+        while (freshVariables < maxFresh) {
+            update();
+            if (!sub.any()) break;
+            int md = mode == MIX ? (int)(r.raw() % MIX) : mode;
+            Pair s = select(md, r);
+            replace(s.i, s.j);
+        }
+    }
+
+    void partialInitialize(const std::vector<std::pair<int, int>> &bestVars, int count) {
+        for (int q = 0; q < count && q < (int)bestVars.size(); q++) replace(bestVars[q].first, bestVars[q].second);
+    }
+};
+
+const int kModes[15] = {GREEDY_INTER, GREEDY_INTER, GREEDY_INTER, GREEDY_INTER, GREEDY_INTER, GREEDY_INTER,
+                        GREEDY_INTER, GREEDY_INTER, GREEDY_ALT, GREEDY_ALT, GREEDY_ALT, GREEDY_ALT,
+                        GREEDY_RANDOM, GREEDY_RANDOM, MIX};
+
+}  // namespace
+
+struct fgo_reducer_state {
+    std::vector<std::pair<int, int>> vars[3];
+};
+
+extern "C" {
+
+void fgo_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]) { philox(ctr, key, out); }
+
+void fgo_set_fma(int fuse_float, int fuse_double) { g_fuse_float = fuse_float; g_fuse_double = fuse_double; }
+
+int fgo_init_naive(const fgo_walk_cfg *cfg, int S, int n1, int n2, int n3, fgo_batch *b) {
+    int bad = 0;
+    if (cfg->ring == FGO_RING_Z2) {
+        Z2 *s = new Z2;
+        for (int w = 0; w < S; w++) {
+            s->status = &b->status[w];
+            s->initNaive(n1, n2, n3);
+            storeZ2(*s, b, w, cfg->cap);
+            storeBestZ2(*s, b, w, cfg->cap);
+            b->best_rank[w] = n1 * n2 * n3;
+            b->flips[w] = 0;
+            bad += b->status[w] != 0;
+        }
+        delete s;
+    } else {
+        ZT *s = new ZT;
+        for (int w = 0; w < S; w++) {
+            s->status = &b->status[w];
+            s->initNaive(n1, n2, n3);
+            storeZT(*s, b, w, cfg->cap);
+            storeBestZT(*s, b, w, cfg->cap);
+            b->best_rank[w] = n1 * n2 * n3;
+            b->flips[w] = 0;
+            bad += b->status[w] != 0;
+        }
+        delete s;
+    }
+    return bad;
+}
+
+int fgo_walk(const fgo_walk_cfg *cfg, int S, fgo_batch *b, const fgo_tape *tape) {
+    if (cfg->ring == FGO_RING_Z2) runWalks<Z2>(cfg, S, b, tape);
+    else runWalks<ZT>(cfg, S, b, tape);
+    int bad = 0;
+    for (int w = 0; w < S; w++) bad += b->status[w] != 0;
+    return bad;
+}
+
+int fgo_minimize(const fgo_walk_cfg *cfg, int S, fgo_batch *b, const fgo_tape *tape, int32_t *best_complexity) {
+    if (cfg->ring == FGO_RING_Z2) runMinimize<Z2>(cfg, S, b, tape, best_complexity);
+    else runMinimize<ZT>(cfg, S, b, tape, best_complexity);
+    int bad = 0;
+    for (int w = 0; w < S; w++) bad += b->status[w] != 0;
+    return bad;
+}
+
+int fgo_validate(int ring, int S, int cap, const int32_t *n, const int32_t *m, const uint64_t *fac,
+                 const uint64_t *sgn, const uint8_t *valid, uint8_t *valid_out) {
+    int good = 0;
+    for (int w = 0; w < S; w++) {
+        int n0 = n[w * 3], n1 = n[w * 3 + 1], n2 = n[w * 3 + 2];
+        int nn0 = n0 * n1, nn1 = n1 * n2, nn2 = n2 * n0, mm = m[w];
+        bool ok = true;
+        const uint64_t *u = fac + facIndex(w, 0, 0, cap), *v = fac + facIndex(w, 1, 0, cap), *x = fac + facIndex(w, 2, 0, cap);
+        if (ring == FGO_RING_Z2) {
+            // Bit-sliced over k: the reference's per-(i,j,k) XOR (scheme_z2.cu:3-29).
+            for (int i = 0; i < nn0 && ok; i++)
+                for (int j = 0; j < nn1 && ok; j++) {
+                    uint64_t acc = 0;
+                    for (int t = 0; t < mm; t++)
+                        if (((u[t] >> i) & 1) && ((v[t] >> j) & 1)) acc ^= x[t];
+                    for (int k = 0; k < nn2 && ok; k++) {
+                        int target = (i % n1 == j / n2) && (i / n1 == k % n0) && (j % n2 == k / n0);
+                        if ((int)((acc >> k) & 1) != target) ok = false;
+                    }
+                }
+        } else {
+            const uint64_t *us = sgn + facIndex(w, 0, 0, cap), *vs = sgn + facIndex(w, 1, 0, cap), *xs = sgn + facIndex(w, 2, 0, cap);
+            auto coef = [](uint64_t vv, uint64_t ss, int idx) { int r = (int)((vv >> idx) & 1); return ((ss >> idx) & 1) ? -r : r; };
+            for (int i = 0; i < nn0 && ok; i++)
+                for (int j = 0; j < nn1 && ok; j++)
+                    for (int k = 0; k < nn2 && ok; k++) {
+                        int target = (i % n1 == j / n2) && (i / n1 == k % n0) && (j % n2 == k / n0);
+                        int e = 0;
+                        for (int t = 0; t < mm; t++) e += coef(u[t], us[t], i) * coef(v[t], vs[t], j) * coef(x[t], xs[t], k);
+                        if (e != target) ok = false;
+                    }
+            for (int c = 0; c < 3 && ok; c++)
+                for (int t = 0; t < mm; t++)
+                    if (!valid[facIndex(w, c, t, cap)]) { ok = false; break; }
+        }
+        valid_out[w] = ok;
+        good += ok;
+    }
+    return good;
+}
+
+int fgo_complexity(int ring, int S, int cap, const int32_t *n, const int32_t *m, const uint64_t *fac, int32_t *out) {
+    (void)ring;
+    for (int w = 0; w < S; w++) {
+        int count = 0;
+        for (int c = 0; c < 3; c++)
+            for (int t = 0; t < m[w]; t++) count += popc64(fac[facIndex(w, c, t, cap)]);
+        out[w] = count - 2 * m[w] - n[w * 3 + 2] * n[w * 3];
+    }
+    return 0;
+}
+
+// Reducer sizes per config.cuh:16-32 with AdditionsReducer's template order
+// <maxExpressions, maxFresh, maxExpressionLength, maxSubexpressions>.
+int fgo_reduce(int n1, int n2, int n3, int m, const int8_t *coef, int count, int independent,
+               const fgo_tape *tape, int rng, uint64_t seed, int32_t *out, int32_t *modes,
+               int64_t *consumed, const fgo_reducer_state *best, fgo_reducer_state **best_out) {
+    const int nn[3] = {n1 * n2, n2 * n3, n3 * n1};
+    const int maxFresh[3] = {250, 250, 500};
+    const int maxLen[3] = {32, 32, 175};
+    const int maxSub[3] = {2016, 2016, 61075};
+    int bad = 0;
+    std::vector<Reducer> all((size_t)count * 3);
+    for (int idx = 0; idx < count; idx++) {
+        int32_t status = 0;
+        RefDraws rt;
+        FastDraws rf;
+        if (rng == FGO_RNG_TAPE) {
+            rt.d = tape->draws + tape->offsets[idx];
+            rt.u = tape->uniforms + tape->offsets[idx];
+            rt.n = tape->offsets[idx + 1] - tape->offsets[idx];
+            rt.status = &status;
+        } else {
+            rf.key[0] = (uint32_t)seed;
+            rf.key[1] = (uint32_t)(seed >> 32);
+            rf.walk = (uint32_t)idx;
+            rf.status = &status;
+        }
+        Reducer *R = &all[(size_t)idx * 3];
+        for (int p = 0; p < 3; p++) {
+            R[p].maxFresh = maxFresh[p];
+            R[p].maxLen = maxLen[p];
+            R[p].sub.maxPairs = maxSub[p];
+        }
+        // copySchemeToReducers (scheme_additions_reducer.cu:463-492)
+        std::vector<int> row(std::max(m, 64));
+        for (int t = 0; t < m; t++) {
+            for (int i = 0; i < nn[0]; i++) row[i] = coef[((size_t)0 * m + t) * 64 + i];
+            R[0].addExpression(row.data(), nn[0]);
+        }
+        for (int t = 0; t < m; t++) {
+            for (int i = 0; i < nn[1]; i++) row[i] = coef[((size_t)1 * m + t) * 64 + i];
+            R[1].addExpression(row.data(), nn[1]);
+        }
+        for (int i = 0; i < nn[2]; i++) {
+            for (int t = 0; t < m; t++) row[t] = coef[((size_t)2 * m + t) * 64 + i];
+            R[2].addExpression(row.data(), m);
+        }
+        auto body = [&](auto &r) {
+            for (int p = 0; p < 3; p++) R[p].setMode(idx == 0 ? GREEDY : kModes[r.raw() % 15]);
+            static const std::vector<std::pair<int, int>> empty;
+            const std::vector<std::pair<int, int>> *bv[3] = {&empty, &empty, &empty};
+            if (best) for (int p = 0; p < 3; p++) bv[p] = &best->vars[p];
+            if (independent) {
+                for (int p = 0; p < 3; p++)
+                    if ((double)r.uniform() < 0.3 && !bv[p]->empty())
+                        R[p].partialInitialize(*bv[p], 1 + (int)(r.raw() % (uint32_t)bv[p]->size()));
+            } else if ((double)r.uniform() < 0.3) {
+                for (int p = 0; p < 3; p++)
+                    if (!bv[p]->empty()) R[p].partialInitialize(*bv[p], 1 + (int)(r.raw() % (uint32_t)bv[p]->size()));
+            }
+            for (int p = 0; p < 3; p++) R[p].reduce(r);
+        };
+        if (rng == FGO_RNG_TAPE) { body(rt); if (consumed) consumed[idx] = rt.pos; }
+        else { body(rf); if (consumed) consumed[idx] = rf.pos; }
+        for (int p = 0; p < 3; p++) {
+            out[idx * 9 + p * 3 + 0] = R[p].additions();
+            out[idx * 9 + p * 3 + 1] = R[p].freshVariables;
+            out[idx * 9 + p * 3 + 2] = R[p].naiveAdditions;
+            if (modes) modes[idx * 3 + p] = R[p].mode;
+        }
+        bad += status != 0;
+    }
+    if (best_out) {
+        fgo_reducer_state *st = new fgo_reducer_state;
+        // Per-component incumbents: lowest (additions, fresh) over reducers, first index on ties.
+        for (int p = 0; p < 3; p++) {
+            int bi = 0;
+            for (int idx = 1; idx < count; idx++) {
+                const Reducer &a = all[(size_t)idx * 3 + p], &c = all[(size_t)bi * 3 + p];
+                if (a.additions() < c.additions() || (a.additions() == c.additions() && a.freshVariables < c.freshVariables)) bi = idx;
+            }
+            st->vars[p] = all[(size_t)bi * 3 + p].vars;
+        }
+        *best_out = st;
+    }
+    return bad;
+}
+
+void fgo_reducer_state_free(fgo_reducer_state *s) { delete s; }
+
+}  // extern "C"

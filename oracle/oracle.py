@@ -1,0 +1,211 @@
+"""ctypes binding of the CPU oracle (oracle/fg_oracle.cpp) -- TEST INFRASTRUCTURE.
+
+Only tests/, __graft_entry__.smoke() and bench.py's cpu_baseline leg import
+this module, and only as the checker / the CPU baseline; the product never
+does.  The walk-record arrays here have the same layout as the CUDA
+library's exported records (include/flipgraph.h), so results compare with
+numpy equality.
+"""
+import ctypes
+import os
+import platform
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+MAX_PAIRS = 500
+RING = {"z2": 0, "zt": 1}
+RNG = {"tape": 0, "philox": 1}
+
+
+def lib_path():
+    return os.path.join(HERE, "build", platform.machine(), "libfg_oracle.so")
+
+
+def build():
+    subprocess.run(["make", "-s", "-C", HERE], check=True)
+    return lib_path()
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = lib_path()
+        if not os.path.exists(path):
+            build()
+        _lib = ctypes.CDLL(path)
+        _lib.fgo_walk.restype = ctypes.c_int
+        _lib.fgo_init_naive.restype = ctypes.c_int
+        _lib.fgo_minimize.restype = ctypes.c_int
+        _lib.fgo_validate.restype = ctypes.c_int
+        _lib.fgo_reduce.restype = ctypes.c_int
+    return _lib
+
+
+class WalkCfg(ctypes.Structure):
+    _fields_ = [("ring", ctypes.c_int32), ("rng", ctypes.c_int32), ("cap", ctypes.c_int32),
+                ("iterations", ctypes.c_int32), ("plus_iterations", ctypes.c_int32),
+                ("launches", ctypes.c_int32), ("expand_p", ctypes.c_double),
+                ("reduce_p", ctypes.c_double), ("seed", ctypes.c_uint64)]
+
+
+class _Batch(ctypes.Structure):
+    _fields_ = [(name, ctypes.c_void_p) for name in
+                ("n", "m", "fac", "sgn", "valid", "list_size", "list_pairs", "flips", "best_rank",
+                 "best_m", "best_fac", "best_sgn", "best_valid", "rng_pos", "status")]
+
+
+class _Tape(ctypes.Structure):
+    _fields_ = [("draws", ctypes.c_void_p), ("uniforms", ctypes.c_void_p), ("offsets", ctypes.c_void_p)]
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+class WalkBatch:
+    """S walk records with `cap` factor slots each (numpy, C-contiguous)."""
+
+    FIELDS = ("n", "m", "fac", "sgn", "valid", "list_size", "list_pairs", "flips", "best_rank",
+              "best_m", "best_fac", "best_sgn", "best_valid", "rng_pos", "status")
+
+    def __init__(self, S, cap, ring="z2"):
+        self.S, self.cap, self.ring = S, cap, ring
+        zt = ring == "zt"
+        self.n = np.zeros((S, 3), np.int32)
+        self.m = np.zeros(S, np.int32)
+        self.fac = np.zeros((S, 3, cap), np.uint64)
+        self.sgn = np.zeros((S, 3, cap), np.uint64) if zt else None
+        self.valid = np.zeros((S, 3, cap), np.uint8) if zt else None
+        self.list_size = np.zeros((S, 3), np.int32)
+        self.list_pairs = np.zeros((S, 3, MAX_PAIRS), np.uint32)
+        self.flips = np.zeros(S, np.int32)
+        self.best_rank = np.zeros(S, np.int32)
+        self.best_m = np.zeros(S, np.int32)
+        self.best_fac = np.zeros((S, 3, cap), np.uint64)
+        self.best_sgn = np.zeros((S, 3, cap), np.uint64) if zt else None
+        self.best_valid = np.zeros((S, 3, cap), np.uint8) if zt else None
+        self.rng_pos = np.zeros(S, np.int64)
+        self.status = np.zeros(S, np.int32)
+
+    def copy(self):
+        b = WalkBatch.__new__(WalkBatch)
+        b.S, b.cap, b.ring = self.S, self.cap, self.ring
+        for f in self.FIELDS:
+            v = getattr(self, f)
+            setattr(b, f, None if v is None else v.copy())
+        return b
+
+    def _c(self):
+        return _Batch(*[_ptr(getattr(self, f)) for f in self.FIELDS])
+
+    def cfg(self, rng="tape", iterations=1000, plus_iterations=8000, launches=1, expand_p=0.01,
+            reduce_p=0.0, seed=0):
+        return WalkCfg(RING[self.ring], RNG[rng], self.cap, iterations, plus_iterations, launches,
+                       expand_p, reduce_p, seed)
+
+
+def make_tape(tapes):
+    """tapes: list of (draws uint32 array, uniforms float32 array) per walk."""
+    offs = np.zeros(len(tapes) + 1, np.int64)
+    for i, (d, _) in enumerate(tapes):
+        offs[i + 1] = offs[i] + len(d)
+    draws = np.concatenate([np.asarray(d, np.uint32) for d, _ in tapes]) if tapes else np.zeros(0, np.uint32)
+    unis = np.concatenate([np.asarray(u, np.float32) for _, u in tapes]) if tapes else np.zeros(0, np.float32)
+    draws = np.ascontiguousarray(draws)
+    unis = np.ascontiguousarray(unis)
+    return (draws, unis, offs)
+
+
+def _tape_c(tape):
+    if tape is None:
+        return None, None
+    draws, unis, offs = tape
+    return _Tape(_ptr(draws), _ptr(unis), _ptr(offs)), (draws, unis, offs)
+
+
+def init_naive(batch, n1, n2, n3):
+    cfg = batch.cfg()
+    cb = batch._c()
+    return lib().fgo_init_naive(ctypes.byref(cfg), batch.S, n1, n2, n3, ctypes.byref(cb))
+
+
+def walk(batch, cfg, tape=None):
+    cb = batch._c()
+    t, _keep = _tape_c(tape)
+    return lib().fgo_walk(ctypes.byref(cfg), batch.S, ctypes.byref(cb), ctypes.byref(t) if t else None)
+
+
+def minimize(batch, cfg, best_complexity, tape=None):
+    cb = batch._c()
+    t, _keep = _tape_c(tape)
+    return lib().fgo_minimize(ctypes.byref(cfg), batch.S, ctypes.byref(cb), ctypes.byref(t) if t else None,
+                              _ptr(best_complexity))
+
+
+def validate(batch, best=False):
+    out = np.zeros(batch.S, np.uint8)
+    m = batch.best_m if best else batch.m
+    fac = batch.best_fac if best else batch.fac
+    sgn = batch.best_sgn if best else batch.sgn
+    val = batch.best_valid if best else batch.valid
+    lib().fgo_validate(RING[batch.ring], batch.S, batch.cap, _ptr(batch.n), _ptr(m), _ptr(fac),
+                       _ptr(sgn), _ptr(val), _ptr(out))
+    return out.astype(bool)
+
+
+def validate_arrays(ring, n, m, fac, sgn=None, valid=None):
+    n = np.ascontiguousarray(n, np.int32)
+    m = np.ascontiguousarray(m, np.int32)
+    fac = np.ascontiguousarray(fac, np.uint64)
+    S, _, cap = fac.shape
+    out = np.zeros(S, np.uint8)
+    lib().fgo_validate(RING[ring], S, cap, _ptr(n), _ptr(m), _ptr(fac),
+                       _ptr(None if sgn is None else np.ascontiguousarray(sgn, np.uint64)),
+                       _ptr(None if valid is None else np.ascontiguousarray(valid, np.uint8)), _ptr(out))
+    return out.astype(bool)
+
+
+def complexity(ring, n, m, fac):
+    n = np.ascontiguousarray(n, np.int32)
+    m = np.ascontiguousarray(m, np.int32)
+    fac = np.ascontiguousarray(fac, np.uint64)
+    S, _, cap = fac.shape
+    out = np.zeros(S, np.int32)
+    lib().fgo_complexity(RING[ring], S, cap, _ptr(n), _ptr(m), _ptr(fac), _ptr(out))
+    return out
+
+
+def set_fma(fuse_float, fuse_double):
+    lib().fgo_set_fma(int(fuse_float), int(fuse_double))
+
+
+def reduce(n, m, coef, count, tape=None, independent=True, rng="tape", seed=0, best=None):
+    """One additions-reducer launch; returns (out[count,9], modes[count,3], consumed[count], state)."""
+    coef = np.ascontiguousarray(coef, np.int8)
+    assert coef.shape == (3, m, 64)
+    out = np.zeros((count, 9), np.int32)
+    modes = np.zeros((count, 3), np.int32)
+    consumed = np.zeros(count, np.int64)
+    t, _keep = _tape_c(tape)
+    state = ctypes.c_void_p()
+    lib().fgo_reduce(n[0], n[1], n[2], m, _ptr(coef), count, int(independent),
+                     ctypes.byref(t) if t else None, RNG[rng], ctypes.c_uint64(seed), _ptr(out), _ptr(modes),
+                     _ptr(consumed), best, ctypes.byref(state))
+    return out, modes, consumed, state
+
+
+def reducer_state_free(state):
+    lib().fgo_reducer_state_free(state)
+
+
+def philox(ctr, key):
+    c = (ctypes.c_uint32 * 4)(*ctr)
+    k = (ctypes.c_uint32 * 2)(*key)
+    o = (ctypes.c_uint32 * 4)()
+    lib().fgo_philox4x32_10(c, k, o)
+    return list(o)

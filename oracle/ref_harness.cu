@@ -1,0 +1,221 @@
+// Test infrastructure: drives the reference's own, unmodified CUDA kernels and
+// dumps their complete state so that golden fixtures can be cut from it.
+//
+// This file is compiled only against a staged copy of the reference sources
+// (oracle/build_ref.sh) and only ever runs to GENERATE fixtures under
+// tests/golden/.  Nothing in the product links or runs it.
+//
+// Commands
+//   walk  N1 N2 N3 S ITERS PLUS_ITERS EXPAND_P REDUCE_P SEED LAUNCHES OUT
+//       Follows FlipGraph's naive path (flip_graph.cu:185,229,192,236) with
+//       --resize-probability 0 (so randomIterations=false, flip_graph.cu:530)
+//       and sandwiching/basis probabilities 0.  After every launch of
+//       randomWalkKernel (flip_graph.cu:520-573) the full per-walk state is
+//       written.  After the last launch the XORWOW draw tape of every walk is
+//       written, cut exactly at the number of draws the walk consumed (found
+//       by stepping a fresh curand_init(seed, idx, 0) state until it equals
+//       the walk's final state).
+//   reduce IN COUNT SCHEMES_COUNT SEED OUT
+//       Reads one scheme body (n1 n2 n3 m + U,V,W rows) with
+//       checkValidity=false, runs initializeKernel and one runReducersKernel
+//       (scheme_additions_reducer.cu:433-540) and writes per-reducer
+//       additions / fresh-variable counts / modes plus the reducer tapes.
+//
+// Binary output: little-endian int32 / uint32 / uint64 / float records; the
+// layout is documented in tests/golden/make_golden.py which parses it.
+
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <string>
+#include <vector>
+
+#include "entities/flip_graph.cuh"
+#include "entities/scheme_additions_reducer.cuh"
+
+#define HCHECK(call) do { cudaError_t e_ = (call); if (e_ != cudaSuccess) { \
+    fprintf(stderr, "CUDA error %s at %s:%d\n", cudaGetErrorString(e_), __FILE__, __LINE__); exit(2); } } while (0)
+
+static void put_i32(FILE *f, int32_t v) { fwrite(&v, 4, 1, f); }
+static void put_u32(FILE *f, uint32_t v) { fwrite(&v, 4, 1, f); }
+static void put_u64(FILE *f, uint64_t v) { fwrite(&v, 8, 1, f); }
+
+#ifdef SCHEME_INTEGER
+static const int kRingIsZT = 1;
+static void put_factor(FILE *f, const Addition &a) { put_u64(f, a.values); put_u64(f, a.signs); put_i32(f, a.valid ? 1 : 0); }
+#else
+static const int kRingIsZT = 0;
+static void put_factor(FILE *f, const T &a) { put_u64(f, (uint64_t)a); }
+#endif
+
+static void put_scheme(FILE *f, const Scheme &s, bool withFlips) {
+    for (int i = 0; i < 3; i++) put_i32(f, s.n[i]);
+    put_i32(f, s.m);
+    for (int c = 0; c < 3; c++)
+        for (int t = 0; t < s.m; t++) put_factor(f, s.uvw[c][t]);
+    if (withFlips) {
+        for (int c = 0; c < 3; c++) {
+            put_i32(f, (int32_t)s.flips[c].size);
+            for (size_t p = 0; p < s.flips[c].size; p++) put_u32(f, s.flips[c].pairs[p]);
+        }
+    }
+}
+
+// Steps a fresh XORWOW stream (curand_init(seed, idx, 0)) and records every
+// draw as (curand() value, curand_uniform() value) until the stream equals the
+// walk's final state or maxDraws is reached.  Both values come from cuRAND
+// itself: one copy of the state is advanced with curand(), a second copy with
+// curand_uniform(); both consume exactly one 32-bit output per call.
+__global__ void tapeKernel(const curandState *finalStates, int count, int seed, int maxDraws,
+                           uint32_t *draws, float *uniforms, int *consumed) {
+    int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= count) return;
+    curandState a, b;
+    curand_init(seed, idx, 0, &a);
+    b = a;
+    const curandState &fin = finalStates[idx];
+    int used = -1;
+    for (int n = 0; n <= maxDraws; n++) {
+        bool same = a.d == fin.d;
+        for (int q = 0; q < 5; q++) same = same && a.v[q] == fin.v[q];
+        if (same) { used = n; break; }
+        if (n == maxDraws) break;
+        draws[(size_t)idx * maxDraws + n] = curand(&a);
+        uniforms[(size_t)idx * maxDraws + n] = curand_uniform(&b);
+    }
+    consumed[idx] = used;
+}
+
+static void write_tapes(FILE *f, const curandState *states, int count, int seed, int maxDraws) {
+    curandState *dStates; uint32_t *dDraws; float *dUni; int *dUsed;
+    HCHECK(cudaMalloc(&dStates, count * sizeof(curandState)));
+    HCHECK(cudaMemcpy(dStates, states, count * sizeof(curandState), cudaMemcpyDefault));
+    HCHECK(cudaMalloc(&dDraws, (size_t)count * maxDraws * 4));
+    HCHECK(cudaMalloc(&dUni, (size_t)count * maxDraws * 4));
+    HCHECK(cudaMalloc(&dUsed, count * 4));
+    tapeKernel<<<(count + 63) / 64, 64>>>(dStates, count, seed, maxDraws, dDraws, dUni, dUsed);
+    HCHECK(cudaGetLastError());
+    HCHECK(cudaDeviceSynchronize());
+    std::vector<uint32_t> draws((size_t)count * maxDraws);
+    std::vector<float> uni((size_t)count * maxDraws);
+    std::vector<int> used(count);
+    HCHECK(cudaMemcpy(draws.data(), dDraws, draws.size() * 4, cudaMemcpyDeviceToHost));
+    HCHECK(cudaMemcpy(uni.data(), dUni, uni.size() * 4, cudaMemcpyDeviceToHost));
+    HCHECK(cudaMemcpy(used.data(), dUsed, count * 4, cudaMemcpyDeviceToHost));
+    for (int w = 0; w < count; w++) {
+        put_i32(f, used[w]);
+        int n = used[w] < 0 ? 0 : used[w];
+        fwrite(&draws[(size_t)w * maxDraws], 4, n, f);
+        fwrite(&uni[(size_t)w * maxDraws], 4, n, f);
+    }
+    cudaFree(dStates); cudaFree(dDraws); cudaFree(dUni); cudaFree(dUsed);
+}
+
+static int cmd_walk(int argc, char **argv) {
+    if (argc != 13) { fprintf(stderr, "walk: bad arguments\n"); return 1; }
+    int n1 = atoi(argv[2]), n2 = atoi(argv[3]), n3 = atoi(argv[4]);
+    int S = atoi(argv[5]), iters = atoi(argv[6]), plusIters = atoi(argv[7]);
+    double expandP = atof(argv[8]), reduceP = atof(argv[9]);
+    int seed = atoi(argv[10]), launches = atoi(argv[11]);
+    const char *out = argv[12];
+    int blockSize = 32, numBlocks = (S + blockSize - 1) / blockSize;
+
+    Scheme *schemes, *best; int *bestRanks, *flips; curandState *states;
+    HCHECK(cudaMallocManaged(&schemes, S * sizeof(Scheme)));
+    HCHECK(cudaMallocManaged(&best, S * sizeof(Scheme)));
+    HCHECK(cudaMallocManaged(&bestRanks, S * sizeof(int)));
+    HCHECK(cudaMallocManaged(&flips, S * sizeof(int)));
+    HCHECK(cudaMallocManaged(&states, S * sizeof(curandState)));
+
+    initializeRandomStatesKernel<<<numBlocks, blockSize>>>(states, S, seed);
+    HCHECK(cudaDeviceSynchronize());
+    initializeNaiveKernel<<<numBlocks, blockSize>>>(schemes, S, n1, n2, n3);
+    HCHECK(cudaDeviceSynchronize());
+    initializeSchemesKernel<<<numBlocks, blockSize>>>(schemes, best, bestRanks, flips, n1, n2, n3, S);
+    HCHECK(cudaDeviceSynchronize());
+
+    FILE *f = fopen(out, "wb");
+    if (!f) { fprintf(stderr, "cannot open %s\n", out); return 1; }
+    put_i32(f, 0x46475731);  // magic "FGW1"
+    put_i32(f, kRingIsZT);
+    put_i32(f, n1); put_i32(f, n2); put_i32(f, n3);
+    put_i32(f, S); put_i32(f, iters); put_i32(f, plusIters);
+    fwrite(&expandP, 8, 1, f); fwrite(&reduceP, 8, 1, f);
+    put_i32(f, seed); put_i32(f, launches);
+    for (int w = 0; w < S; w++) put_scheme(f, schemes[w], true);   // initial state
+
+    for (int L = 0; L < launches; L++) {
+        randomWalkKernel<<<numBlocks, blockSize>>>(schemes, best, bestRanks, flips, states, S, iters, plusIters,
+                                                   reduceP, expandP, 0.0, 0.0, false);
+        HCHECK(cudaGetLastError());
+        HCHECK(cudaDeviceSynchronize());
+        for (int w = 0; w < S; w++) {
+            put_i32(f, flips[w]);
+            put_i32(f, bestRanks[w]);
+            put_scheme(f, schemes[w], true);
+            put_scheme(f, best[w], false);
+            put_i32(f, schemes[w].validate() ? 1 : 0);
+        }
+    }
+    // Tape long enough for any walk: bounded by the device buffer size.
+    size_t budget = (size_t)1 << 28;  // bytes for draws + uniforms
+    size_t perIter = kRingIsZT ? 700 : 40;  // ZT flips draw a permutation of all pairs
+    if (getenv("FG_NO_TAPE")) perIter = 0, budget = 0;  // walks run only to produce input schemes
+    int maxDraws = (int)std::min<size_t>(budget / (8 * (size_t)S), perIter * iters * launches + 4096);
+    write_tapes(f, states, S, seed, maxDraws);
+    fclose(f);
+    cudaFree(schemes); cudaFree(best); cudaFree(bestRanks); cudaFree(flips); cudaFree(states);
+    return 0;
+}
+
+static int cmd_reduce(int argc, char **argv) {
+    if (argc != 7) { fprintf(stderr, "reduce: bad arguments\n"); return 1; }
+    const char *in = argv[2];
+    int count = atoi(argv[3]), schemesCount = atoi(argv[4]), seed = atoi(argv[5]);
+    const char *out = argv[6];
+    typedef AdditionsReducer<MAX_U_EXPRESSIONS, MAX_U_FRESH_VARIABLES, MAX_U_REAL_VARIABLES, MAX_U_SUBEXPRESSIONS> RU;
+    typedef AdditionsReducer<MAX_V_EXPRESSIONS, MAX_V_FRESH_VARIABLES, MAX_V_REAL_VARIABLES, MAX_V_SUBEXPRESSIONS> RV;
+    typedef AdditionsReducer<MAX_W_EXPRESSIONS, MAX_W_FRESH_VARIABLES, MAX_W_REAL_VARIABLES, MAX_W_SUBEXPRESSIONS> RW;
+    RU *ru; RV *rv; RW *rw; SchemeInteger *schemes; curandState *states;
+    HCHECK(cudaMallocManaged(&ru, (count + 1) * sizeof(RU)));
+    HCHECK(cudaMallocManaged(&rv, (count + 1) * sizeof(RV)));
+    HCHECK(cudaMallocManaged(&rw, (count + 1) * sizeof(RW)));
+    HCHECK(cudaMallocManaged(&schemes, (count + 1) * sizeof(SchemeInteger)));
+    HCHECK(cudaMallocManaged(&states, count * sizeof(curandState)));
+    std::ifstream fin(in);
+    int n1, n2, n3, m;
+    fin >> n1 >> n2 >> n3 >> m;
+    if (!schemes[0].read(fin, n1, n2, n3, m, false)) { fprintf(stderr, "read failed\n"); return 1; }
+    int blockSize = 32, numBlocks = (count + blockSize - 1) / blockSize;
+    initializeKernel<<<numBlocks, blockSize>>>(ru, rv, rw, schemes, states, count, schemesCount, seed);
+    HCHECK(cudaGetLastError());
+    HCHECK(cudaDeviceSynchronize());
+    runReducersKernel<<<numBlocks, blockSize>>>(ru, rv, rw, schemes, states, count, schemesCount, true);
+    HCHECK(cudaGetLastError());
+    HCHECK(cudaDeviceSynchronize());
+    FILE *f = fopen(out, "wb");
+    put_i32(f, 0x46475231);  // magic "FGR1"
+    put_i32(f, count); put_i32(f, seed);
+    for (int r = 0; r <= count; r++) {
+        put_i32(f, ru[r].getAdditions()); put_i32(f, ru[r].getFreshVars()); put_i32(f, ru[r].getNaiveAdditions());
+        put_i32(f, rv[r].getAdditions()); put_i32(f, rv[r].getFreshVars()); put_i32(f, rv[r].getNaiveAdditions());
+        put_i32(f, rw[r].getAdditions()); put_i32(f, rw[r].getFreshVars()); put_i32(f, rw[r].getNaiveAdditions());
+        std::string modes = ru[r].getMode() + "," + rv[r].getMode() + "," + rw[r].getMode();
+        put_i32(f, (int)modes.size());
+        fwrite(modes.data(), 1, modes.size(), f);
+    }
+    int maxDraws = 1 << 18;
+    write_tapes(f, states, count, seed, maxDraws);
+    fclose(f);
+    return 0;
+}
+
+int main(int argc, char **argv) {
+    if (argc < 2) { fprintf(stderr, "usage: ref_harness walk|reduce ...\n"); return 1; }
+    std::string cmd = argv[1];
+    if (cmd == "walk") return cmd_walk(argc, argv);
+    if (cmd == "reduce") return cmd_reduce(argc, argv);
+    fprintf(stderr, "unknown command %s\n", argv[1]);
+    return 1;
+}

@@ -1,0 +1,193 @@
+#!/usr/bin/env python3
+"""Generates the golden fixtures under tests/golden/ from the reference itself.
+
+The reference (dronperminov/FlipGraphGPU) has no tests and ships no fixtures,
+so its behaviour is pinned by running its own CUDA code on a GB300 and
+recording what it does.  This script is run in two steps:
+
+  --run DIR   (on a GPU machine; needs the staged reference sources that
+              oracle/build_ref.sh puts under oracle/_ref/)
+              builds the reference, runs oracle/ref_harness (which drives the
+              reference's unmodified kernels) and the reference's three
+              executables, and writes raw outputs to DIR.
+  --pack DIR  (anywhere) copies the raw outputs into tests/golden/ as gzip
+              files plus a manifest.
+
+Walk dumps hold the complete per-walk state after each launch (scheme,
+FlipSet lists, flips counter, best rank, best scheme) and the exact XORWOW
+draw tape each walk consumed; the CPU oracle replays the tape and must
+reproduce every byte.  Binary layout: see tests/golden/golden_io.py.
+"""
+import argparse
+import glob
+import gzip
+import json
+import os
+import shutil
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, HERE)
+import golden_io  # noqa: E402
+
+# (name, ring, n1, n2, n3, walks, iterations, plus_iterations, expand_p, reduce_p, seed, launches)
+WALK_CASES = [
+    ("z2_333", "z2", 3, 3, 3, 6, 300, 50, 0.01, 0.0, 11, 2),
+    ("z2_222", "z2", 2, 2, 2, 6, 200, 20, 0.01, 0.0, 12, 2),
+    ("z2_444", "z2", 4, 4, 4, 3, 300, 100, 0.01, 0.0, 13, 1),
+    ("z2_234_expand", "z2", 2, 3, 4, 4, 300, 30, 60.0, 0.0, 14, 1),
+    ("z2_345_reduce", "z2", 3, 4, 5, 3, 200, 60, 0.01, 40.0, 15, 1),
+    ("zt_333", "zt", 3, 3, 3, 4, 100, 40, 0.01, 0.0, 21, 2),
+    ("zt_223_expand", "zt", 2, 2, 3, 6, 150, 20, 40.0, 0.0, 22, 1),
+    ("zt_444", "zt", 4, 4, 4, 2, 30, 100, 0.01, 0.0, 23, 1),
+    ("zt_233_reduce", "zt", 2, 3, 3, 4, 150, 30, 0.01, 40.0, 24, 1),
+]
+
+# Long walks used only to produce low-rank input schemes for the reducer and
+# minimizer runs (their dumps are not kept as fixtures).
+SOURCE_WALKS = [
+    ("src_zt_333", "zt", 3, 3, 3, 64, 3000, 2000, 0.01, 0.0, 31, 2),
+    ("src_z2_333", "z2", 3, 3, 3, 64, 4000, 2000, 0.01, 0.0, 32, 3),
+]
+
+
+def run(cmd, **kw):
+    print("+", " ".join(cmd), flush=True)
+    return subprocess.run(cmd, check=True, **kw)
+
+
+def binary(ring, name):
+    return os.path.join(ROOT, "oracle", "_ref", f"{ring}-{os.uname().machine}", name)
+
+
+def harness(ring):
+    return binary(ring, "ref_harness")
+
+
+def walk(out_dir, case, tape=True):
+    name, ring, n1, n2, n3, S, iters, plus, ep, rp, seed, launches = case
+    path = os.path.join(out_dir, f"walk_{name}.bin")
+    env = dict(os.environ)
+    if not tape:
+        env["FG_NO_TAPE"] = "1"
+    run([harness(ring), "walk", str(n1), str(n2), str(n3), str(S), str(iters), str(plus),
+         repr(ep), repr(rp), str(seed), str(launches), path], env=env)
+    return path
+
+
+def best_scheme_text(dump, header=True):
+    """Lowest-rank best scheme of a walk dump as reference input text."""
+    last = dump["launches"][-1]
+    k = min(range(len(last)), key=lambda w: last[w]["best"]["m"])
+    s = last[k]["best"]
+    return golden_io.scheme_to_text(s, dump["ring"], header=header), s
+
+
+def do_run(out_dir):
+    os.makedirs(out_dir, exist_ok=True)
+    run([os.path.join(ROOT, "oracle", "build_ref.sh")])
+    for case in WALK_CASES:
+        walk(out_dir, case)
+
+    # Input schemes for the reducer / minimizer / CLI runs.
+    inputs = {}
+    for case in SOURCE_WALKS:
+        path = walk(out_dir, case, tape=False)
+        dump = golden_io.read_walk(path)
+        os.remove(path)
+        text, s = best_scheme_text(dump)
+        inputs[case[1]] = (text, s)
+        with open(os.path.join(out_dir, f"input_{case[1]}_333.txt"), "w") as f:
+            f.write(text)
+
+    # Reducer kernel, one iteration, per-reducer counts + tapes.
+    for ring in ("zt", "z2"):
+        inp = os.path.join(out_dir, f"input_{ring}_333.txt")
+        run([harness("zt"), "reduce", inp, "12", "1", "41", os.path.join(out_dir, f"reduce_{ring}_333.bin")])
+
+    # End-to-end executables (outputs compared file for file).
+    ref_reduced = os.path.join(out_dir, "cli_additions_reducer")
+    os.makedirs(ref_reduced, exist_ok=True)
+    with open(os.path.join(out_dir, "cli_additions_reducer.log"), "w") as log:
+        run([binary("zt", "additions_reducer"), "-i", os.path.join(out_dir, "input_zt_333.txt"),
+             "-o", ref_reduced, "--count", "64", "--seed", "51"], stdout=log, stderr=subprocess.STDOUT)
+
+    # The minimizer reads "n1 n2 n3 m count" followed by the bodies.
+    text, s = inputs["z2"]
+    body = golden_io.scheme_to_text(s, "z2", header=False)
+    with open(os.path.join(out_dir, "input_minimizer_z2_333.txt"), "w") as f:
+        f.write(f"{s['n'][0]} {s['n'][1]} {s['n'][2]} {s['m']} 1\n" + body)
+    cm_dir = os.path.join(out_dir, "cli_complexity_minimizer")
+    os.makedirs(cm_dir, exist_ok=True)
+    with open(os.path.join(out_dir, "cli_complexity_minimizer.log"), "w") as log:
+        run([binary("z2", "complexity_minimizer"), "--input-path",
+             os.path.join(out_dir, "input_minimizer_z2_333.txt"), "--path", cm_dir,
+             "--schemes", "256", "--max-iterations", "2000", "--seed", "61"],
+            stdout=log, stderr=subprocess.STDOUT)
+
+    # flip_graph never returns (flip_graph.cu:286): run it for a bounded time;
+    # files named with iterations that completed are deterministic.
+    fg_dir = os.path.join(out_dir, "cli_flip_graph")
+    os.makedirs(fg_dir, exist_ok=True)
+    with open(os.path.join(out_dir, "cli_flip_graph.log"), "w") as log:
+        subprocess.run(["timeout", "20", binary("z2", "flip_graph"), "-n1", "3", "-n2", "3", "-n3", "3",
+                        "--schemes", "128", "--max-iterations", "1000", "--plus-iterations", "300",
+                        "--resize-probability", "0", "--path", fg_dir, "--seed", "71"],
+                       stdout=log, stderr=subprocess.STDOUT)
+    print("golden raw outputs written to", out_dir)
+
+
+# Reducer tapes above this many draws are dropped from the committed fixture
+# (their counts stay; tests skip reducers without a tape).
+MAX_REDUCER_TAPE = 4000
+
+
+def trimmed_reduce(path):
+    """Re-serialises a reduce dump, dropping tapes longer than MAX_REDUCER_TAPE."""
+    import struct
+    d = golden_io.read_reduce(path)
+    out = bytearray(struct.pack("<iii", 0x46475231, d["count"], d["seed"]))
+    for r in d["reducers"]:
+        out += struct.pack("<9i", *r["u"], *r["v"], *r["w"])
+        modes = ",".join(r["modes"]).encode()
+        out += struct.pack("<i", len(modes)) + modes
+    for t in d["tapes"]:
+        if t["used"] > MAX_REDUCER_TAPE or t["used"] < 0:
+            out += struct.pack("<i", -1)
+        else:
+            out += struct.pack("<i", t["used"]) + t["draws"].tobytes() + t["uniforms"].tobytes()
+    return bytes(out)
+
+
+def do_pack(raw_dir):
+    manifest = {"walk_cases": [list(c) for c in WALK_CASES], "files": []}
+    for path in sorted(glob.glob(os.path.join(raw_dir, "*.bin")) + glob.glob(os.path.join(raw_dir, "*.txt"))
+                       + glob.glob(os.path.join(raw_dir, "*.log"))):
+        base = os.path.basename(path)
+        dst = os.path.join(HERE, base + ".gz")
+        data = trimmed_reduce(path) if base.startswith("reduce_") else open(path, "rb").read()
+        with gzip.open(dst, "wb", compresslevel=9) as fo:
+            fo.write(data)
+        manifest["files"].append(base)
+    for sub in ("cli_additions_reducer", "cli_complexity_minimizer", "cli_flip_graph"):
+        src = os.path.join(raw_dir, sub)
+        if os.path.isdir(src):
+            dst = os.path.join(HERE, sub)
+            shutil.rmtree(dst, ignore_errors=True)
+            shutil.copytree(src, dst)
+            manifest["files"] += [f"{sub}/{x}" for x in sorted(os.listdir(dst))]
+    with open(os.path.join(HERE, "manifest.json"), "w") as f:
+        json.dump(manifest, f, indent=1)
+
+
+if __name__ == "__main__":
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--run")
+    ap.add_argument("--pack")
+    a = ap.parse_args()
+    if a.run:
+        do_run(a.run)
+    if a.pack:
+        do_pack(a.pack)

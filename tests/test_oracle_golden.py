@@ -1,0 +1,104 @@
+"""The CPU oracle against the reference's own outputs (tests/golden/).
+
+The fixtures were recorded from the reference's unmodified CUDA kernels on a
+GB300 (tests/golden/make_golden.py).  Replaying each walk's recorded XORWOW
+tape, the oracle must reproduce every launch's state byte for byte: factors,
+FlipSet list order, flips counter, best rank, best scheme, and the exact
+number of draws the reference consumed.
+"""
+import gzip
+import os
+
+import numpy as np
+import pytest
+
+import golden_io
+from helpers import diff_walk, golden, read_scheme_text, walk_fixtures
+from oracle import oracle as O
+
+
+@pytest.mark.parametrize("path", walk_fixtures(), ids=lambda p: os.path.basename(p).split(".")[0])
+def test_walk_matches_reference(path):
+    d = golden_io.read_walk(path)
+    ring, S = d["ring"], d["walks"]
+    n1, n2, n3 = d["n"]
+    batch = O.WalkBatch(S, n1 * n2 * n3, ring)
+    O.init_naive(batch, n1, n2, n3)
+    for w in range(S):
+        init = {"scheme": d["initial"][w], "flips": 0, "best_rank": n1 * n2 * n3, "best": d["initial"][w]}
+        assert not diff_walk(batch, w, init, ring), "naive scheme differs from the reference's"
+    tape = O.make_tape([(t["draws"], t["uniforms"]) for t in d["tapes"]])
+    for L, block in enumerate(d["launches"]):
+        cfg = batch.cfg("tape", d["iterations"], d["plus_iterations"], 1, d["expand_p"], d["reduce_p"])
+        O.walk(batch, cfg, tape)
+        assert not batch.status.any()
+        for w in range(S):
+            assert not diff_walk(batch, w, block[w], ring), f"launch {L} walk {w}"
+        assert O.validate(batch).all()
+    assert [int(x) for x in batch.rng_pos] == [t["used"] for t in d["tapes"]]
+
+
+@pytest.mark.parametrize("ring", ["zt", "z2"])
+def test_reducer_matches_reference(ring):
+    with gzip.open(golden(f"input_{ring}_333.txt.gz"), "rt") as f:
+        n, m, coef = read_scheme_text(f.read())
+    d = golden_io.read_reduce(golden(f"reduce_{ring}_333.bin.gz"))
+    keep = [r for r in range(d["count"]) if d["tapes"][r]["used"] >= 0]
+    assert len(keep) >= 3
+    tape = O.make_tape([(t["draws"], t["uniforms"]) for t in d["tapes"]])
+    out, modes, consumed, state = O.reduce(n, m, coef, d["count"], tape)
+    O.reducer_state_free(state)
+    for r in keep:
+        ref = d["reducers"][r]
+        assert (tuple(out[r, 0:3]), tuple(out[r, 3:6]), tuple(out[r, 6:9])) == (ref["u"], ref["v"], ref["w"]), r
+        assert consumed[r] == d["tapes"][r]["used"], r
+
+
+@pytest.mark.parametrize("shape", [(2, 2, 2), (2, 3, 4), (3, 3, 3), (4, 4, 4), (3, 4, 5), (4, 5, 8)])
+def test_naive_schemes_validate(shape):
+    n1, n2, n3 = shape
+    for ring in ("z2", "zt"):
+        b = O.WalkBatch(2, n1 * n2 * n3, ring)
+        O.init_naive(b, n1, n2, n3)
+        assert O.validate(b).all()
+        # A single flipped bit breaks the Brent equations.
+        b.fac[1, 2, 0] ^= 1
+        assert list(O.validate(b)) == [True, False]
+
+
+def test_reference_inputs_validate():
+    for ring in ("z2", "zt"):
+        with gzip.open(golden(f"input_{ring}_333.txt.gz"), "rt") as f:
+            (n1, n2, n3), m, coef = read_scheme_text(f.read())
+        fac = np.zeros((1, 3, m), np.uint64)
+        sgn = np.zeros((1, 3, m), np.uint64)
+        for c in range(3):
+            for t in range(m):
+                for j in range(64):
+                    if coef[c, t, j]:
+                        fac[0, c, t] |= np.uint64(1 << j)
+                        if coef[c, t, j] < 0:
+                            sgn[0, c, t] |= np.uint64(1 << j)
+        n = np.array([[n1, n2, n3]], np.int32)
+        mm = np.array([m], np.int32)
+        assert O.validate_arrays("z2", n, mm, fac)[0]  # every ZT scheme is also valid mod 2
+        ok_zt = O.validate_arrays("zt", n, mm, fac, sgn, np.ones((1, 3, m), np.uint8))[0]
+        assert ok_zt == (ring == "zt")
+
+
+def test_philox_known_answer():
+    # Random123 known-answer vector for Philox4x32-10 with zero counter and key.
+    assert O.philox([0, 0, 0, 0], [0, 0]) == [0x6627E8D5, 0xE169C58D, 0xBC57AC4C, 0x9B00DBD8]
+
+
+def test_fast_mode_walk_is_deterministic_and_valid():
+    b1 = O.WalkBatch(8, 27, "z2")
+    O.init_naive(b1, 3, 3, 3)
+    b2 = b1.copy()
+    cfg = b1.cfg("philox", iterations=2000, plus_iterations=300, launches=2, seed=7)
+    O.walk(b1, cfg)
+    O.walk(b2, cfg)
+    for f in ("m", "fac", "list_size", "list_pairs", "rng_pos", "best_m", "best_fac"):
+        assert np.array_equal(getattr(b1, f), getattr(b2, f))
+    assert O.validate(b1).all() and O.validate(b1, best=True).all()
+    assert (b1.best_m < 27).any()
