@@ -1,0 +1,189 @@
+"""flipgraphgpu_gb300 -- GB300-native flip-graph search for matrix multiplication schemes.
+
+Python view of libflipgraph.so's C ABI (include/flipgraph.h).  The search
+itself runs in hand-written sm_103a CUDA kernels; this module only moves
+records and calls the library.  There is no CPU fallback: if the CUDA
+library cannot be loaded every entry point raises.
+
+    from flipgraphgpu_gb300 import Engine
+    eng = Engine(walks=1024, cap=27, seed=1, iterations=10000, plus_iterations=50000)
+    eng.init_naive(3, 3, 3)
+    stats = eng.run(launches=1)
+    rec = eng.records()
+"""
+import ctypes
+import os
+import platform
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "_lib", platform.machine(), "libflipgraph.so")
+LIST_CAP = 500
+MAX_RANK = 350
+RINGS = {"z2": 0, "zt": 1}
+RNGS = {"xorwow": 0, "philox": 1}
+STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "capacity", 4: "state", 5: "walk failure"}
+
+
+class FlipGraphError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__(f"{STATUS.get(status, status)}: {msg}")
+        self.status = status
+
+
+class Config(ctypes.Structure):
+    _fields_ = [("ring", ctypes.c_int32), ("rng", ctypes.c_int32), ("walks", ctypes.c_int32),
+                ("cap", ctypes.c_int32), ("seed", ctypes.c_uint64), ("iterations", ctypes.c_int32),
+                ("plus_iterations", ctypes.c_int32), ("expand_p", ctypes.c_double), ("reduce_p", ctypes.c_double),
+                ("device", ctypes.c_int32), ("walks_per_block", ctypes.c_int32)]
+
+
+class _Records(ctypes.Structure):
+    _fields_ = [(name, ctypes.c_void_p) for name in
+                ("n", "m", "fac", "sgn", "valid", "list_size", "list_pairs", "flips", "best_rank",
+                 "best_m", "best_fac", "best_sgn", "best_valid", "rng_pos", "status")]
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [("flips", ctypes.c_uint64), ("verified_flips", ctypes.c_uint64), ("walks_valid", ctypes.c_int32),
+                ("walks_failed", ctypes.c_int32), ("min_rank", ctypes.c_int32), ("min_best_rank", ctypes.c_int32),
+                ("kernel_ms", ctypes.c_float), ("verify_ms", ctypes.c_float)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+_lib = None
+
+
+def library():
+    """Loads libflipgraph.so (building it first when only sources are present)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        from . import build as _build
+        _build.build()
+    lib = ctypes.CDLL(LIB_PATH)
+    lib.fg_last_error.restype = ctypes.c_char_p
+    lib.fg_version.restype = ctypes.c_char_p
+    for name in ("fg_create", "fg_destroy", "fg_init_naive", "fg_set_records", "fg_get_records", "fg_run",
+                 "fg_minimize", "fg_validate", "fg_xorwow_tape", "fg_philox_blocks"):
+        getattr(lib, name).restype = ctypes.c_int
+    _lib = lib
+    return lib
+
+
+def _check(status):
+    if status != 0:
+        raise FlipGraphError(status, library().fg_last_error().decode())
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+class Records:
+    """Host walk records (the C ABI's fg_records), numpy arrays."""
+
+    FIELDS = _Records._fields_
+
+    def __init__(self, walks, cap, ring="z2"):
+        zt = ring == "zt"
+        self.walks, self.cap, self.ring = walks, cap, ring
+        self.n = np.zeros((walks, 3), np.int32)
+        self.m = np.zeros(walks, np.int32)
+        self.fac = np.zeros((walks, 3, cap), np.uint64)
+        self.sgn = np.zeros((walks, 3, cap), np.uint64) if zt else None
+        self.valid = np.zeros((walks, 3, cap), np.uint8) if zt else None
+        self.list_size = np.zeros((walks, 3), np.int32)
+        self.list_pairs = np.zeros((walks, 3, LIST_CAP), np.uint32)
+        self.flips = np.zeros(walks, np.int32)
+        self.best_rank = np.zeros(walks, np.int32)
+        self.best_m = np.zeros(walks, np.int32)
+        self.best_fac = np.zeros((walks, 3, cap), np.uint64)
+        self.best_sgn = np.zeros((walks, 3, cap), np.uint64) if zt else None
+        self.best_valid = np.zeros((walks, 3, cap), np.uint8) if zt else None
+        self.rng_pos = np.zeros(walks, np.int64)
+        self.status = np.zeros(walks, np.int32)
+
+    def _c(self):
+        return _Records(*[_ptr(getattr(self, f)) for f, _ in self.FIELDS])
+
+
+class Engine:
+    """One fg_handle: `walks` independent walks on one GPU."""
+
+    def __init__(self, walks, cap, ring="z2", rng="xorwow", seed=1, iterations=10000, plus_iterations=8000,
+                 expand_p=0.01, reduce_p=0.0, device=0, walks_per_block=0):
+        self.lib = library()
+        self.cfg = Config(RINGS[ring], RNGS[rng], walks, cap, seed, iterations, plus_iterations, expand_p,
+                          reduce_p, device, walks_per_block)
+        self.walks, self.cap, self.ring = walks, cap, ring
+        self.h = ctypes.c_void_p()
+        _check(self.lib.fg_create(ctypes.byref(self.cfg), ctypes.byref(self.h)))
+
+    def close(self):
+        if self.h:
+            self.lib.fg_destroy(self.h)
+            self.h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def init_naive(self, n1, n2, n3):
+        _check(self.lib.fg_init_naive(self.h, n1, n2, n3))
+
+    def set_records(self, rec):
+        c = rec._c()
+        _check(self.lib.fg_set_records(self.h, ctypes.byref(c)))
+
+    def records(self):
+        rec = Records(self.walks, self.cap, self.ring)
+        c = rec._c()
+        _check(self.lib.fg_get_records(self.h, ctypes.byref(c)))
+        return rec
+
+    def run(self, launches=1):
+        st = Stats()
+        _check(self.lib.fg_run(self.h, launches, ctypes.byref(st)))
+        return st.as_dict()
+
+    def minimize(self, best_complexity):
+        bc = np.ascontiguousarray(best_complexity, np.int32)
+        _check(self.lib.fg_minimize(self.h, _ptr(bc)))
+        return bc
+
+    def validate(self, best=False):
+        out = np.zeros(self.walks, np.uint8)
+        _check(self.lib.fg_validate(self.h, int(best), _ptr(out)))
+        return out.astype(bool)
+
+
+def xorwow_tape(seed, first_walk, count, draws, device=0):
+    """The reference's per-walk cuRAND XORWOW stream, recorded on the GPU."""
+    d = np.zeros((count, draws), np.uint32)
+    u = np.zeros((count, draws), np.float32)
+    _check(library().fg_xorwow_tape(ctypes.c_uint64(seed), first_walk, count, draws, device, _ptr(d), _ptr(u)))
+    return d, u
+
+
+def philox_blocks(ctr, key, device=0):
+    ctr = np.ascontiguousarray(ctr, np.uint32).reshape(-1, 4)
+    out = np.zeros_like(ctr)
+    _check(library().fg_philox_blocks(_ptr(ctr), len(ctr), key[0], key[1], device, _ptr(out)))
+    return out
+
+
+def version():
+    return library().fg_version().decode()

@@ -1,0 +1,444 @@
+// C-ABI of libflipgraph (include/flipgraph.h): handle lifetime, record
+// transfer, launches, exact verification and test-support streams.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/flipgraph.h"
+#include "launch.h"
+
+using namespace fg;
+
+namespace {
+
+thread_local std::string g_err;
+
+fg_status fail(fg_status st, const std::string &msg) {
+    g_err = msg;
+    return st;
+}
+
+#define FG_CUDA(call)                                                                              \
+    do {                                                                                           \
+        cudaError_t e_ = (call);                                                                   \
+        if (e_ != cudaSuccess)                                                                     \
+            return fail(FG_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));          \
+    } while (0)
+
+// ---------------------------------------------------------------- small kernels
+__global__ void k_init_xorwow(curandStateXORWOW_t *st, int S, unsigned long long seed) {
+    int w = blockIdx.x * blockDim.x + threadIdx.x;
+    if (w < S) curand_init(seed, (unsigned long long)w, 0ull, &st[w]);  // flip_graph.cu:450
+}
+
+// initializeNaive (scheme_z2.cu:32-55 / scheme_integer.cu:41-64) + initializeSchemesKernel
+// (flip_graph.cu:510-518); lists are built afterwards by the rebuild kernel.
+__global__ void k_init_naive(DevBatch B, int n1, int n2, int n3, int zt) {
+    int w = blockIdx.x * blockDim.x + threadIdx.x;
+    if (w >= B.S) return;
+    const int cap = B.cap;
+    uint64_t *f = B.fac + (size_t)w * 3 * cap, *bf = B.best_fac + (size_t)w * 3 * cap;
+    for (int q = 0; q < 3 * cap; q++) { f[q] = 0; bf[q] = 0; }
+    if (zt) {
+        uint64_t *g = B.sgn + (size_t)w * 3 * cap, *bg = B.best_sgn + (size_t)w * 3 * cap;
+        uint8_t *v = B.valid + (size_t)w * 3 * cap, *bv = B.best_valid + (size_t)w * 3 * cap;
+        for (int q = 0; q < 3 * cap; q++) { g[q] = 0; bg[q] = 0; v[q] = 0; bv[q] = 0; }
+    }
+    for (int i = 0; i < n1; i++)
+        for (int j = 0; j < n3; j++)
+            for (int k = 0; k < n2; k++) {
+                int t = (i * n3 + j) * n2 + k;
+                uint64_t a = 1ull << (i * n2 + k), b = 1ull << (k * n3 + j), c = 1ull << (j * n1 + i);
+                f[t] = bf[t] = a;
+                f[cap + t] = bf[cap + t] = b;
+                f[2 * cap + t] = bf[2 * cap + t] = c;
+                if (zt)
+                    for (int q = 0; q < 3; q++) {
+                        B.valid[(size_t)w * 3 * cap + q * cap + t] = 1;
+                        B.best_valid[(size_t)w * 3 * cap + q * cap + t] = 1;
+                    }
+            }
+    WalkHeader h = B.hdr[w];
+    h.n[0] = n1; h.n[1] = n2; h.n[2] = n3;
+    h.m = n1 * n2 * n3;
+    h.flips = 0;
+    h.best_rank = n1 * n2 * n3;
+    h.best_m = n1 * n2 * n3;
+    h.status = 0;
+    h.list_size[0] = h.list_size[1] = h.list_size[2] = 0;
+    h.valid = 0;
+    h.flips_done = 0;
+    B.hdr[w] = h;
+}
+
+// Exact Brent check (scheme_z2.cu:3-29), one warp per walk, bit-sliced over k:
+// for every (i, j), XOR over terms of [u_t(i) & v_t(j)] * w_t must equal the
+// single target bit k = (j % n2) * n0 + i / n1 when i % n1 == j / n2, else 0.
+__global__ void k_verify_z2(DevBatch B, int best, uint8_t *out) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int wpb = blockDim.x >> 5, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int cap = B.cap;
+    uint64_t *x = reinterpret_cast<uint64_t *>(smem) + (size_t)warp * 3 * cap;
+    for (int w = blockIdx.x * wpb + warp; w < B.S; w += gridDim.x * wpb) {
+        const WalkHeader h = B.hdr[w];
+        const uint64_t *src = (best ? B.best_fac : B.fac) + (size_t)w * 3 * cap;
+        for (int q = lane; q < 3 * cap; q += 32) x[q] = src[q];
+        __syncwarp();
+        const int n0 = h.n[0], n1 = h.n[1], n2 = h.n[2];
+        const int nn0 = n0 * n1, nn1 = n1 * n2, nn2 = n2 * n0;
+        const int m = best ? h.best_m : h.m;
+        const uint64_t kmask = nn2 >= 64 ? ~0ull : ((1ull << nn2) - 1);
+        bool ok = m >= 0 && m <= cap;
+        for (int q = lane; ok && q < nn0 * nn1; q += 32) {
+            const int i = q / nn1, j = q % nn1;
+            uint64_t acc = 0;
+            for (int t = 0; t < m; t++)
+                if (((x[t] >> i) & (x[cap + t] >> j)) & 1ull) acc ^= x[2 * cap + t];
+            uint64_t target = (i % n1 == j / n2) ? (1ull << ((j % n2) * n0 + i / n1)) : 0ull;
+            ok = (acc & kmask) == target;
+        }
+        ok = __all_sync(kFull, ok);
+        if (lane == 0) {
+            out[w] = ok;
+            if (!best) B.hdr[w].valid = ok;
+        }
+        __syncwarp();
+    }
+}
+
+__global__ void k_tape(unsigned long long seed, int first, int count, int draws, uint32_t *d, float *u) {
+    int w = blockIdx.x * blockDim.x + threadIdx.x;
+    if (w >= count) return;
+    curandStateXORWOW_t a, b;
+    curand_init(seed, (unsigned long long)(first + w), 0ull, &a);
+    b = a;
+    for (int q = 0; q < draws; q++) {
+        d[(size_t)w * draws + q] = curand(&a);
+        u[(size_t)w * draws + q] = curand_uniform(&b);
+    }
+}
+
+__global__ void k_philox(const uint4 *ctr, int count, uint32_t k0, uint32_t k1, uint4 *out) {
+    int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q < count) out[q] = philox4x32_10(ctr[q], k0, k1);
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------- handle
+struct fg_handle {
+    fg_config cfg;
+    int dev = 0, sms = 0, wpb = 4, grid = 1;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    DevBatch B{};
+    WalkParams P{};
+    int32_t *d_bestC = nullptr;
+    uint8_t *d_valid = nullptr;
+    bool ready = false;
+};
+
+namespace {
+
+template <class T> fg_status dalloc(T **p, size_t count) {
+    *p = nullptr;
+    if (!count) return FG_OK;
+    FG_CUDA(cudaMalloc((void **)p, count * sizeof(T)));
+    FG_CUDA(cudaMemset(*p, 0, count * sizeof(T)));
+    return FG_OK;
+}
+
+void compute_params(fg_handle *h) {
+    const fg_config &c = h->cfg;
+    WalkParams &P = h->P;
+    P.iterations = c.iterations;
+    P.plus_iterations = c.plus_iterations;
+    P.reduce_gate_f = ceil_to_float(c.reduce_p);
+    P.expand_gate_f = ceil_to_float(c.expand_p);
+    P.zero_gate_f = 0.0f;
+    P.tie_gate_f = ceil_to_float(0.01);
+    auto thr = [&](double p) -> uint64_t {
+        if (!(p > 0)) return 0;
+        double q = p / (double)c.iterations;
+        return q >= 1.0 ? (1ull << 32) : (uint64_t)(q * 4294967296.0);
+    };
+    P.reduce_T = thr(c.reduce_p);
+    P.expand_T = thr(c.expand_p);
+    P.key0 = (uint32_t)c.seed;
+    P.key1 = (uint32_t)(c.seed >> 32);
+}
+
+int verify_grid(fg_handle *h) { return (h->B.S + 3) / 4; }
+size_t verify_smem(fg_handle *h) { return (size_t)4 * 3 * h->B.cap * sizeof(uint64_t); }
+
+fg_status launch_verify(fg_handle *h, int best) {
+    if (h->cfg.ring != FG_RING_Z2) return fail(FG_ERR_ARG, "ring not supported");
+    size_t smem = verify_smem(h);
+    FG_CUDA(cudaFuncSetAttribute(k_verify_z2, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    k_verify_z2<<<verify_grid(h), 128, smem, h->stream>>>(h->B, best, h->d_valid);
+    FG_CUDA(cudaGetLastError());
+    return FG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *fg_last_error(void) { return g_err.c_str(); }
+const char *fg_version(void) { return "flipgraph-gb300 0.1 (sm_103a)"; }
+
+fg_status fg_create(const fg_config *cfg, fg_handle **out) {
+    if (!cfg || !out) return fail(FG_ERR_ARG, "null argument");
+    *out = nullptr;
+    if (cfg->walks <= 0) return fail(FG_ERR_ARG, "walks must be positive");
+    if (cfg->ring != FG_RING_Z2) return fail(FG_ERR_ARG, "only the Z2 ring is available in this build");
+    if (cfg->rng != FG_RNG_XORWOW && cfg->rng != FG_RNG_PHILOX) return fail(FG_ERR_ARG, "unknown rng");
+    if (cfg->cap <= 0 || slots_for_cap(cfg->cap) == 0 || cfg->cap > FG_MAX_RANK + 2)
+        return fail(FG_ERR_CAPACITY, "cap must be in [1, 352]");
+    if (cfg->iterations <= 0) return fail(FG_ERR_ARG, "iterations must be positive");
+    fg_handle *h = new fg_handle;
+    h->cfg = *cfg;
+    h->dev = cfg->device;
+    if (cudaSetDevice(h->dev) != cudaSuccess) { delete h; return fail(FG_ERR_CUDA, "cudaSetDevice failed"); }
+    cudaDeviceGetAttribute(&h->sms, cudaDevAttrMultiProcessorCount, h->dev);
+    h->wpb = cfg->walks_per_block > 0 ? cfg->walks_per_block : 4;
+    const int S = cfg->walks, cap = cfg->cap;
+    h->B.S = S;
+    h->B.cap = cap;
+    fg_status st = FG_OK;
+    size_t nf = (size_t)S * 3 * cap;
+    if ((st = dalloc(&h->B.hdr, (size_t)S)) || (st = dalloc(&h->B.fac, nf)) || (st = dalloc(&h->B.best_fac, nf)) ||
+        (st = dalloc(&h->B.lists, (size_t)S * 3 * kListCap)) || (st = dalloc(&h->d_bestC, (size_t)S)) ||
+        (st = dalloc(&h->d_valid, (size_t)S))) {
+        fg_destroy(h);
+        return st;
+    }
+    if (cfg->ring == FG_RING_ZT) {
+        if ((st = dalloc(&h->B.sgn, nf)) || (st = dalloc(&h->B.best_sgn, nf)) || (st = dalloc(&h->B.valid, nf)) ||
+            (st = dalloc(&h->B.best_valid, nf))) {
+            fg_destroy(h);
+            return st;
+        }
+    }
+    if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        fg_destroy(h);
+        return fail(FG_ERR_CUDA, "stream creation failed");
+    }
+    for (auto &e : h->ev) cudaEventCreate(&e);
+    compute_params(h);
+    if (cfg->rng == FG_RNG_XORWOW) {
+        if ((st = dalloc(&h->B.xorwow, (size_t)S))) { fg_destroy(h); return st; }
+        k_init_xorwow<<<(S + 127) / 128, 128, 0, h->stream>>>(h->B.xorwow, S, (unsigned long long)cfg->seed);
+        if (cudaGetLastError() != cudaSuccess || cudaStreamSynchronize(h->stream) != cudaSuccess) {
+            fg_destroy(h);
+            return fail(FG_ERR_CUDA, "seeding failed");
+        }
+    }
+    int occ = occupancy_walk_z2(cap, cfg->rng, h->wpb);
+    if (occ <= 0) occ = 1;
+    int need = (S + h->wpb - 1) / h->wpb;
+    h->grid = need < occ * h->sms ? need : occ * h->sms;
+    *out = h;
+    return FG_OK;
+}
+
+fg_status fg_destroy(fg_handle *h) {
+    if (!h) return FG_OK;
+    cudaSetDevice(h->dev);
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    void *ptrs[] = {h->B.hdr, h->B.fac, h->B.sgn, h->B.valid, h->B.lists, h->B.best_fac, h->B.best_sgn,
+                    h->B.best_valid, h->B.xorwow, h->d_bestC, h->d_valid};
+    for (void *p : ptrs)
+        if (p) cudaFree(p);
+    for (auto &e : h->ev)
+        if (e) cudaEventDestroy(e);
+    if (h->stream) cudaStreamDestroy(h->stream);
+    delete h;
+    return FG_OK;
+}
+
+fg_status fg_init_naive(fg_handle *h, int n1, int n2, int n3) {
+    if (!h) return fail(FG_ERR_ARG, "null handle");
+    if (n1 <= 0 || n2 <= 0 || n3 <= 0 || n1 * n2 > 64 || n2 * n3 > 64 || n3 * n1 > 64)
+        return fail(FG_ERR_ARG, "matrix sizes exceed 64 elements");
+    if (n1 * n2 * n3 > h->B.cap) return fail(FG_ERR_CAPACITY, "naive rank exceeds cap");
+    FG_CUDA(cudaSetDevice(h->dev));
+    k_init_naive<<<(h->B.S + 127) / 128, 128, 0, h->stream>>>(h->B, n1, n2, n3, h->cfg.ring == FG_RING_ZT);
+    FG_CUDA(cudaGetLastError());
+    FG_CUDA(launch_rebuild_z2(h->B, h->wpb, h->grid, h->stream));
+    FG_CUDA(cudaStreamSynchronize(h->stream));
+    h->ready = true;
+    return FG_OK;
+}
+
+fg_status fg_set_records(fg_handle *h, const fg_records *rec) {
+    if (!h || !rec || !rec->n || !rec->m || !rec->fac || !rec->list_size || !rec->list_pairs)
+        return fail(FG_ERR_ARG, "null argument");
+    FG_CUDA(cudaSetDevice(h->dev));
+    const int S = h->B.S, cap = h->B.cap;
+    size_t nf = (size_t)S * 3 * cap;
+    std::vector<WalkHeader> hdr(S);
+    FG_CUDA(cudaMemcpy(hdr.data(), h->B.hdr, sizeof(WalkHeader) * S, cudaMemcpyDeviceToHost));
+    for (int w = 0; w < S; w++) {
+        WalkHeader &o = hdr[w];
+        for (int c = 0; c < 3; c++) o.n[c] = rec->n[w * 3 + c];
+        o.m = rec->m[w];
+        if (o.m < 0 || o.m > cap) return fail(FG_ERR_CAPACITY, "record rank exceeds cap");
+        for (int c = 0; c < 3; c++) {
+            o.list_size[c] = rec->list_size[w * 3 + c];
+            if (o.list_size[c] < 0 || o.list_size[c] > kListCap) return fail(FG_ERR_CAPACITY, "list size");
+        }
+        o.flips = rec->flips ? rec->flips[w] : 0;
+        o.best_rank = rec->best_rank ? rec->best_rank[w] : o.m;
+        o.best_m = rec->best_m ? rec->best_m[w] : o.m;
+        o.status = rec->status ? rec->status[w] : 0;
+        o.valid = 0;
+    }
+    FG_CUDA(cudaMemcpy(h->B.hdr, hdr.data(), sizeof(WalkHeader) * S, cudaMemcpyHostToDevice));
+    FG_CUDA(cudaMemcpy(h->B.fac, rec->fac, nf * sizeof(uint64_t), cudaMemcpyHostToDevice));
+    FG_CUDA(cudaMemcpy(h->B.lists, rec->list_pairs, (size_t)S * 3 * kListCap * 4, cudaMemcpyHostToDevice));
+    FG_CUDA(cudaMemcpy(h->B.best_fac, rec->best_fac ? rec->best_fac : rec->fac, nf * sizeof(uint64_t),
+                       cudaMemcpyHostToDevice));
+    if (h->cfg.ring == FG_RING_ZT) {
+        if (!rec->sgn || !rec->valid) return fail(FG_ERR_ARG, "ZT records need sgn and valid");
+        FG_CUDA(cudaMemcpy(h->B.sgn, rec->sgn, nf * 8, cudaMemcpyHostToDevice));
+        FG_CUDA(cudaMemcpy(h->B.valid, rec->valid, nf, cudaMemcpyHostToDevice));
+        FG_CUDA(cudaMemcpy(h->B.best_sgn, rec->best_sgn ? rec->best_sgn : rec->sgn, nf * 8, cudaMemcpyHostToDevice));
+        FG_CUDA(cudaMemcpy(h->B.best_valid, rec->best_valid ? rec->best_valid : rec->valid, nf, cudaMemcpyHostToDevice));
+    }
+    h->ready = true;
+    return FG_OK;
+}
+
+fg_status fg_get_records(fg_handle *h, fg_records *rec) {
+    if (!h || !rec) return fail(FG_ERR_ARG, "null argument");
+    FG_CUDA(cudaSetDevice(h->dev));
+    FG_CUDA(cudaStreamSynchronize(h->stream));
+    const int S = h->B.S, cap = h->B.cap;
+    size_t nf = (size_t)S * 3 * cap;
+    std::vector<WalkHeader> hdr(S);
+    FG_CUDA(cudaMemcpy(hdr.data(), h->B.hdr, sizeof(WalkHeader) * S, cudaMemcpyDeviceToHost));
+    for (int w = 0; w < S; w++) {
+        const WalkHeader &o = hdr[w];
+        if (rec->n) for (int c = 0; c < 3; c++) rec->n[w * 3 + c] = o.n[c];
+        if (rec->m) rec->m[w] = o.m;
+        if (rec->list_size) for (int c = 0; c < 3; c++) rec->list_size[w * 3 + c] = o.list_size[c];
+        if (rec->flips) rec->flips[w] = o.flips;
+        if (rec->best_rank) rec->best_rank[w] = o.best_rank;
+        if (rec->best_m) rec->best_m[w] = o.best_m;
+        if (rec->rng_pos) rec->rng_pos[w] = (int64_t)o.draws;
+        if (rec->status) rec->status[w] = o.status;
+    }
+    if (rec->fac) FG_CUDA(cudaMemcpy(rec->fac, h->B.fac, nf * 8, cudaMemcpyDeviceToHost));
+    if (rec->best_fac) FG_CUDA(cudaMemcpy(rec->best_fac, h->B.best_fac, nf * 8, cudaMemcpyDeviceToHost));
+    if (rec->list_pairs) FG_CUDA(cudaMemcpy(rec->list_pairs, h->B.lists, (size_t)S * 3 * kListCap * 4, cudaMemcpyDeviceToHost));
+    if (h->cfg.ring == FG_RING_ZT) {
+        if (rec->sgn) FG_CUDA(cudaMemcpy(rec->sgn, h->B.sgn, nf * 8, cudaMemcpyDeviceToHost));
+        if (rec->valid) FG_CUDA(cudaMemcpy(rec->valid, h->B.valid, nf, cudaMemcpyDeviceToHost));
+        if (rec->best_sgn) FG_CUDA(cudaMemcpy(rec->best_sgn, h->B.best_sgn, nf * 8, cudaMemcpyDeviceToHost));
+        if (rec->best_valid) FG_CUDA(cudaMemcpy(rec->best_valid, h->B.best_valid, nf, cudaMemcpyDeviceToHost));
+    }
+    return FG_OK;
+}
+
+fg_status fg_run(fg_handle *h, int launches, fg_stats *stats) {
+    if (!h) return fail(FG_ERR_ARG, "null handle");
+    if (!h->ready) return fail(FG_ERR_STATE, "records not initialised");
+    if (launches < 0) return fail(FG_ERR_ARG, "launches must be >= 0");
+    FG_CUDA(cudaSetDevice(h->dev));
+    const int S = h->B.S;
+    fg_stats acc{};
+    acc.min_rank = acc.min_best_rank = 1 << 30;
+    std::vector<WalkHeader> hdr(S);
+    for (int L = 0; L < launches; L++) {
+        FG_CUDA(cudaEventRecord(h->ev[0], h->stream));
+        FG_CUDA(launch_walk_z2(h->B, h->P, h->cfg.rng, h->wpb, h->grid, h->stream));
+        FG_CUDA(cudaEventRecord(h->ev[1], h->stream));
+        fg_status st = launch_verify(h, 0);
+        if (st) return st;
+        FG_CUDA(cudaEventRecord(h->ev[2], h->stream));
+        FG_CUDA(cudaMemcpyAsync(hdr.data(), h->B.hdr, sizeof(WalkHeader) * S, cudaMemcpyDeviceToHost, h->stream));
+        FG_CUDA(cudaStreamSynchronize(h->stream));
+        float a = 0, b = 0;
+        cudaEventElapsedTime(&a, h->ev[0], h->ev[1]);
+        cudaEventElapsedTime(&b, h->ev[1], h->ev[2]);
+        acc.kernel_ms += a;
+        acc.verify_ms += b;
+        for (int w = 0; w < S; w++) {
+            acc.flips += hdr[w].flips_done;
+            if (hdr[w].valid) acc.verified_flips += hdr[w].flips_done;
+        }
+    }
+    for (int w = 0; w < S && launches > 0; w++) {
+        acc.walks_valid += hdr[w].valid != 0;
+        acc.walks_failed += hdr[w].status != 0;
+        if (hdr[w].m < acc.min_rank) acc.min_rank = hdr[w].m;
+        if (hdr[w].best_rank < acc.min_best_rank) acc.min_best_rank = hdr[w].best_rank;
+    }
+    if (stats) *stats = acc;
+    if (acc.walks_failed) return fail(FG_ERR_WALK, "some walks reported a nonzero status");
+    return FG_OK;
+}
+
+fg_status fg_minimize(fg_handle *h, int32_t *best_complexity) {
+    if (!h || !best_complexity) return fail(FG_ERR_ARG, "null argument");
+    if (!h->ready) return fail(FG_ERR_STATE, "records not initialised");
+    FG_CUDA(cudaSetDevice(h->dev));
+    const int S = h->B.S;
+    FG_CUDA(cudaMemcpyAsync(h->d_bestC, best_complexity, S * 4, cudaMemcpyHostToDevice, h->stream));
+    FG_CUDA(launch_minimize_z2(h->B, h->P, h->cfg.rng, h->wpb, h->grid, h->d_bestC, h->stream));
+    FG_CUDA(cudaMemcpyAsync(best_complexity, h->d_bestC, S * 4, cudaMemcpyDeviceToHost, h->stream));
+    FG_CUDA(cudaStreamSynchronize(h->stream));
+    return FG_OK;
+}
+
+fg_status fg_validate(fg_handle *h, int best, uint8_t *out) {
+    if (!h || !out) return fail(FG_ERR_ARG, "null argument");
+    FG_CUDA(cudaSetDevice(h->dev));
+    fg_status st = launch_verify(h, best);
+    if (st) return st;
+    FG_CUDA(cudaMemcpyAsync(out, h->d_valid, h->B.S, cudaMemcpyDeviceToHost, h->stream));
+    FG_CUDA(cudaStreamSynchronize(h->stream));
+    return FG_OK;
+}
+
+fg_status fg_xorwow_tape(uint64_t seed, int first_walk, int count, int draws, int device, uint32_t *out_draws,
+                         float *out_uniforms) {
+    if (count <= 0 || draws < 0 || !out_draws || !out_uniforms) return fail(FG_ERR_ARG, "bad tape arguments");
+    FG_CUDA(cudaSetDevice(device));
+    size_t n = (size_t)count * draws;
+    uint32_t *d = nullptr;
+    float *u = nullptr;
+    FG_CUDA(cudaMalloc(&d, n * 4 + 4));
+    if (cudaMalloc(&u, n * 4 + 4) != cudaSuccess) { cudaFree(d); return fail(FG_ERR_CUDA, "tape allocation"); }
+    k_tape<<<(count + 63) / 64, 64>>>((unsigned long long)seed, first_walk, count, draws, d, u);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpy(out_draws, d, n * 4, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(out_uniforms, u, n * 4, cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    cudaFree(u);
+    if (e != cudaSuccess) return fail(FG_ERR_CUDA, cudaGetErrorString(e));
+    return FG_OK;
+}
+
+fg_status fg_philox_blocks(const uint32_t *ctr, int count, uint32_t key0, uint32_t key1, int device, uint32_t *out) {
+    if (count <= 0 || !ctr || !out) return fail(FG_ERR_ARG, "bad philox arguments");
+    FG_CUDA(cudaSetDevice(device));
+    uint4 *dc = nullptr, *dout = nullptr;
+    FG_CUDA(cudaMalloc(&dc, count * 16));
+    if (cudaMalloc(&dout, count * 16) != cudaSuccess) { cudaFree(dc); return fail(FG_ERR_CUDA, "allocation"); }
+    cudaError_t e = cudaMemcpy(dc, ctr, count * 16, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) {
+        k_philox<<<(count + 127) / 128, 128>>>(dc, count, key0, key1, dout);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpy(out, dout, count * 16, cudaMemcpyDeviceToHost);
+    cudaFree(dc);
+    cudaFree(dout);
+    if (e != cudaSuccess) return fail(FG_ERR_CUDA, cudaGetErrorString(e));
+    return FG_OK;
+}
+
+}  // extern "C"

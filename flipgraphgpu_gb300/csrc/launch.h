@@ -1,0 +1,21 @@
+// Internal launch interface between the C-ABI (capi.cu) and the kernel
+// translation units.  Not part of the public ABI.
+#pragma once
+#include <cuda_runtime.h>
+#include "fg_device.cuh"
+
+namespace fg {
+
+enum { RNG_XORWOW = 0, RNG_PHILOX = 1 };
+
+// Smallest supported slots-per-lane S with 32*S >= cap (0 when cap is too large).
+int slots_for_cap(int cap);
+
+cudaError_t launch_walk_z2(const DevBatch &B, const WalkParams &P, int rng, int wpb, int grid, cudaStream_t s);
+cudaError_t launch_minimize_z2(const DevBatch &B, const WalkParams &P, int rng, int wpb, int grid, int32_t *bestC,
+                               cudaStream_t s);
+cudaError_t launch_rebuild_z2(const DevBatch &B, int wpb, int grid, cudaStream_t s);
+// Max resident blocks per SM of the Z2 walk kernel for this configuration.
+int occupancy_walk_z2(int cap, int rng, int wpb);
+
+}  // namespace fg

@@ -1,0 +1,4 @@
+#include "launch_z2_impl.cuh"
+namespace fg {
+FG_INSTANTIATE_Z2(11)
+}

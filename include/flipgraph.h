@@ -1,0 +1,161 @@
+/* flipgraph.h -- C ABI of the GB300 flip-graph search library (libflipgraph.so).
+ *
+ * The reference (dronperminov/FlipGraphGPU) has no library API: its three
+ * executables drive CUDA kernels directly from host classes.  This header is
+ * the boundary those host classes cross in this project; each entry point
+ * names the reference code it replaces.  Plain C types only: pointers and
+ * sizes, no CUDA or C++ types.  Every call returns an fg_status; no call
+ * exits the process (the reference's CUDA_CHECK does, utils.cuh:12-19).
+ *
+ * Ownership: the library owns all device memory of a handle; the caller
+ * owns every host buffer passed in.  One handle must not be used from two
+ * threads at once.
+ */
+#ifndef FLIPGRAPH_H
+#define FLIPGRAPH_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    FG_OK = 0,
+    FG_ERR_ARG = 1,       /* invalid argument (sizes, null pointers, unsupported combination) */
+    FG_ERR_CUDA = 2,      /* a CUDA runtime call failed; fg_last_error() has the message */
+    FG_ERR_CAPACITY = 3,  /* a scheme does not fit the handle's slot / list capacity */
+    FG_ERR_STATE = 4,     /* call order violated (e.g. run before init) */
+    FG_ERR_WALK = 5       /* a walk hit a retry bound or overflow; see the status array */
+} fg_status;
+
+typedef enum { FG_RING_Z2 = 0, FG_RING_ZT = 1 } fg_ring;
+
+/* Draw stream.  FG_RNG_XORWOW is the reference's stream: cuRAND XORWOW with
+ * curand_init(seed, walk_index, 0) per walk (flip_graph.cu:445-451), consumed
+ * at exactly the reference's draw sites, so trajectories match the reference
+ * bit for bit.  FG_RNG_PHILOX is the fast stream: Philox4x32-10 keyed by the
+ * seed, with multiply-high ranges and integer gate thresholds. */
+typedef enum { FG_RNG_XORWOW = 0, FG_RNG_PHILOX = 1 } fg_rng;
+
+/* Walk status bits (per walk). */
+enum { FG_WALK_RETRY = 2, FG_WALK_OVERFLOW = 4 };
+
+/* Mirrors the options of the reference's flip_graph executable
+ * (main_flip_graph.cu:10-25) that reach the walk kernel
+ * (randomWalkKernel, flip_graph.cu:520). */
+typedef struct {
+    int32_t ring;             /* fg_ring */
+    int32_t rng;              /* fg_rng */
+    int32_t walks;            /* --schemes */
+    int32_t cap;              /* factor slots per walk: >= max(initial rank, n1*n2*n3) */
+    uint64_t seed;            /* --seed (nonzero; the CLI maps 0 to time(0) as the reference does) */
+    int32_t iterations;       /* --max-iterations: walk steps per launch */
+    int32_t plus_iterations;  /* --plus-iterations */
+    double expand_p;          /* --expand-probability (per step: expand_p / iterations) */
+    double reduce_p;          /* --reduce-probability (per step: reduce_p / iterations) */
+    int32_t device;           /* CUDA device ordinal */
+    int32_t walks_per_block;  /* 0 = library default */
+} fg_config;
+
+/* Host-side walk records, structure of arrays over `walks` records with
+ * `cap` factor slots each.  Factor arrays are [walks][3][cap]: for Z2 a
+ * factor is a bitmask over the n_i*n_{i+1} matrix entries (bit r = entry r,
+ * W stored transposed as in scheme_z2.cu:47-49); for ZT it is the
+ * reference's Addition (values, signs, valid) split over fac / sgn / valid.
+ * Lists are the three FlipSets of equal-factor pairs (flip_set.cu), sizes
+ * [walks][3] and pairs [walks][3][500] packed (a << 16) | b, in the
+ * reference's order.  Unused slots and list entries read as zero. */
+typedef struct {
+    int32_t *n;           /* [walks][3] */
+    int32_t *m;           /* [walks] current rank */
+    uint64_t *fac;        /* [walks][3][cap] */
+    uint64_t *sgn;        /* ZT only, else NULL */
+    uint8_t *valid;       /* ZT only, else NULL */
+    int32_t *list_size;   /* [walks][3] */
+    uint32_t *list_pairs; /* [walks][3][500] */
+    int32_t *flips;       /* [walks] flips since the last rank drop */
+    int32_t *best_rank;   /* [walks] */
+    int32_t *best_m;      /* [walks] */
+    uint64_t *best_fac;   /* [walks][3][cap] */
+    uint64_t *best_sgn;   /* ZT only */
+    uint8_t *best_valid;  /* ZT only */
+    int64_t *rng_pos;     /* [walks] draws consumed since seeding */
+    int32_t *status;      /* [walks] FG_WALK_* bits */
+} fg_records;
+
+typedef struct {
+    uint64_t flips;            /* accepted flips in the call, all walks */
+    uint64_t verified_flips;   /* flips of walks whose scheme passed the exact Brent check */
+    int32_t walks_valid;       /* walks whose current scheme verified */
+    int32_t walks_failed;      /* walks with a nonzero status */
+    int32_t min_rank;          /* lowest current rank */
+    int32_t min_best_rank;     /* lowest best rank */
+    float kernel_ms;           /* device time of the walk kernel(s), CUDA events */
+    float verify_ms;           /* device time of the verification kernel */
+} fg_stats;
+
+#define FG_LIST_CAP 500   /* FlipSet capacity, config.cuh:14 */
+#define FG_MAX_RANK 350   /* config.cuh:10 */
+
+typedef struct fg_handle fg_handle;
+
+/* Allocates device state for cfg->walks walks and seeds their streams
+ * (replaces FlipGraph's constructor: cudaMallocManaged x5 and
+ * initializeRandomStatesKernel, flip_graph.cu:4-188,445-451). */
+fg_status fg_create(const fg_config *cfg, fg_handle **out);
+fg_status fg_destroy(fg_handle *h);
+
+/* Every walk := naive n1 x n2 x n3 scheme, best := current, best_rank :=
+ * n1*n2*n3, flips := 0 (initializeNaiveKernel + initializeSchemesKernel,
+ * flip_graph.cu:453-457,510-518). */
+fg_status fg_init_naive(fg_handle *h, int n1, int n2, int n3);
+
+/* Copies host records into the handle (FlipGraph::initializeFromFile +
+ * initializeCopyKernel, flip_graph.cu:201-224,459-470, after the host has
+ * parsed and replicated the schemes).  rng_pos is not read: streams keep
+ * their position. */
+fg_status fg_set_records(fg_handle *h, const fg_records *rec);
+
+/* Copies the handle's records to host buffers (the reference reads managed
+ * memory in place, flip_graph.cu:253-265,303-380). */
+fg_status fg_get_records(fg_handle *h, fg_records *rec);
+
+/* Runs `launches` launches of the walk (randomWalkKernel, flip_graph.cu:520-573,
+ * with resize, sandwiching and basis probabilities 0) on every walk, then
+ * verifies every walk's scheme exactly (flip_graph.cu:571-572).  Stats
+ * cover this call. */
+fg_status fg_run(fg_handle *h, int launches, fg_stats *stats);
+
+/* One launch of the complexity minimizer's flip walk (minimizeKernel,
+ * complexity_minimizer.cu:190-214): checkReduce=false flips; best_* records
+ * receive the lowest-complexity scheme seen.  best_complexity [walks] is
+ * read (the running bests) and written. */
+fg_status fg_minimize(fg_handle *h, int32_t *best_complexity);
+
+/* Exact Brent-equation check of every walk's current (best=0) or best
+ * (best=1) scheme; out [walks] = 1 when valid (Scheme::validate,
+ * scheme_z2.cu:20-29, scheme_integer.cu:20-38). */
+fg_status fg_validate(fg_handle *h, int best, uint8_t *out);
+
+/* Records `draws` cuRAND XORWOW outputs of walks [first_walk, first_walk+count)
+ * from curand_init(seed, walk, 0): out_draws[w][q] = q-th curand() value,
+ * out_uniforms[w][q] = q-th curand_uniform() value.  Test support: lets a
+ * CPU checker replay the reference's stream. */
+fg_status fg_xorwow_tape(uint64_t seed, int first_walk, int count, int draws, int device,
+                         uint32_t *out_draws, float *out_uniforms);
+
+/* Philox4x32-10 blocks computed on the device (test support):
+ * out[q] = Philox(ctr[q], key) for q < count, ctr [count][4], out [count][4]. */
+fg_status fg_philox_blocks(const uint32_t *ctr, int count, uint32_t key0, uint32_t key1, int device,
+                           uint32_t *out);
+
+/* Message of the last failing call on this thread ("" when none). */
+const char *fg_last_error(void);
+
+/* Library version string. */
+const char *fg_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

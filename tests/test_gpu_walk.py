@@ -1,0 +1,141 @@
+"""GPU walk parity through the C ABI.
+
+* Reference stream (XORWOW): the library's kernels against the reference's
+  own recorded kernel states (tests/golden), byte for byte; and against the
+  CPU oracle replaying the same cuRAND stream on larger batches.
+* Fast stream (Philox): the library's kernels against the oracle's fast mode.
+"""
+import numpy as np
+import pytest
+
+import golden_io
+from helpers import diff_walk, walk_fixtures
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+fg = pytest.importorskip("flipgraphgpu_gb300")
+
+
+def z2_fixtures():
+    return [p for p in walk_fixtures() if "/walk_z2_" in p]
+
+
+def compare_records(rec, b, ctx=""):
+    """Library records vs oracle batch: every field, exactly."""
+    for f in ("n", "m", "fac", "list_size", "list_pairs", "flips", "best_rank", "best_m", "best_fac",
+              "rng_pos", "status"):
+        a, o = getattr(rec, f), getattr(b, f)
+        if not np.array_equal(a, o):
+            bad = np.argwhere(a != o)
+            raise AssertionError(f"{ctx}: field {f} differs at {bad[:5].tolist()} (of {len(bad)})")
+
+
+def test_xorwow_tape_is_the_reference_stream():
+    d = golden_io.read_walk([p for p in walk_fixtures() if "z2_333" in p][0])
+    n = min(len(t["draws"]) for t in d["tapes"])
+    draws, unis = fg.xorwow_tape(d["seed"], 0, d["walks"], n)
+    for w, t in enumerate(d["tapes"]):
+        assert np.array_equal(draws[w], t["draws"][:n])
+        assert np.array_equal(unis[w].view(np.uint32), t["uniforms"][:n].view(np.uint32))
+
+
+def test_philox_device_matches_oracle():
+    rng = np.random.default_rng(5)
+    ctr = rng.integers(0, 2**32, size=(257, 4), dtype=np.uint64).astype(np.uint32)
+    key = (0xDEADBEEF, 0x12345678)
+    out = fg.philox_blocks(ctr, key)
+    for q in range(len(ctr)):
+        assert list(out[q]) == O.philox([int(x) for x in ctr[q]], list(key))
+
+
+@pytest.mark.parametrize("path", z2_fixtures(), ids=lambda p: p.split("/")[-1].split(".")[0])
+def test_walk_matches_reference_kernel(path):
+    """Same seed, same flags: the library reproduces the reference's per-launch state."""
+    d = golden_io.read_walk(path)
+    n1, n2, n3 = d["n"]
+    with fg.Engine(d["walks"], n1 * n2 * n3, "z2", "xorwow", d["seed"], d["iterations"], d["plus_iterations"],
+                   d["expand_p"], d["reduce_p"]) as eng:
+        eng.init_naive(n1, n2, n3)
+        for L, block in enumerate(d["launches"]):
+            eng.run(1)
+            rec = eng.records()
+            for w in range(d["walks"]):
+                errs = diff_walk(rec, w, block[w], "z2")
+                assert not errs, f"launch {L} walk {w}: {errs}"
+        assert [int(x) for x in rec.rng_pos] == [t["used"] for t in d["tapes"]]
+
+
+def run_oracle_like(rec0, cfg_kw, launches, rng, tape=None):
+    b = O.WalkBatch(rec0.walks, rec0.cap, "z2")
+    for f in ("n", "m", "fac", "list_size", "list_pairs", "flips", "best_rank", "best_m", "best_fac"):
+        getattr(b, f)[...] = getattr(rec0, f)
+    cfg = b.cfg(rng, launches=launches, **cfg_kw)
+    O.walk(b, cfg, tape)
+    return b
+
+
+@pytest.mark.parametrize("shape,S,iters,plus,expand_p,reduce_p,launches", [
+    ((3, 3, 3), 96, 3000, 400, 0.01, 0.0, 2),
+    ((2, 2, 3), 64, 2000, 100, 5.0, 0.0, 1),
+    ((2, 3, 4), 64, 2000, 300, 0.01, 10.0, 1),
+    ((4, 4, 4), 32, 1500, 600, 0.01, 0.0, 1),
+    ((3, 4, 5), 32, 1200, 500, 3.0, 0.0, 1),
+    ((2, 5, 5), 16, 800, 200, 0.01, 0.0, 1),   # nn = 25 x 25 x 10, cap 50 -> two slots per lane
+    ((4, 5, 8), 8, 400, 200, 0.01, 0.0, 1),    # nn = 20 x 40 x 32, cap 160, > 32-bit factors
+])
+def test_walk_reference_stream_vs_oracle(shape, S, iters, plus, expand_p, reduce_p, launches):
+    n1, n2, n3 = shape
+    cap = n1 * n2 * n3
+    seed = 1000 + n1 * 100 + n2 * 10 + n3
+    kw = dict(iterations=iters, plus_iterations=plus, expand_p=expand_p, reduce_p=reduce_p)
+    with fg.Engine(S, cap, "z2", "xorwow", seed, iters, plus, expand_p, reduce_p) as eng:
+        eng.init_naive(n1, n2, n3)
+        rec0 = eng.records()
+        eng.run(launches)
+        rec = eng.records()
+        assert eng.validate().all() and eng.validate(best=True).all()
+    used = int(rec.rng_pos.max())
+    draws, unis = fg.xorwow_tape(seed, 0, S, used)
+    tape = O.make_tape([(draws[w, :rec.rng_pos[w]], unis[w, :rec.rng_pos[w]]) for w in range(S)])
+    b = run_oracle_like(rec0, kw, launches, "tape", tape)
+    compare_records(rec, b, f"{shape}")
+
+
+@pytest.mark.parametrize("shape,S,iters,plus,expand_p,reduce_p", [
+    ((3, 3, 3), 128, 4000, 300, 0.01, 0.0),
+    ((2, 2, 2), 64, 2000, 50, 2.0, 0.0),
+    ((2, 3, 4), 64, 2000, 300, 0.01, 20.0),
+    ((4, 4, 4), 32, 2000, 800, 0.01, 0.0),
+    ((3, 4, 5), 32, 1500, 600, 4.0, 0.0),
+    ((4, 5, 8), 8, 500, 200, 0.01, 0.0),
+])
+def test_walk_fast_stream_vs_oracle(shape, S, iters, plus, expand_p, reduce_p):
+    n1, n2, n3 = shape
+    cap = n1 * n2 * n3
+    seed = 77 + n1 + n2 + n3
+    kw = dict(iterations=iters, plus_iterations=plus, expand_p=expand_p, reduce_p=reduce_p, seed=seed)
+    with fg.Engine(S, cap, "z2", "philox", seed, iters, plus, expand_p, reduce_p) as eng:
+        eng.init_naive(n1, n2, n3)
+        rec0 = eng.records()
+        eng.run(2)
+        rec = eng.records()
+        assert eng.validate().all() and eng.validate(best=True).all()
+    b = run_oracle_like(rec0, kw, 2, "philox")
+    compare_records(rec, b, f"{shape}")
+
+
+def test_validate_matches_oracle_on_corrupted_schemes():
+    with fg.Engine(64, 27, "z2", "philox", 3, 500, 100) as eng:
+        eng.init_naive(3, 3, 3)
+        eng.run(1)
+        rec = eng.records()
+        rng = np.random.default_rng(0)
+        for w in range(0, 64, 2):
+            c, t = rng.integers(0, 3), rng.integers(0, rec.m[w])
+            rec.fac[w, c, t] ^= np.uint64(1 << int(rng.integers(0, 9)))
+        eng.set_records(rec)
+        got = eng.validate()
+    want = O.validate_arrays("z2", rec.n, rec.m, rec.fac)
+    assert np.array_equal(got, want)
+    assert not got[::2].any() and got[1::2].all()
