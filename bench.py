@@ -1,0 +1,352 @@
+#!/usr/bin/env python3
+"""Benchmark: verified flips/s of the batched uneven Z2 flip-graph search on one GB300.
+
+Workload (the batched uneven search): 65,536 concurrent walks split evenly
+over the shapes (2,2,2), (2,2,3), (2,3,4), (3,3,4), (3,4,5), (4,4,4), each
+starting from its naive rank n1*n2*n3 scheme, uniform flip-pair proposal
+(fast Philox stream), plus transition after 10^5 flips without a rank drop,
+expand probability 0.01 (the reference's default).  One step = one launch of
+the walk kernel over every walk (`--iterations` steps each, default 10,000 =
+the reference's --max-iterations) followed by the exact Brent check of every
+walk; only flips of walks whose scheme verifies are counted.
+
+Timing: W warm-up steps, then K timed steps bracketed by a device sync (and a
+barrier under torchrun); device time comes from CUDA events recorded by the
+library on its launching stream.  The walk records (~600 MB) exceed the
+129 MB L2, so no L2 flush is needed between steps.
+
+`e2e` repeats the step through the C ABI with page-locked host records: each
+step uploads the records (fg_set_records), runs, and downloads them
+(fg_get_records); the copies are inside the timed region.
+
+`--impl reference` times the reference's algorithm on the host CPU cores (the
+CPU restatement in oracle/, all cores): the reference has no host walker of
+its own (its walk operators are __device__-only, scheme_z2.cuh:40-54).
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+SHAPES = [(2, 2, 2), (2, 2, 3), (2, 3, 4), (3, 3, 4), (3, 4, 5), (4, 4, 4)]
+WORD_BYTES = 8  # factor word of the Z2 kernels (uint64 bitmasks)
+METRIC = "verified flips/s"
+CONFIG_NAME = "batched uneven Z2 search: 65,536 walks over (2,2,2),(2,2,3),(2,3,4),(3,3,4),(3,4,5),(4,4,4)"
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    return ws, rank
+
+
+def shape_ranges(walks):
+    """Contiguous, even split of the walks over SHAPES: [(shape, first, count)]."""
+    out, first = [], 0
+    for i, s in enumerate(SHAPES):
+        last = (i + 1) * walks // len(SHAPES)
+        out.append((s, first, last - first))
+        first = last
+    return out
+
+
+def shapes_for(walks):
+    sh = np.zeros((walks, 3), np.int32)
+    for s, first, count in shape_ranges(walks):
+        sh[first:first + count] = s
+    return sh
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device=0):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            p = [x.strip() for x in ln.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                mx.append(float(p[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, p[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def smem_peak_gbs():
+    """Shared-memory bandwidth of the GPU: 32 banks x 4 B per clock per SM."""
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peaks = json.load(f)
+    except OSError:
+        pass
+    mhz = peaks.get("sm_max_mhz", 2070.0)
+    sms = 152
+    try:
+        import ctypes
+        cudart = ctypes.CDLL("libcudart.so")
+        v = ctypes.c_int()
+        if cudart.cudaDeviceGetAttribute(ctypes.byref(v), 16, 0) == 0:  # cudaDevAttrMultiProcessorCount
+            sms = v.value
+    except OSError:
+        pass
+    return 128.0 * sms * mhz * 1e6 / 1e9, peaks, sms, mhz
+
+
+# ------------------------------------------------------------------ CPU side
+def cpu_walks(walks_per_shape, iterations, plus, seed, threads):
+    """Oracle (CPU restatement) walks over every shape; returns (verified flips, seconds, walks)."""
+    from oracle import oracle as O
+    jobs = []
+    for si, (n1, n2, n3) in enumerate(SHAPES):
+        for part in range(threads):
+            k = walks_per_shape // threads + (1 if part < walks_per_shape % threads else 0)
+            if k:
+                jobs.append((n1, n2, n3, k, seed * 1000 + si * 64 + part))
+    results = []
+
+    def work(job):
+        n1, n2, n3, k, sd = job
+        b = O.WalkBatch(k, 64, "z2")
+        O.init_naive(b, n1, n2, n3)
+        cfg = b.cfg("fast", iterations=iterations, plus_iterations=plus, launches=1, expand_p=0.01, seed=sd)
+        O.walk(b, cfg)
+        ok = O.validate(b)
+        results.append((int(b.accepted[ok].sum()), int(b.accepted.sum())))
+
+    import concurrent.futures as cf
+    t0 = time.perf_counter()
+    with cf.ThreadPoolExecutor(threads) as ex:
+        list(ex.map(work, jobs))
+    dt = time.perf_counter() - t0
+    return sum(r[0] for r in results), dt, sum(j[3] for j in jobs)
+
+
+def cpu_baseline(args, seconds_target=15.0):
+    threads = os.cpu_count() or 1
+    wps = max(threads, 16)
+    iters = 200
+    v, dt, nw = cpu_walks(wps, iters, 100000, 7, threads)
+    # Scale the sample to roughly seconds_target of CPU work.
+    scale = max(1.0, seconds_target / max(dt, 1e-3))
+    iters2 = int(iters * scale)
+    v, dt, nw = cpu_walks(wps, iters2, 100000, 8, threads)
+    return {"value": v / dt, "unit": METRIC, "cores": threads, "kind": "port",
+            "sample": f"{nw} walks ({wps} per shape) x {iters2} steps of the oracle's fast-stream walk, "
+                      f"{threads} host threads, {dt:.1f} s"}
+
+
+def reference_arm(args):
+    ws, rank = dist_env()
+    if rank != 0:
+        return 0
+    threads = os.cpu_count() or 1
+    wps = max(threads, 16)
+    iters = args.ref_iterations
+    for _ in range(args.warmup):
+        cpu_walks(wps, max(10, iters // 10), 100000, 3, threads)
+    tot_v, tot_t = 0, 0.0
+    nw = 0
+    for k in range(args.steps):
+        v, dt, nw = cpu_walks(wps, iters, 100000, 100 + k, threads)
+        tot_v += v
+        tot_t += dt
+    value = tot_v / tot_t
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * tot_t / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
+            "data": "synthetic (naive starting schemes)",
+            "config": {"workload": CONFIG_NAME, "walks_sampled": nw, "iterations_per_step": iters,
+                       "plus_iterations": 100000, "expand_p": 0.01, "mode": "fast"},
+            "cpu_baseline": {"value": value, "unit": METRIC, "cores": threads, "kind": "port",
+                             "sample": f"{nw} walks x {iters} steps per step on {threads} threads"},
+            "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+# ------------------------------------------------------------------ GPU side
+def gpu_arm(args):
+    ws, rank = dist_env()
+    dist = None
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    device = int(os.environ.get("LOCAL_RANK", "0"))
+    import flipgraphgpu_gb300 as fg
+    walks, cap, iters = args.walks, 64, args.iterations
+    seed = args.seed + rank
+    eng = fg.Engine(walks, cap, "z2", args.mode, seed, iters, args.plus_iterations, 0.01, 0.0, device,
+                    args.walks_per_block)
+    shapes = shapes_for(walks)
+    eng.init_naive_shapes(shapes)
+    for _ in range(args.warmup):
+        eng.run(1)
+
+    def barrier():
+        if dist:
+            dist.barrier()
+
+    clocks = ClockSampler(device)
+    # ---- device-resident timed region
+    barrier()
+    clocks.start()
+    wall0 = time.perf_counter()
+    kern_ms = ver_ms = 0.0
+    flips = vflips = 0
+    algo_bytes = 0.0
+    per_shape = {s: [0, 0] for s in SHAPES}
+    m_prev = eng.counters()["m"]
+    for _ in range(args.steps):
+        st = eng.run(1)
+        kern_ms += st["kernel_ms"]
+        ver_ms += st["verify_ms"]
+        flips += st["flips"]
+        vflips += st["verified_flips"]
+        c = eng.counters()
+        mavg = 0.5 * (c["m"] + m_prev)
+        m_prev = c["m"]
+        f = c["flips"].astype(np.float64)
+        algo_bytes += float(np.sum(f * (2 * mavg + 4) * WORD_BYTES))
+        for s, first, count in shape_ranges(walks):
+            sel = slice(first, first + count)
+            per_shape[s][0] += int(c["flips"][sel][c["valid"][sel]].sum())
+    wall = time.perf_counter() - wall0
+    barrier()
+    clk = clocks.stop()
+    dev_s = (kern_ms + ver_ms) / 1000.0
+    if dist:
+        import torch
+        t = torch.tensor([dev_s], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        dev_s = float(t[0])
+        v = torch.tensor([float(vflips)], dtype=torch.float64)
+        dist.all_reduce(v)
+        vflips_all = float(v[0])
+    else:
+        vflips_all = float(vflips)
+    value = vflips_all / dev_s
+    best = eng.counters()
+    best_rank = {f"{a}x{b}x{c}": int(best["best_rank"][f:f + n].min()) for (a, b, c), f, n in shape_ranges(walks)}
+    shape_rate = {f"{a}x{b}x{c}": per_shape[(a, b, c)][0] / dev_s for (a, b, c) in SHAPES}
+
+    # ---- end to end through the C ABI with page-locked host records
+    rec = fg.Records(walks, cap, "z2", pinned=True)
+    eng.records(into=rec)
+    h2d = d2h = rec.nbytes()
+    barrier()
+    e0 = time.perf_counter()
+    ev = 0
+    for _ in range(args.e2e_steps):
+        eng.set_records(rec)
+        st = eng.run(1)
+        eng.records(into=rec)
+        ev += st["verified_flips"]
+    e_wall = time.perf_counter() - e0
+    barrier()
+    e2e_value = ev * ws / e_wall
+
+    smem_peak, peaks, sms, mhz = smem_peak_gbs()
+    achieved = algo_bytes / (kern_ms / 1000.0) / 1e9
+    if rank == 0:
+        cpu = cpu_baseline(args) if (ws == 1 and not args.no_cpu) else None
+        line = {
+            "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1000 * dev_s / args.steps, "wall_ms_per_step": 1000 * wall / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
+            "data": "synthetic (naive starting schemes)",
+            "config": {"workload": CONFIG_NAME, "walks": walks, "iterations_per_step": iters,
+                       "plus_iterations": args.plus_iterations, "expand_p": 0.01, "mode": args.mode,
+                       "walks_per_block": args.walks_per_block, "l2": "records larger than L2 (no flush)",
+                       "parallelism": f"replicas x{ws}"},
+            "flips_per_s_by_shape": shape_rate, "best_rank_by_shape": best_rank,
+            "flips": flips, "verified_flips": vflips,
+            "kernel_ms_per_step": kern_ms / args.steps, "verify_ms_per_step": ver_ms / args.steps,
+            "gpu_launches": args.steps * (1 + (len(SHAPES) if args.mode == "fast" else 1)),
+            "roofline": {"bound": "smem", "achieved": achieved, "peak": smem_peak, "unit": "GB/s",
+                         "frac": achieved / smem_peak, "traffic": None,
+                         "peak_source": f"derived: 128 B/clk/SM x {sms} SMs x {mhz:.0f} MHz (sm_max_mhz, MEASURED_PEAKS.json)",
+                         "algorithmic_bytes": "per accepted flip (2m+4) x 8 B of shared-memory traffic"},
+            "clocks": clk,
+            "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                    "steps": args.e2e_steps},
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line))
+    eng.close()
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--walks", type=int, default=65536)
+    ap.add_argument("--iterations", type=int, default=10000)
+    ap.add_argument("--plus-iterations", type=int, default=100000)
+    ap.add_argument("--mode", default="fast", choices=["fast", "philox", "reference"])
+    ap.add_argument("--seed", type=int, default=1)
+    ap.add_argument("--walks-per-block", type=int, default=0)
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--ref-iterations", type=int, default=20000)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return reference_arm(args)
+    return gpu_arm(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -22,7 +22,7 @@ LIB_PATH = os.path.join(PKG, "_lib", platform.machine(), "libflipgraph.so")
 LIST_CAP = 500
 MAX_RANK = 350
 RINGS = {"z2": 0, "zt": 1}
-RNGS = {"xorwow": 0, "philox": 1}
+MODES = {"reference": 0, "philox": 1, "fast": 2, "xorwow": 0}
 STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "capacity", 4: "state", 5: "walk failure"}
 
 
@@ -33,7 +33,7 @@ class FlipGraphError(RuntimeError):
 
 
 class Config(ctypes.Structure):
-    _fields_ = [("ring", ctypes.c_int32), ("rng", ctypes.c_int32), ("walks", ctypes.c_int32),
+    _fields_ = [("ring", ctypes.c_int32), ("mode", ctypes.c_int32), ("walks", ctypes.c_int32),
                 ("cap", ctypes.c_int32), ("seed", ctypes.c_uint64), ("iterations", ctypes.c_int32),
                 ("plus_iterations", ctypes.c_int32), ("expand_p", ctypes.c_double), ("reduce_p", ctypes.c_double),
                 ("device", ctypes.c_int32), ("walks_per_block", ctypes.c_int32)]
@@ -69,7 +69,8 @@ def library():
     lib.fg_last_error.restype = ctypes.c_char_p
     lib.fg_version.restype = ctypes.c_char_p
     for name in ("fg_create", "fg_destroy", "fg_init_naive", "fg_set_records", "fg_get_records", "fg_run",
-                 "fg_minimize", "fg_validate", "fg_xorwow_tape", "fg_philox_blocks"):
+                 "fg_minimize", "fg_validate", "fg_xorwow_tape", "fg_philox_blocks", "fg_init_naive_shapes",
+                 "fg_get_counters", "fg_host_alloc", "fg_host_free"):
         getattr(lib, name).restype = ctypes.c_int
     _lib = lib
     return lib
@@ -84,14 +85,38 @@ def _ptr(a):
     return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
 
 
+class PinnedBuffer:
+    """Page-locked host memory (fg_host_alloc) viewed as a numpy array."""
+
+    def __init__(self, shape, dtype):
+        self.nbytes = int(np.prod(shape)) * np.dtype(dtype).itemsize
+        self.p = ctypes.c_void_p()
+        _check(library().fg_host_alloc(ctypes.c_uint64(self.nbytes), ctypes.byref(self.p)))
+        buf = (ctypes.c_uint8 * self.nbytes).from_address(self.p.value)
+        self.array = np.frombuffer(buf, dtype=dtype).reshape(shape)
+
+    def __del__(self):
+        try:
+            if self.p:
+                library().fg_host_free(self.p)
+        except Exception:
+            pass
+
+
 class Records:
-    """Host walk records (the C ABI's fg_records), numpy arrays."""
+    """Host walk records (the C ABI's fg_records), numpy arrays.
+
+    With pinned=True every array lives in page-locked memory (fast DMA)."""
 
     FIELDS = _Records._fields_
 
-    def __init__(self, walks, cap, ring="z2"):
+    def __init__(self, walks, cap, ring="z2", pinned=False):
         zt = ring == "zt"
         self.walks, self.cap, self.ring = walks, cap, ring
+        self._pins = []
+        if pinned:
+            self._alloc_pinned(walks, cap, zt)
+            return
         self.n = np.zeros((walks, 3), np.int32)
         self.m = np.zeros(walks, np.int32)
         self.fac = np.zeros((walks, 3, cap), np.uint64)
@@ -108,6 +133,31 @@ class Records:
         self.rng_pos = np.zeros(walks, np.int64)
         self.status = np.zeros(walks, np.int32)
 
+    def _alloc_pinned(self, walks, cap, zt):
+        def pin(shape, dtype):
+            b = PinnedBuffer(shape, dtype)
+            self._pins.append(b)
+            b.array[...] = 0
+            return b.array
+        self.n = pin((walks, 3), np.int32)
+        self.m = pin((walks,), np.int32)
+        self.fac = pin((walks, 3, cap), np.uint64)
+        self.sgn = pin((walks, 3, cap), np.uint64) if zt else None
+        self.valid = pin((walks, 3, cap), np.uint8) if zt else None
+        self.list_size = pin((walks, 3), np.int32)
+        self.list_pairs = pin((walks, 3, LIST_CAP), np.uint32)
+        self.flips = pin((walks,), np.int32)
+        self.best_rank = pin((walks,), np.int32)
+        self.best_m = pin((walks,), np.int32)
+        self.best_fac = pin((walks, 3, cap), np.uint64)
+        self.best_sgn = pin((walks, 3, cap), np.uint64) if zt else None
+        self.best_valid = pin((walks, 3, cap), np.uint8) if zt else None
+        self.rng_pos = pin((walks,), np.int64)
+        self.status = pin((walks,), np.int32)
+
+    def nbytes(self):
+        return sum(getattr(self, f).nbytes for f, _ in self.FIELDS if getattr(self, f) is not None)
+
     def _c(self):
         return _Records(*[_ptr(getattr(self, f)) for f, _ in self.FIELDS])
 
@@ -115,10 +165,12 @@ class Records:
 class Engine:
     """One fg_handle: `walks` independent walks on one GPU."""
 
-    def __init__(self, walks, cap, ring="z2", rng="xorwow", seed=1, iterations=10000, plus_iterations=8000,
+    def __init__(self, walks, cap, ring="z2", mode="reference", seed=1, iterations=10000, plus_iterations=8000,
                  expand_p=0.01, reduce_p=0.0, device=0, walks_per_block=0):
+        """mode: "reference" (XORWOW, reference lists, bit-exact), "philox" (Philox, lists) or
+        "fast" (Philox, implicit pair enumeration, thread-per-walk kernel)."""
         self.lib = library()
-        self.cfg = Config(RINGS[ring], RNGS[rng], walks, cap, seed, iterations, plus_iterations, expand_p,
+        self.cfg = Config(RINGS[ring], MODES[mode], walks, cap, seed, iterations, plus_iterations, expand_p,
                           reduce_p, device, walks_per_block)
         self.walks, self.cap, self.ring = walks, cap, ring
         self.h = ctypes.c_void_p()
@@ -144,12 +196,25 @@ class Engine:
     def init_naive(self, n1, n2, n3):
         _check(self.lib.fg_init_naive(self.h, n1, n2, n3))
 
+    def init_naive_shapes(self, shapes):
+        """Walk w starts from the naive shapes[w] scheme (many shapes in one batch)."""
+        sh = np.ascontiguousarray(shapes, np.int32).reshape(self.walks, 3)
+        _check(self.lib.fg_init_naive_shapes(self.h, _ptr(sh)))
+
+    def counters(self):
+        m = np.zeros(self.walks, np.int32)
+        best = np.zeros(self.walks, np.int32)
+        flips = np.zeros(self.walks, np.uint64)
+        valid = np.zeros(self.walks, np.uint8)
+        _check(self.lib.fg_get_counters(self.h, _ptr(m), _ptr(best), _ptr(flips), _ptr(valid)))
+        return {"m": m, "best_rank": best, "flips": flips, "valid": valid.astype(bool)}
+
     def set_records(self, rec):
         c = rec._c()
         _check(self.lib.fg_set_records(self.h, ctypes.byref(c)))
 
-    def records(self):
-        rec = Records(self.walks, self.cap, self.ring)
+    def records(self, into=None):
+        rec = into if into is not None else Records(self.walks, self.cap, self.ring)
         c = rec._c()
         _check(self.lib.fg_get_records(self.h, ctypes.byref(c)))
         return rec

@@ -35,9 +35,10 @@ __global__ void k_init_xorwow(curandStateXORWOW_t *st, int S, unsigned long long
 
 // initializeNaive (scheme_z2.cu:32-55 / scheme_integer.cu:41-64) + initializeSchemesKernel
 // (flip_graph.cu:510-518); lists are built afterwards by the rebuild kernel.
-__global__ void k_init_naive(DevBatch B, int n1, int n2, int n3, int zt) {
+__global__ void k_init_naive(DevBatch B, int n1_, int n2_, int n3_, const int32_t *shapes, int zt) {
     int w = blockIdx.x * blockDim.x + threadIdx.x;
     if (w >= B.S) return;
+    const int n1 = shapes ? shapes[w * 3] : n1_, n2 = shapes ? shapes[w * 3 + 1] : n2_, n3 = shapes ? shapes[w * 3 + 2] : n3_;
     const int cap = B.cap;
     uint64_t *f = B.fac + (size_t)w * 3 * cap, *bf = B.best_fac + (size_t)w * 3 * cap;
     for (int q = 0; q < 3 * cap; q++) { f[q] = 0; bf[q] = 0; }
@@ -128,11 +129,21 @@ __global__ void k_philox(const uint4 *ctr, int count, uint32_t k0, uint32_t k1, 
 }  // namespace
 
 // ---------------------------------------------------------------- handle
+// A run of consecutive walks sharing one shared-memory layout in fast mode.
+struct Segment {
+    int first, count, scap, wide, nnmax;
+};
+
+constexpr int kSideStreams = 8;
+
 struct fg_handle {
     fg_config cfg;
     int dev = 0, sms = 0, wpb = 4, grid = 1;
     cudaStream_t stream = nullptr;
+    cudaStream_t side[kSideStreams] = {};
+    cudaEvent_t fork = nullptr, join[kSideStreams] = {};
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    std::vector<Segment> segs;
     DevBatch B{};
     WalkParams P{};
     int32_t *d_bestC = nullptr;
@@ -182,6 +193,73 @@ fg_status launch_verify(fg_handle *h, int best) {
     return FG_OK;
 }
 
+// Fast-mode segments: maximal runs of walks with the same slot count and word
+// width.  Slots = max(rank, n1*n2*n3) rounded up to 4 (ranks never exceed it:
+// plus and split stop at n1*n2*n3, scheme_z2.cu:1030,1053,1081).  Too many
+// segments (shapes interleaved walk by walk) collapse into one segment sized
+// for the largest walk.
+void plan_segments(fg_handle *h, const std::vector<WalkHeader> &hdr) {
+    const int S = h->B.S, cap = h->B.cap;
+    std::vector<Segment> segs;
+    int maxScap = 4, anyWide = 0, maxNN = 0;
+    for (int w = 0; w < S; w++) {
+        const WalkHeader &o = hdr[w];
+        int full = o.n[0] * o.n[1] * o.n[2];
+        int need = o.m > full ? o.m : full;
+        int scap = (need + 3) / 4 * 4;
+        if (scap > cap) scap = cap;
+        int nnmax = o.n[0] * o.n[1];
+        if (o.n[1] * o.n[2] > nnmax) nnmax = o.n[1] * o.n[2];
+        if (o.n[2] * o.n[0] > nnmax) nnmax = o.n[2] * o.n[0];
+        int wide = nnmax > 24;
+        if (scap > maxScap) maxScap = scap;
+        anyWide |= wide;
+        if (!segs.empty() && segs.back().scap == scap && segs.back().wide == wide && segs.back().first + segs.back().count == w) {
+            segs.back().count++;
+            if (nnmax > segs.back().nnmax) segs.back().nnmax = nnmax;
+        } else {
+            segs.push_back({w, 1, scap, wide, nnmax});
+        }
+        if (nnmax > maxNN) maxNN = nnmax;
+    }
+    if ((int)segs.size() > kSideStreams) segs.assign(1, Segment{0, S, maxScap, anyWide, maxNN});
+    h->segs = segs;
+}
+
+fg_status refresh_plan(fg_handle *h) {
+    std::vector<WalkHeader> hdr(h->B.S);
+    FG_CUDA(cudaMemcpy(hdr.data(), h->B.hdr, sizeof(WalkHeader) * h->B.S, cudaMemcpyDeviceToHost));
+    plan_segments(h, hdr);
+    return FG_OK;
+}
+
+// Launches one walk pass over every walk on h->stream (fast mode: one kernel
+// per segment on side streams, forked from and joined back into h->stream).
+fg_status launch_walks(fg_handle *h) {
+    if (h->cfg.mode != FG_MODE_FAST) {
+        FG_CUDA(launch_walk_z2(h->B, h->P, h->cfg.mode == FG_MODE_REFERENCE ? RNG_XORWOW : RNG_PHILOX, h->wpb,
+                               h->grid, h->stream));
+        return FG_OK;
+    }
+    const int wpb = h->cfg.walks_per_block > 0 ? h->cfg.walks_per_block : 2;
+    for (const Segment &g : h->segs)
+        if (g.nnmax > 56) return fail(FG_ERR_CAPACITY, "fast mode holds factors of at most 56 entries");
+    if (h->segs.size() == 1) {
+        const Segment &g = h->segs[0];
+        FG_CUDA(launch_walk_simt(h->B, h->P, g.first, g.count, g.scap, g.wide, wpb, h->sms, h->stream));
+        return FG_OK;
+    }
+    FG_CUDA(cudaEventRecord(h->fork, h->stream));
+    for (size_t i = 0; i < h->segs.size(); i++) {
+        const Segment &g = h->segs[i];
+        FG_CUDA(cudaStreamWaitEvent(h->side[i], h->fork, 0));
+        FG_CUDA(launch_walk_simt(h->B, h->P, g.first, g.count, g.scap, g.wide, wpb, h->sms, h->side[i]));
+        FG_CUDA(cudaEventRecord(h->join[i], h->side[i]));
+        FG_CUDA(cudaStreamWaitEvent(h->stream, h->join[i], 0));
+    }
+    return FG_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -194,7 +272,8 @@ fg_status fg_create(const fg_config *cfg, fg_handle **out) {
     *out = nullptr;
     if (cfg->walks <= 0) return fail(FG_ERR_ARG, "walks must be positive");
     if (cfg->ring != FG_RING_Z2) return fail(FG_ERR_ARG, "only the Z2 ring is available in this build");
-    if (cfg->rng != FG_RNG_XORWOW && cfg->rng != FG_RNG_PHILOX) return fail(FG_ERR_ARG, "unknown rng");
+    if (cfg->mode != FG_MODE_REFERENCE && cfg->mode != FG_MODE_PHILOX_LISTS && cfg->mode != FG_MODE_FAST)
+        return fail(FG_ERR_ARG, "unknown mode");
     if (cfg->cap <= 0 || slots_for_cap(cfg->cap) == 0 || cfg->cap > FG_MAX_RANK + 2)
         return fail(FG_ERR_CAPACITY, "cap must be in [1, 352]");
     if (cfg->iterations <= 0) return fail(FG_ERR_ARG, "iterations must be positive");
@@ -227,8 +306,13 @@ fg_status fg_create(const fg_config *cfg, fg_handle **out) {
         return fail(FG_ERR_CUDA, "stream creation failed");
     }
     for (auto &e : h->ev) cudaEventCreate(&e);
+    cudaEventCreateWithFlags(&h->fork, cudaEventDisableTiming);
+    for (int i = 0; i < kSideStreams; i++) {
+        cudaStreamCreateWithFlags(&h->side[i], cudaStreamNonBlocking);
+        cudaEventCreateWithFlags(&h->join[i], cudaEventDisableTiming);
+    }
     compute_params(h);
-    if (cfg->rng == FG_RNG_XORWOW) {
+    if (cfg->mode == FG_MODE_REFERENCE) {
         if ((st = dalloc(&h->B.xorwow, (size_t)S))) { fg_destroy(h); return st; }
         k_init_xorwow<<<(S + 127) / 128, 128, 0, h->stream>>>(h->B.xorwow, S, (unsigned long long)cfg->seed);
         if (cudaGetLastError() != cudaSuccess || cudaStreamSynchronize(h->stream) != cudaSuccess) {
@@ -236,7 +320,7 @@ fg_status fg_create(const fg_config *cfg, fg_handle **out) {
             return fail(FG_ERR_CUDA, "seeding failed");
         }
     }
-    int occ = occupancy_walk_z2(cap, cfg->rng, h->wpb);
+    int occ = occupancy_walk_z2(cap, cfg->mode == FG_MODE_REFERENCE ? RNG_XORWOW : RNG_PHILOX, h->wpb);
     if (occ <= 0) occ = 1;
     int need = (S + h->wpb - 1) / h->wpb;
     h->grid = need < occ * h->sms ? need : occ * h->sms;
@@ -254,6 +338,11 @@ fg_status fg_destroy(fg_handle *h) {
         if (p) cudaFree(p);
     for (auto &e : h->ev)
         if (e) cudaEventDestroy(e);
+    for (int i = 0; i < kSideStreams; i++) {
+        if (h->side[i]) cudaStreamDestroy(h->side[i]);
+        if (h->join[i]) cudaEventDestroy(h->join[i]);
+    }
+    if (h->fork) cudaEventDestroy(h->fork);
     if (h->stream) cudaStreamDestroy(h->stream);
     delete h;
     return FG_OK;
@@ -265,11 +354,67 @@ fg_status fg_init_naive(fg_handle *h, int n1, int n2, int n3) {
         return fail(FG_ERR_ARG, "matrix sizes exceed 64 elements");
     if (n1 * n2 * n3 > h->B.cap) return fail(FG_ERR_CAPACITY, "naive rank exceeds cap");
     FG_CUDA(cudaSetDevice(h->dev));
-    k_init_naive<<<(h->B.S + 127) / 128, 128, 0, h->stream>>>(h->B, n1, n2, n3, h->cfg.ring == FG_RING_ZT);
+    k_init_naive<<<(h->B.S + 127) / 128, 128, 0, h->stream>>>(h->B, n1, n2, n3, nullptr, h->cfg.ring == FG_RING_ZT);
     FG_CUDA(cudaGetLastError());
-    FG_CUDA(launch_rebuild_z2(h->B, h->wpb, h->grid, h->stream));
+    if (h->cfg.mode != FG_MODE_FAST) FG_CUDA(launch_rebuild_z2(h->B, h->wpb, h->grid, h->stream));
     FG_CUDA(cudaStreamSynchronize(h->stream));
+    fg_status st = refresh_plan(h);
+    if (st) return st;
     h->ready = true;
+    return FG_OK;
+}
+
+fg_status fg_init_naive_shapes(fg_handle *h, const int32_t *shapes) {
+    if (!h || !shapes) return fail(FG_ERR_ARG, "null argument");
+    const int S = h->B.S;
+    for (int w = 0; w < S; w++) {
+        int n1 = shapes[w * 3], n2 = shapes[w * 3 + 1], n3 = shapes[w * 3 + 2];
+        if (n1 <= 0 || n2 <= 0 || n3 <= 0 || n1 * n2 > 64 || n2 * n3 > 64 || n3 * n1 > 64)
+            return fail(FG_ERR_ARG, "matrix sizes exceed 64 elements");
+        if (n1 * n2 * n3 > h->B.cap) return fail(FG_ERR_CAPACITY, "naive rank exceeds cap");
+    }
+    FG_CUDA(cudaSetDevice(h->dev));
+    int32_t *d = nullptr;
+    FG_CUDA(cudaMalloc(&d, (size_t)S * 12));
+    cudaError_t e = cudaMemcpy(d, shapes, (size_t)S * 12, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) {
+        k_init_naive<<<(S + 127) / 128, 128, 0, h->stream>>>(h->B, 0, 0, 0, d, h->cfg.ring == FG_RING_ZT);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess && h->cfg.mode != FG_MODE_FAST) e = launch_rebuild_z2(h->B, h->wpb, h->grid, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    cudaFree(d);
+    if (e != cudaSuccess) return fail(FG_ERR_CUDA, cudaGetErrorString(e));
+    fg_status st = refresh_plan(h);
+    if (st) return st;
+    h->ready = true;
+    return FG_OK;
+}
+
+fg_status fg_get_counters(fg_handle *h, int32_t *m, int32_t *best_rank, uint64_t *flips, uint8_t *valid) {
+    if (!h) return fail(FG_ERR_ARG, "null handle");
+    FG_CUDA(cudaSetDevice(h->dev));
+    FG_CUDA(cudaStreamSynchronize(h->stream));
+    const int S = h->B.S;
+    std::vector<WalkHeader> hdr(S);
+    FG_CUDA(cudaMemcpy(hdr.data(), h->B.hdr, sizeof(WalkHeader) * S, cudaMemcpyDeviceToHost));
+    for (int w = 0; w < S; w++) {
+        if (m) m[w] = hdr[w].m;
+        if (best_rank) best_rank[w] = hdr[w].best_rank;
+        if (flips) flips[w] = hdr[w].flips_done;
+        if (valid) valid[w] = (uint8_t)hdr[w].valid;
+    }
+    return FG_OK;
+}
+
+fg_status fg_host_alloc(uint64_t bytes, void **out) {
+    if (!out) return fail(FG_ERR_ARG, "null argument");
+    FG_CUDA(cudaHostAlloc(out, bytes ? bytes : 1, cudaHostAllocDefault));
+    return FG_OK;
+}
+
+fg_status fg_host_free(void *p) {
+    if (p) FG_CUDA(cudaFreeHost(p));
     return FG_OK;
 }
 
@@ -308,6 +453,7 @@ fg_status fg_set_records(fg_handle *h, const fg_records *rec) {
         FG_CUDA(cudaMemcpy(h->B.best_sgn, rec->best_sgn ? rec->best_sgn : rec->sgn, nf * 8, cudaMemcpyHostToDevice));
         FG_CUDA(cudaMemcpy(h->B.best_valid, rec->best_valid ? rec->best_valid : rec->valid, nf, cudaMemcpyHostToDevice));
     }
+    plan_segments(h, hdr);
     h->ready = true;
     return FG_OK;
 }
@@ -354,7 +500,8 @@ fg_status fg_run(fg_handle *h, int launches, fg_stats *stats) {
     std::vector<WalkHeader> hdr(S);
     for (int L = 0; L < launches; L++) {
         FG_CUDA(cudaEventRecord(h->ev[0], h->stream));
-        FG_CUDA(launch_walk_z2(h->B, h->P, h->cfg.rng, h->wpb, h->grid, h->stream));
+        fg_status ls = launch_walks(h);
+        if (ls) return ls;
         FG_CUDA(cudaEventRecord(h->ev[1], h->stream));
         fg_status st = launch_verify(h, 0);
         if (st) return st;
@@ -388,7 +535,9 @@ fg_status fg_minimize(fg_handle *h, int32_t *best_complexity) {
     FG_CUDA(cudaSetDevice(h->dev));
     const int S = h->B.S;
     FG_CUDA(cudaMemcpyAsync(h->d_bestC, best_complexity, S * 4, cudaMemcpyHostToDevice, h->stream));
-    FG_CUDA(launch_minimize_z2(h->B, h->P, h->cfg.rng, h->wpb, h->grid, h->d_bestC, h->stream));
+    if (h->cfg.mode == FG_MODE_FAST) return fail(FG_ERR_ARG, "the minimizer runs in a list mode");
+    FG_CUDA(launch_minimize_z2(h->B, h->P, h->cfg.mode == FG_MODE_REFERENCE ? RNG_XORWOW : RNG_PHILOX, h->wpb,
+                               h->grid, h->d_bestC, h->stream));
     FG_CUDA(cudaMemcpyAsync(best_complexity, h->d_bestC, S * 4, cudaMemcpyDeviceToHost, h->stream));
     FG_CUDA(cudaStreamSynchronize(h->stream));
     return FG_OK;

@@ -18,4 +18,9 @@ cudaError_t launch_rebuild_z2(const DevBatch &B, int wpb, int grid, cudaStream_t
 // Max resident blocks per SM of the Z2 walk kernel for this configuration.
 int occupancy_walk_z2(int cap, int rng, int wpb);
 
+// Fast mode: thread-per-walk kernel over walks [first, first + count), `scap`
+// factor slots per walk in shared memory; wide = 64-bit words (nn > 24).
+cudaError_t launch_walk_simt(const DevBatch &B, const WalkParams &P, int first, int count, int scap, int wide,
+                             int wpb, int sms, cudaStream_t s);
+
 }  // namespace fg

@@ -1,0 +1,117 @@
+// Fast-mode (SIMT, one thread per walk) Z2 walk kernel and launcher.
+#include "launch.h"
+#include "walk_simt.cuh"
+
+namespace fg {
+
+namespace {
+
+template <class W>
+__device__ __forceinline__ void simt_copy_best(const SimtZ2<W> &z, const DevBatch &B, int w) {
+    uint64_t *dst = B.best_fac + (size_t)w * 3 * B.cap;
+    for (int c = 0; c < 3; c++)
+        for (int t = 0; t < B.cap; t++) dst[c * B.cap + t] = t < z.m ? (uint64_t)z.F(c, t) : 0ull;
+}
+
+// randomWalkKernel (flip_graph.cu:520-573) for one walk, one thread.
+template <class W>
+__device__ void simt_walk_one(const DevBatch &B, const WalkParams &P, int w, W *s, int scap) {
+    const WalkHeader h = B.hdr[w];
+    ThreadPhilox r;
+    r.k0 = P.key0; r.k1 = P.key1; r.walk = (uint32_t)w; r.count = h.draws; r.blk = -1; r.P = &P;
+    SimtZ2<W> z(r);
+    z.s = s;
+    z.cap = scap;
+    z.n0 = h.n[0]; z.n1 = h.n[1]; z.n2 = h.n[2];
+    z.nn0 = z.n0 * z.n1; z.nn1 = z.n1 * z.n2; z.nn2 = z.n2 * z.n0;
+    z.full = z.n0 * z.n1 * z.n2;
+    z.m = h.m;
+    z.status = h.status;
+    const uint64_t *src = B.fac + (size_t)w * 3 * B.cap;
+    for (int c = 0; c < 3; c++)
+        for (int t = 0; t < z.m; t++) z.A(c, t) = (W)src[c * B.cap + t];
+    z.rebuild();
+    int flipsCount = h.flips, bestRank = h.best_rank, bestM = h.best_m;
+    uint64_t accepted = 0;
+    for (int it = 0; it < P.iterations; it++) {
+        const int rank = z.m;
+        if (!z.tryFlip(true)) {
+            z.tryExpand(randint(1, 2, r));
+            if (z.status) break;
+            continue;
+        }
+        accepted++;
+        if (z.m < rank) flipsCount = 0;
+        flipsCount++;
+        if (z.m < bestRank || (z.m == bestRank && r.tie())) {
+            bestRank = z.m;
+            bestM = z.m;
+            simt_copy_best(z, B, w);
+        }
+        if (r.gate_reduce()) z.tryReduce();
+        if (r.gate_expand() && z.m <= bestM + 2) {
+            if (z.tryExpand(randint(1, 2, r))) flipsCount = 0;
+        }
+        if (flipsCount >= P.plus_iterations && z.tryPlus()) flipsCount = 0;
+        if (z.status) break;
+    }
+    uint64_t *dst = B.fac + (size_t)w * 3 * B.cap;
+    for (int c = 0; c < 3; c++)
+        for (int t = 0; t < B.cap; t++) dst[c * B.cap + t] = t < z.m ? (uint64_t)z.F(c, t) : 0ull;
+    WalkHeader o = h;
+    o.m = z.m;
+    o.flips = flipsCount;
+    o.best_rank = bestRank;
+    o.best_m = bestM;
+    o.status = z.status;
+    o.list_size[0] = o.list_size[1] = o.list_size[2] = 0;
+    o.draws = r.count;
+    o.flips_done = accepted;
+    B.hdr[w] = o;
+}
+
+// Walks [first, first + count) of the batch; scap = slots per walk in shared memory.
+template <class W>
+__global__ void k_walk_simt(DevBatch B, WalkParams P, int first, int count, int scap) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, wpb = blockDim.x >> 5;
+    W *s = reinterpret_cast<W *>(smem) + (size_t)warp * 3 * scap * 32 + lane;
+    for (int base = (blockIdx.x * wpb + warp) * 32; base < count; base += gridDim.x * wpb * 32) {
+        const int q = base + lane;
+        if (q < count) simt_walk_one<W>(B, P, first + q, s, scap);
+    }
+}
+
+template <class W> size_t simt_smem(int scap, int wpb) { return (size_t)wpb * 3 * scap * 32 * sizeof(W); }
+
+template <class W>
+cudaError_t walk_simt_t(const DevBatch &B, const WalkParams &P, int first, int count, int scap, int wpb, int sms,
+                        cudaStream_t s) {
+    int dev = 0, optin = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    const size_t perWarp = simt_smem<W>(scap, 1);
+    if (perWarp > (size_t)optin) return cudaErrorInvalidConfiguration;  // rank too large for this mode
+    while (wpb > 1 && simt_smem<W>(scap, wpb) > (size_t)optin) wpb--;
+    size_t smem = simt_smem<W>(scap, wpb);
+    cudaError_t e = cudaFuncSetAttribute(k_walk_simt<W>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    int blocks = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, k_walk_simt<W>, 32 * wpb, smem);
+    if (e != cudaSuccess) return e;
+    if (blocks < 1) return cudaErrorInvalidConfiguration;
+    int need = (count + 32 * wpb - 1) / (32 * wpb);
+    int grid = need < blocks * sms ? need : blocks * sms;
+    k_walk_simt<W><<<grid, 32 * wpb, smem, s>>>(B, P, first, count, scap);
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t launch_walk_simt(const DevBatch &B, const WalkParams &P, int first, int count, int scap, int wide,
+                             int wpb, int sms, cudaStream_t s) {
+    if (wide) return walk_simt_t<unsigned long long>(B, P, first, count, scap, wpb, sms, s);
+    return walk_simt_t<uint32_t>(B, P, first, count, scap, wpb, sms, s);
+}
+
+}  // namespace fg

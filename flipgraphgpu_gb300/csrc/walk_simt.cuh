@@ -1,0 +1,299 @@
+// Fast-mode Z2 walk: one THREAD per walk (SIMT across walks).
+//
+// Each warp holds 32 walks in shared memory, interleaved by lane:
+// word (c, t, lane) = factor c of term t of the lane's walk, so every access
+// a thread makes to its own walk hits bank (lane) -- conflict free for any
+// per-thread index.  The top byte of each word counts the term's equal
+// partners in that component (how many other terms carry the same factor);
+// the factor itself uses the low bits (<= 24 bits in a 32-bit word, <= 56 in
+// a 64-bit word).  With these counts a uniformly random ordered equal pair is
+// located by a prefix walk over the counts, and after a flip the counts are
+// updated in the same O(m) scan that looks for reductions -- no FlipSet lists.
+//
+// Semantics: the reference's walk (flip_graph.cu:520-573, scheme_z2.cu) with
+// the Philox stream and implicit pair enumeration: the flip proposal is
+// uniform over equal-factor pairs with a uniform orientation, exactly the
+// reference's distribution; ranks drop, plus transitions, splits and
+// compaction orders follow the reference.
+#pragma once
+#include "fg_device.cuh"
+
+namespace fg {
+
+// Per-thread Philox stream: the same word sequence as PhiloxDraws (word q of
+// walk w = Philox(ctr = (q/4 lo, q/4 hi, w, 0), key)[q % 4]).
+struct ThreadPhilox {
+    uint32_t k0, k1, walk;
+    uint64_t count;
+    int64_t blk;
+    uint4 buf;
+    const WalkParams *P;
+    __device__ __forceinline__ uint32_t raw() {
+        int64_t b = (int64_t)(count >> 2);
+        if (b != blk) {
+            buf = philox4x32_10(make_uint4((uint32_t)b, (uint32_t)((uint64_t)b >> 32), walk, 0u), k0, k1);
+            blk = b;
+        }
+        uint32_t e = (uint32_t)count & 3u;
+        count++;
+        return e == 0 ? buf.x : e == 1 ? buf.y : e == 2 ? buf.z : buf.w;
+    }
+    __device__ __forceinline__ uint32_t below(uint32_t k) { return __umulhi(raw(), k); }
+    __device__ __forceinline__ bool coin() { return raw() >> 31; }
+    __device__ __forceinline__ bool gate_reduce() { return P->reduce_T && (uint64_t)raw() < P->reduce_T; }
+    __device__ __forceinline__ bool gate_expand() { return P->expand_T && (uint64_t)raw() < P->expand_T; }
+    __device__ __forceinline__ void gate_zero() {}
+    __device__ __forceinline__ bool tie() { return raw() < 42949672u; }
+    __device__ __forceinline__ uint64_t mask(int nn) { return nn >= 32 ? (uint64_t)raw() : (uint64_t)(raw() & ((1u << nn) - 1u)); }
+};
+
+template <class W>
+struct SimtZ2 {
+    static constexpr int HS = (int)sizeof(W) * 8 - 8;  // partner count lives in bits [HS, HS+8)
+    static constexpr W FM = ((W)1 << HS) - 1;
+    static constexpr W ONE = (W)1 << HS;
+
+    W *s;  // this lane's walk: word (c, t) at s[(c * cap + t) * 32]
+    int cap;
+    int n0, n1, n2, nn0, nn1, nn2, full;
+    int m;
+    int P0, P1, P2;  // ordered equal pairs per component
+    int status;
+    ThreadPhilox &r;
+
+    __device__ SimtZ2(ThreadPhilox &rr) : r(rr) {}
+
+    __device__ __forceinline__ W &A(int c, int t) const { return s[(c * cap + t) << 5]; }
+    __device__ __forceinline__ W F(int c, int t) const { return A(c, t) & FM; }
+    __device__ __forceinline__ int nn(int c) const { return c == 0 ? nn0 : (c == 1 ? nn1 : nn2); }
+    __device__ __forceinline__ bool nonzero(int t) const { return F(0, t) && F(1, t) && F(2, t); }
+    __device__ __forceinline__ void addP(int c, int d) { if (c == 0) P0 += d; else if (c == 1) P1 += d; else P2 += d; }
+
+    // Partner counts of every term from scratch (after structural edits).
+    __device__ void rebuild() {
+        int tot[3] = {0, 0, 0};
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            for (int t = 0; t < m; t++) {
+                const W v = F(c, t);
+                int h = 0;
+                for (int u = 0; u < m; u++) h += (u != t) & (F(c, u) == v);
+                A(c, t) = v | ((W)h << HS);
+                tot[c] += h;
+            }
+        }
+        P0 = tot[0]; P1 = tot[1]; P2 = tot[2];
+    }
+
+    __device__ __forceinline__ void moveTerm(int dst, int src) {
+#pragma unroll
+        for (int c = 0; c < 3; c++) A(c, dst) = F(c, src);
+    }
+
+    __device__ void removeZeroes() {  // scheme_z2.cu:152-164 (no re-check of the moved term)
+        while (m > 0 && !nonzero(m - 1)) m--;
+        for (int t = 0; t < m; t++)
+            if (!nonzero(t)) { m--; moveTerm(t, m); }
+    }
+
+    __device__ void removeAt(int t) {
+        m--;
+        if (t != m) moveTerm(t, m);
+    }
+
+    __device__ void addTriplet(int i, int j, int k, W a, W b, W c) {
+        if (m >= cap) { status |= ST_OVERFLOW; return; }
+        A(i, m) = a; A(j, m) = b; A(k, m) = c;
+        m++;
+    }
+
+    __device__ void reduce(int i, int a, int b) {  // scheme_z2.cu:631-641
+        const W v = F(i, a) ^ F(i, b);
+        A(i, a) = v;
+        removeAt(b);
+        if (!v) removeZeroes();
+        rebuild();
+    }
+
+    // flip (scheme_z2.cu:531-577) with the count update fused into the reduction scan.
+    __device__ void flip(int i, int j, int k, int a, int b, bool checkReduce) {
+        const W wja = A(j, a), wjb = A(j, b), wka = A(k, a), wkb = A(k, b);
+        const W oldA = wja & FM, newA = oldA ^ (wjb & FM);
+        const W oldB = wkb & FM, newB = oldB ^ (wka & FM);
+        const int oldHa = (int)(wja >> HS), oldHb = (int)(wkb >> HS);
+        A(j, a) = newA;
+        A(k, b) = newB;
+        if (!newA || !newB) {
+            removeZeroes();
+            rebuild();
+            return;
+        }
+        const W xia = F(i, a), xka = wka & FM, xib = F(i, b), xjb = wjb & FM;
+        int cntA = 0, cntB = 0, red = -1, part = 0;
+        for (int t = 0; t < m; t++) {
+            const W wj = A(j, t), wk = A(k, t);
+            const W vj = wj & FM, vk = wk & FM;
+            if (t != a) {
+                const bool o = vj == oldA, nw = vj == newA;
+                if (nw) {
+                    cntA++;
+                    if (checkReduce && red < 0 && (F(i, t) == xia || vk == xka)) { red = t; part = 0; }
+                }
+                if (o | nw) A(j, t) = wj + (nw ? ONE : (W)0) - (o ? ONE : (W)0);
+            }
+            if (t != b) {
+                const bool o = vk == oldB, nw = vk == newB;
+                if (nw) {
+                    cntB++;
+                    if (checkReduce && red < 0 && (F(i, t) == xib || vj == xjb)) { red = t; part = 1; }
+                }
+                if (o | nw) A(k, t) = wk + (nw ? ONE : (W)0) - (o ? ONE : (W)0);
+            }
+        }
+        A(j, a) = newA | ((W)cntA << HS);
+        A(k, b) = newB | ((W)cntB << HS);
+        addP(j, 2 * (cntA - oldHa));
+        addP(k, 2 * (cntB - oldHb));
+        if (red >= 0) {
+            // The reference tests, at the first such term, the j-part before the k-part.
+            const int t = red;
+            if (part == 0) {
+                if (F(i, t) == xia) reduce(k, t, a);
+                else reduce(i, t, a);
+            } else {
+                if (F(i, t) == xib) reduce(j, t, b);
+                else reduce(i, t, b);
+            }
+        }
+    }
+
+    // Uniform ordered equal pair in canonical order (component, term, partner).
+    __device__ bool tryFlip(bool checkReduce) {
+        const int Ptot = P0 + P1 + P2;
+        if (Ptot <= 0) return false;
+        int q = (int)r.below((uint32_t)Ptot);
+        int c;
+        if (q < P0) c = 0;
+        else if (q < P0 + P1) { c = 1; q -= P0; }
+        else { c = 2; q -= P0 + P1; }
+        int a = 0;
+        for (;; a++) {
+            const int h = (int)(A(c, a) >> HS);
+            if (q < h) break;
+            q -= h;
+        }
+        const W va = F(c, a);
+        int b = 0;
+        for (;; b++)
+            if (b != a && F(c, b) == va) {
+                if (q == 0) break;
+                q--;
+            }
+        int i = c, j = c == 0 ? 1 : 0, k = c == 2 ? 1 : 2;
+        if (r.coin()) { int tmp = j; j = k; k = tmp; }
+        flip(i, j, k, a, b, checkReduce);
+        return true;
+    }
+
+    __device__ void plus(int i, int j, int k, int p, int q, int variant) {  // scheme_z2.cu:579-612
+        const W a1 = F(i, p), b1 = F(j, p), c1 = F(k, p);
+        const W a2 = F(i, q), b2 = F(j, q), c2 = F(k, q);
+        const W a = a1 ^ a2, b = b1 ^ b2, c = c1 ^ c2;
+        if (variant == 0) { A(j, p) = b; A(i, q) = a; addTriplet(i, j, k, a1, b2, c); }
+        else if (variant == 1) { A(k, p) = c; A(j, q) = b; addTriplet(i, j, k, a, b1, c2); }
+        else { A(i, p) = a; A(k, q) = c; addTriplet(i, j, k, a2, b, c1); }
+        if (!a || !b || !c) removeZeroes();
+        rebuild();
+    }
+
+    __device__ void split(int i, int j, int k, int t, W a1) {  // scheme_z2.cu:614-619
+        const W a2 = F(i, t) ^ a1, bj = F(j, t), bk = F(k, t);
+        A(i, t) = a1;
+        addTriplet(i, j, k, a2, bj, bk);
+        rebuild();
+    }
+
+    __device__ __forceinline__ void perm3(int &i, int &j, int &k) {
+        int p0 = 0, p1 = 1, p2 = 2;
+        int q = (int)r.below(3);
+        if (q == 0) { int t = p2; p2 = p0; p0 = t; } else if (q == 1) { int t = p2; p2 = p1; p1 = t; }
+        q = (int)r.below(2);
+        if (q == 0) { int t = p1; p1 = p0; p0 = t; }
+        i = p0; j = p1; k = p2;
+    }
+
+    __device__ bool tryPlus() {  // scheme_z2.cu:1029-1050
+        if (m >= kMaxRank || m >= full) return false;
+        int a = (int)r.below((uint32_t)m), b = (int)r.below((uint32_t)m);
+        int guard = 0;
+        while (a == b || F(0, a) == F(0, b) || F(1, a) == F(1, b) || F(2, a) == F(2, b)) {
+            if (++guard > kRetryCap) { status |= ST_RETRY; return false; }
+            a = (int)r.below((uint32_t)m);
+            b = (int)r.below((uint32_t)m);
+        }
+        int i, j, k;
+        perm3(i, j, k);
+        int variant = (int)r.below(3);
+        plus(i, j, k, a, b, variant);
+        return true;
+    }
+
+    __device__ bool trySplit() {  // scheme_z2.cu:1052-1078
+        if (m >= kMaxRank || m >= full) return false;
+        int t = (int)r.below((uint32_t)m);
+        int i, j, k;
+        perm3(i, j, k);
+        W a1 = (W)r.mask(nn(i));
+        const W a2 = F(i, t);
+        int loop = 0;
+        while (loop < 5 && a1 == a2) { a1 = (W)r.mask(nn(i)); loop++; }
+        if (loop == 5) return false;
+        split(i, j, k, t, a1);
+        return true;
+    }
+
+    __device__ bool trySplitExisted() {  // scheme_z2.cu:1080-1104
+        if (m >= kMaxRank || m >= full) return false;
+        int i, j, k;
+        perm3(i, j, k);
+        int a = (int)r.below((uint32_t)m), b = (int)r.below((uint32_t)m);
+        int loop = 0;
+        while (loop < 5 && (a == b || F(i, a) == F(i, b))) { b = (int)r.below((uint32_t)m); loop++; }
+        if (loop == 5) return false;
+        split(i, j, k, a, F(i, b));
+        return true;
+    }
+
+    __device__ bool tryExpand(int count) {  // scheme_z2.cu:1106-1125
+        bool result = false;
+        for (int q = 0; q < count && m < full; q++) {
+            int v = (int)r.below(3);
+            if (v == 0) result |= tryPlus();
+            else if (v == 1) result |= trySplit();
+            else result |= trySplitExisted();
+        }
+        return result;
+    }
+
+    // tryReduce (scheme_z2.cu:1127-1154) over the equal pairs in canonical order.
+    __device__ bool tryReduce() {
+        for (int a = 0; a < m; a++)
+            for (int b = a + 1; b < m; b++)
+                if (F(0, a) == F(0, b)) {
+                    if (F(1, a) == F(1, b)) { reduce(2, a, b); return true; }
+                    if (F(2, a) == F(2, b)) { reduce(1, a, b); return true; }
+                }
+        for (int a = 0; a < m; a++)
+            for (int b = a + 1; b < m; b++)
+                if (F(1, a) == F(1, b) && F(2, a) == F(2, b)) { reduce(0, a, b); return true; }
+        return false;
+    }
+
+    __device__ int complexity() const {
+        int c = 0;
+        for (int t = 0; t < m; t++) c += __popcll((uint64_t)F(0, t)) + __popcll((uint64_t)F(1, t)) + __popcll((uint64_t)F(2, t));
+        return c - 2 * m - nn2;
+    }
+};
+
+}  // namespace fg

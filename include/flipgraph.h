@@ -30,12 +30,17 @@ typedef enum {
 
 typedef enum { FG_RING_Z2 = 0, FG_RING_ZT = 1 } fg_ring;
 
-/* Draw stream.  FG_RNG_XORWOW is the reference's stream: cuRAND XORWOW with
- * curand_init(seed, walk_index, 0) per walk (flip_graph.cu:445-451), consumed
- * at exactly the reference's draw sites, so trajectories match the reference
- * bit for bit.  FG_RNG_PHILOX is the fast stream: Philox4x32-10 keyed by the
- * seed, with multiply-high ranges and integer gate thresholds. */
-typedef enum { FG_RNG_XORWOW = 0, FG_RNG_PHILOX = 1 } fg_rng;
+/* Walk mode.
+ * FG_MODE_REFERENCE: the reference's stream -- cuRAND XORWOW with
+ *   curand_init(seed, walk_index, 0) per walk (flip_graph.cu:445-451) -- drawn
+ *   at exactly the reference's draw sites over the reference's FlipSet lists,
+ *   so trajectories match the reference bit for bit.  One warp per walk.
+ * FG_MODE_PHILOX_LISTS: the same list semantics with the Philox4x32-10 stream
+ *   (multiply-high ranges, integer gate thresholds).  One warp per walk.
+ * FG_MODE_FAST: Philox stream, implicit pair enumeration (no lists: an ordered
+ *   equal-factor pair is drawn uniformly in canonical order -- the reference's
+ *   proposal distribution), one thread per walk.  The throughput mode. */
+typedef enum { FG_MODE_REFERENCE = 0, FG_MODE_PHILOX_LISTS = 1, FG_MODE_FAST = 2 } fg_mode;
 
 /* Walk status bits (per walk). */
 enum { FG_WALK_RETRY = 2, FG_WALK_OVERFLOW = 4 };
@@ -45,7 +50,7 @@ enum { FG_WALK_RETRY = 2, FG_WALK_OVERFLOW = 4 };
  * (randomWalkKernel, flip_graph.cu:520). */
 typedef struct {
     int32_t ring;             /* fg_ring */
-    int32_t rng;              /* fg_rng */
+    int32_t mode;             /* fg_mode */
     int32_t walks;            /* --schemes */
     int32_t cap;              /* factor slots per walk: >= max(initial rank, n1*n2*n3) */
     uint64_t seed;            /* --seed (nonzero; the CLI maps 0 to time(0) as the reference does) */
@@ -110,6 +115,12 @@ fg_status fg_destroy(fg_handle *h);
  * flip_graph.cu:453-457,510-518). */
 fg_status fg_init_naive(fg_handle *h, int n1, int n2, int n3);
 
+/* Per-walk shapes: walk w := naive shapes[w][0] x shapes[w][1] x shapes[w][2]
+ * scheme (the batched uneven search: many shapes in one launch).  The
+ * reference can only do this through --input-path with one scheme per shape
+ * replicated idx % count (flip_graph.cu:459-470). */
+fg_status fg_init_naive_shapes(fg_handle *h, const int32_t *shapes);
+
 /* Copies host records into the handle (FlipGraph::initializeFromFile +
  * initializeCopyKernel, flip_graph.cu:201-224,459-470, after the host has
  * parsed and replicated the schemes).  rng_pos is not read: streams keep
@@ -148,6 +159,15 @@ fg_status fg_xorwow_tape(uint64_t seed, int first_walk, int count, int draws, in
  * out[q] = Philox(ctr[q], key) for q < count, ctr [count][4], out [count][4]. */
 fg_status fg_philox_blocks(const uint32_t *ctr, int count, uint32_t key0, uint32_t key1, int device,
                            uint32_t *out);
+
+/* Per-walk counters of the last launch without copying records:
+ * m, best_rank [walks]; flips [walks] accepted in the last launch; valid [walks]
+ * result of the last verification.  Any pointer may be NULL. */
+fg_status fg_get_counters(fg_handle *h, int32_t *m, int32_t *best_rank, uint64_t *flips, uint8_t *valid);
+
+/* Page-locked host buffers for fast record transfers (cudaHostAlloc). */
+fg_status fg_host_alloc(uint64_t bytes, void **out);
+fg_status fg_host_free(void *p);
 
 /* Message of the last failing call on this thread ("" when none). */
 const char *fg_last_error(void);

@@ -147,6 +147,10 @@ struct Z2 {
     uint64_t x[3][kMaxRank];
     FlipList lists[3];
     int32_t *status;
+    // Implicit pair enumeration (the library's fast mode): no FlipSet lists;
+    // a flip samples an ordered equal-factor pair uniformly in the canonical
+    // order (component c, term t ascending, partner t' ascending).
+    bool implicit = false;
 
     bool nonzero(int t) const { return x[0][t] && x[1][t] && x[2][t]; }
 
@@ -168,10 +172,47 @@ struct Z2 {
     void rebuildLists() {  // initFlips, scheme_z2.cu:141-150
         for (int c = 0; c < 3; c++) {
             lists[c].clear();
+            if (implicit) continue;
             for (int a = 0; a < m; a++)
                 for (int b = a + 1; b < m; b++)
                     if (x[c][a] == x[c][b]) lists[c].add(a, b);
         }
+    }
+
+    int partners(int c, int t) const {
+        int k = 0;
+        for (int u = 0; u < m; u++) k += u != t && x[c][u] == x[c][t];
+        return k;
+    }
+
+    // Fast-mode flip proposal: q uniform over the ordered equal pairs, located in
+    // canonical order; the orientation of the pair comes from the ordering, one
+    // coin orients (j, k) as in the reference.
+    template <class R> bool tryFlipImplicit(R &r, bool checkReduce) {
+        int total[3] = {0, 0, 0};
+        for (int c = 0; c < 3; c++)
+            for (int t = 0; t < m; t++) total[c] += partners(c, t);
+        uint32_t P = (uint32_t)(total[0] + total[1] + total[2]);
+        if (!P) return false;
+        uint32_t q = r.below(P);
+        int c = 0;
+        while (q >= (uint32_t)total[c]) { q -= total[c]; c++; }
+        int a = 0;
+        for (;; a++) {
+            uint32_t h = (uint32_t)partners(c, a);
+            if (q < h) break;
+            q -= h;
+        }
+        int b = 0;
+        for (;; b++)
+            if (b != a && x[c][b] == x[c][a]) {
+                if (q == 0) break;
+                q--;
+            }
+        int i = c, j = c == 0 ? 1 : 0, k = c == 2 ? 1 : 2;
+        if (r.coin()) std::swap(j, k);
+        flip(i, j, k, a, b, checkReduce);
+        return true;
     }
 
     void moveTerm(int dst, int src) { for (int c = 0; c < 3; c++) x[c][dst] = x[c][src]; }
@@ -218,14 +259,14 @@ struct Z2 {
                     if (x[i][t] == x[i][a]) { reduce(k, t, a); return; }
                     if (x[k][t] == x[k][a]) { reduce(i, t, a); return; }
                 }
-                lists[j].add(a, t);
+                if (!implicit) lists[j].add(a, t);
             }
             if (t != b && x[k][t] == x[k][b]) {
                 if (checkReduce) {
                     if (x[i][t] == x[i][b]) { reduce(j, t, b); return; }
                     if (x[j][t] == x[j][b]) { reduce(i, t, b); return; }
                 }
-                lists[k].add(b, t);
+                if (!implicit) lists[k].add(b, t);
             }
         }
     }
@@ -249,6 +290,7 @@ struct Z2 {
     }
 
     template <class R> bool tryFlip(R &r, bool checkReduce) {  // scheme_z2.cu:982-1027
+        if (implicit) return tryFlipImplicit(r, checkReduce);
         int size = lists[0].size + lists[1].size + lists[2].size;
         if (!size) return false;
         int idx = (int)r.below((uint32_t)size);
@@ -322,6 +364,18 @@ struct Z2 {
     }
 
     bool tryReduce() {  // scheme_z2.cu:1127-1154
+        if (implicit) {  // same tests over the equal pairs in canonical order
+            for (int a = 0; a < m; a++)
+                for (int b = a + 1; b < m; b++)
+                    if (x[0][a] == x[0][b]) {
+                        if (x[1][a] == x[1][b]) { reduce(2, a, b); return true; }
+                        if (x[2][a] == x[2][b]) { reduce(1, a, b); return true; }
+                    }
+            for (int a = 0; a < m; a++)
+                for (int b = a + 1; b < m; b++)
+                    if (x[1][a] == x[1][b] && x[2][a] == x[2][b]) { reduce(0, a, b); return true; }
+            return false;
+        }
         for (int p = 0; p < lists[0].size; p++) {
             int a = lists[0].first(p), b = lists[0].second(p);
             if (x[1][a] == x[1][b]) { reduce(2, a, b); return true; }
@@ -780,6 +834,7 @@ void walkLaunch(Scheme &s, R &r, const fgo_walk_cfg *cfg, fgo_batch *b, int w) {
             s.tryExpand(randint(1, 2, r), r);
             continue;
         }
+        if (b->accepted) b->accepted[w]++;
         if (s.m < rank) flipsCount = 0;
         flipsCount++;
         if (s.m < bestRank || (s.m == bestRank && r.tie())) {
@@ -806,11 +861,15 @@ template <> void loadScheme<ZT>(ZT &s, const fgo_batch *b, int w, int cap) { loa
 inline void storeScheme(const Z2 &s, fgo_batch *b, int w, int cap) { storeZ2(s, b, w, cap); }
 inline void storeScheme(const ZT &s, fgo_batch *b, int w, int cap) { storeZT(s, b, w, cap); }
 
+inline void setImplicit(Z2 &s, bool on) { s.implicit = on; }
+inline void setImplicit(ZT &, bool) {}
+
 template <class Scheme>
 void runWalks(const fgo_walk_cfg *cfg, int S, fgo_batch *b, const fgo_tape *tape) {
     Scheme *s = new Scheme;
     for (int w = 0; w < S; w++) {
         loadScheme(*s, b, w, cfg->cap);
+        setImplicit(*s, cfg->rng == FGO_RNG_FAST);
         s->status = &b->status[w];
         if (cfg->rng == FGO_RNG_TAPE) {
             RefDraws r;
@@ -857,6 +916,7 @@ void runMinimize(const fgo_walk_cfg *cfg, int S, fgo_batch *b, const fgo_tape *t
     Scheme *s = new Scheme;
     for (int w = 0; w < S; w++) {
         loadScheme(*s, b, w, cfg->cap);  // lists keep their persisted order
+        setImplicit(*s, cfg->rng == FGO_RNG_FAST);
         s->status = &b->status[w];
         if (cfg->rng == FGO_RNG_TAPE) {
             RefDraws r;

@@ -20,11 +20,14 @@
 extern "C" {
 #endif
 
-/* Draw source.  FGO_RNG_TAPE replays recorded cuRAND XORWOW outputs (both the
- * curand() word and the curand_uniform() float of every draw), which is the
- * reference's stream; FGO_RNG_PHILOX is the library's fast-mode stream
- * (Philox4x32-10 keyed by the seed, one counter stream per walk). */
-enum { FGO_RNG_TAPE = 0, FGO_RNG_PHILOX = 1 };
+/* Draw source and pair enumeration.  FGO_RNG_TAPE replays recorded cuRAND
+ * XORWOW outputs (both the curand() word and the curand_uniform() float of
+ * every draw), which is the reference's stream, over the reference's FlipSet
+ * lists; FGO_RNG_PHILOX is the library's Philox4x32-10 stream (keyed by the
+ * seed, one counter stream per walk) over the same lists; FGO_RNG_FAST is the
+ * Philox stream with implicit pair enumeration (no lists: an ordered equal
+ * pair is drawn uniformly in canonical order), the library's fast mode. */
+enum { FGO_RNG_TAPE = 0, FGO_RNG_PHILOX = 1, FGO_RNG_FAST = 2 };
 enum { FGO_RING_Z2 = 0, FGO_RING_ZT = 1 };
 
 typedef struct {
@@ -60,6 +63,7 @@ typedef struct {
     uint8_t *best_valid; /* ZT only */
     int64_t *rng_pos;    /* [S] draws consumed so far (tape position / Philox word index) */
     int32_t *status;     /* [S] 0 ok; bit 1 tape exhausted; bit 2 capped retry loop; bit 4 slot overflow */
+    int64_t *accepted;   /* [S] accepted flips, accumulated (may be NULL) */
 } fgo_batch;
 
 /* Tape: draws for walk w are tape_draws[tape_off[w] .. tape_off[w+1]). */

@@ -16,7 +16,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 MAX_PAIRS = 500
 RING = {"z2": 0, "zt": 1}
-RNG = {"tape": 0, "philox": 1}
+RNG = {"tape": 0, "philox": 1, "fast": 2}
 
 
 def lib_path():
@@ -56,7 +56,7 @@ class WalkCfg(ctypes.Structure):
 class _Batch(ctypes.Structure):
     _fields_ = [(name, ctypes.c_void_p) for name in
                 ("n", "m", "fac", "sgn", "valid", "list_size", "list_pairs", "flips", "best_rank",
-                 "best_m", "best_fac", "best_sgn", "best_valid", "rng_pos", "status")]
+                 "best_m", "best_fac", "best_sgn", "best_valid", "rng_pos", "status", "accepted")]
 
 
 class _Tape(ctypes.Structure):
@@ -71,7 +71,7 @@ class WalkBatch:
     """S walk records with `cap` factor slots each (numpy, C-contiguous)."""
 
     FIELDS = ("n", "m", "fac", "sgn", "valid", "list_size", "list_pairs", "flips", "best_rank",
-              "best_m", "best_fac", "best_sgn", "best_valid", "rng_pos", "status")
+              "best_m", "best_fac", "best_sgn", "best_valid", "rng_pos", "status", "accepted")
 
     def __init__(self, S, cap, ring="z2"):
         self.S, self.cap, self.ring = S, cap, ring
@@ -91,6 +91,7 @@ class WalkBatch:
         self.best_valid = np.zeros((S, 3, cap), np.uint8) if zt else None
         self.rng_pos = np.zeros(S, np.int64)
         self.status = np.zeros(S, np.int32)
+        self.accepted = np.zeros(S, np.int64)
 
     def copy(self):
         b = WalkBatch.__new__(WalkBatch)

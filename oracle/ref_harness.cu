@@ -211,11 +211,79 @@ static int cmd_reduce(int argc, char **argv) {
     return 0;
 }
 
+// time S ITERS LAUNCHES SEED PLUS_ITERS shape... (e.g. 2x2x2 3x3x3)
+//   Throughput of the reference's own walk kernel on the batched uneven
+//   workload, set up the way the reference runs several shapes: one naive
+//   scheme per shape replicated idx % count by initializeCopyKernel
+//   (flip_graph.cu:459-470), best ranks per shape as updateRanks leaves them
+//   (flip_graph.cu:249-266), resize off.  Each launch is timed with CUDA
+//   events; flips are counted as S * ITERS per launch, an upper bound (every
+//   step of randomWalkKernel that finds no flip candidate is not a flip).
+static int cmd_time(int argc, char **argv) {
+    if (argc < 8) { fprintf(stderr, "time: bad arguments\n"); return 1; }
+    int S = atoi(argv[2]), iters = atoi(argv[3]), launches = atoi(argv[4]), seed = atoi(argv[5]);
+    int plusIters = atoi(argv[6]);
+    int count = argc - 7;
+    int blockSize = 32, numBlocks = (S + blockSize - 1) / blockSize;
+    Scheme *schemes, *best; int *bestRanks, *flips; curandState *states;
+    HCHECK(cudaMallocManaged(&schemes, S * sizeof(Scheme)));
+    HCHECK(cudaMallocManaged(&best, S * sizeof(Scheme)));
+    HCHECK(cudaMallocManaged(&bestRanks, S * sizeof(int)));
+    HCHECK(cudaMallocManaged(&flips, S * sizeof(int)));
+    HCHECK(cudaMallocManaged(&states, S * sizeof(curandState)));
+    for (int i = 0; i < count; i++) {
+        int a, b, c;
+        if (sscanf(argv[7 + i], "%dx%dx%d", &a, &b, &c) != 3) { fprintf(stderr, "bad shape\n"); return 1; }
+        schemes[i].initializeNaive(a, b, c);
+    }
+    initializeRandomStatesKernel<<<numBlocks, blockSize>>>(states, S, seed);
+    initializeCopyKernel<<<numBlocks, blockSize>>>(schemes, S, count);
+    HCHECK(cudaDeviceSynchronize());
+    initializeSchemesKernel<<<numBlocks, blockSize>>>(schemes, best, bestRanks, flips, 1, 1, 1, S);
+    HCHECK(cudaDeviceSynchronize());
+    for (int w = 0; w < S; w++) bestRanks[w] = schemes[w].m;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    // One untimed launch brings managed memory to the device.
+    randomWalkKernel<<<numBlocks, blockSize>>>(schemes, best, bestRanks, flips, states, S, iters, plusIters,
+                                               0.0, 0.01, 0.0, 0.0, false);
+    HCHECK(cudaDeviceSynchronize());
+    double total_ms = 0;
+    for (int L = 0; L < launches; L++) {
+        cudaEventRecord(e0);
+        randomWalkKernel<<<numBlocks, blockSize>>>(schemes, best, bestRanks, flips, states, S, iters, plusIters,
+                                                   0.0, 0.01, 0.0, 0.0, false);
+        cudaEventRecord(e1);
+        HCHECK(cudaEventSynchronize(e1));
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        total_ms += ms;
+        printf("launch %d: %.3f ms\n", L, ms);
+    }
+    int minRank[64];
+    for (int i = 0; i < count && i < 64; i++) minRank[i] = 1 << 30;
+    int valid = 0;
+    for (int w = 0; w < S; w++) {
+        int i = w % count;
+        if (i < 64 && bestRanks[w] < minRank[i]) minRank[i] = bestRanks[w];
+        valid += schemes[w].validate();
+    }
+    double flipsUpper = (double)S * iters * launches;
+    printf("{\"walks\": %d, \"iterations\": %d, \"launches\": %d, \"ms_per_launch\": %.3f, "
+           "\"flips_per_s_upper_bound\": %.6e, \"valid_walks\": %d, \"best_ranks\": [",
+           S, iters, launches, total_ms / launches, flipsUpper / (total_ms / 1000.0), valid);
+    for (int i = 0; i < count && i < 64; i++) printf("%s%d", i ? ", " : "", minRank[i]);
+    printf("]}\n");
+    return 0;
+}
+
 int main(int argc, char **argv) {
-    if (argc < 2) { fprintf(stderr, "usage: ref_harness walk|reduce ...\n"); return 1; }
+    if (argc < 2) { fprintf(stderr, "usage: ref_harness walk|reduce|time ...\n"); return 1; }
     std::string cmd = argv[1];
     if (cmd == "walk") return cmd_walk(argc, argv);
     if (cmd == "reduce") return cmd_reduce(argc, argv);
+    if (cmd == "time") return cmd_time(argc, argv);
     fprintf(stderr, "unknown command %s\n", argv[1]);
     return 1;
 }

@@ -75,6 +75,35 @@ def run_oracle_like(rec0, cfg_kw, launches, rng, tape=None):
     return b
 
 
+@pytest.mark.parametrize("shapes,iters,plus,expand_p,reduce_p", [
+    ([(3, 3, 3)], 4000, 300, 0.01, 0.0),
+    ([(2, 2, 2)], 2000, 50, 2.0, 0.0),
+    ([(2, 3, 4)], 2000, 300, 0.01, 20.0),
+    ([(4, 4, 4)], 2000, 800, 0.01, 0.0),
+    ([(3, 4, 5)], 1500, 600, 4.0, 0.0),
+    ([(2, 2, 2), (2, 2, 3), (2, 3, 4), (3, 3, 4), (3, 4, 5), (4, 4, 4)], 1500, 500, 0.01, 0.0),  # segments
+    ([(2, 4, 8)], 600, 200, 0.01, 0.0),   # nn = 8 x 32 x 16: 64-bit words
+    ([(4, 5, 8)], 300, 200, 0.01, 0.0),   # nn = 20 x 40 x 32, cap 160
+])
+def test_walk_fast_mode_vs_oracle(shapes, iters, plus, expand_p, reduce_p):
+    per = 40
+    S = per * len(shapes)
+    cap = max(a * b * c for a, b, c in shapes)
+    sh = np.array([shapes[w // per] for w in range(S)], np.int32)
+    seed = 9001 + len(shapes)
+    kw = dict(iterations=iters, plus_iterations=plus, expand_p=expand_p, reduce_p=reduce_p, seed=seed)
+    with fg.Engine(S, cap, "z2", "fast", seed, iters, plus, expand_p, reduce_p) as eng:
+        eng.init_naive_shapes(sh)
+        rec0 = eng.records()
+        st = eng.run(2)
+        rec = eng.records()
+        assert eng.validate().all() and eng.validate(best=True).all()
+    assert st["walks_valid"] == S and st["flips"] > 0
+    assert not rec.list_size.any()
+    b = run_oracle_like(rec0, kw, 2, "fast")
+    compare_records(rec, b, f"{shapes}")
+
+
 @pytest.mark.parametrize("shape,S,iters,plus,expand_p,reduce_p,launches", [
     ((3, 3, 3), 96, 3000, 400, 0.01, 0.0, 2),
     ((2, 2, 3), 64, 2000, 100, 5.0, 0.0, 1),
