@@ -1,0 +1,32 @@
+"""One batch of walks from the command line (profiling and quick checks).
+
+    python -m flipgraphgpu_gb300.run --shape 4x4x4 --walks 9728 --iterations 500 --mode fast
+
+Runs `--launches` walk launches on naive starting schemes and prints the
+library's statistics (accepted / verified flips, ranks, device times).
+"""
+import argparse
+import json
+
+from . import Engine
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--shape", default="3x3x3")
+    ap.add_argument("--walks", type=int, default=1024)
+    ap.add_argument("--iterations", type=int, default=1000)
+    ap.add_argument("--plus-iterations", type=int, default=100000)
+    ap.add_argument("--launches", type=int, default=1)
+    ap.add_argument("--mode", default="fast", choices=["fast", "philox", "reference"])
+    ap.add_argument("--seed", type=int, default=3)
+    a = ap.parse_args()
+    n = tuple(int(x) for x in a.shape.split("x"))
+    with Engine(a.walks, n[0] * n[1] * n[2], "z2", a.mode, a.seed, a.iterations, a.plus_iterations) as eng:
+        eng.init_naive(*n)
+        st = eng.run(a.launches)
+    print(json.dumps({"shape": a.shape, "walks": a.walks, "iterations": a.iterations, "mode": a.mode, **st}))
+
+
+if __name__ == "__main__":
+    main()
