@@ -109,6 +109,52 @@ __global__ void k_verify_z2(DevBatch B, int best, uint8_t *out) {
     }
 }
 
+// Exact integer Brent check (scheme_integer.cu:3-38), one warp per walk: every
+// (i, j, k) equation sum_t u_t[i] v_t[j] w_t[k] equals its 0/1 target, and no
+// coefficient carries the overflow flag.
+__global__ void k_verify_zt(DevBatch B, int best, uint8_t *out) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int wpb = blockDim.x >> 5, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int cap = B.cap;
+    uint64_t *xv = reinterpret_cast<uint64_t *>(smem) + (size_t)warp * 6 * cap;
+    uint64_t *xs = xv + 3 * cap;
+    for (int w = blockIdx.x * wpb + warp; w < B.S; w += gridDim.x * wpb) {
+        const WalkHeader h = B.hdr[w];
+        const size_t o = (size_t)w * 3 * cap;
+        const uint64_t *sv = best ? B.best_fac : B.fac, *ss = best ? B.best_sgn : B.sgn;
+        const uint8_t *sk = best ? B.best_valid : B.valid;
+        const int m = best ? h.best_m : h.m;
+        bool ok = m >= 0 && m <= cap;
+        for (int q = lane; q < 3 * cap; q += 32) {
+            xv[q] = sv[o + q];
+            xs[q] = ss[o + q];
+            if ((q % cap) < m && !sk[o + q]) ok = false;
+        }
+        __syncwarp();
+        const int n0 = h.n[0], n1 = h.n[1], n2 = h.n[2];
+        const int nn0 = n0 * n1, nn1 = n1 * n2, nn2 = n2 * n0;
+        for (int q = lane; ok && q < nn0 * nn1 * nn2; q += 32) {
+            const int i = q / (nn1 * nn2), j = (q / nn2) % nn1, k = q % nn2;
+            int e = 0;
+            for (int t = 0; t < m; t++) {
+                int cu = (int)((xv[t] >> i) & 1), cv = (int)((xv[cap + t] >> j) & 1), cw = (int)((xv[2 * cap + t] >> k) & 1);
+                if (cu & cv & cw) {
+                    int sg = (int)(((xs[t] >> i) ^ (xs[cap + t] >> j) ^ (xs[2 * cap + t] >> k)) & 1);
+                    e += sg ? -1 : 1;
+                }
+            }
+            const int target = (i % n1 == j / n2) && (i / n1 == k % n0) && (j % n2 == k / n0);
+            ok = e == target;
+        }
+        ok = __all_sync(kFull, ok);
+        if (lane == 0) {
+            out[w] = ok;
+            if (!best) B.hdr[w].valid = ok;
+        }
+        __syncwarp();
+    }
+}
+
 __global__ void k_tape(unsigned long long seed, int first, int count, int draws, uint32_t *d, float *u) {
     int w = blockIdx.x * blockDim.x + threadIdx.x;
     if (w >= count) return;
@@ -185,10 +231,15 @@ int verify_grid(fg_handle *h) { return (h->B.S + 3) / 4; }
 size_t verify_smem(fg_handle *h) { return (size_t)4 * 3 * h->B.cap * sizeof(uint64_t); }
 
 fg_status launch_verify(fg_handle *h, int best) {
-    if (h->cfg.ring != FG_RING_Z2) return fail(FG_ERR_ARG, "ring not supported");
-    size_t smem = verify_smem(h);
-    FG_CUDA(cudaFuncSetAttribute(k_verify_z2, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    k_verify_z2<<<verify_grid(h), 128, smem, h->stream>>>(h->B, best, h->d_valid);
+    if (h->cfg.ring == FG_RING_ZT) {
+        size_t smem = 2 * verify_smem(h);
+        FG_CUDA(cudaFuncSetAttribute(k_verify_zt, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        k_verify_zt<<<verify_grid(h), 128, smem, h->stream>>>(h->B, best, h->d_valid);
+    } else {
+        size_t smem = verify_smem(h);
+        FG_CUDA(cudaFuncSetAttribute(k_verify_z2, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        k_verify_z2<<<verify_grid(h), 128, smem, h->stream>>>(h->B, best, h->d_valid);
+    }
     FG_CUDA(cudaGetLastError());
     return FG_OK;
 }
@@ -237,8 +288,8 @@ fg_status refresh_plan(fg_handle *h) {
 // per segment on side streams, forked from and joined back into h->stream).
 fg_status launch_walks(fg_handle *h) {
     if (h->cfg.mode != FG_MODE_FAST) {
-        FG_CUDA(launch_walk_z2(h->B, h->P, h->cfg.mode == FG_MODE_REFERENCE ? RNG_XORWOW : RNG_PHILOX, h->wpb,
-                               h->grid, h->stream));
+        FG_CUDA(launch_walk(h->cfg.ring, h->B, h->P, h->cfg.mode == FG_MODE_REFERENCE ? RNG_XORWOW : RNG_PHILOX,
+                            h->wpb, h->grid, h->stream));
         return FG_OK;
     }
     const int wpb = h->cfg.walks_per_block > 0 ? h->cfg.walks_per_block : 2;
@@ -271,7 +322,9 @@ fg_status fg_create(const fg_config *cfg, fg_handle **out) {
     if (!cfg || !out) return fail(FG_ERR_ARG, "null argument");
     *out = nullptr;
     if (cfg->walks <= 0) return fail(FG_ERR_ARG, "walks must be positive");
-    if (cfg->ring != FG_RING_Z2) return fail(FG_ERR_ARG, "only the Z2 ring is available in this build");
+    if (cfg->ring != FG_RING_Z2 && cfg->ring != FG_RING_ZT) return fail(FG_ERR_ARG, "unknown ring");
+    if (cfg->ring == FG_RING_ZT && cfg->mode == FG_MODE_FAST)
+        return fail(FG_ERR_ARG, "the fast mode is available for the Z2 ring; use a list mode for ZT");
     if (cfg->mode != FG_MODE_REFERENCE && cfg->mode != FG_MODE_PHILOX_LISTS && cfg->mode != FG_MODE_FAST)
         return fail(FG_ERR_ARG, "unknown mode");
     if (cfg->cap <= 0 || slots_for_cap(cfg->cap) == 0 || cfg->cap > FG_MAX_RANK + 2)
@@ -320,7 +373,7 @@ fg_status fg_create(const fg_config *cfg, fg_handle **out) {
             return fail(FG_ERR_CUDA, "seeding failed");
         }
     }
-    int occ = occupancy_walk_z2(cap, cfg->mode == FG_MODE_REFERENCE ? RNG_XORWOW : RNG_PHILOX, h->wpb);
+    int occ = occupancy_walk(cfg->ring, cap, cfg->mode == FG_MODE_REFERENCE ? RNG_XORWOW : RNG_PHILOX, h->wpb);
     if (occ <= 0) occ = 1;
     int need = (S + h->wpb - 1) / h->wpb;
     h->grid = need < occ * h->sms ? need : occ * h->sms;
@@ -356,7 +409,7 @@ fg_status fg_init_naive(fg_handle *h, int n1, int n2, int n3) {
     FG_CUDA(cudaSetDevice(h->dev));
     k_init_naive<<<(h->B.S + 127) / 128, 128, 0, h->stream>>>(h->B, n1, n2, n3, nullptr, h->cfg.ring == FG_RING_ZT);
     FG_CUDA(cudaGetLastError());
-    if (h->cfg.mode != FG_MODE_FAST) FG_CUDA(launch_rebuild_z2(h->B, h->wpb, h->grid, h->stream));
+    if (h->cfg.mode != FG_MODE_FAST) FG_CUDA(launch_rebuild(h->cfg.ring, h->B, h->wpb, h->grid, h->stream));
     FG_CUDA(cudaStreamSynchronize(h->stream));
     fg_status st = refresh_plan(h);
     if (st) return st;
@@ -381,7 +434,7 @@ fg_status fg_init_naive_shapes(fg_handle *h, const int32_t *shapes) {
         k_init_naive<<<(S + 127) / 128, 128, 0, h->stream>>>(h->B, 0, 0, 0, d, h->cfg.ring == FG_RING_ZT);
         e = cudaGetLastError();
     }
-    if (e == cudaSuccess && h->cfg.mode != FG_MODE_FAST) e = launch_rebuild_z2(h->B, h->wpb, h->grid, h->stream);
+    if (e == cudaSuccess && h->cfg.mode != FG_MODE_FAST) e = launch_rebuild(h->cfg.ring, h->B, h->wpb, h->grid, h->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
     cudaFree(d);
     if (e != cudaSuccess) return fail(FG_ERR_CUDA, cudaGetErrorString(e));
@@ -536,8 +589,8 @@ fg_status fg_minimize(fg_handle *h, int32_t *best_complexity) {
     const int S = h->B.S;
     FG_CUDA(cudaMemcpyAsync(h->d_bestC, best_complexity, S * 4, cudaMemcpyHostToDevice, h->stream));
     if (h->cfg.mode == FG_MODE_FAST) return fail(FG_ERR_ARG, "the minimizer runs in a list mode");
-    FG_CUDA(launch_minimize_z2(h->B, h->P, h->cfg.mode == FG_MODE_REFERENCE ? RNG_XORWOW : RNG_PHILOX, h->wpb,
-                               h->grid, h->d_bestC, h->stream));
+    FG_CUDA(launch_minimize(h->cfg.ring, h->B, h->P, h->cfg.mode == FG_MODE_REFERENCE ? RNG_XORWOW : RNG_PHILOX,
+                            h->wpb, h->grid, h->d_bestC, h->stream));
     FG_CUDA(cudaMemcpyAsync(best_complexity, h->d_bestC, S * 4, cudaMemcpyDeviceToHost, h->stream));
     FG_CUDA(cudaStreamSynchronize(h->stream));
     return FG_OK;

@@ -1,11 +1,12 @@
-// Kernel templates: walk / minimize / init / verify, one warp per walk.
+// Kernel templates over both rings: walk / minimize / list rebuild, one warp per walk.
 #pragma once
 #include "fg_device.cuh"
 #include "walk_z2.cuh"
+#include "walk_zt.cuh"
 
 namespace fg {
 
-// Per-warp shared-memory footprint of a walk: factors [3][cap] + lists [3][500].
+// Per-warp shared-memory footprint of a Z2 walk: factors [3][cap] + lists [3][500].
 __host__ __device__ inline size_t walk_smem_bytes(int cap) {
     return (size_t)3 * cap * sizeof(uint64_t) + (size_t)3 * kListCap * sizeof(uint32_t);
 }
@@ -39,16 +40,83 @@ template <> struct DrawsIO<PhiloxDraws> {
     static __device__ void store(const DevBatch &, int, const PhiloxDraws &) {}
 };
 
-template <class R, int S>
-__device__ __forceinline__ void z2_load(Z2Walk<R, S> &z, const DevBatch &B, const WalkHeader &h, int w) {
-    const int cap = B.cap;
-    const uint64_t *src = B.fac + (size_t)w * 3 * cap;
-    for (int q = lane_id(); q < 3 * cap; q += 32) z.x[q] = src[q];
+// ---------------------------------------------------------------- per-ring I/O
+template <class Wk> struct RingIO;
+
+template <class R, int S> struct RingIO<Z2Walk<R, S>> {
+    using Walker = Z2Walk<R, S>;
+    static __host__ __device__ size_t smem(int cap) { return walk_smem_bytes(cap); }
+    static __device__ void bind(Walker &z, unsigned char *base, int cap) {
+        z.x = reinterpret_cast<uint64_t *>(base);
+        z.L = reinterpret_cast<uint32_t *>(z.x + 3 * cap);
+    }
+    static __device__ void load(Walker &z, const DevBatch &B, int w) {
+        const uint64_t *src = B.fac + (size_t)w * 3 * B.cap;
+        for (int q = lane_id(); q < 3 * B.cap; q += 32) z.x[q] = src[q];
+    }
+    static __device__ void store(Walker &z, const DevBatch &B, int w, bool best) {
+        uint64_t *dst = (best ? B.best_fac : B.fac) + (size_t)w * 3 * B.cap;
+        for (int q = lane_id(); q < 3 * B.cap; q += 32) dst[q] = (q % B.cap) < z.m ? z.x[q] : 0;
+    }
+    static __device__ int complexity(const Walker &z) {
+        int c = 0;
+        for (int t = lane_id(); t < z.m; t += 32) c += __popcll(z.X(0, t)) + __popcll(z.X(1, t)) + __popcll(z.X(2, t));
+#pragma unroll
+        for (int d = 16; d; d >>= 1) c += __shfl_xor_sync(kFull, c, d);
+        return c - 2 * z.m - z.nn2;
+    }
+};
+
+template <class R, int S> struct RingIO<ZTWalk<R, S>> {
+    using Walker = ZTWalk<R, S>;
+    static __host__ __device__ size_t smem(int cap) { return zt_smem_bytes(cap); }
+    static __device__ void bind(Walker &z, unsigned char *base, int cap) {
+        z.xv = reinterpret_cast<uint64_t *>(base);
+        z.xs = z.xv + 3 * cap;
+        z.xo = reinterpret_cast<uint8_t *>(z.xs + 3 * cap);
+        z.L = reinterpret_cast<uint32_t *>(z.xo + ((size_t)3 * cap + 7) / 8 * 8);
+        z.J = reinterpret_cast<uint16_t *>(z.L + 3 * kListCap);
+    }
+    static __device__ void load(Walker &z, const DevBatch &B, int w) {
+        const size_t o = (size_t)w * 3 * B.cap;
+        for (int q = lane_id(); q < 3 * B.cap; q += 32) {
+            z.xv[q] = B.fac[o + q];
+            z.xs[q] = B.sgn[o + q];
+            z.xo[q] = B.valid[o + q];
+        }
+    }
+    static __device__ void store(Walker &z, const DevBatch &B, int w, bool best) {
+        const size_t o = (size_t)w * 3 * B.cap;
+        uint64_t *dv = best ? B.best_fac : B.fac;
+        uint64_t *ds = best ? B.best_sgn : B.sgn;
+        uint8_t *dk = best ? B.best_valid : B.valid;
+        for (int q = lane_id(); q < 3 * B.cap; q += 32) {
+            bool in = (q % B.cap) < z.m;
+            dv[o + q] = in ? z.xv[q] : 0;
+            ds[o + q] = in ? z.xs[q] : 0;
+            dk[o + q] = in ? z.xo[q] : 0;
+        }
+    }
+    static __device__ int complexity(const Walker &z) {  // scheme_integer.cu:139-147
+        int c = 0;
+        for (int t = lane_id(); t < z.m; t += 32)
+            c += __popcll(z.xv[t]) + __popcll(z.xv[z.cap + t]) + __popcll(z.xv[2 * z.cap + t]);
+#pragma unroll
+        for (int d = 16; d; d >>= 1) c += __shfl_xor_sync(kFull, c, d);
+        return c - 2 * z.m - z.nn2;
+    }
+};
+
+template <class Walker>
+__device__ __forceinline__ void walk_bind(Walker &z, const DevBatch &B, const WalkHeader &h, int w,
+                                          unsigned char *base) {
+    RingIO<Walker>::bind(z, base, B.cap);
+    RingIO<Walker>::load(z, B, w);
     for (int c = 0; c < 3; c++) {
         const uint32_t *ls = B.lists + ((size_t)w * 3 + c) * kListCap;
         for (int q = lane_id(); q < h.list_size[c]; q += 32) z.L[c * kListCap + q] = ls[q];
     }
-    z.cap = cap;
+    z.cap = B.cap;
     z.n0 = h.n[0]; z.n1 = h.n[1]; z.n2 = h.n[2];
     z.nn0 = z.n0 * z.n1; z.nn1 = z.n1 * z.n2; z.nn2 = z.n2 * z.n0;
     z.full = z.n0 * z.n1 * z.n2;
@@ -58,13 +126,10 @@ __device__ __forceinline__ void z2_load(Z2Walk<R, S> &z, const DevBatch &B, cons
     __syncwarp();
 }
 
-// Writes factors (zero beyond m) and lists (zero beyond size) back to HBM.
-template <class R, int S>
-__device__ __forceinline__ void z2_store(Z2Walk<R, S> &z, const DevBatch &B, int w) {
-    const int cap = B.cap;
+template <class Walker>
+__device__ __forceinline__ void walk_store(Walker &z, const DevBatch &B, int w) {
     __syncwarp();
-    uint64_t *dst = B.fac + (size_t)w * 3 * cap;
-    for (int q = lane_id(); q < 3 * cap; q += 32) dst[q] = (q % cap) < z.m ? z.x[q] : 0;
+    RingIO<Walker>::store(z, B, w, false);
     for (int c = 0; c < 3; c++) {
         uint32_t *ls = B.lists + ((size_t)w * 3 + c) * kListCap;
         int s = z.sz(c);
@@ -72,22 +137,13 @@ __device__ __forceinline__ void z2_store(Z2Walk<R, S> &z, const DevBatch &B, int
     }
 }
 
-template <class R, int S>
-__device__ __forceinline__ void z2_copy_best(Z2Walk<R, S> &z, const DevBatch &B, int w) {
-    const int cap = B.cap;
-    uint64_t *dst = B.best_fac + (size_t)w * 3 * cap;
-    for (int q = lane_id(); q < 3 * cap; q += 32) dst[q] = (q % cap) < z.m ? z.x[q] : 0;
-}
-
 // randomWalkKernel (flip_graph.cu:520-573) for one walk, `iterations` steps.
-template <class R, int S>
-__device__ void z2_walk_one(const DevBatch &B, const WalkParams &P, int w, uint64_t *xs, uint32_t *Ls) {
+template <class Walker, class R>
+__device__ void walk_one(const DevBatch &B, const WalkParams &P, int w, unsigned char *base) {
     const WalkHeader h = B.hdr[w];
     R r = DrawsIO<R>::load(B, P, w, h);
-    Z2Walk<R, S> z(r);
-    z.x = xs;
-    z.L = Ls;
-    z2_load(z, B, h, w);
+    Walker z(r);
+    walk_bind(z, B, h, w, base);
     int flipsCount = h.flips, bestRank = h.best_rank, bestM = h.best_m;
     uint64_t accepted = 0;
     for (int it = 0; it < P.iterations; it++) {
@@ -103,7 +159,7 @@ __device__ void z2_walk_one(const DevBatch &B, const WalkParams &P, int w, uint6
         if (z.m < bestRank || (z.m == bestRank && r.tie())) {
             bestRank = z.m;
             bestM = z.m;
-            z2_copy_best(z, B, w);
+            RingIO<Walker>::store(z, B, w, true);
         }
         if (r.gate_reduce()) z.tryReduce();
         if (r.gate_expand() && z.m <= bestM + 2) {
@@ -114,7 +170,7 @@ __device__ void z2_walk_one(const DevBatch &B, const WalkParams &P, int w, uint6
         if (flipsCount >= P.plus_iterations && z.tryPlus()) flipsCount = 0;
         if (z.status) break;
     }
-    z2_store(z, B, w);
+    walk_store(z, B, w);
     DrawsIO<R>::store(B, w, r);
     if (lane_id() == 0) {
         WalkHeader o = h;
@@ -130,45 +186,28 @@ __device__ void z2_walk_one(const DevBatch &B, const WalkParams &P, int w, uint6
     }
 }
 
-// Warp sum of popcounts over the current scheme: complexity (scheme_z2.cu:127-139).
-template <class R, int S>
-__device__ __forceinline__ int z2_complexity(const Z2Walk<R, S> &z) {
-    int c = 0;
-#pragma unroll
-    for (int s = 0; s < S; s++) {
-        int t = 32 * s + lane_id();
-        if (t < z.m) c += __popcll(z.X(0, t)) + __popcll(z.X(1, t)) + __popcll(z.X(2, t));
-    }
-#pragma unroll
-    for (int d = 16; d; d >>= 1) c += __shfl_xor_sync(kFull, c, d);
-    return c - 2 * z.m - z.nn2;
-}
-
 // minimizeKernel (complexity_minimizer.cu:245-263) for one walk.
-template <class R, int S>
-__device__ void z2_minimize_one(const DevBatch &B, const WalkParams &P, int w, uint64_t *xs, uint32_t *Ls,
-                                int32_t *bestC) {
+template <class Walker, class R>
+__device__ void minimize_one(const DevBatch &B, const WalkParams &P, int w, unsigned char *base, int32_t *bestC) {
     const WalkHeader h = B.hdr[w];
     R r = DrawsIO<R>::load(B, P, w, h);
-    Z2Walk<R, S> z(r);
-    z.x = xs;
-    z.L = Ls;
-    z2_load(z, B, h, w);
+    Walker z(r);
+    walk_bind(z, B, h, w, base);
     int best = bestC[w];
     int bestM = h.best_m;
     uint64_t accepted = 0;
     for (int it = 0; it < P.iterations; it++) {
         if (!z.tryFlip(false)) break;
         accepted++;
-        int c = z2_complexity(z);
+        int c = RingIO<Walker>::complexity(z);
         if (c < best) {
             best = c;
             bestM = z.m;
-            z2_copy_best(z, B, w);
+            RingIO<Walker>::store(z, B, w, true);
         }
         if (z.status) break;
     }
-    z2_store(z, B, w);
+    walk_store(z, B, w);
     DrawsIO<R>::store(B, w, r);
     if (lane_id() == 0) {
         WalkHeader o = h;
@@ -183,45 +222,36 @@ __device__ void z2_minimize_one(const DevBatch &B, const WalkParams &P, int w, u
     }
 }
 
-template <class R, int S>
-__global__ void k_walk_z2(DevBatch B, WalkParams P) {
+template <class Walker, class R>
+__global__ void k_walk(DevBatch B, WalkParams P) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int wpb = blockDim.x >> 5, warp = threadIdx.x >> 5;
-    const size_t per = walk_smem_bytes(B.cap);
-    uint64_t *xs = reinterpret_cast<uint64_t *>(smem + per * warp);
-    uint32_t *Ls = reinterpret_cast<uint32_t *>(xs + 3 * B.cap);
-    for (int w = blockIdx.x * wpb + warp; w < B.S; w += gridDim.x * wpb) z2_walk_one<R, S>(B, P, w, xs, Ls);
+    unsigned char *base = smem + RingIO<Walker>::smem(B.cap) * warp;
+    for (int w = blockIdx.x * wpb + warp; w < B.S; w += gridDim.x * wpb) walk_one<Walker, R>(B, P, w, base);
 }
 
-template <class R, int S>
-__global__ void k_minimize_z2(DevBatch B, WalkParams P, int32_t *bestC) {
+template <class Walker, class R>
+__global__ void k_minimize(DevBatch B, WalkParams P, int32_t *bestC) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int wpb = blockDim.x >> 5, warp = threadIdx.x >> 5;
-    const size_t per = walk_smem_bytes(B.cap);
-    uint64_t *xs = reinterpret_cast<uint64_t *>(smem + per * warp);
-    uint32_t *Ls = reinterpret_cast<uint32_t *>(xs + 3 * B.cap);
-    for (int w = blockIdx.x * wpb + warp; w < B.S; w += gridDim.x * wpb) z2_minimize_one<R, S>(B, P, w, xs, Ls, bestC);
+    unsigned char *base = smem + RingIO<Walker>::smem(B.cap) * warp;
+    for (int w = blockIdx.x * wpb + warp; w < B.S; w += gridDim.x * wpb) minimize_one<Walker, R>(B, P, w, base, bestC);
 }
 
-// Rebuilds the lists of every walk from its factors (initFlips); used after
-// naive initialisation and after host-provided records without lists.
-template <int S>
-__global__ void k_rebuild_lists_z2(DevBatch B) {
+// Rebuilds every walk's lists from its factors (initFlips).
+template <class Walker>
+__global__ void k_rebuild(DevBatch B) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int wpb = blockDim.x >> 5, warp = threadIdx.x >> 5;
-    const size_t per = walk_smem_bytes(B.cap);
-    uint64_t *xs = reinterpret_cast<uint64_t *>(smem + per * warp);
-    uint32_t *Ls = reinterpret_cast<uint32_t *>(xs + 3 * B.cap);
+    unsigned char *base = smem + RingIO<Walker>::smem(B.cap) * warp;
     for (int w = blockIdx.x * wpb + warp; w < B.S; w += gridDim.x * wpb) {
         WalkHeader h = B.hdr[w];
         h.list_size[0] = h.list_size[1] = h.list_size[2] = 0;
         PhiloxDraws unused;
-        Z2Walk<PhiloxDraws, S> z(unused);
-        z.x = xs;
-        z.L = Ls;
-        z2_load(z, B, h, w);
+        Walker z(unused);
+        walk_bind(z, B, h, w, base);
         z.rebuild();
-        z2_store(z, B, w);
+        walk_store(z, B, w);
         if (lane_id() == 0) {
             B.hdr[w].list_size[0] = z.sz0;
             B.hdr[w].list_size[1] = z.sz1;

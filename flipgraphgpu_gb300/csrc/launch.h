@@ -11,12 +11,13 @@ enum { RNG_XORWOW = 0, RNG_PHILOX = 1 };
 // Smallest supported slots-per-lane S with 32*S >= cap (0 when cap is too large).
 int slots_for_cap(int cap);
 
-cudaError_t launch_walk_z2(const DevBatch &B, const WalkParams &P, int rng, int wpb, int grid, cudaStream_t s);
-cudaError_t launch_minimize_z2(const DevBatch &B, const WalkParams &P, int rng, int wpb, int grid, int32_t *bestC,
-                               cudaStream_t s);
-cudaError_t launch_rebuild_z2(const DevBatch &B, int wpb, int grid, cudaStream_t s);
-// Max resident blocks per SM of the Z2 walk kernel for this configuration.
-int occupancy_walk_z2(int cap, int rng, int wpb);
+// Warp-per-walk kernels (list modes); ring 0 = Z2, 1 = ZT.
+cudaError_t launch_walk(int ring, const DevBatch &B, const WalkParams &P, int rng, int wpb, int grid, cudaStream_t s);
+cudaError_t launch_minimize(int ring, const DevBatch &B, const WalkParams &P, int rng, int wpb, int grid,
+                            int32_t *bestC, cudaStream_t s);
+cudaError_t launch_rebuild(int ring, const DevBatch &B, int wpb, int grid, cudaStream_t s);
+// Max resident blocks per SM of the walk kernel for this configuration.
+int occupancy_walk(int ring, int cap, int rng, int wpb);
 
 // Fast mode: thread-per-walk kernel over walks [first, first + count), `scap`
 // factor slots per walk in shared memory; wide = 64-bit words (nn > 24).

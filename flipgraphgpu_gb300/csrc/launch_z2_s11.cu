@@ -1,4 +1,4 @@
-#include "launch_z2_impl.cuh"
+#include "launch_impl.cuh"
 namespace fg {
-FG_INSTANTIATE_Z2(11)
+FG_INSTANTIATE(0, 11)
 }

@@ -33,7 +33,7 @@ struct Z2Walk {
 
     // ------------------------------------------------------------ structure
     // initFlips (scheme_z2.cu:141-150): all equal pairs, lexicographic, capped.
-    __device__ void rebuild() {
+    __device__ __noinline__ void rebuild() {
         __syncwarp();
         for (int c = 0; c < 3; c++) {
             uint32_t *Lc = list(c);
@@ -65,7 +65,7 @@ struct Z2Walk {
     }
 
     // removeZeroes (scheme_z2.cu:152-164); the moved term is not re-checked.
-    __device__ void removeZeroes() {
+    __device__ __noinline__ void removeZeroes() {
         __syncwarp();
         int mm = m;
         if (lane_id() == 0) {
@@ -91,7 +91,7 @@ struct Z2Walk {
         __syncwarp();
     }
 
-    __device__ void reduce(int i, int a, int b) {  // scheme_z2.cu:631-641
+    __device__ __noinline__ void reduce(int i, int a, int b) {  // scheme_z2.cu:631-641
         uint64_t v = X(i, a) ^ X(i, b);
         __syncwarp();
         if (lane_id() == 0) setX(i, a, v);
@@ -149,7 +149,7 @@ struct Z2Walk {
     }
 
     // plus (scheme_z2.cu:579-612).
-    __device__ void plus(int i, int j, int k, int p, int q, int variant) {
+    __device__ __noinline__ void plus(int i, int j, int k, int p, int q, int variant) {
         const uint64_t a1 = X(i, p), b1 = X(j, p), c1 = X(k, p);
         const uint64_t a2 = X(i, q), b2 = X(j, q), c2 = X(k, q);
         const uint64_t a = a1 ^ a2, b = b1 ^ b2, c = c1 ^ c2;
@@ -169,7 +169,7 @@ struct Z2Walk {
         rebuild();
     }
 
-    __device__ void split(int i, int j, int k, int t, uint64_t a1) {  // scheme_z2.cu:614-619
+    __device__ __noinline__ void split(int i, int j, int k, int t, uint64_t a1) {  // scheme_z2.cu:614-619
         const uint64_t a2 = X(i, t) ^ a1, bj = X(j, t), bk = X(k, t);
         __syncwarp();
         if (lane_id() == 0) setX(i, t, a1);
@@ -203,7 +203,7 @@ struct Z2Walk {
         i = p0; j = p1; k = p2;
     }
 
-    __device__ bool tryPlus() {  // scheme_z2.cu:1029-1050
+    __device__ __noinline__ bool tryPlus() {  // scheme_z2.cu:1029-1050
         if (m >= kMaxRank || m >= full) return false;
         int a = (int)r.below((uint32_t)m), b = (int)r.below((uint32_t)m);
         int guard = 0;
@@ -219,7 +219,7 @@ struct Z2Walk {
         return true;
     }
 
-    __device__ bool trySplit() {  // scheme_z2.cu:1052-1078
+    __device__ __noinline__ bool trySplit() {  // scheme_z2.cu:1052-1078
         if (m >= kMaxRank || m >= full) return false;
         int t = (int)r.below((uint32_t)m);
         int i, j, k;
@@ -233,7 +233,7 @@ struct Z2Walk {
         return true;
     }
 
-    __device__ bool trySplitExisted() {  // scheme_z2.cu:1080-1104
+    __device__ __noinline__ bool trySplitExisted() {  // scheme_z2.cu:1080-1104
         if (m >= kMaxRank || m >= full) return false;
         int i, j, k;
         perm3(i, j, k);
@@ -258,7 +258,7 @@ struct Z2Walk {
 
     // tryReduce (scheme_z2.cu:1127-1154): first list-0 pair sharing a second
     // factor, else first list-1 pair sharing the third; ballots over list chunks.
-    __device__ bool tryReduce() {
+    __device__ __noinline__ bool tryReduce() {
         for (int base = 0; base < sz0; base += 32) {
             int p = base + lane_id();
             int hit = 0;

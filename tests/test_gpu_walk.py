@@ -17,14 +17,12 @@ pytestmark = pytest.mark.gpu
 fg = pytest.importorskip("flipgraphgpu_gb300")
 
 
-def z2_fixtures():
-    return [p for p in walk_fixtures() if "/walk_z2_" in p]
-
-
 def compare_records(rec, b, ctx=""):
     """Library records vs oracle batch: every field, exactly."""
-    for f in ("n", "m", "fac", "list_size", "list_pairs", "flips", "best_rank", "best_m", "best_fac",
-              "rng_pos", "status"):
+    fields = ["n", "m", "fac", "list_size", "list_pairs", "flips", "best_rank", "best_m", "best_fac", "rng_pos", "status"]
+    if rec.ring == "zt":
+        fields += ["sgn", "valid", "best_sgn", "best_valid"]
+    for f in fields:
         a, o = getattr(rec, f), getattr(b, f)
         if not np.array_equal(a, o):
             bad = np.argwhere(a != o)
@@ -49,30 +47,94 @@ def test_philox_device_matches_oracle():
         assert list(out[q]) == O.philox([int(x) for x in ctr[q]], list(key))
 
 
-@pytest.mark.parametrize("path", z2_fixtures(), ids=lambda p: p.split("/")[-1].split(".")[0])
+@pytest.mark.parametrize("path", walk_fixtures(), ids=lambda p: p.split("/")[-1].split(".")[0])
 def test_walk_matches_reference_kernel(path):
     """Same seed, same flags: the library reproduces the reference's per-launch state."""
     d = golden_io.read_walk(path)
+    ring = d["ring"]
     n1, n2, n3 = d["n"]
-    with fg.Engine(d["walks"], n1 * n2 * n3, "z2", "xorwow", d["seed"], d["iterations"], d["plus_iterations"],
+    with fg.Engine(d["walks"], n1 * n2 * n3, ring, "reference", d["seed"], d["iterations"], d["plus_iterations"],
                    d["expand_p"], d["reduce_p"]) as eng:
         eng.init_naive(n1, n2, n3)
         for L, block in enumerate(d["launches"]):
             eng.run(1)
             rec = eng.records()
             for w in range(d["walks"]):
-                errs = diff_walk(rec, w, block[w], "z2")
+                errs = diff_walk(rec, w, block[w], ring)
                 assert not errs, f"launch {L} walk {w}: {errs}"
         assert [int(x) for x in rec.rng_pos] == [t["used"] for t in d["tapes"]]
+        assert eng.validate().all()
+
+
+def batch_from(rec0):
+    """Oracle batch holding a copy of library records (including stream positions)."""
+    b = O.WalkBatch(rec0.walks, rec0.cap, rec0.ring)
+    fields = ["n", "m", "fac", "list_size", "list_pairs", "flips", "best_rank", "best_m", "best_fac", "rng_pos"]
+    if rec0.ring == "zt":
+        fields += ["sgn", "valid", "best_sgn", "best_valid"]
+    for f in fields:
+        getattr(b, f)[...] = getattr(rec0, f)
+    return b
 
 
 def run_oracle_like(rec0, cfg_kw, launches, rng, tape=None):
-    b = O.WalkBatch(rec0.walks, rec0.cap, "z2")
-    for f in ("n", "m", "fac", "list_size", "list_pairs", "flips", "best_rank", "best_m", "best_fac"):
-        getattr(b, f)[...] = getattr(rec0, f)
+    b = batch_from(rec0)
     cfg = b.cfg(rng, launches=launches, **cfg_kw)
     O.walk(b, cfg, tape)
     return b
+
+
+def xorwow_tape_for(rec, seed):
+    used = int(rec.rng_pos.max())
+    draws, unis = fg.xorwow_tape(seed, 0, rec.walks, used)
+    return O.make_tape([(draws[w, :rec.rng_pos[w]], unis[w, :rec.rng_pos[w]]) for w in range(rec.walks)])
+
+
+@pytest.mark.parametrize("shape,S,iters,plus,expand_p,reduce_p", [
+    ((3, 3, 3), 64, 400, 100, 0.01, 0.0),
+    ((2, 2, 3), 64, 600, 50, 10.0, 0.0),
+    ((2, 3, 3), 32, 600, 100, 0.01, 20.0),
+    ((4, 4, 4), 16, 150, 100, 0.01, 0.0),
+    ((2, 4, 5), 16, 300, 100, 2.0, 0.0),   # nn = 8 x 20 x 10: sign-extended random splits
+])
+def test_zt_walk_reference_stream_vs_oracle(shape, S, iters, plus, expand_p, reduce_p):
+    n1, n2, n3 = shape
+    cap = n1 * n2 * n3
+    seed = 500 + n1 * 100 + n2 * 10 + n3
+    kw = dict(iterations=iters, plus_iterations=plus, expand_p=expand_p, reduce_p=reduce_p)
+    with fg.Engine(S, cap, "zt", "reference", seed, iters, plus, expand_p, reduce_p) as eng:
+        eng.init_naive(n1, n2, n3)
+        rec0 = eng.records()
+        eng.run(2)
+        rec = eng.records()
+        assert eng.validate().all() and eng.validate(best=True).all()
+    b = run_oracle_like(rec0, kw, 2, "tape", xorwow_tape_for(rec, seed))
+    compare_records(rec, b, f"zt {shape}")
+
+
+@pytest.mark.parametrize("ring,shape", [("z2", (3, 3, 3)), ("z2", (4, 4, 4)), ("zt", (3, 3, 3)), ("zt", (2, 3, 4))])
+def test_minimize_vs_oracle(ring, shape):
+    """One walk launch to leave the naive scheme, then one minimizer launch (flips without reductions)."""
+    n1, n2, n3 = shape
+    S, cap, seed = 32, n1 * n2 * n3, 4242
+    with fg.Engine(S, cap, ring, "reference", seed, 300, 100000) as eng:
+        eng.init_naive(n1, n2, n3)
+        eng.run(1)
+        rec0 = eng.records()
+        best0 = O.complexity(ring, rec0.n, rec0.m, rec0.fac)
+        bc = eng.minimize(best0.copy())
+        rec = eng.records()
+        assert eng.validate().all() and eng.validate(best=True).all()
+    # Oracle: the same launch, replaying the stream from where the walk left it.
+    draws, unis = fg.xorwow_tape(seed, 0, S, int(rec.rng_pos.max()))
+    tape = O.make_tape([(draws[w, :rec.rng_pos[w]], unis[w, :rec.rng_pos[w]]) for w in range(S)])
+    b = batch_from(rec0)
+    obc = best0.copy()
+    O.minimize(b, b.cfg("tape", iterations=300, plus_iterations=100000), obc, tape)
+    assert np.array_equal(bc, obc)
+    assert (bc <= best0).all() and (bc < best0).any()
+    compare_records(rec, b, f"minimize {ring} {shape}")
+    assert np.array_equal(O.complexity(ring, rec.n, rec.best_m, rec.best_fac)[bc < best0], bc[bc < best0])
 
 
 @pytest.mark.parametrize("shapes,iters,plus,expand_p,reduce_p", [
