@@ -70,7 +70,8 @@ def library():
     lib.fg_version.restype = ctypes.c_char_p
     for name in ("fg_create", "fg_destroy", "fg_init_naive", "fg_set_records", "fg_get_records", "fg_run",
                  "fg_minimize", "fg_validate", "fg_xorwow_tape", "fg_philox_blocks", "fg_init_naive_shapes",
-                 "fg_get_counters", "fg_host_alloc", "fg_host_free"):
+                 "fg_get_counters", "fg_host_alloc", "fg_host_free", "fg_reducer_create", "fg_reducer_run",
+                 "fg_reducer_destroy"):
         getattr(lib, name).restype = ctypes.c_int
     _lib = lib
     return lib
@@ -233,6 +234,60 @@ class Engine:
         out = np.zeros(self.walks, np.uint8)
         _check(self.lib.fg_validate(self.h, int(best), _ptr(out)))
         return out.astype(bool)
+
+
+class ReducerConfig(ctypes.Structure):
+    _fields_ = [("count", ctypes.c_int32), ("schemes", ctypes.c_int32), ("seed", ctypes.c_uint64),
+                ("device", ctypes.c_int32)]
+
+
+MODE_NAMES = {0: "g", 1: "ga", 2: "gr", 3: "gi", 4: "wr", 5: "mix", 6: "rnd"}
+
+
+def mode_name(mode, scale):
+    """AdditionsReducer::getMode (additions_reducer.cuh:183-204)."""
+    name = MODE_NAMES[int(mode)]
+    if name in ("gr", "gi"):
+        name += str(int(np.float32(scale) * np.float32(100)))
+    return name
+
+
+class Reducer:
+    """Additions reducers on the GPU: `count` reducers over `schemes` schemes.
+
+    coef: int8 [schemes][3][m][64] coefficients (U rows, V rows, W rows)."""
+
+    def __init__(self, n, m, coef, count=32, schemes=1, seed=1, device=0):
+        self.lib = library()
+        self.count, self.m, self.n = count, m, tuple(n)
+        self.coef = np.ascontiguousarray(coef, np.int8).reshape(schemes, 3, m, 64)
+        self.cfg = ReducerConfig(count, schemes, seed, device)
+        self.h = ctypes.c_void_p()
+        _check(self.lib.fg_reducer_create(ctypes.byref(self.cfg), n[0], n[1], n[2], m, _ptr(self.coef),
+                                          ctypes.byref(self.h)))
+
+    def run(self, independent=True, best_fresh=None, best_vars=None):
+        counts = np.zeros((self.count, 13), np.int32)
+        scale = np.zeros((self.count, 3), np.float32)
+        vars_ = np.zeros((self.count, 3, 500, 2), np.int32)
+        bf = np.ascontiguousarray(best_fresh if best_fresh is not None else np.zeros(3), np.int32)
+        bv = np.ascontiguousarray(best_vars if best_vars is not None else np.zeros((3, 500, 2)), np.int32)
+        _check(self.lib.fg_reducer_run(self.h, int(independent), _ptr(bf), _ptr(bv), _ptr(counts), _ptr(scale),
+                                       _ptr(vars_)))
+        per = counts[:, :12].reshape(self.count, 3, 4)
+        return {"additions": per[:, :, 0].copy(), "fresh": per[:, :, 1].copy(), "naive": per[:, :, 2].copy(),
+                "mode": per[:, :, 3].copy(), "draws": counts[:, 12].copy(), "scale": scale, "vars": vars_}
+
+    def close(self):
+        if self.h:
+            self.lib.fg_reducer_destroy(self.h)
+            self.h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def xorwow_tape(seed, first_walk, count, draws, device=0):

@@ -11,12 +11,17 @@
 
 using namespace fg;
 
+namespace fg {
+std::string &last_error() {
+    thread_local std::string err;
+    return err;
+}
+}  // namespace fg
+
 namespace {
 
-thread_local std::string g_err;
-
 fg_status fail(fg_status st, const std::string &msg) {
-    g_err = msg;
+    fg::last_error() = msg;
     return st;
 }
 
@@ -315,7 +320,7 @@ fg_status launch_walks(fg_handle *h) {
 
 extern "C" {
 
-const char *fg_last_error(void) { return g_err.c_str(); }
+const char *fg_last_error(void) { return fg::last_error().c_str(); }
 const char *fg_version(void) { return "flipgraph-gb300 0.1 (sm_103a)"; }
 
 fg_status fg_create(const fg_config *cfg, fg_handle **out) {

@@ -1,12 +1,16 @@
 // Internal launch interface between the C-ABI (capi.cu) and the kernel
 // translation units.  Not part of the public ABI.
 #pragma once
+#include <string>
 #include <cuda_runtime.h>
 #include "fg_device.cuh"
 
 namespace fg {
 
 enum { RNG_XORWOW = 0, RNG_PHILOX = 1 };
+
+// Message of the last failing C-ABI call on this thread (fg_last_error).
+std::string &last_error();
 
 // Smallest supported slots-per-lane S with 32*S >= cap (0 when cap is too large).
 int slots_for_cap(int cap);

@@ -1,0 +1,540 @@
+// Additions reducer: greedy / randomised common-subexpression elimination
+// over the U rows, V rows and W columns of a scheme, one thread block per
+// reducer.  Restates runReducersKernel (scheme_additions_reducer.cu:494-540),
+// AdditionsReducer (additions_reducer.cuh) and PairsCounter (pairs_counter.cuh).
+//
+// The hot part, the pair-frequency count, is block parallel: every signed pair
+// occurrence (expression e, positions i < j) gets its sequence number in the
+// reference's insertion order; occurrences are counted in a shared-memory hash
+// (atomicCAS / atomicAdd / atomicMin of the first occurrence), and the distinct
+// pairs are then laid out by first occurrence, which is exactly the order the
+// reference's PairsCounter stores them in.  The reference's partial sort
+// (pairs_counter.cuh:73-101), the selection modes and every draw run on one
+// thread, so the XORWOW stream is consumed exactly as the reference does.
+#include <cstdint>
+#include <vector>
+
+#include <string>
+
+#include "../../include/flipgraph.h"
+#include "fg_device.cuh"
+#include "launch.h"
+
+namespace fg {
+
+namespace {
+
+enum { GREEDY = 0, GREEDY_ALT = 1, GREEDY_RANDOM = 2, GREEDY_INTER = 3, WEIGHTED_RANDOM = 4, MIX = 5, RANDOM = 6 };
+
+__constant__ int c_modes[15] = {GREEDY_INTER, GREEDY_INTER, GREEDY_INTER, GREEDY_INTER, GREEDY_INTER,
+                                GREEDY_INTER, GREEDY_INTER, GREEDY_INTER, GREEDY_ALT,   GREEDY_ALT,
+                                GREEDY_ALT,   GREEDY_ALT,   GREEDY_RANDOM, GREEDY_RANDOM, MIX};
+
+// Fresh-variable caps (config.cuh:29-31) and PairsCounter capacities (config.cuh:25-27).
+__device__ __forceinline__ int max_fresh(int c) { return c == 2 ? 500 : 250; }
+__device__ __forceinline__ int max_pairs(int c) { return c == 2 ? 61075 : 2016; }
+
+struct ReduceDims {
+    int E[3];      // expressions per component: m, m, nn2
+    int L[3];      // initial max length (real variables): nn0, nn1, m
+    int nocc;      // max pair occurrences over components (initial)
+    int tbits;     // hash table size = 1 << tbits
+};
+
+// Shared-memory carve-up for one block.
+struct RedSmem {
+    int16_t *ex;      // [E][L] expression entries (signed variable ids)
+    int16_t *es;      // [E] sizes
+    int *off;         // [E+1] occurrence offsets
+    uint32_t *hkey;   // [T]
+    int *hcnt;        // [T]
+    int *hfirst;      // [T]
+    int *byfirst;     // [nocc] slot of the pair first seen at occurrence q, or -1
+    int *pi, *pj, *pc;// [nocc] distinct pairs (insertion order, then sorted)
+    int16_t *vars;    // [500][2] fresh variables of the component being reduced
+};
+
+__device__ __forceinline__ uint32_t pair_key(int i, int j) {  // canonizePair (pairs_counter.cuh:214-225)
+    if (abs(i) > abs(j)) { int t = i; i = j; j = t; }
+    if (i < 0) { i = -i; j = -j; }
+    return ((uint32_t)i << 16) | ((uint32_t)j & 0xFFFFu);
+}
+
+__device__ __forceinline__ int key_i(uint32_t k) { return (int)(k >> 16); }
+__device__ __forceinline__ int key_j(uint32_t k) { return (int)(int16_t)(k & 0xFFFFu); }
+
+__device__ __forceinline__ uint32_t hash_slot(uint32_t key, int tbits) { return (key * 2654435761u) >> (32 - tbits); }
+
+__device__ int block_sum(int v, int *scratch) {
+    for (int d = 16; d; d >>= 1) v += __shfl_xor_sync(kFull, v, d);
+    const int warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    __syncthreads();
+    if (lane_id() == 0) scratch[warp] = v;
+    __syncthreads();
+    int t = 0;
+    for (int q = 0; q < nw; q++) t += scratch[q];
+    __syncthreads();
+    return t;
+}
+
+// Serial-thread state of one component's AdditionsReducer.
+struct RedState {
+    int E, real, fresh, naive, mode, maxFresh, maxPairs;
+    float scale;
+};
+
+// binarySearch (additions_reducer.cuh:247-269) by absolute value.
+__device__ __forceinline__ int bsearch_abs(const int16_t *e, int size, int value, int start) {
+    int lo = start, hi = size - 1, va = abs(value);
+    while (lo <= hi) {
+        int mid = lo + (hi - lo) / 2;
+        int ma = abs((int)e[mid]);
+        if (ma < va) lo = mid + 1;
+        else if (ma > va) hi = mid - 1;
+        else return mid;
+    }
+    return -1;
+}
+
+// replaceSubexpression (additions_reducer.cuh:218-245), expressions in parallel.
+__device__ void replace_pair(RedSmem &sm, RedState &st, int L, int pi, int pj) {
+    const int var = st.real + st.fresh + 1;
+    for (int e = threadIdx.x; e < st.E; e += blockDim.x) {
+        int16_t *x = sm.ex + (size_t)e * L;
+        int size = sm.es[e];
+        if (size < 2) continue;
+        int i = bsearch_abs(x, size, pi, 0);
+        if (i == -1) continue;
+        int j = bsearch_abs(x, size, pj, i + 1);
+        if (j == -1) continue;
+        int v;
+        if (x[i] == pi && x[j] == pj) v = var;
+        else if (x[i] == -pi && x[j] == -pj) v = -var;
+        else continue;
+        int w = i;
+        for (int q = i + 1; q < size; q++)
+            if (q != j) x[w++] = x[q];
+        x[w] = (int16_t)v;
+        sm.es[e] = (int16_t)(size - 1);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        sm.vars[2 * st.fresh] = (int16_t)pi;
+        sm.vars[2 * st.fresh + 1] = (int16_t)pj;
+    }
+    st.fresh++;
+    __syncthreads();
+}
+
+__device__ __forceinline__ bool intersects(int ai, int aj, int bi, int bj) {
+    return ai == bi || ai == abs(bj) || abs(aj) == bi || abs(aj) == abs(bj);
+}
+
+// updateSubexpressions + sort (additions_reducer.cuh:207-216, pairs_counter.cuh:61-101).
+// Leaves the sorted pairs in sm.pi/pj/pc [0, *size), returns maxCount; *top = topSize.
+__device__ int count_pairs(RedSmem &sm, RedState &st, const ReduceDims &D, int L, int *size_out, int *top_out,
+                           int *scratch) {
+    const int T = 1 << D.tbits;
+    // occurrence offsets (sequential prefix over expressions by thread 0)
+    if (threadIdx.x == 0) {
+        int acc = 0;
+        for (int e = 0; e < st.E; e++) {
+            sm.off[e] = acc;
+            int s = sm.es[e];
+            acc += s * (s - 1) / 2;
+        }
+        sm.off[st.E] = acc;
+    }
+    for (int q = threadIdx.x; q < T; q += blockDim.x) { sm.hkey[q] = 0xFFFFFFFFu; sm.hcnt[q] = 0; sm.hfirst[q] = 0x7FFFFFFF; }
+    __syncthreads();
+    const int N = sm.off[st.E];
+    for (int q = threadIdx.x; q < N; q += blockDim.x) sm.byfirst[q] = -1;
+    for (int q = threadIdx.x; q < N; q += blockDim.x) {
+        int lo = 0, hi = st.E - 1;  // last e with off[e] <= q
+        while (lo < hi) {
+            int mid = (lo + hi + 1) >> 1;
+            if (sm.off[mid] <= q) lo = mid; else hi = mid - 1;
+        }
+        const int e = lo, s = sm.es[e];
+        int r = q - sm.off[e], i = 0;
+        while (r >= s - 1 - i) { r -= s - 1 - i; i++; }
+        const int j = i + 1 + r;
+        const int16_t *x = sm.ex + (size_t)e * L;
+        const uint32_t key = pair_key(x[i], x[j]);
+        uint32_t h = hash_slot(key, D.tbits);
+        for (;;) {
+            uint32_t prev = atomicCAS(&sm.hkey[h], 0xFFFFFFFFu, key);
+            if (prev == 0xFFFFFFFFu || prev == key) break;
+            h = (h + 1) & (T - 1);
+        }
+        atomicAdd(&sm.hcnt[h], 1);
+        atomicMin(&sm.hfirst[h], q);
+    }
+    __syncthreads();
+    for (int q = threadIdx.x; q < T; q += blockDim.x)
+        if (sm.hkey[q] != 0xFFFFFFFFu) sm.byfirst[sm.hfirst[q]] = q;
+    __syncthreads();
+    // Distinct pairs in first-occurrence order (= PairsCounter insertion order), capped.
+    if (threadIdx.x == 0) {
+        int d = 0, maxCount = 0;
+        for (int q = 0; q < N; q++) {
+            int slot = sm.byfirst[q];
+            if (slot < 0) continue;
+            if (d >= st.maxPairs) break;
+            uint32_t k = sm.hkey[slot];
+            sm.pi[d] = key_i(k);
+            sm.pj[d] = key_j(k);
+            sm.pc[d] = sm.hcnt[slot];
+            if (sm.pc[d] > maxCount) maxCount = sm.pc[d];
+            d++;
+        }
+        // sort(): move max-count pairs to the front by swapping, then drop count-1 pairs.
+        int top = 0, size = d;
+        if (maxCount >= 2) {
+            for (int i = 0; i < size; i++) {
+                if (sm.pc[i] != maxCount) continue;
+                if (i != top) {
+                    int a = sm.pi[i], b = sm.pj[i], c = sm.pc[i];
+                    sm.pi[i] = sm.pi[top]; sm.pj[i] = sm.pj[top]; sm.pc[i] = sm.pc[top];
+                    sm.pi[top] = a; sm.pj[top] = b; sm.pc[top] = c;
+                }
+                top++;
+            }
+            int j = top;
+            for (int i = top; i < size; i++)
+                if (sm.pc[i] > 1) { sm.pi[j] = sm.pi[i]; sm.pj[j] = sm.pj[i]; sm.pc[j] = sm.pc[i]; j++; }
+            size = j;
+        } else {
+            top = size;
+        }
+        scratch[32] = size;
+        scratch[33] = top;
+        scratch[34] = maxCount;
+    }
+    __syncthreads();
+    *size_out = scratch[32];
+    *top_out = scratch[33];
+    int mc = scratch[34];
+    __syncthreads();
+    return mc;
+}
+
+// selectSubexpression (additions_reducer.cuh:272-289) on thread 0; returns the pair index.
+__device__ int select_pair(const RedSmem &sm, const RedState &st, int md, int size, int top, XorwowDraws &r) {
+    if (md == GREEDY) return 0;
+    if (md == GREEDY_ALT) return (int)(r.raw() % (uint32_t)top);
+    if (md == GREEDY_RANDOM) {
+        if (r.uniform() < st.scale) return (int)(r.raw() % (uint32_t)size);
+        return (int)(r.raw() % (uint32_t)top);
+    }
+    if (md == GREEDY_INTER) {  // pairs_counter.cuh:148-176
+        int imax = 0;
+        float maxScore = 0;
+        for (int i = 0; i < size; i++) {
+            float inter = 0;
+            for (int j = 0; j < size; j++) {
+                if (i == j) continue;
+                if (!intersects(sm.pi[i], sm.pj[i], sm.pi[j], sm.pj[j])) {
+                    inter += (float)(sm.pc[j] - 1);
+                } else if (!(r.raw() % 2)) {
+                    inter = (float)__fma_rn(0.69, (double)sm.pc[j], (double)inter);
+                }
+            }
+            float score = __fmaf_rn(st.scale, inter, (float)(sm.pc[i] - 1));
+            if (score > maxScore) { maxScore = score; imax = i; }
+        }
+        return imax;
+    }
+    if (md == WEIGHTED_RANDOM) {  // pairs_counter.cuh:178-196
+        float total = 0;
+        for (int i = 0; i < size; i++) total += (float)sm.pc[i];
+        float x = r.uniform() * total;
+        float sum = 0;
+        for (int i = 0; i < size; i++) {
+            sum += (float)sm.pc[i];
+            if (x <= sum) return i;
+        }
+        return size - 1;
+    }
+    return (int)(r.raw() % (uint32_t)size);
+}
+
+struct ReduceArgs {
+    int count, schemes, n1, n2, n3, m;
+    const int8_t *coef;              // [schemes][3][m][64]
+    curandStateXORWOW_t *states;     // [count]
+    int independent;
+    int best_fresh[3];
+    const int16_t *best_vars;        // [3][500][2]
+    int32_t *out;                    // [count][13]: per component additions, fresh, naive, mode; draws
+    float *out_scale;                // [count][3]
+    int16_t *out_vars;               // [count][3][500][2] or null
+    ReduceDims D;
+};
+
+__global__ void k_reduce(ReduceArgs A) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ int scratch[40];
+    const int idx = blockIdx.x;
+    if (idx >= A.count) return;
+    const ReduceDims &D = A.D;
+    const int Lmax = max(D.L[0], max(D.L[1], D.L[2]));
+    const int Emax = max(D.E[0], max(D.E[1], D.E[2]));
+    const int T = 1 << D.tbits;
+    RedSmem sm;
+    unsigned char *p = smem;
+    sm.hkey = reinterpret_cast<uint32_t *>(p); p += 4 * (size_t)T;
+    sm.hcnt = reinterpret_cast<int *>(p); p += 4 * (size_t)T;
+    sm.hfirst = reinterpret_cast<int *>(p); p += 4 * (size_t)T;
+    sm.byfirst = reinterpret_cast<int *>(p); p += 4 * (size_t)D.nocc;
+    sm.pi = reinterpret_cast<int *>(p); p += 4 * (size_t)D.nocc;
+    sm.pj = reinterpret_cast<int *>(p); p += 4 * (size_t)D.nocc;
+    sm.pc = reinterpret_cast<int *>(p); p += 4 * (size_t)D.nocc;
+    sm.off = reinterpret_cast<int *>(p); p += 4 * (size_t)(Emax + 1);
+    sm.vars = reinterpret_cast<int16_t *>(p); p += 2 * 2 * 500;
+    sm.es = reinterpret_cast<int16_t *>(p); p += 2 * (size_t)((Emax + 1) & ~1);
+    sm.ex = reinterpret_cast<int16_t *>(p);
+
+    XorwowDraws r;
+    r.st = A.states[idx];
+    r.count = 0;
+    r.P = nullptr;
+    const int8_t *coef = A.coef + (size_t)(idx % A.schemes) * 3 * A.m * 64;
+    const int nn[3] = {A.n1 * A.n2, A.n2 * A.n3, A.n3 * A.n1};
+
+    // Modes (scheme_additions_reducer.cu:600-602): reducer 0 is plain greedy, no draws.
+    int modes[3];
+    float scales[3];
+    for (int c = 0; c < 3; c++) modes[c] = idx == 0 ? GREEDY : c_modes[r.raw() % 15];
+    // Partial initialisation draws (scheme_additions_reducer.cu:604-623).
+    int partial[3] = {0, 0, 0};
+    if (A.independent) {
+        for (int c = 0; c < 3; c++)
+            if ((double)r.uniform() < 0.3 && A.best_fresh[c] > 0) partial[c] = 1 + (int)(r.raw() % (uint32_t)A.best_fresh[c]);
+    } else if ((double)r.uniform() < 0.3) {
+        for (int c = 0; c < 3; c++)
+            if (A.best_fresh[c] > 0) partial[c] = 1 + (int)(r.raw() % (uint32_t)A.best_fresh[c]);
+    }
+    for (int c = 0; c < 3; c++) {
+        // copySchemeToReducers (scheme_additions_reducer.cu:463-492): naive expressions.
+        RedState st;
+        st.E = D.E[c];
+        st.real = c < 2 ? nn[c] : A.m;
+        st.fresh = 0;
+        st.mode = modes[c];
+        st.maxFresh = max_fresh(c);
+        st.maxPairs = max_pairs(c);
+        const int L = Lmax;
+        for (int e = threadIdx.x; e < st.E; e += blockDim.x) {
+            int16_t *x = sm.ex + (size_t)e * L;
+            int size = 0;
+            if (c < 2) {
+                for (int q = 0; q < nn[c]; q++) {
+                    int v = coef[((size_t)c * A.m + e) * 64 + q];
+                    if (v) x[size++] = (int16_t)(v > 0 ? q + 1 : -(q + 1));
+                }
+            } else {
+                for (int t = 0; t < A.m; t++) {
+                    int v = coef[((size_t)2 * A.m + t) * 64 + e];
+                    if (v) x[size++] = (int16_t)(v > 0 ? t + 1 : -(t + 1));
+                }
+            }
+            sm.es[e] = (int16_t)size;
+        }
+        __syncthreads();
+        int naiveLocal = 0;
+        for (int e = threadIdx.x; e < st.E; e += blockDim.x) naiveLocal += sm.es[e] - 1;
+        st.naive = block_sum(naiveLocal, scratch);
+        // partialInitialize (additions_reducer.cuh:129-136) from the incumbent's variables.
+        for (int q = 0; q < partial[c] && q < A.best_fresh[c]; q++) {
+            const int16_t *bv = A.best_vars + ((size_t)c * 500 + q) * 2;
+            replace_pair(sm, st, L, bv[0], bv[1]);
+        }
+        // reduce (additions_reducer.cuh:89-103).
+        st.scale = -1;
+        if (threadIdx.x == 0) st.scale = r.uniform() / 2;
+        while (st.fresh < st.maxFresh) {
+            int size, top;
+            int maxCount = count_pairs(sm, st, D, L, &size, &top, scratch);
+            if (!(size > 0 && maxCount > 1)) break;
+            if (threadIdx.x == 0) {
+                int md = st.mode == MIX ? (int)(r.raw() % MIX) : st.mode;
+                int k = select_pair(sm, st, md, size, top, r);
+                scratch[35] = sm.pi[k];
+                scratch[36] = sm.pj[k];
+            }
+            __syncthreads();
+            int pi = scratch[35], pj = scratch[36];
+            __syncthreads();
+            replace_pair(sm, st, L, pi, pj);
+        }
+        int addLocal = 0;
+        for (int e = threadIdx.x; e < st.E; e += blockDim.x) addLocal += sm.es[e] - 1;
+        int adds = block_sum(addLocal, scratch) + st.fresh;
+        if (threadIdx.x == 0) {
+            A.out[idx * 13 + c * 4 + 0] = adds;
+            A.out[idx * 13 + c * 4 + 1] = st.fresh;
+            A.out[idx * 13 + c * 4 + 2] = st.naive;
+            A.out[idx * 13 + c * 4 + 3] = st.mode;
+            scales[c] = st.scale;
+            A.out_scale[idx * 3 + c] = st.scale;
+        }
+        if (A.out_vars)
+            for (int q = threadIdx.x; q < 2 * st.fresh; q += blockDim.x)
+                A.out_vars[((size_t)idx * 3 + c) * 1000 + q] = sm.vars[q];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        A.states[idx] = r.st;
+        A.out[idx * 13 + 12] = (int32_t)r.count;
+    }
+    (void)scales;
+}
+
+__global__ void k_seed_reducers(curandStateXORWOW_t *st, int count, unsigned long long seed) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < count) curand_init(seed, (unsigned long long)i, 0ull, &st[i]);  // scheme_additions_reducer.cu:445
+}
+
+}  // namespace
+}  // namespace fg
+
+using namespace fg;
+
+struct fg_reducer {
+    fg_reducer_config cfg;
+    int n1, n2, n3, m;
+    ReduceDims D;
+    int8_t *d_coef = nullptr;
+    curandStateXORWOW_t *d_states = nullptr;
+    int16_t *d_best = nullptr;
+    int32_t *d_out = nullptr;
+    float *d_scale = nullptr;
+    int16_t *d_vars = nullptr;
+    size_t smem = 0;
+};
+
+namespace {
+fg_status rfail(fg_status s, const char *msg) {
+    fg::last_error() = msg;
+    return s;
+}
+#define RCUDA(call)                                                             \
+    do {                                                                        \
+        cudaError_t e_ = (call);                                                \
+        if (e_ != cudaSuccess) return rfail(FG_ERR_CUDA, cudaGetErrorString(e_)); \
+    } while (0)
+}  // namespace
+
+extern "C" {
+
+fg_status fg_reducer_create(const fg_reducer_config *cfg, int n1, int n2, int n3, int m, const int8_t *coef,
+                            fg_reducer **out) {
+    if (!cfg || !coef || !out) return rfail(FG_ERR_ARG, "null argument");
+    *out = nullptr;
+    if (cfg->count <= 0 || cfg->schemes <= 0) return rfail(FG_ERR_ARG, "count and schemes must be positive");
+    if (n1 <= 0 || n2 <= 0 || n3 <= 0 || n1 * n2 > 64 || n2 * n3 > 64 || n3 * n1 > 64 || m <= 0 || m > FG_MAX_RANK)
+        return rfail(FG_ERR_ARG, "scheme sizes out of range");
+    // Capacities of the reference's compiled configuration (config.cuh:16-27).
+    if (n3 * n1 > 64) return rfail(FG_ERR_CAPACITY, "too many W expressions");
+    fg_reducer *h = new fg_reducer;
+    h->cfg = *cfg;
+    h->n1 = n1; h->n2 = n2; h->n3 = n3; h->m = m;
+    const int nn[3] = {n1 * n2, n2 * n3, n3 * n1};
+    ReduceDims &D = h->D;
+    D.E[0] = m; D.E[1] = m; D.E[2] = nn[2];
+    D.L[0] = nn[0]; D.L[1] = nn[1]; D.L[2] = m;
+    // Largest initial pair-occurrence count over schemes and components.
+    long nocc = 1;
+    for (int s = 0; s < cfg->schemes; s++) {
+        const int8_t *cf = coef + (size_t)s * 3 * m * 64;
+        for (int c = 0; c < 3; c++) {
+            long tot = 0;
+            for (int e = 0; e < D.E[c]; e++) {
+                int size = 0;
+                if (c < 2) { for (int q = 0; q < nn[c]; q++) size += cf[((size_t)c * m + e) * 64 + q] != 0; }
+                else { for (int t = 0; t < m; t++) size += cf[((size_t)2 * m + t) * 64 + e] != 0; }
+                tot += (long)size * (size - 1) / 2;
+            }
+            if (tot > nocc) nocc = tot;
+        }
+    }
+    D.nocc = (int)nocc;
+    D.tbits = 4;
+    while ((1L << D.tbits) < 2 * nocc) D.tbits++;
+    const int T = 1 << D.tbits;
+    const int Lmax = nn[0] > nn[1] ? (nn[0] > m ? nn[0] : m) : (nn[1] > m ? nn[1] : m);
+    const int Emax = m > nn[2] ? m : nn[2];
+    h->smem = (size_t)12 * T + (size_t)16 * D.nocc + 4 * (size_t)(Emax + 1) + 2000 + 2 * (size_t)((Emax + 1 + 1) & ~1) +
+              2 * (size_t)Emax * Lmax + 64;
+    int dev = cfg->device, optin = 0;
+    if (cudaSetDevice(dev) != cudaSuccess) { delete h; return rfail(FG_ERR_CUDA, "cudaSetDevice failed"); }
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    if (h->smem > (size_t)optin) { delete h; return rfail(FG_ERR_CAPACITY, "scheme too large for the shared-memory reducer"); }
+    size_t ncoef = (size_t)cfg->schemes * 3 * m * 64;
+    cudaError_t e = cudaMalloc(&h->d_coef, ncoef);
+    if (e == cudaSuccess) e = cudaMemcpy(h->d_coef, coef, ncoef, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMalloc(&h->d_states, sizeof(curandStateXORWOW_t) * cfg->count);
+    if (e == cudaSuccess) e = cudaMalloc(&h->d_best, 2 * 3 * 500 * 2);
+    if (e == cudaSuccess) e = cudaMalloc(&h->d_out, 4 * 13 * (size_t)cfg->count);
+    if (e == cudaSuccess) e = cudaMalloc(&h->d_scale, 4 * 3 * (size_t)cfg->count);
+    if (e == cudaSuccess) e = cudaMalloc(&h->d_vars, 2 * (size_t)cfg->count * 3 * 1000);
+    if (e == cudaSuccess) {
+        k_seed_reducers<<<(cfg->count + 127) / 128, 128>>>(h->d_states, cfg->count, (unsigned long long)cfg->seed);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_reduce, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)h->smem);
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) {
+        fg_reducer_destroy(h);
+        return rfail(FG_ERR_CUDA, cudaGetErrorString(e));
+    }
+    *out = h;
+    return FG_OK;
+}
+
+fg_status fg_reducer_run(fg_reducer *h, int independent, const int32_t *best_fresh, const int32_t *best_vars,
+                         int32_t *out_counts, float *out_scale, int32_t *out_vars) {
+    if (!h || !out_counts) return rfail(FG_ERR_ARG, "null argument");
+    RCUDA(cudaSetDevice(h->cfg.device));
+    ReduceArgs A;
+    A.count = h->cfg.count;
+    A.schemes = h->cfg.schemes;
+    A.n1 = h->n1; A.n2 = h->n2; A.n3 = h->n3; A.m = h->m;
+    A.coef = h->d_coef;
+    A.states = h->d_states;
+    A.independent = independent;
+    std::vector<int16_t> bv(3 * 500 * 2, 0);
+    for (int c = 0; c < 3; c++) {
+        A.best_fresh[c] = best_fresh ? best_fresh[c] : 0;
+        if (A.best_fresh[c] < 0 || A.best_fresh[c] > 500) return rfail(FG_ERR_ARG, "best fresh count out of range");
+        for (int q = 0; q < 2 * A.best_fresh[c]; q++) bv[c * 1000 + q] = (int16_t)best_vars[c * 1000 + q];
+    }
+    RCUDA(cudaMemcpy(h->d_best, bv.data(), bv.size() * 2, cudaMemcpyHostToDevice));
+    A.best_vars = h->d_best;
+    A.out = h->d_out;
+    A.out_scale = h->d_scale;
+    A.out_vars = h->d_vars;
+    A.D = h->D;
+    k_reduce<<<A.count, 128, h->smem>>>(A);
+    RCUDA(cudaGetLastError());
+    RCUDA(cudaMemcpy(out_counts, h->d_out, 4 * 13 * (size_t)A.count, cudaMemcpyDeviceToHost));
+    if (out_scale) RCUDA(cudaMemcpy(out_scale, h->d_scale, 4 * 3 * (size_t)A.count, cudaMemcpyDeviceToHost));
+    if (out_vars) {
+        std::vector<int16_t> v((size_t)A.count * 3 * 1000);
+        RCUDA(cudaMemcpy(v.data(), h->d_vars, v.size() * 2, cudaMemcpyDeviceToHost));
+        for (size_t q = 0; q < v.size(); q++) out_vars[q] = v[q];
+    }
+    return FG_OK;
+}
+
+fg_status fg_reducer_destroy(fg_reducer *h) {
+    if (!h) return FG_OK;
+    void *ptrs[] = {h->d_coef, h->d_states, h->d_best, h->d_out, h->d_scale, h->d_vars};
+    for (void *p : ptrs)
+        if (p) cudaFree(p);
+    delete h;
+    return FG_OK;
+}
+
+}  // extern "C"

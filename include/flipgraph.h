@@ -169,6 +169,39 @@ fg_status fg_get_counters(fg_handle *h, int32_t *m, int32_t *best_rank, uint64_t
 fg_status fg_host_alloc(uint64_t bytes, void **out);
 fg_status fg_host_free(void *p);
 
+/* ------------------------------------------------------------------------
+ * Additions reducer (greedy / randomised common-subexpression elimination),
+ * the reference's SchemeAdditionsReducer (scheme_additions_reducer.cu) with
+ * runReducersKernel (scheme_additions_reducer.cu:494-540) on the GPU.
+ * Reducer r uses cuRAND XORWOW seeded curand_init(seed, r, 0)
+ * (scheme_additions_reducer.cu:445); its stream persists across runs.
+ * ------------------------------------------------------------------------ */
+typedef struct {
+    int32_t count;    /* --count: parallel reducers */
+    int32_t schemes;  /* --schemes-count: reducer r reduces scheme r % schemes */
+    uint64_t seed;    /* --seed */
+    int32_t device;
+} fg_reducer_config;
+
+typedef struct fg_reducer fg_reducer;
+
+/* coef [schemes][3][m][64] int8 in {-1,0,1}: row t of U (nn0 entries), of V
+ * (nn1), of W (nn2 entries, W stored transposed as in the scheme files). */
+fg_status fg_reducer_create(const fg_reducer_config *cfg, int n1, int n2, int n3, int m, const int8_t *coef,
+                            fg_reducer **out);
+
+/* One runReducersKernel launch.  best_fresh [3] and best_vars [3][500][2] are
+ * the incumbent's fresh variables per component (partial initialisation);
+ * independent = 1 when --max-flips is 0 (scheme_additions_reducer.cu:604).
+ * out_counts [count][13] = per component (U, V, W) four ints: additions, fresh
+ * variables, naive additions, selection mode; then the number of draws the
+ * reducer consumed in this run.  out_scale [count][3]; out_vars [count][3][500][2]
+ * the fresh variables (pairs of signed variable ids).  Either of the last two
+ * may be NULL. */
+fg_status fg_reducer_run(fg_reducer *h, int independent, const int32_t *best_fresh, const int32_t *best_vars,
+                         int32_t *out_counts, float *out_scale, int32_t *out_vars);
+fg_status fg_reducer_destroy(fg_reducer *h);
+
 /* Message of the last failing call on this thread ("" when none). */
 const char *fg_last_error(void);
 

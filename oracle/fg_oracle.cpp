@@ -1341,4 +1341,12 @@ int fgo_reduce(int n1, int n2, int n3, int m, const int8_t *coef, int count, int
 
 void fgo_reducer_state_free(fgo_reducer_state *s) { delete s; }
 
+fgo_reducer_state *fgo_reducer_state_make(const int32_t *fresh, const int32_t *vars) {
+    fgo_reducer_state *st = new fgo_reducer_state;
+    for (int p = 0; p < 3; p++)
+        for (int q = 0; q < fresh[p]; q++)
+            st->vars[p].push_back({vars[(p * 500 + q) * 2], vars[(p * 500 + q) * 2 + 1]});
+    return st;
+}
+
 }  // extern "C"

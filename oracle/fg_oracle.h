@@ -109,6 +109,8 @@ int fgo_reduce(int n1, int n2, int n3, int m, const int8_t *coef, int count, int
                const fgo_tape *tape, int rng, uint64_t seed, int32_t *out, int32_t *modes,
                int64_t *consumed, const fgo_reducer_state *best, fgo_reducer_state **best_out);
 void fgo_reducer_state_free(fgo_reducer_state *s);
+/* Incumbent from explicit fresh-variable lists: fresh [3], vars [3][500][2]. */
+fgo_reducer_state *fgo_reducer_state_make(const int32_t *fresh, const int32_t *vars);
 
 /* Selects whether the multiply-adds of the greedy-intersections score are
  * evaluated fused (as nvcc contracts them by default) or unfused. */

@@ -197,11 +197,20 @@ def reduce(n, m, coef, count, tape=None, independent=True, rng="tape", seed=0, b
     lib().fgo_reduce(n[0], n[1], n[2], m, _ptr(coef), count, int(independent),
                      ctypes.byref(t) if t else None, RNG[rng], ctypes.c_uint64(seed), _ptr(out), _ptr(modes),
                      _ptr(consumed), best, ctypes.byref(state))
+    # out columns per component: additions, fresh, naive
     return out, modes, consumed, state
 
 
 def reducer_state_free(state):
     lib().fgo_reducer_state_free(state)
+
+
+def reducer_state(fresh, vars_):
+    """Incumbent state from fresh counts [3] and variables [3][500][2]."""
+    f = np.ascontiguousarray(fresh, np.int32)
+    v = np.ascontiguousarray(vars_, np.int32)
+    lib().fgo_reducer_state_make.restype = ctypes.c_void_p
+    return ctypes.c_void_p(lib().fgo_reducer_state_make(_ptr(f), _ptr(v)))
 
 
 def philox(ctr, key):
