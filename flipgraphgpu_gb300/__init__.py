@@ -203,12 +203,17 @@ class Engine:
         _check(self.lib.fg_init_naive_shapes(self.h, _ptr(sh)))
 
     def counters(self):
+        """Per-walk m, best_rank, best_m, flips since the last rank drop, flips of the last launch, validity."""
         m = np.zeros(self.walks, np.int32)
         best = np.zeros(self.walks, np.int32)
+        best_m = np.zeros(self.walks, np.int32)
+        since = np.zeros(self.walks, np.int32)
         flips = np.zeros(self.walks, np.uint64)
         valid = np.zeros(self.walks, np.uint8)
-        _check(self.lib.fg_get_counters(self.h, _ptr(m), _ptr(best), _ptr(flips), _ptr(valid)))
-        return {"m": m, "best_rank": best, "flips": flips, "valid": valid.astype(bool)}
+        _check(self.lib.fg_get_counters(self.h, _ptr(m), _ptr(best), _ptr(best_m), _ptr(since), _ptr(flips),
+                                        _ptr(valid)))
+        return {"m": m, "best_rank": best, "best_m": best_m, "flips_since_drop": since, "flips": flips,
+                "valid": valid.astype(bool)}
 
     def set_records(self, rec):
         c = rec._c()

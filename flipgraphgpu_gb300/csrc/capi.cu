@@ -449,7 +449,8 @@ fg_status fg_init_naive_shapes(fg_handle *h, const int32_t *shapes) {
     return FG_OK;
 }
 
-fg_status fg_get_counters(fg_handle *h, int32_t *m, int32_t *best_rank, uint64_t *flips, uint8_t *valid) {
+fg_status fg_get_counters(fg_handle *h, int32_t *m, int32_t *best_rank, int32_t *best_m, int32_t *flips_since_drop,
+                          uint64_t *flips_last_launch, uint8_t *valid) {
     if (!h) return fail(FG_ERR_ARG, "null handle");
     FG_CUDA(cudaSetDevice(h->dev));
     FG_CUDA(cudaStreamSynchronize(h->stream));
@@ -459,8 +460,28 @@ fg_status fg_get_counters(fg_handle *h, int32_t *m, int32_t *best_rank, uint64_t
     for (int w = 0; w < S; w++) {
         if (m) m[w] = hdr[w].m;
         if (best_rank) best_rank[w] = hdr[w].best_rank;
-        if (flips) flips[w] = hdr[w].flips_done;
+        if (best_m) best_m[w] = hdr[w].best_m;
+        if (flips_since_drop) flips_since_drop[w] = hdr[w].flips;
+        if (flips_last_launch) flips_last_launch[w] = hdr[w].flips_done;
         if (valid) valid[w] = (uint8_t)hdr[w].valid;
+    }
+    return FG_OK;
+}
+
+fg_status fg_get_scheme(fg_handle *h, int walk, int best, int32_t *n, int32_t *m, uint64_t *fac, uint64_t *sgn,
+                        uint8_t *valid) {
+    if (!h || walk < 0 || walk >= h->B.S) return fail(FG_ERR_ARG, "bad walk index");
+    FG_CUDA(cudaSetDevice(h->dev));
+    FG_CUDA(cudaStreamSynchronize(h->stream));
+    WalkHeader hd;
+    FG_CUDA(cudaMemcpy(&hd, h->B.hdr + walk, sizeof(WalkHeader), cudaMemcpyDeviceToHost));
+    if (n) for (int c = 0; c < 3; c++) n[c] = hd.n[c];
+    if (m) *m = best ? hd.best_m : hd.m;
+    const size_t o = (size_t)walk * 3 * h->B.cap, nf = (size_t)3 * h->B.cap;
+    if (fac) FG_CUDA(cudaMemcpy(fac, (best ? h->B.best_fac : h->B.fac) + o, nf * 8, cudaMemcpyDeviceToHost));
+    if (h->cfg.ring == FG_RING_ZT) {
+        if (sgn) FG_CUDA(cudaMemcpy(sgn, (best ? h->B.best_sgn : h->B.sgn) + o, nf * 8, cudaMemcpyDeviceToHost));
+        if (valid) FG_CUDA(cudaMemcpy(valid, (best ? h->B.best_valid : h->B.valid) + o, nf, cudaMemcpyDeviceToHost));
     }
     return FG_OK;
 }

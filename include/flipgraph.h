@@ -160,10 +160,17 @@ fg_status fg_xorwow_tape(uint64_t seed, int first_walk, int count, int draws, in
 fg_status fg_philox_blocks(const uint32_t *ctr, int count, uint32_t key0, uint32_t key1, int device,
                            uint32_t *out);
 
-/* Per-walk counters of the last launch without copying records:
- * m, best_rank [walks]; flips [walks] accepted in the last launch; valid [walks]
- * result of the last verification.  Any pointer may be NULL. */
-fg_status fg_get_counters(fg_handle *h, int32_t *m, int32_t *best_rank, uint64_t *flips, uint8_t *valid);
+/* Per-walk counters without copying records (any pointer may be NULL), each
+ * [walks]: current rank m, best rank, rank of the stored best scheme, flips
+ * since the last rank drop, flips accepted in the last launch, and the result
+ * of the last verification. */
+fg_status fg_get_counters(fg_handle *h, int32_t *m, int32_t *best_rank, int32_t *best_m, int32_t *flips_since_drop,
+                          uint64_t *flips_last_launch, uint8_t *valid);
+
+/* One walk's current (best=0) or best (best=1) scheme: n [3], m, factors
+ * [3][cap] (fac; sgn and valid for ZT, else may be NULL). */
+fg_status fg_get_scheme(fg_handle *h, int walk, int best, int32_t *n, int32_t *m, uint64_t *fac, uint64_t *sgn,
+                        uint8_t *valid);
 
 /* Page-locked host buffers for fast record transfers (cudaHostAlloc). */
 fg_status fg_host_alloc(uint64_t bytes, void **out);

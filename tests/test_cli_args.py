@@ -1,0 +1,62 @@
+"""Flag grammar of the executables (no GPU needed: parsing fails before any device work)."""
+import os
+import platform
+import subprocess
+
+import pytest
+
+fg = pytest.importorskip("flipgraphgpu_gb300")
+BIN = os.path.join(os.path.dirname(fg.__file__), "_lib", platform.machine())
+
+
+def run(*args):
+    exe = os.path.join(BIN, args[0])
+    if not os.path.exists(exe):
+        pytest.skip("executables not built")
+    r = subprocess.run([exe, *args[1:]], stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True, timeout=60)
+    return r.returncode, r.stdout, r.stderr
+
+
+def test_help_lists_reference_flags():
+    rc, out, _ = run("flip_graph", "--help")
+    assert rc == 0
+    for flag in ["-n1 INT", "[--schemes 1024]", "[--max-iterations 10000]", "[--path schemes]", "[--input-path null]",
+                 "[--block-size 32]", "[--expand-probability 0.01]", "[--reduce-probability 0.0]",
+                 "[--sandwiching-probability 0.0]", "[--basis-probability 0.0]", "[--resize-probability 0.2]",
+                 "[--plus-iterations 8000]", "[--log-period 0]", "[--seed 0]"]:
+        assert flag in out, flag
+    rc, out, _ = run("complexity_minimizer", "--help")
+    for flag in ["[--schemes 1024]", "[--max-iterations 10000]", "--input-path PATH", "[--target-complexity 0]",
+                 "[--max-no-improvements 3]"]:
+        assert flag in out, flag
+    rc, out, _ = run("additions_reducer", "--help")
+    for flag in ["-i PATH", "[-o schemes/additions_reduced]", "[--count 32]", "[--schemes-count 1]",
+                 "[--start-additions 0]", "[--max-flips 0]", "[--max-no-improvements 3]"]:
+        assert flag in out, flag
+
+
+def test_grammar_errors():
+    rc, _, err = run("flip_graph", "-n1", "3", "-n2")
+    assert "Invalid number of arguments" in err
+    rc, _, err = run("flip_graph", "-n1", "3", "-n2", "3", "-n3", "x3")
+    assert 'value for arg "-n3" is not natural (x3)' in err
+    rc, _, err = run("flip_graph", "-n1", "3", "-n2", "3", "-n3", "3", "--expand-probability", "0.1.2")
+    assert 'is not real (0.1.2)' in err
+    rc, _, err = run("flip_graph", "-n1", "3", "-n2", "3", "-n3", "3", "--bogus", "1")
+    assert 'unknown argument "--bogus"' in err
+    rc, _, err = run("flip_graph", "-n1", "3", "-n3", "3")
+    assert 'no value for argument "-n2"' in err
+
+
+def test_size_limits():
+    rc, out, _ = run("flip_graph", "-n1", "9", "-n2", "8", "-n3", "2")
+    assert "Error sizes, please increase MAX_MATRIX_ELEMENTS (now: 64)" in out and rc == 0
+    rc, out, _ = run("flip_graph", "-n1", "8", "-n2", "8", "-n3", "8")
+    assert "Error sizes, please increase MAX_RANK (now: 350)" in out and rc == 0
+
+
+def test_missing_input_files():
+    rc, out, _ = run("complexity_minimizer", "--input-path", "/nonexistent/x.txt")
+    assert 'Unable to open file "/nonexistent/x.txt"' in out and rc == 255
+    rc, out, _ = run("additions_reducer", "-i", "/nonexistent/x.txt")
+    assert 'Unable to open file "/nonexistent/x.txt"' in out and rc == 255

@@ -1,0 +1,91 @@
+"""The three executables against the reference's own executables' outputs.
+
+tests/golden/cli_* hold the files the reference's flip_graph (Z2 build),
+complexity_minimizer (Z2 build) and additions_reducer (ZT build) saved for
+the argument lists below; this project's executables, given the same
+arguments (plus --ring for the compile-time ring choice), must save the same
+files with the same names and byte-identical contents.
+"""
+import gzip
+import os
+import platform
+import shutil
+import subprocess
+
+import pytest
+
+from helpers import GOLDEN
+
+pytestmark = pytest.mark.gpu
+fg = pytest.importorskip("flipgraphgpu_gb300")
+
+BIN = os.path.join(os.path.dirname(fg.__file__), "_lib", platform.machine())
+
+
+def unpack(name, dst):
+    with gzip.open(os.path.join(GOLDEN, name + ".gz"), "rb") as f:
+        data = f.read()
+    path = os.path.join(dst, name)
+    with open(path, "wb") as o:
+        o.write(data)
+    return path
+
+
+def run(args, cwd, timeout=300):
+    r = subprocess.run(args, cwd=cwd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True, timeout=timeout)
+    assert r.returncode == 0, r.stdout[-3000:]
+    return r.stdout
+
+
+def same_files(out_dir, golden_dir):
+    want = sorted(os.listdir(os.path.join(GOLDEN, golden_dir)))
+    got = sorted(os.listdir(out_dir))
+    assert got[:len(want)] == want, (got, want)
+    for name in want:
+        with open(os.path.join(GOLDEN, golden_dir, name)) as a, open(os.path.join(out_dir, name)) as b:
+            assert a.read() == b.read(), name
+
+
+@pytest.fixture
+def work(tmp_path):
+    return str(tmp_path)
+
+
+def test_flip_graph_matches_reference_executable(work):
+    out = os.path.join(work, "fg")
+    os.makedirs(out)
+    log = run([os.path.join(BIN, "flip_graph"), "-n1", "3", "-n2", "3", "-n3", "3", "--schemes", "128",
+               "--max-iterations", "1000", "--plus-iterations", "300", "--resize-probability", "0", "--path", out,
+               "--seed", "71", "--ring", "Z2", "--max-launches", "5"], work)
+    assert "Best rank of 3x3x3 was improved" in log
+    same_files(out, "cli_flip_graph")
+
+
+def test_complexity_minimizer_matches_reference_executable(work):
+    inp = unpack("input_minimizer_z2_333.txt", work)
+    out = os.path.join(work, "cm")
+    os.makedirs(out)
+    run([os.path.join(BIN, "complexity_minimizer"), "--input-path", inp, "--path", out, "--schemes", "256",
+         "--max-iterations", "2000", "--seed", "61", "--ring", "Z2"], work)
+    same_files(out, "cli_complexity_minimizer")
+
+
+def test_additions_reducer_matches_reference_executable(work):
+    inp = unpack("input_zt_333.txt", work)
+    out = os.path.join(work, "ar")
+    os.makedirs(out)
+    run([os.path.join(BIN, "additions_reducer"), "-i", inp, "-o", out, "--count", "64", "--seed", "51"], work)
+    same_files(out, "cli_additions_reducer")
+
+
+def test_additions_reducer_rejects_z2_only_scheme(work):
+    inp = unpack("input_z2_333.txt", work)
+    r = subprocess.run([os.path.join(BIN, "additions_reducer"), "-i", inp, "-o", work, "--seed", "3"], cwd=work,
+                       stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True, timeout=120)
+    assert "Error: readed scheme is invalid" in r.stdout
+    # The additive --z2-input flag lifts the integer validity check.
+    out = os.path.join(work, "z2")
+    os.makedirs(out)
+    run([os.path.join(BIN, "additions_reducer"), "-i", inp, "-o", out, "--seed", "3", "--z2-input", "1",
+         "--count", "8", "--max-no-improvements", "1"], work)
+    assert os.listdir(out)
