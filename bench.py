@@ -224,6 +224,8 @@ def gpu_arm(args):
     seed = args.seed + rank
     eng = fg.Engine(walks, cap, "z2", args.mode, seed, iters, args.plus_iterations, 0.01, 0.0, device,
                     args.walks_per_block)
+    if args.fast_split is not None:
+        eng.set_fast_split(args.fast_split)
     shapes = shapes_for(walks)
     eng.init_naive_shapes(shapes)
     for _ in range(args.warmup):
@@ -325,6 +327,64 @@ def gpu_arm(args):
     return 0
 
 
+def ttr_arm(args):
+    """Time to target rank over Z2 from the naive scheme: --ttr-walks walks of --ttr-shape, plus
+    transition after --ttr-plus flips without a rank drop, flip limit 10^7 per walk, stop when a
+    verified best scheme reaches --ttr-target.  Launches of --ttr-iterations steps; wall time from
+    engine creation.  Prints one JSON line per mode."""
+    import flipgraphgpu_gb300 as fg
+    n1, n2, n3 = (int(x) for x in args.ttr_shape.split("x"))
+    cap = n1 * n2 * n3
+    with fg.Engine(32, cap, "z2", "fast", args.seed, 10, args.ttr_plus) as warm:  # CUDA context + module load
+        warm.init_naive(n1, n2, n3)
+        warm.run(1)
+    for mode in args.ttr_modes.split(","):
+        iters = args.ttr_iterations
+        t0 = time.perf_counter()
+        eng = fg.Engine(args.ttr_walks, cap, "z2", mode, args.seed, iters, args.ttr_plus, 0.01, 0.0, 0, 0)
+        eng.init_naive(n1, n2, n3)
+        reached, launches, best, flips = False, 0, cap, 0
+        while launches * iters < 10_000_000 and time.perf_counter() - t0 < args.ttr_seconds:
+            st = eng.run(1)
+            launches += 1
+            flips += st["verified_flips"]
+            best = min(best, st["min_best_rank"])
+            if st["min_best_rank"] <= args.ttr_target:
+                c = eng.counters()
+                w = int(np.argmin(c["best_rank"]))
+                reached = bool(eng.validate(best=True)[w])
+                break
+        dt = time.perf_counter() - t0
+        eng.close()
+        print(json.dumps({"workload": f"time to rank {args.ttr_target}, {args.ttr_shape} Z2, {args.ttr_walks} walks",
+                          "mode": mode, "reached": reached, "seconds": dt, "launches": launches,
+                          "steps_per_walk": launches * iters, "best_rank": best, "verified_flips": flips,
+                          "plus_iterations": args.ttr_plus, "seed": args.seed}))
+    return 0
+
+
+def zt_arm(args):
+    """Ternary search: 16,384 walks per shape of (3,3,3) and (4,4,4) from the naive schemes,
+    reference stream, exact integer verification; verified flips/s and ranks reached."""
+    import flipgraphgpu_gb300 as fg
+    for shape in ((3, 3, 3), (4, 4, 4)):
+        n1, n2, n3 = shape
+        eng = fg.Engine(args.zt_walks, n1 * n2 * n3, "zt", "reference", args.seed, args.zt_iterations, 100000, 0.01, 0.0, 0, 0)
+        eng.init_naive(n1, n2, n3)
+        eng.run(1)
+        tot_v, tot_ms = 0, 0.0
+        for _ in range(args.steps):
+            st = eng.run(1)
+            tot_v += st["verified_flips"]
+            tot_ms += st["kernel_ms"] + st["verify_ms"]
+        c = eng.counters()
+        print(json.dumps({"workload": f"ZT {n1}x{n2}x{n3}, {args.zt_walks} walks", "verified_flips_per_s": tot_v / (tot_ms / 1000),
+                          "steps": args.steps, "iterations_per_step": args.zt_iterations, "best_rank": int(c["best_rank"].min()),
+                          "walks_valid": int(c["valid"].sum())}))
+        eng.close()
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -340,9 +400,25 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--ref-iterations", type=int, default=20000)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--fast-split", type=int, default=None,
+                    help="fast mode: one thread per walk up to this many slots, one warp per walk above")
+    ap.add_argument("--workload", default="batched", choices=["batched", "ttr", "zt"])
+    ap.add_argument("--ttr-modes", default="fast,reference")
+    ap.add_argument("--ttr-seconds", type=float, default=300.0)
+    ap.add_argument("--ttr-shape", default="3x3x3")
+    ap.add_argument("--ttr-target", type=int, default=23)
+    ap.add_argument("--ttr-walks", type=int, default=1024)
+    ap.add_argument("--ttr-iterations", type=int, default=1000)
+    ap.add_argument("--ttr-plus", type=int, default=50000)
+    ap.add_argument("--zt-walks", type=int, default=16384)
+    ap.add_argument("--zt-iterations", type=int, default=200)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    if args.workload == "ttr":
+        return ttr_arm(args)
+    if args.workload == "zt":
+        return zt_arm(args)
     if args.impl == "reference":
         return reference_arm(args)
     return gpu_arm(args)

@@ -71,7 +71,7 @@ def library():
     for name in ("fg_create", "fg_destroy", "fg_init_naive", "fg_set_records", "fg_get_records", "fg_run",
                  "fg_minimize", "fg_validate", "fg_xorwow_tape", "fg_philox_blocks", "fg_init_naive_shapes",
                  "fg_get_counters", "fg_host_alloc", "fg_host_free", "fg_reducer_create", "fg_reducer_run",
-                 "fg_reducer_destroy"):
+                 "fg_reducer_destroy", "fg_set_fast_split", "fg_get_scheme"):
         getattr(lib, name).restype = ctypes.c_int
     _lib = lib
     return lib
@@ -196,6 +196,11 @@ class Engine:
 
     def init_naive(self, n1, n2, n3):
         _check(self.lib.fg_init_naive(self.h, n1, n2, n3))
+
+    def set_fast_split(self, simt_max_cap):
+        """Fast mode kernel choice (same results): -1 automatic, else one thread per walk up to
+        this slot count and one warp per walk above."""
+        _check(self.lib.fg_set_fast_split(self.h, int(simt_max_cap)))
 
     def init_naive_shapes(self, shapes):
         """Walk w starts from the naive shapes[w] scheme (many shapes in one batch)."""

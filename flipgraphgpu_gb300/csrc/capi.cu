@@ -195,6 +195,7 @@ struct fg_handle {
     cudaEvent_t fork = nullptr, join[kSideStreams] = {};
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
     std::vector<Segment> segs;
+    int simtMaxCap = -1;  // fast mode: -1 = automatic choice per segment, else thread per walk up to this slot count
     DevBatch B{};
     WalkParams P{};
     int32_t *d_bestC = nullptr;
@@ -282,6 +283,22 @@ void plan_segments(fg_handle *h, const std::vector<WalkHeader> &hdr) {
     h->segs = segs;
 }
 
+// Fast mode kernel choice for a segment.  One thread per walk does O(m) work
+// per flip for 32 walks at once but needs many walks to hide its latency and
+// 3 * slots * 32 words of shared memory per warp; one warp per walk does a
+// fixed ~300 warp instructions per flip and fills the GPU with few walks.
+// Measured crossovers on GB300 (fast mode, 1000 iterations): thread per walk
+// wins up to 32 slots from 2 walk-warps per SM, up to 64 slots from 8, up to
+// 80 slots from 16; warp per walk wins everywhere else.  `count` is the whole
+// batch: the segments run concurrently and share the SMs.
+bool thread_per_walk(int scap, int count, int sms) {
+    const double warpsPerSM = (double)count / 32.0 / (sms > 0 ? sms : 1);
+    if (scap <= 32) return warpsPerSM >= 2.0;
+    if (scap <= 64) return warpsPerSM >= 8.0;
+    if (scap <= 80) return warpsPerSM >= 16.0;
+    return false;
+}
+
 fg_status refresh_plan(fg_handle *h) {
     std::vector<WalkHeader> hdr(h->B.S);
     FG_CUDA(cudaMemcpy(hdr.data(), h->B.hdr, sizeof(WalkHeader) * h->B.S, cudaMemcpyDeviceToHost));
@@ -300,16 +317,20 @@ fg_status launch_walks(fg_handle *h) {
     const int wpb = h->cfg.walks_per_block > 0 ? h->cfg.walks_per_block : 2;
     for (const Segment &g : h->segs)
         if (g.nnmax > 56) return fail(FG_ERR_CAPACITY, "fast mode holds factors of at most 56 entries");
+    auto launch = [&](const Segment &g, cudaStream_t st) {
+        const bool simt = h->simtMaxCap >= 0 ? g.scap <= h->simtMaxCap : thread_per_walk(g.scap, h->B.S, h->sms);
+        return simt ? launch_walk_simt(h->B, h->P, g.first, g.count, g.scap, g.wide, wpb, h->sms, st)
+                    : launch_walk_warpfast(h->B, h->P, g.first, g.count, g.scap, g.wide, h->sms, st);
+    };
     if (h->segs.size() == 1) {
-        const Segment &g = h->segs[0];
-        FG_CUDA(launch_walk_simt(h->B, h->P, g.first, g.count, g.scap, g.wide, wpb, h->sms, h->stream));
+        FG_CUDA(launch(h->segs[0], h->stream));
         return FG_OK;
     }
     FG_CUDA(cudaEventRecord(h->fork, h->stream));
     for (size_t i = 0; i < h->segs.size(); i++) {
         const Segment &g = h->segs[i];
         FG_CUDA(cudaStreamWaitEvent(h->side[i], h->fork, 0));
-        FG_CUDA(launch_walk_simt(h->B, h->P, g.first, g.count, g.scap, g.wide, wpb, h->sms, h->side[i]));
+        FG_CUDA(launch(g, h->side[i]));
         FG_CUDA(cudaEventRecord(h->join[i], h->side[i]));
         FG_CUDA(cudaStreamWaitEvent(h->stream, h->join[i], 0));
     }
@@ -446,6 +467,12 @@ fg_status fg_init_naive_shapes(fg_handle *h, const int32_t *shapes) {
     fg_status st = refresh_plan(h);
     if (st) return st;
     h->ready = true;
+    return FG_OK;
+}
+
+fg_status fg_set_fast_split(fg_handle *h, int simt_max_cap) {
+    if (!h || simt_max_cap < -1) return fail(FG_ERR_ARG, "bad argument");
+    h->simtMaxCap = simt_max_cap;
     return FG_OK;
 }
 

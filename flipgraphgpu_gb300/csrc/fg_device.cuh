@@ -15,7 +15,7 @@ constexpr int kMaxRank = 350;   // reference config.cuh:10
 constexpr int kListCap = 500;   // reference config.cuh:14 (FlipSet capacity)
 constexpr unsigned kFull = 0xffffffffu;
 constexpr int kRetryCap = 1 << 20;  // bound on the reference's unbounded retry loops
-enum : int { ST_RETRY = 2, ST_OVERFLOW = 4 };
+enum : int { ST_RETRY = 2, ST_OVERFLOW = 4, ST_INTERNAL = 8 };  // ST_INTERNAL: pair counts inconsistent
 
 // Per-walk header in HBM (64 bytes).
 struct WalkHeader {

@@ -6,11 +6,19 @@ namespace fg {
 
 namespace {
 
+// Snapshot of the live terms; the slots past the final best rank are cleared
+// once at the end of the launch (simt_clear_best_tail).
 template <class W>
 __device__ __forceinline__ void simt_copy_best(const SimtZ2<W> &z, const DevBatch &B, int w) {
     uint64_t *dst = B.best_fac + (size_t)w * 3 * B.cap;
     for (int c = 0; c < 3; c++)
-        for (int t = 0; t < B.cap; t++) dst[c * B.cap + t] = t < z.m ? (uint64_t)z.F(c, t) : 0ull;
+        for (int t = 0; t < z.m; t++) dst[c * B.cap + t] = (uint64_t)z.F(c, t);
+}
+
+__device__ __forceinline__ void simt_clear_best_tail(const DevBatch &B, int w, int bestM) {
+    uint64_t *dst = B.best_fac + (size_t)w * 3 * B.cap;
+    for (int c = 0; c < 3; c++)
+        for (int t = bestM < 0 ? 0 : bestM; t < B.cap; t++) dst[c * B.cap + t] = 0ull;
 }
 
 // randomWalkKernel (flip_graph.cu:520-573) for one walk, one thread.
@@ -33,9 +41,11 @@ __device__ void simt_walk_one(const DevBatch &B, const WalkParams &P, int w, W *
     z.rebuild();
     int flipsCount = h.flips, bestRank = h.best_rank, bestM = h.best_m;
     uint64_t accepted = 0;
+    bool copied = false;
     for (int it = 0; it < P.iterations; it++) {
         const int rank = z.m;
         if (!z.tryFlip(true)) {
+            if (z.status) break;
             z.tryExpand(randint(1, 2, r));
             if (z.status) break;
             continue;
@@ -47,6 +57,7 @@ __device__ void simt_walk_one(const DevBatch &B, const WalkParams &P, int w, W *
             bestRank = z.m;
             bestM = z.m;
             simt_copy_best(z, B, w);
+            copied = true;
         }
         if (r.gate_reduce()) z.tryReduce();
         if (r.gate_expand() && z.m <= bestM + 2) {
@@ -58,6 +69,7 @@ __device__ void simt_walk_one(const DevBatch &B, const WalkParams &P, int w, W *
     uint64_t *dst = B.fac + (size_t)w * 3 * B.cap;
     for (int c = 0; c < 3; c++)
         for (int t = 0; t < B.cap; t++) dst[c * B.cap + t] = t < z.m ? (uint64_t)z.F(c, t) : 0ull;
+    if (copied) simt_clear_best_tail(B, w, bestM);
     WalkHeader o = h;
     o.m = z.m;
     o.flips = flipsCount;

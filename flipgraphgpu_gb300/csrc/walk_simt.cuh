@@ -47,13 +47,16 @@ struct ThreadPhilox {
     __device__ __forceinline__ uint64_t mask(int nn) { return nn >= 32 ? (uint64_t)raw() : (uint64_t)(raw() & ((1u << nn) - 1u)); }
 };
 
-template <class W>
+// SH = log2 of the word stride: 5 for the thread-per-walk layout (32 walks
+// interleaved by lane), 0 for one walk stored compactly (the warp-per-walk
+// kernel runs its rare structural edits through this code on lane 0).
+template <class W, int SH = 5>
 struct SimtZ2 {
     static constexpr int HS = (int)sizeof(W) * 8 - 8;  // partner count lives in bits [HS, HS+8)
     static constexpr W FM = ((W)1 << HS) - 1;
     static constexpr W ONE = (W)1 << HS;
 
-    W *s;  // this lane's walk: word (c, t) at s[(c * cap + t) * 32]
+    W *s;  // this walk: word (c, t) at s[(c * cap + t) << SH]
     int cap;
     int n0, n1, n2, nn0, nn1, nn2, full;
     int m;
@@ -63,13 +66,14 @@ struct SimtZ2 {
 
     __device__ SimtZ2(ThreadPhilox &rr) : r(rr) {}
 
-    __device__ __forceinline__ W &A(int c, int t) const { return s[(c * cap + t) << 5]; }
+    __device__ __forceinline__ W &A(int c, int t) const { return s[(c * cap + t) << SH]; }
     __device__ __forceinline__ W F(int c, int t) const { return A(c, t) & FM; }
     __device__ __forceinline__ int nn(int c) const { return c == 0 ? nn0 : (c == 1 ? nn1 : nn2); }
     __device__ __forceinline__ bool nonzero(int t) const { return F(0, t) && F(1, t) && F(2, t); }
     __device__ __forceinline__ void addP(int c, int d) { if (c == 0) P0 += d; else if (c == 1) P1 += d; else P2 += d; }
 
-    // Partner counts of every term from scratch (after structural edits).
+    // Partner counts of every term from scratch (once per launch; every edit
+    // below keeps them exact incrementally, in O(m) per changed word).
     __device__ void rebuild() {
         int tot[3] = {0, 0, 0};
 #pragma unroll
@@ -85,18 +89,64 @@ struct SimtZ2 {
         P0 = tot[0]; P1 = tot[1]; P2 = tot[2];
     }
 
-    __device__ __forceinline__ void moveTerm(int dst, int src) {
+    // Word (c, t) becomes v; the partner counts of t and of the terms that
+    // shared its old or share its new factor follow.
+    __device__ void setWord(int c, int t, W v) {
+        const W w0 = A(c, t), old = w0 & FM;
+        if (old == v) return;
+        W *p = &A(c, 0);
+        int h = 0;
+        for (int u = 0; u < m; u++) {
+            const W w = p[(size_t)u << SH], f = w & FM;
+            if (u == t) continue;
+            if (f == old) p[(size_t)u << SH] = w - ONE;
+            else if (f == v) { p[(size_t)u << SH] = w + ONE; h++; }
+        }
+        A(c, t) = v | ((W)h << HS);
+        addP(c, 2 * (h - (int)(w0 >> HS)));
+    }
+
+    // Term t leaves the partner sets of the other terms [0, m).
+    __device__ void dropCounts(int t) {
+#pragma unroll 1
+        for (int c = 0; c < 3; c++) {
+            const W w0 = A(c, t), v = w0 & FM;
+            const int h = (int)(w0 >> HS);
+            if (!h) continue;
+            W *p = &A(c, 0);
+            for (int u = 0; u < m; u++)
+                if (u != t && (p[(size_t)u << SH] & FM) == v) p[(size_t)u << SH] -= ONE;
+            addP(c, -2 * h);
+        }
+    }
+
+    // Term t (holding bare factors) joins the partner sets of the terms [0, m).
+    __device__ void addCounts(int t) {
+#pragma unroll 1
+        for (int c = 0; c < 3; c++) {
+            const W v = F(c, t);
+            W *p = &A(c, 0);
+            int h = 0;
+            for (int u = 0; u < m; u++)
+                if (u != t && (p[(size_t)u << SH] & FM) == v) { p[(size_t)u << SH] += ONE; h++; }
+            A(c, t) = v | ((W)h << HS);
+            addP(c, 2 * h);
+        }
+    }
+
+    __device__ __forceinline__ void moveTerm(int dst, int src) {  // words keep their counts
 #pragma unroll
-        for (int c = 0; c < 3; c++) A(c, dst) = F(c, src);
+        for (int c = 0; c < 3; c++) A(c, dst) = A(c, src);
     }
 
     __device__ void removeZeroes() {  // scheme_z2.cu:152-164 (no re-check of the moved term)
-        while (m > 0 && !nonzero(m - 1)) m--;
+        while (m > 0 && !nonzero(m - 1)) { dropCounts(m - 1); m--; }
         for (int t = 0; t < m; t++)
-            if (!nonzero(t)) { m--; moveTerm(t, m); }
+            if (!nonzero(t)) { dropCounts(t); m--; moveTerm(t, m); }
     }
 
     __device__ void removeAt(int t) {
+        dropCounts(t);
         m--;
         if (t != m) moveTerm(t, m);
     }
@@ -104,15 +154,15 @@ struct SimtZ2 {
     __device__ void addTriplet(int i, int j, int k, W a, W b, W c) {
         if (m >= cap) { status |= ST_OVERFLOW; return; }
         A(i, m) = a; A(j, m) = b; A(k, m) = c;
+        addCounts(m);
         m++;
     }
 
     __device__ void reduce(int i, int a, int b) {  // scheme_z2.cu:631-641
         const W v = F(i, a) ^ F(i, b);
-        A(i, a) = v;
+        setWord(i, a, v);
         removeAt(b);
         if (!v) removeZeroes();
-        rebuild();
     }
 
     // flip (scheme_z2.cu:531-577) with the count update fused into the reduction scan.
@@ -121,33 +171,45 @@ struct SimtZ2 {
         const W oldA = wja & FM, newA = oldA ^ (wjb & FM);
         const W oldB = wkb & FM, newB = oldB ^ (wka & FM);
         const int oldHa = (int)(wja >> HS), oldHb = (int)(wkb >> HS);
-        A(j, a) = newA;
-        A(k, b) = newB;
         if (!newA || !newB) {
+            setWord(j, a, newA);
+            setWord(k, b, newB);
             removeZeroes();
-            rebuild();
             return;
         }
+        A(j, a) = newA;
+        A(k, b) = newB;
         const W xia = F(i, a), xka = wka & FM, xib = F(i, b), xjb = wjb & FM;
         int cntA = 0, cntB = 0, red = -1, part = 0;
+        // Branch-free count update over all terms; the rare new-partner terms are
+        // collected in bit masks and checked for reductions afterwards in order.
+        W *pj = &A(j, 0), *pk = &A(k, 0);
+        uint64_t newJ = 0, newK = 0;  // terms t < 64 that became partners
+        bool overflow = false;        // a partner beyond term 63: fall back to an exact rescan
+#pragma unroll 4
         for (int t = 0; t < m; t++) {
-            const W wj = A(j, t), wk = A(k, t);
+            const W wj = pj[(size_t)t << SH], wk = pk[(size_t)t << SH];
             const W vj = wj & FM, vk = wk & FM;
-            if (t != a) {
-                const bool o = vj == oldA, nw = vj == newA;
-                if (nw) {
-                    cntA++;
-                    if (checkReduce && red < 0 && (F(i, t) == xia || vk == xka)) { red = t; part = 0; }
-                }
-                if (o | nw) A(j, t) = wj + (nw ? ONE : (W)0) - (o ? ONE : (W)0);
-            }
-            if (t != b) {
-                const bool o = vk == oldB, nw = vk == newB;
-                if (nw) {
-                    cntB++;
-                    if (checkReduce && red < 0 && (F(i, t) == xib || vj == xjb)) { red = t; part = 1; }
-                }
-                if (o | nw) A(k, t) = wk + (nw ? ONE : (W)0) - (o ? ONE : (W)0);
+            const bool oj = (vj == oldA) & (t != a), nj = (vj == newA) & (t != a);
+            const bool ok = (vk == oldB) & (t != b), nk = (vk == newB) & (t != b);
+            cntA += nj;
+            cntB += nk;
+            if (oj | nj) pj[(size_t)t << SH] = wj + (nj ? ONE : (W)0) - (oj ? ONE : (W)0);
+            if (ok | nk) pk[(size_t)t << SH] = wk + (nk ? ONE : (W)0) - (ok ? ONE : (W)0);
+            const uint64_t bit = t < 64 ? (1ull << t) : 0ull;
+            newJ |= nj ? bit : 0ull;
+            newK |= nk ? bit : 0ull;
+            overflow |= (nj | nk) & (t >= 64);
+        }
+        if (checkReduce && (newJ | newK | (uint64_t)overflow)) {
+            // First term (ascending) whose j-part or k-part triggers a reduction.
+            for (int t = 0; t < m; t++) {
+                const bool inJ = t < 64 ? ((newJ >> t) & 1) : (F(j, t) == newA && t != a);
+                const bool inK = t < 64 ? ((newK >> t) & 1) : (F(k, t) == newB && t != b);
+                if (!inJ && !inK) continue;
+                const W vi = F(i, t);
+                if (inJ && (vi == xia || F(k, t) == xka)) { red = t; part = 0; break; }
+                if (inK && (vi == xib || F(j, t) == xjb)) { red = t; part = 1; break; }
             }
         }
         A(j, a) = newA | ((W)cntA << HS);
@@ -176,19 +238,48 @@ struct SimtZ2 {
         if (q < P0) c = 0;
         else if (q < P0 + P1) { c = 1; q -= P0; }
         else { c = 2; q -= P0 + P1; }
+        // Term a: prefix walk over the partner counts, four terms per step
+        // (loads past the last term read 0).
+        const W *pc = &A(c, 0);
         int a = 0;
-        for (;; a++) {
-            const int h = (int)(A(c, a) >> HS);
-            if (q < h) break;
-            q -= h;
-        }
-        const W va = F(c, a);
-        int b = 0;
-        for (;; b++)
-            if (b != a && F(c, b) == va) {
-                if (q == 0) break;
-                q--;
+        for (; a < m; a += 4) {
+            const int h0 = (int)(pc[(size_t)a << SH] >> HS);
+            const int h1 = a + 1 < m ? (int)(pc[(size_t)(a + 1) << SH] >> HS) : 0;
+            const int h2 = a + 2 < m ? (int)(pc[(size_t)(a + 2) << SH] >> HS) : 0;
+            const int h3 = a + 3 < m ? (int)(pc[(size_t)(a + 3) << SH] >> HS) : 0;
+            const int s4 = h0 + h1 + h2 + h3;
+            if (q < s4) {
+                if (q < h0) break;
+                q -= h0;
+                if (q < h1) { a += 1; break; }
+                q -= h1;
+                if (q < h2) { a += 2; break; }
+                q -= h2;
+                a += 3;
+                break;
             }
+            q -= s4;
+        }
+        if (a >= m) { status |= ST_INTERNAL; return false; }
+        // Partner b: the q-th other term (ascending) with the same factor.
+        const W va = pc[(size_t)a << SH] & FM;
+        int b = 0;
+        for (; b < m; b += 4) {
+            const bool e0 = ((pc[(size_t)b << SH] & FM) == va) & (b != a);
+            const bool e1 = (b + 1 < m) && ((pc[(size_t)(b + 1) << SH] & FM) == va) && (b + 1 != a);
+            const bool e2 = (b + 2 < m) && ((pc[(size_t)(b + 2) << SH] & FM) == va) && (b + 2 != a);
+            const bool e3 = (b + 3 < m) && ((pc[(size_t)(b + 3) << SH] & FM) == va) && (b + 3 != a);
+            const int s4 = (int)e0 + (int)e1 + (int)e2 + (int)e3;
+            if (q < s4) {
+                if (e0) { if (q == 0) break; q--; }
+                if (e1) { if (q == 0) { b += 1; break; } q--; }
+                if (e2) { if (q == 0) { b += 2; break; } q--; }
+                b += 3;
+                break;
+            }
+            q -= s4;
+        }
+        if (b >= m) { status |= ST_INTERNAL; return false; }
         int i = c, j = c == 0 ? 1 : 0, k = c == 2 ? 1 : 2;
         if (r.coin()) { int tmp = j; j = k; k = tmp; }
         flip(i, j, k, a, b, checkReduce);
@@ -199,18 +290,16 @@ struct SimtZ2 {
         const W a1 = F(i, p), b1 = F(j, p), c1 = F(k, p);
         const W a2 = F(i, q), b2 = F(j, q), c2 = F(k, q);
         const W a = a1 ^ a2, b = b1 ^ b2, c = c1 ^ c2;
-        if (variant == 0) { A(j, p) = b; A(i, q) = a; addTriplet(i, j, k, a1, b2, c); }
-        else if (variant == 1) { A(k, p) = c; A(j, q) = b; addTriplet(i, j, k, a, b1, c2); }
-        else { A(i, p) = a; A(k, q) = c; addTriplet(i, j, k, a2, b, c1); }
+        if (variant == 0) { setWord(j, p, b); setWord(i, q, a); addTriplet(i, j, k, a1, b2, c); }
+        else if (variant == 1) { setWord(k, p, c); setWord(j, q, b); addTriplet(i, j, k, a, b1, c2); }
+        else { setWord(i, p, a); setWord(k, q, c); addTriplet(i, j, k, a2, b, c1); }
         if (!a || !b || !c) removeZeroes();
-        rebuild();
     }
 
     __device__ void split(int i, int j, int k, int t, W a1) {  // scheme_z2.cu:614-619
         const W a2 = F(i, t) ^ a1, bj = F(j, t), bk = F(k, t);
-        A(i, t) = a1;
+        setWord(i, t, a1);
         addTriplet(i, j, k, a2, bj, bk);
-        rebuild();
     }
 
     __device__ __forceinline__ void perm3(int &i, int &j, int &k) {

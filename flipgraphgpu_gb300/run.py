@@ -20,12 +20,18 @@ def main():
     ap.add_argument("--launches", type=int, default=1)
     ap.add_argument("--mode", default="fast", choices=["fast", "philox", "reference"])
     ap.add_argument("--seed", type=int, default=3)
+    ap.add_argument("--fast-split", type=int, default=None,
+                    help="fast mode: one thread per walk up to this many slots, one warp per walk above")
     a = ap.parse_args()
     n = tuple(int(x) for x in a.shape.split("x"))
     with Engine(a.walks, n[0] * n[1] * n[2], "z2", a.mode, a.seed, a.iterations, a.plus_iterations) as eng:
+        if a.fast_split is not None:
+            eng.set_fast_split(a.fast_split)
         eng.init_naive(*n)
+        eng.run(1)  # warm-up
         st = eng.run(a.launches)
-    print(json.dumps({"shape": a.shape, "walks": a.walks, "iterations": a.iterations, "mode": a.mode, **st}))
+    print(json.dumps({"shape": a.shape, "walks": a.walks, "iterations": a.iterations, "mode": a.mode,
+                      "fast_split": a.fast_split, **st}))
 
 
 if __name__ == "__main__":

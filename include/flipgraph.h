@@ -43,7 +43,7 @@ typedef enum { FG_RING_Z2 = 0, FG_RING_ZT = 1 } fg_ring;
 typedef enum { FG_MODE_REFERENCE = 0, FG_MODE_PHILOX_LISTS = 1, FG_MODE_FAST = 2 } fg_mode;
 
 /* Walk status bits (per walk). */
-enum { FG_WALK_RETRY = 2, FG_WALK_OVERFLOW = 4 };
+enum { FG_WALK_RETRY = 2, FG_WALK_OVERFLOW = 4, FG_WALK_INTERNAL = 8 /* fast mode: pair counts inconsistent */ };
 
 /* Mirrors the options of the reference's flip_graph executable
  * (main_flip_graph.cu:10-25) that reach the walk kernel
@@ -171,6 +171,13 @@ fg_status fg_get_counters(fg_handle *h, int32_t *m, int32_t *best_rank, int32_t 
  * [3][cap] (fac; sgn and valid for ZT, else may be NULL). */
 fg_status fg_get_scheme(fg_handle *h, int walk, int best, int32_t *n, int32_t *m, uint64_t *fac, uint64_t *sgn,
                         uint8_t *valid);
+
+/* Fast mode runs each shape segment either one thread per walk or one warp
+ * per walk; both kernels give identical results, the choice only sets speed.
+ * -1 (the default) chooses per segment from its slot count and walk count;
+ * n >= 0 forces one thread per walk for segments of at most n slots and one
+ * warp per walk above (0 = always warp, a large n = always thread). */
+fg_status fg_set_fast_split(fg_handle *h, int simt_max_cap);
 
 /* Page-locked host buffers for fast record transfers (cudaHostAlloc). */
 fg_status fg_host_alloc(uint64_t bytes, void **out);

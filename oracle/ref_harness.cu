@@ -24,6 +24,7 @@
 // Binary output: little-endian int32 / uint32 / uint64 / float records; the
 // layout is documented in tests/golden/make_golden.py which parses it.
 
+#include <chrono>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -278,8 +279,48 @@ static int cmd_time(int argc, char **argv) {
     return 0;
 }
 
+// ttr N1 N2 N3 S ITERS PLUS_ITERS SEED TARGET MAX_SECONDS
+//   Time to target rank of the reference's own walk kernel: naive starts,
+//   launches of randomWalkKernel (resize off) until some walk's best rank
+//   reaches TARGET or MAX_SECONDS elapse; prints the wall time.
+static int cmd_ttr(int argc, char **argv) {
+    if (argc != 11) { fprintf(stderr, "ttr: bad arguments\n"); return 1; }
+    int n1 = atoi(argv[2]), n2 = atoi(argv[3]), n3 = atoi(argv[4]), S = atoi(argv[5]);
+    int iters = atoi(argv[6]), plusIters = atoi(argv[7]), seed = atoi(argv[8]), target = atoi(argv[9]);
+    double maxSeconds = atof(argv[10]);
+    int blockSize = 32, numBlocks = (S + blockSize - 1) / blockSize;
+    Scheme *schemes, *best; int *bestRanks, *flips; curandState *states;
+    HCHECK(cudaMallocManaged(&schemes, S * sizeof(Scheme)));
+    HCHECK(cudaMallocManaged(&best, S * sizeof(Scheme)));
+    HCHECK(cudaMallocManaged(&bestRanks, S * sizeof(int)));
+    HCHECK(cudaMallocManaged(&flips, S * sizeof(int)));
+    HCHECK(cudaMallocManaged(&states, S * sizeof(curandState)));
+    auto t0 = std::chrono::steady_clock::now();
+    initializeRandomStatesKernel<<<numBlocks, blockSize>>>(states, S, seed);
+    initializeNaiveKernel<<<numBlocks, blockSize>>>(schemes, S, n1, n2, n3);
+    initializeSchemesKernel<<<numBlocks, blockSize>>>(schemes, best, bestRanks, flips, n1, n2, n3, S);
+    HCHECK(cudaDeviceSynchronize());
+    int launches = 0, reached = 0, bestSeen = n1 * n2 * n3;
+    double secs = 0;
+    while (!reached && secs < maxSeconds) {
+        randomWalkKernel<<<numBlocks, blockSize>>>(schemes, best, bestRanks, flips, states, S, iters, plusIters, 0.0,
+                                                   0.01, 0.0, 0.0, false);
+        HCHECK(cudaDeviceSynchronize());
+        launches++;
+        for (int w = 0; w < S; w++) {
+            if (bestRanks[w] < bestSeen) bestSeen = bestRanks[w];
+            if (bestRanks[w] <= target && best[w].validate()) reached = 1;
+        }
+        secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    }
+    printf("{\"reached\": %d, \"seconds\": %.3f, \"launches\": %d, \"steps_per_walk\": %lld, \"best_rank\": %d}\n",
+           reached, secs, launches, (long long)launches * iters, bestSeen);
+    return 0;
+}
+
 int main(int argc, char **argv) {
-    if (argc < 2) { fprintf(stderr, "usage: ref_harness walk|reduce|time ...\n"); return 1; }
+    if (argc < 2) { fprintf(stderr, "usage: ref_harness walk|reduce|time|ttr ...\n"); return 1; }
+    if (std::string(argv[1]) == "ttr") return cmd_ttr(argc, argv);
     std::string cmd = argv[1];
     if (cmd == "walk") return cmd_walk(argc, argv);
     if (cmd == "reduce") return cmd_reduce(argc, argv);
