@@ -300,6 +300,27 @@ class Reducer:
             pass
 
 
+def reducer_run_noalloc(n, m, coef, count=32, schemes=1, seed=1, device=0, independent=True, best_fresh=None,
+                        best_vars=None):
+    """One reducer pass with no device allocation (fg_reducer_run_noalloc): the same counts as
+    Reducer(...).run() on a fresh Reducer.  Calls share one static scratch array in the library
+    and must not overlap."""
+    lib = library()
+    fn = lib.fg_reducer_run_noalloc
+    fn.restype = ctypes.c_int
+    coef = np.ascontiguousarray(coef, np.int8).reshape(schemes, 3, m, 64)
+    cfg = ReducerConfig(count, schemes, seed, device)
+    counts = np.zeros((count, 13), np.int32)
+    scale = np.zeros((count, 3), np.float32)
+    bf = np.ascontiguousarray(best_fresh if best_fresh is not None else np.zeros(3), np.int32)
+    bv = np.ascontiguousarray(best_vars if best_vars is not None else np.zeros((3, 500, 2)), np.int32)
+    _check(fn(ctypes.byref(cfg), n[0], n[1], n[2], m, _ptr(coef), int(independent), _ptr(bf), _ptr(bv),
+              _ptr(counts), _ptr(scale)))
+    per = counts[:, :12].reshape(count, 3, 4)
+    return {"additions": per[:, :, 0].copy(), "fresh": per[:, :, 1].copy(), "naive": per[:, :, 2].copy(),
+            "mode": per[:, :, 3].copy(), "draws": counts[:, 12].copy(), "scale": scale}
+
+
 def xorwow_tape(seed, first_walk, count, draws, device=0):
     """The reference's per-walk cuRAND XORWOW stream, recorded on the GPU."""
     d = np.zeros((count, draws), np.uint32)

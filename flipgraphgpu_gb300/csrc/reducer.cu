@@ -12,6 +12,7 @@
 // (pairs_counter.cuh:73-101), the selection modes and every draw run on one
 // thread, so the XORWOW stream is consumed exactly as the reference does.
 #include <cstdint>
+#include <mutex>
 #include <vector>
 
 #include <string>
@@ -534,6 +535,142 @@ fg_status fg_reducer_destroy(fg_reducer *h) {
     for (void *p : ptrs)
         if (p) cudaFree(p);
     delete h;
+    return FG_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------- no-allocation variant
+// fg_reducer_run_noalloc keeps every device buffer of one reducer pass in a
+// single file-scope scratch array, so a call makes no device allocation.  All
+// calls in the process share that array: calls that overlap in time (from two
+// host threads, or two devices' calls interleaved) race on it and must be
+// serialised by the caller.
+namespace {
+
+constexpr size_t kNoallocScratchBytes = (size_t)4 << 20;
+constexpr int kNoallocMaxCount = 1024;
+constexpr int kNoallocMaxDevices = 64;
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoallocScratchBytes];
+
+std::mutex g_noalloc_mu;
+unsigned char *g_noalloc_base[kNoallocMaxDevices] = {};
+
+// Device address of the scratch array on `dev`, looked up once per device.
+cudaError_t noalloc_base(int dev, unsigned char **base) {
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_base[dev]) {
+        void *p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess) return e;
+        if (!p) return cudaErrorInvalidSymbol;
+        g_noalloc_base[dev] = static_cast<unsigned char *>(p);
+    }
+    *base = g_noalloc_base[dev];
+    return cudaSuccess;
+}
+
+size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+}  // namespace
+
+extern "C" {
+
+fg_status fg_reducer_run_noalloc(const fg_reducer_config *cfg, int n1, int n2, int n3, int m, const int8_t *coef,
+                                 int independent, const int32_t *best_fresh, const int32_t *best_vars,
+                                 int32_t *out_counts, float *out_scale) {
+    if (!cfg || !coef || !out_counts) return rfail(FG_ERR_ARG, "null argument");
+    if (cfg->count <= 0 || cfg->schemes <= 0) return rfail(FG_ERR_ARG, "count and schemes must be positive");
+    if (n1 <= 0 || n2 <= 0 || n3 <= 0 || n1 * n2 > 64 || n2 * n3 > 64 || n3 * n1 > 64 || m <= 0 || m > FG_MAX_RANK)
+        return rfail(FG_ERR_ARG, "scheme sizes out of range");
+    if (cfg->device < 0 || cfg->device >= kNoallocMaxDevices) return rfail(FG_ERR_ARG, "device out of range");
+    if (cfg->count > kNoallocMaxCount) return rfail(FG_ERR_CAPACITY, "count above the no-allocation limit (1024)");
+    int bf[3] = {0, 0, 0};
+    for (int c = 0; c < 3; c++) {
+        bf[c] = best_fresh ? best_fresh[c] : 0;
+        if (bf[c] < 0 || bf[c] > 500) return rfail(FG_ERR_ARG, "best fresh count out of range");
+        if (bf[c] > 0 && !best_vars) return rfail(FG_ERR_ARG, "best_vars is null");
+    }
+    // Scratch layout, each region on a 256-byte boundary.
+    const size_t nCoef = (size_t)cfg->schemes * 3 * m * 64;
+    const size_t oCoef = 0;
+    const size_t oStates = align256(oCoef + nCoef);
+    const size_t oBest = align256(oStates + sizeof(curandStateXORWOW_t) * (size_t)cfg->count);
+    const size_t oOut = align256(oBest + (size_t)2 * 3 * 500 * 2);
+    const size_t oScale = align256(oOut + (size_t)4 * 13 * cfg->count);
+    const size_t total = oScale + (size_t)4 * 3 * cfg->count;
+    if (total > kNoallocScratchBytes) return rfail(FG_ERR_CAPACITY, "schemes too large for the no-allocation scratch (4 MiB)");
+
+    // Problem dimensions, as fg_reducer_create derives them.
+    const int nn[3] = {n1 * n2, n2 * n3, n3 * n1};
+    ReduceDims D;
+    D.E[0] = m; D.E[1] = m; D.E[2] = nn[2];
+    D.L[0] = nn[0]; D.L[1] = nn[1]; D.L[2] = m;
+    long nocc = 1;
+    for (int sc = 0; sc < cfg->schemes; sc++) {
+        const int8_t *cf = coef + (size_t)sc * 3 * m * 64;
+        for (int c = 0; c < 3; c++) {
+            long tot = 0;
+            for (int e = 0; e < D.E[c]; e++) {
+                int size = 0;
+                if (c < 2) { for (int q = 0; q < nn[c]; q++) size += cf[((size_t)c * m + e) * 64 + q] != 0; }
+                else { for (int t = 0; t < m; t++) size += cf[((size_t)2 * m + t) * 64 + e] != 0; }
+                tot += (long)size * (size - 1) / 2;
+            }
+            if (tot > nocc) nocc = tot;
+        }
+    }
+    D.nocc = (int)nocc;
+    D.tbits = 4;
+    while ((1L << D.tbits) < 2 * nocc) D.tbits++;
+    const int T = 1 << D.tbits;
+    const int Lmax = nn[0] > nn[1] ? (nn[0] > m ? nn[0] : m) : (nn[1] > m ? nn[1] : m);
+    const int Emax = m > nn[2] ? m : nn[2];
+    const size_t smem = (size_t)12 * T + (size_t)16 * D.nocc + 4 * (size_t)(Emax + 1) + 2000 +
+                        2 * (size_t)((Emax + 1 + 1) & ~1) + 2 * (size_t)Emax * Lmax + 64;
+
+    RCUDA(cudaSetDevice(cfg->device));
+    int optin = 0;
+    RCUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, cfg->device));
+    if (smem > (size_t)optin) return rfail(FG_ERR_CAPACITY, "scheme too large for the shared-memory reducer");
+    unsigned char *base = nullptr;
+    RCUDA(noalloc_base(cfg->device, &base));
+
+    std::vector<int16_t> bv(3 * 500 * 2, 0);
+    for (int c = 0; c < 3; c++)
+        for (int q = 0; q < 2 * bf[c]; q++) bv[c * 1000 + q] = (int16_t)best_vars[c * 1000 + q];
+    // Everything on the legacy default stream, in order.
+    RCUDA(cudaMemcpy(base + oCoef, coef, nCoef, cudaMemcpyHostToDevice));
+    RCUDA(cudaMemcpy(base + oBest, bv.data(), bv.size() * 2, cudaMemcpyHostToDevice));
+    RCUDA(cudaMemset(base + oOut, 0, (size_t)4 * 13 * cfg->count));
+    RCUDA(cudaMemset(base + oScale, 0, (size_t)4 * 3 * cfg->count));
+    auto *states = reinterpret_cast<curandStateXORWOW_t *>(base + oStates);
+    k_seed_reducers<<<(cfg->count + 127) / 128, 128>>>(states, cfg->count, (unsigned long long)cfg->seed);
+    RCUDA(cudaGetLastError());
+    // Raise (never lower) the kernel's dynamic shared-memory limit, so handles
+    // made by fg_reducer_create keep theirs.
+    cudaFuncAttributes fa;
+    RCUDA(cudaFuncGetAttributes(&fa, k_reduce));
+    if ((size_t)fa.maxDynamicSharedSizeBytes < smem)
+        RCUDA(cudaFuncSetAttribute(k_reduce, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+
+    ReduceArgs A;
+    A.count = cfg->count;
+    A.schemes = cfg->schemes;
+    A.n1 = n1; A.n2 = n2; A.n3 = n3; A.m = m;
+    A.coef = reinterpret_cast<const int8_t *>(base + oCoef);
+    A.states = states;
+    A.independent = independent;
+    for (int c = 0; c < 3; c++) A.best_fresh[c] = bf[c];
+    A.best_vars = reinterpret_cast<const int16_t *>(base + oBest);
+    A.out = reinterpret_cast<int32_t *>(base + oOut);
+    A.out_scale = reinterpret_cast<float *>(base + oScale);
+    A.out_vars = nullptr;
+    A.D = D;
+    k_reduce<<<A.count, 128, smem>>>(A);
+    RCUDA(cudaGetLastError());
+    RCUDA(cudaMemcpy(out_counts, base + oOut, (size_t)4 * 13 * A.count, cudaMemcpyDeviceToHost));
+    if (out_scale) RCUDA(cudaMemcpy(out_scale, base + oScale, (size_t)4 * 3 * A.count, cudaMemcpyDeviceToHost));
     return FG_OK;
 }
 

@@ -216,6 +216,20 @@ fg_status fg_reducer_run(fg_reducer *h, int independent, const int32_t *best_fre
                          int32_t *out_counts, float *out_scale, int32_t *out_vars);
 fg_status fg_reducer_destroy(fg_reducer *h);
 
+/* One reducer pass without any device allocation: the same result as
+ * fg_reducer_create + one fg_reducer_run (out_vars omitted) +
+ * fg_reducer_destroy, with every device buffer (coefficients, cuRAND states,
+ * incumbent variables, outputs) placed in one static scratch array of 4 MiB
+ * inside the library.  No counterpart in the reference, whose reducer always
+ * allocates managed memory (scheme_additions_reducer.cu:4-29).  Inputs that
+ * do not fit (count > 1024, or schemes * 3 * m * 64 coefficient bytes plus the
+ * per-reducer buffers above 4 MiB) return FG_ERR_CAPACITY.  All calls share the
+ * one scratch array: calls that overlap in time race on it, so the caller
+ * serialises them. */
+fg_status fg_reducer_run_noalloc(const fg_reducer_config *cfg, int n1, int n2, int n3, int m, const int8_t *coef,
+                                 int independent, const int32_t *best_fresh, const int32_t *best_vars,
+                                 int32_t *out_counts, float *out_scale);
+
 /* Message of the last failing call on this thread ("" when none). */
 const char *fg_last_error(void);
 
