@@ -321,6 +321,29 @@ def reducer_run_noalloc(n, m, coef, count=32, schemes=1, seed=1, device=0, indep
             "mode": per[:, :, 3].copy(), "draws": counts[:, 12].copy(), "scale": scale}
 
 
+def gemm_bf16(a_bits, b_bits, mode=0, bias=None, mask=None, accumulate=None, device=0):
+    """Tensor-core GEMM D = A B^T on bf16 bit patterns (uint16): mode 0 -> fp32 D (plus
+    `accumulate` when given), 1 -> bf16 relu(D + bias), 2 -> bf16 D masked where mask > 0."""
+    lib = library()
+    fn = lib.fg_gemm_bf16
+    fn.restype = ctypes.c_int
+    a = np.ascontiguousarray(a_bits, np.uint16)
+    b = np.ascontiguousarray(b_bits, np.uint16)
+    (m, k), (n, k2) = a.shape, b.shape
+    if k != k2:
+        raise ValueError("inner dimensions differ")
+    bias = None if bias is None else np.ascontiguousarray(bias, np.float32)
+    mask = None if mask is None else np.ascontiguousarray(mask, np.uint16)
+    if mode == 0:
+        out = np.zeros((m, n), np.float32) if accumulate is None else np.ascontiguousarray(accumulate, np.float32)
+        _check(fn(_ptr(a), _ptr(b), _ptr(bias), _ptr(mask), m, n, k, 0, int(accumulate is not None), _ptr(out), None,
+                  device))
+    else:
+        out = np.zeros((m, n), np.uint16)
+        _check(fn(_ptr(a), _ptr(b), _ptr(bias), _ptr(mask), m, n, k, mode, 0, None, _ptr(out), device))
+    return out
+
+
 def xorwow_tape(seed, first_walk, count, draws, device=0):
     """The reference's per-walk cuRAND XORWOW stream, recorded on the GPU."""
     d = np.zeros((count, draws), np.uint32)

@@ -179,6 +179,16 @@ fg_status fg_get_scheme(fg_handle *h, int walk, int best, int32_t *n, int32_t *m
  * warp per walk above (0 = always warp, a large n = always thread). */
 fg_status fg_set_fast_split(fg_handle *h, int simt_max_cap);
 
+/* Tensor-core (tcgen05) bf16 GEMM of the learned proposal's MLP, on host
+ * buffers (test and support entry; no reference counterpart):
+ *   D[M][N] = A[M][K] * B[N][K]^T, A and B bf16 bit patterns, row-major;
+ *   mode 0: outF (fp32) = D, or outF += D when `accumulate`;
+ *   mode 1: outH (bf16) = relu(D + bias) (bias [N] or NULL);
+ *   mode 2: outH (bf16) = D where mask[M][N] > 0, else 0.
+ * M % 128 == 0, K % 64 == 0, N % 64 == 0. */
+fg_status fg_gemm_bf16(const uint16_t *A, const uint16_t *B, const float *bias, const uint16_t *mask, int M, int N,
+                       int K, int mode, int accumulate, float *outF, uint16_t *outH, int device);
+
 /* Page-locked host buffers for fast record transfers (cudaHostAlloc). */
 fg_status fg_host_alloc(uint64_t bytes, void **out);
 fg_status fg_host_free(void *p);
