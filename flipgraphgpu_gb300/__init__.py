@@ -344,6 +344,63 @@ def gemm_bf16(a_bits, b_bits, mode=0, bias=None, mask=None, accumulate=None, dev
     return out
 
 
+class Mlp:
+    """The learned proposal's scoring network on the GPU (fg_mlp_*).  Features are
+    [rows][3] uint64 words (192 binary features); params one fp32 vector."""
+
+    def __init__(self, seed=1, device=0):
+        self.lib = library()
+        for name in ("fg_mlp_create", "fg_mlp_destroy", "fg_mlp_set_params", "fg_mlp_get_params",
+                     "fg_mlp_gradients", "fg_mlp_score", "fg_mlp_train", "fg_mlp_param_count"):
+            getattr(self.lib, name).restype = ctypes.c_int
+        self.n_params = int(self.lib.fg_mlp_param_count())
+        self.h = ctypes.c_void_p()
+        _check(self.lib.fg_mlp_create(device, ctypes.c_uint64(seed), ctypes.byref(self.h)))
+
+    def params(self):
+        p = np.zeros(self.n_params, np.float32)
+        _check(self.lib.fg_mlp_get_params(self.h, _ptr(p)))
+        return p
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, np.float32)
+        assert p.size == self.n_params
+        _check(self.lib.fg_mlp_set_params(self.h, _ptr(p)))
+
+    def gradients(self, features, labels):
+        f = np.ascontiguousarray(features, np.uint64)
+        y = np.ascontiguousarray(labels, np.float32)
+        g = np.zeros(self.n_params, np.float32)
+        loss = ctypes.c_float()
+        _check(self.lib.fg_mlp_gradients(self.h, _ptr(f), _ptr(y), len(y), ctypes.byref(loss), _ptr(g)))
+        return float(loss.value), g
+
+    def score(self, features):
+        f = np.ascontiguousarray(features, np.uint64)
+        out = np.zeros(len(f), np.float32)
+        _check(self.lib.fg_mlp_score(self.h, _ptr(f), len(f), _ptr(out)))
+        return out
+
+    def train(self, features, labels, batch=4096, epochs=1, lr=1e-3, seed=1):
+        f = np.ascontiguousarray(features, np.uint64)
+        y = np.ascontiguousarray(labels, np.float32)
+        loss = ctypes.c_float()
+        _check(self.lib.fg_mlp_train(self.h, _ptr(f), _ptr(y), ctypes.c_int64(len(y)), batch, epochs,
+                                     ctypes.c_float(lr), ctypes.c_uint64(seed), ctypes.byref(loss)))
+        return float(loss.value)
+
+    def close(self):
+        if self.h:
+            self.lib.fg_mlp_destroy(self.h)
+            self.h = ctypes.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+
 def xorwow_tape(seed, first_walk, count, draws, device=0):
     """The reference's per-walk cuRAND XORWOW stream, recorded on the GPU."""
     d = np.zeros((count, draws), np.uint32)

@@ -189,6 +189,34 @@ fg_status fg_set_fast_split(fg_handle *h, int simt_max_cap);
 fg_status fg_gemm_bf16(const uint16_t *A, const uint16_t *B, const float *bias, const uint16_t *mask, int M, int N,
                        int K, int mode, int accumulate, float *outF, uint16_t *outH, int device);
 
+/* ------------------------------------------------------------------------
+ * Learned flip proposal: the scoring network (no reference counterpart).
+ * A candidate flip is described by 192 binary features packed in three
+ * uint64 words (bit q of word w = feature 64w + q).  The network is
+ * 192 -> 256 -> 256 -> 1 with ReLU, bf16 weights and activations, fp32
+ * accumulation on the tensor cores; its score is the logit of "the rank drops
+ * within the next 1000 flips".  Parameters are one fp32 block of
+ * fg_mlp_param_count() floats: W1 [256][192], b1 [256], W2 [256][256],
+ * b2 [256], w3 [256], b3.
+ * ------------------------------------------------------------------------ */
+typedef struct fg_mlp fg_mlp;
+
+int fg_mlp_param_count(void);
+/* He-uniform weights from `seed`, zero biases. */
+fg_status fg_mlp_create(int device, uint64_t seed, fg_mlp **out);
+fg_status fg_mlp_destroy(fg_mlp *m);
+fg_status fg_mlp_set_params(fg_mlp *m, const float *params);
+fg_status fg_mlp_get_params(fg_mlp *m, float *params);
+/* Mean binary cross-entropy of one batch (labels 0/1) and its gradient
+ * (same layout as the parameters); no update. */
+fg_status fg_mlp_gradients(fg_mlp *m, const uint64_t *features, const float *labels, int rows, float *loss,
+                           float *grads);
+fg_status fg_mlp_score(fg_mlp *m, const uint64_t *features, int rows, float *scores);
+/* Adam (lr, betas 0.9/0.999) over shuffled mini-batches (`batch` a multiple
+ * of 128) for `epochs` passes; *last_loss = mean loss of the last pass. */
+fg_status fg_mlp_train(fg_mlp *m, const uint64_t *features, const float *labels, int64_t n, int batch, int epochs,
+                       float lr, uint64_t seed, float *last_loss);
+
 /* Page-locked host buffers for fast record transfers (cudaHostAlloc). */
 fg_status fg_host_alloc(uint64_t bytes, void **out);
 fg_status fg_host_free(void *p);
