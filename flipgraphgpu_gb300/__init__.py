@@ -22,7 +22,7 @@ LIB_PATH = os.path.join(PKG, "_lib", platform.machine(), "libflipgraph.so")
 LIST_CAP = 500
 MAX_RANK = 350
 RINGS = {"z2": 0, "zt": 1}
-MODES = {"reference": 0, "philox": 1, "fast": 2, "xorwow": 0}
+MODES = {"reference": 0, "philox": 1, "fast": 2, "xorwow": 0, "learned": 3}
 STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "capacity", 4: "state", 5: "walk failure"}
 
 
@@ -196,6 +196,25 @@ class Engine:
 
     def init_naive(self, n1, n2, n3):
         _check(self.lib.fg_init_naive(self.h, n1, n2, n3))
+
+    def set_proposal(self, mlp=None, candidates=1, temperature=1.0, min_entropy=0.0):
+        """Learned mode: score `candidates` uniform candidate flips per step with `mlp` (an Mlp,
+        or None for a uniform choice) and sample from softmax(score / temperature)."""
+        self.lib.fg_set_proposal.restype = ctypes.c_int
+        _check(self.lib.fg_set_proposal(self.h, mlp.h if mlp is not None else None, int(candidates),
+                                        ctypes.c_float(temperature), ctypes.c_float(min_entropy)))
+        self._mlp = mlp  # keep the network alive while it is in use
+
+    def collect_records(self, every=16, horizon=1000, launches=1, capacity=1 << 20):
+        """Learned mode, one candidate: run plain walks and return (features [n][3] uint64,
+        labels [n] float32) -- label 1 if the rank dropped within `horizon` flips."""
+        f = np.zeros((capacity, 3), np.uint64)
+        y = np.zeros(capacity, np.float32)
+        n = ctypes.c_int64()
+        self.lib.fg_collect_records.restype = ctypes.c_int
+        _check(self.lib.fg_collect_records(self.h, int(every), int(horizon), int(launches), ctypes.c_int64(capacity),
+                                           _ptr(f), _ptr(y), ctypes.byref(n)))
+        return f[:n.value].copy(), y[:n.value].copy()
 
     def set_fast_split(self, simt_max_cap):
         """Fast mode kernel choice (same results): -1 automatic, else one thread per walk up to

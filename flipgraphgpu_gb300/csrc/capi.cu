@@ -1,5 +1,6 @@
 // C-ABI of libflipgraph (include/flipgraph.h): handle lifetime, record
 // transfer, launches, exact verification and test-support streams.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -8,6 +9,7 @@
 
 #include "../../include/flipgraph.h"
 #include "launch.h"
+#include "learned.h"
 
 using namespace fg;
 
@@ -195,6 +197,9 @@ struct fg_handle {
     cudaEvent_t fork = nullptr, join[kSideStreams] = {};
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
     std::vector<Segment> segs;
+    LearnedBuffers learned;
+    LearnedConfig lcfg;
+    fg_mlp *mlp = nullptr;
     int simtMaxCap = -1;  // fast mode: -1 = automatic choice per segment, else thread per walk up to this slot count
     DevBatch B{};
     WalkParams P{};
@@ -299,6 +304,10 @@ bool thread_per_walk(int scap, int count, int sms) {
     return false;
 }
 
+bool uses_lists(const fg_handle *h) {
+    return h->cfg.mode == FG_MODE_REFERENCE || h->cfg.mode == FG_MODE_PHILOX_LISTS;
+}
+
 fg_status refresh_plan(fg_handle *h) {
     std::vector<WalkHeader> hdr(h->B.S);
     FG_CUDA(cudaMemcpy(hdr.data(), h->B.hdr, sizeof(WalkHeader) * h->B.S, cudaMemcpyDeviceToHost));
@@ -309,6 +318,12 @@ fg_status refresh_plan(fg_handle *h) {
 // Launches one walk pass over every walk on h->stream (fast mode: one kernel
 // per segment on side streams, forked from and joined back into h->stream).
 fg_status launch_walks(fg_handle *h) {
+    if (h->cfg.mode == FG_MODE_LEARNED) {
+        for (const Segment &g : h->segs)
+            if (g.nnmax > 21) return fail(FG_ERR_CAPACITY, "the learned mode takes factors of at most 21 entries");
+        FG_CUDA(learned_launch(h->learned, h->B, h->P, h->lcfg, h->mlp, h->stream));
+        return FG_OK;
+    }
     if (h->cfg.mode != FG_MODE_FAST) {
         FG_CUDA(launch_walk(h->cfg.ring, h->B, h->P, h->cfg.mode == FG_MODE_REFERENCE ? RNG_XORWOW : RNG_PHILOX,
                             h->wpb, h->grid, h->stream));
@@ -349,9 +364,10 @@ fg_status fg_create(const fg_config *cfg, fg_handle **out) {
     *out = nullptr;
     if (cfg->walks <= 0) return fail(FG_ERR_ARG, "walks must be positive");
     if (cfg->ring != FG_RING_Z2 && cfg->ring != FG_RING_ZT) return fail(FG_ERR_ARG, "unknown ring");
-    if (cfg->ring == FG_RING_ZT && cfg->mode == FG_MODE_FAST)
-        return fail(FG_ERR_ARG, "the fast mode is available for the Z2 ring; use a list mode for ZT");
-    if (cfg->mode != FG_MODE_REFERENCE && cfg->mode != FG_MODE_PHILOX_LISTS && cfg->mode != FG_MODE_FAST)
+    if (cfg->ring == FG_RING_ZT && (cfg->mode == FG_MODE_FAST || cfg->mode == FG_MODE_LEARNED))
+        return fail(FG_ERR_ARG, "the fast and learned modes are available for the Z2 ring; use a list mode for ZT");
+    if (cfg->mode != FG_MODE_REFERENCE && cfg->mode != FG_MODE_PHILOX_LISTS && cfg->mode != FG_MODE_FAST &&
+        cfg->mode != FG_MODE_LEARNED)
         return fail(FG_ERR_ARG, "unknown mode");
     if (cfg->cap <= 0 || slots_for_cap(cfg->cap) == 0 || cfg->cap > FG_MAX_RANK + 2)
         return fail(FG_ERR_CAPACITY, "cap must be in [1, 352]");
@@ -399,6 +415,13 @@ fg_status fg_create(const fg_config *cfg, fg_handle **out) {
             return fail(FG_ERR_CUDA, "seeding failed");
         }
     }
+    if (cfg->mode == FG_MODE_LEARNED) {
+        cudaError_t le = learned_alloc(h->learned, S, cap, 1);
+        if (le != cudaSuccess) {
+            fg_destroy(h);
+            return fail(FG_ERR_CUDA, cudaGetErrorString(le));
+        }
+    }
     int occ = occupancy_walk(cfg->ring, cap, cfg->mode == FG_MODE_REFERENCE ? RNG_XORWOW : RNG_PHILOX, h->wpb);
     if (occ <= 0) occ = 1;
     int need = (S + h->wpb - 1) / h->wpb;
@@ -411,6 +434,7 @@ fg_status fg_destroy(fg_handle *h) {
     if (!h) return FG_OK;
     cudaSetDevice(h->dev);
     if (h->stream) cudaStreamSynchronize(h->stream);
+    learned_free(h->learned);
     void *ptrs[] = {h->B.hdr, h->B.fac, h->B.sgn, h->B.valid, h->B.lists, h->B.best_fac, h->B.best_sgn,
                     h->B.best_valid, h->B.xorwow, h->d_bestC, h->d_valid};
     for (void *p : ptrs)
@@ -435,7 +459,7 @@ fg_status fg_init_naive(fg_handle *h, int n1, int n2, int n3) {
     FG_CUDA(cudaSetDevice(h->dev));
     k_init_naive<<<(h->B.S + 127) / 128, 128, 0, h->stream>>>(h->B, n1, n2, n3, nullptr, h->cfg.ring == FG_RING_ZT);
     FG_CUDA(cudaGetLastError());
-    if (h->cfg.mode != FG_MODE_FAST) FG_CUDA(launch_rebuild(h->cfg.ring, h->B, h->wpb, h->grid, h->stream));
+    if (uses_lists(h)) FG_CUDA(launch_rebuild(h->cfg.ring, h->B, h->wpb, h->grid, h->stream));
     FG_CUDA(cudaStreamSynchronize(h->stream));
     fg_status st = refresh_plan(h);
     if (st) return st;
@@ -460,13 +484,55 @@ fg_status fg_init_naive_shapes(fg_handle *h, const int32_t *shapes) {
         k_init_naive<<<(S + 127) / 128, 128, 0, h->stream>>>(h->B, 0, 0, 0, d, h->cfg.ring == FG_RING_ZT);
         e = cudaGetLastError();
     }
-    if (e == cudaSuccess && h->cfg.mode != FG_MODE_FAST) e = launch_rebuild(h->cfg.ring, h->B, h->wpb, h->grid, h->stream);
+    if (e == cudaSuccess && uses_lists(h)) e = launch_rebuild(h->cfg.ring, h->B, h->wpb, h->grid, h->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
     cudaFree(d);
     if (e != cudaSuccess) return fail(FG_ERR_CUDA, cudaGetErrorString(e));
     fg_status st = refresh_plan(h);
     if (st) return st;
     h->ready = true;
+    return FG_OK;
+}
+
+fg_status fg_set_proposal(fg_handle *h, fg_mlp *mlp, int candidates, float temperature, float min_entropy) {
+    if (!h) return fail(FG_ERR_ARG, "null handle");
+    if (h->cfg.mode != FG_MODE_LEARNED) return fail(FG_ERR_STATE, "the proposal is set in the learned mode");
+    if (candidates < 1 || candidates > 16 || !(temperature > 0.0f) || !(min_entropy >= 0.0f))
+        return fail(FG_ERR_ARG, "candidates in [1, 16], temperature > 0, min_entropy >= 0");
+    FG_CUDA(cudaSetDevice(h->dev));
+    FG_CUDA(cudaStreamSynchronize(h->stream));
+    if (candidates != h->learned.K) FG_CUDA(learned_alloc(h->learned, h->B.S, h->B.cap, candidates));
+    h->mlp = mlp;
+    h->lcfg.K = candidates;
+    h->lcfg.invTemp = 1.0f / temperature;
+    h->lcfg.minEntropy = min_entropy;
+    return FG_OK;
+}
+
+fg_status fg_collect_records(fg_handle *h, int every, int horizon, int launches, int64_t capacity, uint64_t *features,
+                             float *labels, int64_t *count) {
+    if (!h || !features || !labels || !count) return fail(FG_ERR_ARG, "null argument");
+    if (h->cfg.mode != FG_MODE_LEARNED || h->learned.K != 1)
+        return fail(FG_ERR_STATE, "records are collected in the learned mode with one candidate");
+    if (!h->ready) return fail(FG_ERR_STATE, "records not initialised");
+    if (every <= 0 || horizon <= 0 || launches < 0 || capacity <= 0) return fail(FG_ERR_ARG, "bad argument");
+    FG_CUDA(cudaSetDevice(h->dev));
+    FG_CUDA(cudaStreamSynchronize(h->stream));
+    FG_CUDA(learned_alloc_records(h->learned, capacity, 1024));
+    h->lcfg.recordEvery = every;
+    fg_status st = FG_OK;
+    for (int L = 0; L < launches && st == FG_OK; L++) st = launch_walks(h);
+    h->lcfg.recordEvery = 0;
+    std::vector<uint64_t> f;
+    std::vector<float> y;
+    cudaError_t e = st == FG_OK ? learned_take_records(h->learned, horizon, f, y, h->stream) : cudaSuccess;
+    cudaError_t e2 = learned_alloc_records(h->learned, 0, 0);
+    if (st) return st;
+    if (e != cudaSuccess || e2 != cudaSuccess) return fail(FG_ERR_CUDA, cudaGetErrorString(e != cudaSuccess ? e : e2));
+    const size_t n = std::min(y.size(), (size_t)capacity);
+    std::copy(f.begin(), f.begin() + n * 3, features);
+    std::copy(y.begin(), y.begin() + n, labels);
+    *count = (int64_t)n;
     return FG_OK;
 }
 
@@ -641,7 +707,7 @@ fg_status fg_minimize(fg_handle *h, int32_t *best_complexity) {
     FG_CUDA(cudaSetDevice(h->dev));
     const int S = h->B.S;
     FG_CUDA(cudaMemcpyAsync(h->d_bestC, best_complexity, S * 4, cudaMemcpyHostToDevice, h->stream));
-    if (h->cfg.mode == FG_MODE_FAST) return fail(FG_ERR_ARG, "the minimizer runs in a list mode");
+    if (!uses_lists(h)) return fail(FG_ERR_ARG, "the minimizer runs in a list mode");
     FG_CUDA(launch_minimize(h->cfg.ring, h->B, h->P, h->cfg.mode == FG_MODE_REFERENCE ? RNG_XORWOW : RNG_PHILOX,
                             h->wpb, h->grid, h->d_bestC, h->stream));
     FG_CUDA(cudaMemcpyAsync(best_complexity, h->d_bestC, S * 4, cudaMemcpyDeviceToHost, h->stream));

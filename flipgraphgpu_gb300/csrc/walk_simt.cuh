@@ -49,14 +49,17 @@ struct ThreadPhilox {
 
 // SH = log2 of the word stride: 5 for the thread-per-walk layout (32 walks
 // interleaved by lane), 0 for one walk stored compactly (the warp-per-walk
-// kernel runs its rare structural edits through this code on lane 0).
+// kernel runs its rare structural edits through this code on lane 0), -1 for
+// a stride chosen at run time (the learned walk's global-memory layout, all
+// walks interleaved).
 template <class W, int SH = 5>
 struct SimtZ2 {
     static constexpr int HS = (int)sizeof(W) * 8 - 8;  // partner count lives in bits [HS, HS+8)
     static constexpr W FM = ((W)1 << HS) - 1;
     static constexpr W ONE = (W)1 << HS;
 
-    W *s;  // this walk: word (c, t) at s[(c * cap + t) << SH]
+    W *s;  // this walk: word (c, t) at s[(c * cap + t) << SH] (SH < 0: shift rsh, set at run time)
+    int rsh = 0;
     int cap;
     int n0, n1, n2, nn0, nn1, nn2, full;
     int m;
@@ -66,7 +69,8 @@ struct SimtZ2 {
 
     __device__ SimtZ2(ThreadPhilox &rr) : r(rr) {}
 
-    __device__ __forceinline__ W &A(int c, int t) const { return s[(c * cap + t) << SH]; }
+    __device__ __forceinline__ int sh() const { return SH >= 0 ? SH : rsh; }
+    __device__ __forceinline__ W &A(int c, int t) const { return s[(size_t)(c * cap + t) << sh()]; }
     __device__ __forceinline__ W F(int c, int t) const { return A(c, t) & FM; }
     __device__ __forceinline__ int nn(int c) const { return c == 0 ? nn0 : (c == 1 ? nn1 : nn2); }
     __device__ __forceinline__ bool nonzero(int t) const { return F(0, t) && F(1, t) && F(2, t); }
@@ -97,10 +101,10 @@ struct SimtZ2 {
         W *p = &A(c, 0);
         int h = 0;
         for (int u = 0; u < m; u++) {
-            const W w = p[(size_t)u << SH], f = w & FM;
+            const W w = p[(size_t)u << sh()], f = w & FM;
             if (u == t) continue;
-            if (f == old) p[(size_t)u << SH] = w - ONE;
-            else if (f == v) { p[(size_t)u << SH] = w + ONE; h++; }
+            if (f == old) p[(size_t)u << sh()] = w - ONE;
+            else if (f == v) { p[(size_t)u << sh()] = w + ONE; h++; }
         }
         A(c, t) = v | ((W)h << HS);
         addP(c, 2 * (h - (int)(w0 >> HS)));
@@ -115,7 +119,7 @@ struct SimtZ2 {
             if (!h) continue;
             W *p = &A(c, 0);
             for (int u = 0; u < m; u++)
-                if (u != t && (p[(size_t)u << SH] & FM) == v) p[(size_t)u << SH] -= ONE;
+                if (u != t && (p[(size_t)u << sh()] & FM) == v) p[(size_t)u << sh()] -= ONE;
             addP(c, -2 * h);
         }
     }
@@ -128,7 +132,7 @@ struct SimtZ2 {
             W *p = &A(c, 0);
             int h = 0;
             for (int u = 0; u < m; u++)
-                if (u != t && (p[(size_t)u << SH] & FM) == v) { p[(size_t)u << SH] += ONE; h++; }
+                if (u != t && (p[(size_t)u << sh()] & FM) == v) { p[(size_t)u << sh()] += ONE; h++; }
             A(c, t) = v | ((W)h << HS);
             addP(c, 2 * h);
         }
@@ -188,14 +192,14 @@ struct SimtZ2 {
         bool overflow = false;        // a partner beyond term 63: fall back to an exact rescan
 #pragma unroll 4
         for (int t = 0; t < m; t++) {
-            const W wj = pj[(size_t)t << SH], wk = pk[(size_t)t << SH];
+            const W wj = pj[(size_t)t << sh()], wk = pk[(size_t)t << sh()];
             const W vj = wj & FM, vk = wk & FM;
             const bool oj = (vj == oldA) & (t != a), nj = (vj == newA) & (t != a);
             const bool ok = (vk == oldB) & (t != b), nk = (vk == newB) & (t != b);
             cntA += nj;
             cntB += nk;
-            if (oj | nj) pj[(size_t)t << SH] = wj + (nj ? ONE : (W)0) - (oj ? ONE : (W)0);
-            if (ok | nk) pk[(size_t)t << SH] = wk + (nk ? ONE : (W)0) - (ok ? ONE : (W)0);
+            if (oj | nj) pj[(size_t)t << sh()] = wj + (nj ? ONE : (W)0) - (oj ? ONE : (W)0);
+            if (ok | nk) pk[(size_t)t << sh()] = wk + (nk ? ONE : (W)0) - (ok ? ONE : (W)0);
             const uint64_t bit = t < 64 ? (1ull << t) : 0ull;
             newJ |= nj ? bit : 0ull;
             newK |= nk ? bit : 0ull;
@@ -229,24 +233,34 @@ struct SimtZ2 {
         }
     }
 
-    // Uniform ordered equal pair in canonical order (component, term, partner).
-    __device__ bool tryFlip(bool checkReduce) {
+    // Uniform ordered equal pair in canonical order (component, term, partner), then
+    // a uniform orientation and the flip.
+    __device__ __forceinline__ bool tryFlip(bool checkReduce) {
+        int c, a, b;
+        if (!pickPair(c, a, b)) return false;
+        int i = c, j = c == 0 ? 1 : 0, k = c == 2 ? 1 : 2;
+        if (r.coin()) { int tmp = j; j = k; k = tmp; }
+        flip(i, j, k, a, b, checkReduce);
+        return true;
+    }
+
+    // One draw: the q-th ordered equal pair in canonical order.
+    __device__ __forceinline__ bool pickPair(int &c, int &a, int &b) {
         const int Ptot = P0 + P1 + P2;
         if (Ptot <= 0) return false;
         int q = (int)r.below((uint32_t)Ptot);
-        int c;
         if (q < P0) c = 0;
         else if (q < P0 + P1) { c = 1; q -= P0; }
         else { c = 2; q -= P0 + P1; }
         // Term a: prefix walk over the partner counts, four terms per step
         // (loads past the last term read 0).
         const W *pc = &A(c, 0);
-        int a = 0;
+        a = 0;
         for (; a < m; a += 4) {
-            const int h0 = (int)(pc[(size_t)a << SH] >> HS);
-            const int h1 = a + 1 < m ? (int)(pc[(size_t)(a + 1) << SH] >> HS) : 0;
-            const int h2 = a + 2 < m ? (int)(pc[(size_t)(a + 2) << SH] >> HS) : 0;
-            const int h3 = a + 3 < m ? (int)(pc[(size_t)(a + 3) << SH] >> HS) : 0;
+            const int h0 = (int)(pc[(size_t)a << sh()] >> HS);
+            const int h1 = a + 1 < m ? (int)(pc[(size_t)(a + 1) << sh()] >> HS) : 0;
+            const int h2 = a + 2 < m ? (int)(pc[(size_t)(a + 2) << sh()] >> HS) : 0;
+            const int h3 = a + 3 < m ? (int)(pc[(size_t)(a + 3) << sh()] >> HS) : 0;
             const int s4 = h0 + h1 + h2 + h3;
             if (q < s4) {
                 if (q < h0) break;
@@ -262,13 +276,13 @@ struct SimtZ2 {
         }
         if (a >= m) { status |= ST_INTERNAL; return false; }
         // Partner b: the q-th other term (ascending) with the same factor.
-        const W va = pc[(size_t)a << SH] & FM;
-        int b = 0;
+        const W va = pc[(size_t)a << sh()] & FM;
+        b = 0;
         for (; b < m; b += 4) {
-            const bool e0 = ((pc[(size_t)b << SH] & FM) == va) & (b != a);
-            const bool e1 = (b + 1 < m) && ((pc[(size_t)(b + 1) << SH] & FM) == va) && (b + 1 != a);
-            const bool e2 = (b + 2 < m) && ((pc[(size_t)(b + 2) << SH] & FM) == va) && (b + 2 != a);
-            const bool e3 = (b + 3 < m) && ((pc[(size_t)(b + 3) << SH] & FM) == va) && (b + 3 != a);
+            const bool e0 = ((pc[(size_t)b << sh()] & FM) == va) & (b != a);
+            const bool e1 = (b + 1 < m) && ((pc[(size_t)(b + 1) << sh()] & FM) == va) && (b + 1 != a);
+            const bool e2 = (b + 2 < m) && ((pc[(size_t)(b + 2) << sh()] & FM) == va) && (b + 2 != a);
+            const bool e3 = (b + 3 < m) && ((pc[(size_t)(b + 3) << sh()] & FM) == va) && (b + 3 != a);
             const int s4 = (int)e0 + (int)e1 + (int)e2 + (int)e3;
             if (q < s4) {
                 if (e0) { if (q == 0) break; q--; }
@@ -280,9 +294,6 @@ struct SimtZ2 {
             q -= s4;
         }
         if (b >= m) { status |= ST_INTERNAL; return false; }
-        int i = c, j = c == 0 ? 1 : 0, k = c == 2 ? 1 : 2;
-        if (r.coin()) { int tmp = j; j = k; k = tmp; }
-        flip(i, j, k, a, b, checkReduce);
         return true;
     }
 

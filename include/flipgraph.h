@@ -39,8 +39,14 @@ typedef enum { FG_RING_Z2 = 0, FG_RING_ZT = 1 } fg_ring;
  *   (multiply-high ranges, integer gate thresholds).  One warp per walk.
  * FG_MODE_FAST: Philox stream, implicit pair enumeration (no lists: an ordered
  *   equal-factor pair is drawn uniformly in canonical order -- the reference's
- *   proposal distribution), one thread per walk.  The throughput mode. */
-typedef enum { FG_MODE_REFERENCE = 0, FG_MODE_PHILOX_LISTS = 1, FG_MODE_FAST = 2 } fg_mode;
+ *   proposal distribution), one thread or one warp per walk.  The throughput mode.
+ * FG_MODE_LEARNED: the fast mode's walk stepped in lockstep over the batch so
+ *   that each step draws K candidate flips per walk, scores them with the
+ *   learned network (fg_set_proposal) and samples one.  Without a network, or
+ *   with K = 1, the proposal is the uniform one (K = 1 reproduces FG_MODE_FAST
+ *   exactly).  Z2 only, factors of at most 21 entries.  No reference
+ *   counterpart. */
+typedef enum { FG_MODE_REFERENCE = 0, FG_MODE_PHILOX_LISTS = 1, FG_MODE_FAST = 2, FG_MODE_LEARNED = 3 } fg_mode;
 
 /* Walk status bits (per walk). */
 enum { FG_WALK_RETRY = 2, FG_WALK_OVERFLOW = 4, FG_WALK_INTERNAL = 8 /* fast mode: pair counts inconsistent */ };
@@ -216,6 +222,23 @@ fg_status fg_mlp_score(fg_mlp *m, const uint64_t *features, int rows, float *sco
  * of 128) for `epochs` passes; *last_loss = mean loss of the last pass. */
 fg_status fg_mlp_train(fg_mlp *m, const uint64_t *features, const float *labels, int64_t n, int batch, int epochs,
                        float lr, uint64_t seed, float *last_loss);
+
+/* FG_MODE_LEARNED: proposal of the following launches.  `mlp` NULL = uniform
+ * choice among the candidates; candidates in [1, 16]; the sampling
+ * distribution is softmax(score / temperature), replaced by a uniform choice
+ * when its entropy (nats) is below min_entropy.  The network is borrowed
+ * (not owned) and must outlive its use. */
+fg_status fg_set_proposal(fg_handle *h, fg_mlp *mlp, int candidates, float temperature, float min_entropy);
+
+/* FG_MODE_LEARNED with one candidate: runs `launches` launches of plain
+ * (uniform-proposal) walks and logs every `every`-th accepted flip of each
+ * walk as a training record -- its 192 features and label 1 if the walk's
+ * rank dropped at that flip or within the next `horizon` accepted flips, else
+ * 0.  Records whose outcome the run did not see are dropped.  At most
+ * `capacity` records are logged; *count receives how many were written to
+ * features [count][3] and labels [count]. */
+fg_status fg_collect_records(fg_handle *h, int every, int horizon, int launches, int64_t capacity, uint64_t *features,
+                             float *labels, int64_t *count);
 
 /* Page-locked host buffers for fast record transfers (cudaHostAlloc). */
 fg_status fg_host_alloc(uint64_t bytes, void **out);
