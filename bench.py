@@ -38,7 +38,9 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 SHAPES = [(2, 2, 2), (2, 2, 3), (2, 3, 4), (3, 3, 4), (3, 4, 5), (4, 4, 4)]
-WORD_BYTES = 8  # factor word of the Z2 kernels (uint64 bitmasks)
+# factor word of the Z2 kernels: 32-bit in the fast mode (factors of <= 24 entries,
+# every shape here), 64-bit in the list modes
+WORD_BYTES = {"fast": 4, "philox": 8, "reference": 8}
 METRIC = "verified flips/s"
 CONFIG_NAME = "batched uneven Z2 search: 65,536 walks over (2,2,2),(2,2,3),(2,3,4),(3,3,4),(3,4,5),(4,4,4)"
 
@@ -255,7 +257,7 @@ def gpu_arm(args):
         mavg = 0.5 * (c["m"] + m_prev)
         m_prev = c["m"]
         f = c["flips"].astype(np.float64)
-        algo_bytes += float(np.sum(f * (2 * mavg + 4) * WORD_BYTES))
+        algo_bytes += float(np.sum(f * (2 * mavg + 4) * WORD_BYTES[args.mode]))
         for s, first, count in shape_ranges(walks):
             sel = slice(first, first + count)
             per_shape[s][0] += int(c["flips"][sel][c["valid"][sel]].sum())
@@ -296,6 +298,12 @@ def gpu_arm(args):
 
     smem_peak, peaks, sms, mhz = smem_peak_gbs()
     achieved = algo_bytes / (kern_ms / 1000.0) / 1e9
+    traffic = None
+    try:
+        with open(os.path.join(ROOT, "profiles", "bench_traffic.json")) as f:
+            traffic = json.load(f)["dram_bytes_per_step"]
+    except (OSError, KeyError, ValueError):
+        pass
     if rank == 0:
         cpu = cpu_baseline(args) if (ws == 1 and not args.no_cpu) else None
         line = {
@@ -312,9 +320,10 @@ def gpu_arm(args):
             "kernel_ms_per_step": kern_ms / args.steps, "verify_ms_per_step": ver_ms / args.steps,
             "gpu_launches": args.steps * (1 + (len(SHAPES) if args.mode == "fast" else 1)),
             "roofline": {"bound": "smem", "achieved": achieved, "peak": smem_peak, "unit": "GB/s",
-                         "frac": achieved / smem_peak, "traffic": None,
+                         "frac": achieved / smem_peak, "traffic": traffic,
+                         "traffic_note": "DRAM bytes of one step's walk launches (ncu capture, profiles/bench_launch_list.md)",
                          "peak_source": f"derived: 128 B/clk/SM x {sms} SMs x {mhz:.0f} MHz (sm_max_mhz, MEASURED_PEAKS.json)",
-                         "algorithmic_bytes": "per accepted flip (2m+4) x 8 B of shared-memory traffic"},
+                         "algorithmic_bytes": f"per accepted flip (2m+4) x {WORD_BYTES[args.mode]} B of shared-memory traffic"},
             "clocks": clk,
             "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "steps": args.e2e_steps},
@@ -363,6 +372,97 @@ def ttr_arm(args):
     return 0
 
 
+def learned_arm(args):
+    """Learned flip proposal against the uniform one on the same GPU.
+
+    1. Records: plain (uniform-proposal) walks from the naive schemes of (3,3,3), (3,4,5) and
+       (4,4,4) log every 16th accepted flip with label "rank dropped within the next 1000 flips",
+       until --learned-records labelled records exist.
+    2. Training: the 192-256-256-1 bf16 MLP on the tensor cores (Adam, --learned-epochs).
+    3. Held-out AUC of the scores (a uniform proposal scores 0.5).
+    4. Search: for (4,4,4) and (3,4,5), --learned-walks walks each from the naive scheme for
+       --learned-seconds seconds with the uniform proposal (fast mode) and with the learned one
+       (--learned-candidates candidates per step); flips/s and best verified rank.
+    5. Time to rank 23 on (3,3,3) (1,024 walks) with each proposal.
+    One JSON line per item."""
+    import flipgraphgpu_gb300 as fg
+    t0 = time.perf_counter()
+    shapes = [(3, 3, 3), (3, 4, 5), (4, 4, 4)]
+    per = 16384
+    sh = np.array([shapes[w // per] for w in range(per * len(shapes))], np.int32)
+    feats, labels = [], []
+    total, launches = 0, 0
+    with fg.Engine(len(sh), 64, "z2", "learned", args.seed, 2000, 50000, 0.01, 0.0) as eng:
+        eng.init_naive_shapes(sh)
+        while total < args.learned_records and launches < 64:
+            f, y = eng.collect_records(every=16, horizon=1000, launches=2, capacity=1 << 23)
+            feats.append(f)
+            labels.append(y)
+            total += len(y)
+            launches += 2
+    f = np.concatenate(feats)[:args.learned_records]
+    y = np.concatenate(labels)[:args.learned_records]
+    t_collect = time.perf_counter() - t0
+    perm = np.random.default_rng(args.seed).permutation(len(y))
+    f, y = f[perm], y[perm]
+    split = int(len(y) * 0.95)
+    net = fg.Mlp(seed=args.seed)
+    t1 = time.perf_counter()
+    loss = net.train(f[:split], y[:split], batch=8192, epochs=args.learned_epochs, lr=1e-3, seed=args.seed)
+    t_train = time.perf_counter() - t1
+    s = net.score(f[split:])
+    order = np.argsort(s, kind="stable")
+    ranks = np.empty(len(s))
+    ranks[order] = np.arange(len(s))
+    pos = y[split:] > 0
+    auc = float((ranks[pos].mean() - (pos.sum() - 1) / 2) / max((~pos).sum(), 1))
+    print(json.dumps({"workload": "learned proposal: records and training", "records": int(len(y)),
+                      "positive_fraction": float(y.mean()), "collect_seconds": t_collect, "train_seconds": t_train,
+                      "epochs": args.learned_epochs, "final_loss": loss, "heldout_auc": auc}))
+    sys.stdout.flush()
+
+    def search(shape, mode, walks, seconds, iters, target=None):
+        n1, n2, n3 = shape
+        eng = fg.Engine(walks, n1 * n2 * n3, "z2", mode, args.seed, iters, 50000, 0.01, 0.0)
+        if mode == "learned":
+            eng.set_proposal(net, candidates=args.learned_candidates, temperature=1.0, min_entropy=0.05)
+        eng.init_naive(n1, n2, n3)
+        t = time.perf_counter()
+        flips, kernel_ms, best, reached = 0, 0.0, n1 * n2 * n3, None
+        while time.perf_counter() - t < seconds:
+            st = eng.run(1)
+            flips += st["verified_flips"]
+            kernel_ms += st["kernel_ms"] + st["verify_ms"]
+            best = min(best, st["min_best_rank"])
+            if target is not None and best <= target:
+                c = eng.counters()
+                w = int(np.argmin(c["best_rank"]))
+                if eng.validate(best=True)[w]:
+                    reached = time.perf_counter() - t
+                    break
+        wall = time.perf_counter() - t
+        eng.close()
+        return {"flips_per_s": flips / max(kernel_ms / 1000, 1e-9), "best_rank": int(best), "seconds": wall,
+                "reached_seconds": reached}
+
+    for shape in ((4, 4, 4), (3, 4, 5)):
+        for mode in ("fast", "learned"):
+            iters = 1000 if mode == "fast" else 200
+            r = search(shape, mode, args.learned_walks, args.learned_seconds, iters)
+            print(json.dumps({"workload": f"search {shape[0]}x{shape[1]}x{shape[2]} Z2, {args.learned_walks} walks, "
+                                          f"{args.learned_seconds:.0f} s", "proposal": "uniform" if mode == "fast" else
+                              f"learned ({args.learned_candidates} candidates)", **r}))
+            sys.stdout.flush()
+    for mode in ("fast", "learned"):
+        r = search((3, 3, 3), mode, 1024, 60.0, 200, target=23)
+        print(json.dumps({"workload": "time to rank 23, 3x3x3 Z2, 1024 walks",
+                          "proposal": "uniform" if mode == "fast" else f"learned ({args.learned_candidates} candidates)",
+                          **r}))
+        sys.stdout.flush()
+    net.close()
+    return 0
+
+
 def zt_arm(args):
     """Ternary search: 16,384 walks per shape of (3,3,3) and (4,4,4) from the naive schemes,
     reference stream, exact integer verification; verified flips/s and ranks reached."""
@@ -402,7 +502,12 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--fast-split", type=int, default=None,
                     help="fast mode: one thread per walk up to this many slots, one warp per walk above")
-    ap.add_argument("--workload", default="batched", choices=["batched", "ttr", "zt"])
+    ap.add_argument("--workload", default="batched", choices=["batched", "ttr", "zt", "learned"])
+    ap.add_argument("--learned-records", type=int, default=10_000_000)
+    ap.add_argument("--learned-epochs", type=int, default=1)
+    ap.add_argument("--learned-walks", type=int, default=65536)
+    ap.add_argument("--learned-seconds", type=float, default=30.0)
+    ap.add_argument("--learned-candidates", type=int, default=8)
     ap.add_argument("--ttr-modes", default="fast,reference")
     ap.add_argument("--ttr-seconds", type=float, default=300.0)
     ap.add_argument("--ttr-shape", default="3x3x3")
@@ -419,6 +524,8 @@ def main():
         return ttr_arm(args)
     if args.workload == "zt":
         return zt_arm(args)
+    if args.workload == "learned":
+        return learned_arm(args)
     if args.impl == "reference":
         return reference_arm(args)
     return gpu_arm(args)

@@ -18,7 +18,9 @@ def main():
     ap.add_argument("--iterations", type=int, default=1000)
     ap.add_argument("--plus-iterations", type=int, default=100000)
     ap.add_argument("--launches", type=int, default=1)
-    ap.add_argument("--mode", default="fast", choices=["fast", "philox", "reference"])
+    ap.add_argument("--mode", default="fast", choices=["fast", "philox", "reference", "learned"])
+    ap.add_argument("--candidates", type=int, default=1,
+                    help="learned mode: candidates per step, scored by a freshly initialised network when > 1")
     ap.add_argument("--seed", type=int, default=3)
     ap.add_argument("--fast-split", type=int, default=None,
                     help="fast mode: one thread per walk up to this many slots, one warp per walk above")
@@ -27,9 +29,17 @@ def main():
     with Engine(a.walks, n[0] * n[1] * n[2], "z2", a.mode, a.seed, a.iterations, a.plus_iterations) as eng:
         if a.fast_split is not None:
             eng.set_fast_split(a.fast_split)
+        net = None
+        if a.mode == "learned" and a.candidates > 1:
+            from . import Mlp
+            net = Mlp(seed=a.seed)
+            eng.set_proposal(net, candidates=a.candidates)
         eng.init_naive(*n)
         eng.run(1)  # warm-up
         st = eng.run(a.launches)
+        if net is not None:
+            eng.set_proposal(None, candidates=1)
+            net.close()
     print(json.dumps({"shape": a.shape, "walks": a.walks, "iterations": a.iterations, "mode": a.mode,
                       "fast_split": a.fast_split, **st}))
 
