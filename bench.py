@@ -228,6 +228,8 @@ def gpu_arm(args):
                     args.walks_per_block)
     if args.fast_split is not None:
         eng.set_fast_split(args.fast_split)
+    if args.fast_kernel is not None:
+        eng.set_fast_kernel(args.fast_kernel, args.lanes)
     shapes = shapes_for(walks)
     eng.init_naive_shapes(shapes)
     for _ in range(args.warmup):
@@ -500,6 +502,9 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--ref-iterations", type=int, default=20000)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--fast-kernel", default=None, choices=["auto", "thread", "group", "warp"],
+                    help="fast mode: one kernel for every shape instead of the automatic choice")
+    ap.add_argument("--lanes", type=int, default=0, help="group kernel: lanes per walk (4, 8, 16; 0 = by slots)")
     ap.add_argument("--fast-split", type=int, default=None,
                     help="fast mode: one thread per walk up to this many slots, one warp per walk above")
     ap.add_argument("--workload", default="batched", choices=["batched", "ttr", "zt", "learned"])

@@ -216,6 +216,13 @@ class Engine:
                                            _ptr(f), _ptr(y), ctypes.byref(n)))
         return f[:n.value].copy(), y[:n.value].copy()
 
+    def set_fast_kernel(self, kernel, lanes=0):
+        """Fast mode kernel for every segment: 'thread', 'group' (lanes 4/8/16, 0 = auto),
+        'warp', or 'auto'.  Results are identical; only speed changes."""
+        kinds = {"auto": -1, "thread": 0, "group": 1, "warp": 2}
+        self.lib.fg_set_fast_kernel.restype = ctypes.c_int
+        _check(self.lib.fg_set_fast_kernel(self.h, kinds[kernel], int(lanes)))
+
     def set_fast_split(self, simt_max_cap):
         """Fast mode kernel choice (same results): -1 automatic, else one thread per walk up to
         this slot count and one warp per walk above."""

@@ -200,7 +200,8 @@ struct fg_handle {
     LearnedBuffers learned;
     LearnedConfig lcfg;
     fg_mlp *mlp = nullptr;
-    int simtMaxCap = -1;  // fast mode: -1 = automatic choice per segment, else thread per walk up to this slot count
+    int simtMaxCap = -1;
+    int fastKernel = -1, groupLanes = 0;  // fg_set_fast_kernel override  // fast mode: -1 = automatic choice per segment, else thread per walk up to this slot count
     DevBatch B{};
     WalkParams P{};
     int32_t *d_bestC = nullptr;
@@ -333,9 +334,14 @@ fg_status launch_walks(fg_handle *h) {
     for (const Segment &g : h->segs)
         if (g.nnmax > 56) return fail(FG_ERR_CAPACITY, "fast mode holds factors of at most 56 entries");
     auto launch = [&](const Segment &g, cudaStream_t st) {
-        const bool simt = h->simtMaxCap >= 0 ? g.scap <= h->simtMaxCap : thread_per_walk(g.scap, h->B.S, h->sms);
-        return simt ? launch_walk_simt(h->B, h->P, g.first, g.count, g.scap, g.wide, wpb, h->sms, st)
-                    : launch_walk_warpfast(h->B, h->P, g.first, g.count, g.scap, g.wide, h->sms, st);
+        int kind;
+        if (h->fastKernel >= 0) kind = h->fastKernel;
+        else if (h->simtMaxCap >= 0) kind = g.scap <= h->simtMaxCap ? FG_FAST_THREAD : FG_FAST_WARP;
+        else kind = thread_per_walk(g.scap, h->B.S, h->sms) ? FG_FAST_THREAD : FG_FAST_WARP;
+        if (kind == FG_FAST_THREAD) return launch_walk_simt(h->B, h->P, g.first, g.count, g.scap, g.wide, wpb, h->sms, st);
+        if (kind == FG_FAST_GROUP)
+            return launch_walk_group(h->B, h->P, g.first, g.count, g.scap, g.wide, h->groupLanes, h->sms, st);
+        return launch_walk_warpfast(h->B, h->P, g.first, g.count, g.scap, g.wide, h->sms, st);
     };
     if (h->segs.size() == 1) {
         FG_CUDA(launch(h->segs[0], h->stream));
@@ -533,6 +539,14 @@ fg_status fg_collect_records(fg_handle *h, int every, int horizon, int launches,
     std::copy(f.begin(), f.begin() + n * 3, features);
     std::copy(y.begin(), y.begin() + n, labels);
     *count = (int64_t)n;
+    return FG_OK;
+}
+
+fg_status fg_set_fast_kernel(fg_handle *h, int kernel, int lanes) {
+    if (!h || kernel < -1 || kernel > FG_FAST_WARP || !(lanes == 0 || lanes == 4 || lanes == 8 || lanes == 16))
+        return fail(FG_ERR_ARG, "kernel in -1..2, lanes 0, 4, 8 or 16");
+    h->fastKernel = kernel;
+    h->groupLanes = lanes;
     return FG_OK;
 }
 

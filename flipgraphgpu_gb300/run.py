@@ -22,6 +22,8 @@ def main():
     ap.add_argument("--candidates", type=int, default=1,
                     help="learned mode: candidates per step, scored by a freshly initialised network when > 1")
     ap.add_argument("--seed", type=int, default=3)
+    ap.add_argument("--fast-kernel", default=None, choices=["auto", "thread", "group", "warp"])
+    ap.add_argument("--lanes", type=int, default=0, help="group kernel: lanes per walk (4, 8, 16; 0 = auto)")
     ap.add_argument("--fast-split", type=int, default=None,
                     help="fast mode: one thread per walk up to this many slots, one warp per walk above")
     a = ap.parse_args()
@@ -29,6 +31,8 @@ def main():
     with Engine(a.walks, n[0] * n[1] * n[2], "z2", a.mode, a.seed, a.iterations, a.plus_iterations) as eng:
         if a.fast_split is not None:
             eng.set_fast_split(a.fast_split)
+        if a.fast_kernel is not None:
+            eng.set_fast_kernel(a.fast_kernel, a.lanes)
         net = None
         if a.mode == "learned" and a.candidates > 1:
             from . import Mlp
@@ -41,7 +45,7 @@ def main():
             eng.set_proposal(None, candidates=1)
             net.close()
     print(json.dumps({"shape": a.shape, "walks": a.walks, "iterations": a.iterations, "mode": a.mode,
-                      "fast_split": a.fast_split, **st}))
+                      "fast_split": a.fast_split, "fast_kernel": a.fast_kernel, "lanes": a.lanes, **st}))
 
 
 if __name__ == "__main__":

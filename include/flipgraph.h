@@ -185,6 +185,14 @@ fg_status fg_get_scheme(fg_handle *h, int walk, int best, int32_t *n, int32_t *m
  * warp per walk above (0 = always warp, a large n = always thread). */
 fg_status fg_set_fast_split(fg_handle *h, int simt_max_cap);
 
+/* Fast mode kernel for every segment, overriding the automatic choice:
+ * FG_FAST_THREAD (one thread per walk), FG_FAST_GROUP (`lanes` = 4, 8 or 16
+ * lanes per walk; 0 = by slot count, widened when the slots need it),
+ * FG_FAST_WARP (one warp per walk); -1 restores the automatic choice.  All
+ * three give identical results. */
+enum { FG_FAST_THREAD = 0, FG_FAST_GROUP = 1, FG_FAST_WARP = 2 };
+fg_status fg_set_fast_kernel(fg_handle *h, int kernel, int lanes);
+
 /* Tensor-core (tcgen05) bf16 GEMM of the learned proposal's MLP, on host
  * buffers (test and support entry; no reference counterpart):
  *   D[M][N] = A[M][K] * B[N][K]^T, A and B bf16 bit patterns, row-major;

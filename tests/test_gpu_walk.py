@@ -147,9 +147,11 @@ def test_minimize_vs_oracle(ring, shape):
     ([(2, 4, 8)], 600, 200, 0.01, 0.0),   # nn = 8 x 32 x 16: 64-bit words
     ([(4, 5, 8)], 300, 200, 0.01, 0.0),   # nn = 20 x 40 x 32, cap 160
 ])
-@pytest.mark.parametrize("split", [None, 0, 1000], ids=["auto", "warp", "thread"])
-def test_walk_fast_mode_vs_oracle(shapes, iters, plus, expand_p, reduce_p, split):
-    """Fast mode runs one thread per walk or one warp per walk; both follow the oracle exactly."""
+@pytest.mark.parametrize("kernel,lanes", [("auto", 0), ("thread", 0), ("group", 4), ("group", 8), ("group", 16),
+                                          ("warp", 0)],
+                         ids=["auto", "thread", "group4", "group8", "group16", "warp"])
+def test_walk_fast_mode_vs_oracle(shapes, iters, plus, expand_p, reduce_p, kernel, lanes):
+    """Fast mode runs one thread, a group of lanes or one warp per walk; all follow the oracle exactly."""
     per = 40
     S = per * len(shapes)
     cap = max(a * b * c for a, b, c in shapes)
@@ -157,8 +159,7 @@ def test_walk_fast_mode_vs_oracle(shapes, iters, plus, expand_p, reduce_p, split
     seed = 9001 + len(shapes)
     kw = dict(iterations=iters, plus_iterations=plus, expand_p=expand_p, reduce_p=reduce_p, seed=seed)
     with fg.Engine(S, cap, "z2", "fast", seed, iters, plus, expand_p, reduce_p) as eng:
-        if split is not None:
-            eng.set_fast_split(split)
+        eng.set_fast_kernel(kernel, lanes)
         eng.init_naive_shapes(sh)
         rec0 = eng.records()
         st = eng.run(2)
