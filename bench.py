@@ -465,6 +465,90 @@ def learned_arm(args):
     return 0
 
 
+def post_arm(args):
+    """Post-search workload on --post-schemes Z2 schemes of 4x4x4.
+
+    1. Search (config 1's method): 65,536 fast-mode walks of 4x4x4 from the naive scheme for
+       --post-search-seconds; the --post-schemes walks with the lowest verified best rank are kept
+       (ranks 47-50 typically).
+    2. Complexity minimizer: rank-preserving flip walks (philox-lists mode) on those schemes,
+       --post-launches launches of --post-iterations steps; flips/s and complexities.
+    3. Additions reducer: --post-reducers reducers per scheme on the minimized schemes, one GPU
+       launch per rank group; reducer runs/s and addition counts.
+    The addition counts are the reference's for the same scheme and seed (tests/test_gpu_reducer.py
+    checks 32 reducers on the rank-47 scheme of tests/golden against the reference kernel)."""
+    import flipgraphgpu_gb300 as fg
+    log = lambda msg: print(f"[post] {msg}", file=sys.stderr, flush=True)  # noqa: E731
+    n, cap, S = (4, 4, 4), 64, args.post_schemes
+    nn = [n[0] * n[1], n[1] * n[2], n[2] * n[0]]
+    t = time.perf_counter()
+    with fg.Engine(65536, cap, "z2", "fast", args.seed, 5000, 100000, 0.01, 0.0) as search:
+        search.init_naive(*n)
+        while time.perf_counter() - t < args.post_search_seconds:
+            search.run(1)
+        full = search.records()
+        ok = search.validate(best=True)
+    t_search = time.perf_counter() - t
+    order = np.lexsort((np.arange(len(ok)), full.best_m + 1000 * (~ok)))[:S]
+    ranks = full.best_m[order]
+    log(f"search {t_search:.1f} s; ranks kept {np.unique(ranks, return_counts=True)}")
+    rec = fg.Records(S, cap, "z2")
+    rec.n[:] = n
+    rec.m[:] = ranks
+    rec.fac[:] = full.best_fac[order]
+    rec.best_fac[:] = rec.fac
+    rec.best_rank[:] = ranks
+    rec.best_m[:] = ranks
+    c0 = np.array([sum(bin(int(x)).count("1") for x in rec.fac[w, :, :ranks[w]].ravel()) for w in range(S)],
+                  np.int64) - 2 * ranks - nn[2]
+    eng = fg.Engine(S, cap, "z2", "philox", args.seed, args.post_iterations, 10**9, 0.0, 0.0)
+    eng.set_records(rec)
+    eng.rebuild_lists()
+    bc = c0.astype(np.int32)
+    bc = eng.minimize(bc)  # first launch (warm-up, counted in the complexities)
+    t = time.perf_counter()
+    flips = 0
+    for _ in range(args.post_launches):
+        bc = eng.minimize(bc)
+        flips += int(eng.counters()["flips"].sum())
+    t_min = time.perf_counter() - t
+    rec = eng.records()
+    ok = eng.validate(best=True)
+    eng.close()
+    log(f"minimizer {t_min:.2f} s, {flips} flips")
+    runs, t_red, best_adds, naive_adds = 0, 0.0, [], []
+    for m in np.unique(ranks):
+        sel = np.nonzero(ranks == m)[0]
+        coef = np.zeros((len(sel), 3, m, 64), np.int8)
+        for c in range(3):
+            bits = (rec.best_fac[sel][:, c, :m, None] >> np.arange(64, dtype=np.uint64)[None, None, :]) & np.uint64(1)
+            coef[:, c, :, :nn[c]] = bits[:, :, :nn[c]].astype(np.int8)
+        R = args.post_reducers
+        red = fg.Reducer(n, int(m), coef, count=len(sel) * R, schemes=len(sel), seed=args.seed)
+        tt = time.perf_counter()
+        out = red.run()
+        t_red += time.perf_counter() - tt
+        red.close()
+        runs += len(sel) * R
+        adds = out["additions"].sum(axis=1).reshape(R, len(sel))  # reducer r reduces scheme r % schemes
+        best_adds.append(adds.min(axis=0))
+        naive_adds.append(out["naive"].sum(axis=1)[:len(sel)])
+        log(f"rank {m}: {len(sel)} schemes, reducer total {t_red:.2f} s")
+    best_adds, naive_adds = np.concatenate(best_adds), np.concatenate(naive_adds)
+    print(json.dumps({
+        "workload": f"post-search: complexity minimizer + additions reducer on {S} Z2 schemes of 4x4x4",
+        "search_seconds": t_search, "ranks": {int(k): int(v) for k, v in zip(*np.unique(ranks, return_counts=True))},
+        "schemes_valid": int(ok.sum()), "schemes_distinct": len({rec.best_fac[w].tobytes() for w in range(S)}),
+        "minimizer": {"flips_per_s": flips / t_min if t_min > 0 else None, "flips": flips, "seconds": t_min,
+                      "iterations": args.post_iterations, "launches": args.post_launches,
+                      "complexity_start_mean": float(c0.mean()), "complexity_best_mean": float(bc.mean()),
+                      "complexity_best_min": int(bc.min())},
+        "reducer": {"runs": runs, "runs_per_s": runs / t_red, "seconds": t_red, "reducers_per_scheme": args.post_reducers,
+                    "naive_additions_mean": float(naive_adds.mean()), "best_additions_mean": float(best_adds.mean()),
+                    "best_additions_min": int(best_adds.min())}}))
+    return 0
+
+
 def zt_arm(args):
     """Ternary search: 16,384 walks per shape of (3,3,3) and (4,4,4) from the naive schemes,
     reference stream, exact integer verification; verified flips/s and ranks reached."""
@@ -507,7 +591,12 @@ def main():
     ap.add_argument("--lanes", type=int, default=0, help="group kernel: lanes per walk (4, 8, 16; 0 = by slots)")
     ap.add_argument("--fast-split", type=int, default=None,
                     help="fast mode: one thread per walk up to this many slots, one warp per walk above")
-    ap.add_argument("--workload", default="batched", choices=["batched", "ttr", "zt", "learned"])
+    ap.add_argument("--workload", default="batched", choices=["batched", "ttr", "zt", "learned", "post"])
+    ap.add_argument("--post-schemes", type=int, default=4096)
+    ap.add_argument("--post-iterations", type=int, default=2000)
+    ap.add_argument("--post-launches", type=int, default=3)
+    ap.add_argument("--post-reducers", type=int, default=32)
+    ap.add_argument("--post-search-seconds", type=float, default=60.0)
     ap.add_argument("--learned-records", type=int, default=10_000_000)
     ap.add_argument("--learned-epochs", type=int, default=1)
     ap.add_argument("--learned-walks", type=int, default=65536)
@@ -531,6 +620,8 @@ def main():
         return zt_arm(args)
     if args.workload == "learned":
         return learned_arm(args)
+    if args.workload == "post":
+        return post_arm(args)
     if args.impl == "reference":
         return reference_arm(args)
     return gpu_arm(args)

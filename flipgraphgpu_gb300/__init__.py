@@ -216,6 +216,11 @@ class Engine:
                                            _ptr(f), _ptr(y), ctypes.byref(n)))
         return f[:n.value].copy(), y[:n.value].copy()
 
+    def rebuild_lists(self):
+        """List modes: rebuild the FlipSet lists from the current factors (initFlips order)."""
+        self.lib.fg_rebuild_lists.restype = ctypes.c_int
+        _check(self.lib.fg_rebuild_lists(self.h))
+
     def set_fast_kernel(self, kernel, lanes=0):
         """Fast mode kernel for every segment: 'thread', 'group' (lanes 4/8/16, 0 = auto),
         'warp', or 'auto'.  Results are identical; only speed changes."""

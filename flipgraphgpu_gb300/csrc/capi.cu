@@ -542,6 +542,15 @@ fg_status fg_collect_records(fg_handle *h, int every, int horizon, int launches,
     return FG_OK;
 }
 
+fg_status fg_rebuild_lists(fg_handle *h) {
+    if (!h) return fail(FG_ERR_ARG, "null handle");
+    if (!h->ready) return fail(FG_ERR_STATE, "records not initialised");
+    FG_CUDA(cudaSetDevice(h->dev));
+    if (uses_lists(h)) FG_CUDA(launch_rebuild(h->cfg.ring, h->B, h->wpb, h->grid, h->stream));
+    FG_CUDA(cudaStreamSynchronize(h->stream));
+    return FG_OK;
+}
+
 fg_status fg_set_fast_kernel(fg_handle *h, int kernel, int lanes) {
     if (!h || kernel < -1 || kernel > FG_FAST_WARP || !(lanes == 0 || lanes == 4 || lanes == 8 || lanes == 16))
         return fail(FG_ERR_ARG, "kernel in -1..2, lanes 0, 4, 8 or 16");

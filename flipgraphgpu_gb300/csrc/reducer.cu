@@ -175,20 +175,40 @@ __device__ int count_pairs(RedSmem &sm, RedState &st, const ReduceDims &D, int L
     for (int q = threadIdx.x; q < T; q += blockDim.x)
         if (sm.hkey[q] != 0xFFFFFFFFu) sm.byfirst[sm.hfirst[q]] = q;
     __syncthreads();
-    // Distinct pairs in first-occurrence order (= PairsCounter insertion order), capped.
-    if (threadIdx.x == 0) {
-        int d = 0, maxCount = 0;
-        for (int q = 0; q < N; q++) {
-            int slot = sm.byfirst[q];
-            if (slot < 0) continue;
-            if (d >= st.maxPairs) break;
-            uint32_t k = sm.hkey[slot];
-            sm.pi[d] = key_i(k);
-            sm.pj[d] = key_j(k);
-            sm.pc[d] = sm.hcnt[slot];
-            if (sm.pc[d] > maxCount) maxCount = sm.pc[d];
-            d++;
+    // Distinct pairs in first-occurrence order (= PairsCounter insertion order), capped:
+    // a block-wide stream compaction of the occurrences that first saw a pair.
+    int d0 = 0, localMax = 0;
+    const int warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int base = 0; base < N; base += blockDim.x) {
+        const int q = base + threadIdx.x;
+        const int slot = q < N ? sm.byfirst[q] : -1;
+        const unsigned bal = __ballot_sync(kFull, slot >= 0);
+        __syncthreads();
+        if (lane_id() == 0) scratch[warp] = __popc(bal);
+        __syncthreads();
+        int before = d0;
+        for (int w = 0; w < warp; w++) before += scratch[w];
+        int total = 0;
+        for (int w = 0; w < nw; w++) total += scratch[w];
+        if (slot >= 0) {
+            const int d = before + __popc(bal & lanemask_lt());
+            if (d < st.maxPairs) {
+                const uint32_t k = sm.hkey[slot];
+                sm.pi[d] = key_i(k);
+                sm.pj[d] = key_j(k);
+                sm.pc[d] = sm.hcnt[slot];
+                if (sm.pc[d] > localMax) localMax = sm.pc[d];
+            }
         }
+        d0 += total;
+    }
+    for (int dd = 16; dd; dd >>= 1) localMax = max(localMax, __shfl_xor_sync(kFull, localMax, dd));
+    __syncthreads();
+    if (lane_id() == 0) scratch[warp] = localMax;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int d = d0 < st.maxPairs ? d0 : st.maxPairs, maxCount = 0;
+        for (int w = 0; w < nw; w++) maxCount = max(maxCount, scratch[w]);
         // sort(): move max-count pairs to the front by swapping, then drop count-1 pairs.
         int top = 0, size = d;
         if (maxCount >= 2) {
@@ -218,6 +238,85 @@ __device__ int count_pairs(RedSmem &sm, RedState &st, const ReduceDims &D, int L
     int mc = scratch[34];
     __syncthreads();
     return mc;
+}
+
+// Greedy-intersections choice (pairs_counter.cuh:148-176) by the whole block.  The
+// serial loop visits (i, j) in order and draws once per intersecting pair; here
+// every thread scores a contiguous range of rows i in that same inner order,
+// starting its copy of the reducer's XORWOW stream at the draw the serial loop
+// would be at (prefix over the rows' intersecting-pair counts, then cuRAND's
+// skipahead), and the first row with the largest score wins, as in the serial
+// strict-greater scan.  The reducer's own stream then advances by all the draws.
+__device__ int select_gi(const RedSmem &sm, float scale, int size, XorwowDraws &r, int *rowCnt, int *scratch) {
+    __shared__ curandStateXORWOW_t base;
+    __shared__ float wbest[32];
+    __shared__ int widx[32], wtot[32];
+    const int tid = threadIdx.x, nt = blockDim.x, warp = tid >> 5, nw = nt >> 5;
+    for (int i = tid; i < size; i += nt) {
+        const int ai = sm.pi[i], aj = sm.pj[i];
+        int cnt = 0;
+        for (int j = 0; j < size; j++) cnt += (j != i) & intersects(ai, aj, sm.pi[j], sm.pj[j]);
+        rowCnt[i] = cnt;
+    }
+    __syncthreads();
+    const int per = (size + nt - 1) / nt;
+    const int lo = min(size, tid * per), hi = min(size, lo + per);
+    int local = 0;
+    for (int i = lo; i < hi; i++) local += rowCnt[i];
+    int incl = local;  // inclusive scan over threads (ranges are in thread order)
+    for (int d = 1; d < 32; d <<= 1) {
+        const int o = __shfl_up_sync(kFull, incl, d);
+        if (lane_id() >= d) incl += o;
+    }
+    if (lane_id() == 31) wtot[warp] = incl;
+    if (tid == 0) base = r.st;
+    __syncthreads();
+    int start = incl - local, total = 0;
+    for (int w = 0; w < nw; w++) {
+        if (w < warp) start += wtot[w];
+        total += wtot[w];
+    }
+    curandStateXORWOW_t s = base;
+    if (start > 0) skipahead((unsigned long long)start, &s);
+    float myBest = 0.0f;
+    int myIdx = -1;
+    for (int i = lo; i < hi; i++) {
+        const int ai = sm.pi[i], aj = sm.pj[i];
+        float inter = 0;
+        for (int j = 0; j < size; j++) {
+            if (i == j) continue;
+            if (!intersects(ai, aj, sm.pi[j], sm.pj[j])) {
+                inter += (float)(sm.pc[j] - 1);
+            } else if (!(curand(&s) % 2)) {
+                inter = (float)__fma_rn(0.69, (double)sm.pc[j], (double)inter);
+            }
+        }
+        const float score = __fmaf_rn(scale, inter, (float)(sm.pc[i] - 1));
+        if (score > myBest) { myBest = score; myIdx = i; }
+    }
+    // block arg-max: larger score first, then the smaller row
+    for (int d = 16; d; d >>= 1) {
+        const float os = __shfl_xor_sync(kFull, myBest, d);
+        const int oi = __shfl_xor_sync(kFull, myIdx, d);
+        if (oi >= 0 && (myIdx < 0 || os > myBest || (os == myBest && oi < myIdx))) { myBest = os; myIdx = oi; }
+    }
+    if (lane_id() == 0) { wbest[warp] = myBest; widx[warp] = myIdx; }
+    __syncthreads();
+    int imax = 0;
+    if (tid == 0) {
+        float b = 0.0f;
+        int bi = -1;
+        for (int w = 0; w < nw; w++)
+            if (widx[w] >= 0 && (bi < 0 || wbest[w] > b || (wbest[w] == b && widx[w] < bi))) { b = wbest[w]; bi = widx[w]; }
+        imax = bi < 0 ? 0 : bi;
+        if (total > 0) skipahead((unsigned long long)total, &r.st);
+        r.count += (uint64_t)total;
+        scratch[38] = imax;
+    }
+    __syncthreads();
+    imax = scratch[38];
+    __syncthreads();
+    return imax;
 }
 
 // selectSubexpression (additions_reducer.cuh:272-289) on thread 0; returns the pair index.
@@ -359,8 +458,19 @@ __global__ void k_reduce(ReduceArgs A) {
             int maxCount = count_pairs(sm, st, D, L, &size, &top, scratch);
             if (!(size > 0 && maxCount > 1)) break;
             if (threadIdx.x == 0) {
-                int md = st.mode == MIX ? (int)(r.raw() % MIX) : st.mode;
-                int k = select_pair(sm, st, md, size, top, r);
+                scratch[37] = st.mode == MIX ? (int)(r.raw() % MIX) : st.mode;
+                scratch[39] = __float_as_int(st.scale);
+            }
+            __syncthreads();
+            const int md = scratch[37];
+            if (md == GREEDY_INTER) {
+                const int k = select_gi(sm, __int_as_float(scratch[39]), size, r, sm.byfirst, scratch);
+                if (threadIdx.x == 0) {
+                    scratch[35] = sm.pi[k];
+                    scratch[36] = sm.pj[k];
+                }
+            } else if (threadIdx.x == 0) {
+                const int k = select_pair(sm, st, md, size, top, r);
                 scratch[35] = sm.pi[k];
                 scratch[36] = sm.pj[k];
             }

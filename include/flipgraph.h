@@ -185,6 +185,11 @@ fg_status fg_get_scheme(fg_handle *h, int walk, int best, int32_t *n, int32_t *m
  * warp per walk above (0 = always warp, a large n = always thread). */
 fg_status fg_set_fast_split(fg_handle *h, int simt_max_cap);
 
+/* List modes: rebuilds every walk's three FlipSet lists from its current
+ * factors in the reference's initFlips order (scheme_z2.cu:166-175) -- for
+ * records set with empty lists.  A no-op in the fast and learned modes. */
+fg_status fg_rebuild_lists(fg_handle *h);
+
 /* Fast mode kernel for every segment, overriding the automatic choice:
  * FG_FAST_THREAD (one thread per walk), FG_FAST_GROUP (`lanes` = 4, 8 or 16
  * lanes per walk; 0 = by slot count, widened when the slots need it),

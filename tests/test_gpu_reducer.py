@@ -73,3 +73,23 @@ def test_reducer_two_iterations_vs_oracle(ring, seed, independent):
         assert np.array_equal(o[:, 1::3], g["fresh"])
         assert np.array_equal(o[:, 2::3], g["naive"])
         assert np.array_equal(c, g["draws"])
+
+
+@pytest.mark.parametrize("seed", [5, 6])
+def test_reducer_matches_reference_on_444_rank47(seed):
+    """32 reducers on a 4x4x4 Z2 scheme of rank 47 (the config the post-search benchmark runs):
+    additions, fresh variables, naive counts and modes equal the reference kernel's, including the
+    greedy-intersections reducers whose scores the GPU computes block-parallel."""
+    import json
+    with open(golden("scheme_444_z2_r47.txt")) as f:
+        n, m, coef = read_scheme_text(f.read())
+    with open(golden("reduce_444_r47.json")) as f:
+        ref = json.load(f)["seeds"][str(seed)]
+    red = fg.Reducer(n, m, coef[None], count=len(ref), schemes=1, seed=seed)
+    out = red.run(independent=True)
+    red.close()
+    for r, want in enumerate(ref):
+        got = [[int(out[k][r, c]) for k in ("additions", "fresh", "naive")] for c in range(3)]
+        assert got == [want["u"], want["v"], want["w"]], r
+        names = [fg.mode_name(out["mode"][r, c], out["scale"][r, c]) for c in range(3)]
+        assert names == want["modes"], r
