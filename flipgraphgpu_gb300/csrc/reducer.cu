@@ -11,6 +11,7 @@
 // reference's PairsCounter stores them in.  The reference's partial sort
 // (pairs_counter.cuh:73-101), the selection modes and every draw run on one
 // thread, so the XORWOW stream is consumed exactly as the reference does.
+#include <algorithm>
 #include <cstdint>
 #include <mutex>
 #include <vector>
@@ -370,19 +371,18 @@ struct ReduceArgs {
     float *out_scale;                // [count][3]
     int16_t *out_vars;               // [count][3][500][2] or null
     ReduceDims D;
+    unsigned char *gscratch;         // non-null: per-block tables in global memory (slotBytes each)
+    size_t slotBytes;
 };
 
-__global__ void k_reduce(ReduceArgs A) {
-    extern __shared__ __align__(16) unsigned char smem[];
-    __shared__ int scratch[40];
-    const int idx = blockIdx.x;
-    if (idx >= A.count) return;
+// One reducer (runReducersKernel body for reducer idx); its pair tables start at `base`.
+__device__ void reduce_one(const ReduceArgs &A, int idx, unsigned char *base, int *scratch) {
     const ReduceDims &D = A.D;
     const int Lmax = max(D.L[0], max(D.L[1], D.L[2]));
     const int Emax = max(D.E[0], max(D.E[1], D.E[2]));
     const int T = 1 << D.tbits;
     RedSmem sm;
-    unsigned char *p = smem;
+    unsigned char *p = base;
     sm.hkey = reinterpret_cast<uint32_t *>(p); p += 4 * (size_t)T;
     sm.hcnt = reinterpret_cast<int *>(p); p += 4 * (size_t)T;
     sm.hfirst = reinterpret_cast<int *>(p); p += 4 * (size_t)T;
@@ -502,6 +502,18 @@ __global__ void k_reduce(ReduceArgs A) {
     (void)scales;
 }
 
+// Reducers blockIdx.x, blockIdx.x + gridDim.x, ...; tables in dynamic shared memory, or in
+// this block's global scratch slot when they do not fit on chip.
+__global__ void k_reduce(ReduceArgs A) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ int scratch[40];
+    unsigned char *base = A.gscratch ? A.gscratch + (size_t)blockIdx.x * A.slotBytes : smem;
+    for (int idx = blockIdx.x; idx < A.count; idx += gridDim.x) {
+        reduce_one(A, idx, base, scratch);
+        __syncthreads();
+    }
+}
+
 __global__ void k_seed_reducers(curandStateXORWOW_t *st, int count, unsigned long long seed) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < count) curand_init(seed, (unsigned long long)i, 0ull, &st[i]);  // scheme_additions_reducer.cu:445
@@ -523,6 +535,9 @@ struct fg_reducer {
     float *d_scale = nullptr;
     int16_t *d_vars = nullptr;
     size_t smem = 0;
+    unsigned char *d_scratch = nullptr;  // global-memory tables when they exceed shared memory
+    size_t slotBytes = 0;
+    int slots = 0;
 };
 
 namespace {
@@ -581,7 +596,18 @@ fg_status fg_reducer_create(const fg_reducer_config *cfg, int n1, int n2, int n3
     int dev = cfg->device, optin = 0;
     if (cudaSetDevice(dev) != cudaSuccess) { delete h; return rfail(FG_ERR_CUDA, "cudaSetDevice failed"); }
     cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-    if (h->smem > (size_t)optin) { delete h; return rfail(FG_ERR_CAPACITY, "scheme too large for the shared-memory reducer"); }
+    if (h->smem > (size_t)optin) {
+        // Tables in global memory (L2-resident per block), blocks loop over the reducers.
+        int sms = 0;
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        h->slotBytes = (h->smem + 255) / 256 * 256;
+        h->slots = std::min(cfg->count, 4 * (sms > 0 ? sms : 1));
+        h->smem = 0;
+        if (cudaMalloc(&h->d_scratch, h->slotBytes * h->slots) != cudaSuccess) {
+            delete h;
+            return rfail(FG_ERR_CAPACITY, "scheme too large for the reducer's global tables");
+        }
+    }
     size_t ncoef = (size_t)cfg->schemes * 3 * m * 64;
     cudaError_t e = cudaMalloc(&h->d_coef, ncoef);
     if (e == cudaSuccess) e = cudaMemcpy(h->d_coef, coef, ncoef, cudaMemcpyHostToDevice);
@@ -594,7 +620,8 @@ fg_status fg_reducer_create(const fg_reducer_config *cfg, int n1, int n2, int n3
         k_seed_reducers<<<(cfg->count + 127) / 128, 128>>>(h->d_states, cfg->count, (unsigned long long)cfg->seed);
         e = cudaGetLastError();
     }
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_reduce, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)h->smem);
+    if (e == cudaSuccess && h->smem)
+        e = cudaFuncSetAttribute(k_reduce, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)h->smem);
     if (e == cudaSuccess) e = cudaDeviceSynchronize();
     if (e != cudaSuccess) {
         fg_reducer_destroy(h);
@@ -627,7 +654,9 @@ fg_status fg_reducer_run(fg_reducer *h, int independent, const int32_t *best_fre
     A.out_scale = h->d_scale;
     A.out_vars = h->d_vars;
     A.D = h->D;
-    k_reduce<<<A.count, 128, h->smem>>>(A);
+    A.gscratch = h->d_scratch;
+    A.slotBytes = h->slotBytes;
+    k_reduce<<<h->d_scratch ? h->slots : A.count, 128, h->smem>>>(A);
     RCUDA(cudaGetLastError());
     RCUDA(cudaMemcpy(out_counts, h->d_out, 4 * 13 * (size_t)A.count, cudaMemcpyDeviceToHost));
     if (out_scale) RCUDA(cudaMemcpy(out_scale, h->d_scale, 4 * 3 * (size_t)A.count, cudaMemcpyDeviceToHost));
@@ -641,7 +670,7 @@ fg_status fg_reducer_run(fg_reducer *h, int independent, const int32_t *best_fre
 
 fg_status fg_reducer_destroy(fg_reducer *h) {
     if (!h) return FG_OK;
-    void *ptrs[] = {h->d_coef, h->d_states, h->d_best, h->d_out, h->d_scale, h->d_vars};
+    void *ptrs[] = {h->d_coef, h->d_states, h->d_best, h->d_out, h->d_scale, h->d_vars, h->d_scratch};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     delete h;
@@ -777,6 +806,8 @@ fg_status fg_reducer_run_noalloc(const fg_reducer_config *cfg, int n1, int n2, i
     A.out_scale = reinterpret_cast<float *>(base + oScale);
     A.out_vars = nullptr;
     A.D = D;
+    A.gscratch = nullptr;
+    A.slotBytes = 0;
     k_reduce<<<A.count, 128, smem>>>(A);
     RCUDA(cudaGetLastError());
     RCUDA(cudaMemcpy(out_counts, base + oOut, (size_t)4 * 13 * A.count, cudaMemcpyDeviceToHost));

@@ -93,3 +93,24 @@ def test_reducer_matches_reference_on_444_rank47(seed):
         assert got == [want["u"], want["v"], want["w"]], r
         names = [fg.mode_name(out["mode"][r, c], out["scale"][r, c]) for c in range(3)]
         assert names == want["modes"], r
+
+
+def test_reducer_with_tables_in_global_memory_vs_oracle():
+    """Dense expressions whose pair tables exceed shared memory (the reducer then keeps them in
+    global memory, blocks looping over reducers): results and draw counts equal the oracle's."""
+    rng = np.random.default_rng(21)
+    n, m = (4, 4, 4), 48
+    coef = np.zeros((3, m, 64), np.int8)
+    for c in range(3):
+        coef[c, :, :16] = (rng.random((m, 16)) < 0.5).astype(np.int8)
+    coef[:, :, :16][coef[:, :, :16].sum(axis=2) == 0] = 1
+    count, seed = 6, 12
+    red = fg.Reducer(n, m, coef[None], count=count, schemes=1, seed=seed)
+    out = red.run(independent=True)
+    red.close()
+    draws, unis = fg.xorwow_tape(seed, 0, count, int(out["draws"].max()))
+    o, _, c = oracle_run(n, m, coef, count, draws, unis, np.zeros(count, np.int64), out["draws"], True)
+    assert np.array_equal(o[:, 0::3], out["additions"])
+    assert np.array_equal(o[:, 1::3], out["fresh"])
+    assert np.array_equal(o[:, 2::3], out["naive"])
+    assert np.array_equal(c, out["draws"])
