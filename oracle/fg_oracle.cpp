@@ -30,6 +30,8 @@
 #include <cstdlib>
 #include <cstring>
 #include <cmath>
+#include <map>
+#include <string>
 #include <unordered_map>
 #include <vector>
 
@@ -38,6 +40,8 @@ namespace {
 constexpr int kMaxRank = 350;   // config.cuh:10
 constexpr int kMaxPairs = 500;  // config.cuh:14
 constexpr int kRetryCap = 1 << 20;
+constexpr int kMaxMatrix = 64;      // config.cuh:11 (64-bit factors)
+constexpr int kMaxExtensionN = 16;  // config.cuh:37
 enum { ST_TAPE = 1, ST_RETRY = 2, ST_OVERFLOW = 4 };
 
 inline int popc64(uint64_t x) { return __builtin_popcountll(x); }
@@ -393,6 +397,262 @@ struct Z2 {
         for (int t = 0; t < m; t++)
             for (int c = 0; c < 3; c++) count += popc64(x[c][t]);
         return count - 2 * m - nn[2];
+    }
+
+    // ---------------------------------------------------------------- resize
+    // Meta-operators that change the matrix sizes (scheme_z2.cu:184-310,
+    // 643-979, 1165-1275).  Matrix c is n[c] x n[c+1] (W transposed), entry
+    // (i, j) at bit i * n[c+1] + j.
+    void setN(int a, int b, int c) {
+        n[0] = a; n[1] = b; n[2] = c;
+        for (int q = 0; q < 3; q++) nn[q] = n[q] * n[(q + 1) % 3];
+    }
+    static uint64_t bit(uint64_t v, int k) { return (v >> k) & 1ull; }
+
+    void excludeRow(int c, int row) {  // scheme_z2.cu:205-224
+        const int r = n[c], cols = n[(c + 1) % 3];
+        for (int t = 0; t < m; t++) {
+            uint64_t v = 0;
+            for (int i = 0, i2 = 0; i < r; i++) {
+                if (i == row) continue;
+                for (int j = 0; j < cols; j++) v |= bit(x[c][t], i * cols + j) << (i2 * cols + j);
+                i2++;
+            }
+            x[c][t] = v;
+        }
+    }
+    void excludeColumn(int c, int col) {  // scheme_z2.cu:184-203
+        const int r = n[c], cols = n[(c + 1) % 3];
+        for (int t = 0; t < m; t++) {
+            uint64_t v = 0;
+            for (int i = 0; i < r; i++)
+                for (int j = 0, j2 = 0; j < cols; j++) {
+                    if (j == col) continue;
+                    v |= bit(x[c][t], i * cols + j) << (i * (cols - 1) + j2);
+                    j2++;
+                }
+            x[c][t] = v;
+        }
+    }
+    void addColumn(int c) {  // scheme_z2.cu:226-239 (addRow, 241-254, leaves the bits in place)
+        const int r = n[c], cols = n[(c + 1) % 3];
+        for (int t = 0; t < m; t++) {
+            uint64_t v = 0;
+            for (int i = 0; i < r; i++)
+                for (int j = 0; j < cols; j++) v |= bit(x[c][t], i * cols + j) << (i * (cols + 1) + j);
+            x[c][t] = v;
+        }
+    }
+
+    bool isValidProject(int i, int minN) const {  // scheme_z2.cu:256-258
+        return n[i] - 1 >= minN && n[(i + 1) % 3] >= minN && n[(i + 2) % 3] >= minN;
+    }
+    bool isValidGrown(const int g[3], int extraRank, int maxN) const {  // scheme_z2.cu:260-294
+        if (extraRank > kMaxRank) return false;
+        for (int q = 0; q < 3; q++)
+            if (g[q] * g[(q + 1) % 3] > kMaxMatrix || g[q] > maxN) return false;
+        return true;
+    }
+    bool isValidExtension(int i, int maxN) const {
+        int g[3] = {n[0], n[1], n[2]};
+        g[i] += 1;
+        return isValidGrown(g, m + g[(i + 1) % 3] * g[(i + 2) % 3], maxN);
+    }
+    bool isValidProduct(int i, int maxN) const {
+        int g[3] = {n[0], n[1], n[2]};
+        g[i] *= 2;
+        return isValidGrown(g, m * 2, maxN);
+    }
+
+    void project(int p, int q) {  // scheme_z2.cu:643-653
+        excludeRow(p, q);
+        excludeColumn((p + 2) % 3, q);
+        int g[3] = {n[0], n[1], n[2]};
+        g[p]--;
+        setN(g[0], g[1], g[2]);
+        removeZeroes();
+        rebuildLists();
+    }
+
+    void extend(int p) {  // scheme_z2.cu:655-687 (terms added with the old sizes)
+        const int a = n[0], b = n[1], c = n[2];
+        if (p == 0) {
+            addColumn(2);
+            for (int i = 0; i < c; i++)
+                for (int j = 0; j < b; j++)
+                    addTriplet(0, 1, 2, 1ull << (a * b + j), 1ull << (j * c + i), 1ull << (i * (a + 1) + a));
+        } else if (p == 1) {
+            addColumn(0);
+            for (int i = 0; i < a; i++)
+                for (int j = 0; j < c; j++)
+                    addTriplet(0, 1, 2, 1ull << (i * (b + 1) + b), 1ull << (b * c + j), 1ull << (j * a + i));
+        } else {
+            addColumn(1);
+            for (int i = 0; i < a; i++)
+                for (int j = 0; j < b; j++)
+                    addTriplet(0, 1, 2, 1ull << (i * b + j), 1ull << (j * (c + 1) + c), 1ull << (c * a + i));
+        }
+        int g[3] = {a, b, c};
+        g[p]++;
+        setN(g[0], g[1], g[2]);
+        rebuildLists();
+    }
+
+    // Copies of a term's three matrices placed at block offsets (d0, d1, d2) of
+    // new sizes g: matrix c entry (i, j) -> (i + d[c], j + d[c+1]).
+    static uint64_t place(uint64_t v, int rows, int cols, int newCols, int di, int dj) {
+        uint64_t o = 0;
+        for (int i = 0; i < rows; i++)
+            for (int j = 0; j < cols; j++) o |= bit(v, i * cols + j) << ((i + di) * newCols + j + dj);
+        return o;
+    }
+
+    void product(int p) {  // scheme_z2.cu:689-747: block-diagonal doubling of size p
+        int g[3] = {n[0], n[1], n[2]}, d[3];
+        g[p] *= 2;
+        for (int q = 0; q < 3; q++) d[q] = q == p ? n[q] : 0;
+        for (int t = 0; t < m; t++)
+            for (int c = 0; c < 3; c++) {
+                const int c1 = (c + 1) % 3;
+                const uint64_t v = x[c][t];
+                x[c][t] = place(v, n[c], n[c1], g[c1], 0, 0);
+                x[c][t + m] = place(v, n[c], n[c1], g[c1], d[c], d[c1]);
+            }
+        m *= 2;
+        setN(g[0], g[1], g[2]);
+        rebuildLists();
+    }
+
+    void merge(const Z2 &o, int p) {  // scheme_z2.cu:749-817: o's terms in the new block of size p
+        int g[3] = {n[0], n[1], n[2]}, d[3];
+        for (int q = 0; q < 3; q++) {
+            g[q] = q == p ? n[q] + o.n[q] : n[q];
+            d[q] = q == p ? n[q] : 0;
+        }
+        for (int t = 0; t < m; t++)
+            for (int c = 0; c < 3; c++) x[c][t] = place(x[c][t], n[c], n[(c + 1) % 3], g[(c + 1) % 3], 0, 0);
+        for (int t = 0; t < o.m; t++)
+            for (int c = 0; c < 3; c++) {
+                const int c1 = (c + 1) % 3;
+                x[c][m + t] = place(o.x[c][t], o.n[c], o.n[c1], g[c1], d[c], d[c1]);
+            }
+        m += o.m;
+        setN(g[0], g[1], g[2]);
+        rebuildLists();
+    }
+
+    void productWith(const Z2 &o) {  // scheme_z2.cu:819-862: tensor product, terms (t1, t2) row-major
+        Z2 *a = new Z2(*this);
+        setN(a->n[0] * o.n[0], a->n[1] * o.n[1], a->n[2] * o.n[2]);
+        m = a->m * o.m;
+        for (int t1 = 0; t1 < a->m; t1++)
+            for (int t2 = 0; t2 < o.m; t2++) {
+                const int t = t1 * o.m + t2;
+                for (int c = 0; c < 3; c++) {
+                    const int c1 = (c + 1) % 3;
+                    uint64_t v = 0;
+                    for (int e1 = 0; e1 < a->nn[c]; e1++) {
+                        if (!bit(a->x[c][t1], e1)) continue;
+                        const int r1 = e1 / a->n[c1], q1 = e1 % a->n[c1];
+                        for (int e2 = 0; e2 < o.nn[c]; e2++) {
+                            if (!bit(o.x[c][t2], e2)) continue;
+                            const int r2 = e2 / o.n[c1], q2 = e2 % o.n[c1];
+                            v |= 1ull << ((r1 * o.n[c] + r2) * n[c1] + q1 * o.n[c1] + q2);
+                        }
+                    }
+                    x[c][t] = v;
+                }
+            }
+        delete a;
+        rebuildLists();
+    }
+
+    void swapSize(int p1, int p2) {  // scheme_z2.cu:916-979
+        if (p1 == p2) return;
+        if (p1 > p2) std::swap(p1, p2);
+        int idx[3];
+        if (p1 == 0 && p2 == 1) { idx[0] = 0; idx[1] = 2; idx[2] = 1; }
+        else if (p1 == 0 && p2 == 2) { idx[0] = 1; idx[1] = 0; idx[2] = 2; }
+        else { idx[0] = 2; idx[1] = 1; idx[2] = 0; }
+        int g[3];
+        for (int q = 0; q < 3; q++) g[q] = n[(idx[q] + 1) % 3];
+        for (int t = 0; t < m; t++) {
+            uint64_t v[3];
+            for (int c = 0; c < 3; c++) {
+                // new matrix c (g[c] x g[c+1]) is the transpose of old matrix idx[c]
+                const int rows = g[c], cols = g[(c + 1) % 3];
+                uint64_t o = 0;
+                for (int i = 0; i < rows; i++)
+                    for (int j = 0; j < cols; j++) o |= bit(x[idx[c]][t], j * rows + i) << (i * cols + j);
+                v[c] = o;
+            }
+            for (int c = 0; c < 3; c++) x[c][t] = v[c];
+        }
+        setN(g[0], g[1], g[2]);
+        rebuildLists();
+    }
+
+    void reduceAll() {  // while (tryReduce()) ; (bounded)
+        for (int guard = 0; tryReduce(); guard++)
+            if (guard > kRetryCap) { *status |= ST_RETRY; return; }
+    }
+
+    template <class R> bool tryProject(R &r, int minN = 2) {  // scheme_z2.cu:1165-1185
+        int idx[3], size = 0;
+        for (int i = 0; i < 3; i++)
+            if (isValidProject(i, minN)) idx[size++] = i;
+        if (!size) return false;
+        const int p = idx[r.raw() % (uint32_t)size];
+        const int q = (int)(r.raw() % (uint32_t)n[p]);
+        project(p, q);
+        reduceAll();
+        return true;
+    }
+    template <class R> bool tryExtend(R &r, int maxN = 16) {  // scheme_z2.cu:1187-1206
+        int idx[3], size = 0;
+        for (int i = 0; i < 3; i++)
+            if (isValidExtension(i, maxN)) idx[size++] = i;
+        if (!size) return false;
+        extend(idx[r.raw() % (uint32_t)size]);
+        reduceAll();
+        return true;
+    }
+    template <class R> bool tryProduct(R &r, int maxN = 16) {  // scheme_z2.cu:1208-1223
+        int idx[3], size = 0;
+        for (int i = 0; i < 3; i++)
+            if (isValidProduct(i, maxN)) idx[size++] = i;
+        if (!size) return false;
+        product(idx[r.raw() % (uint32_t)size]);
+        return true;
+    }
+    template <class R> bool tryMerge(const Z2 &o, R &r) {  // scheme_z2.cu:1225-1254
+        if (m + o.m > kMaxRank) return false;
+        const bool eq0 = n[0] == o.n[0], eq1 = n[1] == o.n[1], eq2 = n[2] == o.n[2];
+        const int s0 = n[0] + o.n[0], s1 = n[1] + o.n[1], s2 = n[2] + o.n[2];
+        int p[3], size = 0;
+        if (s0 <= kMaxExtensionN && s0 * n[1] <= kMaxMatrix && s0 * n[2] <= kMaxMatrix && eq1 && eq2) p[size++] = 0;
+        if (eq0 && s1 <= kMaxExtensionN && n[0] * s1 <= kMaxMatrix && n[2] * s1 <= kMaxMatrix && eq2) p[size++] = 1;
+        if (eq0 && eq1 && s2 <= kMaxExtensionN && n[0] * s2 <= kMaxMatrix && n[1] * s2 <= kMaxMatrix) p[size++] = 2;
+        if (!size) return false;
+        merge(o, p[r.raw() % (uint32_t)size]);
+        return true;
+    }
+    bool tryProductWith(const Z2 &o) {  // scheme_z2.cu:1256-1275
+        if (m * o.m > kMaxRank) return false;
+        int g[3];
+        for (int q = 0; q < 3; q++) g[q] = n[q] * o.n[q];
+        for (int q = 0; q < 3; q++)
+            if (g[q] > kMaxExtensionN || g[q] * g[(q + 1) % 3] > kMaxMatrix) return false;
+        productWith(o);
+        return true;
+    }
+    template <class R> void swapSizeRandom(R &r) {  // scheme_z2.cu:1315-1323
+        int p1, p2;
+        do {
+            p1 = (int)(r.raw() % 3u);
+            p2 = (int)(r.raw() % 3u);
+        } while (p1 == p2);
+        swapSize(p1, p2);
     }
 };
 
@@ -799,6 +1059,8 @@ void storeZT(const ZT &s, fgo_batch *b, int w, int cap) {
 void storeBestZ2(const Z2 &s, fgo_batch *b, int w, int cap) {
     if (s.m > cap) { b->status[w] |= ST_OVERFLOW; return; }
     b->best_m[w] = s.m;
+    if (b->best_n)
+        for (int c = 0; c < 3; c++) b->best_n[w * 3 + c] = s.n[c];
     for (int c = 0; c < 3; c++)
         for (int t = 0; t < cap; t++) b->best_fac[facIndex(w, c, t, cap)] = t < s.m ? s.x[c][t] : 0;
 }
@@ -827,7 +1089,8 @@ void walkLaunch(Scheme &s, R &r, const fgo_walk_cfg *cfg, fgo_batch *b, int w) {
     int flipsCount = b->flips[w];
     int bestRank = b->best_rank[w];
     int bestM = b->best_m[w];
-    const int iters = cfg->iterations;
+    // randomIterations (flip_graph.cu:531): with resizing on, a launch runs randint(1, iterations) steps
+    const int iters = cfg->resize_p > 0 ? randint(1, cfg->iterations, r) : cfg->iterations;
     for (int it = 0; it < iters; it++) {
         int rank = s.m;
         if (!s.tryFlip(r, true)) {
@@ -842,12 +1105,12 @@ void walkLaunch(Scheme &s, R &r, const fgo_walk_cfg *cfg, fgo_batch *b, int w) {
             storeBest(s, b, w, cap);
             bestM = s.m;
         }
-        if (r.gate(cfg->reduce_p, iters)) s.tryReduce();
-        if (r.gate(cfg->expand_p, iters) && s.m <= bestM + 2) {
+        if (r.gate(cfg->reduce_p, cfg->iterations)) s.tryReduce();
+        if (r.gate(cfg->expand_p, cfg->iterations) && s.m <= bestM + 2) {
             if (s.tryExpand(randint(1, 2, r), r)) flipsCount = 0;
         }
-        r.gate(0.0, iters);  // sandwiching gate (probability 0)
-        r.gate(0.0, iters);  // basis gate (probability 0)
+        r.gate(0.0, cfg->iterations);  // sandwiching gate (probability 0)
+        r.gate(0.0, cfg->iterations);  // basis gate (probability 0)
         if (flipsCount >= cfg->plus_iterations && s.tryPlus(r)) flipsCount = 0;
         if (b->status[w]) break;
     }
@@ -1148,6 +1411,115 @@ struct fgo_reducer_state {
     std::vector<std::pair<int, int>> vars[3];
 };
 
+// ------------------------------------------------------------ resizing
+std::string sizeKey(const int n[3]) {  // getKey(scheme) with sorted sizes (utils.cu:3-25)
+    int a[3] = {n[0], n[1], n[2]};
+    std::sort(a, a + 3);
+    return std::to_string(a[0]) + "x" + std::to_string(a[1]) + "x" + std::to_string(a[2]);
+}
+
+void loadBestZ2(Z2 &s, const fgo_batch *b, int w, int cap) {
+    for (int c = 0; c < 3; c++) s.n[c] = b->best_n ? b->best_n[w * 3 + c] : b->n[w * 3 + c];
+    for (int c = 0; c < 3; c++) s.nn[c] = s.n[c] * s.n[(c + 1) % 3];
+    s.m = b->best_m[w];
+    for (int c = 0; c < 3; c++)
+        for (int t = 0; t < s.m; t++) s.x[c][t] = b->best_fac[facIndex(w, c, t, cap)];
+}
+
+// resizeKernel body (flip_graph.cu:575-613) for walk w; `best` holds every walk's best scheme.
+template <class R>
+void resizeStep(Z2 &s, R &r, const std::vector<Z2> &best, int S, double p) {
+    if ((double)r.uniform() > p) return;
+    if ((double)r.uniform() < 0.5) s.swapSizeRandom(r);
+    bool merged = false;
+    for (int i = 0; i < 3 && !merged; i++) {
+        const int index = (int)(r.raw() % (uint32_t)S);
+        merged |= s.tryMerge(best[index], r);
+    }
+    if (merged) return;
+    const double q = (double)r.uniform();
+    if (q < 0.05) s.tryProject(r);
+    else if (q < 0.55) s.tryProductWith(best[(int)(r.raw() % (uint32_t)S)]);
+    else if (q < 0.85) s.tryProduct(r);
+    else s.tryExtend(r);
+}
+
+// updateRanks (flip_graph.cu:249-266): the best rank per (sorted) size; a walk that
+// improves it has its current scheme copied to its best slot; every walk's best rank
+// becomes its size's.
+void updateRanks(std::map<std::string, int> &table, std::vector<Z2> &cur, std::vector<Z2> &best, fgo_batch *b,
+                 int S, int cap) {
+    std::vector<std::string> keys(S);
+    for (int w = 0; w < S; w++) {
+        keys[w] = sizeKey(cur[w].n);
+        auto it = table.find(keys[w]);
+        if (it == table.end() || cur[w].m < it->second) {
+            table[keys[w]] = cur[w].m;
+            best[w] = cur[w];
+            storeBestZ2(cur[w], b, w, cap);
+        }
+    }
+    for (int w = 0; w < S; w++) b->best_rank[w] = table[keys[w]];
+}
+
+// FlipGraph::run with --resize-probability > 0 (flip_graph.cu:286-299): launches of every
+// walk, then the resize step of every walk, then the best-rank table.  The table starts from
+// the first walk's size at the naive rank, as the constructor sets it (flip_graph.cu:19), and
+// an update over the starting schemes (FlipGraph::initialize, flip_graph.cu:190-198).
+template <class R>
+void runResize(const fgo_walk_cfg *cfg, int S, fgo_batch *b, std::vector<R> &rs) {
+    const int cap = cfg->cap;
+    std::vector<Z2> cur(S), best(S);
+    for (int w = 0; w < S; w++) {
+        loadZ2(cur[w], b, w, cap);
+        loadBestZ2(best[w], b, w, cap);
+        cur[w].status = best[w].status = &b->status[w];
+    }
+    std::map<std::string, int> table;
+    table[sizeKey(cur[0].n)] = cur[0].n[0] * cur[0].n[1] * cur[0].n[2];
+    updateRanks(table, cur, best, b, S, cap);
+    for (int L = 0; L < cfg->launches; L++) {
+        for (int w = 0; w < S; w++) {
+            if (b->status[w]) continue;
+            walkLaunch(cur[w], rs[w], cfg, b, w);
+            loadBestZ2(best[w], b, w, cap);
+        }
+        for (int w = 0; w < S; w++)
+            if (!b->status[w]) resizeStep(cur[w], rs[w], best, S, cfg->resize_p);
+        updateRanks(table, cur, best, b, S, cap);
+    }
+    for (int w = 0; w < S; w++) {
+        storeZ2(cur[w], b, w, cap);
+        b->rng_pos[w] = rs[w].pos;
+    }
+}
+
+void runWalksResizeZ2(const fgo_walk_cfg *cfg, int S, fgo_batch *b, const fgo_tape *tape) {
+    if (cfg->rng == FGO_RNG_TAPE) {
+        std::vector<RefDraws> rs(S);
+        for (int w = 0; w < S; w++) {
+            RefDraws &r = rs[w];
+            r.d = tape->draws + tape->offsets[w];
+            r.u = tape->uniforms + tape->offsets[w];
+            r.n = tape->offsets[w + 1] - tape->offsets[w];
+            r.pos = b->rng_pos[w];
+            r.status = &b->status[w];
+        }
+        runResize(cfg, S, b, rs);
+    } else {
+        std::vector<FastDraws> rs(S);
+        for (int w = 0; w < S; w++) {
+            FastDraws &r = rs[w];
+            r.key[0] = (uint32_t)cfg->seed;
+            r.key[1] = (uint32_t)(cfg->seed >> 32);
+            r.walk = (uint32_t)w;
+            r.pos = b->rng_pos[w];
+            r.status = &b->status[w];
+        }
+        runResize(cfg, S, b, rs);
+    }
+}
+
 extern "C" {
 
 void fgo_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]) { philox(ctr, key, out); }
@@ -1185,6 +1557,13 @@ int fgo_init_naive(const fgo_walk_cfg *cfg, int S, int n1, int n2, int n3, fgo_b
 }
 
 int fgo_walk(const fgo_walk_cfg *cfg, int S, fgo_batch *b, const fgo_tape *tape) {
+    if (cfg->resize_p > 0) {
+        if (cfg->ring != FGO_RING_Z2 || cfg->rng == FGO_RNG_FAST) return -1;
+        runWalksResizeZ2(cfg, S, b, tape);
+        int bad = 0;
+        for (int w = 0; w < S; w++) bad += b->status[w] != 0;
+        return bad;
+    }
     if (cfg->ring == FGO_RING_Z2) runWalks<Z2>(cfg, S, b, tape);
     else runWalks<ZT>(cfg, S, b, tape);
     int bad = 0;

@@ -40,6 +40,9 @@ typedef struct {
     double expand_p;          /* --expand-probability (divided by iterations per step) */
     double reduce_p;          /* --reduce-probability (divided by iterations per step) */
     uint64_t seed;            /* Philox key (FGO_RNG_PHILOX) */
+    double resize_p;          /* --resize-probability; > 0: random iterations per launch, a resize
+                                 step after every launch and the per-shape best-rank table
+                                 (flip_graph.cu:236,286-299,249-277,575-613); Z2 only */
 } fgo_walk_cfg;
 
 /* Structure-of-arrays batch of S walk records.  Factor arrays are [S][3][cap];
@@ -64,6 +67,7 @@ typedef struct {
     int64_t *rng_pos;    /* [S] draws consumed so far (tape position / Philox word index) */
     int32_t *status;     /* [S] 0 ok; bit 1 tape exhausted; bit 2 capped retry loop; bit 4 slot overflow */
     int64_t *accepted;   /* [S] accepted flips, accumulated (may be NULL) */
+    int32_t *best_n;     /* [S][3] sizes of the best scheme (resize; may be NULL = n) */
 } fgo_batch;
 
 /* Tape: draws for walk w are tape_draws[tape_off[w] .. tape_off[w+1]). */

@@ -50,13 +50,13 @@ class WalkCfg(ctypes.Structure):
     _fields_ = [("ring", ctypes.c_int32), ("rng", ctypes.c_int32), ("cap", ctypes.c_int32),
                 ("iterations", ctypes.c_int32), ("plus_iterations", ctypes.c_int32),
                 ("launches", ctypes.c_int32), ("expand_p", ctypes.c_double),
-                ("reduce_p", ctypes.c_double), ("seed", ctypes.c_uint64)]
+                ("reduce_p", ctypes.c_double), ("seed", ctypes.c_uint64), ("resize_p", ctypes.c_double)]
 
 
 class _Batch(ctypes.Structure):
     _fields_ = [(name, ctypes.c_void_p) for name in
                 ("n", "m", "fac", "sgn", "valid", "list_size", "list_pairs", "flips", "best_rank",
-                 "best_m", "best_fac", "best_sgn", "best_valid", "rng_pos", "status", "accepted")]
+                 "best_m", "best_fac", "best_sgn", "best_valid", "rng_pos", "status", "accepted", "best_n")]
 
 
 class _Tape(ctypes.Structure):
@@ -71,7 +71,7 @@ class WalkBatch:
     """S walk records with `cap` factor slots each (numpy, C-contiguous)."""
 
     FIELDS = ("n", "m", "fac", "sgn", "valid", "list_size", "list_pairs", "flips", "best_rank",
-              "best_m", "best_fac", "best_sgn", "best_valid", "rng_pos", "status", "accepted")
+              "best_m", "best_fac", "best_sgn", "best_valid", "rng_pos", "status", "accepted", "best_n")
 
     def __init__(self, S, cap, ring="z2"):
         self.S, self.cap, self.ring = S, cap, ring
@@ -92,6 +92,7 @@ class WalkBatch:
         self.rng_pos = np.zeros(S, np.int64)
         self.status = np.zeros(S, np.int32)
         self.accepted = np.zeros(S, np.int64)
+        self.best_n = np.zeros((S, 3), np.int32)
 
     def copy(self):
         b = WalkBatch.__new__(WalkBatch)
@@ -105,9 +106,9 @@ class WalkBatch:
         return _Batch(*[_ptr(getattr(self, f)) for f in self.FIELDS])
 
     def cfg(self, rng="tape", iterations=1000, plus_iterations=8000, launches=1, expand_p=0.01,
-            reduce_p=0.0, seed=0):
+            reduce_p=0.0, seed=0, resize_p=0.0):
         return WalkCfg(RING[self.ring], RNG[rng], self.cap, iterations, plus_iterations, launches,
-                       expand_p, reduce_p, seed)
+                       expand_p, reduce_p, seed, resize_p)
 
 
 def make_tape(tapes):
@@ -151,10 +152,11 @@ def minimize(batch, cfg, best_complexity, tape=None):
 def validate(batch, best=False):
     out = np.zeros(batch.S, np.uint8)
     m = batch.best_m if best else batch.m
+    n = batch.best_n if best and batch.best_n.any() else batch.n
     fac = batch.best_fac if best else batch.fac
     sgn = batch.best_sgn if best else batch.sgn
     val = batch.best_valid if best else batch.valid
-    lib().fgo_validate(RING[batch.ring], batch.S, batch.cap, _ptr(batch.n), _ptr(m), _ptr(fac),
+    lib().fgo_validate(RING[batch.ring], batch.S, batch.cap, _ptr(np.ascontiguousarray(n)), _ptr(m), _ptr(fac),
                        _ptr(sgn), _ptr(val), _ptr(out))
     return out.astype(bool)
 

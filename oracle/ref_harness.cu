@@ -113,8 +113,27 @@ static void write_tapes(FILE *f, const curandState *states, int count, int seed,
     cudaFree(dStates); cudaFree(dDraws); cudaFree(dUni); cudaFree(dUsed);
 }
 
+// FlipGraph::updateRanks (flip_graph.cu:249-266) restated over the harness's
+// managed arrays: per (sorted) size key the best rank; an improving walk's
+// scheme is copied to its best slot; every walk gets its key's best rank.
+static void update_ranks(std::unordered_map<std::string, int> &table, Scheme *schemes, Scheme *best, int *bestRanks,
+                         int S) {
+    std::vector<std::string> keys(S);
+    for (int i = 0; i < S; i++) {
+        keys[i] = getKey(schemes[i]);
+        auto it = table.find(keys[i]);
+        if (it == table.end() || schemes[i].m < it->second) {
+            table[keys[i]] = schemes[i].m;
+            schemes[i].copyTo(best[i]);
+        }
+    }
+    for (int i = 0; i < S; i++) bestRanks[i] = table[keys[i]];
+}
+
 static int cmd_walk(int argc, char **argv) {
-    if (argc != 13) { fprintf(stderr, "walk: bad arguments\n"); return 1; }
+    if (argc != 13 && argc != 14) { fprintf(stderr, "walk: bad arguments\n"); return 1; }
+    // optional 14th argument: --resize-probability (> 0 runs FlipGraph::run's resize loop)
+    const double resizeP = argc == 14 ? atof(argv[13]) : 0.0;
     int n1 = atoi(argv[2]), n2 = atoi(argv[3]), n3 = atoi(argv[4]);
     int S = atoi(argv[5]), iters = atoi(argv[6]), plusIters = atoi(argv[7]);
     double expandP = atof(argv[8]), reduceP = atof(argv[9]);
@@ -135,22 +154,34 @@ static int cmd_walk(int argc, char **argv) {
     HCHECK(cudaDeviceSynchronize());
     initializeSchemesKernel<<<numBlocks, blockSize>>>(schemes, best, bestRanks, flips, n1, n2, n3, S);
     HCHECK(cudaDeviceSynchronize());
+    std::unordered_map<std::string, int> table;
+    if (resizeP > 0) {  // FlipGraph constructor (flip_graph.cu:19) + initialize (190-198)
+        table[getKey(n1, n2, n3)] = n1 * n2 * n3;
+        update_ranks(table, schemes, best, bestRanks, S);
+    }
 
     FILE *f = fopen(out, "wb");
     if (!f) { fprintf(stderr, "cannot open %s\n", out); return 1; }
-    put_i32(f, 0x46475731);  // magic "FGW1"
+    put_i32(f, resizeP > 0 ? 0x46475732 : 0x46475731);  // magic "FGW2" (with resizing) / "FGW1"
     put_i32(f, kRingIsZT);
     put_i32(f, n1); put_i32(f, n2); put_i32(f, n3);
     put_i32(f, S); put_i32(f, iters); put_i32(f, plusIters);
     fwrite(&expandP, 8, 1, f); fwrite(&reduceP, 8, 1, f);
+    if (resizeP > 0) fwrite(&resizeP, 8, 1, f);
     put_i32(f, seed); put_i32(f, launches);
     for (int w = 0; w < S; w++) put_scheme(f, schemes[w], true);   // initial state
 
     for (int L = 0; L < launches; L++) {
         randomWalkKernel<<<numBlocks, blockSize>>>(schemes, best, bestRanks, flips, states, S, iters, plusIters,
-                                                   reduceP, expandP, 0.0, 0.0, false);
+                                                   reduceP, expandP, 0.0, 0.0, resizeP > 0);
         HCHECK(cudaGetLastError());
         HCHECK(cudaDeviceSynchronize());
+        if (resizeP > 0) {  // FlipGraph::run (flip_graph.cu:296-299)
+            resizeKernel<<<numBlocks, blockSize>>>(schemes, best, S, states, resizeP);
+            HCHECK(cudaGetLastError());
+            HCHECK(cudaDeviceSynchronize());
+            update_ranks(table, schemes, best, bestRanks, S);
+        }
         for (int w = 0; w < S; w++) {
             put_i32(f, flips[w]);
             put_i32(f, bestRanks[w]);

@@ -45,6 +45,13 @@ WALK_CASES = [
     ("zt_233_reduce", "zt", 2, 3, 3, 4, 150, 30, 0.01, 40.0, 24, 1),
 ]
 
+# Walks with the resize meta-operators on (FlipGraph::run's resize loop):
+# (name, ring, n1, n2, n3, walks, iterations, plus_iterations, expand_p, reduce_p, seed, launches, resize_p)
+RESIZE_CASES = [
+    ("z2_222_resize", "z2", 2, 2, 2, 12, 150, 40, 0.01, 0.0, 41, 4, 0.5),
+    ("z2_233_resize", "z2", 2, 3, 3, 8, 200, 60, 0.01, 0.0, 42, 3, 0.8),
+]
+
 # Long walks used only to produce low-rank input schemes for the reducer and
 # minimizer runs (their dumps are not kept as fixtures).
 SOURCE_WALKS = [
@@ -67,13 +74,14 @@ def harness(ring):
 
 
 def walk(out_dir, case, tape=True):
-    name, ring, n1, n2, n3, S, iters, plus, ep, rp, seed, launches = case
+    name, ring, n1, n2, n3, S, iters, plus, ep, rp, seed, launches = case[:12]
     path = os.path.join(out_dir, f"walk_{name}.bin")
     env = dict(os.environ)
     if not tape:
         env["FG_NO_TAPE"] = "1"
+    extra = [repr(case[12])] if len(case) > 12 else []
     run([harness(ring), "walk", str(n1), str(n2), str(n3), str(S), str(iters), str(plus),
-         repr(ep), repr(rp), str(seed), str(launches), path], env=env)
+         repr(ep), repr(rp), str(seed), str(launches), path] + extra, env=env)
     return path
 
 
@@ -85,9 +93,13 @@ def best_scheme_text(dump, header=True):
     return golden_io.scheme_to_text(s, dump["ring"], header=header), s
 
 
-def do_run(out_dir):
+def do_run(out_dir, resize_only=False):
     os.makedirs(out_dir, exist_ok=True)
     run([os.path.join(ROOT, "oracle", "build_ref.sh")])
+    for case in RESIZE_CASES:
+        walk(out_dir, case)
+    if resize_only:
+        return
     for case in WALK_CASES:
         walk(out_dir, case)
 
@@ -162,7 +174,12 @@ def trimmed_reduce(path):
 
 
 def do_pack(raw_dir):
-    manifest = {"walk_cases": [list(c) for c in WALK_CASES], "files": []}
+    manifest = {"walk_cases": [list(c) for c in WALK_CASES], "resize_cases": [list(c) for c in RESIZE_CASES],
+                "files": []}
+    old = os.path.join(HERE, "manifest.json")
+    if os.path.exists(old):  # packing a partial run keeps the fixtures already recorded
+        with open(old) as f:
+            manifest["files"] = json.load(f).get("files", [])
     for path in sorted(glob.glob(os.path.join(raw_dir, "*.bin")) + glob.glob(os.path.join(raw_dir, "*.txt"))
                        + glob.glob(os.path.join(raw_dir, "*.log"))):
         base = os.path.basename(path)
@@ -170,14 +187,15 @@ def do_pack(raw_dir):
         data = trimmed_reduce(path) if base.startswith("reduce_") else open(path, "rb").read()
         with gzip.open(dst, "wb", compresslevel=9) as fo:
             fo.write(data)
-        manifest["files"].append(base)
+        if base not in manifest["files"]:
+            manifest["files"].append(base)
     for sub in ("cli_additions_reducer", "cli_complexity_minimizer", "cli_flip_graph"):
         src = os.path.join(raw_dir, sub)
         if os.path.isdir(src):
             dst = os.path.join(HERE, sub)
             shutil.rmtree(dst, ignore_errors=True)
             shutil.copytree(src, dst)
-            manifest["files"] += [f"{sub}/{x}" for x in sorted(os.listdir(dst))]
+            manifest["files"] += [f"{sub}/{x}" for x in sorted(os.listdir(dst)) if f"{sub}/{x}" not in manifest["files"]]
     with open(os.path.join(HERE, "manifest.json"), "w") as f:
         json.dump(manifest, f, indent=1)
 
@@ -186,8 +204,9 @@ if __name__ == "__main__":
     ap = argparse.ArgumentParser()
     ap.add_argument("--run")
     ap.add_argument("--pack")
+    ap.add_argument("--resize-only", action="store_true", help="with --run: only the resize walks")
     a = ap.parse_args()
     if a.run:
-        do_run(a.run)
+        do_run(a.run, a.resize_only)
     if a.pack:
         do_pack(a.pack)

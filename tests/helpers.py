@@ -44,6 +44,8 @@ def diff_walk(batch, w, e, ring):
     s = e["scheme"]
     errs = []
     m = s["m"]
+    if list(batch.n[w]) != list(s["n"]):
+        return [f"sizes {list(batch.n[w])} != {list(s['n'])}"]
     if batch.m[w] != m:
         return [f"m {batch.m[w]} != {m}"]
     if ring == "z2":
@@ -62,6 +64,9 @@ def diff_walk(batch, w, e, ring):
     if batch.best_rank[w] != e["best_rank"]:
         errs.append("best_rank")
     b = e["best"]
+    best_n = getattr(batch, "best_n", None)
+    if best_n is not None and best_n.any() and list(best_n[w]) != list(b["n"]):
+        errs.append("best sizes")
     if batch.best_m[w] != b["m"]:
         errs.append("best_m")
     elif ring == "z2" and not np.array_equal(batch.best_fac[w, :, :b["m"]], b["uvw"]):

@@ -22,6 +22,8 @@ def test_walk_matches_reference(path):
     d = golden_io.read_walk(path)
     ring, S = d["ring"], d["walks"]
     n1, n2, n3 = d["n"]
+    if d["resize_p"] > 0:
+        return check_resize_walk(d)
     batch = O.WalkBatch(S, n1 * n2 * n3, ring)
     O.init_naive(batch, n1, n2, n3)
     for w in range(S):
@@ -35,6 +37,25 @@ def test_walk_matches_reference(path):
         for w in range(S):
             assert not diff_walk(batch, w, block[w], ring), f"launch {L} walk {w}"
         assert O.validate(batch).all()
+    assert [int(x) for x in batch.rng_pos] == [t["used"] for t in d["tapes"]]
+
+
+def check_resize_walk(d):
+    """Resize dumps: the table of best ranks per size spans launches, so the oracle reruns
+    launches 1..L from the naive start and compares every walk after each L (sizes, factors,
+    lists, best sizes and scheme, flips counter, best rank) and the draws consumed."""
+    S, ring = d["walks"], d["ring"]
+    n1, n2, n3 = d["n"]
+    tape = O.make_tape([(t["draws"], t["uniforms"]) for t in d["tapes"]])
+    for L, block in enumerate(d["launches"]):
+        batch = O.WalkBatch(S, 352, ring)
+        O.init_naive(batch, n1, n2, n3)
+        cfg = batch.cfg("tape", d["iterations"], d["plus_iterations"], L + 1, d["expand_p"], d["reduce_p"],
+                        resize_p=d["resize_p"])
+        assert O.walk(batch, cfg, tape) == 0
+        for w in range(S):
+            assert not diff_walk(batch, w, block[w], ring), f"launch {L} walk {w}: {diff_walk(batch, w, block[w], ring)}"
+        assert O.validate(batch).all() and O.validate(batch, best=True).all()
     assert [int(x) for x in batch.rng_pos] == [t["used"] for t in d["tapes"]]
 
 
