@@ -36,13 +36,13 @@ class Config(ctypes.Structure):
     _fields_ = [("ring", ctypes.c_int32), ("mode", ctypes.c_int32), ("walks", ctypes.c_int32),
                 ("cap", ctypes.c_int32), ("seed", ctypes.c_uint64), ("iterations", ctypes.c_int32),
                 ("plus_iterations", ctypes.c_int32), ("expand_p", ctypes.c_double), ("reduce_p", ctypes.c_double),
-                ("device", ctypes.c_int32), ("walks_per_block", ctypes.c_int32)]
+                ("device", ctypes.c_int32), ("walks_per_block", ctypes.c_int32), ("resize_p", ctypes.c_double)]
 
 
 class _Records(ctypes.Structure):
     _fields_ = [(name, ctypes.c_void_p) for name in
                 ("n", "m", "fac", "sgn", "valid", "list_size", "list_pairs", "flips", "best_rank",
-                 "best_m", "best_fac", "best_sgn", "best_valid", "rng_pos", "status")]
+                 "best_m", "best_fac", "best_sgn", "best_valid", "rng_pos", "status", "best_n")]
 
 
 class Stats(ctypes.Structure):
@@ -133,6 +133,7 @@ class Records:
         self.best_valid = np.zeros((walks, 3, cap), np.uint8) if zt else None
         self.rng_pos = np.zeros(walks, np.int64)
         self.status = np.zeros(walks, np.int32)
+        self.best_n = np.zeros((walks, 3), np.int32)
 
     def _alloc_pinned(self, walks, cap, zt):
         def pin(shape, dtype):
@@ -155,6 +156,7 @@ class Records:
         self.best_valid = pin((walks, 3, cap), np.uint8) if zt else None
         self.rng_pos = pin((walks,), np.int64)
         self.status = pin((walks,), np.int32)
+        self.best_n = pin((walks, 3), np.int32)
 
     def nbytes(self):
         return sum(getattr(self, f).nbytes for f, _ in self.FIELDS if getattr(self, f) is not None)
@@ -167,12 +169,12 @@ class Engine:
     """One fg_handle: `walks` independent walks on one GPU."""
 
     def __init__(self, walks, cap, ring="z2", mode="reference", seed=1, iterations=10000, plus_iterations=8000,
-                 expand_p=0.01, reduce_p=0.0, device=0, walks_per_block=0):
+                 expand_p=0.01, reduce_p=0.0, device=0, walks_per_block=0, resize_p=0.0):
         """mode: "reference" (XORWOW, reference lists, bit-exact), "philox" (Philox, lists) or
         "fast" (Philox, implicit pair enumeration, thread-per-walk kernel)."""
         self.lib = library()
         self.cfg = Config(RINGS[ring], MODES[mode], walks, cap, seed, iterations, plus_iterations, expand_p,
-                          reduce_p, device, walks_per_block)
+                          reduce_p, device, walks_per_block, resize_p)
         self.walks, self.cap, self.ring = walks, cap, ring
         self.h = ctypes.c_void_p()
         _check(self.lib.fg_create(ctypes.byref(self.cfg), ctypes.byref(self.h)))

@@ -4,6 +4,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <string>
 #include <vector>
 
@@ -68,6 +69,7 @@ __global__ void k_init_naive(DevBatch B, int n1_, int n2_, int n3_, const int32_
                         B.best_valid[(size_t)w * 3 * cap + q * cap + t] = 1;
                     }
             }
+    if (B.best_n) { B.best_n[w * 3] = n1; B.best_n[w * 3 + 1] = n2; B.best_n[w * 3 + 2] = n3; }
     WalkHeader h = B.hdr[w];
     h.n[0] = n1; h.n[1] = n2; h.n[2] = n3;
     h.m = n1 * n2 * n3;
@@ -94,7 +96,8 @@ __global__ void k_verify_z2(DevBatch B, int best, uint8_t *out) {
         const uint64_t *src = (best ? B.best_fac : B.fac) + (size_t)w * 3 * cap;
         for (int q = lane; q < 3 * cap; q += 32) x[q] = src[q];
         __syncwarp();
-        const int n0 = h.n[0], n1 = h.n[1], n2 = h.n[2];
+        const int32_t *dims = best && B.best_n ? B.best_n + w * 3 : h.n;
+        const int n0 = dims[0], n1 = dims[1], n2 = dims[2];
         const int nn0 = n0 * n1, nn1 = n1 * n2, nn2 = n2 * n0;
         const int m = best ? h.best_m : h.m;
         const uint64_t kmask = nn2 >= 64 ? ~0ull : ((1ull << nn2) - 1);
@@ -205,6 +208,10 @@ struct fg_handle {
     DevBatch B{};
     WalkParams P{};
     int32_t *d_bestC = nullptr;
+    // resizing: best rank per size key (FlipGraph::n2bestRank) and its device-side helpers
+    std::map<std::string, int> table;
+    bool tableReady = false;
+    int32_t *d_copyList = nullptr, *d_bestRanks = nullptr;
     uint8_t *d_valid = nullptr;
     bool ready = false;
 };
@@ -237,6 +244,7 @@ void compute_params(fg_handle *h) {
     P.expand_T = thr(c.expand_p);
     P.key0 = (uint32_t)c.seed;
     P.key1 = (uint32_t)(c.seed >> 32);
+    P.random_iterations = c.resize_p > 0 ? 1 : 0;
 }
 
 int verify_grid(fg_handle *h) { return (h->B.S + 3) / 4; }
@@ -316,6 +324,45 @@ fg_status refresh_plan(fg_handle *h) {
     return FG_OK;
 }
 
+// FlipGraph::updateRanks (flip_graph.cu:249-266) with resizing on: per size key
+// (sizes sorted, utils.cu:3-25) the best rank; a walk that improves it has its
+// current scheme copied to its best slot, and every walk's best rank becomes its
+// key's.  The table starts, as FlipGraph's constructor and initialize() set it
+// (flip_graph.cu:19,190-198), from the first walk's size at the naive rank.
+fg_status update_ranks(fg_handle *h) {
+    const int S = h->B.S;
+    std::vector<WalkHeader> hdr(S);
+    FG_CUDA(cudaMemcpyAsync(hdr.data(), h->B.hdr, sizeof(WalkHeader) * S, cudaMemcpyDeviceToHost, h->stream));
+    FG_CUDA(cudaStreamSynchronize(h->stream));
+    auto key = [](const int32_t *n) {
+        int a[3] = {n[0], n[1], n[2]};
+        std::sort(a, a + 3);
+        return std::to_string(a[0]) + "x" + std::to_string(a[1]) + "x" + std::to_string(a[2]);
+    };
+    if (!h->tableReady) {
+        h->table.clear();
+        h->table[key(hdr[0].n)] = hdr[0].n[0] * hdr[0].n[1] * hdr[0].n[2];
+        h->tableReady = true;
+    }
+    std::vector<std::string> keys(S);
+    std::vector<int32_t> copies, ranks(S);
+    for (int w = 0; w < S; w++) {
+        keys[w] = key(hdr[w].n);
+        auto it = h->table.find(keys[w]);
+        if (it == h->table.end() || hdr[w].m < it->second) {
+            h->table[keys[w]] = hdr[w].m;
+            copies.push_back(w);
+        }
+    }
+    for (int w = 0; w < S; w++) ranks[w] = h->table[keys[w]];
+    if (!copies.empty())
+        FG_CUDA(cudaMemcpyAsync(h->d_copyList, copies.data(), 4 * copies.size(), cudaMemcpyHostToDevice, h->stream));
+    FG_CUDA(cudaMemcpyAsync(h->d_bestRanks, ranks.data(), 4 * (size_t)S, cudaMemcpyHostToDevice, h->stream));
+    FG_CUDA(launch_copy_best(h->B, h->d_copyList, (int)copies.size(), h->d_bestRanks, h->stream));
+    FG_CUDA(cudaStreamSynchronize(h->stream));
+    return FG_OK;
+}
+
 // Launches one walk pass over every walk on h->stream (fast mode: one kernel
 // per segment on side streams, forked from and joined back into h->stream).
 fg_status launch_walks(fg_handle *h) {
@@ -377,6 +424,10 @@ fg_status fg_create(const fg_config *cfg, fg_handle **out) {
         return fail(FG_ERR_ARG, "unknown mode");
     if (cfg->cap <= 0 || slots_for_cap(cfg->cap) == 0 || cfg->cap > FG_MAX_RANK + 2)
         return fail(FG_ERR_CAPACITY, "cap must be in [1, 352]");
+    if (cfg->resize_p > 0 && (cfg->ring != FG_RING_Z2 || (cfg->mode != FG_MODE_REFERENCE && cfg->mode != FG_MODE_PHILOX_LISTS)))
+        return fail(FG_ERR_ARG, "resizing runs on the Z2 ring in a list mode");
+    if (cfg->resize_p > 0 && cfg->cap < FG_MAX_RANK)
+        return fail(FG_ERR_CAPACITY, "resizing needs cap >= 350 (products reach the maximal rank)");
     if (cfg->iterations <= 0) return fail(FG_ERR_ARG, "iterations must be positive");
     fg_handle *h = new fg_handle;
     h->cfg = *cfg;
@@ -421,6 +472,11 @@ fg_status fg_create(const fg_config *cfg, fg_handle **out) {
             return fail(FG_ERR_CUDA, "seeding failed");
         }
     }
+    if (cfg->resize_p > 0 && ((st = dalloc(&h->B.best_n, (size_t)S * 3)) || (st = dalloc(&h->d_copyList, (size_t)S)) ||
+                              (st = dalloc(&h->d_bestRanks, (size_t)S)))) {
+        fg_destroy(h);
+        return st;
+    }
     if (cfg->mode == FG_MODE_LEARNED) {
         cudaError_t le = learned_alloc(h->learned, S, cap, 1);
         if (le != cudaSuccess) {
@@ -442,7 +498,8 @@ fg_status fg_destroy(fg_handle *h) {
     if (h->stream) cudaStreamSynchronize(h->stream);
     learned_free(h->learned);
     void *ptrs[] = {h->B.hdr, h->B.fac, h->B.sgn, h->B.valid, h->B.lists, h->B.best_fac, h->B.best_sgn,
-                    h->B.best_valid, h->B.xorwow, h->d_bestC, h->d_valid};
+                    h->B.best_valid, h->B.xorwow, h->d_bestC, h->d_valid, h->B.best_n, h->d_copyList,
+                    h->d_bestRanks};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     for (auto &e : h->ev)
@@ -470,6 +527,7 @@ fg_status fg_init_naive(fg_handle *h, int n1, int n2, int n3) {
     fg_status st = refresh_plan(h);
     if (st) return st;
     h->ready = true;
+    h->tableReady = false;
     return FG_OK;
 }
 
@@ -497,6 +555,7 @@ fg_status fg_init_naive_shapes(fg_handle *h, const int32_t *shapes) {
     fg_status st = refresh_plan(h);
     if (st) return st;
     h->ready = true;
+    h->tableReady = false;
     return FG_OK;
 }
 
@@ -639,6 +698,12 @@ fg_status fg_set_records(fg_handle *h, const fg_records *rec) {
     FG_CUDA(cudaMemcpy(h->B.hdr, hdr.data(), sizeof(WalkHeader) * S, cudaMemcpyHostToDevice));
     FG_CUDA(cudaMemcpy(h->B.fac, rec->fac, nf * sizeof(uint64_t), cudaMemcpyHostToDevice));
     FG_CUDA(cudaMemcpy(h->B.lists, rec->list_pairs, (size_t)S * 3 * kListCap * 4, cudaMemcpyHostToDevice));
+    if (h->B.best_n) {
+        std::vector<int32_t> bn((size_t)S * 3);
+        for (int w = 0; w < S; w++)
+            for (int c = 0; c < 3; c++) bn[w * 3 + c] = rec->best_n ? rec->best_n[w * 3 + c] : rec->n[w * 3 + c];
+        FG_CUDA(cudaMemcpy(h->B.best_n, bn.data(), bn.size() * 4, cudaMemcpyHostToDevice));
+    }
     FG_CUDA(cudaMemcpy(h->B.best_fac, rec->best_fac ? rec->best_fac : rec->fac, nf * sizeof(uint64_t),
                        cudaMemcpyHostToDevice));
     if (h->cfg.ring == FG_RING_ZT) {
@@ -650,6 +715,7 @@ fg_status fg_set_records(fg_handle *h, const fg_records *rec) {
     }
     plan_segments(h, hdr);
     h->ready = true;
+    h->tableReady = false;
     return FG_OK;
 }
 
@@ -672,6 +738,10 @@ fg_status fg_get_records(fg_handle *h, fg_records *rec) {
         if (rec->rng_pos) rec->rng_pos[w] = (int64_t)o.draws;
         if (rec->status) rec->status[w] = o.status;
     }
+    if (rec->best_n) {
+        if (h->B.best_n) FG_CUDA(cudaMemcpy(rec->best_n, h->B.best_n, (size_t)S * 12, cudaMemcpyDeviceToHost));
+        else for (int w = 0; w < S; w++) for (int c = 0; c < 3; c++) rec->best_n[w * 3 + c] = hdr[w].n[c];
+    }
     if (rec->fac) FG_CUDA(cudaMemcpy(rec->fac, h->B.fac, nf * 8, cudaMemcpyDeviceToHost));
     if (rec->best_fac) FG_CUDA(cudaMemcpy(rec->best_fac, h->B.best_fac, nf * 8, cudaMemcpyDeviceToHost));
     if (rec->list_pairs) FG_CUDA(cudaMemcpy(rec->list_pairs, h->B.lists, (size_t)S * 3 * kListCap * 4, cudaMemcpyDeviceToHost));
@@ -693,10 +763,21 @@ fg_status fg_run(fg_handle *h, int launches, fg_stats *stats) {
     fg_stats acc{};
     acc.min_rank = acc.min_best_rank = 1 << 30;
     std::vector<WalkHeader> hdr(S);
+    const bool resizing = h->cfg.resize_p > 0;
+    if (resizing && !h->tableReady) {
+        fg_status us = update_ranks(h);
+        if (us) return us;
+    }
     for (int L = 0; L < launches; L++) {
         FG_CUDA(cudaEventRecord(h->ev[0], h->stream));
         fg_status ls = launch_walks(h);
         if (ls) return ls;
+        if (resizing) {
+            FG_CUDA(launch_resize(h->B, h->P, h->cfg.mode == FG_MODE_REFERENCE ? RNG_XORWOW : RNG_PHILOX,
+                                  h->cfg.resize_p, h->wpb, h->grid, h->stream));
+            fg_status us = update_ranks(h);
+            if (us) return us;
+        }
         FG_CUDA(cudaEventRecord(h->ev[1], h->stream));
         fg_status st = launch_verify(h, 0);
         if (st) return st;

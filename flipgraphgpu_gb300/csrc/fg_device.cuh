@@ -43,6 +43,7 @@ struct DevBatch {
     uint64_t *best_fac, *best_sgn;
     uint8_t *best_valid;
     curandStateXORWOW_t *xorwow;  // reference stream states (FG_RNG_XORWOW)
+    int32_t *best_n;              // [S][3] sizes of the best scheme (resizing), or null
 };
 
 struct WalkParams {
@@ -54,6 +55,7 @@ struct WalkParams {
     // Fast gates: draw < threshold, threshold = floor(p / iterations * 2^32); 0 = disabled.
     uint64_t reduce_T, expand_T;
     uint32_t key0, key1;  // Philox key (seed)
+    int random_iterations;  // resizing on: each launch runs randint(1, iterations) steps (flip_graph.cu:531)
 };
 
 __device__ __forceinline__ int lane_id() { return threadIdx.x & 31; }

@@ -146,7 +146,8 @@ __device__ void walk_one(const DevBatch &B, const WalkParams &P, int w, unsigned
     walk_bind(z, B, h, w, base);
     int flipsCount = h.flips, bestRank = h.best_rank, bestM = h.best_m;
     uint64_t accepted = 0;
-    for (int it = 0; it < P.iterations; it++) {
+    const int iterations = P.random_iterations ? randint(1, P.iterations, r) : P.iterations;
+    for (int it = 0; it < iterations; it++) {
         const int rank = z.m;
         if (!z.tryFlip(true)) {
             z.tryExpand(randint(1, 2, r));
@@ -160,6 +161,11 @@ __device__ void walk_one(const DevBatch &B, const WalkParams &P, int w, unsigned
             bestRank = z.m;
             bestM = z.m;
             RingIO<Walker>::store(z, B, w, true);
+            if (B.best_n && lane_id() == 0) {
+                B.best_n[w * 3 + 0] = z.n0;
+                B.best_n[w * 3 + 1] = z.n1;
+                B.best_n[w * 3 + 2] = z.n2;
+            }
         }
         if (r.gate_reduce()) z.tryReduce();
         if (r.gate_expand() && z.m <= bestM + 2) {

@@ -66,6 +66,10 @@ typedef struct {
     double reduce_p;          /* --reduce-probability (per step: reduce_p / iterations) */
     int32_t device;           /* CUDA device ordinal */
     int32_t walks_per_block;  /* 0 = library default */
+    double resize_p;          /* --resize-probability: > 0 turns on the resize meta-operators
+                                 (Z2, list modes, cap >= 350): each launch runs a random number
+                                 of steps, then resizes walks and updates the best rank per size
+                                 (flip_graph.cu:286-299,575-613,249-266) */
 } fg_config;
 
 /* Host-side walk records, structure of arrays over `walks` records with
@@ -92,6 +96,7 @@ typedef struct {
     uint8_t *best_valid;  /* ZT only */
     int64_t *rng_pos;     /* [walks] draws consumed since seeding */
     int32_t *status;      /* [walks] FG_WALK_* bits */
+    int32_t *best_n;      /* [walks][3] sizes of the best scheme (resizing; NULL = n) */
 } fg_records;
 
 typedef struct {

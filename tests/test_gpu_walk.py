@@ -53,8 +53,9 @@ def test_walk_matches_reference_kernel(path):
     d = golden_io.read_walk(path)
     ring = d["ring"]
     n1, n2, n3 = d["n"]
-    with fg.Engine(d["walks"], n1 * n2 * n3, ring, "reference", d["seed"], d["iterations"], d["plus_iterations"],
-                   d["expand_p"], d["reduce_p"]) as eng:
+    cap = 352 if d["resize_p"] > 0 else n1 * n2 * n3
+    with fg.Engine(d["walks"], cap, ring, "reference", d["seed"], d["iterations"], d["plus_iterations"],
+                   d["expand_p"], d["reduce_p"], resize_p=d["resize_p"]) as eng:
         eng.init_naive(n1, n2, n3)
         for L, block in enumerate(d["launches"]):
             eng.run(1)
@@ -64,6 +65,38 @@ def test_walk_matches_reference_kernel(path):
                 assert not errs, f"launch {L} walk {w}: {errs}"
         assert [int(x) for x in rec.rng_pos] == [t["used"] for t in d["tapes"]]
         assert eng.validate().all()
+        assert eng.validate(best=True).all()
+
+
+@pytest.mark.parametrize("mode,shape,S,iters,plus,resize_p,launches", [
+    ("reference", (3, 3, 3), 32, 300, 100, 0.3, 3),
+    ("reference", (2, 3, 4), 24, 200, 50, 0.9, 3),
+    ("philox", (2, 2, 3), 24, 200, 50, 0.7, 4),
+])
+def test_resize_vs_oracle(mode, shape, S, iters, plus, resize_p, launches):
+    """Resize meta-operators on the GPU (one warp per walk) against the oracle: sizes, factors,
+    lists, best schemes and sizes, best ranks and stream positions after every launch count."""
+    n1, n2, n3 = shape
+    seed = 500 + n1 + n2 + n3
+    with fg.Engine(S, 352, "z2", mode, seed, iters, plus, 0.01, 0.0, resize_p=resize_p) as eng:
+        eng.init_naive(n1, n2, n3)
+        rec0 = eng.records()
+        eng.run(launches)
+        rec = eng.records()
+        assert eng.validate().all() and eng.validate(best=True).all()
+    assert len({tuple(x) for x in rec.n}) > 1, "no walk changed size"
+    kw = dict(iterations=iters, plus_iterations=plus, expand_p=0.01, reduce_p=0.0, resize_p=resize_p, seed=seed)
+    b = batch_from(rec0)
+    b.best_n[:] = rec0.n
+    if mode == "reference":
+        used = int(rec.rng_pos.max())
+        draws, unis = fg.xorwow_tape(seed, 0, S, used)
+        tape = O.make_tape([(draws[w, :rec.rng_pos[w]], unis[w, :rec.rng_pos[w]]) for w in range(S)])
+        O.walk(b, b.cfg("tape", launches=launches, **kw), tape)
+    else:
+        O.walk(b, b.cfg("philox", launches=launches, **kw))
+    compare_records(rec, b, f"{mode} {shape}")
+    assert np.array_equal(rec.best_n, b.best_n)
 
 
 def batch_from(rec0):
