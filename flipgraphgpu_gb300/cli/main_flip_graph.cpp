@@ -9,8 +9,9 @@
 //   --max-launches N      stop after N launches (0: run forever, as the reference does)
 //   --target-rank R       stop once a walk's best rank reaches R (0: off)
 //   --time-budget S       stop after S seconds (0: off)
-// Not supported: resize, sandwiching and basis-change moves (their
-// probabilities are accepted; a positive value is reported and treated as 0).
+// Resize meta-operators (--resize-probability, default 0.2) run on the Z2 ring
+// in the reference and philox modes; elsewhere, and for sandwiching and
+// basis-change moves, a positive probability is reported and treated as 0.
 #include <algorithm>
 #include <chrono>
 #include <cstdio>
@@ -42,6 +43,7 @@ struct Options {
 class FlipGraph {
 public:
     FlipGraph(const Options &o) : o_(o), zt_(o.ring == "ZT") {
+        resizeOn_ = o.resize > 0 && !zt_ && o.mode != "fast";
         n2bestRank_[key(o.n1, o.n2, o.n3)] = o.n1 * o.n2 * o.n3;
         known_ = knownRanks(zt_);
     }
@@ -90,12 +92,16 @@ public:
         std::vector<double> elapsedTimes;
         for (long iteration = 0;; iteration++) {
             fg_stats st;
-            fg_status s = fg_run(h_, 1, &st);
+            fg_status s = resizeOn_ ? fg_run_walks(h_, 1, &st) : fg_run(h_, 1, &st);
             if (s != FG_OK && s != FG_ERR_WALK) check(s, "fg_run");
             auto t2 = Clock::now();
             elapsedTimes.push_back(std::chrono::duration_cast<std::chrono::milliseconds>(t2 - t1).count() / 1000.0);
             report(startTime, (int)iteration + 1, elapsedTimes);
             t1 = Clock::now();
+            if (resizeOn_) {
+                check(fg_resize(h_), "fg_resize");
+                updateRanks((int)iteration, true);
+            }
             if (o_.maxLaunches > 0 && iteration + 1 >= o_.maxLaunches) break;
             if (o_.targetRank > 0 && st.min_best_rank <= o_.targetRank) break;
             double total = std::chrono::duration_cast<std::chrono::milliseconds>(Clock::now() - startTime).count() / 1000.0;
@@ -138,6 +144,7 @@ private:
     };
 
     void create(int cap) {
+        if (resizeOn_) cap = FG_MAX_RANK + 2;  // products reach the maximal rank
         cap_ = cap;
         fg_config c{};
         c.ring = zt_ ? FG_RING_ZT : FG_RING_Z2;
@@ -150,6 +157,7 @@ private:
         c.expand_p = o_.expand;
         c.reduce_p = o_.reduce;
         c.device = 0;
+        c.resize_p = resizeOn_ ? o_.resize : 0.0;
         check(fg_create(&c, &h_), "fg_create");
     }
 
@@ -191,6 +199,50 @@ private:
         std::cout << "Initialized" << std::endl;
     }
 
+    // Keys of the walks' current sizes (they change while resizing).
+    void refreshKeys() {
+        const int S = o_.schemes;
+        std::vector<int32_t> n(3 * S);
+        check(fg_get_sizes(h_, n.data(), nullptr), "fg_get_sizes");
+        for (int w = 0; w < S; w++) {
+            keys_[w] = key(n[3 * w], n[3 * w + 1], n[3 * w + 2]);
+            unkeys_[w] = key(n[3 * w], n[3 * w + 1], n[3 * w + 2], false);
+            sortKeys_[w] = key(n[3 * w], n[3 * w + 1], n[3 * w + 2], true, true);
+        }
+    }
+
+    // updateRanks (flip_graph.cu:249-277): the best rank per size; an improving walk's
+    // current scheme becomes its best and is saved (with `save`).
+    void updateRanks(int iteration, bool save) {
+        const int S = o_.schemes;
+        refreshKeys();
+        std::vector<int32_t> m(S);
+        check(fg_get_counters(h_, m.data(), nullptr, nullptr, nullptr, nullptr, nullptr), "fg_get_counters");
+        std::unordered_map<std::string, int> n2bestIndex;
+        std::vector<int32_t> copies, ranks(S);
+        for (int i = 0; i < S; i++) {
+            auto it = n2bestRank_.find(keys_[i]);
+            if (it == n2bestRank_.end() || m[i] < it->second) {
+                n2bestRank_[keys_[i]] = m[i];
+                n2bestIndex[keys_[i]] = i;
+                copies.push_back(i);
+            }
+        }
+        check(fg_copy_to_best(h_, copies.data(), (int)copies.size()), "fg_copy_to_best");
+        for (int i = 0; i < S; i++) ranks[i] = n2bestRank_[keys_[i]];
+        check(fg_set_best_ranks(h_, ranks.data()), "fg_set_best_ranks");
+        if (save) {
+            for (auto pair : n2bestIndex) {
+                HostScheme s = fetchScheme(h_, pair.second, cap_, zt_, false);
+                std::string path = savePath(s, iteration, pair.second);
+                s.saveJson(path);
+                std::cout << "Best rank of " << pair.first << " was improved to " << ranks[pair.second]
+                          << " (known: " << known_[pair.first] << ")! Scheme saved to \"" << path << "\"" << std::endl;
+            }
+            if (n2bestIndex.size()) std::cout << std::endl;
+        }
+    }
+
     std::string savePath(const HostScheme &s, int iteration, int runId) const {  // flip_graph.cu:386-399
         std::ostringstream ss;
         ss << o_.path << "/" << key(s.n[0], s.n[1], s.n[2]) << "_m" << s.m << "_c" << s.complexity() << "_iteration"
@@ -201,6 +253,7 @@ private:
 
     void report(Clock::time_point startTime, int iteration, const std::vector<double> &times) {  // flip_graph.cu:303-380
         const int S = o_.schemes, count = 3;
+        if (resizeOn_) refreshKeys();
         std::vector<int32_t> m(S), bestRanks(S), bestM(S), flips(S);
         std::vector<uint8_t> valid(S);
         check(fg_get_counters(h_, m.data(), bestRanks.data(), bestM.data(), flips.data(), nullptr, valid.data()),
@@ -278,6 +331,7 @@ private:
 
     Options o_;
     bool zt_;
+    bool resizeOn_ = false;  // Z2 ring, list mode, resize probability > 0
     fg_handle *h_ = nullptr;
     int cap_ = 0;
     bool fromFile_ = false;
@@ -374,9 +428,11 @@ int main(int argc, char *argv[]) {
     std::cout << "  - resize: " << o.resize << std::endl;
     std::cout << "- log period: " << o.logPeriod << std::endl;
     std::cout << "- seed: " << o.seed << std::endl;
-    if (o.sandwiching > 0 || o.basis > 0 || o.resize > 0)
-        std::cout << "Note: resize, sandwiching and basis-change moves are not available in this engine; "
-                     "their probabilities are treated as 0" << std::endl;
+    const bool resizeHere = o.ring != "ZT" && o.mode != "fast";
+    if (o.sandwiching > 0 || o.basis > 0 || (o.resize > 0 && !resizeHere))
+        std::cout << "Note: sandwiching and basis-change moves, and resizing outside the Z2 ring's reference and "
+                     "philox modes, are not available in this engine; their probabilities are treated as 0"
+                  << std::endl;
 
     FlipGraph graph(o);
     if (o.inputPath != "null") {

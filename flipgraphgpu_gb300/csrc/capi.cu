@@ -651,6 +651,7 @@ fg_status fg_get_scheme(fg_handle *h, int walk, int best, int32_t *n, int32_t *m
     WalkHeader hd;
     FG_CUDA(cudaMemcpy(&hd, h->B.hdr + walk, sizeof(WalkHeader), cudaMemcpyDeviceToHost));
     if (n) for (int c = 0; c < 3; c++) n[c] = hd.n[c];
+    if (n && best && h->B.best_n) FG_CUDA(cudaMemcpy(n, h->B.best_n + walk * 3, 12, cudaMemcpyDeviceToHost));
     if (m) *m = best ? hd.best_m : hd.m;
     const size_t o = (size_t)walk * 3 * h->B.cap, nf = (size_t)3 * h->B.cap;
     if (fac) FG_CUDA(cudaMemcpy(fac, (best ? h->B.best_fac : h->B.fac) + o, nf * 8, cudaMemcpyDeviceToHost));
@@ -754,7 +755,68 @@ fg_status fg_get_records(fg_handle *h, fg_records *rec) {
     return FG_OK;
 }
 
+fg_status run_launches(fg_handle *h, int launches, fg_stats *stats, bool resizing);
+
 fg_status fg_run(fg_handle *h, int launches, fg_stats *stats) {
+    if (!h) return fail(FG_ERR_ARG, "null handle");
+    return run_launches(h, launches, stats, h->cfg.resize_p > 0);
+}
+
+fg_status fg_run_walks(fg_handle *h, int launches, fg_stats *stats) {
+    if (!h) return fail(FG_ERR_ARG, "null handle");
+    return run_launches(h, launches, stats, false);
+}
+
+fg_status fg_resize(fg_handle *h) {
+    if (!h) return fail(FG_ERR_ARG, "null handle");
+    if (!(h->cfg.resize_p > 0)) return fail(FG_ERR_STATE, "the handle was created without resizing");
+    if (!h->ready) return fail(FG_ERR_STATE, "records not initialised");
+    FG_CUDA(cudaSetDevice(h->dev));
+    FG_CUDA(launch_resize(h->B, h->P, h->cfg.mode == FG_MODE_REFERENCE ? RNG_XORWOW : RNG_PHILOX, h->cfg.resize_p,
+                          h->wpb, h->grid, h->stream));
+    FG_CUDA(cudaStreamSynchronize(h->stream));
+    return FG_OK;
+}
+
+fg_status fg_get_sizes(fg_handle *h, int32_t *n, int32_t *best_n) {
+    if (!h) return fail(FG_ERR_ARG, "null handle");
+    FG_CUDA(cudaSetDevice(h->dev));
+    FG_CUDA(cudaStreamSynchronize(h->stream));
+    const int S = h->B.S;
+    std::vector<WalkHeader> hdr(S);
+    FG_CUDA(cudaMemcpy(hdr.data(), h->B.hdr, sizeof(WalkHeader) * S, cudaMemcpyDeviceToHost));
+    for (int w = 0; w < S; w++)
+        for (int c = 0; c < 3; c++) {
+            if (n) n[w * 3 + c] = hdr[w].n[c];
+            if (best_n && !h->B.best_n) best_n[w * 3 + c] = hdr[w].n[c];
+        }
+    if (best_n && h->B.best_n) FG_CUDA(cudaMemcpy(best_n, h->B.best_n, (size_t)S * 12, cudaMemcpyDeviceToHost));
+    return FG_OK;
+}
+
+fg_status fg_copy_to_best(fg_handle *h, const int32_t *walks, int count) {
+    if (!h || (count > 0 && !walks) || count < 0 || count > h->B.S) return fail(FG_ERR_ARG, "bad argument");
+    if (!h->B.best_n) return fail(FG_ERR_STATE, "the handle was created without resizing");
+    for (int i = 0; i < count; i++)
+        if (walks[i] < 0 || walks[i] >= h->B.S) return fail(FG_ERR_ARG, "walk index out of range");
+    FG_CUDA(cudaSetDevice(h->dev));
+    if (count) FG_CUDA(cudaMemcpyAsync(h->d_copyList, walks, 4 * (size_t)count, cudaMemcpyHostToDevice, h->stream));
+    FG_CUDA(launch_copy_best(h->B, h->d_copyList, count, nullptr, h->stream));
+    FG_CUDA(cudaStreamSynchronize(h->stream));
+    return FG_OK;
+}
+
+fg_status fg_set_best_ranks(fg_handle *h, const int32_t *ranks) {
+    if (!h || !ranks) return fail(FG_ERR_ARG, "null argument");
+    if (!h->B.best_n) return fail(FG_ERR_STATE, "the handle was created without resizing");
+    FG_CUDA(cudaSetDevice(h->dev));
+    FG_CUDA(cudaMemcpyAsync(h->d_bestRanks, ranks, 4 * (size_t)h->B.S, cudaMemcpyHostToDevice, h->stream));
+    FG_CUDA(launch_copy_best(h->B, h->d_copyList, 0, h->d_bestRanks, h->stream));
+    FG_CUDA(cudaStreamSynchronize(h->stream));
+    return FG_OK;
+}
+
+fg_status run_launches(fg_handle *h, int launches, fg_stats *stats, bool resizing) {
     if (!h) return fail(FG_ERR_ARG, "null handle");
     if (!h->ready) return fail(FG_ERR_STATE, "records not initialised");
     if (launches < 0) return fail(FG_ERR_ARG, "launches must be >= 0");
@@ -763,7 +825,6 @@ fg_status fg_run(fg_handle *h, int launches, fg_stats *stats) {
     fg_stats acc{};
     acc.min_rank = acc.min_best_rank = 1 << 30;
     std::vector<WalkHeader> hdr(S);
-    const bool resizing = h->cfg.resize_p > 0;
     if (resizing && !h->tableReady) {
         fg_status us = update_ranks(h);
         if (us) return us;

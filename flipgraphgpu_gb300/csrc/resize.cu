@@ -385,8 +385,9 @@ __global__ void k_copy_best(DevBatch B, const int32_t *walks, int count, const i
         }
     }
     // every walk's best rank becomes its size's (one thread per walk)
-    for (int w = blockIdx.x * blockDim.x + threadIdx.x; w < B.S; w += gridDim.x * blockDim.x)
-        B.hdr[w].best_rank = bestRank[w];
+    if (bestRank)
+        for (int w = blockIdx.x * blockDim.x + threadIdx.x; w < B.S; w += gridDim.x * blockDim.x)
+            B.hdr[w].best_rank = bestRank[w];
 }
 
 }  // namespace

@@ -190,6 +190,21 @@ fg_status fg_get_scheme(fg_handle *h, int walk, int best, int32_t *n, int32_t *m
  * warp per walk above (0 = always warp, a large n = always thread). */
 fg_status fg_set_fast_split(fg_handle *h, int simt_max_cap);
 
+/* Resizing (resize_p > 0): fg_run performs, per launch, the walk launch, the
+ * resize step and the per-size best-rank update.  A caller that interleaves
+ * its own reporting (as the flip_graph executable mirrors FlipGraph::run,
+ * flip_graph.cu:286-299) drives the steps itself instead:
+ *   fg_run_walks      walk launches only (random step counts, verification);
+ *   fg_resize         the resize step of every walk (resizeKernel);
+ *   fg_get_sizes      current and best-scheme sizes, [walks][3] each;
+ *   fg_copy_to_best   the current schemes of `walks` become their best ones;
+ *   fg_set_best_ranks every walk's best rank (the per-size table's value). */
+fg_status fg_run_walks(fg_handle *h, int launches, fg_stats *stats);
+fg_status fg_resize(fg_handle *h);
+fg_status fg_get_sizes(fg_handle *h, int32_t *n, int32_t *best_n);
+fg_status fg_copy_to_best(fg_handle *h, const int32_t *walks, int count);
+fg_status fg_set_best_ranks(fg_handle *h, const int32_t *ranks);
+
 /* List modes: rebuilds every walk's three FlipSet lists from its current
  * factors in the reference's initFlips order (scheme_z2.cu:166-175) -- for
  * records set with empty lists.  A no-op in the fast and learned modes. */

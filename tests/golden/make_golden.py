@@ -93,11 +93,31 @@ def best_scheme_text(dump, header=True):
     return golden_io.scheme_to_text(s, dump["ring"], header=header), s
 
 
+# flip_graph with resizing (Z2 build): the run is bounded by time, so only files
+# saved in iterations below RESIZE_CLI_ITERATIONS are kept as the fixture.
+RESIZE_CLI_ARGS = ["-n1", "2", "-n2", "2", "-n3", "3", "--schemes", "64", "--max-iterations", "300",
+                   "--plus-iterations", "100", "--resize-probability", "0.3", "--seed", "73"]
+RESIZE_CLI_ITERATIONS = 4
+
+
+def cli_resize(out_dir):
+    fg_dir = os.path.join(out_dir, "cli_flip_graph_resize")
+    os.makedirs(fg_dir, exist_ok=True)
+    with open(os.path.join(out_dir, "cli_flip_graph_resize.log"), "w") as log:
+        subprocess.run(["timeout", "20", binary("z2", "flip_graph")] + RESIZE_CLI_ARGS + ["--path", fg_dir],
+                       stdout=log, stderr=subprocess.STDOUT)
+    for name in os.listdir(fg_dir):
+        it = int(name.split("_iteration")[1].split("_")[0])
+        if it >= RESIZE_CLI_ITERATIONS:
+            os.remove(os.path.join(fg_dir, name))
+
+
 def do_run(out_dir, resize_only=False):
     os.makedirs(out_dir, exist_ok=True)
     run([os.path.join(ROOT, "oracle", "build_ref.sh")])
     for case in RESIZE_CASES:
         walk(out_dir, case)
+    cli_resize(out_dir)
     if resize_only:
         return
     for case in WALK_CASES:
@@ -189,7 +209,7 @@ def do_pack(raw_dir):
             fo.write(data)
         if base not in manifest["files"]:
             manifest["files"].append(base)
-    for sub in ("cli_additions_reducer", "cli_complexity_minimizer", "cli_flip_graph"):
+    for sub in ("cli_additions_reducer", "cli_complexity_minimizer", "cli_flip_graph", "cli_flip_graph_resize"):
         src = os.path.join(raw_dir, sub)
         if os.path.isdir(src):
             dst = os.path.join(HERE, sub)

@@ -61,6 +61,25 @@ def test_flip_graph_matches_reference_executable(work):
     same_files(out, "cli_flip_graph")
 
 
+def test_flip_graph_with_resizing_matches_reference_executable(work):
+    """Resizing on (Z2 build): walks change size between launches; every scheme the reference saved
+    in its first iterations (report and best-rank table saves) is saved here identically."""
+    import sys
+    sys.path.insert(0, GOLDEN)
+    import make_golden
+    out = os.path.join(work, "fgr")
+    os.makedirs(out)
+    K = make_golden.RESIZE_CLI_ITERATIONS
+    run([os.path.join(BIN, "flip_graph")] + make_golden.RESIZE_CLI_ARGS +
+        ["--path", out, "--ring", "Z2", "--max-launches", str(K)], work)
+    want = sorted(os.listdir(os.path.join(GOLDEN, "cli_flip_graph_resize")))
+    got = sorted(x for x in os.listdir(out) if int(x.split("_iteration")[1].split("_")[0]) < K)
+    assert want and got == want, (got, want)
+    for name in want:
+        with open(os.path.join(GOLDEN, "cli_flip_graph_resize", name)) as a, open(os.path.join(out, name)) as b:
+            assert a.read() == b.read(), name
+
+
 def test_complexity_minimizer_matches_reference_executable(work):
     inp = unpack("input_minimizer_z2_333.txt", work)
     out = os.path.join(work, "cm")
