@@ -990,6 +990,251 @@ struct ZT {
             for (int c = 0; c < 3; c++) count += popc64(x[c][t].v);
         return count - 2 * m - nn[2];
     }
+
+    // ---------------------------------------------------------------- resize
+    // The Z2 operators on both masks of each coefficient vector (entry (i, j)
+    // of matrix c at bit i * n[c+1] + j; a negative entry's sign bit moves
+    // with its value bit): scheme_integer.cu:271-340, 573-905, 1103-1240.
+    void setN(int a, int b, int c) {
+        n[0] = a; n[1] = b; n[2] = c;
+        for (int q = 0; q < 3; q++) nn[q] = n[q] * n[(q + 1) % 3];
+    }
+    static uint64_t bit(uint64_t v, int k) { return (v >> k) & 1ull; }
+    // moves bit `from` of both masks to bit `to` of (ov, os)
+    static void moveBit(const Tern &a, int from, int to, uint64_t &ov, uint64_t &os) {
+        ov |= bit(a.v, from) << to;
+        os |= bit(a.s, from) << to;
+    }
+    static Tern mk(uint64_t v, uint64_t s) { Tern t; t.v = v; t.s = s & v; t.ok = true; return t; }
+    static Tern place(const Tern &a, int rows, int cols, int newCols, int di, int dj) {
+        uint64_t v = 0, sg = 0;
+        for (int i = 0; i < rows; i++)
+            for (int j = 0; j < cols; j++) moveBit(a, i * cols + j, (i + di) * newCols + j + dj, v, sg);
+        return mk(v, sg);
+    }
+
+    bool isValidProject(int i, int minN) const {
+        return n[i] - 1 >= minN && n[(i + 1) % 3] >= minN && n[(i + 2) % 3] >= minN;
+    }
+    bool isValidGrown(const int g[3], int rank, int maxN) const {
+        if (rank > kMaxRank) return false;
+        for (int q = 0; q < 3; q++)
+            if (g[q] * g[(q + 1) % 3] > kMaxMatrix || g[q] > maxN) return false;
+        return true;
+    }
+    bool isValidExtension(int i, int maxN) const {
+        int g[3] = {n[0], n[1], n[2]};
+        g[i] += 1;
+        return isValidGrown(g, m + g[(i + 1) % 3] * g[(i + 2) % 3], maxN);
+    }
+    bool isValidProduct(int i, int maxN) const {
+        int g[3] = {n[0], n[1], n[2]};
+        g[i] *= 2;
+        return isValidGrown(g, m * 2, maxN);
+    }
+
+    void project(int p, int q) {  // scheme_integer.cu:573-584
+        const int rc = (p + 2) % 3;
+        for (int t = 0; t < m; t++) {
+            {
+                const int rows = n[p], cols = n[(p + 1) % 3];
+                uint64_t v = 0, sg = 0;
+                for (int i = 0, i2 = 0; i < rows; i++) {
+                    if (i == q) continue;
+                    for (int j = 0; j < cols; j++) moveBit(x[p][t], i * cols + j, i2 * cols + j, v, sg);
+                    i2++;
+                }
+                x[p][t] = mk(v, sg);
+            }
+            {
+                const int rows = n[rc], cols = n[(rc + 1) % 3];
+                uint64_t v = 0, sg = 0;
+                for (int i = 0; i < rows; i++)
+                    for (int j = 0, j2 = 0; j < cols; j++) {
+                        if (j == q) continue;
+                        moveBit(x[rc][t], i * cols + j, i * (cols - 1) + j2, v, sg);
+                        j2++;
+                    }
+                x[rc][t] = mk(v, sg);
+            }
+        }
+        int g[3] = {n[0], n[1], n[2]};
+        g[p]--;
+        setN(g[0], g[1], g[2]);
+        removeZeroes();
+        fixSigns();
+        rebuildLists();
+    }
+
+    void extend(int p) {  // scheme_integer.cu:586-618
+        const int a = n[0], b = n[1], c = n[2];
+        const int col = p == 0 ? 2 : (p == 1 ? 0 : 1);
+        const int cr = col == 0 ? a : (col == 1 ? b : c), cc = col == 0 ? b : (col == 1 ? c : a);
+        for (int t = 0; t < m; t++) x[col][t] = place(x[col][t], cr, cc, cc + 1, 0, 0);
+        const int outer = p == 0 ? c : a, inner = p == 0 ? b : (p == 1 ? c : b);
+        for (int i = 0; i < outer; i++)
+            for (int j = 0; j < inner; j++) {
+                uint64_t u, v, w;
+                if (p == 0) { u = 1ull << (a * b + j); v = 1ull << (j * c + i); w = 1ull << (i * (a + 1) + a); }
+                else if (p == 1) { u = 1ull << (i * (b + 1) + b); v = 1ull << (b * c + j); w = 1ull << (j * a + i); }
+                else { u = 1ull << (i * b + j); v = 1ull << (j * (c + 1) + c); w = 1ull << (c * a + i); }
+                addTriplet(0, 1, 2, mk(u, 0), mk(v, 0), mk(w, 0));
+            }
+        int g[3] = {a, b, c};
+        g[p]++;
+        setN(g[0], g[1], g[2]);
+        rebuildLists();
+    }
+
+    void product(int p) {  // scheme_integer.cu:620-678
+        int g[3] = {n[0], n[1], n[2]}, d[3];
+        g[p] *= 2;
+        for (int q = 0; q < 3; q++) d[q] = q == p ? n[q] : 0;
+        for (int t = 0; t < m; t++)
+            for (int c = 0; c < 3; c++) {
+                const int c1 = (c + 1) % 3;
+                const Tern v = x[c][t];
+                x[c][t] = place(v, n[c], n[c1], g[c1], 0, 0);
+                x[c][t + m] = place(v, n[c], n[c1], g[c1], d[c], d[c1]);
+            }
+        m *= 2;
+        setN(g[0], g[1], g[2]);
+        rebuildLists();
+    }
+
+    void merge(const ZT &o, int p) {  // scheme_integer.cu:680-745
+        int g[3], d[3];
+        for (int q = 0; q < 3; q++) {
+            g[q] = q == p ? n[q] + o.n[q] : n[q];
+            d[q] = q == p ? n[q] : 0;
+        }
+        for (int t = 0; t < m; t++)
+            for (int c = 0; c < 3; c++) x[c][t] = place(x[c][t], n[c], n[(c + 1) % 3], g[(c + 1) % 3], 0, 0);
+        for (int t = 0; t < o.m; t++)
+            for (int c = 0; c < 3; c++) {
+                const int c1 = (c + 1) % 3;
+                x[c][m + t] = place(o.x[c][t], o.n[c], o.n[c1], g[c1], d[c], d[c1]);
+            }
+        m += o.m;
+        setN(g[0], g[1], g[2]);
+        rebuildLists();
+    }
+
+    void productWith(const ZT &o) {  // scheme_integer.cu:747-841: coefficients multiply
+        ZT *a = new ZT(*this);
+        setN(a->n[0] * o.n[0], a->n[1] * o.n[1], a->n[2] * o.n[2]);
+        m = a->m * o.m;
+        for (int t1 = 0; t1 < a->m; t1++)
+            for (int t2 = 0; t2 < o.m; t2++) {
+                const int t = t1 * o.m + t2;
+                for (int c = 0; c < 3; c++) {
+                    const int c1 = (c + 1) % 3;
+                    uint64_t v = 0, sg = 0;
+                    const Tern &p1 = a->x[c][t1], &p2 = o.x[c][t2];
+                    for (int e1 = 0; e1 < a->nn[c]; e1++) {
+                        if (!bit(p1.v, e1)) continue;
+                        const int r1 = e1 / a->n[c1], q1 = e1 % a->n[c1];
+                        for (int e2 = 0; e2 < o.nn[c]; e2++) {
+                            if (!bit(p2.v, e2)) continue;
+                            const int r2 = e2 / o.n[c1], q2 = e2 % o.n[c1];
+                            const int to = (r1 * o.n[c] + r2) * n[c1] + q1 * o.n[c1] + q2;
+                            v |= 1ull << to;
+                            sg |= (bit(p1.s, e1) ^ bit(p2.s, e2)) << to;
+                        }
+                    }
+                    x[c][t] = mk(v, sg);
+                }
+            }
+        delete a;
+        rebuildLists();
+    }
+
+    void swapSize(int p1, int p2) {  // scheme_integer.cu:843-905
+        if (p1 == p2) return;
+        if (p1 > p2) std::swap(p1, p2);
+        int idx[3];
+        if (p1 == 0 && p2 == 1) { idx[0] = 0; idx[1] = 2; idx[2] = 1; }
+        else if (p1 == 0 && p2 == 2) { idx[0] = 1; idx[1] = 0; idx[2] = 2; }
+        else { idx[0] = 2; idx[1] = 1; idx[2] = 0; }
+        int g[3];
+        for (int q = 0; q < 3; q++) g[q] = n[(idx[q] + 1) % 3];
+        for (int t = 0; t < m; t++) {
+            Tern v[3];
+            for (int c = 0; c < 3; c++) {
+                const int rows = g[c], cols = g[(c + 1) % 3];
+                uint64_t ov = 0, os = 0;
+                for (int i = 0; i < rows; i++)
+                    for (int j = 0; j < cols; j++) moveBit(x[idx[c]][t], j * rows + i, i * cols + j, ov, os);
+                v[c] = mk(ov, os);
+            }
+            for (int c = 0; c < 3; c++) x[c][t] = v[c];
+        }
+        setN(g[0], g[1], g[2]);
+        fixSigns();
+        rebuildLists();
+    }
+
+    void reduceAll() {
+        for (int guard = 0; tryReduce(); guard++)
+            if (guard > kRetryCap) { *status |= ST_RETRY; return; }
+    }
+    template <class R> bool tryProject(R &r, int minN = 2) {  // scheme_integer.cu:1103-1123
+        int idx[3], size = 0;
+        for (int i = 0; i < 3; i++)
+            if (isValidProject(i, minN)) idx[size++] = i;
+        if (!size) return false;
+        const int p = idx[r.raw() % (uint32_t)size];
+        const int q = (int)(r.raw() % (uint32_t)n[p]);
+        project(p, q);
+        reduceAll();
+        return true;
+    }
+    template <class R> bool tryExtend(R &r, int maxN = 16) {  // scheme_integer.cu:1125-1144
+        int idx[3], size = 0;
+        for (int i = 0; i < 3; i++)
+            if (isValidExtension(i, maxN)) idx[size++] = i;
+        if (!size) return false;
+        extend(idx[r.raw() % (uint32_t)size]);
+        reduceAll();
+        return true;
+    }
+    template <class R> bool tryProduct(R &r, int maxN = 16) {  // scheme_integer.cu:1146-1161
+        int idx[3], size = 0;
+        for (int i = 0; i < 3; i++)
+            if (isValidProduct(i, maxN)) idx[size++] = i;
+        if (!size) return false;
+        product(idx[r.raw() % (uint32_t)size]);
+        return true;
+    }
+    template <class R> bool tryMerge(const ZT &o, R &r) {  // scheme_integer.cu:1163-1192
+        if (m + o.m > kMaxRank) return false;
+        const bool eq0 = n[0] == o.n[0], eq1 = n[1] == o.n[1], eq2 = n[2] == o.n[2];
+        const int s0 = n[0] + o.n[0], s1 = n[1] + o.n[1], s2 = n[2] + o.n[2];
+        int p[3], size = 0;
+        if (s0 <= kMaxExtensionN && s0 * n[1] <= kMaxMatrix && s0 * n[2] <= kMaxMatrix && eq1 && eq2) p[size++] = 0;
+        if (eq0 && s1 <= kMaxExtensionN && n[0] * s1 <= kMaxMatrix && n[2] * s1 <= kMaxMatrix && eq2) p[size++] = 1;
+        if (eq0 && eq1 && s2 <= kMaxExtensionN && n[0] * s2 <= kMaxMatrix && n[1] * s2 <= kMaxMatrix) p[size++] = 2;
+        if (!size) return false;
+        merge(o, p[r.raw() % (uint32_t)size]);
+        return true;
+    }
+    bool tryProductWith(const ZT &o) {  // scheme_integer.cu:1194-1213
+        if (m * o.m > kMaxRank) return false;
+        int g[3];
+        for (int q = 0; q < 3; q++) g[q] = n[q] * o.n[q];
+        for (int q = 0; q < 3; q++)
+            if (g[q] > kMaxExtensionN || g[q] * g[(q + 1) % 3] > kMaxMatrix) return false;
+        productWith(o);
+        return true;
+    }
+    template <class R> void swapSizeRandom(R &r) {  // scheme_integer.cu:1235-1243
+        int p1, p2;
+        do {
+            p1 = (int)(r.raw() % 3u);
+            p2 = (int)(r.raw() % 3u);
+        } while (p1 == p2);
+        swapSize(p1, p2);
+    }
 };
 
 // ------------------------------------------------------------ record <-> scheme
@@ -1068,6 +1313,8 @@ void storeBestZ2(const Z2 &s, fgo_batch *b, int w, int cap) {
 void storeBestZT(const ZT &s, fgo_batch *b, int w, int cap) {
     if (s.m > cap) { b->status[w] |= ST_OVERFLOW; return; }
     b->best_m[w] = s.m;
+    if (b->best_n)
+        for (int c = 0; c < 3; c++) b->best_n[w * 3 + c] = s.n[c];
     for (int c = 0; c < 3; c++)
         for (int t = 0; t < cap; t++) {
             size_t q = facIndex(w, c, t, cap);
@@ -1418,7 +1665,7 @@ std::string sizeKey(const int n[3]) {  // getKey(scheme) with sorted sizes (util
     return std::to_string(a[0]) + "x" + std::to_string(a[1]) + "x" + std::to_string(a[2]);
 }
 
-void loadBestZ2(Z2 &s, const fgo_batch *b, int w, int cap) {
+void loadBest(Z2 &s, const fgo_batch *b, int w, int cap) {
     for (int c = 0; c < 3; c++) s.n[c] = b->best_n ? b->best_n[w * 3 + c] : b->n[w * 3 + c];
     for (int c = 0; c < 3; c++) s.nn[c] = s.n[c] * s.n[(c + 1) % 3];
     s.m = b->best_m[w];
@@ -1426,9 +1673,22 @@ void loadBestZ2(Z2 &s, const fgo_batch *b, int w, int cap) {
         for (int t = 0; t < s.m; t++) s.x[c][t] = b->best_fac[facIndex(w, c, t, cap)];
 }
 
+void loadBest(ZT &s, const fgo_batch *b, int w, int cap) {
+    for (int c = 0; c < 3; c++) s.n[c] = b->best_n ? b->best_n[w * 3 + c] : b->n[w * 3 + c];
+    for (int c = 0; c < 3; c++) s.nn[c] = s.n[c] * s.n[(c + 1) % 3];
+    s.m = b->best_m[w];
+    for (int c = 0; c < 3; c++)
+        for (int t = 0; t < s.m; t++) {
+            const size_t q = facIndex(w, c, t, cap);
+            s.x[c][t].v = b->best_fac[q];
+            s.x[c][t].s = b->best_sgn[q];
+            s.x[c][t].ok = b->best_valid[q] != 0;
+        }
+}
+
 // resizeKernel body (flip_graph.cu:575-613) for walk w; `best` holds every walk's best scheme.
-template <class R>
-void resizeStep(Z2 &s, R &r, const std::vector<Z2> &best, int S, double p) {
+template <class Scheme, class R>
+void resizeStep(Scheme &s, R &r, const std::vector<Scheme> &best, int S, double p) {
     if ((double)r.uniform() > p) return;
     if ((double)r.uniform() < 0.5) s.swapSizeRandom(r);
     bool merged = false;
@@ -1447,7 +1707,8 @@ void resizeStep(Z2 &s, R &r, const std::vector<Z2> &best, int S, double p) {
 // updateRanks (flip_graph.cu:249-266): the best rank per (sorted) size; a walk that
 // improves it has its current scheme copied to its best slot; every walk's best rank
 // becomes its size's.
-void updateRanks(std::map<std::string, int> &table, std::vector<Z2> &cur, std::vector<Z2> &best, fgo_batch *b,
+template <class Scheme>
+void updateRanks(std::map<std::string, int> &table, std::vector<Scheme> &cur, std::vector<Scheme> &best, fgo_batch *b,
                  int S, int cap) {
     std::vector<std::string> keys(S);
     for (int w = 0; w < S; w++) {
@@ -1456,7 +1717,7 @@ void updateRanks(std::map<std::string, int> &table, std::vector<Z2> &cur, std::v
         if (it == table.end() || cur[w].m < it->second) {
             table[keys[w]] = cur[w].m;
             best[w] = cur[w];
-            storeBestZ2(cur[w], b, w, cap);
+            storeBest(cur[w], b, w, cap);
         }
     }
     for (int w = 0; w < S; w++) b->best_rank[w] = table[keys[w]];
@@ -1466,13 +1727,13 @@ void updateRanks(std::map<std::string, int> &table, std::vector<Z2> &cur, std::v
 // walk, then the resize step of every walk, then the best-rank table.  The table starts from
 // the first walk's size at the naive rank, as the constructor sets it (flip_graph.cu:19), and
 // an update over the starting schemes (FlipGraph::initialize, flip_graph.cu:190-198).
-template <class R>
+template <class Scheme, class R>
 void runResize(const fgo_walk_cfg *cfg, int S, fgo_batch *b, std::vector<R> &rs) {
     const int cap = cfg->cap;
-    std::vector<Z2> cur(S), best(S);
+    std::vector<Scheme> cur(S), best(S);
     for (int w = 0; w < S; w++) {
-        loadZ2(cur[w], b, w, cap);
-        loadBestZ2(best[w], b, w, cap);
+        loadScheme(cur[w], b, w, cap);
+        loadBest(best[w], b, w, cap);
         cur[w].status = best[w].status = &b->status[w];
     }
     std::map<std::string, int> table;
@@ -1482,19 +1743,20 @@ void runResize(const fgo_walk_cfg *cfg, int S, fgo_batch *b, std::vector<R> &rs)
         for (int w = 0; w < S; w++) {
             if (b->status[w]) continue;
             walkLaunch(cur[w], rs[w], cfg, b, w);
-            loadBestZ2(best[w], b, w, cap);
+            loadBest(best[w], b, w, cap);
         }
         for (int w = 0; w < S; w++)
             if (!b->status[w]) resizeStep(cur[w], rs[w], best, S, cfg->resize_p);
         updateRanks(table, cur, best, b, S, cap);
     }
     for (int w = 0; w < S; w++) {
-        storeZ2(cur[w], b, w, cap);
+        storeScheme(cur[w], b, w, cap);
         b->rng_pos[w] = rs[w].pos;
     }
 }
 
-void runWalksResizeZ2(const fgo_walk_cfg *cfg, int S, fgo_batch *b, const fgo_tape *tape) {
+template <class Scheme>
+void runWalksResize(const fgo_walk_cfg *cfg, int S, fgo_batch *b, const fgo_tape *tape) {
     if (cfg->rng == FGO_RNG_TAPE) {
         std::vector<RefDraws> rs(S);
         for (int w = 0; w < S; w++) {
@@ -1505,7 +1767,7 @@ void runWalksResizeZ2(const fgo_walk_cfg *cfg, int S, fgo_batch *b, const fgo_ta
             r.pos = b->rng_pos[w];
             r.status = &b->status[w];
         }
-        runResize(cfg, S, b, rs);
+        runResize<Scheme>(cfg, S, b, rs);
     } else {
         std::vector<FastDraws> rs(S);
         for (int w = 0; w < S; w++) {
@@ -1516,7 +1778,7 @@ void runWalksResizeZ2(const fgo_walk_cfg *cfg, int S, fgo_batch *b, const fgo_ta
             r.pos = b->rng_pos[w];
             r.status = &b->status[w];
         }
-        runResize(cfg, S, b, rs);
+        runResize<Scheme>(cfg, S, b, rs);
     }
 }
 
@@ -1558,8 +1820,9 @@ int fgo_init_naive(const fgo_walk_cfg *cfg, int S, int n1, int n2, int n3, fgo_b
 
 int fgo_walk(const fgo_walk_cfg *cfg, int S, fgo_batch *b, const fgo_tape *tape) {
     if (cfg->resize_p > 0) {
-        if (cfg->ring != FGO_RING_Z2 || cfg->rng == FGO_RNG_FAST) return -1;
-        runWalksResizeZ2(cfg, S, b, tape);
+        if (cfg->rng == FGO_RNG_FAST) return -1;
+        if (cfg->ring == FGO_RING_Z2) runWalksResize<Z2>(cfg, S, b, tape);
+        else runWalksResize<ZT>(cfg, S, b, tape);
         int bad = 0;
         for (int w = 0; w < S; w++) bad += b->status[w] != 0;
         return bad;

@@ -50,6 +50,8 @@ WALK_CASES = [
 RESIZE_CASES = [
     ("z2_222_resize", "z2", 2, 2, 2, 12, 150, 40, 0.01, 0.0, 41, 4, 0.5),
     ("z2_233_resize", "z2", 2, 3, 3, 8, 200, 60, 0.01, 0.0, 42, 3, 0.8),
+    ("zt_222_resize", "zt", 2, 2, 2, 6, 50, 30, 0.01, 0.0, 51, 4, 0.6),
+    ("zt_223_resize", "zt", 2, 2, 3, 6, 60, 40, 0.01, 0.0, 52, 3, 0.9),
 ]
 
 # Long walks used only to produce low-rank input schemes for the reducer and
@@ -98,18 +100,24 @@ def best_scheme_text(dump, header=True):
 RESIZE_CLI_ARGS = ["-n1", "2", "-n2", "2", "-n3", "3", "--schemes", "64", "--max-iterations", "300",
                    "--plus-iterations", "100", "--resize-probability", "0.3", "--seed", "73"]
 RESIZE_CLI_ITERATIONS = 4
+# The reference's default configuration: the ZT build with its default resize
+# probability (0.2) -- no resize flag at all.
+RESIZE_CLI_ARGS_ZT = ["-n1", "2", "-n2", "2", "-n3", "3", "--schemes", "48", "--max-iterations", "200",
+                      "--plus-iterations", "100", "--seed", "75"]
 
 
 def cli_resize(out_dir):
-    fg_dir = os.path.join(out_dir, "cli_flip_graph_resize")
-    os.makedirs(fg_dir, exist_ok=True)
-    with open(os.path.join(out_dir, "cli_flip_graph_resize.log"), "w") as log:
-        subprocess.run(["timeout", "20", binary("z2", "flip_graph")] + RESIZE_CLI_ARGS + ["--path", fg_dir],
-                       stdout=log, stderr=subprocess.STDOUT)
-    for name in os.listdir(fg_dir):
-        it = int(name.split("_iteration")[1].split("_")[0])
-        if it >= RESIZE_CLI_ITERATIONS:
-            os.remove(os.path.join(fg_dir, name))
+    for ring, sub, args in (("z2", "cli_flip_graph_resize", RESIZE_CLI_ARGS),
+                            ("zt", "cli_flip_graph_resize_zt", RESIZE_CLI_ARGS_ZT)):
+        fg_dir = os.path.join(out_dir, sub)
+        os.makedirs(fg_dir, exist_ok=True)
+        with open(os.path.join(out_dir, sub + ".log"), "w") as log:
+            subprocess.run(["timeout", "20", binary(ring, "flip_graph")] + args + ["--path", fg_dir],
+                           stdout=log, stderr=subprocess.STDOUT)
+        for name in os.listdir(fg_dir):
+            it = int(name.split("_iteration")[1].split("_")[0])
+            if it >= RESIZE_CLI_ITERATIONS:
+                os.remove(os.path.join(fg_dir, name))
 
 
 def do_run(out_dir, resize_only=False):
@@ -209,7 +217,8 @@ def do_pack(raw_dir):
             fo.write(data)
         if base not in manifest["files"]:
             manifest["files"].append(base)
-    for sub in ("cli_additions_reducer", "cli_complexity_minimizer", "cli_flip_graph", "cli_flip_graph_resize"):
+    for sub in ("cli_additions_reducer", "cli_complexity_minimizer", "cli_flip_graph", "cli_flip_graph_resize",
+                "cli_flip_graph_resize_zt"):
         src = os.path.join(raw_dir, sub)
         if os.path.isdir(src):
             dst = os.path.join(HERE, sub)
