@@ -9,8 +9,8 @@
 //   --max-launches N      stop after N launches (0: run forever, as the reference does)
 //   --target-rank R       stop once a walk's best rank reaches R (0: off)
 //   --time-budget S       stop after S seconds (0: off)
-// Resize meta-operators (--resize-probability, default 0.2) run on the Z2 ring
-// in the reference and philox modes; elsewhere, and for sandwiching and
+// Resize meta-operators (--resize-probability, default 0.2) run on both rings
+// in the reference and philox modes; in the fast mode, and for sandwiching and
 // basis-change moves, a positive probability is reported and treated as 0.
 #include <algorithm>
 #include <chrono>
@@ -43,7 +43,7 @@ struct Options {
 class FlipGraph {
 public:
     FlipGraph(const Options &o) : o_(o), zt_(o.ring == "ZT") {
-        resizeOn_ = o.resize > 0 && !zt_ && o.mode != "fast";
+        resizeOn_ = o.resize > 0 && o.mode != "fast";
         n2bestRank_[key(o.n1, o.n2, o.n3)] = o.n1 * o.n2 * o.n3;
         known_ = knownRanks(zt_);
     }
@@ -331,7 +331,7 @@ private:
 
     Options o_;
     bool zt_;
-    bool resizeOn_ = false;  // Z2 ring, list mode, resize probability > 0
+    bool resizeOn_ = false;  // list mode and resize probability > 0
     fg_handle *h_ = nullptr;
     int cap_ = 0;
     bool fromFile_ = false;
@@ -428,10 +428,10 @@ int main(int argc, char *argv[]) {
     std::cout << "  - resize: " << o.resize << std::endl;
     std::cout << "- log period: " << o.logPeriod << std::endl;
     std::cout << "- seed: " << o.seed << std::endl;
-    const bool resizeHere = o.ring != "ZT" && o.mode != "fast";
+    const bool resizeHere = o.mode != "fast";
     if (o.sandwiching > 0 || o.basis > 0 || (o.resize > 0 && !resizeHere))
-        std::cout << "Note: sandwiching and basis-change moves, and resizing outside the Z2 ring's reference and "
-                     "philox modes, are not available in this engine; their probabilities are treated as 0"
+        std::cout << "Note: sandwiching and basis-change moves, and resizing in the fast mode, are not available "
+                     "in this engine; their probabilities are treated as 0"
                   << std::endl;
 
     FlipGraph graph(o);

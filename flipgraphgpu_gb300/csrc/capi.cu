@@ -130,6 +130,7 @@ __global__ void k_verify_zt(DevBatch B, int best, uint8_t *out) {
     uint64_t *xs = xv + 3 * cap;
     for (int w = blockIdx.x * wpb + warp; w < B.S; w += gridDim.x * wpb) {
         const WalkHeader h = B.hdr[w];
+        const int32_t *dims = best && B.best_n ? B.best_n + w * 3 : h.n;
         const size_t o = (size_t)w * 3 * cap;
         const uint64_t *sv = best ? B.best_fac : B.fac, *ss = best ? B.best_sgn : B.sgn;
         const uint8_t *sk = best ? B.best_valid : B.valid;
@@ -141,7 +142,7 @@ __global__ void k_verify_zt(DevBatch B, int best, uint8_t *out) {
             if ((q % cap) < m && !sk[o + q]) ok = false;
         }
         __syncwarp();
-        const int n0 = h.n[0], n1 = h.n[1], n2 = h.n[2];
+        const int n0 = dims[0], n1 = dims[1], n2 = dims[2];
         const int nn0 = n0 * n1, nn1 = n1 * n2, nn2 = n2 * n0;
         for (int q = lane; ok && q < nn0 * nn1 * nn2; q += 32) {
             const int i = q / (nn1 * nn2), j = (q / nn2) % nn1, k = q % nn2;
@@ -424,8 +425,8 @@ fg_status fg_create(const fg_config *cfg, fg_handle **out) {
         return fail(FG_ERR_ARG, "unknown mode");
     if (cfg->cap <= 0 || slots_for_cap(cfg->cap) == 0 || cfg->cap > FG_MAX_RANK + 2)
         return fail(FG_ERR_CAPACITY, "cap must be in [1, 352]");
-    if (cfg->resize_p > 0 && (cfg->ring != FG_RING_Z2 || (cfg->mode != FG_MODE_REFERENCE && cfg->mode != FG_MODE_PHILOX_LISTS)))
-        return fail(FG_ERR_ARG, "resizing runs on the Z2 ring in a list mode");
+    if (cfg->resize_p > 0 && cfg->mode != FG_MODE_REFERENCE && cfg->mode != FG_MODE_PHILOX_LISTS)
+        return fail(FG_ERR_ARG, "resizing runs in a list mode (reference or philox)");
     if (cfg->resize_p > 0 && cfg->cap < FG_MAX_RANK)
         return fail(FG_ERR_CAPACITY, "resizing needs cap >= 350 (products reach the maximal rank)");
     if (cfg->iterations <= 0) return fail(FG_ERR_ARG, "iterations must be positive");
@@ -772,7 +773,7 @@ fg_status fg_resize(fg_handle *h) {
     if (!(h->cfg.resize_p > 0)) return fail(FG_ERR_STATE, "the handle was created without resizing");
     if (!h->ready) return fail(FG_ERR_STATE, "records not initialised");
     FG_CUDA(cudaSetDevice(h->dev));
-    FG_CUDA(launch_resize(h->B, h->P, h->cfg.mode == FG_MODE_REFERENCE ? RNG_XORWOW : RNG_PHILOX, h->cfg.resize_p,
+    FG_CUDA(launch_resize(h->cfg.ring, h->B, h->P, h->cfg.mode == FG_MODE_REFERENCE ? RNG_XORWOW : RNG_PHILOX, h->cfg.resize_p,
                           h->wpb, h->grid, h->stream));
     FG_CUDA(cudaStreamSynchronize(h->stream));
     return FG_OK;
@@ -834,7 +835,7 @@ fg_status run_launches(fg_handle *h, int launches, fg_stats *stats, bool resizin
         fg_status ls = launch_walks(h);
         if (ls) return ls;
         if (resizing) {
-            FG_CUDA(launch_resize(h->B, h->P, h->cfg.mode == FG_MODE_REFERENCE ? RNG_XORWOW : RNG_PHILOX,
+            FG_CUDA(launch_resize(h->cfg.ring, h->B, h->P, h->cfg.mode == FG_MODE_REFERENCE ? RNG_XORWOW : RNG_PHILOX,
                                   h->cfg.resize_p, h->wpb, h->grid, h->stream));
             fg_status us = update_ranks(h);
             if (us) return us;

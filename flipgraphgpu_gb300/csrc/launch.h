@@ -28,7 +28,8 @@ int occupancy_walk(int ring, int cap, int rng, int wpb);
 cudaError_t launch_walk_simt(const DevBatch &B, const WalkParams &P, int first, int count, int scap, int wide,
                              int wpb, int sms, cudaStream_t s);
 // Resize meta-operators (one warp per walk, Z2, cap 352) and the best-rank table's copies.
-cudaError_t launch_resize(const DevBatch &B, const WalkParams &P, int rng, double p, int wpb, int grid, cudaStream_t s);
+cudaError_t launch_resize(int ring, const DevBatch &B, const WalkParams &P, int rng, double p, int wpb, int grid,
+                          cudaStream_t s);
 cudaError_t launch_copy_best(const DevBatch &B, const int32_t *walks, int count, const int32_t *bestRank, cudaStream_t s);
 // Fast mode, `lanes` (4, 8 or 16; 0 = by slot count) lanes per walk (same semantics as launch_walk_simt).
 cudaError_t launch_walk_group(const DevBatch &B, const WalkParams &P, int first, int count, int scap, int wide,

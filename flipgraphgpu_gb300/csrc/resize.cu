@@ -24,11 +24,47 @@ constexpr int kMaxRankRef = 350;    // config.cuh:10
 
 __device__ __forceinline__ uint64_t bit(uint64_t v, int k) { return (v >> k) & 1ull; }
 
+// A coefficient vector: Z2 factor bits in v (s = 0); ZT values in v, signs in s
+// (a negative entry's sign bit moves with its value bit).
+struct Vec {
+    uint64_t v, s;
+};
+
+// Ring access for the two walkers: word (c, t) of the walk in shared memory.
+template <class Z> struct RingOps;
+template <class R, int S> struct RingOps<Z2Walk<R, S>> {
+    using Z = Z2Walk<R, S>;
+    __device__ static Vec get(const Z &z, int c, int t) { return Vec{z.x[c * z.cap + t], 0}; }
+    __device__ static void put(Z &z, int c, int t, Vec w) { z.x[c * z.cap + t] = w.v; }
+    __device__ static void fixSigns(Z &) {}
+    __device__ static void stash(const Z &z, uint64_t *ownV, uint64_t *) {
+        for (int q = lane_id(); q < 3 * z.cap; q += 32) ownV[q] = z.x[q];
+    }
+};
+template <class R, int S> struct RingOps<ZTWalk<R, S>> {
+    using Z = ZTWalk<R, S>;
+    __device__ static Vec get(const Z &z, int c, int t) { return Vec{z.xv[c * z.cap + t], z.xs[c * z.cap + t]}; }
+    __device__ static void put(Z &z, int c, int t, Vec w) {
+        const int q = c * z.cap + t;
+        z.xv[q] = w.v;
+        z.xs[q] = w.s & w.v;
+        z.xo[q] = 1;
+    }
+    __device__ static void fixSigns(Z &z) { z.fixSigns(); }
+    __device__ static void stash(const Z &z, uint64_t *ownV, uint64_t *ownS) {
+        for (int q = lane_id(); q < 3 * z.cap; q += 32) { ownV[q] = z.xv[q]; ownS[q] = z.xs[q]; }
+    }
+};
+
 // Entry (i, j) of a rows x cols matrix to (i + di, j + dj) of a matrix with newCols columns.
-__device__ uint64_t place(uint64_t v, int rows, int cols, int newCols, int di, int dj) {
-    uint64_t o = 0;
+__device__ Vec place(Vec a, int rows, int cols, int newCols, int di, int dj) {
+    Vec o{0, 0};
     for (int i = 0; i < rows; i++)
-        for (int j = 0; j < cols; j++) o |= bit(v, i * cols + j) << ((i + di) * newCols + j + dj);
+        for (int j = 0; j < cols; j++) {
+            const int from = i * cols + j, to = (i + di) * newCols + j + dj;
+            o.v |= bit(a.v, from) << to;
+            o.s |= bit(a.s, from) << to;
+        }
     return o;
 }
 
@@ -44,14 +80,15 @@ __device__ __forceinline__ int nsz(const Z &z, int i) { return i == 0 ? z.n0 : (
 
 // Another walk's best scheme, read in place from the records.
 struct BestView {
-    const uint64_t *fac;  // [3][cap]
+    const uint64_t *fac, *sgn;  // [3][cap]; sgn null for Z2
     int cap, n[3], m;
-    __device__ uint64_t X(int c, int t) const { return fac[c * cap + t]; }
+    __device__ Vec X(int c, int t) const { return Vec{fac[c * cap + t], sgn ? sgn[c * cap + t] : 0}; }
 };
 
 __device__ BestView best_view(const DevBatch &B, int index) {
     BestView o;
     o.fac = B.best_fac + (size_t)index * 3 * B.cap;
+    o.sgn = B.best_sgn ? B.best_sgn + (size_t)index * 3 * B.cap : nullptr;
     o.cap = B.cap;
     o.m = B.hdr[index].best_m;
     for (int c = 0; c < 3; c++) o.n[c] = B.best_n[index * 3 + c];
@@ -59,7 +96,8 @@ __device__ BestView best_view(const DevBatch &B, int index) {
 }
 
 template <class Z>
-__device__ void swap_size(Z &z, int p1, int p2) {  // scheme_z2.cu:916-979
+__device__ void swap_size(Z &z, int p1, int p2) {  // scheme_z2.cu:916-979, scheme_integer.cu:843-905
+    using O = RingOps<Z>;
     if (p1 == p2) return;
     if (p1 > p2) { int t = p1; p1 = p2; p2 = t; }
     int idx[3];
@@ -70,18 +108,23 @@ __device__ void swap_size(Z &z, int p1, int p2) {  // scheme_z2.cu:916-979
     for (int q = 0; q < 3; q++) g[q] = nsz(z, (idx[q] + 1) % 3);
     __syncwarp();
     for (int t = lane_id(); t < z.m; t += 32) {
-        uint64_t v[3];
+        Vec v[3];
         for (int c = 0; c < 3; c++) {  // new matrix c is the transpose of old matrix idx[c]
             const int rows = g[c], cols = g[(c + 1) % 3];
-            uint64_t o = 0;
+            const Vec a = O::get(z, idx[c], t);
+            Vec o{0, 0};
             for (int i = 0; i < rows; i++)
-                for (int j = 0; j < cols; j++) o |= bit(z.X(idx[c], t), j * rows + i) << (i * cols + j);
+                for (int j = 0; j < cols; j++) {
+                    o.v |= bit(a.v, j * rows + i) << (i * cols + j);
+                    o.s |= bit(a.s, j * rows + i) << (i * cols + j);
+                }
             v[c] = o;
         }
-        for (int c = 0; c < 3; c++) z.x[c * z.cap + t] = v[c];
+        for (int c = 0; c < 3; c++) O::put(z, c, t, v[c]);
     }
     __syncwarp();
     set_sizes(z, g[0], g[1], g[2]);
+    O::fixSigns(z);
     z.rebuild();
 }
 
@@ -92,31 +135,38 @@ __device__ void reduce_all(Z &z) {  // while (tryReduce()) ; bounded
 }
 
 template <class Z>
-__device__ void project(Z &z, int p, int q) {  // scheme_z2.cu:643-653 (excludeRow / excludeColumn, 184-224)
+__device__ void project(Z &z, int p, int q) {  // scheme_z2.cu:643-653, scheme_integer.cu:573-584
+    using O = RingOps<Z>;
     const int rc = (p + 2) % 3;  // matrix losing column q
     const int n[3] = {z.n0, z.n1, z.n2};
     __syncwarp();
     for (int t = lane_id(); t < z.m; t += 32) {
         {  // matrix p: drop row q
             const int rows = n[p], cols = n[(p + 1) % 3];
-            uint64_t v = 0;
+            const Vec a = O::get(z, p, t);
+            Vec o{0, 0};
             for (int i = 0, i2 = 0; i < rows; i++) {
                 if (i == q) continue;
-                for (int j = 0; j < cols; j++) v |= bit(z.X(p, t), i * cols + j) << (i2 * cols + j);
+                for (int j = 0; j < cols; j++) {
+                    o.v |= bit(a.v, i * cols + j) << (i2 * cols + j);
+                    o.s |= bit(a.s, i * cols + j) << (i2 * cols + j);
+                }
                 i2++;
             }
-            z.x[p * z.cap + t] = v;
+            O::put(z, p, t, o);
         }
         {  // matrix rc: drop column q
             const int rows = n[rc], cols = n[(rc + 1) % 3];
-            uint64_t v = 0;
+            const Vec a = O::get(z, rc, t);
+            Vec o{0, 0};
             for (int i = 0; i < rows; i++)
                 for (int j = 0, j2 = 0; j < cols; j++) {
                     if (j == q) continue;
-                    v |= bit(z.X(rc, t), i * cols + j) << (i * (cols - 1) + j2);
+                    o.v |= bit(a.v, i * cols + j) << (i * (cols - 1) + j2);
+                    o.s |= bit(a.s, i * cols + j) << (i * (cols - 1) + j2);
                     j2++;
                 }
-            z.x[rc * z.cap + t] = v;
+            O::put(z, rc, t, o);
         }
     }
     __syncwarp();
@@ -124,23 +174,20 @@ __device__ void project(Z &z, int p, int q) {  // scheme_z2.cu:643-653 (excludeR
     g[p]--;
     set_sizes(z, g[0], g[1], g[2]);
     z.removeZeroes();
+    O::fixSigns(z);
     z.rebuild();
 }
 
 template <class Z>
-__device__ void extend(Z &z, int p) {  // scheme_z2.cu:655-687: terms added with the old sizes
+__device__ void extend(Z &z, int p) {  // scheme_z2.cu:655-687, scheme_integer.cu:586-618 (old sizes)
+    using O = RingOps<Z>;
     const int a = z.n0, b = z.n1, c = z.n2;
     const int col = p == 0 ? 2 : (p == 1 ? 0 : 1);  // matrix gaining a column (addColumn)
     const int cr = col == 0 ? a : (col == 1 ? b : c), cc = col == 0 ? b : (col == 1 ? c : a);
     const int m0 = z.m;
     __syncwarp();
-    for (int t = lane_id(); t < m0; t += 32) {
-        uint64_t v = 0;
-        for (int i = 0; i < cr; i++)
-            for (int j = 0; j < cc; j++) v |= bit(z.X(col, t), i * cc + j) << (i * (cc + 1) + j);
-        z.x[col * z.cap + t] = v;
-    }
-    // new terms, in the reference's loop order
+    for (int t = lane_id(); t < m0; t += 32) O::put(z, col, t, place(O::get(z, col, t), cr, cc, cc + 1, 0, 0));
+    // new terms, in the reference's loop order, each a single +1 entry per matrix
     const int outer = p == 0 ? c : a, inner = p == 0 ? b : (p == 1 ? c : b);
     for (int q = lane_id(); q < outer * inner; q += 32) {
         const int i = q / inner, j = q % inner, t = m0 + q;
@@ -148,9 +195,9 @@ __device__ void extend(Z &z, int p) {  // scheme_z2.cu:655-687: terms added with
         if (p == 0) { u = 1ull << (a * b + j); v = 1ull << (j * c + i); w = 1ull << (i * (a + 1) + a); }
         else if (p == 1) { u = 1ull << (i * (b + 1) + b); v = 1ull << (b * c + j); w = 1ull << (j * a + i); }
         else { u = 1ull << (i * b + j); v = 1ull << (j * (c + 1) + c); w = 1ull << (c * a + i); }
-        z.x[t] = u;
-        z.x[z.cap + t] = v;
-        z.x[2 * z.cap + t] = w;
+        O::put(z, 0, t, Vec{u, 0});
+        O::put(z, 1, t, Vec{v, 0});
+        O::put(z, 2, t, Vec{w, 0});
     }
     __syncwarp();
     z.m = m0 + outer * inner;
@@ -161,7 +208,8 @@ __device__ void extend(Z &z, int p) {  // scheme_z2.cu:655-687: terms added with
 }
 
 template <class Z>
-__device__ void product(Z &z, int p) {  // scheme_z2.cu:689-747: block-diagonal doubling of size p
+__device__ void product(Z &z, int p) {  // scheme_z2.cu:689-747, scheme_integer.cu:620-678
+    using O = RingOps<Z>;
     const int n[3] = {z.n0, z.n1, z.n2};
     int g[3] = {n[0], n[1], n[2]}, d[3];
     g[p] *= 2;
@@ -171,9 +219,9 @@ __device__ void product(Z &z, int p) {  // scheme_z2.cu:689-747: block-diagonal 
     for (int t = lane_id(); t < m0; t += 32)
         for (int c = 0; c < 3; c++) {
             const int c1 = (c + 1) % 3;
-            const uint64_t v = z.X(c, t);
-            z.x[c * z.cap + t] = place(v, n[c], n[c1], g[c1], 0, 0);
-            z.x[c * z.cap + t + m0] = place(v, n[c], n[c1], g[c1], d[c], d[c1]);
+            const Vec v = O::get(z, c, t);
+            O::put(z, c, t, place(v, n[c], n[c1], g[c1], 0, 0));
+            O::put(z, c, t + m0, place(v, n[c], n[c1], g[c1], d[c], d[c1]));
         }
     __syncwarp();
     z.m = 2 * m0;
@@ -182,7 +230,8 @@ __device__ void product(Z &z, int p) {  // scheme_z2.cu:689-747: block-diagonal 
 }
 
 template <class Z>
-__device__ void merge(Z &z, const BestView &o, int p) {  // scheme_z2.cu:749-817
+__device__ void merge(Z &z, const BestView &o, int p) {  // scheme_z2.cu:749-817, scheme_integer.cu:680-745
+    using O = RingOps<Z>;
     const int n[3] = {z.n0, z.n1, z.n2};
     int g[3], d[3];
     for (int q = 0; q < 3; q++) {
@@ -192,11 +241,11 @@ __device__ void merge(Z &z, const BestView &o, int p) {  // scheme_z2.cu:749-817
     const int m0 = z.m;
     __syncwarp();
     for (int t = lane_id(); t < m0; t += 32)
-        for (int c = 0; c < 3; c++) z.x[c * z.cap + t] = place(z.X(c, t), n[c], n[(c + 1) % 3], g[(c + 1) % 3], 0, 0);
+        for (int c = 0; c < 3; c++) O::put(z, c, t, place(O::get(z, c, t), n[c], n[(c + 1) % 3], g[(c + 1) % 3], 0, 0));
     for (int t = lane_id(); t < o.m; t += 32)
         for (int c = 0; c < 3; c++) {
             const int c1 = (c + 1) % 3;
-            z.x[c * z.cap + m0 + t] = place(o.X(c, t), o.n[c], o.n[c1], g[c1], d[c], d[c1]);
+            O::put(z, c, m0 + t, place(o.X(c, t), o.n[c], o.n[c1], g[c1], d[c], d[c1]));
         }
     __syncwarp();
     z.m = m0 + o.m;
@@ -204,14 +253,16 @@ __device__ void merge(Z &z, const BestView &o, int p) {  // scheme_z2.cu:749-817
     z.rebuild();
 }
 
-// Tensor product with another walk's best scheme (scheme_z2.cu:819-862): term
-// (t1, t2) -> t1 * m2 + t2.  The walk's own terms are read from `own`, a copy
-// in the walk's global record, since the new terms overwrite them.
+// Tensor product with another walk's best scheme (scheme_z2.cu:819-862,
+// scheme_integer.cu:747-841): term (t1, t2) -> t1 * m2 + t2, coefficients
+// multiplied.  The walk's own terms are read from a copy in its global record,
+// since the new terms overwrite them.
 template <class Z>
-__device__ void product_with(Z &z, const BestView &o, uint64_t *own) {
+__device__ void product_with(Z &z, const BestView &o, uint64_t *ownV, uint64_t *ownS) {
+    using O = RingOps<Z>;
     const int a0 = z.n0, a1 = z.n1, a2 = z.n2, m1 = z.m;
     __syncwarp();
-    for (int q = lane_id(); q < 3 * z.cap; q += 32) own[q] = z.x[q];
+    O::stash(z, ownV, ownS);
     __syncwarp();
     const int an[3] = {a0, a1, a2};
     int g[3];
@@ -220,18 +271,20 @@ __device__ void product_with(Z &z, const BestView &o, uint64_t *own) {
         const int t1 = t / o.m, t2 = t % o.m;
         for (int c = 0; c < 3; c++) {
             const int c1 = (c + 1) % 3;
-            const uint64_t va = own[c * z.cap + t1], vb = o.X(c, t2);
-            uint64_t v = 0;
+            const Vec va{ownV[c * z.cap + t1], ownS ? ownS[c * z.cap + t1] : 0}, vb = o.X(c, t2);
+            Vec v{0, 0};
             for (int e1 = 0; e1 < an[c] * an[c1]; e1++) {
-                if (!bit(va, e1)) continue;
+                if (!bit(va.v, e1)) continue;
                 const int r1 = e1 / an[c1], q1 = e1 % an[c1];
                 for (int e2 = 0; e2 < o.n[c] * o.n[c1]; e2++) {
-                    if (!bit(vb, e2)) continue;
+                    if (!bit(vb.v, e2)) continue;
                     const int r2 = e2 / o.n[c1], q2 = e2 % o.n[c1];
-                    v |= 1ull << ((r1 * o.n[c] + r2) * g[c1] + q1 * o.n[c1] + q2);
+                    const int to = (r1 * o.n[c] + r2) * g[c1] + q1 * o.n[c1] + q2;
+                    v.v |= 1ull << to;
+                    v.s |= (bit(va.s, e1) ^ bit(vb.s, e2)) << to;
                 }
             }
-            z.x[c * z.cap + t] = v;
+            O::put(z, c, t, v);
         }
     }
     __syncwarp();
@@ -240,7 +293,6 @@ __device__ void product_with(Z &z, const BestView &o, uint64_t *own) {
     z.rebuild();
 }
 
-template <class Z>
 __device__ bool valid_grown(const int g[3], int rank, int maxN) {  // scheme_z2.cu:260-294
     if (rank > kMaxRankRef) return false;
     for (int q = 0; q < 3; q++)
@@ -249,7 +301,7 @@ __device__ bool valid_grown(const int g[3], int rank, int maxN) {  // scheme_z2.
 }
 
 template <class Z, class R>
-__device__ bool try_project(Z &z, R &r) {  // scheme_z2.cu:1165-1185
+__device__ bool try_project(Z &z, R &r) {  // scheme_z2.cu:1165-1185, scheme_integer.cu:1103-1123
     const int n[3] = {z.n0, z.n1, z.n2};
     int idx[3], size = 0;
     for (int i = 0; i < 3; i++)
@@ -263,12 +315,12 @@ __device__ bool try_project(Z &z, R &r) {  // scheme_z2.cu:1165-1185
 }
 
 template <class Z, class R>
-__device__ bool try_extend(Z &z, R &r) {  // scheme_z2.cu:1187-1206
+__device__ bool try_extend(Z &z, R &r) {  // scheme_z2.cu:1187-1206, scheme_integer.cu:1125-1144
     int idx[3], size = 0;
     for (int i = 0; i < 3; i++) {
         int g[3] = {z.n0, z.n1, z.n2};
         g[i] += 1;
-        if (valid_grown<Z>(g, z.m + g[(i + 1) % 3] * g[(i + 2) % 3], kMaxExtensionN)) idx[size++] = i;
+        if (valid_grown(g, z.m + g[(i + 1) % 3] * g[(i + 2) % 3], kMaxExtensionN)) idx[size++] = i;
     }
     if (!size) return false;
     extend(z, idx[r.raw() % (uint32_t)size]);
@@ -277,12 +329,12 @@ __device__ bool try_extend(Z &z, R &r) {  // scheme_z2.cu:1187-1206
 }
 
 template <class Z, class R>
-__device__ bool try_product(Z &z, R &r) {  // scheme_z2.cu:1208-1223
+__device__ bool try_product(Z &z, R &r) {  // scheme_z2.cu:1208-1223, scheme_integer.cu:1146-1161
     int idx[3], size = 0;
     for (int i = 0; i < 3; i++) {
         int g[3] = {z.n0, z.n1, z.n2};
         g[i] *= 2;
-        if (valid_grown<Z>(g, z.m * 2, kMaxExtensionN)) idx[size++] = i;
+        if (valid_grown(g, z.m * 2, kMaxExtensionN)) idx[size++] = i;
     }
     if (!size) return false;
     product(z, idx[r.raw() % (uint32_t)size]);
@@ -290,7 +342,7 @@ __device__ bool try_product(Z &z, R &r) {  // scheme_z2.cu:1208-1223
 }
 
 template <class Z, class R>
-__device__ bool try_merge(Z &z, const BestView &o, R &r) {  // scheme_z2.cu:1225-1254
+__device__ bool try_merge(Z &z, const BestView &o, R &r) {  // scheme_z2.cu:1225-1254, scheme_integer.cu:1163-1192
     if (z.m + o.m > kMaxRankRef) return false;
     const int n[3] = {z.n0, z.n1, z.n2};
     const bool eq0 = n[0] == o.n[0], eq1 = n[1] == o.n[1], eq2 = n[2] == o.n[2];
@@ -305,14 +357,14 @@ __device__ bool try_merge(Z &z, const BestView &o, R &r) {  // scheme_z2.cu:1225
 }
 
 template <class Z>
-__device__ bool try_product_with(Z &z, const BestView &o, uint64_t *own) {  // scheme_z2.cu:1256-1275
+__device__ bool try_product_with(Z &z, const BestView &o, uint64_t *ownV, uint64_t *ownS) {  // scheme_z2.cu:1256-1275
     if (z.m * o.m > kMaxRankRef) return false;
     const int n[3] = {z.n0, z.n1, z.n2};
     int g[3];
     for (int q = 0; q < 3; q++) g[q] = n[q] * o.n[q];
     for (int q = 0; q < 3; q++)
         if (g[q] > kMaxExtensionN || g[q] * g[(q + 1) % 3] > kMaxMatrix) return false;
-    product_with(z, o, own);
+    product_with(z, o, ownV, ownS);
     return true;
 }
 
@@ -345,7 +397,9 @@ __device__ void resize_one(const DevBatch &B, const WalkParams &P, int w, unsign
     if (!merged) {
         const double q = (double)r.uniform();
         if (q < 0.05) try_project(z, r);
-        else if (q < 0.55) try_product_with(z, best_view(B, (int)(r.raw() % (uint32_t)B.S)), B.fac + (size_t)w * 3 * B.cap);
+        else if (q < 0.55)
+            try_product_with(z, best_view(B, (int)(r.raw() % (uint32_t)B.S)), B.fac + (size_t)w * 3 * B.cap,
+                             B.sgn ? B.sgn + (size_t)w * 3 * B.cap : nullptr);
         else if (q < 0.85) try_product(z, r);
         else try_extend(z, r);
     }
@@ -378,7 +432,14 @@ __global__ void k_copy_best(DevBatch B, const int32_t *walks, int count, const i
         const int w = walks[warp];
         const size_t o = (size_t)w * 3 * B.cap;
         const int m = B.hdr[w].m;
-        for (int q = lane_id(); q < 3 * B.cap; q += 32) B.best_fac[o + q] = (q % B.cap) < m ? B.fac[o + q] : 0ull;
+        for (int q = lane_id(); q < 3 * B.cap; q += 32) {
+            const bool live = (q % B.cap) < m;
+            B.best_fac[o + q] = live ? B.fac[o + q] : 0ull;
+            if (B.sgn) {
+                B.best_sgn[o + q] = live ? B.sgn[o + q] : 0ull;
+                B.best_valid[o + q] = live ? B.valid[o + q] : 0;
+            }
+        }
         if (lane_id() == 0) {
             B.hdr[w].best_m = m;
             for (int c = 0; c < 3; c++) B.best_n[w * 3 + c] = B.hdr[w].n[c];
@@ -390,24 +451,25 @@ __global__ void k_copy_best(DevBatch B, const int32_t *walks, int count, const i
             B.hdr[w].best_rank = bestRank[w];
 }
 
+template <class Walker, class R>
+cudaError_t resize_t(const DevBatch &B, const WalkParams &P, double p, int wpb, int grid, cudaStream_t s) {
+    const size_t smem = RingIO<Walker>::smem(B.cap) * wpb;
+    cudaError_t e = cudaFuncSetAttribute(k_resize<Walker, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e) return e;
+    k_resize<Walker, R><<<grid, 32 * wpb, smem, s>>>(B, P, p);
+    return cudaGetLastError();
+}
+
 }  // namespace
 
-cudaError_t launch_resize(const DevBatch &B, const WalkParams &P, int rng, double p, int wpb, int grid, cudaStream_t s) {
+cudaError_t launch_resize(int ring, const DevBatch &B, const WalkParams &P, int rng, double p, int wpb, int grid,
+                          cudaStream_t s) {
     if (slots_for_cap(B.cap) != 11 || !B.best_n) return cudaErrorInvalidValue;
-    using X = Z2Walk<XorwowDraws, 11>;
-    using Y = Z2Walk<PhiloxDraws, 11>;
-    const size_t smem = RingIO<X>::smem(B.cap) * wpb;
-    cudaError_t e;
-    if (rng == RNG_XORWOW) {
-        e = cudaFuncSetAttribute(k_resize<X, XorwowDraws>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e) return e;
-        k_resize<X, XorwowDraws><<<grid, 32 * wpb, smem, s>>>(B, P, p);
-    } else {
-        e = cudaFuncSetAttribute(k_resize<Y, PhiloxDraws>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e) return e;
-        k_resize<Y, PhiloxDraws><<<grid, 32 * wpb, smem, s>>>(B, P, p);
-    }
-    return cudaGetLastError();
+    if (ring == 0)
+        return rng == RNG_XORWOW ? resize_t<Z2Walk<XorwowDraws, 11>, XorwowDraws>(B, P, p, wpb, grid, s)
+                                 : resize_t<Z2Walk<PhiloxDraws, 11>, PhiloxDraws>(B, P, p, wpb, grid, s);
+    return rng == RNG_XORWOW ? resize_t<ZTWalk<XorwowDraws, 11>, XorwowDraws>(B, P, p, wpb, grid, s)
+                             : resize_t<ZTWalk<PhiloxDraws, 11>, PhiloxDraws>(B, P, p, wpb, grid, s);
 }
 
 cudaError_t launch_copy_best(const DevBatch &B, const int32_t *walks, int count, const int32_t *bestRank, cudaStream_t s) {

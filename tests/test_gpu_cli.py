@@ -61,22 +61,24 @@ def test_flip_graph_matches_reference_executable(work):
     same_files(out, "cli_flip_graph")
 
 
-def test_flip_graph_with_resizing_matches_reference_executable(work):
-    """Resizing on (Z2 build): walks change size between launches; every scheme the reference saved
-    in its first iterations (report and best-rank table saves) is saved here identically."""
+@pytest.mark.parametrize("ring,sub", [("Z2", "cli_flip_graph_resize"), ("ZT", "cli_flip_graph_resize_zt")])
+def test_flip_graph_with_resizing_matches_reference_executable(work, ring, sub):
+    """Resizing on: walks change size between launches; every scheme the reference saved in its
+    first iterations (report and best-rank table saves) is saved here identically.  The ZT case is
+    the reference's default configuration (ZT build, resize probability 0.2, no flag)."""
     import sys
     sys.path.insert(0, GOLDEN)
     import make_golden
     out = os.path.join(work, "fgr")
     os.makedirs(out)
-    K = make_golden.RESIZE_CLI_ITERATIONS
-    run([os.path.join(BIN, "flip_graph")] + make_golden.RESIZE_CLI_ARGS +
-        ["--path", out, "--ring", "Z2", "--max-launches", str(K)], work)
-    want = sorted(os.listdir(os.path.join(GOLDEN, "cli_flip_graph_resize")))
+    K = make_golden.RESIZE_CLI_ITERATIONS if ring == "Z2" else make_golden.RESIZE_CLI_ITERATIONS_ZT
+    args = make_golden.RESIZE_CLI_ARGS if ring == "Z2" else make_golden.RESIZE_CLI_ARGS_ZT
+    run([os.path.join(BIN, "flip_graph")] + args + ["--path", out, "--ring", ring, "--max-launches", str(K)], work)
+    want = sorted(os.listdir(os.path.join(GOLDEN, sub)))
     got = sorted(x for x in os.listdir(out) if int(x.split("_iteration")[1].split("_")[0]) < K)
     assert want and got == want, (got, want)
     for name in want:
-        with open(os.path.join(GOLDEN, "cli_flip_graph_resize", name)) as a, open(os.path.join(out, name)) as b:
+        with open(os.path.join(GOLDEN, sub, name)) as a, open(os.path.join(out, name)) as b:
             assert a.read() == b.read(), name
 
 

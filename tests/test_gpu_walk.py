@@ -68,17 +68,19 @@ def test_walk_matches_reference_kernel(path):
         assert eng.validate(best=True).all()
 
 
-@pytest.mark.parametrize("mode,shape,S,iters,plus,resize_p,launches", [
-    ("reference", (3, 3, 3), 32, 300, 100, 0.3, 3),
-    ("reference", (2, 3, 4), 24, 200, 50, 0.9, 3),
-    ("philox", (2, 2, 3), 24, 200, 50, 0.7, 4),
+@pytest.mark.parametrize("ring,mode,shape,S,iters,plus,resize_p,launches", [
+    ("z2", "reference", (3, 3, 3), 32, 300, 100, 0.3, 3),
+    ("z2", "reference", (2, 3, 4), 24, 200, 50, 0.9, 3),
+    ("z2", "philox", (2, 2, 3), 24, 200, 50, 0.7, 4),
+    ("zt", "reference", (2, 2, 3), 16, 60, 40, 0.8, 3),
+    ("zt", "reference", (2, 3, 3), 12, 50, 30, 0.5, 3),
 ])
-def test_resize_vs_oracle(mode, shape, S, iters, plus, resize_p, launches):
+def test_resize_vs_oracle(ring, mode, shape, S, iters, plus, resize_p, launches):
     """Resize meta-operators on the GPU (one warp per walk) against the oracle: sizes, factors,
     lists, best schemes and sizes, best ranks and stream positions after every launch count."""
     n1, n2, n3 = shape
     seed = 500 + n1 + n2 + n3
-    with fg.Engine(S, 352, "z2", mode, seed, iters, plus, 0.01, 0.0, resize_p=resize_p) as eng:
+    with fg.Engine(S, 352, ring, mode, seed, iters, plus, 0.01, 0.0, resize_p=resize_p) as eng:
         eng.init_naive(n1, n2, n3)
         rec0 = eng.records()
         eng.run(launches)
@@ -95,7 +97,7 @@ def test_resize_vs_oracle(mode, shape, S, iters, plus, resize_p, launches):
         O.walk(b, b.cfg("tape", launches=launches, **kw), tape)
     else:
         O.walk(b, b.cfg("philox", launches=launches, **kw))
-    compare_records(rec, b, f"{mode} {shape}")
+    compare_records(rec, b, f"{ring} {mode} {shape}")
     assert np.array_equal(rec.best_n, b.best_n)
 
 
