@@ -399,6 +399,100 @@ struct Z2 {
         return count - 2 * m - nn[2];
     }
 
+    // ---------------------------------------------------------------- basis moves
+    // Random invertible n x n matrix over GF(2) and its inverse (scheme_z2.cu:444-492,
+    // random.cuh:24-32): row i = the low n bits of one draw, redrawn until Gauss-Jordan
+    // elimination of [M | I] finds every pivot.  Rows are bit masks (entry (i, j) = bit j).
+    template <class R> bool invertibleMatrix(int n_, uint32_t *mrow, uint32_t *inv, R &r) {
+        const uint32_t low = n_ >= 32 ? 0xFFFFFFFFu : ((1u << n_) - 1u);
+        for (int guard = 0; guard <= kRetryCap; guard++) {
+            for (int i = 0; i < n_; i++) mrow[i] = r.raw() & low;
+            uint64_t aug[16];
+            for (int i = 0; i < n_; i++) aug[i] = (uint64_t)mrow[i] | ((uint64_t)1 << (n_ + i));
+            bool ok = true;
+            for (int col = 0; col < n_ && ok; col++) {
+                int piv = -1;
+                for (int row = col; row < n_; row++)
+                    if ((aug[row] >> col) & 1) { piv = row; break; }
+                if (piv < 0) { ok = false; break; }
+                std::swap(aug[col], aug[piv]);
+                for (int row = 0; row < n_; row++)
+                    if (row != col && ((aug[row] >> col) & 1)) aug[row] ^= aug[col];
+            }
+            if (!ok) continue;
+            for (int i = 0; i < n_; i++) inv[i] = (uint32_t)(aug[i] >> n_) & low;
+            return true;
+        }
+        *status |= ST_RETRY;
+        return false;
+    }
+    // left (n1 x n1) * X (n1 x n2, bit i*n2+j) * right (n2 x n2), over GF(2) (scheme_z2.cu:494-529)
+    static uint64_t conj(uint64_t x, const uint32_t *left, const uint32_t *right, int n1, int n2) {
+        const uint64_t rowMask = n2 >= 64 ? ~0ull : ((1ull << n2) - 1);
+        uint64_t out = 0;
+        for (int i = 0; i < n1; i++) {
+            uint64_t r1 = 0;  // row i of left * X
+            for (int k = 0; k < n1; k++)
+                if ((left[i] >> k) & 1) r1 ^= (x >> (k * n2)) & rowMask;
+            uint64_t r2 = 0;  // row i of (left * X) * right
+            for (int k = 0; k < n2; k++)
+                if ((r1 >> k) & 1) r2 ^= right[k];
+            out |= (r2 & rowMask) << (i * n2);
+        }
+        return out;
+    }
+    template <class R> void sandwiching(R &r) {  // scheme_z2.cu:1277-1300
+        uint32_t u[16], u1[16], v[16], v1[16], w[16], w1[16];
+        if (!invertibleMatrix(n[0], u, u1, r) || !invertibleMatrix(n[1], v, v1, r) || !invertibleMatrix(n[2], w, w1, r))
+            return;
+        for (int t = 0; t < m; t++) {
+            x[0][t] = conj(x[0][t], u, v1, n[0], n[1]);
+            x[1][t] = conj(x[1][t], v, w1, n[1], n[2]);
+            x[2][t] = conj(x[2][t], w, u1, n[2], n[0]);
+        }
+        rebuildLists();
+    }
+    // swapBasisRows / swapBasisColumns (scheme_z2.cu:864-914): two basis vectors trade places.
+    void swapBasisRows(int i1, int i2) {
+        int rows[64];
+        for (int q = 0; q < n[0]; q++) rows[q] = q;
+        rows[i1] = i2;
+        rows[i2] = i1;
+        for (int t = 0; t < m; t++) {
+            uint64_t u = 0, w = 0;
+            for (int i = 0; i < n[0]; i++)
+                for (int j = 0; j < n[1]; j++) u |= ((x[0][t] >> (rows[i] * n[1] + j)) & 1ull) << (i * n[1] + j);
+            for (int i = 0; i < n[2]; i++)
+                for (int j = 0; j < n[0]; j++) w |= ((x[2][t] >> (i * n[0] + rows[j])) & 1ull) << (i * n[0] + j);
+            x[0][t] = u;
+            x[2][t] = w;
+        }
+    }
+    void swapBasisColumns(int j1, int j2) {
+        int cols[64];
+        for (int q = 0; q < n[2]; q++) cols[q] = q;
+        cols[j1] = j2;
+        cols[j2] = j1;
+        for (int t = 0; t < m; t++) {
+            uint64_t v = 0, w = 0;
+            for (int i = 0; i < n[1]; i++)
+                for (int j = 0; j < n[2]; j++) v |= ((x[1][t] >> (i * n[2] + cols[j])) & 1ull) << (i * n[2] + j);
+            for (int i = 0; i < n[2]; i++)
+                for (int j = 0; j < n[0]; j++) w |= ((x[2][t] >> (cols[i] * n[0] + j)) & 1ull) << (i * n[0] + j);
+            x[1][t] = v;
+            x[2][t] = w;
+        }
+    }
+    template <class R> void swapBasis(R &r) {  // scheme_z2.cu:1302-1313 (lists stay valid)
+        if (r.raw() % 2) {
+            const int i1 = (int)(r.raw() % (uint32_t)n[0]), i2 = (int)(r.raw() % (uint32_t)n[0]);
+            swapBasisRows(i1, i2);
+        } else {
+            const int j1 = (int)(r.raw() % (uint32_t)n[2]), j2 = (int)(r.raw() % (uint32_t)n[2]);
+            swapBasisColumns(j1, j2);
+        }
+    }
+
     // ---------------------------------------------------------------- resize
     // Meta-operators that change the matrix sizes (scheme_z2.cu:184-310,
     // 643-979, 1165-1275).  Matrix c is n[c] x n[c+1] (W transposed), entry
@@ -991,6 +1085,49 @@ struct ZT {
         return count - 2 * m - nn[2];
     }
 
+    // ---------------------------------------------------------------- basis moves
+    template <class R> void sandwiching(R &) {}  // scheme_integer.cu:1215-1217: empty in the reference
+    void swapBasisRows(int i1, int i2) {  // scheme_integer.cu:791-815
+        int rows[64];
+        for (int q = 0; q < n[0]; q++) rows[q] = q;
+        rows[i1] = i2;
+        rows[i2] = i1;
+        for (int t = 0; t < m; t++) {
+            uint64_t uv = 0, us = 0, wv = 0, ws = 0;
+            for (int i = 0; i < n[0]; i++)
+                for (int j = 0; j < n[1]; j++) moveBit(x[0][t], rows[i] * n[1] + j, i * n[1] + j, uv, us);
+            for (int i = 0; i < n[2]; i++)
+                for (int j = 0; j < n[0]; j++) moveBit(x[2][t], i * n[0] + rows[j], i * n[0] + j, wv, ws);
+            x[0][t] = mk(uv, us);
+            x[2][t] = mk(wv, ws);
+        }
+    }
+    void swapBasisColumns(int j1, int j2) {  // scheme_integer.cu:817-841
+        int cols[64];
+        for (int q = 0; q < n[2]; q++) cols[q] = q;
+        cols[j1] = j2;
+        cols[j2] = j1;
+        for (int t = 0; t < m; t++) {
+            uint64_t vv = 0, vs = 0, wv = 0, ws = 0;
+            for (int i = 0; i < n[1]; i++)
+                for (int j = 0; j < n[2]; j++) moveBit(x[1][t], i * n[2] + cols[j], i * n[2] + j, vv, vs);
+            for (int i = 0; i < n[2]; i++)
+                for (int j = 0; j < n[0]; j++) moveBit(x[2][t], cols[i] * n[0] + j, i * n[0] + j, wv, ws);
+            x[1][t] = mk(vv, vs);
+            x[2][t] = mk(wv, ws);
+        }
+    }
+    template <class R> void swapBasis(R &r) {  // scheme_integer.cu:1219-1233
+        if (r.raw() % 2) {
+            const int i1 = (int)(r.raw() % (uint32_t)n[0]), i2 = (int)(r.raw() % (uint32_t)n[0]);
+            swapBasisRows(i1, i2);
+        } else {
+            const int j1 = (int)(r.raw() % (uint32_t)n[2]), j2 = (int)(r.raw() % (uint32_t)n[2]);
+            swapBasisColumns(j1, j2);
+        }
+        if (fixSigns()) rebuildLists();
+    }
+
     // ---------------------------------------------------------------- resize
     // The Z2 operators on both masks of each coefficient vector (entry (i, j)
     // of matrix c at bit i * n[c+1] + j; a negative entry's sign bit moves
@@ -1356,8 +1493,8 @@ void walkLaunch(Scheme &s, R &r, const fgo_walk_cfg *cfg, fgo_batch *b, int w) {
         if (r.gate(cfg->expand_p, cfg->iterations) && s.m <= bestM + 2) {
             if (s.tryExpand(randint(1, 2, r), r)) flipsCount = 0;
         }
-        r.gate(0.0, cfg->iterations);  // sandwiching gate (probability 0)
-        r.gate(0.0, cfg->iterations);  // basis gate (probability 0)
+        if (r.gate(cfg->sandwich_p, cfg->iterations)) s.sandwiching(r);  // flip_graph.cu:560-561
+        if (r.gate(cfg->basis_p, cfg->iterations)) s.swapBasis(r);       // flip_graph.cu:563-564
         if (flipsCount >= cfg->plus_iterations && s.tryPlus(r)) flipsCount = 0;
         if (b->status[w]) break;
     }

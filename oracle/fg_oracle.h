@@ -42,7 +42,9 @@ typedef struct {
     uint64_t seed;            /* Philox key (FGO_RNG_PHILOX) */
     double resize_p;          /* --resize-probability; > 0: random iterations per launch, a resize
                                  step after every launch and the per-shape best-rank table
-                                 (flip_graph.cu:236,286-299,249-277,575-613); Z2 only */
+                                 (flip_graph.cu:236,286-299,249-277,575-613) */
+    double sandwich_p;        /* --sandwiching-probability (Z2; the ternary move is empty) */
+    double basis_p;           /* --basis-probability */
 } fgo_walk_cfg;
 
 /* Structure-of-arrays batch of S walk records.  Factor arrays are [S][3][cap];

@@ -50,7 +50,8 @@ class WalkCfg(ctypes.Structure):
     _fields_ = [("ring", ctypes.c_int32), ("rng", ctypes.c_int32), ("cap", ctypes.c_int32),
                 ("iterations", ctypes.c_int32), ("plus_iterations", ctypes.c_int32),
                 ("launches", ctypes.c_int32), ("expand_p", ctypes.c_double),
-                ("reduce_p", ctypes.c_double), ("seed", ctypes.c_uint64), ("resize_p", ctypes.c_double)]
+                ("reduce_p", ctypes.c_double), ("seed", ctypes.c_uint64), ("resize_p", ctypes.c_double),
+                ("sandwich_p", ctypes.c_double), ("basis_p", ctypes.c_double)]
 
 
 class _Batch(ctypes.Structure):
@@ -106,9 +107,9 @@ class WalkBatch:
         return _Batch(*[_ptr(getattr(self, f)) for f in self.FIELDS])
 
     def cfg(self, rng="tape", iterations=1000, plus_iterations=8000, launches=1, expand_p=0.01,
-            reduce_p=0.0, seed=0, resize_p=0.0):
+            reduce_p=0.0, seed=0, resize_p=0.0, sandwich_p=0.0, basis_p=0.0):
         return WalkCfg(RING[self.ring], RNG[rng], self.cap, iterations, plus_iterations, launches,
-                       expand_p, reduce_p, seed, resize_p)
+                       expand_p, reduce_p, seed, resize_p, sandwich_p, basis_p)
 
 
 def make_tape(tapes):

@@ -131,9 +131,13 @@ static void update_ranks(std::unordered_map<std::string, int> &table, Scheme *sc
 }
 
 static int cmd_walk(int argc, char **argv) {
-    if (argc != 13 && argc != 14) { fprintf(stderr, "walk: bad arguments\n"); return 1; }
-    // optional 14th argument: --resize-probability (> 0 runs FlipGraph::run's resize loop)
-    const double resizeP = argc == 14 ? atof(argv[13]) : 0.0;
+    if (argc < 13 || argc > 16) { fprintf(stderr, "walk: bad arguments\n"); return 1; }
+    // optional arguments: --resize-probability (> 0 runs FlipGraph::run's resize loop),
+    // --sandwiching-probability, --basis-probability
+    const double resizeP = argc >= 14 ? atof(argv[13]) : 0.0;
+    const double sandwichP = argc >= 15 ? atof(argv[14]) : 0.0;
+    const double basisP = argc >= 16 ? atof(argv[15]) : 0.0;
+    const bool moves = sandwichP > 0 || basisP > 0;
     int n1 = atoi(argv[2]), n2 = atoi(argv[3]), n3 = atoi(argv[4]);
     int S = atoi(argv[5]), iters = atoi(argv[6]), plusIters = atoi(argv[7]);
     double expandP = atof(argv[8]), reduceP = atof(argv[9]);
@@ -162,18 +166,20 @@ static int cmd_walk(int argc, char **argv) {
 
     FILE *f = fopen(out, "wb");
     if (!f) { fprintf(stderr, "cannot open %s\n", out); return 1; }
-    put_i32(f, resizeP > 0 ? 0x46475732 : 0x46475731);  // magic "FGW2" (with resizing) / "FGW1"
+    // magic "FGW3" (resize + sandwiching + basis probabilities), "FGW2" (resize) or "FGW1"
+    put_i32(f, moves ? 0x46475733 : (resizeP > 0 ? 0x46475732 : 0x46475731));
     put_i32(f, kRingIsZT);
     put_i32(f, n1); put_i32(f, n2); put_i32(f, n3);
     put_i32(f, S); put_i32(f, iters); put_i32(f, plusIters);
     fwrite(&expandP, 8, 1, f); fwrite(&reduceP, 8, 1, f);
-    if (resizeP > 0) fwrite(&resizeP, 8, 1, f);
+    if (resizeP > 0 || moves) fwrite(&resizeP, 8, 1, f);
+    if (moves) { fwrite(&sandwichP, 8, 1, f); fwrite(&basisP, 8, 1, f); }
     put_i32(f, seed); put_i32(f, launches);
     for (int w = 0; w < S; w++) put_scheme(f, schemes[w], true);   // initial state
 
     for (int L = 0; L < launches; L++) {
         randomWalkKernel<<<numBlocks, blockSize>>>(schemes, best, bestRanks, flips, states, S, iters, plusIters,
-                                                   reduceP, expandP, 0.0, 0.0, resizeP > 0);
+                                                   reduceP, expandP, sandwichP, basisP, resizeP > 0);
         HCHECK(cudaGetLastError());
         HCHECK(cudaDeviceSynchronize());
         if (resizeP > 0) {  // FlipGraph::run (flip_graph.cu:296-299)

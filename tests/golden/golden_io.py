@@ -105,7 +105,7 @@ def _tapes(r, count):
 def read_walk(path):
     r = _Reader(_open(path))
     magic = r.i32()
-    assert magic in (0x46475731, 0x46475732), "not a walk dump"
+    assert magic in (0x46475731, 0x46475732, 0x46475733), "not a walk dump"
     zt = r.i32() == 1
     d = {"ring": "zt" if zt else "z2"}
     d["n"] = [r.i32() for _ in range(3)]
@@ -114,7 +114,9 @@ def read_walk(path):
     d["plus_iterations"] = r.i32()
     d["expand_p"] = r.f64()
     d["reduce_p"] = r.f64()
-    d["resize_p"] = r.f64() if magic == 0x46475732 else 0.0
+    d["resize_p"] = r.f64() if magic in (0x46475732, 0x46475733) else 0.0
+    d["sandwich_p"] = r.f64() if magic == 0x46475733 else 0.0
+    d["basis_p"] = r.f64() if magic == 0x46475733 else 0.0
     d["seed"] = r.i32()
     d["n_launches"] = L = r.i32()
     d["initial"] = [_scheme(r, zt, True) for _ in range(S)]

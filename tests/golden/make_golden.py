@@ -54,6 +54,15 @@ RESIZE_CASES = [
     ("zt_223_resize", "zt", 2, 2, 3, 6, 60, 40, 0.01, 0.0, 52, 3, 0.9),
 ]
 
+# Walks with the sandwiching and basis-change moves (no resizing):
+# (name, ring, n1, n2, n3, walks, iterations, plus_iterations, expand_p, reduce_p, seed, launches,
+#  resize_p, sandwiching_p, basis_p)
+MOVE_CASES = [
+    ("z2_333_moves", "z2", 3, 3, 3, 8, 300, 80, 0.01, 0.0, 61, 2, 0.0, 30.0, 30.0),
+    ("z2_234_moves", "z2", 2, 3, 4, 8, 300, 80, 0.01, 0.0, 62, 2, 0.0, 60.0, 10.0),
+    ("zt_333_moves", "zt", 3, 3, 3, 4, 60, 40, 0.01, 0.0, 63, 2, 0.0, 10.0, 20.0),
+]
+
 # Long walks used only to produce low-rank input schemes for the reducer and
 # minimizer runs (their dumps are not kept as fixtures).
 SOURCE_WALKS = [
@@ -81,7 +90,7 @@ def walk(out_dir, case, tape=True):
     env = dict(os.environ)
     if not tape:
         env["FG_NO_TAPE"] = "1"
-    extra = [repr(case[12])] if len(case) > 12 else []
+    extra = [repr(x) for x in case[12:]]
     run([harness(ring), "walk", str(n1), str(n2), str(n3), str(S), str(iters), str(plus),
          repr(ep), repr(rp), str(seed), str(launches), path] + extra, env=env)
     return path
@@ -125,7 +134,7 @@ def cli_resize(out_dir):
 def do_run(out_dir, resize_only=False):
     os.makedirs(out_dir, exist_ok=True)
     run([os.path.join(ROOT, "oracle", "build_ref.sh")])
-    for case in RESIZE_CASES:
+    for case in RESIZE_CASES + MOVE_CASES:
         walk(out_dir, case)
     cli_resize(out_dir)
     if resize_only:
@@ -205,6 +214,7 @@ def trimmed_reduce(path):
 
 def do_pack(raw_dir):
     manifest = {"walk_cases": [list(c) for c in WALK_CASES], "resize_cases": [list(c) for c in RESIZE_CASES],
+                "move_cases": [list(c) for c in MOVE_CASES],
                 "files": []}
     old = os.path.join(HERE, "manifest.json")
     if os.path.exists(old):  # packing a partial run keeps the fixtures already recorded

@@ -25,13 +25,14 @@ def test_walk_matches_reference(path):
     if d["resize_p"] > 0:
         return check_resize_walk(d)
     batch = O.WalkBatch(S, n1 * n2 * n3, ring)
+    moves = dict(sandwich_p=d["sandwich_p"], basis_p=d["basis_p"])
     O.init_naive(batch, n1, n2, n3)
     for w in range(S):
         init = {"scheme": d["initial"][w], "flips": 0, "best_rank": n1 * n2 * n3, "best": d["initial"][w]}
         assert not diff_walk(batch, w, init, ring), "naive scheme differs from the reference's"
     tape = O.make_tape([(t["draws"], t["uniforms"]) for t in d["tapes"]])
     for L, block in enumerate(d["launches"]):
-        cfg = batch.cfg("tape", d["iterations"], d["plus_iterations"], 1, d["expand_p"], d["reduce_p"])
+        cfg = batch.cfg("tape", d["iterations"], d["plus_iterations"], 1, d["expand_p"], d["reduce_p"], **moves)
         O.walk(batch, cfg, tape)
         assert not batch.status.any()
         for w in range(S):
