@@ -9,9 +9,9 @@
 //   --max-launches N      stop after N launches (0: run forever, as the reference does)
 //   --target-rank R       stop once a walk's best rank reaches R (0: off)
 //   --time-budget S       stop after S seconds (0: off)
-// Resize meta-operators (--resize-probability, default 0.2) run on both rings
-// in the reference and philox modes; in the fast mode, and for sandwiching and
-// basis-change moves, a positive probability is reported and treated as 0.
+// Resize meta-operators (--resize-probability, default 0.2), sandwiching and
+// basis-change moves run on both rings in the reference and philox modes; in
+// the fast mode a positive probability is reported and treated as 0.
 #include <algorithm>
 #include <chrono>
 #include <cstdio>
@@ -40,10 +40,13 @@ struct Options {
     int targetRank;
 };
 
+// The meta-operators and basis moves run in the list modes only.
+bool resizeHere(const Options &o) { return o.mode != "fast"; }
+
 class FlipGraph {
 public:
     FlipGraph(const Options &o) : o_(o), zt_(o.ring == "ZT") {
-        resizeOn_ = o.resize > 0 && o.mode != "fast";
+        resizeOn_ = o.resize > 0 && resizeHere(o);
         n2bestRank_[key(o.n1, o.n2, o.n3)] = o.n1 * o.n2 * o.n3;
         known_ = knownRanks(zt_);
     }
@@ -158,6 +161,8 @@ private:
         c.reduce_p = o_.reduce;
         c.device = 0;
         c.resize_p = resizeOn_ ? o_.resize : 0.0;
+        c.sandwich_p = resizeHere(o_) ? o_.sandwiching : 0.0;
+        c.basis_p = resizeHere(o_) ? o_.basis : 0.0;
         check(fg_create(&c, &h_), "fg_create");
     }
 
@@ -428,10 +433,9 @@ int main(int argc, char *argv[]) {
     std::cout << "  - resize: " << o.resize << std::endl;
     std::cout << "- log period: " << o.logPeriod << std::endl;
     std::cout << "- seed: " << o.seed << std::endl;
-    const bool resizeHere = o.mode != "fast";
-    if (o.sandwiching > 0 || o.basis > 0 || (o.resize > 0 && !resizeHere))
-        std::cout << "Note: sandwiching and basis-change moves, and resizing in the fast mode, are not available "
-                     "in this engine; their probabilities are treated as 0"
+    if (!resizeHere(o) && (o.sandwiching > 0 || o.basis > 0 || o.resize > 0))
+        std::cout << "Note: resizing, sandwiching and basis-change moves are not available in the fast mode; "
+                     "their probabilities are treated as 0"
                   << std::endl;
 
     FlipGraph graph(o);

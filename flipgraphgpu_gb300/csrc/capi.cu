@@ -234,15 +234,18 @@ void compute_params(fg_handle *h) {
     P.plus_iterations = c.plus_iterations;
     P.reduce_gate_f = ceil_to_float(c.reduce_p);
     P.expand_gate_f = ceil_to_float(c.expand_p);
-    P.zero_gate_f = 0.0f;
+    P.sandwich_gate_f = ceil_to_float(c.sandwich_p);
+    P.basis_gate_f = ceil_to_float(c.basis_p);
     P.tie_gate_f = ceil_to_float(0.01);
     auto thr = [&](double p) -> uint64_t {
-        if (!(p > 0)) return 0;
+        if (!(p > 0)) return kGateOff;
         double q = p / (double)c.iterations;
         return q >= 1.0 ? (1ull << 32) : (uint64_t)(q * 4294967296.0);
     };
     P.reduce_T = thr(c.reduce_p);
     P.expand_T = thr(c.expand_p);
+    P.sandwich_T = thr(c.sandwich_p);
+    P.basis_T = thr(c.basis_p);
     P.key0 = (uint32_t)c.seed;
     P.key1 = (uint32_t)(c.seed >> 32);
     P.random_iterations = c.resize_p > 0 ? 1 : 0;
@@ -427,6 +430,8 @@ fg_status fg_create(const fg_config *cfg, fg_handle **out) {
         return fail(FG_ERR_CAPACITY, "cap must be in [1, 352]");
     if (cfg->resize_p > 0 && cfg->mode != FG_MODE_REFERENCE && cfg->mode != FG_MODE_PHILOX_LISTS)
         return fail(FG_ERR_ARG, "resizing runs in a list mode (reference or philox)");
+    if ((cfg->sandwich_p > 0 || cfg->basis_p > 0) && cfg->mode != FG_MODE_REFERENCE && cfg->mode != FG_MODE_PHILOX_LISTS)
+        return fail(FG_ERR_ARG, "sandwiching and basis-change moves run in a list mode (reference or philox)");
     if (cfg->resize_p > 0 && cfg->cap < FG_MAX_RANK)
         return fail(FG_ERR_CAPACITY, "resizing needs cap >= 350 (products reach the maximal rank)");
     if (cfg->iterations <= 0) return fail(FG_ERR_ARG, "iterations must be positive");

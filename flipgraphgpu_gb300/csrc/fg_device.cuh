@@ -46,14 +46,17 @@ struct DevBatch {
     int32_t *best_n;              // [S][3] sizes of the best scheme (resizing), or null
 };
 
+constexpr uint64_t kGateOff = ~0ull;
+
 struct WalkParams {
     int iterations;
     int plus_iterations;
     // Reference gates: curand_uniform() * iterations < p  <=>  product < gate_f (the
     // least float >= p), so the comparison stays in single precision.
-    float reduce_gate_f, expand_gate_f, zero_gate_f, tie_gate_f;
-    // Fast gates: draw < threshold, threshold = floor(p / iterations * 2^32); 0 = disabled.
-    uint64_t reduce_T, expand_T;
+    float reduce_gate_f, expand_gate_f, sandwich_gate_f, basis_gate_f, tie_gate_f;
+    // Philox gates: draw < threshold, threshold = floor(p / iterations * 2^32);
+    // kGateOff (p <= 0) = never fires and takes no draw.
+    uint64_t reduce_T, expand_T, sandwich_T, basis_T;
     uint32_t key0, key1;  // Philox key (seed)
     int random_iterations;  // resizing on: each launch runs randint(1, iterations) steps (flip_graph.cu:531)
 };
@@ -75,7 +78,8 @@ struct XorwowDraws {
     __device__ __forceinline__ bool coin() { return raw() & 1u; }
     __device__ __forceinline__ bool gate_reduce() { return uniform() * (float)P->iterations < P->reduce_gate_f; }
     __device__ __forceinline__ bool gate_expand() { return uniform() * (float)P->iterations < P->expand_gate_f; }
-    __device__ __forceinline__ void gate_zero() { uniform(); }  // sandwiching / basis gates (probability 0)
+    __device__ __forceinline__ bool gate_sandwich() { return uniform() * (float)P->iterations < P->sandwich_gate_f; }
+    __device__ __forceinline__ bool gate_basis() { return uniform() * (float)P->iterations < P->basis_gate_f; }
     __device__ __forceinline__ bool tie() { return uniform() < P->tie_gate_f; }
     __device__ __forceinline__ uint64_t mask(int nn) { return (uint64_t)raw() % ((uint64_t)1 << nn); }
 };
@@ -117,9 +121,11 @@ struct PhiloxDraws {
     __device__ __forceinline__ float uniform() { return (float)(raw() >> 8) * (1.0f / 16777216.0f); }
     __device__ __forceinline__ uint32_t below(uint32_t k) { return __umulhi(raw(), k); }
     __device__ __forceinline__ bool coin() { return raw() >> 31; }
-    __device__ __forceinline__ bool gate_reduce() { return P->reduce_T && (uint64_t)raw() < P->reduce_T; }
-    __device__ __forceinline__ bool gate_expand() { return P->expand_T && (uint64_t)raw() < P->expand_T; }
-    __device__ __forceinline__ void gate_zero() {}
+    __device__ __forceinline__ bool gate(uint64_t T) { return T != kGateOff && (uint64_t)raw() < T; }
+    __device__ __forceinline__ bool gate_reduce() { return gate(P->reduce_T); }
+    __device__ __forceinline__ bool gate_expand() { return gate(P->expand_T); }
+    __device__ __forceinline__ bool gate_sandwich() { return gate(P->sandwich_T); }
+    __device__ __forceinline__ bool gate_basis() { return gate(P->basis_T); }
     __device__ __forceinline__ bool tie() { return raw() < 42949672u; }
     __device__ __forceinline__ uint64_t mask(int nn) { return nn >= 32 ? (uint64_t)raw() : (uint64_t)(raw() & ((1u << nn) - 1u)); }
 };

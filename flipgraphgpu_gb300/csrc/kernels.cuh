@@ -3,6 +3,7 @@
 #include "fg_device.cuh"
 #include "walk_z2.cuh"
 #include "walk_zt.cuh"
+#include "walk_moves.cuh"
 
 namespace fg {
 
@@ -171,8 +172,8 @@ __device__ void walk_one(const DevBatch &B, const WalkParams &P, int w, unsigned
         if (r.gate_expand() && z.m <= bestM + 2) {
             if (z.tryExpand(randint(1, 2, r))) flipsCount = 0;
         }
-        r.gate_zero();  // sandwiching (probability 0)
-        r.gate_zero();  // basis change (probability 0)
+        if (r.gate_sandwich()) sandwich_move(z);  // flip_graph.cu:560-561
+        if (r.gate_basis()) basis_move(z);        // flip_graph.cu:563-564
         if (flipsCount >= P.plus_iterations && z.tryPlus()) flipsCount = 0;
         if (z.status) break;
     }

@@ -12,6 +12,7 @@
 // n[c] x n[c+1] (W transposed), entry (i, j) at bit i * n[c+1] + j.
 #include "kernels.cuh"
 #include "launch.h"
+#include "walk_moves.cuh"
 
 namespace fg {
 
@@ -23,38 +24,6 @@ constexpr int kMinProjectN = 2;     // config.cuh:34
 constexpr int kMaxRankRef = 350;    // config.cuh:10
 
 __device__ __forceinline__ uint64_t bit(uint64_t v, int k) { return (v >> k) & 1ull; }
-
-// A coefficient vector: Z2 factor bits in v (s = 0); ZT values in v, signs in s
-// (a negative entry's sign bit moves with its value bit).
-struct Vec {
-    uint64_t v, s;
-};
-
-// Ring access for the two walkers: word (c, t) of the walk in shared memory.
-template <class Z> struct RingOps;
-template <class R, int S> struct RingOps<Z2Walk<R, S>> {
-    using Z = Z2Walk<R, S>;
-    __device__ static Vec get(const Z &z, int c, int t) { return Vec{z.x[c * z.cap + t], 0}; }
-    __device__ static void put(Z &z, int c, int t, Vec w) { z.x[c * z.cap + t] = w.v; }
-    __device__ static void fixSigns(Z &) {}
-    __device__ static void stash(const Z &z, uint64_t *ownV, uint64_t *) {
-        for (int q = lane_id(); q < 3 * z.cap; q += 32) ownV[q] = z.x[q];
-    }
-};
-template <class R, int S> struct RingOps<ZTWalk<R, S>> {
-    using Z = ZTWalk<R, S>;
-    __device__ static Vec get(const Z &z, int c, int t) { return Vec{z.xv[c * z.cap + t], z.xs[c * z.cap + t]}; }
-    __device__ static void put(Z &z, int c, int t, Vec w) {
-        const int q = c * z.cap + t;
-        z.xv[q] = w.v;
-        z.xs[q] = w.s & w.v;
-        z.xo[q] = 1;
-    }
-    __device__ static void fixSigns(Z &z) { z.fixSigns(); }
-    __device__ static void stash(const Z &z, uint64_t *ownV, uint64_t *ownS) {
-        for (int q = lane_id(); q < 3 * z.cap; q += 32) { ownV[q] = z.xv[q]; ownS[q] = z.xs[q]; }
-    }
-};
 
 // Entry (i, j) of a rows x cols matrix to (i + di, j + dj) of a matrix with newCols columns.
 __device__ Vec place(Vec a, int rows, int cols, int newCols, int di, int dj) {

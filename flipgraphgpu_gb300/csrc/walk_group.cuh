@@ -48,8 +48,8 @@ struct GroupDraws {
     }
     __device__ __forceinline__ uint32_t below(uint32_t k) { return __umulhi(raw(), k); }
     __device__ __forceinline__ bool coin() { return raw() >> 31; }
-    __device__ __forceinline__ bool gate_reduce() { return P->reduce_T && (uint64_t)raw() < P->reduce_T; }
-    __device__ __forceinline__ bool gate_expand() { return P->expand_T && (uint64_t)raw() < P->expand_T; }
+    __device__ __forceinline__ bool gate_reduce() { return P->reduce_T != kGateOff && (uint64_t)raw() < P->reduce_T; }
+    __device__ __forceinline__ bool gate_expand() { return P->expand_T != kGateOff && (uint64_t)raw() < P->expand_T; }
     __device__ __forceinline__ bool tie() { return raw() < 42949672u; }
 };
 

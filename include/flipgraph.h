@@ -70,6 +70,13 @@ typedef struct {
                                  (Z2, list modes, cap >= 350): each launch runs a random number
                                  of steps, then resizes walks and updates the best rank per size
                                  (flip_graph.cu:286-299,575-613,249-266) */
+    double sandwich_p;        /* --sandwiching-probability (list modes; per step: sandwich_p / iterations):
+                                 conjugate every term by random invertible GF(2) matrices and rebuild
+                                 the lists (scheme_z2.cu:1277-1300; a no-op that still takes its
+                                 gate draw on ZT, scheme_integer.cu:1215-1217) */
+    double basis_p;           /* --basis-probability (list modes; per step: basis_p / iterations):
+                                 swap two basis vectors (scheme_z2.cu:1302-1313,
+                                 scheme_integer.cu:1219-1233) */
 } fg_config;
 
 /* Host-side walk records, structure of arrays over `walks` records with

@@ -442,6 +442,9 @@ struct Z2 {
         return out;
     }
     template <class R> void sandwiching(R &r) {  // scheme_z2.cu:1277-1300
+        // The reference sizes its matrices for n <= 16 (config.cuh:40, MAX_SANDWICHING_N);
+        // larger sizes overrun them there and are skipped here.
+        if (n[0] > 16 || n[1] > 16 || n[2] > 16) return;
         uint32_t u[16], u1[16], v[16], v1[16], w[16], w1[16];
         if (!invertibleMatrix(n[0], u, u1, r) || !invertibleMatrix(n[1], v, v1, r) || !invertibleMatrix(n[2], w, w1, r))
             return;

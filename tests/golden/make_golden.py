@@ -115,11 +115,28 @@ RESIZE_CLI_ITERATIONS = 4
 RESIZE_CLI_ARGS_ZT = ["-n1", "2", "-n2", "2", "-n3", "3", "--schemes", "48", "--max-iterations", "200",
                       "--plus-iterations", "100", "--seed", "75"]
 RESIZE_CLI_ITERATIONS_ZT = 3
+# Sandwiching and basis-change moves through the executables: with resizing
+# (Z2) and without (ZT, whose sandwiching is empty in the reference).
+MOVES_CLI_ARGS = ["-n1", "2", "-n2", "3", "-n3", "3", "--schemes", "64", "--max-iterations", "300",
+                  "--plus-iterations", "100", "--resize-probability", "0.3", "--sandwiching-probability", "20",
+                  "--basis-probability", "30", "--seed", "77"]
+MOVES_CLI_ITERATIONS = 3
+MOVES_CLI_ARGS_ZT = ["-n1", "3", "-n2", "3", "-n3", "3", "--schemes", "48", "--max-iterations", "200",
+                     "--plus-iterations", "100", "--resize-probability", "0", "--sandwiching-probability", "10",
+                     "--basis-probability", "40", "--seed", "79"]
+MOVES_CLI_ITERATIONS_ZT = 4
+
+# (ring, fixture directory, flags, iterations kept)
+CLI_CASES = [
+    ("z2", "cli_flip_graph_resize", RESIZE_CLI_ARGS, RESIZE_CLI_ITERATIONS),
+    ("zt", "cli_flip_graph_resize_zt", RESIZE_CLI_ARGS_ZT, RESIZE_CLI_ITERATIONS_ZT),
+    ("z2", "cli_flip_graph_moves", MOVES_CLI_ARGS, MOVES_CLI_ITERATIONS),
+    ("zt", "cli_flip_graph_moves_zt", MOVES_CLI_ARGS_ZT, MOVES_CLI_ITERATIONS_ZT),
+]
 
 
 def cli_resize(out_dir):
-    for ring, sub, args, K in (("z2", "cli_flip_graph_resize", RESIZE_CLI_ARGS, RESIZE_CLI_ITERATIONS),
-                               ("zt", "cli_flip_graph_resize_zt", RESIZE_CLI_ARGS_ZT, RESIZE_CLI_ITERATIONS_ZT)):
+    for ring, sub, args, K in CLI_CASES:
         fg_dir = os.path.join(out_dir, sub)
         os.makedirs(fg_dir, exist_ok=True)
         with open(os.path.join(out_dir, sub + ".log"), "w") as log:
@@ -131,9 +148,12 @@ def cli_resize(out_dir):
                 os.remove(os.path.join(fg_dir, name))
 
 
-def do_run(out_dir, resize_only=False):
+def do_run(out_dir, resize_only=False, cli_only=False):
     os.makedirs(out_dir, exist_ok=True)
     run([os.path.join(ROOT, "oracle", "build_ref.sh")])
+    if cli_only:
+        cli_resize(out_dir)
+        return
     for case in RESIZE_CASES + MOVE_CASES:
         walk(out_dir, case)
     cli_resize(out_dir)
@@ -229,8 +249,7 @@ def do_pack(raw_dir):
             fo.write(data)
         if base not in manifest["files"]:
             manifest["files"].append(base)
-    for sub in ("cli_additions_reducer", "cli_complexity_minimizer", "cli_flip_graph", "cli_flip_graph_resize",
-                "cli_flip_graph_resize_zt"):
+    for sub in ["cli_additions_reducer", "cli_complexity_minimizer", "cli_flip_graph"] + [c[1] for c in CLI_CASES]:
         src = os.path.join(raw_dir, sub)
         if os.path.isdir(src):
             dst = os.path.join(HERE, sub)
@@ -246,8 +265,9 @@ if __name__ == "__main__":
     ap.add_argument("--run")
     ap.add_argument("--pack")
     ap.add_argument("--resize-only", action="store_true", help="with --run: only the resize walks")
+    ap.add_argument("--cli-only", action="store_true", help="with --run: only the flip_graph runs of CLI_CASES")
     a = ap.parse_args()
     if a.run:
-        do_run(a.run, a.resize_only)
+        do_run(a.run, a.resize_only, a.cli_only)
     if a.pack:
         do_pack(a.pack)

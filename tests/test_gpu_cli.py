@@ -61,19 +61,22 @@ def test_flip_graph_matches_reference_executable(work):
     same_files(out, "cli_flip_graph")
 
 
-@pytest.mark.parametrize("ring,sub", [("Z2", "cli_flip_graph_resize"), ("ZT", "cli_flip_graph_resize_zt")])
-def test_flip_graph_with_resizing_matches_reference_executable(work, ring, sub):
-    """Resizing on: walks change size between launches; every scheme the reference saved in its
-    first iterations (report and best-rank table saves) is saved here identically.  The ZT case is
-    the reference's default configuration (ZT build, resize probability 0.2, no flag)."""
+@pytest.mark.parametrize("case", [0, 1, 2, 3], ids=["resize_z2", "resize_zt_default", "moves_z2", "moves_zt"])
+def test_flip_graph_with_resizing_matches_reference_executable(work, case):
+    """Resizing, sandwiching and basis changes on: walks change size and basis between launches;
+    every scheme the reference saved in its first iterations (report and best-rank table saves) is
+    saved here identically.  The second case is the reference's default configuration (ZT build,
+    resize probability 0.2, no flag)."""
     import sys
     sys.path.insert(0, GOLDEN)
     import make_golden
+    ring, sub, args, K = make_golden.CLI_CASES[case]
+    if not os.path.isdir(os.path.join(GOLDEN, sub)):
+        pytest.skip(f"fixture {sub} not recorded")
     out = os.path.join(work, "fgr")
     os.makedirs(out)
-    K = make_golden.RESIZE_CLI_ITERATIONS if ring == "Z2" else make_golden.RESIZE_CLI_ITERATIONS_ZT
-    args = make_golden.RESIZE_CLI_ARGS if ring == "Z2" else make_golden.RESIZE_CLI_ARGS_ZT
-    run([os.path.join(BIN, "flip_graph")] + args + ["--path", out, "--ring", ring, "--max-launches", str(K)], work)
+    run([os.path.join(BIN, "flip_graph")] + args + ["--path", out, "--ring", ring.upper(), "--max-launches", str(K)],
+        work)
     want = sorted(os.listdir(os.path.join(GOLDEN, sub)))
     got = sorted(x for x in os.listdir(out) if int(x.split("_iteration")[1].split("_")[0]) < K)
     assert want and got == want, (got, want)

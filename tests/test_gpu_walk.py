@@ -55,7 +55,8 @@ def test_walk_matches_reference_kernel(path):
     n1, n2, n3 = d["n"]
     cap = 352 if d["resize_p"] > 0 else n1 * n2 * n3
     with fg.Engine(d["walks"], cap, ring, "reference", d["seed"], d["iterations"], d["plus_iterations"],
-                   d["expand_p"], d["reduce_p"], resize_p=d["resize_p"]) as eng:
+                   d["expand_p"], d["reduce_p"], resize_p=d["resize_p"], sandwich_p=d["sandwich_p"],
+                   basis_p=d["basis_p"]) as eng:
         eng.init_naive(n1, n2, n3)
         for L, block in enumerate(d["launches"]):
             eng.run(1)
@@ -68,26 +69,35 @@ def test_walk_matches_reference_kernel(path):
         assert eng.validate(best=True).all()
 
 
-@pytest.mark.parametrize("ring,mode,shape,S,iters,plus,resize_p,launches", [
-    ("z2", "reference", (3, 3, 3), 32, 300, 100, 0.3, 3),
-    ("z2", "reference", (2, 3, 4), 24, 200, 50, 0.9, 3),
-    ("z2", "philox", (2, 2, 3), 24, 200, 50, 0.7, 4),
-    ("zt", "reference", (2, 2, 3), 16, 60, 40, 0.8, 3),
-    ("zt", "reference", (2, 3, 3), 12, 50, 30, 0.5, 3),
+@pytest.mark.parametrize("ring,mode,shape,S,iters,plus,resize_p,sandwich_p,basis_p,launches", [
+    ("z2", "reference", (3, 3, 3), 32, 300, 100, 0.3, 0.0, 0.0, 3),
+    ("z2", "reference", (2, 3, 4), 24, 200, 50, 0.9, 0.0, 0.0, 3),
+    ("z2", "philox", (2, 2, 3), 24, 200, 50, 0.7, 0.0, 0.0, 4),
+    ("zt", "reference", (2, 2, 3), 16, 60, 40, 0.8, 0.0, 0.0, 3),
+    ("zt", "reference", (2, 3, 3), 12, 50, 30, 0.5, 0.0, 0.0, 3),
+    ("z2", "reference", (3, 3, 3), 32, 300, 100, 0.0, 20.0, 20.0, 3),
+    ("z2", "philox", (2, 3, 4), 32, 300, 100, 0.0, 40.0, 10.0, 3),
+    ("z2", "reference", (2, 3, 3), 24, 200, 60, 0.6, 15.0, 15.0, 3),
+    ("zt", "reference", (3, 3, 3), 12, 60, 40, 0.0, 10.0, 20.0, 3),
+    ("zt", "philox", (2, 3, 3), 12, 60, 40, 0.5, 5.0, 20.0, 3),
 ])
-def test_resize_vs_oracle(ring, mode, shape, S, iters, plus, resize_p, launches):
-    """Resize meta-operators on the GPU (one warp per walk) against the oracle: sizes, factors,
-    lists, best schemes and sizes, best ranks and stream positions after every launch count."""
+def test_meta_moves_vs_oracle(ring, mode, shape, S, iters, plus, resize_p, sandwich_p, basis_p, launches):
+    """Resize meta-operators, sandwiching and basis changes on the GPU (one warp per walk) against
+    the oracle: sizes, factors, lists, best schemes and sizes, best ranks and stream positions."""
     n1, n2, n3 = shape
     seed = 500 + n1 + n2 + n3
-    with fg.Engine(S, 352, ring, mode, seed, iters, plus, 0.01, 0.0, resize_p=resize_p) as eng:
+    cap = 352 if resize_p > 0 else n1 * n2 * n3
+    with fg.Engine(S, cap, ring, mode, seed, iters, plus, 0.01, 0.0, resize_p=resize_p, sandwich_p=sandwich_p,
+                   basis_p=basis_p) as eng:
         eng.init_naive(n1, n2, n3)
         rec0 = eng.records()
         eng.run(launches)
         rec = eng.records()
         assert eng.validate().all() and eng.validate(best=True).all()
-    assert len({tuple(x) for x in rec.n}) > 1, "no walk changed size"
-    kw = dict(iterations=iters, plus_iterations=plus, expand_p=0.01, reduce_p=0.0, resize_p=resize_p, seed=seed)
+    if resize_p > 0:
+        assert len({tuple(x) for x in rec.n}) > 1, "no walk changed size"
+    kw = dict(iterations=iters, plus_iterations=plus, expand_p=0.01, reduce_p=0.0, resize_p=resize_p,
+              sandwich_p=sandwich_p, basis_p=basis_p, seed=seed)
     b = batch_from(rec0)
     b.best_n[:] = rec0.n
     if mode == "reference":
@@ -98,7 +108,8 @@ def test_resize_vs_oracle(ring, mode, shape, S, iters, plus, resize_p, launches)
     else:
         O.walk(b, b.cfg("philox", launches=launches, **kw))
     compare_records(rec, b, f"{ring} {mode} {shape}")
-    assert np.array_equal(rec.best_n, b.best_n)
+    if resize_p > 0:
+        assert np.array_equal(rec.best_n, b.best_n)
 
 
 def batch_from(rec0):
