@@ -20,6 +20,7 @@
 #include <vector>
 
 #include "common.h"
+#include "scheme_io.h"
 
 using namespace fgcli;
 using Clock = std::chrono::high_resolution_clock;
@@ -488,9 +489,10 @@ int main(int argc, char *argv[]) {
     bool z2input = parser.get("--z2-input") == "1";
     if (seed == 0) seed = (int)time(0);
 
-    std::ifstream f(inputPath);
-    if (!f) {
-        std::cout << "Unable to open file \"" << inputPath << "\"" << std::endl;
+    std::stringstream f;  // the reference's text layout, or JSON saved by a run
+    std::string inputError;
+    if (!openSchemeInput(inputPath, TextLayout::Reducer, f, inputError)) {
+        std::cout << inputError << std::endl;
         return -1;
     }
     if (maxFlips > 0) {
@@ -518,7 +520,6 @@ int main(int argc, char *argv[]) {
 
     SchemeAdditionsReducer reducer(count, schemesCount, seed, outputPath, z2input);
     bool correct = reducer.read(f);
-    f.close();
     if (!correct) return -1;
     reducer.reduce(maxNoImprovements, startAdditions);
     return 0;

@@ -17,6 +17,7 @@
 #include <vector>
 
 #include "common.h"
+#include "scheme_io.h"
 
 using namespace fgcli;
 using Clock = std::chrono::high_resolution_clock;
@@ -219,9 +220,10 @@ int main(int argc, char *argv[]) {
     }
     if (seed == 0) seed = (int)time(0);
 
-    std::ifstream f(inputPath);
-    if (!f) {
-        std::cout << "Unable to open file \"" << inputPath << "\"" << std::endl;
+    std::stringstream f;  // the reference's text layout, or JSON saved by a run
+    std::string inputError;
+    if (!openSchemeInput(inputPath, TextLayout::Minimizer, f, inputError)) {
+        std::cout << inputError << std::endl;
         return -1;
     }
     std::cout << "Start complexity minimization algorithm" << std::endl;
@@ -235,7 +237,6 @@ int main(int argc, char *argv[]) {
 
     ComplexityMinimizer minimizer(schemesCount, maxIterations, path, seed, ring == "ZT");
     bool result = minimizer.read(f);
-    f.close();
     if (!result) {
         printf("Read invalid scheme\n");
         return -1;

@@ -26,6 +26,7 @@
 #include <vector>
 
 #include "common.h"
+#include "scheme_io.h"
 
 using namespace fgcli;
 using Clock = std::chrono::high_resolution_clock;
@@ -59,6 +60,7 @@ public:
         f >> count;
         std::cout << "Start reading " << std::min(count, o_.schemes) << " schemes" << std::endl;
         std::vector<HostScheme> read;
+        if (count <= 0) return false;
         for (int i = 0; i < count && i < o_.schemes; i++) {
             HostScheme s;
             s.zt = zt_;
@@ -440,7 +442,13 @@ int main(int argc, char *argv[]) {
 
     FlipGraph graph(o);
     if (o.inputPath != "null") {
-        std::ifstream f(o.inputPath);
+        // The reference's text layout, or JSON saved by a run (a file or a directory of them).
+        std::stringstream f;
+        std::string error;
+        if (!openSchemeInput(o.inputPath, TextLayout::FlipGraph, f, error)) {
+            std::cout << error << std::endl;
+            return -1;
+        }
         bool ok = graph.initializeFromFile(f);
         if (!ok) return -1;
     } else {

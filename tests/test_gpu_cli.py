@@ -113,3 +113,63 @@ def test_additions_reducer_rejects_z2_only_scheme(work):
     run([os.path.join(BIN, "additions_reducer"), "-i", inp, "-o", out, "--seed", "3", "--z2-input", "1",
          "--count", "8", "--max-no-improvements", "1"], work)
     assert os.listdir(out)
+
+
+# ---------------------------------------------------------------- JSON input
+# The executables read the JSON they save (a file, or a directory of files) wherever they
+# read the reference's text: the same run from JSON and from the equivalent text is
+# identical, and on the reference's own inputs it still matches the reference's outputs.
+
+def to_json(src, dst):
+    run([os.path.join(BIN, "scheme_converter"), "-i", src, "-o", dst, "--to", "json"], os.path.dirname(dst))
+    return dst
+
+
+def test_complexity_minimizer_reads_json_input(work):
+    js = to_json(unpack("input_minimizer_z2_333.txt", work), os.path.join(work, "in.json"))
+    out = os.path.join(work, "cm")
+    os.makedirs(out)
+    run([os.path.join(BIN, "complexity_minimizer"), "--input-path", js, "--path", out, "--schemes", "256",
+         "--max-iterations", "2000", "--seed", "61", "--ring", "Z2"], work)
+    same_files(out, "cli_complexity_minimizer")
+
+
+def test_additions_reducer_reads_json_input(work):
+    js = to_json(unpack("input_zt_333.txt", work), os.path.join(work, "in.json"))
+    out = os.path.join(work, "ar")
+    os.makedirs(out)
+    run([os.path.join(BIN, "additions_reducer"), "-i", js, "-o", out, "--count", "64", "--seed", "51"], work)
+    same_files(out, "cli_additions_reducer")
+    # Its own output, expanded back, is a valid input again.
+    again = os.path.join(work, "ar2")
+    os.makedirs(again)
+    reduced = os.path.join(out, sorted(os.listdir(out))[0])
+    run([os.path.join(BIN, "additions_reducer"), "-i", reduced, "-o", again, "--count", "64", "--seed", "51"], work)
+    same_files(again, "cli_additions_reducer")
+
+
+def test_flip_graph_resumes_from_its_own_json(work):
+    first = os.path.join(work, "first")
+    os.makedirs(first)
+    base = [os.path.join(BIN, "flip_graph"), "-n1", "3", "-n2", "3", "-n3", "3", "--schemes", "128",
+            "--max-iterations", "1000", "--plus-iterations", "300", "--resize-probability", "0", "--ring", "Z2"]
+    run(base + ["--path", first, "--seed", "71", "--max-launches", "5"], work)
+    saved = sorted(os.listdir(first))
+    ranks = [int(x.split("_m")[1].split("_")[0]) for x in saved]
+    # Resume from the directory of JSON files, and from the same schemes as text.
+    text = os.path.join(work, "resume.txt")
+    run([os.path.join(BIN, "scheme_converter"), "-i", first, "-o", text], work)
+    outs = []
+    for src in (first, text):
+        out = os.path.join(work, "resumed_" + os.path.basename(src))
+        os.makedirs(out)
+        log = run(base + ["--path", out, "--seed", "72", "--max-launches", "3", "--input-path", src], work)
+        assert f"Start reading {len(saved)} schemes" in log
+        outs.append((out, sorted(os.listdir(out))))
+    (a, fa), (b, fb) = outs
+    assert fa == fb
+    for name in fa:
+        with open(os.path.join(a, name)) as x, open(os.path.join(b, name)) as y:
+            assert x.read() == y.read(), name
+    # The resumed walks start from the saved schemes: nothing above the best saved rank is saved again.
+    assert all(int(x.split("_m")[1].split("_")[0]) <= min(ranks) for x in fa)
