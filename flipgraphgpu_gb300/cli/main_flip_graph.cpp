@@ -9,6 +9,8 @@
 //   --max-launches N      stop after N launches (0: run forever, as the reference does)
 //   --target-rank R       stop once a walk's best rank reaches R (0: off)
 //   --time-budget S       stop after S seconds (0: off)
+//   --gauss-probability P Gauss (XOR) reduction per step with probability P / max iterations (Z2, list
+//                         modes; the reference defines SchemeZ2::tryReduceGauss but never calls it)
 // Resize meta-operators (--resize-probability, default 0.2), sandwiching and
 // basis-change moves run on both rings in the reference and philox modes; in
 // the fast mode a positive probability is reported and treated as 0.
@@ -36,7 +38,7 @@ namespace {
 struct Options {
     int n1, n2, n3, schemes, maxIterations, plusIterations, logPeriod, seed;
     std::string path, inputPath, ring, mode;
-    double expand, reduce, sandwiching, basis, resize, timeBudget;
+    double expand, reduce, sandwiching, basis, resize, gauss, timeBudget;
     long maxLaunches;
     int targetRank;
 };
@@ -165,6 +167,7 @@ private:
         c.resize_p = resizeOn_ ? o_.resize : 0.0;
         c.sandwich_p = resizeHere(o_) ? o_.sandwiching : 0.0;
         c.basis_p = resizeHere(o_) ? o_.basis : 0.0;
+        c.gauss_p = resizeHere(o_) && !zt_ ? o_.gauss : 0.0;
         check(fg_create(&c, &h_), "fg_create");
     }
 
@@ -369,6 +372,8 @@ int main(int argc, char *argv[]) {
     parser.add("--seed", ArgType::Natural, "INT", "random seed", "0");
     parser.add("--ring", ArgType::String, "ZT|Z2", "coefficient ring", "ZT");
     parser.add("--mode", ArgType::String, "MODE", "reference (bit-exact stream) | fast | philox", "reference");
+    parser.add("--gauss-probability", ArgType::Real, "REAL",
+               "Gauss (XOR) reduction probability (divided by max iterations; Z2, list modes)", "0.0");
     parser.add("--max-launches", ArgType::Natural, "INT", "stop after this many launches (0: never)", "0");
     parser.add("--target-rank", ArgType::Natural, "INT", "stop when a best rank reaches this (0: off)", "0");
     parser.add("--time-budget", ArgType::Real, "REAL", "stop after this many seconds (0: off)", "0");
@@ -390,6 +395,7 @@ int main(int argc, char *argv[]) {
     o.sandwiching = std::stod(parser.get("--sandwiching-probability"));
     o.basis = std::stod(parser.get("--basis-probability"));
     o.resize = std::stod(parser.get("--resize-probability"));
+    o.gauss = std::stod(parser.get("--gauss-probability"));
     o.ring = parser.get("--ring");
     o.mode = parser.get("--mode");
     o.maxLaunches = std::stol(parser.get("--max-launches"));
@@ -433,11 +439,15 @@ int main(int argc, char *argv[]) {
     std::cout << "  - sandwiching: " << o.sandwiching << std::endl;
     std::cout << "  - basis: " << o.basis << std::endl;
     std::cout << "  - resize: " << o.resize << std::endl;
+    if (o.gauss > 0) std::cout << "  - gauss: " << o.gauss << std::endl;  // no reference counterpart
     std::cout << "- log period: " << o.logPeriod << std::endl;
     std::cout << "- seed: " << o.seed << std::endl;
-    if (!resizeHere(o) && (o.sandwiching > 0 || o.basis > 0 || o.resize > 0))
-        std::cout << "Note: resizing, sandwiching and basis-change moves are not available in the fast mode; "
-                     "their probabilities are treated as 0"
+    if (!resizeHere(o) && (o.sandwiching > 0 || o.basis > 0 || o.resize > 0 || o.gauss > 0))
+        std::cout << "Note: resizing, sandwiching, basis-change moves and the Gauss reduction are not available in "
+                     "the fast mode; their probabilities are treated as 0"
+                  << std::endl;
+    if (o.gauss > 0 && o.ring == "ZT")
+        std::cout << "Note: the Gauss reduction is defined for the Z2 ring only; its probability is treated as 0"
                   << std::endl;
 
     FlipGraph graph(o);

@@ -246,6 +246,9 @@ void compute_params(fg_handle *h) {
     P.expand_T = thr(c.expand_p);
     P.sandwich_T = thr(c.sandwich_p);
     P.basis_T = thr(c.basis_p);
+    P.gauss_on = c.gauss_p > 0 ? 1 : 0;
+    P.gauss_gate_f = ceil_to_float(c.gauss_p);
+    P.gauss_T = thr(c.gauss_p);
     P.key0 = (uint32_t)c.seed;
     P.key1 = (uint32_t)(c.seed >> 32);
     P.random_iterations = c.resize_p > 0 ? 1 : 0;
@@ -432,6 +435,8 @@ fg_status fg_create(const fg_config *cfg, fg_handle **out) {
         return fail(FG_ERR_ARG, "resizing runs in a list mode (reference or philox)");
     if ((cfg->sandwich_p > 0 || cfg->basis_p > 0) && cfg->mode != FG_MODE_REFERENCE && cfg->mode != FG_MODE_PHILOX_LISTS)
         return fail(FG_ERR_ARG, "sandwiching and basis-change moves run in a list mode (reference or philox)");
+    if (cfg->gauss_p > 0 && (cfg->ring != FG_RING_Z2 || (cfg->mode != FG_MODE_REFERENCE && cfg->mode != FG_MODE_PHILOX_LISTS)))
+        return fail(FG_ERR_ARG, "the Gauss reduction runs on the Z2 ring in a list mode (reference or philox)");
     if (cfg->resize_p > 0 && cfg->cap < FG_MAX_RANK)
         return fail(FG_ERR_CAPACITY, "resizing needs cap >= 350 (products reach the maximal rank)");
     if (cfg->iterations <= 0) return fail(FG_ERR_ARG, "iterations must be positive");

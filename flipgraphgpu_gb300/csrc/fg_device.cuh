@@ -57,6 +57,10 @@ struct WalkParams {
     // Philox gates: draw < threshold, threshold = floor(p / iterations * 2^32);
     // kGateOff (p <= 0) = never fires and takes no draw.
     uint64_t reduce_T, expand_T, sandwich_T, basis_T;
+    // Gauss (XOR) reduction gate (no reference counterpart in the walk): off takes no draw.
+    int gauss_on;
+    float gauss_gate_f;
+    uint64_t gauss_T;
     uint32_t key0, key1;  // Philox key (seed)
     int random_iterations;  // resizing on: each launch runs randint(1, iterations) steps (flip_graph.cu:531)
 };
@@ -80,6 +84,7 @@ struct XorwowDraws {
     __device__ __forceinline__ bool gate_expand() { return uniform() * (float)P->iterations < P->expand_gate_f; }
     __device__ __forceinline__ bool gate_sandwich() { return uniform() * (float)P->iterations < P->sandwich_gate_f; }
     __device__ __forceinline__ bool gate_basis() { return uniform() * (float)P->iterations < P->basis_gate_f; }
+    __device__ __forceinline__ bool gate_gauss() { return P->gauss_on && uniform() * (float)P->iterations < P->gauss_gate_f; }
     __device__ __forceinline__ bool tie() { return uniform() < P->tie_gate_f; }
     __device__ __forceinline__ uint64_t mask(int nn) { return (uint64_t)raw() % ((uint64_t)1 << nn); }
 };
@@ -126,6 +131,7 @@ struct PhiloxDraws {
     __device__ __forceinline__ bool gate_expand() { return gate(P->expand_T); }
     __device__ __forceinline__ bool gate_sandwich() { return gate(P->sandwich_T); }
     __device__ __forceinline__ bool gate_basis() { return gate(P->basis_T); }
+    __device__ __forceinline__ bool gate_gauss() { return gate(P->gauss_T); }
     __device__ __forceinline__ bool tie() { return raw() < 42949672u; }
     __device__ __forceinline__ uint64_t mask(int nn) { return nn >= 32 ? (uint64_t)raw() : (uint64_t)(raw() & ((1u << nn) - 1u)); }
 };

@@ -169,6 +169,7 @@ __device__ void walk_one(const DevBatch &B, const WalkParams &P, int w, unsigned
             }
         }
         if (r.gate_reduce()) z.tryReduce();
+        if (r.gate_gauss()) z.tryReduceGauss();  // not in the reference's walk
         if (r.gate_expand() && z.m <= bestM + 2) {
             if (z.tryExpand(randint(1, 2, r))) flipsCount = 0;
         }

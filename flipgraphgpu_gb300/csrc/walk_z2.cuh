@@ -292,6 +292,99 @@ struct Z2Walk {
         }
         return false;
     }
+
+    // ------------------------------------------------------------ Gauss (XOR) reduction
+    // tryReduceGauss (scheme_z2.cu:312-442,621-629,1156-1163), which the reference defines
+    // but never calls.  For the components p in a random order, the term indices are
+    // sorted by their p-factor with the reference's Shell sort (gaps 701 ... 1; not
+    // stable, and each sort starts from the previous order, so the order inside a run of
+    // equal factors is the reference's); in each run, a member whose factor in component
+    // p+1 (then p+2) is the XOR of 2, 3 or 4 other members' factors there is folded into
+    // them (its third factor is added to theirs) and removed.  The search is serial on
+    // lane 0 (a rare move); the draws are the lanes' replicated stream.  Unlike the
+    // reference, zero terms are then removed and the lists rebuilt, as a walk needs.
+    __device__ int gaussXor(int j, const int *run, int size, int *comb) const {
+        if (size < 3) return 0;
+        for (int t = 0; t < size; t++) {
+            const uint64_t target = X(j, run[t]);
+            for (int a = 0; a < size; a++) {
+                if (a == t) continue;
+                const uint64_t va = X(j, run[a]);
+                for (int b = a + 1; b < size; b++) {
+                    if (b == t) continue;
+                    const uint64_t vb = X(j, run[b]);
+                    for (int c = b + 1; c < size; c++) {
+                        if (c == t) continue;
+                        const uint64_t vc = X(j, run[c]);
+                        for (int d = c + 1; d < size; d++) {
+                            if (d == t) continue;
+                            if ((va ^ vb ^ vc ^ X(j, run[d])) == target) {
+                                comb[0] = run[a]; comb[1] = run[b]; comb[2] = run[c]; comb[3] = run[d]; comb[4] = run[t];
+                                return 5;
+                            }
+                        }
+                        if ((va ^ vb ^ vc) == target) {
+                            comb[0] = run[a]; comb[1] = run[b]; comb[2] = run[c]; comb[3] = run[t];
+                            return 4;
+                        }
+                    }
+                    if ((va ^ vb) == target) {
+                        comb[0] = run[a]; comb[1] = run[b]; comb[2] = run[t];
+                        return 3;
+                    }
+                }
+            }
+        }
+        return 0;
+    }
+
+    __device__ __noinline__ bool tryReduceGauss() {
+        int perm[3];
+        perm3(perm[0], perm[1], perm[2]);
+        int comp = -1, size = 0, comb[5] = {0, 0, 0, 0, 0};
+        if (lane_id() == 0) {
+            constexpr int gaps[8] = {701, 301, 132, 57, 23, 10, 4, 1};
+            int idx[kMaxRank + 2];
+            const int mm = m < kMaxRank + 2 ? m : kMaxRank + 2;
+            for (int t = 0; t < mm; t++) idx[t] = t;
+            for (int q = 0; q < 3 && comp < 0; q++) {
+                const int p = perm[q];
+                for (int g = 0; g < 8; g++) {
+                    const int gap = gaps[g];
+                    if (gap > mm) continue;
+                    for (int i = gap; i < mm; i++) {
+                        const int tmp = idx[i];
+                        const uint64_t v = X(p, tmp);
+                        int k = i;
+                        while (k >= gap && X(p, idx[k - gap]) > v) {
+                            idx[k] = idx[k - gap];
+                            k -= gap;
+                        }
+                        idx[k] = tmp;
+                    }
+                }
+                int start = 0;
+                for (int e = 1; e <= mm && comp < 0; e++) {
+                    if (e != mm && X(p, idx[e]) == X(p, idx[start])) continue;
+                    if ((size = gaussXor((p + 1) % 3, idx + start, e - start, comb)) > 0) comp = (p + 2) % 3;
+                    else if ((size = gaussXor((p + 2) % 3, idx + start, e - start, comb)) > 0) comp = (p + 1) % 3;
+                    start = e;
+                }
+            }
+        }
+        comp = __shfl_sync(kFull, comp, 0);
+        if (comp < 0) return false;
+        size = __shfl_sync(kFull, size, 0);
+        const int last = __shfl_sync(kFull, comb[size - 1 < 0 ? 0 : size - 1], 0);
+        __syncwarp();
+        if (lane_id() == 0)
+            for (int q = 0; q < size - 1; q++) setX(comp, comb[q], X(comp, comb[q]) ^ X(comp, last));
+        __syncwarp();
+        removeAt(last);
+        removeZeroes();
+        rebuild();
+        return true;
+    }
 };
 
 }  // namespace fg

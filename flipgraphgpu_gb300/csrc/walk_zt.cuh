@@ -193,6 +193,8 @@ struct ZTWalk {
         rebuild();
     }
 
+    __device__ bool tryReduceGauss() { return false; }  // Z2 only (scheme_z2.cu:1156-1163)
+
     // tryReduce (scheme_integer.cu:1062-1101): first listed pair (list order) that can merge.
     __device__ __noinline__ bool tryReduce() {
         for (int base = 0; base < sz0; base += 32) {

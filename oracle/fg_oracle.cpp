@@ -392,6 +392,96 @@ struct Z2 {
         return false;
     }
 
+    // ---------------------------------------------------------------- Gauss (XOR) reduction
+    // tryReduceGauss (scheme_z2.cu:312-442,621-629,1156-1163), defined but never called by the
+    // reference.  For components p in a random order, the terms are sorted by their p-factor
+    // with the reference's Shell sort (gaps 701, 301, 132, 57, 23, 10, 4, 1; not stable, so the
+    // order inside a run of equal factors follows it exactly); in each run, a member whose
+    // factor in component j = p+1 (then p+2) is the XOR of 2, 3 or 4 other members' factors
+    // there is folded into them: its third factor (component i) is added to theirs and the
+    // term is removed, one rank less.  The reference leaves zero factors and the FlipSets as
+    // they are; `cleanup` (the walk's use) removes zero terms and rebuilds the lists.
+    static void shellSort(int *idx, const uint64_t *v, int count) {
+        static const int gaps[8] = {701, 301, 132, 57, 23, 10, 4, 1};
+        for (int g = 0; g < 8; g++) {
+            const int gap = gaps[g];
+            if (gap > count) continue;
+            for (int i = gap; i < count; i++) {
+                const int tmp = idx[i];
+                int j = i;
+                while (j >= gap && v[idx[j - gap]] > v[tmp]) {
+                    idx[j] = idx[j - gap];
+                    j -= gap;
+                }
+                idx[j] = tmp;
+            }
+        }
+    }
+    // First combination (search order of findXorCombination): target member t, then members
+    // a < b < c < d (indices into the run) skipping t; 4-term sums are tested before the
+    // 3-term sum of the same prefix, which is tested before the 2-term sum.
+    int findXor(int j, const int *run, int size, int *comb) const {
+        if (size < 3) return 0;
+        for (int t = 0; t < size; t++) {
+            const uint64_t target = x[j][run[t]];
+            for (int a = 0; a < size; a++) {
+                if (a == t) continue;
+                const uint64_t va = x[j][run[a]];
+                for (int b = a + 1; b < size; b++) {
+                    if (b == t) continue;
+                    const uint64_t vb = x[j][run[b]];
+                    for (int c = b + 1; c < size; c++) {
+                        if (c == t) continue;
+                        const uint64_t vc = x[j][run[c]];
+                        for (int d = c + 1; d < size; d++) {
+                            if (d == t) continue;
+                            if ((va ^ vb ^ vc ^ x[j][run[d]]) == target) {
+                                comb[0] = run[a]; comb[1] = run[b]; comb[2] = run[c]; comb[3] = run[d]; comb[4] = run[t];
+                                return 5;
+                            }
+                        }
+                        if ((va ^ vb ^ vc) == target) {
+                            comb[0] = run[a]; comb[1] = run[b]; comb[2] = run[c]; comb[3] = run[t];
+                            return 4;
+                        }
+                    }
+                    if ((va ^ vb) == target) {
+                        comb[0] = run[a]; comb[1] = run[b]; comb[2] = run[t];
+                        return 3;
+                    }
+                }
+            }
+        }
+        return 0;
+    }
+    template <class R> bool tryReduceGauss(R &r, bool cleanup) {
+        int perm[3];
+        permutation(perm, 3, r);
+        int idx[kMaxRank], comb[5];
+        int i = -1, size = 0;
+        for (int t = 0; t < m; t++) idx[t] = t;  // once: each sort starts from the previous order
+        for (int q = 0; q < 3 && i < 0; q++) {
+            const int p = perm[q];
+            shellSort(idx, x[p], m);
+            int start = 0;
+            for (int e = 1; e <= m && i < 0; e++) {
+                if (e != m && x[p][idx[e]] == x[p][idx[start]]) continue;
+                if ((size = findXor((p + 1) % 3, idx + start, e - start, comb)) > 0) i = (p + 2) % 3;
+                else if ((size = findXor((p + 2) % 3, idx + start, e - start, comb)) > 0) i = (p + 1) % 3;
+                start = e;
+            }
+        }
+        if (i < 0) return false;
+        const int last = comb[size - 1];
+        for (int q = 0; q < size - 1; q++) x[i][comb[q]] ^= x[i][last];  // reduceGauss, scheme_z2.cu:621-629
+        removeAt(last);
+        if (cleanup) {
+            removeZeroes();
+            rebuildLists();
+        }
+        return true;
+    }
+
     int complexity() const {  // scheme_z2.cu:127-139
         int count = 0;
         for (int t = 0; t < m; t++)
@@ -1089,6 +1179,7 @@ struct ZT {
     }
 
     // ---------------------------------------------------------------- basis moves
+    template <class R> bool tryReduceGauss(R &, bool) { return false; }  // Z2 only in the reference
     template <class R> void sandwiching(R &) {}  // scheme_integer.cu:1215-1217: empty in the reference
     void swapBasisRows(int i1, int i2) {  // scheme_integer.cu:791-815
         int rows[64];
@@ -1493,6 +1584,8 @@ void walkLaunch(Scheme &s, R &r, const fgo_walk_cfg *cfg, fgo_batch *b, int w) {
             bestM = s.m;
         }
         if (r.gate(cfg->reduce_p, cfg->iterations)) s.tryReduce();
+        // Gauss reduction: not in the reference's walk; no draw at probability 0
+        if (cfg->gauss_p > 0 && r.gate(cfg->gauss_p, cfg->iterations)) s.tryReduceGauss(r, true);
         if (r.gate(cfg->expand_p, cfg->iterations) && s.m <= bestM + 2) {
             if (s.tryExpand(randint(1, 2, r), r)) flipsCount = 0;
         }
@@ -1972,6 +2065,39 @@ int fgo_walk(const fgo_walk_cfg *cfg, int S, fgo_batch *b, const fgo_tape *tape)
     int bad = 0;
     for (int w = 0; w < S; w++) bad += b->status[w] != 0;
     return bad;
+}
+
+int fgo_reduce_gauss(const fgo_walk_cfg *cfg, int S, fgo_batch *b, const fgo_tape *tape, int32_t *found) {
+    if (cfg->ring != FGO_RING_Z2) return -1;
+    Z2 *s = new Z2;
+    for (int w = 0; w < S; w++) {
+        loadScheme(*s, b, w, cfg->cap);
+        s->status = &b->status[w];
+        bool hit;
+        if (cfg->rng == FGO_RNG_TAPE) {
+            RefDraws r;
+            r.d = tape->draws + tape->offsets[w];
+            r.u = tape->uniforms + tape->offsets[w];
+            r.n = tape->offsets[w + 1] - tape->offsets[w];
+            r.pos = b->rng_pos[w];
+            r.status = &b->status[w];
+            hit = s->tryReduceGauss(r, false);
+            b->rng_pos[w] = r.pos;
+        } else {
+            FastDraws r;
+            r.key[0] = (uint32_t)cfg->seed;
+            r.key[1] = (uint32_t)(cfg->seed >> 32);
+            r.walk = (uint32_t)w;
+            r.pos = b->rng_pos[w];
+            r.status = &b->status[w];
+            hit = s->tryReduceGauss(r, false);
+            b->rng_pos[w] = r.pos;
+        }
+        found[w] = hit ? 1 : 0;
+        storeScheme(*s, b, w, cfg->cap);
+    }
+    delete s;
+    return 0;
 }
 
 int fgo_minimize(const fgo_walk_cfg *cfg, int S, fgo_batch *b, const fgo_tape *tape, int32_t *best_complexity) {

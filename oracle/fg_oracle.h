@@ -45,6 +45,8 @@ typedef struct {
                                  (flip_graph.cu:236,286-299,249-277,575-613) */
     double sandwich_p;        /* --sandwiching-probability (Z2; the ternary move is empty) */
     double basis_p;           /* --basis-probability */
+    double gauss_p;           /* Gauss (XOR) reduction per step, gauss_p / iterations (Z2; not in the
+                                 reference's walk, whose tryReduceGauss is never called) */
 } fgo_walk_cfg;
 
 /* Structure-of-arrays batch of S walk records.  Factor arrays are [S][3][cap];
@@ -87,6 +89,12 @@ int fgo_init_naive(const fgo_walk_cfg *cfg, int S, int n1, int n2, int n3, fgo_b
 /* Runs cfg->launches launches of randomWalkKernel (flip_graph.cu:520-573) on
  * every walk, in place.  Returns the number of walks with a nonzero status. */
 int fgo_walk(const fgo_walk_cfg *cfg, int S, fgo_batch *b, const fgo_tape *tape);
+
+/* One call of SchemeZ2::tryReduceGauss (scheme_z2.cu:1156-1163; never called by the
+ * reference's walk) on every Z2 record, exactly as the reference does it: zero
+ * factors stay and the lists are not rebuilt.  found[w] = 1 when a combination
+ * was folded (rank one less).  Returns -1 for the ternary ring. */
+int fgo_reduce_gauss(const fgo_walk_cfg *cfg, int S, fgo_batch *b, const fgo_tape *tape, int32_t *found);
 
 /* One launch of minimizeKernel (complexity_minimizer.cu:190-214): flips with
  * checkReduce=false; best_* receives the lowest-complexity scheme seen and

@@ -43,6 +43,7 @@ def lib():
         _lib.fgo_minimize.restype = ctypes.c_int
         _lib.fgo_validate.restype = ctypes.c_int
         _lib.fgo_reduce.restype = ctypes.c_int
+        _lib.fgo_reduce_gauss.restype = ctypes.c_int
     return _lib
 
 
@@ -51,7 +52,7 @@ class WalkCfg(ctypes.Structure):
                 ("iterations", ctypes.c_int32), ("plus_iterations", ctypes.c_int32),
                 ("launches", ctypes.c_int32), ("expand_p", ctypes.c_double),
                 ("reduce_p", ctypes.c_double), ("seed", ctypes.c_uint64), ("resize_p", ctypes.c_double),
-                ("sandwich_p", ctypes.c_double), ("basis_p", ctypes.c_double)]
+                ("sandwich_p", ctypes.c_double), ("basis_p", ctypes.c_double), ("gauss_p", ctypes.c_double)]
 
 
 class _Batch(ctypes.Structure):
@@ -107,9 +108,9 @@ class WalkBatch:
         return _Batch(*[_ptr(getattr(self, f)) for f in self.FIELDS])
 
     def cfg(self, rng="tape", iterations=1000, plus_iterations=8000, launches=1, expand_p=0.01,
-            reduce_p=0.0, seed=0, resize_p=0.0, sandwich_p=0.0, basis_p=0.0):
+            reduce_p=0.0, seed=0, resize_p=0.0, sandwich_p=0.0, basis_p=0.0, gauss_p=0.0):
         return WalkCfg(RING[self.ring], RNG[rng], self.cap, iterations, plus_iterations, launches,
-                       expand_p, reduce_p, seed, resize_p, sandwich_p, basis_p)
+                       expand_p, reduce_p, seed, resize_p, sandwich_p, basis_p, gauss_p)
 
 
 def make_tape(tapes):
@@ -141,6 +142,18 @@ def walk(batch, cfg, tape=None):
     cb = batch._c()
     t, _keep = _tape_c(tape)
     return lib().fgo_walk(ctypes.byref(cfg), batch.S, ctypes.byref(cb), ctypes.byref(t) if t else None)
+
+
+def reduce_gauss(batch, cfg, tape=None):
+    """One SchemeZ2::tryReduceGauss call per walk, as the reference makes it; returns the
+    per-walk found flags."""
+    cb = batch._c()
+    t, _keep = _tape_c(tape)
+    found = np.zeros(batch.S, np.int32)
+    rc = lib().fgo_reduce_gauss(ctypes.byref(cfg), batch.S, ctypes.byref(cb), ctypes.byref(t) if t else None,
+                                _ptr(found))
+    assert rc == 0
+    return found
 
 
 def minimize(batch, cfg, best_complexity, tape=None):

@@ -21,6 +21,14 @@
 //       (scheme_additions_reducer.cu:433-540) and writes per-reducer
 //       additions / fresh-variable counts / modes plus the reducer tapes.
 //
+//   gauss IN SEED OUT   (Z2 build)
+//       Reads schemes in flip_graph's text layout (a count, then per scheme
+//       "n1 n2 n3 m" and its rows; checkValidity=false), gives scheme k the
+//       stream curand_init(SEED, k, 0) (initializeRandomStatesKernel) and
+//       calls SchemeZ2::tryReduceGauss once per scheme (scheme_z2.cu:1156-1163,
+//       a function the reference defines but never calls).  Writes the result
+//       flag and the scheme after the call, then the draw tapes.
+//
 // Binary output: little-endian int32 / uint32 / uint64 / float records; the
 // layout is documented in tests/golden/make_golden.py which parses it.
 
@@ -249,6 +257,48 @@ static int cmd_reduce(int argc, char **argv) {
     return 0;
 }
 
+#ifndef SCHEME_INTEGER
+__global__ void gaussKernel(Scheme *schemes, curandState *states, int count, int *found) {
+    int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= count) return;
+    found[idx] = schemes[idx].tryReduceGauss(states[idx]) ? 1 : 0;
+}
+
+static int cmd_gauss(int argc, char **argv) {
+    if (argc != 5) { fprintf(stderr, "gauss: bad arguments\n"); return 1; }
+    std::ifstream fin(argv[2]);
+    int seed = atoi(argv[3]);
+    int count = 0;
+    fin >> count;
+    if (count <= 0) { fprintf(stderr, "gauss: no schemes\n"); return 1; }
+    Scheme *schemes; curandState *states; int *found;
+    HCHECK(cudaMallocManaged(&schemes, count * sizeof(Scheme)));
+    HCHECK(cudaMallocManaged(&states, count * sizeof(curandState)));
+    HCHECK(cudaMallocManaged(&found, count * sizeof(int)));
+    for (int k = 0; k < count; k++)
+        if (!schemes[k].read(fin, false)) { fprintf(stderr, "gauss: read failed at %d\n", k); return 1; }
+    int blockSize = 32, numBlocks = (count + blockSize - 1) / blockSize;
+    initializeRandomStatesKernel<<<numBlocks, blockSize>>>(states, count, seed);
+    HCHECK(cudaGetLastError());
+    HCHECK(cudaDeviceSynchronize());
+    gaussKernel<<<numBlocks, blockSize>>>(schemes, states, count, found);
+    HCHECK(cudaGetLastError());
+    HCHECK(cudaDeviceSynchronize());
+    FILE *f = fopen(argv[4], "wb");
+    if (!f) { fprintf(stderr, "cannot open %s\n", argv[4]); return 1; }
+    put_i32(f, 0x46474731);  // magic "FGG1"
+    put_i32(f, count); put_i32(f, seed);
+    for (int k = 0; k < count; k++) {
+        put_i32(f, found[k]);
+        put_scheme(f, schemes[k], false);
+    }
+    write_tapes(f, states, count, seed, 64);
+    fclose(f);
+    cudaFree(schemes); cudaFree(states); cudaFree(found);
+    return 0;
+}
+#endif
+
 // time S ITERS LAUNCHES SEED PLUS_ITERS shape... (e.g. 2x2x2 3x3x3)
 //   Throughput of the reference's own walk kernel on the batched uneven
 //   workload, set up the way the reference runs several shapes: one naive
@@ -362,6 +412,9 @@ int main(int argc, char **argv) {
     if (cmd == "walk") return cmd_walk(argc, argv);
     if (cmd == "reduce") return cmd_reduce(argc, argv);
     if (cmd == "time") return cmd_time(argc, argv);
+#ifndef SCHEME_INTEGER
+    if (cmd == "gauss") return cmd_gauss(argc, argv);
+#endif
     fprintf(stderr, "unknown command %s\n", argv[1]);
     return 1;
 }

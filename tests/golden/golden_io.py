@@ -15,6 +15,10 @@ curand() values and the curand_uniform() values of those draws.
 
 A reduce file ("FGR1") holds per-reducer (U, V, W) x (additions, fresh
 variables, naive additions), the mode strings, and the per-reducer tapes.
+
+A Gauss file ("FGG1") holds the scheme count and seed, per scheme the
+result of one SchemeZ2::tryReduceGauss call and the Z2 scheme after it
+(without lists), and the per-scheme tapes.
 """
 import gzip
 import struct
@@ -150,6 +154,39 @@ def read_reduce(path):
     d["tapes"] = _tapes(r, count)
     assert r.o == len(r.b), "trailing bytes in reduce dump"
     return d
+
+
+def read_gauss(path):
+    r = _Reader(_open(path))
+    assert r.i32() == 0x46474731, "not a Gauss dump"
+    count = r.i32()
+    d = {"count": count, "seed": r.i32(), "results": []}
+    for _ in range(count):
+        found = r.i32()
+        d["results"].append({"found": found, "scheme": _scheme(r, False, False)})
+    d["tapes"] = _tapes(r, count)
+    assert r.o == len(r.b), "trailing bytes in Gauss dump"
+    return d
+
+
+def read_scheme_text(text):
+    """Schemes of flip_graph's text layout (count, then sized Z2 schemes) as
+    {"n", "m", "uvw"} with uvw[c] a uint64 array of bitmasks (|value| mod 2)."""
+    tok = text.split()
+    p = 1
+    out = []
+    for _ in range(int(tok[0])):
+        n = [int(x) for x in tok[p:p + 3]]
+        m = int(tok[p + 3])
+        p += 4
+        nn = [n[0] * n[1], n[1] * n[2], n[2] * n[0]]
+        uvw = []
+        for c in range(3):
+            vals = np.array(tok[p:p + m * nn[c]], dtype=np.int64).reshape(m, nn[c]) % 2
+            p += m * nn[c]
+            uvw.append((vals.astype(np.uint64) << np.arange(nn[c], dtype=np.uint64)).sum(axis=1).astype(np.uint64))
+        out.append({"n": n, "m": m, "uvw": uvw})
+    return out
 
 
 def factor_values(s, ring, c, t, nn):

@@ -148,14 +148,32 @@ def cli_resize(out_dir):
                 os.remove(os.path.join(fg_dir, name))
 
 
-def do_run(out_dir, resize_only=False, cli_only=False):
+# SchemeZ2::tryReduceGauss (never called by the reference's walk) on the schemes
+# of gauss_input_z2.txt.gz (made by make_gauss_input.py), one call per scheme.
+GAUSS_SEEDS = [91, 92]
+
+
+def gauss(out_dir):
+    inp = os.path.join(out_dir, "gauss_input_z2.txt")
+    with gzip.open(os.path.join(HERE, "gauss_input_z2.txt.gz"), "rb") as f, open(inp, "wb") as o:
+        o.write(f.read())
+    for seed in GAUSS_SEEDS:
+        run([harness("z2"), "gauss", inp, str(seed), os.path.join(out_dir, f"gauss_z2_s{seed}.bin")])
+    os.remove(inp)
+
+
+def do_run(out_dir, resize_only=False, cli_only=False, gauss_only=False):
     os.makedirs(out_dir, exist_ok=True)
     run([os.path.join(ROOT, "oracle", "build_ref.sh")])
+    if gauss_only:
+        gauss(out_dir)
+        return
     if cli_only:
         cli_resize(out_dir)
         return
     for case in RESIZE_CASES + MOVE_CASES:
         walk(out_dir, case)
+    gauss(out_dir)
     cli_resize(out_dir)
     if resize_only:
         return
@@ -266,8 +284,9 @@ if __name__ == "__main__":
     ap.add_argument("--pack")
     ap.add_argument("--resize-only", action="store_true", help="with --run: only the resize walks")
     ap.add_argument("--cli-only", action="store_true", help="with --run: only the flip_graph runs of CLI_CASES")
+    ap.add_argument("--gauss-only", action="store_true", help="with --run: only the tryReduceGauss calls")
     a = ap.parse_args()
     if a.run:
-        do_run(a.run, a.resize_only, a.cli_only)
+        do_run(a.run, a.resize_only, a.cli_only, a.gauss_only)
     if a.pack:
         do_pack(a.pack)

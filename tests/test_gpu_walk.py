@@ -281,3 +281,70 @@ def test_validate_matches_oracle_on_corrupted_schemes():
     want = O.validate_arrays("z2", rec.n, rec.m, rec.fac)
     assert np.array_equal(got, want)
     assert not got[::2].any() and got[1::2].all()
+
+
+def planted_gauss(rec, rng):
+    """Plants in every walk a zero-sum group (a, x_1, c), ..., (a, x_k, c), (a, x_1 ^ ... ^ x_k, c)
+    (k = 2..4) at random positions: the scheme stays exact and the Gauss reduction has a
+    combination to fold."""
+    for w in range(rec.walks):
+        n = [int(x) for x in rec.n[w]]
+        nn = [n[0] * n[1], n[1] * n[2], n[2] * n[0]]
+        m = int(rec.m[w])
+        p = int(rng.integers(3))
+        j, i = ((p + 1) % 3, (p + 2) % 3) if rng.integers(2) else ((p + 2) % 3, (p + 1) % 3)
+        k = int(rng.integers(2, 5))
+        xs = [int(rng.integers(1, 1 << nn[j])) for _ in range(k)]
+        t = 0
+        for x in xs:
+            t ^= x
+        if t == 0:
+            xs[0] ^= 1
+            t ^= 1
+        a = int(rec.fac[w, p, int(rng.integers(m))])
+        c = int(rng.integers(1, 1 << nn[i]))
+        terms = [tuple(int(rec.fac[w, q, s]) for q in range(3)) for s in range(m)]
+        for x in xs + [t]:
+            term = [0, 0, 0]
+            term[p], term[j], term[i] = a, x, c
+            terms.insert(int(rng.integers(len(terms) + 1)), tuple(term))
+        rec.m[w] = len(terms)
+        for q in range(3):
+            rec.fac[w, q, :] = 0
+            rec.fac[w, q, :len(terms)] = [s[q] for s in terms]
+        rec.best_fac[w] = rec.fac[w]
+        rec.best_m[w] = rec.best_rank[w] = len(terms)
+
+
+@pytest.mark.parametrize("mode,shape", [("reference", (3, 3, 3)), ("philox", (3, 3, 3)), ("reference", (2, 3, 4)),
+                                        ("philox", (4, 4, 4))])
+def test_gauss_reduction_vs_oracle(mode, shape):
+    """The Gauss (XOR) reduction gated into the walk (no reference counterpart in the walk;
+    the reduction itself is pinned against the reference's tryReduceGauss on the CPU) against
+    the oracle, on schemes with planted combinations: every field after every launch."""
+    n1, n2, n3 = shape
+    S, cap, seed = 64, n1 * n2 * n3 + 8, 700 + n1 * n2 * n3
+    iters, plus = 40, 100000
+    with fg.Engine(S, cap, "z2", mode, seed, iters, plus, 0.01, 0.0, gauss_p=80.0) as eng:
+        eng.init_naive(n1, n2, n3)
+        rec = eng.records()
+        planted_gauss(rec, np.random.default_rng(seed))
+        eng.set_records(rec)
+        eng.rebuild_lists()
+        rec0 = eng.records()
+        m0 = rec0.m.copy()
+        assert eng.validate().all()
+        eng.run(2)
+        rec = eng.records()
+        assert eng.validate().all() and eng.validate(best=True).all()
+    kw = dict(iterations=iters, plus_iterations=plus, expand_p=0.01, reduce_p=0.0, gauss_p=80.0, seed=seed)
+    b = batch_from(rec0)
+    if mode == "reference":
+        used = int(rec.rng_pos.max())
+        draws, unis = fg.xorwow_tape(seed, 0, S, used)
+        tape = O.make_tape([(draws[w, :rec.rng_pos[w]], unis[w, :rec.rng_pos[w]]) for w in range(S)])
+        O.walk(b, b.cfg("tape", launches=2, **kw), tape)
+    else:
+        O.walk(b, b.cfg("philox", launches=2, **kw))
+    compare_records(rec, b, f"gauss {mode} {shape}")
+    assert (rec.m < m0).mean() > 0.5

@@ -6,6 +6,7 @@ tape, the oracle must reproduce every launch's state byte for byte: factors,
 FlipSet list order, flips counter, best rank, best scheme, and the exact
 number of draws the reference consumed.
 """
+import glob
 import gzip
 import os
 
@@ -124,3 +125,40 @@ def test_fast_mode_walk_is_deterministic_and_valid():
         assert np.array_equal(getattr(b1, f), getattr(b2, f))
     assert O.validate(b1).all() and O.validate(b1, best=True).all()
     assert (b1.best_m < 27).any()
+
+
+def gauss_fixtures():
+    return sorted(glob.glob(golden("gauss_z2_s*.bin.gz")))
+
+
+def gauss_input():
+    with gzip.open(golden("gauss_input_z2.txt.gz"), "rt") as f:
+        return golden_io.read_scheme_text(f.read())
+
+
+@pytest.mark.parametrize("path", gauss_fixtures(), ids=lambda p: os.path.basename(p).split(".")[0])
+def test_reduce_gauss_matches_reference(path):
+    """SchemeZ2::tryReduceGauss (never called by the reference's walk), one call per scheme
+    with the reference's stream: same result flag, same scheme after the call (zero terms and
+    all), same number of draws."""
+    d = golden_io.read_gauss(path)
+    schemes = gauss_input()
+    assert d["count"] == len(schemes)
+    b = O.WalkBatch(len(schemes), 352, "z2")
+    for w, s in enumerate(schemes):
+        b.n[w] = s["n"]
+        b.m[w] = s["m"]
+        for c in range(3):
+            b.fac[w, c, :s["m"]] = s["uvw"][c]
+    tape = O.make_tape([(t["draws"], t["uniforms"]) for t in d["tapes"]])
+    found = O.reduce_gauss(b, b.cfg("tape"), tape)
+    assert not b.status.any()
+    want = np.array([r["found"] for r in d["results"]])
+    assert np.array_equal(found, want)
+    assert 20 < want.sum() < len(want)
+    for w, r in enumerate(d["results"]):
+        s = r["scheme"]
+        assert list(b.n[w]) == s["n"] and b.m[w] == s["m"], w
+        for c in range(3):
+            assert np.array_equal(b.fac[w, c, :s["m"]], np.asarray(s["uvw"][c], np.uint64)), (w, c)
+    assert [int(x) for x in b.rng_pos] == [t["used"] for t in d["tapes"]]
