@@ -21,7 +21,7 @@ PKG = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(PKG, "_lib", platform.machine(), "libflipgraph.so")
 LIST_CAP = 500
 MAX_RANK = 350
-RINGS = {"z2": 0, "zt": 1}
+RINGS = {"z2": 0, "zt": 1, "zb": 2}
 MODES = {"reference": 0, "philox": 1, "fast": 2, "xorwow": 0, "learned": 3}
 STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "capacity", 4: "state", 5: "walk failure"}
 
@@ -43,7 +43,8 @@ class Config(ctypes.Structure):
 class _Records(ctypes.Structure):
     _fields_ = [(name, ctypes.c_void_p) for name in
                 ("n", "m", "fac", "sgn", "valid", "list_size", "list_pairs", "flips", "best_rank",
-                 "best_m", "best_fac", "best_sgn", "best_valid", "rng_pos", "status", "best_n")]
+                 "best_m", "best_fac", "best_sgn", "best_valid", "rng_pos", "status", "best_n",
+                 "fac2", "best_fac2")]
 
 
 class Stats(ctypes.Structure):
@@ -114,15 +115,16 @@ class Records:
 
     def __init__(self, walks, cap, ring="z2", pinned=False):
         zt = ring == "zt"
+        zb = ring == "zb"
         self.walks, self.cap, self.ring = walks, cap, ring
         self._pins = []
         if pinned:
-            self._alloc_pinned(walks, cap, zt)
+            self._alloc_pinned(walks, cap, zt, zb)
             return
         self.n = np.zeros((walks, 3), np.int32)
         self.m = np.zeros(walks, np.int32)
         self.fac = np.zeros((walks, 3, cap), np.uint64)
-        self.sgn = np.zeros((walks, 3, cap), np.uint64) if zt else None
+        self.sgn = np.zeros((walks, 3, cap), np.uint64) if zt or zb else None
         self.valid = np.zeros((walks, 3, cap), np.uint8) if zt else None
         self.list_size = np.zeros((walks, 3), np.int32)
         self.list_pairs = np.zeros((walks, 3, LIST_CAP), np.uint32)
@@ -130,13 +132,23 @@ class Records:
         self.best_rank = np.zeros(walks, np.int32)
         self.best_m = np.zeros(walks, np.int32)
         self.best_fac = np.zeros((walks, 3, cap), np.uint64)
-        self.best_sgn = np.zeros((walks, 3, cap), np.uint64) if zt else None
+        self.best_sgn = np.zeros((walks, 3, cap), np.uint64) if zt or zb else None
         self.best_valid = np.zeros((walks, 3, cap), np.uint8) if zt else None
         self.rng_pos = np.zeros(walks, np.int64)
         self.status = np.zeros(walks, np.int32)
         self.best_n = np.zeros((walks, 3), np.int32)
+        self.fac2 = np.zeros((walks, 3, cap), np.uint64) if zb else None
+        self.best_fac2 = np.zeros((walks, 3, cap), np.uint64) if zb else None
 
-    def _alloc_pinned(self, walks, cap, zt):
+    def coefficients(self, best=False):
+        """ZB: int8 coefficients [walks][3][cap][64] from the sign-magnitude masks."""
+        fac, sgn, two = (self.best_fac, self.best_sgn, self.best_fac2) if best else (self.fac, self.sgn, self.fac2)
+        bits = np.arange(64, dtype=np.uint64)
+        nz = ((fac[..., None] >> bits) & np.uint64(1)).astype(np.int8)
+        mag = nz * (1 + ((two[..., None] >> bits) & np.uint64(1)).astype(np.int8))
+        return np.where(((sgn[..., None] >> bits) & np.uint64(1)).astype(bool), -mag, mag).astype(np.int8)
+
+    def _alloc_pinned(self, walks, cap, zt, zb=False):
         def pin(shape, dtype):
             b = PinnedBuffer(shape, dtype)
             self._pins.append(b)
@@ -145,7 +157,7 @@ class Records:
         self.n = pin((walks, 3), np.int32)
         self.m = pin((walks,), np.int32)
         self.fac = pin((walks, 3, cap), np.uint64)
-        self.sgn = pin((walks, 3, cap), np.uint64) if zt else None
+        self.sgn = pin((walks, 3, cap), np.uint64) if zt or zb else None
         self.valid = pin((walks, 3, cap), np.uint8) if zt else None
         self.list_size = pin((walks, 3), np.int32)
         self.list_pairs = pin((walks, 3, LIST_CAP), np.uint32)
@@ -153,11 +165,13 @@ class Records:
         self.best_rank = pin((walks,), np.int32)
         self.best_m = pin((walks,), np.int32)
         self.best_fac = pin((walks, 3, cap), np.uint64)
-        self.best_sgn = pin((walks, 3, cap), np.uint64) if zt else None
+        self.best_sgn = pin((walks, 3, cap), np.uint64) if zt or zb else None
         self.best_valid = pin((walks, 3, cap), np.uint8) if zt else None
         self.rng_pos = pin((walks,), np.int64)
         self.status = pin((walks,), np.int32)
         self.best_n = pin((walks, 3), np.int32)
+        self.fac2 = pin((walks, 3, cap), np.uint64) if zb else None
+        self.best_fac2 = pin((walks, 3, cap), np.uint64) if zb else None
 
     def nbytes(self):
         return sum(getattr(self, f).nbytes for f, _ in self.FIELDS if getattr(self, f) is not None)

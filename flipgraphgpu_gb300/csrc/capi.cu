@@ -55,6 +55,11 @@ __global__ void k_init_naive(DevBatch B, int n1_, int n2_, int n3_, const int32_
         uint8_t *v = B.valid + (size_t)w * 3 * cap, *bv = B.best_valid + (size_t)w * 3 * cap;
         for (int q = 0; q < 3 * cap; q++) { g[q] = 0; bg[q] = 0; v[q] = 0; bv[q] = 0; }
     }
+    if (B.fac2) {  // ZB: signs and |c| = 2 masks start at zero
+        uint64_t *g = B.sgn + (size_t)w * 3 * cap, *bg = B.best_sgn + (size_t)w * 3 * cap;
+        uint64_t *t2 = B.fac2 + (size_t)w * 3 * cap, *bt2 = B.best_fac2 + (size_t)w * 3 * cap;
+        for (int q = 0; q < 3 * cap; q++) { g[q] = 0; bg[q] = 0; t2[q] = 0; bt2[q] = 0; }
+    }
     for (int i = 0; i < n1; i++)
         for (int j = 0; j < n3; j++)
             for (int k = 0; k < n2; k++) {
@@ -258,6 +263,10 @@ int verify_grid(fg_handle *h) { return (h->B.S + 3) / 4; }
 size_t verify_smem(fg_handle *h) { return (size_t)4 * 3 * h->B.cap * sizeof(uint64_t); }
 
 fg_status launch_verify(fg_handle *h, int best) {
+    if (h->cfg.ring == FG_RING_ZB) {
+        FG_CUDA(launch_verify_zb(h->B, best, h->d_valid, h->stream));
+        return FG_OK;
+    }
     if (h->cfg.ring == FG_RING_ZT) {
         size_t smem = 2 * verify_smem(h);
         FG_CUDA(cudaFuncSetAttribute(k_verify_zt, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -385,9 +394,11 @@ fg_status launch_walks(fg_handle *h) {
         return FG_OK;
     }
     const int wpb = h->cfg.walks_per_block > 0 ? h->cfg.walks_per_block : 2;
-    for (const Segment &g : h->segs)
-        if (g.nnmax > 56) return fail(FG_ERR_CAPACITY, "fast mode holds factors of at most 56 entries");
+    if (h->cfg.ring != FG_RING_ZB)
+        for (const Segment &g : h->segs)
+            if (g.nnmax > 56) return fail(FG_ERR_CAPACITY, "fast mode holds factors of at most 56 entries");
     auto launch = [&](const Segment &g, cudaStream_t st) {
+        if (h->cfg.ring == FG_RING_ZB) return launch_walk_zb(h->B, h->P, g.first, g.count, g.scap, h->sms, st);
         int kind;
         if (h->fastKernel >= 0) kind = h->fastKernel;
         else if (h->simtMaxCap >= 0) kind = g.scap <= h->simtMaxCap ? FG_FAST_THREAD : FG_FAST_WARP;
@@ -423,7 +434,11 @@ fg_status fg_create(const fg_config *cfg, fg_handle **out) {
     if (!cfg || !out) return fail(FG_ERR_ARG, "null argument");
     *out = nullptr;
     if (cfg->walks <= 0) return fail(FG_ERR_ARG, "walks must be positive");
-    if (cfg->ring != FG_RING_Z2 && cfg->ring != FG_RING_ZT) return fail(FG_ERR_ARG, "unknown ring");
+    if (cfg->ring != FG_RING_Z2 && cfg->ring != FG_RING_ZT && cfg->ring != FG_RING_ZB) return fail(FG_ERR_ARG, "unknown ring");
+    if (cfg->ring == FG_RING_ZB && cfg->mode != FG_MODE_FAST)
+        return fail(FG_ERR_ARG, "the bounded-integer ring (ZB) runs in the fast mode");
+    if (cfg->ring == FG_RING_ZB && (cfg->resize_p > 0 || cfg->sandwich_p > 0 || cfg->basis_p > 0 || cfg->gauss_p > 0))
+        return fail(FG_ERR_ARG, "resizing, sandwiching, basis changes and the Gauss reduction are not defined for ZB");
     if (cfg->ring == FG_RING_ZT && (cfg->mode == FG_MODE_FAST || cfg->mode == FG_MODE_LEARNED))
         return fail(FG_ERR_ARG, "the fast and learned modes are available for the Z2 ring; use a list mode for ZT");
     if (cfg->mode != FG_MODE_REFERENCE && cfg->mode != FG_MODE_PHILOX_LISTS && cfg->mode != FG_MODE_FAST &&
@@ -460,6 +475,13 @@ fg_status fg_create(const fg_config *cfg, fg_handle **out) {
     if (cfg->ring == FG_RING_ZT) {
         if ((st = dalloc(&h->B.sgn, nf)) || (st = dalloc(&h->B.best_sgn, nf)) || (st = dalloc(&h->B.valid, nf)) ||
             (st = dalloc(&h->B.best_valid, nf))) {
+            fg_destroy(h);
+            return st;
+        }
+    }
+    if (cfg->ring == FG_RING_ZB) {
+        if ((st = dalloc(&h->B.sgn, nf)) || (st = dalloc(&h->B.best_sgn, nf)) || (st = dalloc(&h->B.fac2, nf)) ||
+            (st = dalloc(&h->B.best_fac2, nf))) {
             fg_destroy(h);
             return st;
         }
@@ -510,7 +532,7 @@ fg_status fg_destroy(fg_handle *h) {
     learned_free(h->learned);
     void *ptrs[] = {h->B.hdr, h->B.fac, h->B.sgn, h->B.valid, h->B.lists, h->B.best_fac, h->B.best_sgn,
                     h->B.best_valid, h->B.xorwow, h->d_bestC, h->d_valid, h->B.best_n, h->d_copyList,
-                    h->d_bestRanks};
+                    h->d_bestRanks, h->B.fac2, h->B.best_fac2};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     for (auto &e : h->ev)
@@ -725,6 +747,13 @@ fg_status fg_set_records(fg_handle *h, const fg_records *rec) {
         FG_CUDA(cudaMemcpy(h->B.best_sgn, rec->best_sgn ? rec->best_sgn : rec->sgn, nf * 8, cudaMemcpyHostToDevice));
         FG_CUDA(cudaMemcpy(h->B.best_valid, rec->best_valid ? rec->best_valid : rec->valid, nf, cudaMemcpyHostToDevice));
     }
+    if (h->cfg.ring == FG_RING_ZB) {
+        if (!rec->sgn || !rec->fac2) return fail(FG_ERR_ARG, "ZB records need sgn and fac2");
+        FG_CUDA(cudaMemcpy(h->B.sgn, rec->sgn, nf * 8, cudaMemcpyHostToDevice));
+        FG_CUDA(cudaMemcpy(h->B.fac2, rec->fac2, nf * 8, cudaMemcpyHostToDevice));
+        FG_CUDA(cudaMemcpy(h->B.best_sgn, rec->best_sgn ? rec->best_sgn : rec->sgn, nf * 8, cudaMemcpyHostToDevice));
+        FG_CUDA(cudaMemcpy(h->B.best_fac2, rec->best_fac2 ? rec->best_fac2 : rec->fac2, nf * 8, cudaMemcpyHostToDevice));
+    }
     plan_segments(h, hdr);
     h->ready = true;
     h->tableReady = false;
@@ -762,6 +791,12 @@ fg_status fg_get_records(fg_handle *h, fg_records *rec) {
         if (rec->valid) FG_CUDA(cudaMemcpy(rec->valid, h->B.valid, nf, cudaMemcpyDeviceToHost));
         if (rec->best_sgn) FG_CUDA(cudaMemcpy(rec->best_sgn, h->B.best_sgn, nf * 8, cudaMemcpyDeviceToHost));
         if (rec->best_valid) FG_CUDA(cudaMemcpy(rec->best_valid, h->B.best_valid, nf, cudaMemcpyDeviceToHost));
+    }
+    if (h->cfg.ring == FG_RING_ZB) {
+        if (rec->sgn) FG_CUDA(cudaMemcpy(rec->sgn, h->B.sgn, nf * 8, cudaMemcpyDeviceToHost));
+        if (rec->fac2) FG_CUDA(cudaMemcpy(rec->fac2, h->B.fac2, nf * 8, cudaMemcpyDeviceToHost));
+        if (rec->best_sgn) FG_CUDA(cudaMemcpy(rec->best_sgn, h->B.best_sgn, nf * 8, cudaMemcpyDeviceToHost));
+        if (rec->best_fac2) FG_CUDA(cudaMemcpy(rec->best_fac2, h->B.best_fac2, nf * 8, cudaMemcpyDeviceToHost));
     }
     return FG_OK;
 }

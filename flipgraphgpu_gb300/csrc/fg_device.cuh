@@ -44,6 +44,7 @@ struct DevBatch {
     uint8_t *best_valid;
     curandStateXORWOW_t *xorwow;  // reference stream states (FG_RNG_XORWOW)
     int32_t *best_n;              // [S][3] sizes of the best scheme (resizing), or null
+    uint64_t *fac2, *best_fac2;   // ZB: |c| = 2 masks (fac = nonzero, sgn = negative)
 };
 
 constexpr uint64_t kGateOff = ~0ull;

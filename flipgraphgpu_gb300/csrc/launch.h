@@ -38,4 +38,9 @@ cudaError_t launch_walk_group(const DevBatch &B, const WalkParams &P, int first,
 cudaError_t launch_walk_warpfast(const DevBatch &B, const WalkParams &P, int first, int count, int scap, int wide,
                                  int sms, cudaStream_t s);
 
+// Bounded-integer (ZB, |c| <= 2) fast-mode walk, one warp per walk, and its exact integer check.
+cudaError_t launch_walk_zb(const DevBatch &B, const WalkParams &P, int first, int count, int scap, int sms,
+                           cudaStream_t s);
+cudaError_t launch_verify_zb(const DevBatch &B, int best, uint8_t *out, cudaStream_t s);
+
 }  // namespace fg

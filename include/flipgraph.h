@@ -28,7 +28,9 @@ typedef enum {
     FG_ERR_WALK = 5       /* a walk hit a retry bound or overflow; see the status array */
 } fg_status;
 
-typedef enum { FG_RING_Z2 = 0, FG_RING_ZT = 1 } fg_ring;
+/* FG_RING_ZB: integer coefficients bounded by |c| <= 2, FG_MODE_FAST only; no
+ * reference counterpart (the reference's integer ring is ZT, {-1, 0, 1}). */
+typedef enum { FG_RING_Z2 = 0, FG_RING_ZT = 1, FG_RING_ZB = 2 } fg_ring;
 
 /* Walk mode.
  * FG_MODE_REFERENCE: the reference's stream -- cuRAND XORWOW with
@@ -108,6 +110,9 @@ typedef struct {
     int64_t *rng_pos;     /* [walks] draws consumed since seeding */
     int32_t *status;      /* [walks] FG_WALK_* bits */
     int32_t *best_n;      /* [walks][3] sizes of the best scheme (resizing; NULL = n) */
+    uint64_t *fac2;       /* ZB only: [walks][3][cap] entries with |c| = 2; for ZB, fac marks the
+                             nonzero entries and sgn the negative ones (valid unused) */
+    uint64_t *best_fac2;  /* ZB only */
 } fg_records;
 
 typedef struct {

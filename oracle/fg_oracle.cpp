@@ -1685,6 +1685,400 @@ void runMinimize(const fgo_walk_cfg *cfg, int S, fgo_batch *b, const fgo_tape *t
     delete s;
 }
 
+// ============================================================ bounded integer ring (ZB)
+// Coefficients in [-2, 2] (integer-coefficient search with |c| <= 2).  No
+// reference counterpart: the reference's integer ring is {-1, 0, 1}
+// (SchemeInteger).  The walk follows SchemeInteger's structure with the
+// library's fast-mode proposal (implicit enumeration of ordered pairs of
+// exactly equal factors in canonical order, Philox stream) and these rules:
+//   pairs are factors equal up to sign (x_b = e x_a, e = +-1: the sign moves
+//     to another slot of the term, so the pair shares the factor);
+//   flip (a, b) sharing factor i, (j, k) = the other two in a coin-chosen
+//     order, s = +-1 by a second coin: y_a += s e y_b, z_b -= s z_a (both
+//     signs are flips, so every flip has its inverse and the walk does not
+//     drift to large coefficients); a proposal whose result leaves [-2, 2]
+//     is rejected (the step is spent);
+//   signs: first nonzero entry of u and of v positive (SchemeInteger::fixSigns,
+//     scheme_integer.cu:398-425), applied to every changed term;
+//   a term with a zero factor is removed (compaction re-checks moved terms);
+//   after a flip, term a then term b: the first term t (ascending) that
+//     shares two factors with it up to sign (component pairs (0,1), (0,2),
+//     (1,2); equal before negated) and whose merged third factor stays in
+//     bounds absorbs it: x_r[t] += e * x_r[a], e = product of the two signs;
+//   plus (a, b with all factors distinct, components permuted i, j, k):
+//     (A_i - B_i, A_j, A_k), (B_i, A_j - B_j, A_k), (B_i, B_j, A_k + B_k),
+//     the third dropped when zero; any bound violation rejects it;
+//   split of factor x by r: (r, y, z) and (x - r, y, z); trySplit draws r
+//     with entries in {-1, 0, 1} (nonzero mask, sign mask), trySplitExisted
+//     takes another term's factor; five redraws at most, as SchemeZ2.
+constexpr int kZBBound = 2;
+
+struct ZBVec {
+    int8_t c[kMaxMatrix];
+};
+inline bool zbEq(const ZBVec &a, const ZBVec &b) { return std::memcmp(a.c, b.c, kMaxMatrix) == 0; }
+inline bool zbNegEq(const ZBVec &a, const ZBVec &b) {
+    for (int e = 0; e < kMaxMatrix; e++)
+        if (a.c[e] != -b.c[e]) return false;
+    return true;
+}
+inline bool zbSim(const ZBVec &a, const ZBVec &b) { return zbEq(a, b) || zbNegEq(a, b); }
+inline bool zbZero(const ZBVec &a) {
+    for (int e = 0; e < kMaxMatrix; e++)
+        if (a.c[e]) return false;
+    return true;
+}
+inline bool zbFirstPositive(const ZBVec &a) {
+    for (int e = 0; e < kMaxMatrix; e++)
+        if (a.c[e]) return a.c[e] > 0;
+    return true;
+}
+inline void zbNegate(ZBVec &a) {
+    for (int e = 0; e < kMaxMatrix; e++) a.c[e] = (int8_t)-a.c[e];
+}
+// a + s*b; false when an entry leaves [-2, 2]
+inline bool zbAdd(const ZBVec &a, const ZBVec &b, int s, ZBVec &out) {
+    bool ok = true;
+    for (int e = 0; e < kMaxMatrix; e++) {
+        const int v = a.c[e] + s * b.c[e];
+        ok &= v >= -kZBBound && v <= kZBBound;
+        out.c[e] = (int8_t)v;
+    }
+    return ok;
+}
+
+struct ZB {
+    int n[3], nn[3], m;
+    ZBVec x[3][kMaxRank];
+    int32_t *status;
+
+    int full() const { return n[0] * n[1] * n[2]; }
+    bool zeroTerm(int t) const { return zbZero(x[0][t]) || zbZero(x[1][t]) || zbZero(x[2][t]); }
+
+    void initNaive(int n1, int n2, int n3) {  // the standard scheme, as scheme_z2.cu:32-55
+        n[0] = n1; n[1] = n2; n[2] = n3;
+        nn[0] = n1 * n2; nn[1] = n2 * n3; nn[2] = n3 * n1;
+        m = n1 * n2 * n3;
+        std::memset(x, 0, sizeof(x));
+        for (int i = 0; i < n1; i++)
+            for (int j = 0; j < n3; j++)
+                for (int k = 0; k < n2; k++) {
+                    int t = (i * n3 + j) * n2 + k;
+                    x[0][t].c[i * n2 + k] = 1;
+                    x[1][t].c[k * n3 + j] = 1;
+                    x[2][t].c[j * n1 + i] = 1;
+                }
+    }
+
+    void fixSigns(int t) {
+        const bool pi = zbFirstPositive(x[0][t]), pj = zbFirstPositive(x[1][t]);
+        if (pi && pj) return;
+        if (!pi && !pj) { zbNegate(x[0][t]); zbNegate(x[1][t]); }
+        else if (!pi) { zbNegate(x[0][t]); zbNegate(x[2][t]); }
+        else { zbNegate(x[1][t]); zbNegate(x[2][t]); }
+    }
+    void moveTerm(int dst, int src) { for (int c = 0; c < 3; c++) x[c][dst] = x[c][src]; }
+    void removeAt(int t) { m--; if (t != m) moveTerm(t, m); }
+    void removeZeroes() {
+        for (int t = 0; t < m; t++)
+            if (zeroTerm(t)) { removeAt(t); t--; }
+    }
+    void append(const ZBVec &a, const ZBVec &b, const ZBVec &c) {
+        if (m >= kMaxRank) { *status |= ST_OVERFLOW; return; }
+        x[0][m] = a; x[1][m] = b; x[2][m] = c;
+        m++;
+    }
+    int partners(int c, int t) const {
+        int k = 0;
+        for (int u = 0; u < m; u++) k += u != t && zbSim(x[c][u], x[c][t]);
+        return k;
+    }
+
+    // Two factors of term t equal term a's up to sign, third merged within bounds.
+    bool mergeable(int a, int t, int &r, ZBVec &merged) const {
+        static const int pairs[3][2] = {{0, 1}, {0, 2}, {1, 2}};
+        for (int q = 0; q < 3; q++) {
+            const int p0 = pairs[q][0], p1 = pairs[q][1];
+            const int e0 = zbEq(x[p0][t], x[p0][a]) ? 1 : (zbNegEq(x[p0][t], x[p0][a]) ? -1 : 0);
+            if (!e0) continue;
+            const int e1 = zbEq(x[p1][t], x[p1][a]) ? 1 : (zbNegEq(x[p1][t], x[p1][a]) ? -1 : 0);
+            if (!e1) continue;
+            r = 3 - p0 - p1;
+            if (zbAdd(x[r][t], x[r][a], e0 * e1, merged)) return true;
+        }
+        return false;
+    }
+    // keep absorbs drop: x_r[keep] = merged, drop removed, keep removed too when merged is zero.
+    void merge(int keep, int drop, int r, const ZBVec &merged) {
+        x[r][keep] = merged;
+        const bool zero = zbZero(merged);
+        removeAt(drop);
+        if (keep == m) keep = drop;  // the last term moved into drop's slot
+        if (zero) removeAt(keep);
+        else fixSigns(keep);
+    }
+    bool reduceWith(int a) {
+        for (int t = 0; t < m; t++) {
+            if (t == a) continue;
+            int r;
+            ZBVec merged;
+            if (mergeable(a, t, r, merged)) { merge(t, a, r, merged); return true; }
+        }
+        return false;
+    }
+    bool tryReduce() {
+        for (int a = 0; a < m; a++)
+            for (int b = a + 1; b < m; b++) {
+                int r;
+                ZBVec merged;
+                if (mergeable(b, a, r, merged)) { merge(a, b, r, merged); return true; }
+            }
+        return false;
+    }
+
+    // 1 accepted, 0 no candidate pair, -1 proposal rejected (bound).
+    template <class R> int tryFlip(R &r) {
+        int total[3] = {0, 0, 0};
+        for (int c = 0; c < 3; c++)
+            for (int t = 0; t < m; t++) total[c] += partners(c, t);
+        const uint32_t P = (uint32_t)(total[0] + total[1] + total[2]);
+        if (!P) return 0;
+        uint32_t q = r.below(P);
+        int c = 0;
+        while (q >= (uint32_t)total[c]) { q -= total[c]; c++; }
+        int a = 0;
+        for (;; a++) {
+            const uint32_t h = (uint32_t)partners(c, a);
+            if (q < h) break;
+            q -= h;
+        }
+        int b = 0;
+        for (;; b++)
+            if (b != a && zbSim(x[c][b], x[c][a])) {
+                if (q == 0) break;
+                q--;
+            }
+        const int e = zbEq(x[c][b], x[c][a]) ? 1 : -1;
+        int j = c == 0 ? 1 : 0, k = c == 2 ? 1 : 2;
+        if (r.coin()) std::swap(j, k);
+        const int sg = r.coin() ? -1 : 1;
+        ZBVec na, nb;
+        if (!zbAdd(x[j][a], x[j][b], sg * e, na) || !zbAdd(x[k][b], x[k][a], -sg, nb)) return -1;
+        x[j][a] = na;
+        x[k][b] = nb;
+        fixSigns(a);
+        fixSigns(b);
+        if (zeroTerm(a) || zeroTerm(b)) {
+            removeZeroes();
+            return 1;
+        }
+        if (!reduceWith(a)) reduceWith(b);
+        return 1;
+    }
+
+    template <class R> bool tryPlus(R &r) {
+        if (m >= kMaxRank || m >= full()) return false;
+        int a = (int)r.below((uint32_t)m), b = (int)r.below((uint32_t)m);
+        int guard = 0;
+        while (a == b || zbSim(x[0][a], x[0][b]) || zbSim(x[1][a], x[1][b]) || zbSim(x[2][a], x[2][b])) {
+            if (++guard > kRetryCap) { *status |= ST_RETRY; return false; }
+            a = (int)r.below((uint32_t)m);
+            b = (int)r.below((uint32_t)m);
+        }
+        int perm[3];
+        permutation(perm, 3, r);
+        const int i = perm[0], j = perm[1], k = perm[2];
+        ZBVec ti, tj, tk;
+        if (!zbAdd(x[i][a], x[i][b], -1, ti) || !zbAdd(x[j][a], x[j][b], -1, tj) || !zbAdd(x[k][a], x[k][b], 1, tk))
+            return false;
+        const ZBVec Bi = x[i][b], Bj = x[j][b], Ak = x[k][a];
+        x[i][a] = ti;
+        x[j][b] = tj;
+        x[k][b] = Ak;
+        fixSigns(a);
+        fixSigns(b);
+        if (!zbZero(tk)) {
+            ZBVec t3[3];
+            t3[i] = Bi; t3[j] = Bj; t3[k] = tk;
+            append(t3[0], t3[1], t3[2]);
+            fixSigns(m - 1);
+        }
+        return true;
+    }
+
+    template <class R> uint64_t mask64(int bits, R &r) {
+        const uint64_t low = bits >= 64 ? ~0ull : ((1ull << bits) - 1);
+        if (bits <= 32) return (uint64_t)r.raw() & low;
+        const uint64_t lo = r.raw();
+        return (lo | ((uint64_t)r.raw() << 32)) & low;
+    }
+    template <class R> ZBVec randomTernary(int bits, R &r) {
+        const uint64_t nz = mask64(bits, r);
+        const uint64_t neg = mask64(bits, r) & nz;
+        ZBVec v;
+        std::memset(v.c, 0, sizeof v.c);
+        for (int e = 0; e < bits; e++)
+            if ((nz >> e) & 1) v.c[e] = ((neg >> e) & 1) ? -1 : 1;
+        return v;
+    }
+    // term t -> (v, y, z) and (x_i - v, y, z)
+    void split(int i, int t, const ZBVec &v, const ZBVec &rest) {
+        ZBVec nt[3] = {x[0][t], x[1][t], x[2][t]};
+        nt[i] = rest;
+        x[i][t] = v;
+        fixSigns(t);
+        append(nt[0], nt[1], nt[2]);
+        fixSigns(m - 1);
+    }
+    template <class R> bool trySplit(R &r) {
+        if (m >= kMaxRank || m >= full()) return false;
+        const int t = (int)r.below((uint32_t)m);
+        int perm[3];
+        permutation(perm, 3, r);
+        const int i = perm[0];
+        ZBVec v = randomTernary(nn[i], r), rest;
+        auto bad = [&]() { return zbZero(v) || zbEq(v, x[i][t]) || !zbAdd(x[i][t], v, -1, rest); };
+        int loop = 0;
+        while (loop < 5 && bad()) { v = randomTernary(nn[i], r); loop++; }
+        if (loop == 5) return false;
+        split(i, t, v, rest);
+        return true;
+    }
+    template <class R> bool trySplitExisted(R &r) {
+        if (m >= kMaxRank || m >= full()) return false;
+        int perm[3];
+        permutation(perm, 3, r);
+        const int i = perm[0];
+        const int a = (int)r.below((uint32_t)m);
+        int b = (int)r.below((uint32_t)m);
+        ZBVec rest;
+        auto bad = [&]() { return a == b || zbEq(x[i][a], x[i][b]) || !zbAdd(x[i][a], x[i][b], -1, rest); };
+        int loop = 0;
+        while (loop < 5 && bad()) { b = (int)r.below((uint32_t)m); loop++; }
+        if (loop == 5) return false;
+        split(i, a, x[i][b], rest);
+        return true;
+    }
+    template <class R> bool tryExpand(int count, R &r) {
+        bool result = false;
+        for (int q = 0; q < count && m < full(); q++) {
+            const int v = (int)r.below(3);
+            if (v == 0) result |= tryPlus(r);
+            else if (v == 1) result |= trySplit(r);
+            else result |= trySplitExisted(r);
+        }
+        return result;
+    }
+};
+
+// Host records of ZB factors: sign-magnitude masks, fac = nonzero, sgn = negative, fac2 = |c| = 2.
+inline void zbToMasks(const ZBVec &v, uint64_t &nz, uint64_t &neg, uint64_t &two) {
+    nz = neg = two = 0;
+    for (int e = 0; e < kMaxMatrix; e++) {
+        if (!v.c[e]) continue;
+        nz |= 1ull << e;
+        if (v.c[e] < 0) neg |= 1ull << e;
+        if (v.c[e] == 2 || v.c[e] == -2) two |= 1ull << e;
+    }
+}
+inline ZBVec zbFromMasks(uint64_t nz, uint64_t neg, uint64_t two) {
+    ZBVec v;
+    for (int e = 0; e < kMaxMatrix; e++) {
+        int c = (nz >> e) & 1 ? (((two >> e) & 1) ? 2 : 1) : 0;
+        v.c[e] = (int8_t)(((neg >> e) & 1) ? -c : c);
+    }
+    return v;
+}
+
+void loadZB(ZB &s, const fgo_batch *b, int w, int cap) {
+    for (int c = 0; c < 3; c++) s.n[c] = b->n[w * 3 + c];
+    for (int c = 0; c < 3; c++) s.nn[c] = s.n[c] * s.n[(c + 1) % 3];
+    s.m = b->m[w];
+    for (int c = 0; c < 3; c++)
+        for (int t = 0; t < s.m; t++) {
+            const size_t q = facIndex(w, c, t, cap);
+            s.x[c][t] = zbFromMasks(b->fac[q], b->sgn[q], b->fac2[q]);
+        }
+}
+
+void storeZBInto(const ZB &s, uint64_t *fac, uint64_t *sgn, uint64_t *fac2, int w, int cap) {
+    for (int c = 0; c < 3; c++)
+        for (int t = 0; t < cap; t++) {
+            const size_t q = facIndex(w, c, t, cap);
+            uint64_t nz = 0, neg = 0, two = 0;
+            if (t < s.m) zbToMasks(s.x[c][t], nz, neg, two);
+            fac[q] = nz; sgn[q] = neg; fac2[q] = two;
+        }
+}
+
+void storeZB(const ZB &s, fgo_batch *b, int w, int cap) {
+    if (s.m > cap) { b->status[w] |= ST_OVERFLOW; return; }
+    b->m[w] = s.m;
+    for (int c = 0; c < 3; c++) b->n[w * 3 + c] = s.n[c];
+    storeZBInto(s, b->fac, b->sgn, b->fac2, w, cap);
+}
+
+void storeBestZB(const ZB &s, fgo_batch *b, int w, int cap) {
+    if (s.m > cap) { b->status[w] |= ST_OVERFLOW; return; }
+    b->best_m[w] = s.m;
+    storeZBInto(s, b->best_fac, b->best_sgn, b->best_fac2, w, cap);
+}
+
+// The fast-mode walk launch over ZB (the Z2 fast walk's loop, flip_graph.cu:526-569
+// shape, with the bound's rejected proposals spending their step).
+template <class R>
+void walkLaunchZB(ZB &s, R &r, const fgo_walk_cfg *cfg, fgo_batch *b, int w) {
+    const int cap = cfg->cap;
+    int flipsCount = b->flips[w];
+    int bestRank = b->best_rank[w];
+    int bestM = b->best_m[w];
+    for (int it = 0; it < cfg->iterations; it++) {
+        const int rank = s.m;
+        const int f = s.tryFlip(r);
+        if (f == 0) {
+            s.tryExpand(randint(1, 2, r), r);
+            if (*s.status) break;
+            continue;
+        }
+        if (f < 0) continue;
+        if (b->accepted) b->accepted[w]++;
+        if (s.m < rank) flipsCount = 0;
+        flipsCount++;
+        if (s.m < bestRank || (s.m == bestRank && r.tie())) {
+            bestRank = s.m;
+            storeBestZB(s, b, w, cap);
+            bestM = s.m;
+        }
+        if (r.gate(cfg->reduce_p, cfg->iterations)) s.tryReduce();
+        if (r.gate(cfg->expand_p, cfg->iterations) && s.m <= bestM + 2) {
+            if (s.tryExpand(randint(1, 2, r), r)) flipsCount = 0;
+        }
+        if (flipsCount >= cfg->plus_iterations && s.tryPlus(r)) flipsCount = 0;
+        if (*s.status) break;
+    }
+    b->flips[w] = flipsCount;
+    b->best_rank[w] = bestRank;
+}
+
+void runWalksZB(const fgo_walk_cfg *cfg, int S, fgo_batch *b) {
+    ZB *s = new ZB;
+    for (int w = 0; w < S; w++) {
+        std::memset(s->x, 0, sizeof(s->x));
+        loadZB(*s, b, w, cfg->cap);
+        s->status = &b->status[w];
+        FastDraws r;
+        r.key[0] = (uint32_t)cfg->seed;
+        r.key[1] = (uint32_t)(cfg->seed >> 32);
+        r.walk = (uint32_t)w;
+        r.pos = b->rng_pos[w];
+        r.status = &b->status[w];
+        for (int L = 0; L < cfg->launches && !b->status[w]; L++) walkLaunchZB(*s, r, cfg, b, w);
+        b->rng_pos[w] = r.pos;
+        storeZB(*s, b, w, cfg->cap);
+    }
+    delete s;
+}
+
 }  // namespace
 
 // ============================================================ additions reducer
@@ -2023,6 +2417,20 @@ void fgo_set_fma(int fuse_float, int fuse_double) { g_fuse_float = fuse_float; g
 
 int fgo_init_naive(const fgo_walk_cfg *cfg, int S, int n1, int n2, int n3, fgo_batch *b) {
     int bad = 0;
+    if (cfg->ring == FGO_RING_ZB) {
+        ZB *s = new ZB;
+        for (int w = 0; w < S; w++) {
+            s->status = &b->status[w];
+            s->initNaive(n1, n2, n3);
+            storeZB(*s, b, w, cfg->cap);
+            storeBestZB(*s, b, w, cfg->cap);
+            b->best_rank[w] = n1 * n2 * n3;
+            b->flips[w] = 0;
+            bad += b->status[w] != 0;
+        }
+        delete s;
+        return bad;
+    }
     if (cfg->ring == FGO_RING_Z2) {
         Z2 *s = new Z2;
         for (int w = 0; w < S; w++) {
@@ -2052,6 +2460,14 @@ int fgo_init_naive(const fgo_walk_cfg *cfg, int S, int n1, int n2, int n3, fgo_b
 }
 
 int fgo_walk(const fgo_walk_cfg *cfg, int S, fgo_batch *b, const fgo_tape *tape) {
+    if (cfg->ring == FGO_RING_ZB) {
+        if (cfg->rng != FGO_RNG_FAST || cfg->resize_p > 0 || cfg->sandwich_p > 0 || cfg->basis_p > 0 || cfg->gauss_p > 0)
+            return -1;
+        runWalksZB(cfg, S, b);
+        int bad = 0;
+        for (int w = 0; w < S; w++) bad += b->status[w] != 0;
+        return bad;
+    }
     if (cfg->resize_p > 0) {
         if (cfg->rng == FGO_RNG_FAST) return -1;
         if (cfg->ring == FGO_RING_Z2) runWalksResize<Z2>(cfg, S, b, tape);
@@ -2143,6 +2559,32 @@ int fgo_validate(int ring, int S, int cap, const int32_t *n, const int32_t *m, c
                 for (int t = 0; t < mm; t++)
                     if (!valid[facIndex(w, c, t, cap)]) { ok = false; break; }
         }
+        valid_out[w] = ok;
+        good += ok;
+    }
+    return good;
+}
+
+int fgo_validate_zb(int S, int cap, const int32_t *n, const int32_t *m, const uint64_t *fac, const uint64_t *sgn,
+                    const uint64_t *fac2, uint8_t *valid_out) {
+    int good = 0;
+    for (int w = 0; w < S; w++) {
+        const int n0 = n[w * 3], n1 = n[w * 3 + 1], n2 = n[w * 3 + 2];
+        const int nn0 = n0 * n1, nn1 = n1 * n2, nn2 = n2 * n0, mm = m[w];
+        auto coef = [&](int c, int t, int e) {
+            const size_t q = facIndex(w, c, t, cap);
+            const int a = (fac[q] >> e) & 1 ? (((fac2[q] >> e) & 1) ? 2 : 1) : 0;
+            return ((sgn[q] >> e) & 1) ? -a : a;
+        };
+        bool ok = true;
+        for (int i = 0; i < nn0 && ok; i++)
+            for (int j = 0; j < nn1 && ok; j++)
+                for (int k = 0; k < nn2 && ok; k++) {
+                    const int target = (i % n1 == j / n2) && (i / n1 == k % n0) && (j % n2 == k / n0);
+                    int e = 0;
+                    for (int t = 0; t < mm; t++) e += coef(0, t, i) * coef(1, t, j) * coef(2, t, k);
+                    if (e != target) ok = false;
+                }
         valid_out[w] = ok;
         good += ok;
     }

@@ -28,7 +28,7 @@ extern "C" {
  * Philox stream with implicit pair enumeration (no lists: an ordered equal
  * pair is drawn uniformly in canonical order), the library's fast mode. */
 enum { FGO_RNG_TAPE = 0, FGO_RNG_PHILOX = 1, FGO_RNG_FAST = 2 };
-enum { FGO_RING_Z2 = 0, FGO_RING_ZT = 1 };
+enum { FGO_RING_Z2 = 0, FGO_RING_ZT = 1, FGO_RING_ZB = 2 /* integers, |c| <= 2 (fast mode only) */ };
 
 typedef struct {
     int32_t ring;             /* FGO_RING_* */
@@ -72,6 +72,8 @@ typedef struct {
     int32_t *status;     /* [S] 0 ok; bit 1 tape exhausted; bit 2 capped retry loop; bit 4 slot overflow */
     int64_t *accepted;   /* [S] accepted flips, accumulated (may be NULL) */
     int32_t *best_n;     /* [S][3] sizes of the best scheme (resize; may be NULL = n) */
+    uint64_t *fac2;      /* ZB only: [S][3][cap] |c| = 2 mask (fac = nonzero, sgn = negative) */
+    uint64_t *best_fac2; /* ZB only */
 } fgo_batch;
 
 /* Tape: draws for walk w are tape_draws[tape_off[w] .. tape_off[w+1]). */
@@ -101,6 +103,11 @@ int fgo_reduce_gauss(const fgo_walk_cfg *cfg, int S, fgo_batch *b, const fgo_tap
  * best_complexity[w] its complexity.  Lists are rebuilt from the factors. */
 int fgo_minimize(const fgo_walk_cfg *cfg, int S, fgo_batch *b, const fgo_tape *tape,
                  int32_t *best_complexity);
+
+/* Exact integer Brent check of ZB records (coefficient = (fac ? (fac2 ? 2 : 1) : 0),
+ * negative where sgn is set). */
+int fgo_validate_zb(int S, int cap, const int32_t *n, const int32_t *m, const uint64_t *fac, const uint64_t *sgn,
+                    const uint64_t *fac2, uint8_t *valid_out);
 
 /* Exact Brent check (scheme_z2.cu:3-29 / scheme_integer.cu:3-38) of every
  * record; valid_out[w] = 1 when it reproduces the n1 x n2 x n3 tensor. */

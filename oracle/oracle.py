@@ -15,7 +15,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 MAX_PAIRS = 500
-RING = {"z2": 0, "zt": 1}
+RING = {"z2": 0, "zt": 1, "zb": 2}
 RNG = {"tape": 0, "philox": 1, "fast": 2}
 
 
@@ -44,6 +44,7 @@ def lib():
         _lib.fgo_validate.restype = ctypes.c_int
         _lib.fgo_reduce.restype = ctypes.c_int
         _lib.fgo_reduce_gauss.restype = ctypes.c_int
+        _lib.fgo_validate_zb.restype = ctypes.c_int
     return _lib
 
 
@@ -58,7 +59,8 @@ class WalkCfg(ctypes.Structure):
 class _Batch(ctypes.Structure):
     _fields_ = [(name, ctypes.c_void_p) for name in
                 ("n", "m", "fac", "sgn", "valid", "list_size", "list_pairs", "flips", "best_rank",
-                 "best_m", "best_fac", "best_sgn", "best_valid", "rng_pos", "status", "accepted", "best_n")]
+                 "best_m", "best_fac", "best_sgn", "best_valid", "rng_pos", "status", "accepted", "best_n",
+                 "fac2", "best_fac2")]
 
 
 class _Tape(ctypes.Structure):
@@ -73,15 +75,18 @@ class WalkBatch:
     """S walk records with `cap` factor slots each (numpy, C-contiguous)."""
 
     FIELDS = ("n", "m", "fac", "sgn", "valid", "list_size", "list_pairs", "flips", "best_rank",
-              "best_m", "best_fac", "best_sgn", "best_valid", "rng_pos", "status", "accepted", "best_n")
+              "best_m", "best_fac", "best_sgn", "best_valid", "rng_pos", "status", "accepted", "best_n",
+              "fac2", "best_fac2")
 
     def __init__(self, S, cap, ring="z2"):
         self.S, self.cap, self.ring = S, cap, ring
         zt = ring == "zt"
+        zb = ring == "zb"
+        signed = zt or zb
         self.n = np.zeros((S, 3), np.int32)
         self.m = np.zeros(S, np.int32)
         self.fac = np.zeros((S, 3, cap), np.uint64)
-        self.sgn = np.zeros((S, 3, cap), np.uint64) if zt else None
+        self.sgn = np.zeros((S, 3, cap), np.uint64) if signed else None
         self.valid = np.zeros((S, 3, cap), np.uint8) if zt else None
         self.list_size = np.zeros((S, 3), np.int32)
         self.list_pairs = np.zeros((S, 3, MAX_PAIRS), np.uint32)
@@ -89,12 +94,14 @@ class WalkBatch:
         self.best_rank = np.zeros(S, np.int32)
         self.best_m = np.zeros(S, np.int32)
         self.best_fac = np.zeros((S, 3, cap), np.uint64)
-        self.best_sgn = np.zeros((S, 3, cap), np.uint64) if zt else None
+        self.best_sgn = np.zeros((S, 3, cap), np.uint64) if signed else None
         self.best_valid = np.zeros((S, 3, cap), np.uint8) if zt else None
         self.rng_pos = np.zeros(S, np.int64)
         self.status = np.zeros(S, np.int32)
         self.accepted = np.zeros(S, np.int64)
         self.best_n = np.zeros((S, 3), np.int32)
+        self.fac2 = np.zeros((S, 3, cap), np.uint64) if zb else None
+        self.best_fac2 = np.zeros((S, 3, cap), np.uint64) if zb else None
 
     def copy(self):
         b = WalkBatch.__new__(WalkBatch)
@@ -170,9 +177,24 @@ def validate(batch, best=False):
     fac = batch.best_fac if best else batch.fac
     sgn = batch.best_sgn if best else batch.sgn
     val = batch.best_valid if best else batch.valid
+    if batch.ring == "zb":
+        fac2 = batch.best_fac2 if best else batch.fac2
+        lib().fgo_validate_zb(batch.S, batch.cap, _ptr(np.ascontiguousarray(n)), _ptr(m), _ptr(fac), _ptr(sgn),
+                              _ptr(fac2), _ptr(out))
+        return out.astype(bool)
     lib().fgo_validate(RING[batch.ring], batch.S, batch.cap, _ptr(np.ascontiguousarray(n)), _ptr(m), _ptr(fac),
                        _ptr(sgn), _ptr(val), _ptr(out))
     return out.astype(bool)
+
+
+def zb_coefficients(fac, sgn, fac2):
+    """int8 coefficient arrays [..., 64] from ZB sign-magnitude masks."""
+    bits = np.arange(64, dtype=np.uint64)
+    nz = (fac[..., None] >> bits) & np.uint64(1)
+    neg = (sgn[..., None] >> bits) & np.uint64(1)
+    two = (fac2[..., None] >> bits) & np.uint64(1)
+    mag = nz.astype(np.int8) * (1 + two.astype(np.int8))
+    return np.where(neg.astype(bool), -mag, mag).astype(np.int8)
 
 
 def validate_arrays(ring, n, m, fac, sgn=None, valid=None):
