@@ -550,8 +550,9 @@ def post_arm(args):
 
 
 def zt_arm(args):
-    """Ternary search: 16,384 walks per shape of (3,3,3) and (4,4,4) from the naive schemes,
-    reference stream, exact integer verification; verified flips/s and ranks reached."""
+    """Integer-coefficient search: 16,384 walks per shape of (3,3,3) and (4,4,4) from the naive
+    schemes, exact integer verification; verified flips/s and ranks reached.  Ternary (ZT,
+    the reference's ring, reference stream) and bounded by |c| <= 2 (ZB, fast mode)."""
     import flipgraphgpu_gb300 as fg
     for shape in ((3, 3, 3), (4, 4, 4)):
         n1, n2, n3 = shape
@@ -566,6 +567,27 @@ def zt_arm(args):
         c = eng.counters()
         print(json.dumps({"workload": f"ZT {n1}x{n2}x{n3}, {args.zt_walks} walks", "verified_flips_per_s": tot_v / (tot_ms / 1000),
                           "steps": args.steps, "iterations_per_step": args.zt_iterations, "best_rank": int(c["best_rank"].min()),
+                          "walks_valid": int(c["valid"].sum())}))
+        eng.close()
+    # Integer coefficients bounded by |c| <= 2 (fast mode; flips leaving the bound are rejected).
+    for shape in ((3, 3, 3), (4, 4, 4)):
+        n1, n2, n3 = shape
+        full = n1 * n2 * n3
+        eng = fg.Engine(args.zt_walks, full + 4, "zb", "fast", args.seed, args.zb_iterations, args.zb_plus, 0.01, 0.0)
+        eng.init_naive(n1, n2, n3)
+        eng.run(1)
+        tot_v, tot_f, tot_ms = 0, 0, 0.0
+        for _ in range(args.steps):
+            st = eng.run(1)
+            tot_v += st["verified_flips"]
+            tot_f += st["flips"]
+            tot_ms += st["kernel_ms"] + st["verify_ms"]
+        c = eng.counters()
+        proposals = args.steps * args.zb_iterations * args.zt_walks
+        print(json.dumps({"workload": f"ZB (|c| <= 2) {n1}x{n2}x{n3}, {args.zt_walks} walks",
+                          "verified_flips_per_s": tot_v / (tot_ms / 1000), "accepted_fraction": tot_f / proposals,
+                          "steps": args.steps, "iterations_per_step": args.zb_iterations,
+                          "plus_iterations": args.zb_plus, "best_rank": int(c["best_rank"].min()),
                           "walks_valid": int(c["valid"].sum())}))
         eng.close()
     return 0
@@ -611,6 +633,8 @@ def main():
     ap.add_argument("--ttr-plus", type=int, default=50000)
     ap.add_argument("--zt-walks", type=int, default=16384)
     ap.add_argument("--zt-iterations", type=int, default=200)
+    ap.add_argument("--zb-iterations", type=int, default=2000)
+    ap.add_argument("--zb-plus", type=int, default=5000)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

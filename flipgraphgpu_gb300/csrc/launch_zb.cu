@@ -105,8 +105,10 @@ __device__ void zb_walk_one(const DevBatch &B, const WalkParams &P, int w, uint6
     }
 }
 
-// Walks [first, first + count), one warp each (grid-stride over walks).
-__global__ void k_walk_zb(DevBatch B, WalkParams P, int first, int count, int scap) {
+// Walks [first, first + count), one warp each (grid-stride over walks).  Six
+// 4-warp blocks per SM (80 registers) measured 7-11 % faster than the
+// unbounded build's four (118 registers), its few spills notwithstanding.
+__global__ void __launch_bounds__(128, 6) k_walk_zb(DevBatch B, WalkParams P, int first, int count, int scap) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int wpb = blockDim.x >> 5, warp = threadIdx.x >> 5;
     uint64_t *base = reinterpret_cast<uint64_t *>(smem) + (size_t)warp * zb_words(scap);

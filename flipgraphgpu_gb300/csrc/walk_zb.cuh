@@ -192,20 +192,29 @@ struct ZBWalk {
         __syncwarp();
     }
 
-    // Term t shares two factors with term a up to sign, third merged within bounds.
-    __device__ bool mergeable(int a, int t, int &rr, Vec3 &merged) const {
-        int e[3];
+    // Term a's factors and their negations, for the merge tests against it.
+    struct Term {
+        Vec3 f[3], nf[3];
+    };
+    __device__ Term term(int a) const {
+        Term T;
         for (int c = 0; c < 3; c++) {
-            const Vec3 A = get(c, a);
-            e[c] = v3rel(get(c, t), A, v3neg(A, Lc[c]));
+            T.f[c] = get(c, a);
+            T.nf[c] = v3neg(T.f[c], Lc[c]);
         }
+        return T;
+    }
+    // Term t shares two factors with term A up to sign, third merged within bounds.
+    __device__ bool mergeable(const Term &A, int t, int &rr, Vec3 &merged) const {
+        int e[3];
+        for (int c = 0; c < 3; c++) e[c] = v3rel(get(c, t), A.f[c], A.nf[c]);
+        if ((e[0] != 0) + (e[1] != 0) + (e[2] != 0) < 2) return false;
         const int p0s[3] = {0, 0, 1}, p1s[3] = {1, 2, 2};
         for (int q = 0; q < 3; q++) {
             const int p0 = p0s[q], p1 = p1s[q];
             if (!e[p0] || !e[p1]) continue;
             const int k = 3 - p0 - p1;
-            const Vec3 A = get(k, a);
-            if (v3add(get(k, t), e[p0] * e[p1] > 0 ? A : v3neg(A, Lc[k]), merged)) {
+            if (v3add(get(k, t), e[p0] * e[p1] > 0 ? A.f[k] : A.nf[k], merged)) {
                 rr = k;
                 return true;
             }
@@ -226,41 +235,47 @@ struct ZBWalk {
     }
     // First term t != a (ascending) that absorbs a.
     __device__ bool reduceWith(int a) {
+        const Term A = term(a);
         for (int q = 0; q < nslot; q++) {
             const int t = 32 * q + lane_id();
             int rr = 0;
             Vec3 mg;
-            const bool ok = t < m && t != a && mergeable(a, t, rr, mg);
+            const bool ok = t < m && t != a && mergeable(A, t, rr, mg);
             const unsigned bm = __ballot_sync(kFull, ok);
             if (bm) {
                 const int src = __ffs(bm) - 1;
-                const int tt = 32 * q + src;
-                Vec3 merged;
-                int rc = 0;
-                mergeable(a, tt, rc, merged);  // every lane, same result
-                merge(tt, a, rc, merged);
+                const int rc = __shfl_sync(kFull, rr, src);
+                const Vec3 merged{__shfl_sync(kFull, mg.b0, src), __shfl_sync(kFull, mg.b1, src),
+                                  __shfl_sync(kFull, mg.b2, src)};
+                merge(32 * q + src, a, rc, merged);
                 return true;
             }
         }
         return false;
     }
     __device__ bool tryReduce() {  // first pair (a < b), b absorbed by a
-        for (int a = 0; a < m; a++)
+        for (int a = 0; a < m; a++) {
             for (int q = (a + 1) / 32; q < nslot; q++) {
                 const int b = 32 * q + lane_id();
                 int rr = 0;
                 Vec3 mg;
-                const bool ok = b > a && b < m && mergeable(b, a, rr, mg);
+                // b absorbed by a: merged = x_r[a] + e x_r[b], the relation being symmetric
+                bool ok = false;
+                if (b > a && b < m) {
+                    const Term B = term(b);
+                    ok = mergeable(B, a, rr, mg);
+                }
                 const unsigned bm = __ballot_sync(kFull, ok);
                 if (bm) {
-                    const int bb = 32 * q + __ffs(bm) - 1;
-                    Vec3 merged;
-                    int rc = 0;
-                    mergeable(bb, a, rc, merged);
-                    merge(a, bb, rc, merged);
+                    const int src = __ffs(bm) - 1;
+                    const int rc = __shfl_sync(kFull, rr, src);
+                    const Vec3 merged{__shfl_sync(kFull, mg.b0, src), __shfl_sync(kFull, mg.b1, src),
+                                      __shfl_sync(kFull, mg.b2, src)};
+                    merge(a, 32 * q + src, rc, merged);
                     return true;
                 }
             }
+        }
         return false;
     }
 

@@ -14,6 +14,8 @@ from . import Engine
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--shape", default="3x3x3")
+    ap.add_argument("--ring", default="z2", choices=["z2", "zt", "zb"],
+                    help="zb (integers, |c| <= 2) runs in the fast mode only")
     ap.add_argument("--walks", type=int, default=1024)
     ap.add_argument("--iterations", type=int, default=1000)
     ap.add_argument("--plus-iterations", type=int, default=100000)
@@ -28,7 +30,8 @@ def main():
                     help="fast mode: one thread per walk up to this many slots, one warp per walk above")
     a = ap.parse_args()
     n = tuple(int(x) for x in a.shape.split("x"))
-    with Engine(a.walks, n[0] * n[1] * n[2], "z2", a.mode, a.seed, a.iterations, a.plus_iterations) as eng:
+    cap = n[0] * n[1] * n[2] + (4 if a.ring == "zb" else 0)
+    with Engine(a.walks, cap, a.ring, a.mode, a.seed, a.iterations, a.plus_iterations) as eng:
         if a.fast_split is not None:
             eng.set_fast_split(a.fast_split)
         if a.fast_kernel is not None:
@@ -44,7 +47,7 @@ def main():
         if net is not None:
             eng.set_proposal(None, candidates=1)
             net.close()
-    print(json.dumps({"shape": a.shape, "walks": a.walks, "iterations": a.iterations, "mode": a.mode,
+    print(json.dumps({"shape": a.shape, "ring": a.ring, "walks": a.walks, "iterations": a.iterations, "mode": a.mode,
                       "fast_split": a.fast_split, "fast_kernel": a.fast_kernel, "lanes": a.lanes, **st}))
 
 
