@@ -11,6 +11,8 @@
 //   --time-budget S       stop after S seconds (0: off)
 //   --gauss-probability P Gauss (XOR) reduction per step with probability P / max iterations (Z2, list
 //                         modes; the reference defines SchemeZ2::tryReduceGauss but never calls it)
+//   --ternary-sandwiching 1  ZT: the sandwiching move conjugates by random signed permutations
+//                         (the reference's ternary sandwiching is empty)
 // Resize meta-operators (--resize-probability, default 0.2), sandwiching and
 // basis-change moves run on both rings in the reference and philox modes; in
 // the fast mode a positive probability is reported and treated as 0.
@@ -39,6 +41,7 @@ struct Options {
     int n1, n2, n3, schemes, maxIterations, plusIterations, logPeriod, seed;
     std::string path, inputPath, ring, mode;
     double expand, reduce, sandwiching, basis, resize, gauss, timeBudget;
+    bool ternarySandwiching;
     long maxLaunches;
     int targetRank;
 };
@@ -168,6 +171,7 @@ private:
         c.sandwich_p = resizeHere(o_) ? o_.sandwiching : 0.0;
         c.basis_p = resizeHere(o_) ? o_.basis : 0.0;
         c.gauss_p = resizeHere(o_) && !zt_ ? o_.gauss : 0.0;
+        c.zt_sandwich = o_.ternarySandwiching ? 1 : 0;
         check(fg_create(&c, &h_), "fg_create");
     }
 
@@ -374,6 +378,8 @@ int main(int argc, char *argv[]) {
     parser.add("--mode", ArgType::String, "MODE", "reference (bit-exact stream) | fast | philox", "reference");
     parser.add("--gauss-probability", ArgType::Real, "REAL",
                "Gauss (XOR) reduction probability (divided by max iterations; Z2, list modes)", "0.0");
+    parser.add("--ternary-sandwiching", ArgType::Natural, "0|1",
+               "ZT: sandwiching conjugates by random signed permutations (the reference's move is empty)", "0");
     parser.add("--max-launches", ArgType::Natural, "INT", "stop after this many launches (0: never)", "0");
     parser.add("--target-rank", ArgType::Natural, "INT", "stop when a best rank reaches this (0: off)", "0");
     parser.add("--time-budget", ArgType::Real, "REAL", "stop after this many seconds (0: off)", "0");
@@ -396,6 +402,7 @@ int main(int argc, char *argv[]) {
     o.basis = std::stod(parser.get("--basis-probability"));
     o.resize = std::stod(parser.get("--resize-probability"));
     o.gauss = std::stod(parser.get("--gauss-probability"));
+    o.ternarySandwiching = parser.get("--ternary-sandwiching") == "1";
     o.ring = parser.get("--ring");
     o.mode = parser.get("--mode");
     o.maxLaunches = std::stol(parser.get("--max-launches"));

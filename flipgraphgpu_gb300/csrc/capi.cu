@@ -254,6 +254,7 @@ void compute_params(fg_handle *h) {
     P.gauss_on = c.gauss_p > 0 ? 1 : 0;
     P.gauss_gate_f = ceil_to_float(c.gauss_p);
     P.gauss_T = thr(c.gauss_p);
+    P.zt_sandwich = c.zt_sandwich;
     P.key0 = (uint32_t)c.seed;
     P.key1 = (uint32_t)(c.seed >> 32);
     P.random_iterations = c.resize_p > 0 ? 1 : 0;

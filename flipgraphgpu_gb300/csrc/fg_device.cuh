@@ -62,6 +62,7 @@ struct WalkParams {
     int gauss_on;
     float gauss_gate_f;
     uint64_t gauss_T;
+    int zt_sandwich;  // ZT: sandwiching by signed permutations (the reference's move is empty)
     uint32_t key0, key1;  // Philox key (seed)
     int random_iterations;  // resizing on: each launch runs randint(1, iterations) steps (flip_graph.cu:531)
 };

@@ -88,9 +88,55 @@ __device__ __forceinline__ uint64_t conj_gf2(uint64_t x, const uint32_t *left, c
     return out;
 }
 
-// The reference's ternary sandwiching is empty: only its gate draw is taken.
+// The reference's ternary sandwiching is empty (only its gate draw is taken).
+// Opt-in (WalkParams::zt_sandwich, no reference counterpart): conjugation by
+// random signed permutation matrices, which keeps every coefficient in
+// {-1, 0, 1}; entry (i, j) of u X v^-1 is sign_u(i) sign_v(j) X(p_u(i), p_v(j)).
+template <class R>
+__device__ void signed_permutation(int n, int *p, uint32_t &signs, R &r) {
+    for (int i = 0; i < n; i++) p[i] = i;
+    for (int i = n - 1; i > 0; i--) {  // randomPermutation, random.cuh:9-22
+        const int j = (int)r.below((uint32_t)(i + 1));
+        const int t = p[i]; p[i] = p[j]; p[j] = t;
+    }
+    signs = r.raw() & (n >= 32 ? 0xFFFFFFFFu : ((1u << n) - 1u));
+}
+
+__device__ __forceinline__ void conj_signed(uint64_t xv, uint64_t xs, const int *pl, uint32_t sl, const int *pr,
+                                            uint32_t sr, int n1, int n2, uint64_t &v, uint64_t &sg) {
+    v = 0;
+    sg = 0;
+    for (int i = 0; i < n1; i++)
+        for (int j = 0; j < n2; j++) {
+            const int src = pl[i] * n2 + pr[j], dst = i * n2 + j;
+            if (!((xv >> src) & 1)) continue;
+            v |= 1ull << dst;
+            if ((((xs >> src) & 1) ^ ((sl >> i) & 1) ^ ((sr >> j) & 1)) != 0) sg |= 1ull << dst;
+        }
+}
+
 template <class R, int S>
-__device__ __noinline__ void sandwich_move(ZTWalk<R, S> &) {}
+__device__ __noinline__ void sandwich_move(ZTWalk<R, S> &z) {
+    if (!z.r.P->zt_sandwich || z.n0 > 16 || z.n1 > 16 || z.n2 > 16) return;
+    int pu[16], pv[16], pw[16];
+    uint32_t su, sv, sw;
+    signed_permutation(z.n0, pu, su, z.r);
+    signed_permutation(z.n1, pv, sv, z.r);
+    signed_permutation(z.n2, pw, sw, z.r);
+    __syncwarp();
+    for (int t = lane_id(); t < z.m; t += 32) {
+        uint64_t v, sg;
+        conj_signed(z.xv[t], z.xs[t], pu, su, pv, sv, z.n0, z.n1, v, sg);
+        z.xv[t] = v; z.xs[t] = sg; z.xo[t] = 1;
+        conj_signed(z.xv[z.cap + t], z.xs[z.cap + t], pv, sv, pw, sw, z.n1, z.n2, v, sg);
+        z.xv[z.cap + t] = v; z.xs[z.cap + t] = sg; z.xo[z.cap + t] = 1;
+        conj_signed(z.xv[2 * z.cap + t], z.xs[2 * z.cap + t], pw, sw, pu, su, z.n2, z.n0, v, sg);
+        z.xv[2 * z.cap + t] = v; z.xs[2 * z.cap + t] = sg; z.xo[2 * z.cap + t] = 1;
+    }
+    __syncwarp();
+    z.fixSigns();
+    z.rebuild();
+}
 
 template <class R, int S>
 __device__ __noinline__ void sandwich_move(Z2Walk<R, S> &z) {

@@ -83,6 +83,9 @@ typedef struct {
                                  Gauss (XOR) reduction SchemeZ2::tryReduceGauss (scheme_z2.cu:312-442,
                                  1156-1163), which the reference defines but its walk never calls;
                                  0 (default) takes no draw, keeping the reference's trajectories */
+    int32_t zt_sandwich;      /* ZT: 1 = the sandwiching move conjugates by random signed permutation
+                                 matrices (coefficients stay in {-1, 0, 1}); 0 (default) = the
+                                 reference's empty ternary move (scheme_integer.cu:1215-1217) */
 } fg_config;
 
 /* Host-side walk records, structure of arrays over `walks` records with

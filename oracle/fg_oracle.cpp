@@ -44,6 +44,9 @@ constexpr int kMaxMatrix = 64;      // config.cuh:11 (64-bit factors)
 constexpr int kMaxExtensionN = 16;  // config.cuh:37
 enum { ST_TAPE = 1, ST_RETRY = 2, ST_OVERFLOW = 4 };
 
+// Ternary sandwiching on (fgo_walk_cfg::zt_sandwich): set for the duration of one fgo_walk call.
+int g_ternarySandwich = 0;
+
 inline int popc64(uint64_t x) { return __builtin_popcountll(x); }
 
 // ------------------------------------------------------------ Philox4x32-10
@@ -1180,7 +1183,41 @@ struct ZT {
 
     // ---------------------------------------------------------------- basis moves
     template <class R> bool tryReduceGauss(R &, bool) { return false; }  // Z2 only in the reference
-    template <class R> void sandwiching(R &) {}  // scheme_integer.cu:1215-1217: empty in the reference
+    // scheme_integer.cu:1215-1217 leaves the ternary move empty (only its gate draw is taken).
+    // Opt-in (zt_sandwich, no reference counterpart): conjugation by random signed permutation
+    // matrices, the integer matrices whose conjugation keeps every coefficient in {-1, 0, 1}:
+    // U' = u U v^-1, V' = v V w^-1, W' = w W u^-1 as the Z2 move, entry (i, j) of the result =
+    // sign_l(i) sign_r(j) X(p_l(i), p_r(j)); then signs are canonicalised and the lists rebuilt.
+    template <class R> void signedPermutation(int n_, int *p, uint32_t &signs, R &r) {
+        permutation(p, n_, r);
+        signs = r.raw() & (n_ >= 32 ? 0xFFFFFFFFu : ((1u << n_) - 1u));
+    }
+    static Tern conjSigned(const Tern &x, const int *pl, uint32_t sl, const int *pr, uint32_t sr, int n1, int n2) {
+        uint64_t v = 0, sg = 0;
+        for (int i = 0; i < n1; i++)
+            for (int j = 0; j < n2; j++) {
+                const int src = pl[i] * n2 + pr[j], dst = i * n2 + j;
+                if (!((x.v >> src) & 1)) continue;
+                v |= 1ull << dst;
+                if ((((x.s >> src) & 1) ^ ((sl >> i) & 1) ^ ((sr >> j) & 1)) != 0) sg |= 1ull << dst;
+            }
+        return mk(v, sg);
+    }
+    template <class R> void sandwiching(R &r) {
+        if (!g_ternarySandwich || n[0] > 16 || n[1] > 16 || n[2] > 16) return;
+        int pu[16], pv[16], pw[16];
+        uint32_t su, sv, sw;
+        signedPermutation(n[0], pu, su, r);
+        signedPermutation(n[1], pv, sv, r);
+        signedPermutation(n[2], pw, sw, r);
+        for (int t = 0; t < m; t++) {
+            x[0][t] = conjSigned(x[0][t], pu, su, pv, sv, n[0], n[1]);
+            x[1][t] = conjSigned(x[1][t], pv, sv, pw, sw, n[1], n[2]);
+            x[2][t] = conjSigned(x[2][t], pw, sw, pu, su, n[2], n[0]);
+        }
+        fixSigns();
+        rebuildLists();
+    }
     void swapBasisRows(int i1, int i2) {  // scheme_integer.cu:791-815
         int rows[64];
         for (int q = 0; q < n[0]; q++) rows[q] = q;
@@ -2460,6 +2497,10 @@ int fgo_init_naive(const fgo_walk_cfg *cfg, int S, int n1, int n2, int n3, fgo_b
 }
 
 int fgo_walk(const fgo_walk_cfg *cfg, int S, fgo_batch *b, const fgo_tape *tape) {
+    struct Flag {
+        explicit Flag(int on) { g_ternarySandwich = on; }
+        ~Flag() { g_ternarySandwich = 0; }
+    } flag(cfg->zt_sandwich);
     if (cfg->ring == FGO_RING_ZB) {
         if (cfg->rng != FGO_RNG_FAST || cfg->resize_p > 0 || cfg->sandwich_p > 0 || cfg->basis_p > 0 || cfg->gauss_p > 0)
             return -1;

@@ -47,6 +47,8 @@ typedef struct {
     double basis_p;           /* --basis-probability */
     double gauss_p;           /* Gauss (XOR) reduction per step, gauss_p / iterations (Z2; not in the
                                  reference's walk, whose tryReduceGauss is never called) */
+    int32_t zt_sandwich;      /* ZT: 1 = sandwiching by random signed permutations (the reference's
+                                 ternary sandwiching is empty); 0 = as the reference */
 } fgo_walk_cfg;
 
 /* Structure-of-arrays batch of S walk records.  Factor arrays are [S][3][cap];

@@ -348,3 +348,32 @@ def test_gauss_reduction_vs_oracle(mode, shape):
         O.walk(b, b.cfg("philox", launches=2, **kw))
     compare_records(rec, b, f"gauss {mode} {shape}")
     assert (rec.m < m0).mean() > 0.5
+
+
+@pytest.mark.parametrize("mode,shape,resize_p", [("reference", (3, 3, 3), 0.0), ("philox", (2, 3, 3), 0.0),
+                                                 ("reference", (2, 2, 3), 0.6)])
+def test_ternary_sandwiching_vs_oracle(mode, shape, resize_p):
+    """Opt-in ternary sandwiching (signed permutations; the reference's move is empty) against
+    the oracle, with the basis changes on: every field after the launches, schemes exact."""
+    n1, n2, n3 = shape
+    S, iters, plus, launches = 16, 80, 40, 3
+    seed = 800 + n1 + n2 + n3
+    cap = 352 if resize_p > 0 else n1 * n2 * n3
+    kw = dict(resize_p=resize_p, sandwich_p=20.0, basis_p=10.0)
+    with fg.Engine(S, cap, "zt", mode, seed, iters, plus, 0.01, 0.0, zt_sandwich=True, **kw) as eng:
+        eng.init_naive(n1, n2, n3)
+        rec0 = eng.records()
+        eng.run(launches)
+        rec = eng.records()
+        assert eng.validate().all() and eng.validate(best=True).all()
+    b = batch_from(rec0)
+    b.best_n[:] = rec0.n
+    cfg = dict(iterations=iters, plus_iterations=plus, expand_p=0.01, reduce_p=0.0, seed=seed, zt_sandwich=1, **kw)
+    if mode == "reference":
+        used = int(rec.rng_pos.max())
+        draws, unis = fg.xorwow_tape(seed, 0, S, used)
+        tape = O.make_tape([(draws[w, :rec.rng_pos[w]], unis[w, :rec.rng_pos[w]]) for w in range(S)])
+        O.walk(b, b.cfg("tape", launches=launches, **cfg), tape)
+    else:
+        O.walk(b, b.cfg("philox", launches=launches, **cfg))
+    compare_records(rec, b, f"ternary sandwiching {mode} {shape}")
