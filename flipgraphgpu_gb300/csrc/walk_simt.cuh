@@ -184,11 +184,10 @@ struct SimtZ2 {
         A(k, b) = newB;
         const W xia = F(i, a), xka = wka & FM, xib = F(i, b), xjb = wjb & FM;
         int cntA = 0, cntB = 0, red = -1, part = 0;
-        // Branch-free count update over all terms; the rare new-partner terms are
-        // collected in bit masks and checked for reductions afterwards in order.
+        // One pass: count updates over all terms, and at the (rare) new partners the
+        // reduction test; the first term (ascending) that triggers one wins, its
+        // j-part tested before its k-part.  Factor bits do not change in the pass.
         W *pj = &A(j, 0), *pk = &A(k, 0);
-        uint64_t newJ = 0, newK = 0;  // terms t < 64 that became partners
-        bool overflow = false;        // a partner beyond term 63: fall back to an exact rescan
 #pragma unroll 4
         for (int t = 0; t < m; t++) {
             const W wj = pj[(size_t)t << sh()], wk = pk[(size_t)t << sh()];
@@ -199,20 +198,10 @@ struct SimtZ2 {
             cntB += nk;
             if (oj | nj) pj[(size_t)t << sh()] = wj + (nj ? ONE : (W)0) - (oj ? ONE : (W)0);
             if (ok | nk) pk[(size_t)t << sh()] = wk + (nk ? ONE : (W)0) - (ok ? ONE : (W)0);
-            const uint64_t bit = t < 64 ? (1ull << t) : 0ull;
-            newJ |= nj ? bit : 0ull;
-            newK |= nk ? bit : 0ull;
-            overflow |= (nj | nk) & (t >= 64);
-        }
-        if (checkReduce && (newJ | newK | (uint64_t)overflow)) {
-            // First term (ascending) whose j-part or k-part triggers a reduction.
-            for (int t = 0; t < m; t++) {
-                const bool inJ = t < 64 ? ((newJ >> t) & 1) : (F(j, t) == newA && t != a);
-                const bool inK = t < 64 ? ((newK >> t) & 1) : (F(k, t) == newB && t != b);
-                if (!inJ && !inK) continue;
+            if (checkReduce && (nj | nk) && red < 0) {
                 const W vi = F(i, t);
-                if (inJ && (vi == xia || F(k, t) == xka)) { red = t; part = 0; break; }
-                if (inK && (vi == xib || F(j, t) == xjb)) { red = t; part = 1; break; }
+                if (nj && (vi == xia || vk == xka)) { red = t; part = 0; }
+                else if (nk && (vi == xib || vj == xjb)) { red = t; part = 1; }
             }
         }
         A(j, a) = newA | ((W)cntA << HS);
