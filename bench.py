@@ -173,14 +173,16 @@ def cpu_walks(walks_per_shape, iterations, plus, seed, threads):
 def cpu_baseline(args, seconds_target=15.0):
     threads = os.cpu_count() or 1
     wps = max(threads, 16)
+    cpu_walks(wps, 10, 100000, 6, threads)  # loads the oracle library outside the timed samples
+    # Grow the sample until it is about seconds_target of CPU work (at least a third of it).
     iters = 200
-    v, dt, nw = cpu_walks(wps, iters, 100000, 7, threads)
-    # Scale the sample to roughly seconds_target of CPU work.
-    scale = max(1.0, seconds_target / max(dt, 1e-3))
-    iters2 = int(iters * scale)
-    v, dt, nw = cpu_walks(wps, iters2, 100000, 8, threads)
+    while True:
+        v, dt, nw = cpu_walks(wps, iters, 100000, 8, threads)
+        if dt >= seconds_target / 3 or iters >= 10_000_000:
+            break
+        iters = int(iters * min(50.0, max(2.0, seconds_target / max(dt, 1e-3))))
     return {"value": v / dt, "unit": METRIC, "cores": threads, "kind": "port",
-            "sample": f"{nw} walks ({wps} per shape) x {iters2} steps of the oracle's fast-stream walk, "
+            "sample": f"{nw} walks ({wps} per shape) x {iters} steps of the oracle's fast-stream walk, "
                       f"{threads} host threads, {dt:.1f} s"}
 
 
@@ -300,10 +302,13 @@ def gpu_arm(args):
 
     smem_peak, peaks, sms, mhz = smem_peak_gbs()
     achieved = algo_bytes / (kern_ms / 1000.0) / 1e9
-    traffic = None
+    traffic, issue = None, None
     try:
         with open(os.path.join(ROOT, "profiles", "bench_traffic.json")) as f:
-            traffic = json.load(f)["dram_bytes_per_step"]
+            prof = json.load(f)
+        traffic = prof["dram_bytes_per_step"]
+        issue = {"bound": "issue", "frac": prof["issue_active_pct"] / 100.0, "kernel": prof["issue_kernel"],
+                 "source": prof["issue_source"]}
     except (OSError, KeyError, ValueError):
         pass
     if rank == 0:
@@ -325,7 +330,8 @@ def gpu_arm(args):
                          "frac": achieved / smem_peak, "traffic": traffic,
                          "traffic_note": "DRAM bytes of one step's walk launches (ncu capture, profiles/bench_launch_list.md)",
                          "peak_source": f"derived: 128 B/clk/SM x {sms} SMs x {mhz:.0f} MHz (sm_max_mhz, MEASURED_PEAKS.json)",
-                         "algorithmic_bytes": f"per accepted flip (2m+4) x {WORD_BYTES[args.mode]} B of shared-memory traffic"},
+                         "algorithmic_bytes": f"per accepted flip (2m+4) x {WORD_BYTES[args.mode]} B of shared-memory traffic",
+                         "binding": issue},
             "clocks": clk,
             "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "steps": args.e2e_steps},
