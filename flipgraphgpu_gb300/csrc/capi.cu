@@ -407,7 +407,7 @@ fg_status launch_walks(fg_handle *h) {
         if (kind == FG_FAST_THREAD) return launch_walk_simt(h->B, h->P, g.first, g.count, g.scap, g.wide, wpb, h->sms, st);
         if (kind == FG_FAST_GROUP)
             return launch_walk_group(h->B, h->P, g.first, g.count, g.scap, g.wide, h->groupLanes, h->sms, st);
-        return launch_walk_warpfast(h->B, h->P, g.first, g.count, g.scap, g.wide, h->sms, st);
+        return launch_walk_group(h->B, h->P, g.first, g.count, g.scap, g.wide, 32, h->sms, st);  // one warp per walk
     };
     if (h->segs.size() == 1) {
         FG_CUDA(launch(h->segs[0], h->stream));
@@ -645,8 +645,8 @@ fg_status fg_rebuild_lists(fg_handle *h) {
 }
 
 fg_status fg_set_fast_kernel(fg_handle *h, int kernel, int lanes) {
-    if (!h || kernel < -1 || kernel > FG_FAST_WARP || !(lanes == 0 || lanes == 4 || lanes == 8 || lanes == 16))
-        return fail(FG_ERR_ARG, "kernel in -1..2, lanes 0, 4, 8 or 16");
+    if (!h || kernel < -1 || kernel > FG_FAST_WARP || !(lanes == 0 || lanes == 4 || lanes == 8 || lanes == 16 || lanes == 32))
+        return fail(FG_ERR_ARG, "kernel in -1..2, lanes 0, 4, 8, 16 or 32");
     h->fastKernel = kernel;
     h->groupLanes = lanes;
     return FG_OK;

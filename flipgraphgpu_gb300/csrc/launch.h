@@ -31,13 +31,10 @@ cudaError_t launch_walk_simt(const DevBatch &B, const WalkParams &P, int first, 
 cudaError_t launch_resize(int ring, const DevBatch &B, const WalkParams &P, int rng, double p, int wpb, int grid,
                           cudaStream_t s);
 cudaError_t launch_copy_best(const DevBatch &B, const int32_t *walks, int count, const int32_t *bestRank, cudaStream_t s);
-// Fast mode, `lanes` (4, 8 or 16; 0 = by slot count) lanes per walk (same semantics as launch_walk_simt).
+// Fast mode, `lanes` (4, 8, 16 or 32; 0 = by slot count) lanes per walk (same semantics as
+// launch_walk_simt); 32 lanes is the one-warp-per-walk kernel.
 cudaError_t launch_walk_group(const DevBatch &B, const WalkParams &P, int first, int count, int scap, int wide,
                               int lanes, int sms, cudaStream_t s);
-// Fast mode, one warp per walk (same semantics as launch_walk_simt); scap = slots per walk.
-cudaError_t launch_walk_warpfast(const DevBatch &B, const WalkParams &P, int first, int count, int scap, int wide,
-                                 int sms, cudaStream_t s);
-
 // Bounded-integer (ZB, |c| <= 2) fast-mode walk, one warp per walk, and its exact integer check.
 cudaError_t launch_walk_zb(const DevBatch &B, const WalkParams &P, int first, int count, int scap, int sms,
                            cudaStream_t s);

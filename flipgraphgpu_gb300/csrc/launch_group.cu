@@ -90,7 +90,7 @@ __global__ void k_walk_group(DevBatch B, WalkParams P, int first, int count, int
     constexpr int GPW = 32 / G;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, wpb = blockDim.x >> 5;
     const int gi = lane / G, g = lane % G, gbase = gi * G;
-    const unsigned mask = ((1u << G) - 1u) << gbase;
+    const unsigned mask = group_bits<G>() << gbase;
     W *base = reinterpret_cast<W *>(smem) + (size_t)(warp * GPW + gi) * ws;
     for (int q0 = (blockIdx.x * wpb + warp) * GPW; q0 < count; q0 += gridDim.x * wpb * GPW) {
         const int q = q0 + gi;
@@ -137,6 +137,13 @@ cudaError_t group_w(const DevBatch &B, const WalkParams &P, int first, int count
     if (lanes == 16) {
         if (scap <= 256) return group_t<W, 16, 16>(B, P, first, count, scap, sms, s);
         if (scap <= 352) return group_t<W, 16, 22>(B, P, first, count, scap, sms, s);
+        return cudaErrorInvalidValue;
+    }
+    if (lanes == 32) {  // one walk per warp, terms slot-major (conflict-free)
+        if (scap <= 32) return group_t<W, 32, 1>(B, P, first, count, scap, sms, s);
+        if (scap <= 64) return group_t<W, 32, 2>(B, P, first, count, scap, sms, s);
+        if (scap <= 128) return group_t<W, 32, 4>(B, P, first, count, scap, sms, s);
+        if (scap <= 352) return group_t<W, 32, 11>(B, P, first, count, scap, sms, s);
         return cudaErrorInvalidValue;
     }
     return cudaErrorInvalidValue;

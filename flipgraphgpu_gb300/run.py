@@ -25,7 +25,7 @@ def main():
                     help="learned mode: candidates per step, scored by a freshly initialised network when > 1")
     ap.add_argument("--seed", type=int, default=3)
     ap.add_argument("--fast-kernel", default=None, choices=["auto", "thread", "group", "warp"])
-    ap.add_argument("--lanes", type=int, default=0, help="group kernel: lanes per walk (4, 8, 16; 0 = auto)")
+    ap.add_argument("--lanes", type=int, default=0, help="group kernel: lanes per walk (4, 8, 16, 32; 0 = auto)")
     ap.add_argument("--fast-split", type=int, default=None,
                     help="fast mode: one thread per walk up to this many slots, one warp per walk above")
     a = ap.parse_args()

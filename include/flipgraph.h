@@ -230,7 +230,7 @@ fg_status fg_set_best_ranks(fg_handle *h, const int32_t *ranks);
 fg_status fg_rebuild_lists(fg_handle *h);
 
 /* Fast mode kernel for every segment, overriding the automatic choice:
- * FG_FAST_THREAD (one thread per walk), FG_FAST_GROUP (`lanes` = 4, 8 or 16
+ * FG_FAST_THREAD (one thread per walk), FG_FAST_GROUP (`lanes` = 4, 8, 16 or 32
  * lanes per walk; 0 = by slot count, widened when the slots need it),
  * FG_FAST_WARP (one warp per walk); -1 restores the automatic choice.  All
  * three give identical results. */
