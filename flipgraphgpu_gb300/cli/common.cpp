@@ -197,6 +197,7 @@ void HostScheme::resize() {
         v[c].assign(kMaxRank, 0);
         s[c].assign(kMaxRank, 0);
         ok[c].assign(kMaxRank, 1);
+        t2[c].assign(kMaxRank, 0);
     }
 }
 
@@ -362,6 +363,7 @@ bool HostScheme::tryReduce() {
 
 int HostScheme::coefficient(int c, int t, int entry) const {
     int x = (int)((v[c][t] >> entry) & 1);
+    if (zb && ((t2[c][t] >> entry) & 1)) x *= 2;
     return ((s[c][t] >> entry) & 1) ? -x : x;
 }
 
@@ -398,7 +400,7 @@ void HostScheme::saveJson(const std::string &path) const {
     f << "{" << std::endl;
     f << "    \"n\": [" << n[0] << ", " << n[1] << ", " << n[2] << "]," << std::endl;
     f << "    \"m\": " << m << "," << std::endl;
-    f << "    \"z2\": " << (zt ? "false" : "true") << "," << std::endl;
+    f << "    \"z2\": " << (zt || zb ? "false" : "true") << "," << std::endl;
     f << "    \"complexity\": " << complexity() << "," << std::endl;
     const char *names[3] = {"u", "v", "w"};
     for (int c = 0; c < 3; c++) {
@@ -407,7 +409,7 @@ void HostScheme::saveJson(const std::string &path) const {
             f << "        [";
             for (int e = 0; e < nn[c]; e++) {
                 if (e > 0) f << ", ";
-                f << (zt ? coefficient(c, t, e) : (int)((v[c][t] >> e) & 1));
+                f << (zt || zb ? coefficient(c, t, e) : (int)((v[c][t] >> e) & 1));
             }
             f << "]" << (t < m - 1 ? "," : "") << std::endl;
         }
@@ -472,6 +474,25 @@ HostScheme fetchScheme(fg_handle *hd, int w, int cap, bool zt, bool best) {
             h.v[c][t] = fv[(size_t)c * cap + t];
             h.s[c][t] = zt ? fs[(size_t)c * cap + t] : 0;
             h.ok[c][t] = zt ? fk[(size_t)c * cap + t] : 1;
+        }
+    return h;
+}
+
+HostScheme fetchSchemeZB(fg_handle *hd, int w, int cap, bool best) {
+    HostScheme h;
+    h.zt = false;
+    h.zb = true;
+    h.resize();
+    std::vector<uint64_t> fv(3 * (size_t)cap), fs(3 * (size_t)cap), f2(3 * (size_t)cap);
+    int m = 0;
+    check(fg_get_scheme_zb(hd, w, best, h.n, &m, fv.data(), fs.data(), f2.data()), "fg_get_scheme_zb");
+    for (int c = 0; c < 3; c++) h.nn[c] = h.n[c] * h.n[(c + 1) % 3];
+    h.m = m;
+    for (int c = 0; c < 3; c++)
+        for (int t = 0; t < m; t++) {
+            h.v[c][t] = fv[(size_t)c * cap + t];
+            h.s[c][t] = fs[(size_t)c * cap + t];
+            h.t2[c][t] = f2[(size_t)c * cap + t];
         }
     return h;
 }

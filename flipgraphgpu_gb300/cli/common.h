@@ -55,9 +55,11 @@ const std::unordered_map<std::string, int> &knownRanks(bool zt);
 // bitmasks in v; ZT factors are (v, s, ok) as the reference's Addition.
 struct HostScheme {
     bool zt = true;
+    bool zb = false;  // integers with |c| <= 2: t2 marks the entries of magnitude 2 (v nonzero, s negative)
     int n[3] = {0, 0, 0}, nn[3] = {0, 0, 0}, m = 0;
     std::vector<uint64_t> v[3], s[3];
     std::vector<uint8_t> ok[3];
+    std::vector<uint64_t> t2[3];
     std::vector<uint32_t> lists[3];
 
     // "n1 n2 n3 m" followed by the U, V, W rows (scheme_z2.cu:72-96, scheme_integer.cu:81-107).
@@ -88,6 +90,8 @@ void toRecords(const HostScheme &src, fg_records &rec, int w, int cap, bool with
 HostScheme fromRecords(const fg_records &rec, int w, int cap, bool zt, bool best);
 // One walk's scheme straight from the library.
 HostScheme fetchScheme(fg_handle *h, int w, int cap, bool zt, bool best);
+// One ZB walk's scheme (integers with |c| <= 2).
+HostScheme fetchSchemeZB(fg_handle *h, int w, int cap, bool best);
 
 std::string ringName(bool zt);
 bool check(fg_status st, const char *what);

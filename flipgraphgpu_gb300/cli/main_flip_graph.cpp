@@ -4,7 +4,8 @@
 // walks run in libflipgraph (include/flipgraph.h).
 //
 // Additive flags (defaults reproduce the reference's behaviour):
-//   --ring ZT|Z2          the reference picks the ring at compile time (ZT by default)
+//   --ring ZT|Z2|ZB       the reference picks the ring at compile time (ZT by default); ZB
+//                         (integers with |c| <= 2, fast mode, naive starts) has no reference counterpart
 //   --mode reference|fast reference = the reference's cuRAND stream, bit-exact trajectories
 //   --max-launches N      stop after N launches (0: run forever, as the reference does)
 //   --target-rank R       stop once a walk's best rank reaches R (0: off)
@@ -51,10 +52,10 @@ bool resizeHere(const Options &o) { return o.mode != "fast"; }
 
 class FlipGraph {
 public:
-    FlipGraph(const Options &o) : o_(o), zt_(o.ring == "ZT") {
+    FlipGraph(const Options &o) : o_(o), zt_(o.ring == "ZT"), zb_(o.ring == "ZB") {
         resizeOn_ = o.resize > 0 && resizeHere(o);
         n2bestRank_[key(o.n1, o.n2, o.n3)] = o.n1 * o.n2 * o.n3;
-        known_ = knownRanks(zt_);
+        known_ = knownRanks(zt_ || zb_);
     }
     ~FlipGraph() {
         if (h_) fg_destroy(h_);
@@ -157,7 +158,7 @@ private:
         if (resizeOn_) cap = FG_MAX_RANK + 2;  // products reach the maximal rank
         cap_ = cap;
         fg_config c{};
-        c.ring = zt_ ? FG_RING_ZT : FG_RING_Z2;
+        c.ring = zb_ ? FG_RING_ZB : (zt_ ? FG_RING_ZT : FG_RING_Z2);
         c.mode = o_.mode == "fast" ? FG_MODE_FAST : (o_.mode == "philox" ? FG_MODE_PHILOX_LISTS : FG_MODE_REFERENCE);
         c.walks = o_.schemes;
         c.cap = cap;
@@ -247,7 +248,7 @@ private:
         check(fg_set_best_ranks(h_, ranks.data()), "fg_set_best_ranks");
         if (save) {
             for (auto pair : n2bestIndex) {
-                HostScheme s = fetchScheme(h_, pair.second, cap_, zt_, false);
+                HostScheme s = fetch(pair.second, false);
                 std::string path = savePath(s, iteration, pair.second);
                 s.saveJson(path);
                 std::cout << "Best rank of " << pair.first << " was improved to " << ranks[pair.second]
@@ -257,10 +258,14 @@ private:
         }
     }
 
+    HostScheme fetch(int walk, bool best) {
+        return zb_ ? fetchSchemeZB(h_, walk, cap_, best) : fetchScheme(h_, walk, cap_, zt_, best);
+    }
+
     std::string savePath(const HostScheme &s, int iteration, int runId) const {  // flip_graph.cu:386-399
         std::ostringstream ss;
         ss << o_.path << "/" << key(s.n[0], s.n[1], s.n[2]) << "_m" << s.m << "_c" << s.complexity() << "_iteration"
-           << iteration << "_run" << runId << "_" << key(s.n[0], s.n[1], s.n[2], false) << "_" << ringName(zt_)
+           << iteration << "_run" << runId << "_" << key(s.n[0], s.n[1], s.n[2], false) << "_" << o_.ring
            << ".json";
         return ss.str();
     }
@@ -296,7 +301,7 @@ private:
             int index = pair.second[0];
             keys.push_back(n);
             if (bestRanks[index] < n2bestRank_[n]) {
-                HostScheme best = fetchScheme(h_, index, cap_, zt_, true);
+                HostScheme best = fetch(index, true);
                 std::string path = savePath(best, iteration, index);
                 best.saveJson(path);
                 std::cout << "Best rank of " << n << " was improved from " << n2bestRank_[n] << " to "
@@ -344,7 +349,7 @@ private:
     }
 
     Options o_;
-    bool zt_;
+    bool zt_, zb_;
     bool resizeOn_ = false;  // list mode and resize probability > 0
     fg_handle *h_ = nullptr;
     int cap_ = 0;
@@ -374,7 +379,7 @@ int main(int argc, char *argv[]) {
     parser.add("--plus-iterations", ArgType::Natural, "INT", "number of iterations of plus call", "8000");
     parser.add("--log-period", ArgType::Natural, "INT", "period of report printing", "0");
     parser.add("--seed", ArgType::Natural, "INT", "random seed", "0");
-    parser.add("--ring", ArgType::String, "ZT|Z2", "coefficient ring", "ZT");
+    parser.add("--ring", ArgType::String, "ZT|Z2|ZB", "coefficient ring (ZB: integers with |c| <= 2, fast mode)", "ZT");
     parser.add("--mode", ArgType::String, "MODE", "reference (bit-exact stream) | fast | philox", "reference");
     parser.add("--gauss-probability", ArgType::Real, "REAL",
                "Gauss (XOR) reduction probability (divided by max iterations; Z2, list modes)", "0.0");
@@ -408,9 +413,19 @@ int main(int argc, char *argv[]) {
     o.maxLaunches = std::stol(parser.get("--max-launches"));
     o.targetRank = std::stoi(parser.get("--target-rank"));
     o.timeBudget = std::stod(parser.get("--time-budget"));
-    if (o.ring != "ZT" && o.ring != "Z2") {
+    if (o.ring != "ZT" && o.ring != "Z2" && o.ring != "ZB") {
         std::cerr << "unknown ring \"" << o.ring << "\"" << std::endl;
         return 0;
+    }
+    if (o.ring == "ZB") {  // integers with |c| <= 2: fast mode, naive starts
+        if (o.mode != "fast") {
+            std::cout << "Note: the ZB ring (|c| <= 2) runs in the fast mode" << std::endl;
+            o.mode = "fast";
+        }
+        if (o.inputPath != "null") {
+            std::cout << "Error: the ZB ring starts from the naive scheme (--input-path is not supported)" << std::endl;
+            return -1;
+        }
     }
     if (o.seed == 0) o.seed = (int)time(0);
 

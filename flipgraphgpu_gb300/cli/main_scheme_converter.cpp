@@ -15,10 +15,12 @@
 // written to OUT, several to the directory OUT as
 // <index, 6 digits>_<sorted size>_m<rank>_c<complexity>_<n1>x<n2>x<n3>_<ring>.json,
 // so that reading the directory back (name order) keeps the input order.
-// The ring decides how JSON is written: Z2 writes |value| mod 2, ZT the values;
-// "auto" takes a JSON input's "z2" key, and ZT for text (the reference's default
-// build).  Exit status 0 on success, 1 on any error (message on stderr).
+// The ring decides how JSON is written: Z2 writes |value| mod 2, ZT and ZB the
+// values (bound 1 and 2); "auto" takes a JSON input's "z2" key, and ZT for text
+// (the reference's default build), ZB when an integer entry has magnitude 2.  Exit status 0 on success, 1 on any error (message on stderr).
+#include <algorithm>
 #include <cstdio>
+#include <cstdlib>
 #include <fstream>
 #include <iostream>
 #include <sstream>
@@ -46,11 +48,12 @@ int fail(const std::string &msg) {
 }
 
 // The zero-padded index leads the name, so that name order is input order.
-std::string jsonName(const RawScheme &s, int index, bool zt, int complexity) {
+std::string jsonName(const RawScheme &s, int index, bool zt, int complexity, const std::string &ringOverride) {
     char idx[16];
     std::snprintf(idx, sizeof idx, "%06d", index);
     return std::string(idx) + "_" + key(s.n[0], s.n[1], s.n[2]) + "_m" + std::to_string(s.m) + "_c" +
-           std::to_string(complexity) + "_" + key(s.n[0], s.n[1], s.n[2], false) + "_" + ringName(zt) + ".json";
+           std::to_string(complexity) + "_" + key(s.n[0], s.n[1], s.n[2], false) + "_" +
+           (ringOverride.empty() ? ringName(zt) : ringOverride) + ".json";
 }
 
 int complexityOf(const RawScheme &s, bool zt) {
@@ -69,14 +72,14 @@ int main(int argc, char *argv[]) {
     parser.add("--to", ArgType::String, "auto|text|json", "output format (auto: the other one)", "auto");
     parser.add("--layout", ArgType::String, "auto|flip_graph|complexity_minimizer|additions_reducer",
                "text layout written, or read (auto: flip_graph when writing, detected when reading)", "auto");
-    parser.add("--ring", ArgType::String, "auto|ZT|Z2", "ring of the JSON written", "auto");
+    parser.add("--ring", ArgType::String, "auto|ZT|Z2|ZB", "ring of the JSON written (ZB: integers, |c| <= 2)", "auto");
     if (!parser.parse(argc, argv)) return 0;
 
     const std::string in = parser.get("-i"), out = parser.get("-o"), to = parser.get("--to");
     const std::string layoutArg = parser.get("--layout"), ring = parser.get("--ring");
     if (in.empty() || out.empty()) return fail("-i and -o are required");
     if (to != "auto" && to != "text" && to != "json") return fail("unknown --to \"" + to + "\"");
-    if (ring != "auto" && ring != "ZT" && ring != "Z2") return fail("unknown --ring \"" + ring + "\"");
+    if (ring != "auto" && ring != "ZT" && ring != "Z2" && ring != "ZB") return fail("unknown --ring \"" + ring + "\"");
     bool layoutGiven = layoutArg != "auto";
     TextLayout layout = TextLayout::FlipGraph;
     if (layoutArg == "complexity_minimizer") layout = TextLayout::Minimizer;
@@ -116,11 +119,17 @@ int main(int argc, char *argv[]) {
     if (schemes.size() > 1) mkdir(out.c_str(), 0755);
     for (size_t i = 0; i < schemes.size(); i++) {
         const RawScheme &s = schemes[i];
-        const bool zt = ring == "ZT" || (ring == "auto" && s.z2 != 1);
-        const std::string path = schemes.size() == 1 ? out : out + "/" + jsonName(s, (int)i, zt, complexityOf(s, zt));
+        const bool zt = ring == "ZT" || ring == "ZB" || (ring == "auto" && s.z2 != 1);
+        // auto: an integer scheme with an entry of magnitude 2 is written as the |c| <= 2 ring
+        int maxAbs = 0;
+        for (int c = 0; c < 3; c++)
+            for (int x : s.rows[c]) maxAbs = std::max(maxAbs, std::abs(x));
+        const bool zb = ring == "ZB" || (ring == "auto" && zt && maxAbs == 2);
+        const std::string path =
+            schemes.size() == 1 ? out : out + "/" + jsonName(s, (int)i, zt, complexityOf(s, zt), zb ? "ZB" : "");
         std::ofstream f(path);
         if (!f) return fail("unable to write \"" + path + "\"");
-        if (!writeSchemeJson(s, zt, f, error)) return fail("scheme " + std::to_string(i) + ": " + error);
+        if (!writeSchemeJson(s, zt, f, error, zb ? 2 : 1)) return fail("scheme " + std::to_string(i) + ": " + error);
     }
     std::cout << "Wrote " << schemes.size() << " scheme(s) to \"" << out << "\" (JSON)" << std::endl;
     return 0;

@@ -513,12 +513,12 @@ std::vector<TextLayout> detectTextLayouts(const std::string &text) {
     return fits;
 }
 
-bool writeSchemeJson(const RawScheme &s, bool zt, std::ostream &os, std::string &error) {
+bool writeSchemeJson(const RawScheme &s, bool zt, std::ostream &os, std::string &error, int bound) {
     int nonzero = 0;
     for (int c = 0; c < 3; c++)
         for (int x : s.rows[c]) {
-            if (zt && (x < -1 || x > 1)) {
-                error = "coefficient " + std::to_string(x) + " is not ternary";
+            if (zt && (x < -bound || x > bound)) {
+                error = "coefficient " + std::to_string(x) + (bound == 1 ? " is not ternary" : " exceeds the bound");
                 return false;
             }
             nonzero += zt ? (x != 0) : (std::abs(x) % 2);

@@ -66,8 +66,9 @@ bool openSchemeInput(const std::string &path, TextLayout layout, std::stringstre
 const char *layoutName(TextLayout layout);
 
 // The scheme JSON exactly as SchemeZ2::save / SchemeInteger::save write it,
-// from raw integers: Z2 writes |value| mod 2, ZT writes the values, which must
-// lie in {-1, 0, 1}.  Complexity = nonzero entries - 2m - n3*n1 (getComplexity).
-bool writeSchemeJson(const RawScheme &s, bool zt, std::ostream &os, std::string &error);
+// from raw integers: Z2 writes |value| mod 2, the integer rings write the
+// values, which must lie in [-bound, bound] (1: ZT, 2: the |c| <= 2 ring).
+// Complexity = nonzero entries - 2m - n3*n1 (getComplexity).
+bool writeSchemeJson(const RawScheme &s, bool zt, std::ostream &os, std::string &error, int bound = 1);
 
 }  // namespace fgcli

@@ -696,6 +696,17 @@ fg_status fg_get_scheme(fg_handle *h, int walk, int best, int32_t *n, int32_t *m
     return FG_OK;
 }
 
+fg_status fg_get_scheme_zb(fg_handle *h, int walk, int best, int32_t *n, int32_t *m, uint64_t *fac, uint64_t *sgn,
+                           uint64_t *fac2) {
+    if (!h || h->cfg.ring != FG_RING_ZB) return fail(FG_ERR_ARG, "not a ZB handle");
+    fg_status st = fg_get_scheme(h, walk, best, n, m, fac, nullptr, nullptr);
+    if (st) return st;
+    const size_t o = (size_t)walk * 3 * h->B.cap, nf = (size_t)3 * h->B.cap;
+    if (sgn) FG_CUDA(cudaMemcpy(sgn, (best ? h->B.best_sgn : h->B.sgn) + o, nf * 8, cudaMemcpyDeviceToHost));
+    if (fac2) FG_CUDA(cudaMemcpy(fac2, (best ? h->B.best_fac2 : h->B.fac2) + o, nf * 8, cudaMemcpyDeviceToHost));
+    return FG_OK;
+}
+
 fg_status fg_host_alloc(uint64_t bytes, void **out) {
     if (!out) return fail(FG_ERR_ARG, "null argument");
     FG_CUDA(cudaHostAlloc(out, bytes ? bytes : 1, cudaHostAllocDefault));

@@ -201,6 +201,10 @@ fg_status fg_get_counters(fg_handle *h, int32_t *m, int32_t *best_rank, int32_t 
  * [3][cap] (fac; sgn and valid for ZT, else may be NULL). */
 fg_status fg_get_scheme(fg_handle *h, int walk, int best, int32_t *n, int32_t *m, uint64_t *fac, uint64_t *sgn,
                         uint8_t *valid);
+/* ZB walks: as fg_get_scheme with the sign-magnitude masks (fac nonzero, sgn
+ * negative, fac2 |c| = 2).  No reference counterpart. */
+fg_status fg_get_scheme_zb(fg_handle *h, int walk, int best, int32_t *n, int32_t *m, uint64_t *fac, uint64_t *sgn,
+                           uint64_t *fac2);
 
 /* Fast mode runs each shape segment either one thread per walk or one warp
  * per walk; both kernels give identical results, the choice only sets speed.

@@ -173,3 +173,46 @@ def test_flip_graph_resumes_from_its_own_json(work):
             assert x.read() == y.read(), name
     # The resumed walks start from the saved schemes: nothing above the best saved rank is saved again.
     assert all(int(x.split("_m")[1].split("_")[0]) <= min(ranks) for x in fa)
+
+
+def test_flip_graph_zb_ring_saves_exact_schemes(work):
+    """The |c| <= 2 ring (no reference counterpart) through flip_graph: fast mode, naive starts;
+    every saved scheme is exact over the integers, within the bound, named with the ring."""
+    import json
+    import numpy as np
+    from oracle import oracle as O
+    out = os.path.join(work, "zb")
+    os.makedirs(out)
+    log = run([os.path.join(BIN, "flip_graph"), "-n1", "2", "-n2", "2", "-n3", "3", "--ring", "ZB", "--schemes", "512",
+               "--max-iterations", "3000", "--plus-iterations", "3000", "--resize-probability", "0", "--seed", "5",
+               "--max-launches", "3", "--path", out], work)
+    assert "runs in the fast mode" in log
+    files = sorted(os.listdir(out))
+    assert files and all(f.endswith("_ZB.json") for f in files)
+    for name in files:
+        d = json.load(open(os.path.join(out, name)))
+        assert d["z2"] is False and d["m"] < 12
+        n, m = d["n"], d["m"]
+        fac = np.zeros((1, 3, m), np.uint64)
+        sgn = np.zeros((1, 3, m), np.uint64)
+        two = np.zeros((1, 3, m), np.uint64)
+        for c, key_ in enumerate("uvw"):
+            for t, row in enumerate(d[key_]):
+                for e, x in enumerate(row):
+                    assert -2 <= x <= 2
+                    if x:
+                        fac[0, c, t] |= np.uint64(1 << e)
+                    if x < 0:
+                        sgn[0, c, t] |= np.uint64(1 << e)
+                    if abs(x) == 2:
+                        two[0, c, t] |= np.uint64(1 << e)
+        ok = np.zeros(1, np.uint8)
+        O.lib().fgo_validate_zb(1, m, O._ptr(np.array([n], np.int32)), O._ptr(np.array([m], np.int32)), O._ptr(fac),
+                                O._ptr(sgn), O._ptr(two), O._ptr(ok))
+        assert ok[0] == 1, name
+    # and the converter reads them back (values of magnitude 2 kept)
+    txt = os.path.join(work, "zb.txt")
+    run([os.path.join(BIN, "scheme_converter"), "-i", out, "-o", txt], work)
+    back = os.path.join(work, "zb_back")
+    run([os.path.join(BIN, "scheme_converter"), "-i", txt, "-o", back, "--ring", "ZB"], work)
+    assert (len(os.listdir(back)) if os.path.isdir(back) else 1) == len(files)
