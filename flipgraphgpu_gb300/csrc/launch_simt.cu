@@ -6,6 +6,10 @@ namespace fg {
 
 namespace {
 
+// Words between components of a walk in shared memory: the slot count rounded up
+// to a multiple of 4, so the pair search reads whole groups of 4 without bounds tests.
+__host__ __device__ __forceinline__ int simt_ld(int scap) { return (scap + 3) / 4 * 4; }
+
 // Snapshot of the live terms; the slots past the final best rank are cleared
 // once at the end of the launch (simt_clear_best_tail).
 template <class W>
@@ -30,14 +34,15 @@ __device__ void simt_walk_one(const DevBatch &B, const WalkParams &P, int w, W *
     SimtZ2<W> z(r);
     z.s = s;
     z.cap = scap;
+    z.ld = simt_ld(scap);
     z.n0 = h.n[0]; z.n1 = h.n[1]; z.n2 = h.n[2];
     z.nn0 = z.n0 * z.n1; z.nn1 = z.n1 * z.n2; z.nn2 = z.n2 * z.n0;
     z.full = z.n0 * z.n1 * z.n2;
     z.m = h.m;
     z.status = h.status;
     const uint64_t *src = B.fac + (size_t)w * 3 * B.cap;
-    for (int c = 0; c < 3; c++)
-        for (int t = 0; t < z.m; t++) z.A(c, t) = (W)src[c * B.cap + t];
+    for (int c = 0; c < 3; c++)  // slots past the rank stay zero (SimtZ2::pickPair relies on it)
+        for (int t = 0; t < z.ld; t++) z.A(c, t) = t < z.m ? (W)src[c * B.cap + t] : (W)0;
     z.rebuild();
     int flipsCount = h.flips, bestRank = h.best_rank, bestM = h.best_m;
     uint64_t accepted = 0;
@@ -87,14 +92,14 @@ template <class W>
 __global__ void k_walk_simt(DevBatch B, WalkParams P, int first, int count, int scap) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, wpb = blockDim.x >> 5;
-    W *s = reinterpret_cast<W *>(smem) + (size_t)warp * 3 * scap * 32 + lane;
+    W *s = reinterpret_cast<W *>(smem) + (size_t)warp * 3 * simt_ld(scap) * 32 + lane;
     for (int base = (blockIdx.x * wpb + warp) * 32; base < count; base += gridDim.x * wpb * 32) {
         const int q = base + lane;
         if (q < count) simt_walk_one<W>(B, P, first + q, s, scap);
     }
 }
 
-template <class W> size_t simt_smem(int scap, int wpb) { return (size_t)wpb * 3 * scap * 32 * sizeof(W); }
+template <class W> size_t simt_smem(int scap, int wpb) { return (size_t)wpb * 3 * simt_ld(scap) * 32 * sizeof(W); }
 
 template <class W>
 cudaError_t walk_simt_t(const DevBatch &B, const WalkParams &P, int first, int count, int scap, int wpb, int sms,

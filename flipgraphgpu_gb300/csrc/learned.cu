@@ -36,6 +36,7 @@ __device__ __forceinline__ void bind(Z &z, const LearnedBuffers &L, const WalkHe
     z.s = L.words + w;
     z.rsh = L.sh;
     z.cap = L.scap;
+    z.ld = L.scap;
     z.n0 = h.n[0]; z.n1 = h.n[1]; z.n2 = h.n[2];
     z.nn0 = z.n0 * z.n1; z.nn1 = z.n1 * z.n2; z.nn2 = z.n2 * z.n0;
     z.full = z.n0 * z.n1 * z.n2;
