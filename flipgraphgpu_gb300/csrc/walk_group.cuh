@@ -213,8 +213,9 @@ struct GroupFast {
                 const bool ok = (vk == oldB) & (t != b), nk = (vk == newB) & (t != b);
                 cA += nj;
                 cB += nk;
-                if (oj | nj) A(j, t) = wj + (nj ? ONE : (W)0) - (oj ? ONE : (W)0);
-                if (ok | nk) A(k, t) = wk + (nk ? ONE : (W)0) - (ok ? ONE : (W)0);
+                // unconditional write-back (no divergence; 0-3 % faster)
+                A(j, t) = wj + (nj ? ONE : (W)0) - (oj ? ONE : (W)0);
+                A(k, t) = wk + (nk ? ONE : (W)0) - (ok ? ONE : (W)0);
                 if (checkReduce && (nj | nk)) {
                     const W vi = F(i, t);
                     if (nj && (vi == xia || vk == xka)) candJ |= 1u << x;
