@@ -215,6 +215,19 @@ def reference_arm(args):
     return 0
 
 
+def reduce_over_ranks(seconds, units, dist=None):
+    """Whole-job figures of the replicas: the slowest rank's time and the units of all ranks
+    (one gloo all-reduce each; the walks themselves exchange nothing)."""
+    if not dist:
+        return seconds, float(units)
+    import torch
+    t = torch.tensor([seconds], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    u = torch.tensor([float(units)], dtype=torch.float64)
+    dist.all_reduce(u)
+    return float(t[0]), float(u[0])
+
+
 # ------------------------------------------------------------------ GPU side
 def gpu_arm(args):
     ws, rank = dist_env()
@@ -268,17 +281,7 @@ def gpu_arm(args):
     wall = time.perf_counter() - wall0
     barrier()
     clk = clocks.stop()
-    dev_s = (kern_ms + ver_ms) / 1000.0
-    if dist:
-        import torch
-        t = torch.tensor([dev_s], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        dev_s = float(t[0])
-        v = torch.tensor([float(vflips)], dtype=torch.float64)
-        dist.all_reduce(v)
-        vflips_all = float(v[0])
-    else:
-        vflips_all = float(vflips)
+    dev_s, vflips_all = reduce_over_ranks((kern_ms + ver_ms) / 1000.0, vflips, dist)
     value = vflips_all / dev_s
     best = eng.counters()
     best_rank = {f"{a}x{b}x{c}": int(best["best_rank"][f:f + n].min()) for (a, b, c), f, n in shape_ranges(walks)}
