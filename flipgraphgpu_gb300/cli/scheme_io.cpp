@@ -5,8 +5,6 @@
 #include <cstdlib>
 #include <dirent.h>
 #include <fstream>
-#include <iostream>
-#include <map>
 #include <sys/stat.h>
 
 namespace fgcli {
