@@ -288,7 +288,7 @@ def gpu_arm(args):
     shape_rate = {f"{a}x{b}x{c}": per_shape[(a, b, c)][0] / dev_s for (a, b, c) in SHAPES}
 
     # ---- end to end through the C ABI with page-locked host records
-    rec = fg.Records(walks, cap, "z2", pinned=True)
+    rec = fg.Records(walks, cap, "z2", pinned=True, lists=args.mode != "fast")  # the fast mode keeps no lists
     eng.records(into=rec)
     h2d = d2h = rec.nbytes()
     barrier()

@@ -114,13 +114,14 @@ class Records:
 
     FIELDS = _Records._fields_
 
-    def __init__(self, walks, cap, ring="z2", pinned=False):
+    def __init__(self, walks, cap, ring="z2", pinned=False, lists=True):
+        """lists=False leaves out the FlipSet pairs (the fast and learned modes keep none)."""
         zt = ring == "zt"
         zb = ring == "zb"
         self.walks, self.cap, self.ring = walks, cap, ring
         self._pins = []
         if pinned:
-            self._alloc_pinned(walks, cap, zt, zb)
+            self._alloc_pinned(walks, cap, zt, zb, lists)
             return
         self.n = np.zeros((walks, 3), np.int32)
         self.m = np.zeros(walks, np.int32)
@@ -128,7 +129,7 @@ class Records:
         self.sgn = np.zeros((walks, 3, cap), np.uint64) if zt or zb else None
         self.valid = np.zeros((walks, 3, cap), np.uint8) if zt else None
         self.list_size = np.zeros((walks, 3), np.int32)
-        self.list_pairs = np.zeros((walks, 3, LIST_CAP), np.uint32)
+        self.list_pairs = np.zeros((walks, 3, LIST_CAP), np.uint32) if lists else None
         self.flips = np.zeros(walks, np.int32)
         self.best_rank = np.zeros(walks, np.int32)
         self.best_m = np.zeros(walks, np.int32)
@@ -149,7 +150,7 @@ class Records:
         mag = nz * (1 + ((two[..., None] >> bits) & np.uint64(1)).astype(np.int8))
         return np.where(((sgn[..., None] >> bits) & np.uint64(1)).astype(bool), -mag, mag).astype(np.int8)
 
-    def _alloc_pinned(self, walks, cap, zt, zb=False):
+    def _alloc_pinned(self, walks, cap, zt, zb=False, lists=True):
         def pin(shape, dtype):
             b = PinnedBuffer(shape, dtype)
             self._pins.append(b)
@@ -161,7 +162,7 @@ class Records:
         self.sgn = pin((walks, 3, cap), np.uint64) if zt or zb else None
         self.valid = pin((walks, 3, cap), np.uint8) if zt else None
         self.list_size = pin((walks, 3), np.int32)
-        self.list_pairs = pin((walks, 3, LIST_CAP), np.uint32)
+        self.list_pairs = pin((walks, 3, LIST_CAP), np.uint32) if lists else None
         self.flips = pin((walks,), np.int32)
         self.best_rank = pin((walks,), np.int32)
         self.best_m = pin((walks,), np.int32)

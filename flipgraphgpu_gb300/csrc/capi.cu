@@ -719,8 +719,9 @@ fg_status fg_host_free(void *p) {
 }
 
 fg_status fg_set_records(fg_handle *h, const fg_records *rec) {
-    if (!h || !rec || !rec->n || !rec->m || !rec->fac || !rec->list_size || !rec->list_pairs)
-        return fail(FG_ERR_ARG, "null argument");
+    if (!h || !rec || !rec->n || !rec->m || !rec->fac) return fail(FG_ERR_ARG, "null argument");
+    // The list modes take the FlipSets from the records; the fast modes keep no lists.
+    if (uses_lists(h) && (!rec->list_size || !rec->list_pairs)) return fail(FG_ERR_ARG, "list modes need the lists");
     FG_CUDA(cudaSetDevice(h->dev));
     const int S = h->B.S, cap = h->B.cap;
     size_t nf = (size_t)S * 3 * cap;
@@ -732,7 +733,7 @@ fg_status fg_set_records(fg_handle *h, const fg_records *rec) {
         o.m = rec->m[w];
         if (o.m < 0 || o.m > cap) return fail(FG_ERR_CAPACITY, "record rank exceeds cap");
         for (int c = 0; c < 3; c++) {
-            o.list_size[c] = rec->list_size[w * 3 + c];
+            o.list_size[c] = rec->list_size ? rec->list_size[w * 3 + c] : 0;
             if (o.list_size[c] < 0 || o.list_size[c] > kListCap) return fail(FG_ERR_CAPACITY, "list size");
         }
         o.flips = rec->flips ? rec->flips[w] : 0;
@@ -743,7 +744,8 @@ fg_status fg_set_records(fg_handle *h, const fg_records *rec) {
     }
     FG_CUDA(cudaMemcpy(h->B.hdr, hdr.data(), sizeof(WalkHeader) * S, cudaMemcpyHostToDevice));
     FG_CUDA(cudaMemcpy(h->B.fac, rec->fac, nf * sizeof(uint64_t), cudaMemcpyHostToDevice));
-    FG_CUDA(cudaMemcpy(h->B.lists, rec->list_pairs, (size_t)S * 3 * kListCap * 4, cudaMemcpyHostToDevice));
+    if (uses_lists(h))
+        FG_CUDA(cudaMemcpy(h->B.lists, rec->list_pairs, (size_t)S * 3 * kListCap * 4, cudaMemcpyHostToDevice));
     if (h->B.best_n) {
         std::vector<int32_t> bn((size_t)S * 3);
         for (int w = 0; w < S; w++)
@@ -797,7 +799,12 @@ fg_status fg_get_records(fg_handle *h, fg_records *rec) {
     }
     if (rec->fac) FG_CUDA(cudaMemcpy(rec->fac, h->B.fac, nf * 8, cudaMemcpyDeviceToHost));
     if (rec->best_fac) FG_CUDA(cudaMemcpy(rec->best_fac, h->B.best_fac, nf * 8, cudaMemcpyDeviceToHost));
-    if (rec->list_pairs) FG_CUDA(cudaMemcpy(rec->list_pairs, h->B.lists, (size_t)S * 3 * kListCap * 4, cudaMemcpyDeviceToHost));
+    if (rec->list_pairs) {
+        if (uses_lists(h))
+            FG_CUDA(cudaMemcpy(rec->list_pairs, h->B.lists, (size_t)S * 3 * kListCap * 4, cudaMemcpyDeviceToHost));
+        else
+            std::memset(rec->list_pairs, 0, (size_t)S * 3 * kListCap * 4);  // the fast modes keep no lists
+    }
     if (h->cfg.ring == FG_RING_ZT) {
         if (rec->sgn) FG_CUDA(cudaMemcpy(rec->sgn, h->B.sgn, nf * 8, cudaMemcpyDeviceToHost));
         if (rec->valid) FG_CUDA(cudaMemcpy(rec->valid, h->B.valid, nf, cudaMemcpyDeviceToHost));

@@ -154,11 +154,13 @@ fg_status fg_init_naive_shapes(fg_handle *h, const int32_t *shapes);
 /* Copies host records into the handle (FlipGraph::initializeFromFile +
  * initializeCopyKernel, flip_graph.cu:201-224,459-470, after the host has
  * parsed and replicated the schemes).  rng_pos is not read: streams keep
- * their position. */
+ * their position.  The fast and learned modes keep no lists: list_size and
+ * list_pairs may be NULL there and are not copied. */
 fg_status fg_set_records(fg_handle *h, const fg_records *rec);
 
 /* Copies the handle's records to host buffers (the reference reads managed
- * memory in place, flip_graph.cu:253-265,303-380). */
+ * memory in place, flip_graph.cu:253-265,303-380).  NULL fields are skipped;
+ * in the fast and learned modes list_pairs, when given, reads as zero. */
 fg_status fg_get_records(fg_handle *h, fg_records *rec);
 
 /* Runs `launches` launches of the walk (randomWalkKernel, flip_graph.cu:520-573,
