@@ -247,6 +247,10 @@ def gpu_arm(args):
         eng.set_fast_kernel(args.fast_kernel, args.lanes)
     shapes = shapes_for(walks)
     eng.init_naive_shapes(shapes)
+    kernels = None
+    if args.mode == "fast" and not args.no_autotune:  # per-segment kernel choice, trajectories unchanged
+        names = {0: "thread", 1: "group", 2: "warp"}
+        kernels = [f"{names.get(k, 'auto')}{l if k == 1 else ''}" for k, l in eng.autotune(200)]
     for _ in range(args.warmup):
         eng.run(1)
 
@@ -324,7 +328,8 @@ def gpu_arm(args):
             "config": {"workload": CONFIG_NAME, "walks": walks, "iterations_per_step": iters,
                        "plus_iterations": args.plus_iterations, "expand_p": 0.01, "mode": args.mode,
                        "walks_per_block": args.walks_per_block, "l2": "records larger than L2 (no flush)",
-                       "parallelism": f"replicas x{ws}"},
+                       "parallelism": f"replicas x{ws}", "kernels_by_shape": kernels,
+                       "launch": "per step: one CUDA graph of the shape segments' kernels, then the exact check"},
             "flips_per_s_by_shape": shape_rate, "best_rank_by_shape": best_rank,
             "flips": flips, "verified_flips": vflips,
             "kernel_ms_per_step": kern_ms / args.steps, "verify_ms_per_step": ver_ms / args.steps,
@@ -617,6 +622,7 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--ref-iterations", type=int, default=20000)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true", help="keep the static kernel choice")
     ap.add_argument("--fast-kernel", default=None, choices=["auto", "thread", "group", "warp"],
                     help="fast mode: one kernel for every shape instead of the automatic choice")
     ap.add_argument("--lanes", type=int, default=0, help="group kernel: lanes per walk (4, 8, 16; 0 = by slots)")

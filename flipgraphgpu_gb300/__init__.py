@@ -249,6 +249,15 @@ class Engine:
         self.lib.fg_set_fast_kernel.restype = ctypes.c_int
         _check(self.lib.fg_set_fast_kernel(self.h, kinds[kernel], int(lanes)))
 
+    def autotune(self, iterations=200):
+        """Z2 fast mode: per shape segment, the fastest kernel over `iterations` steps (trajectories
+        unchanged).  Returns [(kind, lanes)] per segment, kind 0 thread, 1 group, 2 warp per walk."""
+        n = self.lib.fg_segment_count(self.h)
+        kinds = np.zeros(max(n, 1), np.int32)
+        lanes = np.zeros(max(n, 1), np.int32)
+        _check(self.lib.fg_autotune(self.h, iterations, _ptr(kinds), _ptr(lanes)))
+        return [(int(k), int(l)) for k, l in zip(kinds[:n], lanes[:n])]
+
     def set_fast_split(self, simt_max_cap):
         """Fast mode kernel choice (same results): -1 automatic, else one thread per walk up to
         this slot count and one warp per walk above."""

@@ -194,6 +194,7 @@ __global__ void k_philox(const uint4 *ctr, int count, uint32_t k0, uint32_t k1, 
 // A run of consecutive walks sharing one shared-memory layout in fast mode.
 struct Segment {
     int first, count, scap, wide, nnmax;
+    int kind = -1, lanes = 0;  // fg_autotune's choice (-1: none)
 };
 
 constexpr int kSideStreams = 8;
@@ -209,8 +210,12 @@ struct fg_handle {
     LearnedBuffers learned;
     LearnedConfig lcfg;
     fg_mlp *mlp = nullptr;
-    int simtMaxCap = -1;
-    int fastKernel = -1, groupLanes = 0;  // fg_set_fast_kernel override  // fast mode: -1 = automatic choice per segment, else thread per walk up to this slot count
+    int simtMaxCap = -1;                  // fg_set_fast_split: thread per walk up to this slot count (-1: off)
+    int fastKernel = -1, groupLanes = 0;  // fg_set_fast_kernel override (-1: per-segment choice)
+    // Fast mode: the walk launches of one step (all segments, forked and joined) as a CUDA
+    // graph, captured on first use and dropped whenever the launch plan changes.
+    cudaGraphExec_t walkGraph = nullptr;
+    bool graphPrimed = false;  // the plan's kernels ran once directly (attributes set) before capture
     DevBatch B{};
     WalkParams P{};
     int32_t *d_bestC = nullptr;
@@ -286,6 +291,12 @@ fg_status launch_verify(fg_handle *h, int best) {
 // plus and split stop at n1*n2*n3, scheme_z2.cu:1030,1053,1081).  Too many
 // segments (shapes interleaved walk by walk) collapse into one segment sized
 // for the largest walk.
+void drop_graph(fg_handle *h) {
+    if (h->walkGraph) cudaGraphExecDestroy(h->walkGraph);
+    h->walkGraph = nullptr;
+    h->graphPrimed = false;
+}
+
 void plan_segments(fg_handle *h, const std::vector<WalkHeader> &hdr) {
     const int S = h->B.S, cap = h->B.cap;
     std::vector<Segment> segs;
@@ -312,6 +323,7 @@ void plan_segments(fg_handle *h, const std::vector<WalkHeader> &hdr) {
     }
     if ((int)segs.size() > kSideStreams) segs.assign(1, Segment{0, S, maxScap, anyWide, maxNN});
     h->segs = segs;
+    drop_graph(h);
 }
 
 // Fast mode kernel choice for a segment.  One thread per walk does O(m) work
@@ -380,6 +392,45 @@ fg_status update_ranks(fg_handle *h) {
     return FG_OK;
 }
 
+// Fast-mode kernel of segment g: fg_set_fast_kernel's override, else fg_autotune's
+// choice, else fg_set_fast_split's split, else the measured crossover.
+void segment_kernel(const fg_handle *h, const Segment &g, int &kind, int &lanes) {
+    lanes = 32;
+    if (h->fastKernel >= 0) { kind = h->fastKernel; lanes = kind == FG_FAST_GROUP ? h->groupLanes : 32; return; }
+    if (g.kind >= 0) { kind = g.kind; lanes = g.lanes; return; }
+    if (h->simtMaxCap >= 0) kind = g.scap <= h->simtMaxCap ? FG_FAST_THREAD : FG_FAST_WARP;
+    else kind = thread_per_walk(g.scap, h->B.S, h->sms) ? FG_FAST_THREAD : FG_FAST_WARP;
+}
+
+cudaError_t launch_segment(const fg_handle *h, const Segment &g, int kind, int lanes, cudaStream_t st) {
+    if (h->cfg.ring == FG_RING_ZB) return launch_walk_zb(h->B, h->P, g.first, g.count, g.scap, h->sms, st);
+    const int wpb = h->cfg.walks_per_block > 0 ? h->cfg.walks_per_block : 2;
+    if (kind == FG_FAST_THREAD) return launch_walk_simt(h->B, h->P, g.first, g.count, g.scap, g.wide, wpb, h->sms, st);
+    if (kind == FG_FAST_GROUP) return launch_walk_group(h->B, h->P, g.first, g.count, g.scap, g.wide, lanes, h->sms, st);
+    return launch_walk_group(h->B, h->P, g.first, g.count, g.scap, g.wide, 32, h->sms, st);  // one warp per walk
+}
+
+// Every segment's kernel, one side stream each, forked from and joined into h->stream.
+cudaError_t launch_segments(fg_handle *h) {
+    cudaError_t e;
+    if (h->segs.size() == 1) {
+        int kind, lanes;
+        segment_kernel(h, h->segs[0], kind, lanes);
+        return launch_segment(h, h->segs[0], kind, lanes, h->stream);
+    }
+    if ((e = cudaEventRecord(h->fork, h->stream)) != cudaSuccess) return e;
+    for (size_t i = 0; i < h->segs.size(); i++) {
+        const Segment &g = h->segs[i];
+        int kind, lanes;
+        segment_kernel(h, g, kind, lanes);
+        if ((e = cudaStreamWaitEvent(h->side[i], h->fork, 0)) != cudaSuccess) return e;
+        if ((e = launch_segment(h, g, kind, lanes, h->side[i])) != cudaSuccess) return e;
+        if ((e = cudaEventRecord(h->join[i], h->side[i])) != cudaSuccess) return e;
+        if ((e = cudaStreamWaitEvent(h->stream, h->join[i], 0)) != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
 // Launches one walk pass over every walk on h->stream (fast mode: one kernel
 // per segment on side streams, forked from and joined back into h->stream).
 fg_status launch_walks(fg_handle *h) {
@@ -394,33 +445,35 @@ fg_status launch_walks(fg_handle *h) {
                             h->wpb, h->grid, h->stream));
         return FG_OK;
     }
-    const int wpb = h->cfg.walks_per_block > 0 ? h->cfg.walks_per_block : 2;
     if (h->cfg.ring != FG_RING_ZB)
         for (const Segment &g : h->segs)
             if (g.nnmax > 56) return fail(FG_ERR_CAPACITY, "fast mode holds factors of at most 56 entries");
-    auto launch = [&](const Segment &g, cudaStream_t st) {
-        if (h->cfg.ring == FG_RING_ZB) return launch_walk_zb(h->B, h->P, g.first, g.count, g.scap, h->sms, st);
-        int kind;
-        if (h->fastKernel >= 0) kind = h->fastKernel;
-        else if (h->simtMaxCap >= 0) kind = g.scap <= h->simtMaxCap ? FG_FAST_THREAD : FG_FAST_WARP;
-        else kind = thread_per_walk(g.scap, h->B.S, h->sms) ? FG_FAST_THREAD : FG_FAST_WARP;
-        if (kind == FG_FAST_THREAD) return launch_walk_simt(h->B, h->P, g.first, g.count, g.scap, g.wide, wpb, h->sms, st);
-        if (kind == FG_FAST_GROUP)
-            return launch_walk_group(h->B, h->P, g.first, g.count, g.scap, g.wide, h->groupLanes, h->sms, st);
-        return launch_walk_group(h->B, h->P, g.first, g.count, g.scap, g.wide, 32, h->sms, st);  // one warp per walk
-    };
-    if (h->segs.size() == 1) {
-        FG_CUDA(launch(h->segs[0], h->stream));
+    if (h->walkGraph) {
+        FG_CUDA(cudaGraphLaunch(h->walkGraph, h->stream));
         return FG_OK;
     }
-    FG_CUDA(cudaEventRecord(h->fork, h->stream));
-    for (size_t i = 0; i < h->segs.size(); i++) {
-        const Segment &g = h->segs[i];
-        FG_CUDA(cudaStreamWaitEvent(h->side[i], h->fork, 0));
-        FG_CUDA(launch(g, h->side[i]));
-        FG_CUDA(cudaEventRecord(h->join[i], h->side[i]));
-        FG_CUDA(cudaStreamWaitEvent(h->stream, h->join[i], 0));
+    if (!h->graphPrimed) {  // first step of a plan: direct launches (they set the kernels' attributes)
+        FG_CUDA(launch_segments(h));
+        h->graphPrimed = true;
+        return FG_OK;
     }
+    // Capture this step's launches once; later steps replay the graph.
+    cudaGraph_t g = nullptr;
+    FG_CUDA(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeRelaxed));
+    cudaError_t le = launch_segments(h);
+    cudaError_t ce = cudaStreamEndCapture(h->stream, &g);
+    if (le != cudaSuccess || ce != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        cudaGetLastError();
+        return fail(FG_ERR_CUDA, cudaGetErrorString(le != cudaSuccess ? le : ce));
+    }
+    cudaError_t ie = cudaGraphInstantiate(&h->walkGraph, g, 0);
+    cudaGraphDestroy(g);
+    if (ie != cudaSuccess) {
+        h->walkGraph = nullptr;
+        return fail(FG_ERR_CUDA, cudaGetErrorString(ie));
+    }
+    FG_CUDA(cudaGraphLaunch(h->walkGraph, h->stream));
     return FG_OK;
 }
 
@@ -531,6 +584,7 @@ fg_status fg_destroy(fg_handle *h) {
     cudaSetDevice(h->dev);
     if (h->stream) cudaStreamSynchronize(h->stream);
     learned_free(h->learned);
+    drop_graph(h);
     void *ptrs[] = {h->B.hdr, h->B.fac, h->B.sgn, h->B.valid, h->B.lists, h->B.best_fac, h->B.best_sgn,
                     h->B.best_valid, h->B.xorwow, h->d_bestC, h->d_valid, h->B.best_n, h->d_copyList,
                     h->d_bestRanks, h->B.fac2, h->B.best_fac2};
@@ -649,12 +703,83 @@ fg_status fg_set_fast_kernel(fg_handle *h, int kernel, int lanes) {
         return fail(FG_ERR_ARG, "kernel in -1..2, lanes 0, 4, 8, 16 or 32");
     h->fastKernel = kernel;
     h->groupLanes = lanes;
+    drop_graph(h);
     return FG_OK;
 }
+
+fg_status fg_autotune(fg_handle *h, int iterations, int32_t *kinds, int32_t *lanes) {
+    if (!h || iterations <= 0) return fail(FG_ERR_ARG, "bad argument");
+    if (!h->ready) return fail(FG_ERR_STATE, "records not initialised");
+    if (h->cfg.mode != FG_MODE_FAST || h->cfg.ring != FG_RING_Z2)
+        return fail(FG_ERR_ARG, "the autotuner chooses among the Z2 fast-mode kernels");
+    FG_CUDA(cudaSetDevice(h->dev));
+    FG_CUDA(cudaStreamSynchronize(h->stream));
+    const size_t S = (size_t)h->B.S, nf = S * 3 * h->B.cap;
+    // Snapshot of everything a fast-mode launch changes; every trial starts from it and it
+    // is put back at the end, so tuning leaves trajectories and stream positions untouched.
+    WalkHeader *hdr0 = nullptr;
+    uint64_t *fac0 = nullptr, *best0 = nullptr;
+    auto release = [&]() { cudaFree(hdr0); cudaFree(fac0); cudaFree(best0); };
+    if (cudaMalloc(&hdr0, S * sizeof(WalkHeader)) != cudaSuccess || cudaMalloc(&fac0, nf * 8) != cudaSuccess ||
+        cudaMalloc(&best0, nf * 8) != cudaSuccess) {
+        release();
+        return fail(FG_ERR_CUDA, "autotune snapshot allocation failed");
+    }
+    auto restore = [&](bool save) -> cudaError_t {
+        cudaError_t e;
+        WalkHeader *hs = save ? h->B.hdr : hdr0, *hd = save ? hdr0 : h->B.hdr;
+        uint64_t *fs = save ? h->B.fac : fac0, *fd = save ? fac0 : h->B.fac;
+        uint64_t *bs = save ? h->B.best_fac : best0, *bd = save ? best0 : h->B.best_fac;
+        if ((e = cudaMemcpyAsync(hd, hs, S * sizeof(WalkHeader), cudaMemcpyDeviceToDevice, h->stream)) != cudaSuccess) return e;
+        if ((e = cudaMemcpyAsync(fd, fs, nf * 8, cudaMemcpyDeviceToDevice, h->stream)) != cudaSuccess) return e;
+        return cudaMemcpyAsync(bd, bs, nf * 8, cudaMemcpyDeviceToDevice, h->stream);
+    };
+    cudaError_t e = restore(true);
+    const int savedIterations = h->P.iterations;
+    h->P.iterations = iterations;
+    drop_graph(h);
+    const int cand[4][2] = {{FG_FAST_THREAD, 0}, {FG_FAST_GROUP, 8}, {FG_FAST_GROUP, 16}, {FG_FAST_WARP, 32}};
+    for (size_t i = 0; e == cudaSuccess && i < h->segs.size(); i++) {
+        Segment &g = h->segs[i];
+        float best = 1e30f;
+        g.kind = -1;
+        for (const auto &c : cand) {
+            if ((e = restore(false)) != cudaSuccess) break;
+            launch_segment(h, g, c[0], c[1], h->stream);  // warm (kernel attributes); not timed
+            if ((e = restore(false)) != cudaSuccess) break;
+            cudaEventRecord(h->ev[0], h->stream);
+            cudaError_t le = launch_segment(h, g, c[0], c[1], h->stream);
+            cudaEventRecord(h->ev[1], h->stream);
+            if ((e = cudaStreamSynchronize(h->stream)) != cudaSuccess) break;
+            if (le != cudaSuccess) {  // not available for this segment (e.g. shared memory): skip
+                cudaGetLastError();
+                continue;
+            }
+            float ms = 0;
+            cudaEventElapsedTime(&ms, h->ev[0], h->ev[1]);
+            if (ms < best) { best = ms; g.kind = c[0]; g.lanes = c[1]; }
+        }
+    }
+    h->P.iterations = savedIterations;
+    cudaError_t re = restore(false);
+    if (e == cudaSuccess) e = re;
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    release();
+    drop_graph(h);
+    if (e != cudaSuccess) return fail(FG_ERR_CUDA, cudaGetErrorString(e));
+    for (size_t i = 0; i < h->segs.size(); i++) {
+        if (kinds) kinds[i] = h->segs[i].kind;
+        if (lanes) lanes[i] = h->segs[i].lanes;
+    }
+    return FG_OK;
+}
+
+int fg_segment_count(fg_handle *h) { return h ? (int)h->segs.size() : 0; }
 
 fg_status fg_set_fast_split(fg_handle *h, int simt_max_cap) {
     if (!h || simt_max_cap < -1) return fail(FG_ERR_ARG, "bad argument");
     h->simtMaxCap = simt_max_cap;
+    drop_graph(h);
     return FG_OK;
 }
 

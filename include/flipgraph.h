@@ -243,6 +243,16 @@ fg_status fg_rebuild_lists(fg_handle *h);
 enum { FG_FAST_THREAD = 0, FG_FAST_GROUP = 1, FG_FAST_WARP = 2 };
 fg_status fg_set_fast_kernel(fg_handle *h, int kernel, int lanes);
 
+/* Z2 fast mode: times every kernel (thread per walk; 8, 16 and 32 lanes per
+ * walk) on each shape segment for `iterations` steps and keeps the fastest per
+ * segment.  Each trial starts from a snapshot of the records, which is put back
+ * afterwards, so tuning changes no trajectory and no stream position.  The
+ * choice holds until the records are replaced (fg_set_records, fg_init_naive*)
+ * and yields to fg_set_fast_kernel.  kinds / lanes (fg_segment_count entries,
+ * may be NULL) receive the choices.  No reference counterpart. */
+fg_status fg_autotune(fg_handle *h, int iterations, int32_t *kinds, int32_t *lanes);
+int fg_segment_count(fg_handle *h);
+
 /* Tensor-core (tcgen05) bf16 GEMM of the learned proposal's MLP, on host
  * buffers (test and support entry; no reference counterpart):
  *   D[M][N] = A[M][K] * B[N][K]^T, A and B bf16 bit patterns, row-major;

@@ -377,3 +377,26 @@ def test_ternary_sandwiching_vs_oracle(mode, shape, resize_p):
     else:
         O.walk(b, b.cfg("philox", launches=launches, **cfg))
     compare_records(rec, b, f"ternary sandwiching {mode} {shape}")
+
+
+def test_autotune_and_graph_replay_keep_trajectories():
+    """fg_autotune times the kernels on a snapshot it puts back, and the later launches replay a
+    captured CUDA graph: the records after four launches equal those of an untuned run."""
+    shapes = [(2, 2, 3), (3, 3, 3), (3, 4, 5), (4, 4, 4), (5, 5, 5)]
+    per = 640
+    S = per * len(shapes)
+    sh = np.array([shapes[w // per] for w in range(S)], np.int32)
+    out = []
+    for tune in (False, True):
+        with fg.Engine(S, 125, "z2", "fast", 31, 400, 2000, 0.5, 0.0) as eng:
+            eng.init_naive_shapes(sh)
+            if tune:
+                choice = eng.autotune(100)
+                assert len(choice) == len(shapes)
+                assert all(k in (0, 1, 2) for k, _ in choice)
+            for _ in range(4):
+                eng.run(1)
+            out.append(eng.records())
+            assert eng.validate().all()
+    for f in ("n", "m", "fac", "flips", "best_rank", "best_m", "best_fac", "rng_pos", "status"):
+        assert np.array_equal(getattr(out[0], f), getattr(out[1], f)), f
