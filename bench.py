@@ -250,7 +250,8 @@ def gpu_arm(args):
     kernels = None
     if args.mode == "fast" and not args.no_autotune:  # per-segment kernel choice, trajectories unchanged
         names = {0: "thread", 1: "group", 2: "warp"}
-        kernels = [f"{names.get(k, 'auto')}{l if k == 1 else ''}" for k, l in eng.autotune(200)]
+        kernels = [f"{names.get(k, 'auto')}{l if k == 1 else ''}{f'/{w}w' if k == 0 else ''}"
+                   for k, l, w in eng.autotune(200)]
     for _ in range(args.warmup):
         eng.run(1)
 

@@ -251,12 +251,14 @@ class Engine:
 
     def autotune(self, iterations=200):
         """Z2 fast mode: per shape segment, the fastest kernel over `iterations` steps (trajectories
-        unchanged).  Returns [(kind, lanes)] per segment, kind 0 thread, 1 group, 2 warp per walk."""
+        unchanged).  Returns [(kind, lanes, warps_per_block)] per segment, kind 0 thread, 1 group,
+        2 warp per walk."""
         n = self.lib.fg_segment_count(self.h)
         kinds = np.zeros(max(n, 1), np.int32)
         lanes = np.zeros(max(n, 1), np.int32)
-        _check(self.lib.fg_autotune(self.h, iterations, _ptr(kinds), _ptr(lanes)))
-        return [(int(k), int(l)) for k, l in zip(kinds[:n], lanes[:n])]
+        warps = np.zeros(max(n, 1), np.int32)
+        _check(self.lib.fg_autotune(self.h, iterations, _ptr(kinds), _ptr(lanes), _ptr(warps)))
+        return [(int(k), int(l), int(w)) for k, l, w in zip(kinds[:n], lanes[:n], warps[:n])]
 
     def set_fast_split(self, simt_max_cap):
         """Fast mode kernel choice (same results): -1 automatic, else one thread per walk up to

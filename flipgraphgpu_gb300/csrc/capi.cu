@@ -194,7 +194,7 @@ __global__ void k_philox(const uint4 *ctr, int count, uint32_t k0, uint32_t k1, 
 // A run of consecutive walks sharing one shared-memory layout in fast mode.
 struct Segment {
     int first, count, scap, wide, nnmax;
-    int kind = -1, lanes = 0;  // fg_autotune's choice (-1: none)
+    int kind = -1, lanes = 0, wpb = 0;  // fg_autotune's choice (kind -1: none; wpb: warps per block, thread kernel)
 };
 
 constexpr int kSideStreams = 8;
@@ -394,17 +394,22 @@ fg_status update_ranks(fg_handle *h) {
 
 // Fast-mode kernel of segment g: fg_set_fast_kernel's override, else fg_autotune's
 // choice, else fg_set_fast_split's split, else the measured crossover.
-void segment_kernel(const fg_handle *h, const Segment &g, int &kind, int &lanes) {
+void segment_kernel(const fg_handle *h, const Segment &g, int &kind, int &lanes, int &wpb) {
     lanes = 32;
+    wpb = h->cfg.walks_per_block > 0 ? h->cfg.walks_per_block : 2;
     if (h->fastKernel >= 0) { kind = h->fastKernel; lanes = kind == FG_FAST_GROUP ? h->groupLanes : 32; return; }
-    if (g.kind >= 0) { kind = g.kind; lanes = g.lanes; return; }
+    if (g.kind >= 0) {
+        kind = g.kind;
+        lanes = g.lanes;
+        if (g.wpb > 0) wpb = g.wpb;
+        return;
+    }
     if (h->simtMaxCap >= 0) kind = g.scap <= h->simtMaxCap ? FG_FAST_THREAD : FG_FAST_WARP;
     else kind = thread_per_walk(g.scap, h->B.S, h->sms) ? FG_FAST_THREAD : FG_FAST_WARP;
 }
 
-cudaError_t launch_segment(const fg_handle *h, const Segment &g, int kind, int lanes, cudaStream_t st) {
+cudaError_t launch_segment(const fg_handle *h, const Segment &g, int kind, int lanes, int wpb, cudaStream_t st) {
     if (h->cfg.ring == FG_RING_ZB) return launch_walk_zb(h->B, h->P, g.first, g.count, g.scap, h->sms, st);
-    const int wpb = h->cfg.walks_per_block > 0 ? h->cfg.walks_per_block : 2;
     if (kind == FG_FAST_THREAD) return launch_walk_simt(h->B, h->P, g.first, g.count, g.scap, g.wide, wpb, h->sms, st);
     if (kind == FG_FAST_GROUP) return launch_walk_group(h->B, h->P, g.first, g.count, g.scap, g.wide, lanes, h->sms, st);
     return launch_walk_group(h->B, h->P, g.first, g.count, g.scap, g.wide, 32, h->sms, st);  // one warp per walk
@@ -414,17 +419,17 @@ cudaError_t launch_segment(const fg_handle *h, const Segment &g, int kind, int l
 cudaError_t launch_segments(fg_handle *h) {
     cudaError_t e;
     if (h->segs.size() == 1) {
-        int kind, lanes;
-        segment_kernel(h, h->segs[0], kind, lanes);
-        return launch_segment(h, h->segs[0], kind, lanes, h->stream);
+        int kind, lanes, wpb;
+        segment_kernel(h, h->segs[0], kind, lanes, wpb);
+        return launch_segment(h, h->segs[0], kind, lanes, wpb, h->stream);
     }
     if ((e = cudaEventRecord(h->fork, h->stream)) != cudaSuccess) return e;
     for (size_t i = 0; i < h->segs.size(); i++) {
         const Segment &g = h->segs[i];
-        int kind, lanes;
-        segment_kernel(h, g, kind, lanes);
+        int kind, lanes, wpb;
+        segment_kernel(h, g, kind, lanes, wpb);
         if ((e = cudaStreamWaitEvent(h->side[i], h->fork, 0)) != cudaSuccess) return e;
-        if ((e = launch_segment(h, g, kind, lanes, h->side[i])) != cudaSuccess) return e;
+        if ((e = launch_segment(h, g, kind, lanes, wpb, h->side[i])) != cudaSuccess) return e;
         if ((e = cudaEventRecord(h->join[i], h->side[i])) != cudaSuccess) return e;
         if ((e = cudaStreamWaitEvent(h->stream, h->join[i], 0)) != cudaSuccess) return e;
     }
@@ -707,7 +712,7 @@ fg_status fg_set_fast_kernel(fg_handle *h, int kernel, int lanes) {
     return FG_OK;
 }
 
-fg_status fg_autotune(fg_handle *h, int iterations, int32_t *kinds, int32_t *lanes) {
+fg_status fg_autotune(fg_handle *h, int iterations, int32_t *kinds, int32_t *lanes, int32_t *warps) {
     if (!h || iterations <= 0) return fail(FG_ERR_ARG, "bad argument");
     if (!h->ready) return fail(FG_ERR_STATE, "records not initialised");
     if (h->cfg.mode != FG_MODE_FAST || h->cfg.ring != FG_RING_Z2)
@@ -738,27 +743,47 @@ fg_status fg_autotune(fg_handle *h, int iterations, int32_t *kinds, int32_t *lan
     const int savedIterations = h->P.iterations;
     h->P.iterations = iterations;
     drop_graph(h);
-    const int cand[4][2] = {{FG_FAST_THREAD, 0}, {FG_FAST_GROUP, 8}, {FG_FAST_GROUP, 16}, {FG_FAST_WARP, 32}};
+    // (kind, lanes, warps per block): thread per walk with 1, 2, 4 warps per block; 8, 16, 32 lanes per walk
+    const int cand[6][3] = {{FG_FAST_THREAD, 0, 1}, {FG_FAST_THREAD, 0, 2}, {FG_FAST_THREAD, 0, 4},
+                            {FG_FAST_GROUP, 8, 0},  {FG_FAST_GROUP, 16, 0}, {FG_FAST_WARP, 32, 0}};
+    // The segments run concurrently, so a choice is judged by the whole step: starting from
+    // the static choice, each segment in turn takes the candidate that minimises the time of
+    // all segments' launches with the others fixed (one sweep of coordinate descent).
+    auto trial = [&](float &ms) -> cudaError_t {
+        cudaError_t te;
+        if ((te = restore(false)) != cudaSuccess) return te;
+        launch_segments(h);  // warm (kernel attributes); not timed
+        if ((te = restore(false)) != cudaSuccess) return te;
+        cudaEventRecord(h->ev[0], h->stream);
+        cudaError_t le = launch_segments(h);
+        cudaEventRecord(h->ev[1], h->stream);
+        if ((te = cudaStreamSynchronize(h->stream)) != cudaSuccess) return te;
+        if (le != cudaSuccess) {  // a candidate this segment cannot run (e.g. shared memory)
+            cudaGetLastError();
+            ms = 1e30f;
+            return cudaSuccess;
+        }
+        cudaEventElapsedTime(&ms, h->ev[0], h->ev[1]);
+        return cudaSuccess;
+    };
+    for (Segment &g : h->segs) {  // explicit static choice as the starting point
+        int k, l, w;
+        g.kind = -1;
+        segment_kernel(h, g, k, l, w);
+        g.kind = k; g.lanes = l; g.wpb = k == FG_FAST_THREAD ? w : 0;
+    }
     for (size_t i = 0; e == cudaSuccess && i < h->segs.size(); i++) {
         Segment &g = h->segs[i];
+        const Segment keep = g;
         float best = 1e30f;
-        g.kind = -1;
+        Segment choice = keep;
         for (const auto &c : cand) {
-            if ((e = restore(false)) != cudaSuccess) break;
-            launch_segment(h, g, c[0], c[1], h->stream);  // warm (kernel attributes); not timed
-            if ((e = restore(false)) != cudaSuccess) break;
-            cudaEventRecord(h->ev[0], h->stream);
-            cudaError_t le = launch_segment(h, g, c[0], c[1], h->stream);
-            cudaEventRecord(h->ev[1], h->stream);
-            if ((e = cudaStreamSynchronize(h->stream)) != cudaSuccess) break;
-            if (le != cudaSuccess) {  // not available for this segment (e.g. shared memory): skip
-                cudaGetLastError();
-                continue;
-            }
+            g.kind = c[0]; g.lanes = c[1]; g.wpb = c[2];
             float ms = 0;
-            cudaEventElapsedTime(&ms, h->ev[0], h->ev[1]);
-            if (ms < best) { best = ms; g.kind = c[0]; g.lanes = c[1]; }
+            if ((e = trial(ms)) != cudaSuccess) break;
+            if (ms < best) { best = ms; choice = g; }
         }
+        g = best < 1e30f ? choice : keep;
     }
     h->P.iterations = savedIterations;
     cudaError_t re = restore(false);
@@ -770,6 +795,7 @@ fg_status fg_autotune(fg_handle *h, int iterations, int32_t *kinds, int32_t *lan
     for (size_t i = 0; i < h->segs.size(); i++) {
         if (kinds) kinds[i] = h->segs[i].kind;
         if (lanes) lanes[i] = h->segs[i].lanes;
+        if (warps) warps[i] = h->segs[i].wpb;
     }
     return FG_OK;
 }

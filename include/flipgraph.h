@@ -243,14 +243,17 @@ fg_status fg_rebuild_lists(fg_handle *h);
 enum { FG_FAST_THREAD = 0, FG_FAST_GROUP = 1, FG_FAST_WARP = 2 };
 fg_status fg_set_fast_kernel(fg_handle *h, int kernel, int lanes);
 
-/* Z2 fast mode: times every kernel (thread per walk; 8, 16 and 32 lanes per
- * walk) on each shape segment for `iterations` steps and keeps the fastest per
- * segment.  Each trial starts from a snapshot of the records, which is put back
+/* Z2 fast mode: chooses each shape segment's kernel (thread per walk with 1, 2
+ * or 4 warps per block; 8, 16 or 32 lanes per walk) by timing the step's
+ * concurrent launches of all segments for `iterations` steps: from the static
+ * choice, each segment in turn takes the candidate with the shortest step.
+ * Each trial starts from a snapshot of the records, which is put back
  * afterwards, so tuning changes no trajectory and no stream position.  The
  * choice holds until the records are replaced (fg_set_records, fg_init_naive*)
- * and yields to fg_set_fast_kernel.  kinds / lanes (fg_segment_count entries,
- * may be NULL) receive the choices.  No reference counterpart. */
-fg_status fg_autotune(fg_handle *h, int iterations, int32_t *kinds, int32_t *lanes);
+ * and yields to fg_set_fast_kernel.  kinds / lanes / warps (fg_segment_count
+ * entries each, may be NULL) receive the choices (warps: warps per block of
+ * the thread-per-walk kernel, else 0).  No reference counterpart. */
+fg_status fg_autotune(fg_handle *h, int iterations, int32_t *kinds, int32_t *lanes, int32_t *warps);
 int fg_segment_count(fg_handle *h);
 
 /* Tensor-core (tcgen05) bf16 GEMM of the learned proposal's MLP, on host

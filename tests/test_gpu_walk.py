@@ -393,7 +393,7 @@ def test_autotune_and_graph_replay_keep_trajectories():
             if tune:
                 choice = eng.autotune(100)
                 assert len(choice) == len(shapes)
-                assert all(k in (0, 1, 2) for k, _ in choice)
+                assert all(k in (0, 1, 2) and (w in (1, 2, 4) if k == 0 else w == 0) for k, _, w in choice)
             for _ in range(4):
                 eng.run(1)
             out.append(eng.records())
