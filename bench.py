@@ -393,8 +393,8 @@ def learned_arm(args):
     """Learned flip proposal against the uniform one on the same GPU.
 
     1. Records: plain (uniform-proposal) walks from the naive schemes of (3,3,3), (3,4,5) and
-       (4,4,4) log every 16th accepted flip with label "rank dropped within the next 1000 flips",
-       until --learned-records labelled records exist.
+       (4,4,4) log every --learned-every-th accepted flip with label "rank dropped within the next
+       --learned-horizon flips" (16 and 1000 by default), until --learned-records records exist.
     2. Training: the 192-256-256-1 bf16 MLP on the tensor cores (Adam, --learned-epochs).
     3. Held-out AUC of the scores (a uniform proposal scores 0.5).
     4. Search: for (4,4,4) and (3,4,5), --learned-walks walks each from the naive scheme for
@@ -412,7 +412,8 @@ def learned_arm(args):
     with fg.Engine(len(sh), 64, "z2", "learned", args.seed, 2000, 50000, 0.01, 0.0) as eng:
         eng.init_naive_shapes(sh)
         while total < args.learned_records and launches < 64:
-            f, y = eng.collect_records(every=16, horizon=1000, launches=2, capacity=1 << 23)
+            f, y = eng.collect_records(every=args.learned_every, horizon=args.learned_horizon, launches=2,
+                                       capacity=1 << 23)
             feats.append(f)
             labels.append(y)
             total += len(y)
@@ -434,6 +435,7 @@ def learned_arm(args):
     pos = y[split:] > 0
     auc = float((ranks[pos].mean() - (pos.sum() - 1) / 2) / max((~pos).sum(), 1))
     print(json.dumps({"workload": "learned proposal: records and training", "records": int(len(y)),
+                      "horizon": args.learned_horizon, "every": args.learned_every,
                       "positive_fraction": float(y.mean()), "collect_seconds": t_collect, "train_seconds": t_train,
                       "epochs": args.learned_epochs, "final_loss": loss, "heldout_auc": auc}))
     sys.stdout.flush()
@@ -445,9 +447,10 @@ def learned_arm(args):
             eng.set_proposal(net, candidates=args.learned_candidates, temperature=1.0, min_entropy=0.05)
         eng.init_naive(n1, n2, n3)
         t = time.perf_counter()
-        flips, kernel_ms, best, reached = 0, 0.0, n1 * n2 * n3, None
+        flips, kernel_ms, best, reached, launches = 0, 0.0, n1 * n2 * n3, None, 0
         while time.perf_counter() - t < seconds:
             st = eng.run(1)
+            launches += 1
             flips += st["verified_flips"]
             kernel_ms += st["kernel_ms"] + st["verify_ms"]
             best = min(best, st["min_best_rank"])
@@ -460,7 +463,7 @@ def learned_arm(args):
         wall = time.perf_counter() - t
         eng.close()
         return {"flips_per_s": flips / max(kernel_ms / 1000, 1e-9), "best_rank": int(best), "seconds": wall,
-                "reached_seconds": reached}
+                "reached_seconds": reached, "launches": launches, "steps_per_walk": launches * iters}
 
     for shape in ((4, 4, 4), (3, 4, 5)):
         for mode in ("fast", "learned"):
@@ -640,6 +643,8 @@ def main():
     ap.add_argument("--learned-walks", type=int, default=65536)
     ap.add_argument("--learned-seconds", type=float, default=30.0)
     ap.add_argument("--learned-candidates", type=int, default=8)
+    ap.add_argument("--learned-horizon", type=int, default=1000, help="label: rank drop within this many flips")
+    ap.add_argument("--learned-every", type=int, default=16, help="record every n-th accepted flip")
     ap.add_argument("--ttr-modes", default="fast,reference")
     ap.add_argument("--ttr-seconds", type=float, default=300.0)
     ap.add_argument("--ttr-shape", default="3x3x3")
