@@ -489,8 +489,8 @@ def post_arm(args):
     1. Search (config 1's method): 65,536 fast-mode walks of 4x4x4 from the naive scheme for
        --post-search-seconds; the --post-schemes walks with the lowest verified best rank are kept
        (ranks 47-50 typically).
-    2. Complexity minimizer: rank-preserving flip walks (philox-lists mode) on those schemes,
-       --post-launches launches of --post-iterations steps; flips/s and complexities.
+    2. Complexity minimizer: rank-preserving flip walks (fast mode, one thread per walk) on those
+       schemes, --post-launches launches of --post-iterations steps; flips/s and complexities.
     3. Additions reducer: --post-reducers reducers per scheme on the minimized schemes, one GPU
        launch per rank group; reducer runs/s and addition counts.
     The addition counts are the reference's for the same scheme and seed (tests/test_gpu_reducer.py
@@ -519,9 +519,9 @@ def post_arm(args):
     rec.best_m[:] = ranks
     c0 = np.array([sum(bin(int(x)).count("1") for x in rec.fac[w, :, :ranks[w]].ravel()) for w in range(S)],
                   np.int64) - 2 * ranks - nn[2]
-    eng = fg.Engine(S, cap, "z2", "philox", args.seed, args.post_iterations, 10**9, 0.0, 0.0)
+    # fast mode: the minimizer's flips with the fast walk's stream and pair order, one thread per walk
+    eng = fg.Engine(S, cap, "z2", "fast", args.seed, args.post_iterations, 10**9, 0.0, 0.0)
     eng.set_records(rec)
-    eng.rebuild_lists()
     bc = c0.astype(np.int32)
     bc = eng.minimize(bc)  # first launch (warm-up, counted in the complexities)
     t = time.perf_counter()

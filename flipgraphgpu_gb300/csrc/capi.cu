@@ -1088,9 +1088,23 @@ fg_status fg_minimize(fg_handle *h, int32_t *best_complexity) {
     FG_CUDA(cudaSetDevice(h->dev));
     const int S = h->B.S;
     FG_CUDA(cudaMemcpyAsync(h->d_bestC, best_complexity, S * 4, cudaMemcpyHostToDevice, h->stream));
-    if (!uses_lists(h)) return fail(FG_ERR_ARG, "the minimizer runs in a list mode");
-    FG_CUDA(launch_minimize(h->cfg.ring, h->B, h->P, h->cfg.mode == FG_MODE_REFERENCE ? RNG_XORWOW : RNG_PHILOX,
-                            h->wpb, h->grid, h->d_bestC, h->stream));
+    if (h->cfg.mode == FG_MODE_FAST && h->cfg.ring == FG_RING_Z2) {  // per shape segment, the walk's kernel choice
+        for (const Segment &g : h->segs) {
+            if (g.nnmax > 56) return fail(FG_ERR_CAPACITY, "fast mode holds factors of at most 56 entries");
+            int kind, lanes, wpb;
+            segment_kernel(h, g, kind, lanes, wpb);
+            if (kind == FG_FAST_THREAD)
+                FG_CUDA(launch_minimize_simt(h->B, h->P, g.first, g.count, g.scap, g.wide, wpb, h->sms, h->d_bestC,
+                                             h->stream));
+            else
+                FG_CUDA(launch_minimize_group(h->B, h->P, g.first, g.count, g.scap, g.wide, h->sms, h->d_bestC,
+                                              h->stream));
+        }
+    } else {
+        if (!uses_lists(h)) return fail(FG_ERR_ARG, "the minimizer runs in a list mode or the Z2 fast mode");
+        FG_CUDA(launch_minimize(h->cfg.ring, h->B, h->P, h->cfg.mode == FG_MODE_REFERENCE ? RNG_XORWOW : RNG_PHILOX,
+                                h->wpb, h->grid, h->d_bestC, h->stream));
+    }
     FG_CUDA(cudaMemcpyAsync(best_complexity, h->d_bestC, S * 4, cudaMemcpyDeviceToHost, h->stream));
     FG_CUDA(cudaStreamSynchronize(h->stream));
     return FG_OK;

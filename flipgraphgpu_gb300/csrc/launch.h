@@ -27,6 +27,13 @@ int occupancy_walk(int ring, int cap, int rng, int wpb);
 // factor slots per walk in shared memory; wide = 64-bit words (nn > 24).
 cudaError_t launch_walk_simt(const DevBatch &B, const WalkParams &P, int first, int count, int scap, int wide,
                              int wpb, int sms, cudaStream_t s);
+// Fast mode complexity minimizer (minimizeKernel), one thread per walk; bestC[w] is the
+// walk's best complexity so far, lowered in place.
+cudaError_t launch_minimize_simt(const DevBatch &B, const WalkParams &P, int first, int count, int scap, int wide,
+                                 int wpb, int sms, int32_t *bestC, cudaStream_t s);
+// The same minimizer, one warp per walk (for few walks or large schemes).
+cudaError_t launch_minimize_group(const DevBatch &B, const WalkParams &P, int first, int count, int scap, int wide,
+                                  int sms, int32_t *bestC, cudaStream_t s);
 // Resize meta-operators (one warp per walk, Z2, cap 352) and the best-rank table's copies.
 cudaError_t launch_resize(int ring, const DevBatch &B, const WalkParams &P, int rng, double p, int wpb, int grid,
                           cudaStream_t s);

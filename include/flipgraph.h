@@ -172,7 +172,9 @@ fg_status fg_run(fg_handle *h, int launches, fg_stats *stats);
 /* One launch of the complexity minimizer's flip walk (minimizeKernel,
  * complexity_minimizer.cu:190-214): checkReduce=false flips; best_* records
  * receive the lowest-complexity scheme seen.  best_complexity [walks] is
- * read (the running bests) and written. */
+ * read (the running bests) and written.  List modes: the reference's walk
+ * (one warp per walk); Z2 fast mode: the fast walk's stream and pair order,
+ * one thread per walk. */
 fg_status fg_minimize(fg_handle *h, int32_t *best_complexity);
 
 /* Exact Brent-equation check of every walk's current (best=0) or best

@@ -400,3 +400,28 @@ def test_autotune_and_graph_replay_keep_trajectories():
             assert eng.validate().all()
     for f in ("n", "m", "fac", "flips", "best_rank", "best_m", "best_fac", "rng_pos", "status"):
         assert np.array_equal(getattr(out[0], f), getattr(out[1], f)), f
+
+
+@pytest.mark.parametrize("shape,S", [((3, 3, 3), 256), ((4, 4, 4), 256), ((2, 4, 8), 256), ((3, 3, 3), 10240)])
+def test_fast_minimize_vs_oracle(shape, S):
+    """The fast-mode minimizer (warp per walk for few walks, thread per walk for many; Philox,
+    implicit pairs) against the oracle's fast-mode minimizeKernel: best complexities, schemes
+    and stream positions."""
+    n1, n2, n3 = shape
+    cap, seed = n1 * n2 * n3, 515
+    with fg.Engine(S, cap, "z2", "fast", seed, 600, 100000) as eng:
+        eng.init_naive(n1, n2, n3)
+        eng.run(1)
+        rec0 = eng.records()
+        best0 = O.complexity("z2", rec0.n, rec0.m, rec0.fac)
+        bc = eng.minimize(best0.copy())
+        rec = eng.records()
+        assert eng.validate().all() and eng.validate(best=True).all()
+    b = batch_from(rec0)
+    obc = best0.copy()
+    O.minimize(b, b.cfg("fast", iterations=600, plus_iterations=100000, seed=seed), obc)
+    assert np.array_equal(bc, obc)
+    assert (bc <= best0).all() and (bc < best0).any()
+    for f in ("m", "fac", "best_m", "best_fac", "rng_pos", "status"):
+        a, o = getattr(rec, f), getattr(b, f)
+        assert np.array_equal(a, o), f
