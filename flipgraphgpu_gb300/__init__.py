@@ -311,7 +311,7 @@ class Engine:
 
 class ReducerConfig(ctypes.Structure):
     _fields_ = [("count", ctypes.c_int32), ("schemes", ctypes.c_int32), ("seed", ctypes.c_uint64),
-                ("device", ctypes.c_int32)]
+                ("device", ctypes.c_int32), ("threads", ctypes.c_int32)]
 
 
 MODE_NAMES = {0: "g", 1: "ga", 2: "gr", 3: "gi", 4: "wr", 5: "mix", 6: "rnd"}
@@ -330,11 +330,11 @@ class Reducer:
 
     coef: int8 [schemes][3][m][64] coefficients (U rows, V rows, W rows)."""
 
-    def __init__(self, n, m, coef, count=32, schemes=1, seed=1, device=0):
+    def __init__(self, n, m, coef, count=32, schemes=1, seed=1, device=0, threads=0):
         self.lib = library()
         self.count, self.m, self.n = count, m, tuple(n)
         self.coef = np.ascontiguousarray(coef, np.int8).reshape(schemes, 3, m, 64)
-        self.cfg = ReducerConfig(count, schemes, seed, device)
+        self.cfg = ReducerConfig(count, schemes, seed, device, threads)
         self.h = ctypes.c_void_p()
         _check(self.lib.fg_reducer_create(ctypes.byref(self.cfg), n[0], n[1], n[2], m, _ptr(self.coef),
                                           ctypes.byref(self.h)))

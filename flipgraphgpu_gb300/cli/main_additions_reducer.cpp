@@ -288,7 +288,8 @@ private:
                 for (int t = 0; t < m_; t++)
                     for (int i = 0; i < scheme_.nn[c]; i++)
                         coef[(((size_t)s * 3 + c) * m_ + t) * 64 + i] = (int8_t)scheme_.coefficient(c, t, i);
-        fg_reducer_config cfg{count_, schemesCount_, (uint64_t)(long long)seed_, 0};
+        // One scheme and few reducers leave most SMs idle: wide blocks (results unchanged).
+        fg_reducer_config cfg{count_, schemesCount_, (uint64_t)(long long)seed_, 0, 512};
         check(fg_reducer_create(&cfg, n1_, n2_, n3_, m_, coef.data(), &h_), "fg_reducer_create");
         for (int c = 0; c < 3; c++) {
             best_[c] = ReducerView();

@@ -28,10 +28,15 @@ namespace {
 
 enum { GREEDY = 0, GREEDY_ALT = 1, GREEDY_RANDOM = 2, GREEDY_INTER = 3, WEIGHTED_RANDOM = 4, MIX = 5, RANDOM = 6 };
 
-// Threads per reducer block.  The shared-memory tables of a 4x4x4 rank-47 scheme (160 KB)
-// leave one block per SM, so wider blocks hide the pair counting's latency: 4,071 runs/s
-// at 128 threads, 5,557 at 256, 5,854 at 512 (8,192 reducers on one scheme).
-constexpr int kReduceThreads = 512;
+// Threads per reducer block (fg_reducer_config::threads, 0 = 128).  Many reducers over many
+// schemes run best at 128 (post-search workload, 4,096 schemes x 32 reducers: 13.6 K runs/s,
+// 10.6 K at 512); many reducers over one 4x4x4 rank-47 scheme at 512 (4,071 runs/s at 128,
+// 5,557 at 256, 5,854 at 512).  The count never changes a result.
+int reduce_threads(int requested) {
+    if (requested <= 0) return 128;
+    if (requested > 1024) return 1024;
+    return (requested + 31) / 32 * 32;
+}
 
 __constant__ int c_modes[15] = {GREEDY_INTER, GREEDY_INTER, GREEDY_INTER, GREEDY_INTER, GREEDY_INTER,
                                 GREEDY_INTER, GREEDY_INTER, GREEDY_INTER, GREEDY_ALT,   GREEDY_ALT,
@@ -661,7 +666,7 @@ fg_status fg_reducer_run(fg_reducer *h, int independent, const int32_t *best_fre
     A.D = h->D;
     A.gscratch = h->d_scratch;
     A.slotBytes = h->slotBytes;
-    k_reduce<<<h->d_scratch ? h->slots : A.count, kReduceThreads, h->smem>>>(A);
+    k_reduce<<<h->d_scratch ? h->slots : A.count, reduce_threads(h->cfg.threads), h->smem>>>(A);
     RCUDA(cudaGetLastError());
     RCUDA(cudaMemcpy(out_counts, h->d_out, 4 * 13 * (size_t)A.count, cudaMemcpyDeviceToHost));
     if (out_scale) RCUDA(cudaMemcpy(out_scale, h->d_scale, 4 * 3 * (size_t)A.count, cudaMemcpyDeviceToHost));
@@ -813,7 +818,7 @@ fg_status fg_reducer_run_noalloc(const fg_reducer_config *cfg, int n1, int n2, i
     A.D = D;
     A.gscratch = nullptr;
     A.slotBytes = 0;
-    k_reduce<<<A.count, kReduceThreads, smem>>>(A);
+    k_reduce<<<A.count, reduce_threads(cfg->threads), smem>>>(A);
     RCUDA(cudaGetLastError());
     RCUDA(cudaMemcpy(out_counts, base + oOut, (size_t)4 * 13 * A.count, cudaMemcpyDeviceToHost));
     if (out_scale) RCUDA(cudaMemcpy(out_scale, base + oScale, (size_t)4 * 3 * A.count, cudaMemcpyDeviceToHost));

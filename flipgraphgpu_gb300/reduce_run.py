@@ -21,6 +21,7 @@ def main():
     ap.add_argument("--count", type=int, default=4096)
     ap.add_argument("--launches", type=int, default=2)
     ap.add_argument("--seed", type=int, default=1)
+    ap.add_argument("--threads", type=int, default=512, help="threads per reducer block (0: the library's 128)")
     a = ap.parse_args()
     tok = [int(x) for x in open(a.scheme).read().split()]
     n, m = tok[:3], tok[3]
@@ -31,7 +32,7 @@ def main():
         for t in range(m):
             coef[0, c, t, :nn[c]] = tok[p:p + nn[c]]
             p += nn[c]
-    red = Reducer(n, m, coef, count=a.count, schemes=1, seed=a.seed)
+    red = Reducer(n, m, coef, count=a.count, schemes=1, seed=a.seed, threads=a.threads)
     red.run()  # warm-up
     t = time.perf_counter()
     best = None

@@ -329,6 +329,8 @@ typedef struct {
     int32_t schemes;  /* --schemes-count: reducer r reduces scheme r % schemes */
     uint64_t seed;    /* --seed */
     int32_t device;
+    int32_t threads;  /* threads per reducer block: 0 = 128; wider helps when few reducers (one
+                         scheme, large pair tables) leave the SMs half idle, results unchanged */
 } fg_reducer_config;
 
 typedef struct fg_reducer fg_reducer;
