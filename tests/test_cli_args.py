@@ -60,3 +60,27 @@ def test_missing_input_files():
     assert 'Unable to open file "/nonexistent/x.txt"' in out and rc == 255
     rc, out, _ = run("additions_reducer", "-i", "/nonexistent/x.txt")
     assert 'Unable to open file "/nonexistent/x.txt"' in out and rc == 255
+
+
+def test_ring_and_input_checks():
+    rc, _, err = run("flip_graph", "-n1", "3", "-n2", "3", "-n3", "3", "--ring", "ZQ")
+    assert 'unknown ring "ZQ"' in err
+    rc, out, _ = run("flip_graph", "-n1", "3", "-n2", "3", "-n3", "3", "--ring", "ZB", "--input-path", "x.json")
+    assert "the ZB ring starts from the naive scheme" in out and rc == 255
+    rc, out, _ = run("flip_graph", "-n1", "3", "-n2", "3", "-n3", "3", "--input-path", "/nonexistent/x.txt",
+                     "--ring", "Z2")
+    assert 'Unable to open file "/nonexistent/x.txt"' in out and rc == 255
+    rc, out, _ = run("flip_graph", "--help")
+    for flag in ["[--gauss-probability 0.0]", "[--ternary-sandwiching 0]", "[--max-launches 0]"]:
+        assert flag in out, flag
+
+
+def test_json_input_errors(tmp_path):
+    bad = tmp_path / "bad.json"
+    bad.write_text('{"n": [2, 2, 2], "u": [[1, 0, 0, 0]], "v": [], "w": []}')
+    rc, out, _ = run("complexity_minimizer", "--input-path", str(bad))
+    assert '"v" has 0 rows' in out and rc == 255
+    empty = tmp_path / "empty"
+    empty.mkdir()
+    rc, out, _ = run("additions_reducer", "-i", str(empty))
+    assert "no .json files" in out and rc == 255
