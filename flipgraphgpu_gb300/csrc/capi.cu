@@ -704,7 +704,8 @@ fg_status fg_rebuild_lists(fg_handle *h) {
 }
 
 fg_status fg_set_fast_kernel(fg_handle *h, int kernel, int lanes) {
-    if (!h || kernel < -1 || kernel > FG_FAST_WARP || !(lanes == 0 || lanes == 4 || lanes == 8 || lanes == 16 || lanes == 32))
+    if (!h) return fail(FG_ERR_ARG, "null handle");
+    if (kernel < -1 || kernel > FG_FAST_WARP || !(lanes == 0 || lanes == 4 || lanes == 8 || lanes == 16 || lanes == 32))
         return fail(FG_ERR_ARG, "kernel in -1..2, lanes 0, 4, 8, 16 or 32");
     h->fastKernel = kernel;
     h->groupLanes = lanes;
@@ -873,20 +874,45 @@ fg_status fg_set_records(fg_handle *h, const fg_records *rec) {
     if (!h || !rec || !rec->n || !rec->m || !rec->fac) return fail(FG_ERR_ARG, "null argument");
     // The list modes take the FlipSets from the records; the fast modes keep no lists.
     if (uses_lists(h) && (!rec->list_size || !rec->list_pairs)) return fail(FG_ERR_ARG, "list modes need the lists");
+    if (h->cfg.ring == FG_RING_ZT && (!rec->sgn || !rec->valid)) return fail(FG_ERR_ARG, "ZT records need sgn and valid");
+    if (h->cfg.ring == FG_RING_ZB && (!rec->sgn || !rec->fac2)) return fail(FG_ERR_ARG, "ZB records need sgn and fac2");
     FG_CUDA(cudaSetDevice(h->dev));
     const int S = h->B.S, cap = h->B.cap;
     size_t nf = (size_t)S * 3 * cap;
+    // Everything the kernels index by is checked before anything is copied, so a
+    // rejected record leaves the handle as it was: sizes (the matrix entries index
+    // factor bits; best sizes only where resizing reads them), ranks (slots) and, in
+    // the list modes, every pair (two distinct slots below the rank).
+    auto shape_ok = [](const int32_t *n) {
+        for (int c = 0; c < 3; c++)
+            if (n[c] <= 0 || n[c] > 64) return false;
+        return n[0] * n[1] <= 64 && n[1] * n[2] <= 64 && n[2] * n[0] <= 64;
+    };
+    for (int w = 0; w < S; w++) {
+        if (!shape_ok(rec->n + w * 3) || (h->B.best_n && rec->best_n && !shape_ok(rec->best_n + w * 3)))
+            return fail(FG_ERR_ARG, "record " + std::to_string(w) + ": matrix sizes out of range");
+        const int m = rec->m[w], bm = rec->best_m ? rec->best_m[w] : m;
+        if (m < 0 || m > cap || bm < 0 || bm > cap)
+            return fail(FG_ERR_CAPACITY, "record " + std::to_string(w) + ": rank exceeds cap");
+        if (!uses_lists(h)) continue;
+        for (int c = 0; c < 3; c++) {
+            const int size = rec->list_size[w * 3 + c];
+            if (size < 0 || size > kListCap) return fail(FG_ERR_CAPACITY, "record " + std::to_string(w) + ": list size");
+            const uint32_t *pairs = rec->list_pairs + ((size_t)w * 3 + c) * kListCap;
+            for (int q = 0; q < size; q++) {
+                const int a = (int)(pairs[q] >> 16), b = (int)(pairs[q] & 0xFFFFu);
+                if (a >= m || b >= m || a == b)
+                    return fail(FG_ERR_ARG, "record " + std::to_string(w) + ": list pair outside the scheme");
+            }
+        }
+    }
     std::vector<WalkHeader> hdr(S);
     FG_CUDA(cudaMemcpy(hdr.data(), h->B.hdr, sizeof(WalkHeader) * S, cudaMemcpyDeviceToHost));
     for (int w = 0; w < S; w++) {
         WalkHeader &o = hdr[w];
         for (int c = 0; c < 3; c++) o.n[c] = rec->n[w * 3 + c];
         o.m = rec->m[w];
-        if (o.m < 0 || o.m > cap) return fail(FG_ERR_CAPACITY, "record rank exceeds cap");
-        for (int c = 0; c < 3; c++) {
-            o.list_size[c] = rec->list_size ? rec->list_size[w * 3 + c] : 0;
-            if (o.list_size[c] < 0 || o.list_size[c] > kListCap) return fail(FG_ERR_CAPACITY, "list size");
-        }
+        for (int c = 0; c < 3; c++) o.list_size[c] = uses_lists(h) ? rec->list_size[w * 3 + c] : 0;
         o.flips = rec->flips ? rec->flips[w] : 0;
         o.best_rank = rec->best_rank ? rec->best_rank[w] : o.m;
         o.best_m = rec->best_m ? rec->best_m[w] : o.m;
@@ -906,14 +932,12 @@ fg_status fg_set_records(fg_handle *h, const fg_records *rec) {
     FG_CUDA(cudaMemcpy(h->B.best_fac, rec->best_fac ? rec->best_fac : rec->fac, nf * sizeof(uint64_t),
                        cudaMemcpyHostToDevice));
     if (h->cfg.ring == FG_RING_ZT) {
-        if (!rec->sgn || !rec->valid) return fail(FG_ERR_ARG, "ZT records need sgn and valid");
         FG_CUDA(cudaMemcpy(h->B.sgn, rec->sgn, nf * 8, cudaMemcpyHostToDevice));
         FG_CUDA(cudaMemcpy(h->B.valid, rec->valid, nf, cudaMemcpyHostToDevice));
         FG_CUDA(cudaMemcpy(h->B.best_sgn, rec->best_sgn ? rec->best_sgn : rec->sgn, nf * 8, cudaMemcpyHostToDevice));
         FG_CUDA(cudaMemcpy(h->B.best_valid, rec->best_valid ? rec->best_valid : rec->valid, nf, cudaMemcpyHostToDevice));
     }
     if (h->cfg.ring == FG_RING_ZB) {
-        if (!rec->sgn || !rec->fac2) return fail(FG_ERR_ARG, "ZB records need sgn and fac2");
         FG_CUDA(cudaMemcpy(h->B.sgn, rec->sgn, nf * 8, cudaMemcpyHostToDevice));
         FG_CUDA(cudaMemcpy(h->B.fac2, rec->fac2, nf * 8, cudaMemcpyHostToDevice));
         FG_CUDA(cudaMemcpy(h->B.best_sgn, rec->best_sgn ? rec->best_sgn : rec->sgn, nf * 8, cudaMemcpyHostToDevice));
@@ -1087,7 +1111,7 @@ fg_status fg_minimize(fg_handle *h, int32_t *best_complexity) {
     if (!h->ready) return fail(FG_ERR_STATE, "records not initialised");
     FG_CUDA(cudaSetDevice(h->dev));
     const int S = h->B.S;
-    FG_CUDA(cudaMemcpyAsync(h->d_bestC, best_complexity, S * 4, cudaMemcpyHostToDevice, h->stream));
+    FG_CUDA(cudaMemcpyAsync(h->d_bestC, best_complexity, (size_t)S * 4, cudaMemcpyHostToDevice, h->stream));
     if (h->cfg.mode == FG_MODE_FAST && h->cfg.ring == FG_RING_Z2) {  // per shape segment, the walk's kernel choice
         for (const Segment &g : h->segs) {
             if (g.nnmax > 56) return fail(FG_ERR_CAPACITY, "fast mode holds factors of at most 56 entries");
@@ -1105,7 +1129,7 @@ fg_status fg_minimize(fg_handle *h, int32_t *best_complexity) {
         FG_CUDA(launch_minimize(h->cfg.ring, h->B, h->P, h->cfg.mode == FG_MODE_REFERENCE ? RNG_XORWOW : RNG_PHILOX,
                                 h->wpb, h->grid, h->d_bestC, h->stream));
     }
-    FG_CUDA(cudaMemcpyAsync(best_complexity, h->d_bestC, S * 4, cudaMemcpyDeviceToHost, h->stream));
+    FG_CUDA(cudaMemcpyAsync(best_complexity, h->d_bestC, (size_t)S * 4, cudaMemcpyDeviceToHost, h->stream));
     FG_CUDA(cudaStreamSynchronize(h->stream));
     return FG_OK;
 }
@@ -1143,14 +1167,15 @@ fg_status fg_philox_blocks(const uint32_t *ctr, int count, uint32_t key0, uint32
     if (count <= 0 || !ctr || !out) return fail(FG_ERR_ARG, "bad philox arguments");
     FG_CUDA(cudaSetDevice(device));
     uint4 *dc = nullptr, *dout = nullptr;
-    FG_CUDA(cudaMalloc(&dc, count * 16));
-    if (cudaMalloc(&dout, count * 16) != cudaSuccess) { cudaFree(dc); return fail(FG_ERR_CUDA, "allocation"); }
-    cudaError_t e = cudaMemcpy(dc, ctr, count * 16, cudaMemcpyHostToDevice);
+    const size_t bytes = (size_t)count * 16;
+    FG_CUDA(cudaMalloc(&dc, bytes));
+    if (cudaMalloc(&dout, bytes) != cudaSuccess) { cudaFree(dc); return fail(FG_ERR_CUDA, "allocation"); }
+    cudaError_t e = cudaMemcpy(dc, ctr, bytes, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) {
         k_philox<<<(count + 127) / 128, 128>>>(dc, count, key0, key1, dout);
         e = cudaGetLastError();
     }
-    if (e == cudaSuccess) e = cudaMemcpy(out, dout, count * 16, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(out, dout, bytes, cudaMemcpyDeviceToHost);
     cudaFree(dc);
     cudaFree(dout);
     if (e != cudaSuccess) return fail(FG_ERR_CUDA, cudaGetErrorString(e));

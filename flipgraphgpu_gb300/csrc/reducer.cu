@@ -656,6 +656,7 @@ fg_status fg_reducer_run(fg_reducer *h, int independent, const int32_t *best_fre
     for (int c = 0; c < 3; c++) {
         A.best_fresh[c] = best_fresh ? best_fresh[c] : 0;
         if (A.best_fresh[c] < 0 || A.best_fresh[c] > 500) return rfail(FG_ERR_ARG, "best fresh count out of range");
+        if (A.best_fresh[c] > 0 && !best_vars) return rfail(FG_ERR_ARG, "best_vars is null");
         for (int q = 0; q < 2 * A.best_fresh[c]; q++) bv[c * 1000 + q] = (int16_t)best_vars[c * 1000 + q];
     }
     RCUDA(cudaMemcpy(h->d_best, bv.data(), bv.size() * 2, cudaMemcpyHostToDevice));

@@ -283,6 +283,38 @@ def test_validate_matches_oracle_on_corrupted_schemes():
     assert not got[::2].any() and got[1::2].all()
 
 
+@pytest.mark.parametrize("ring", ["z2", "zt"])
+def test_malformed_records_are_rejected_before_any_copy(ring):
+    """A record whose sizes, ranks or FlipSet pairs fall outside the scheme is refused on
+    the host with a message, and the handle keeps its state: the next launch is the one
+    an untouched handle makes."""
+    with fg.Engine(8, 27, ring, "reference", 5, 300, 100) as eng, \
+            fg.Engine(8, 27, ring, "reference", 5, 300, 100) as twin:
+        for e in (eng, twin):
+            e.init_naive(3, 3, 3)
+            e.run(1)
+        good = eng.records()
+        cases = []
+        r = eng.records(); r.list_pairs[3, 1, 0] = (30 << 16) | 2; r.list_size[3, 1] = max(r.list_size[3, 1], 1)
+        cases.append(("pair above the rank", r))
+        r = eng.records(); r.list_pairs[2, 0, 0] = (4 << 16) | 4; r.list_size[2, 0] = max(r.list_size[2, 0], 1)
+        cases.append(("pair of one slot", r))
+        r = eng.records(); r.list_size[0, 2] = fg.LIST_CAP + 1; cases.append(("list size", r))
+        r = eng.records(); r.m[5] = 28; cases.append(("rank above cap", r))
+        r = eng.records(); r.best_m[6] = -1; cases.append(("negative best rank", r))
+        r = eng.records(); r.n[1] = (0, 3, 3); cases.append(("empty matrix", r))
+        r = eng.records(); r.n[1] = (9, 9, 1); cases.append(("81 entries", r))
+        for name, bad in cases:
+            with pytest.raises(fg.FlipGraphError):
+                eng.set_records(bad)
+            assert fg.library().fg_last_error(), name
+        for e in (eng, twin):
+            e.run(1)
+        a, b = eng.records(), twin.records()
+        compare_records(a, b, "after rejected records")
+        assert not np.array_equal(a.fac, good.fac)  # the walks did move
+
+
 def planted_gauss(rec, rng):
     """Plants in every walk a zero-sum group (a, x_1, c), ..., (a, x_k, c), (a, x_1 ^ ... ^ x_k, c)
     (k = 2..4) at random positions: the scheme stays exact and the Gauss reduction has a
