@@ -48,6 +48,17 @@ class _Records(ctypes.Structure):
                  "fac2", "best_fac2")]
 
 
+# Element type and per-walk shape of every records field ("cap": the handle's slot count).
+_FIELD_LAYOUT = {
+    "n": (np.int32, (3,)), "m": (np.int32, ()), "fac": (np.uint64, (3, "cap")), "sgn": (np.uint64, (3, "cap")),
+    "valid": (np.uint8, (3, "cap")), "list_size": (np.int32, (3,)), "list_pairs": (np.uint32, (3, LIST_CAP)),
+    "flips": (np.int32, ()), "best_rank": (np.int32, ()), "best_m": (np.int32, ()),
+    "best_fac": (np.uint64, (3, "cap")), "best_sgn": (np.uint64, (3, "cap")), "best_valid": (np.uint8, (3, "cap")),
+    "rng_pos": (np.int64, ()), "status": (np.int32, ()), "best_n": (np.int32, (3,)),
+    "fac2": (np.uint64, (3, "cap")), "best_fac2": (np.uint64, (3, "cap")),
+}
+
+
 class Stats(ctypes.Structure):
     _fields_ = [("flips", ctypes.c_uint64), ("verified_flips", ctypes.c_uint64), ("walks_valid", ctypes.c_int32),
                 ("walks_failed", ctypes.c_int32), ("min_rank", ctypes.c_int32), ("min_best_rank", ctypes.c_int32),
@@ -283,12 +294,29 @@ class Engine:
         return {"m": m, "best_rank": best, "best_m": best_m, "flips_since_drop": since, "flips": flips,
                 "valid": valid.astype(bool)}
 
+    def _match(self, rec):
+        """The library reads and writes every array of `rec` at this handle's sizes."""
+        if (rec.walks, rec.cap, rec.ring) != (self.walks, self.cap, self.ring):
+            raise ValueError(f"records for {rec.walks} walks, cap {rec.cap}, ring {rec.ring}; "
+                             f"the engine has {self.walks}, {self.cap}, {self.ring}")
+        for f, _ in Records.FIELDS:
+            a = getattr(rec, f)
+            if a is None:
+                continue
+            dtype, per_walk = _FIELD_LAYOUT[f]
+            shape = (self.walks,) + tuple(self.cap if d == "cap" else d for d in per_walk)
+            if not (a.flags.c_contiguous and a.dtype == dtype and a.shape == shape):
+                raise ValueError(f"records field {f}: contiguous {np.dtype(dtype).name} {list(shape)} expected, "
+                                 f"got {a.dtype.name} {list(a.shape)}")
+
     def set_records(self, rec):
+        self._match(rec)
         c = rec._c()
         _check(self.lib.fg_set_records(self.h, ctypes.byref(c)))
 
     def records(self, into=None):
         rec = into if into is not None else Records(self.walks, self.cap, self.ring)
+        self._match(rec)
         c = rec._c()
         _check(self.lib.fg_get_records(self.h, ctypes.byref(c)))
         return rec
