@@ -155,7 +155,12 @@ fg_status fg_init_naive_shapes(fg_handle *h, const int32_t *shapes);
  * initializeCopyKernel, flip_graph.cu:201-224,459-470, after the host has
  * parsed and replicated the schemes).  rng_pos is not read: streams keep
  * their position.  The fast and learned modes keep no lists: list_size and
- * list_pairs may be NULL there and are not copied. */
+ * list_pairs may be NULL there and are not copied.  Before anything is
+ * copied every walk is checked: sizes positive with n1*n2, n2*n3, n3*n1 <= 64
+ * (best_n too when resizing), m and best_m in [0, cap], and in the list modes
+ * list sizes in [0, 500] with every pair two distinct slots below m.  A
+ * failing record returns FG_ERR_ARG / FG_ERR_CAPACITY naming the walk, and
+ * the handle keeps its state. */
 fg_status fg_set_records(fg_handle *h, const fg_records *rec);
 
 /* Copies the handle's records to host buffers (the reference reads managed
