@@ -100,7 +100,7 @@ typedef struct {
     int32_t *n;           /* [walks][3] */
     int32_t *m;           /* [walks] current rank */
     uint64_t *fac;        /* [walks][3][cap] */
-    uint64_t *sgn;        /* ZT only, else NULL */
+    uint64_t *sgn;        /* ZT and ZB, else NULL */
     uint8_t *valid;       /* ZT only, else NULL */
     int32_t *list_size;   /* [walks][3] */
     uint32_t *list_pairs; /* [walks][3][500] */
@@ -108,7 +108,7 @@ typedef struct {
     int32_t *best_rank;   /* [walks] */
     int32_t *best_m;      /* [walks] */
     uint64_t *best_fac;   /* [walks][3][cap] */
-    uint64_t *best_sgn;   /* ZT only */
+    uint64_t *best_sgn;   /* ZT and ZB */
     uint8_t *best_valid;  /* ZT only */
     int64_t *rng_pos;     /* [walks] draws consumed since seeding */
     int32_t *status;      /* [walks] FG_WALK_* bits */

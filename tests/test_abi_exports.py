@@ -43,3 +43,37 @@ def test_library_answers_without_a_device():
     h = ctypes.c_void_p()
     assert lib.fg_create(None, ctypes.byref(h)) != 0
     assert lib.fg_reducer_create(None, 3, 3, 3, 23, None, ctypes.byref(h)) != 0
+
+
+C_TYPES = {"int32_t": ctypes.c_int32, "uint64_t": ctypes.c_uint64, "int64_t": ctypes.c_int64, "double": ctypes.c_double,
+           "float": ctypes.c_float, "uint32_t": ctypes.c_uint32}
+
+
+def declared_structs():
+    """{typedef name: [(field, C type or 'pointer')]} for every `typedef struct { ... } name;`."""
+    text = re.sub(r"/\*.*?\*/", " ", open(HEADER).read(), flags=re.S)
+    out = {}
+    for body, name in re.findall(r"typedef struct\s*\{(.*?)\}\s*(\w+)\s*;", text, flags=re.S):
+        fields = []
+        for decl in body.split(";"):
+            decl = decl.strip()
+            if not decl:
+                continue
+            m = re.fullmatch(r"([a-z0-9_]+)\s*(\*?)\s*(\w+)", decl)
+            assert m, decl
+            fields.append((m.group(3), "pointer" if m.group(2) else m.group(1)))
+        out[name] = fields
+    return out
+
+
+@pytest.mark.parametrize("c_name,py_name", [("fg_config", "Config"), ("fg_records", "_Records"),
+                                            ("fg_stats", "Stats"), ("fg_reducer_config", "ReducerConfig")])
+def test_ctypes_structs_mirror_the_header(c_name, py_name):
+    """The Python mirror passes these structs by pointer: every field, in order, with the
+    header's type (a missing trailing field would let the library read past the struct)."""
+    c_fields = declared_structs()[c_name]
+    py_fields = getattr(fg, py_name)._fields_
+    assert [n for n, _ in py_fields] == [n for n, _ in c_fields]
+    for (name, ctype), (_, pytype) in zip(c_fields, py_fields):
+        want = ctypes.c_void_p if ctype == "pointer" else C_TYPES[ctype]
+        assert pytype == want, (c_name, name, ctype, pytype)
