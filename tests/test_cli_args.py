@@ -84,3 +84,18 @@ def test_json_input_errors(tmp_path):
     empty.mkdir()
     rc, out, _ = run("additions_reducer", "-i", str(empty))
     assert "no .json files" in out and rc == 255
+
+
+def test_ternary_input_flags_coefficients_outside_the_ring(tmp_path):
+    """A ZT text input with a coefficient outside {-1, 0, 1} is reported while it is read
+    (Addition::set, addition.cu:41-60), before any device work."""
+    import gzip
+    from helpers import GOLDEN
+    tokens = gzip.open(os.path.join(GOLDEN, "input_zt_333.txt.gz"), "rt").read().split()
+    head, body = tokens[:4], tokens[4:]
+    body[0] = "2"
+    src = tmp_path / "two.txt"
+    src.write_text("1\n" + " ".join(head) + "\n" + " ".join(body) + "\n")
+    rc, out, _ = run("flip_graph", "-n1", "3", "-n2", "3", "-n3", "3", "--input-path", str(src), "--ring", "ZT",
+                     "--schemes", "32", "--max-iterations", "10", "--max-launches", "1", "--path", str(tmp_path / "o"))
+    assert "invalid set (0, 2)" in out
