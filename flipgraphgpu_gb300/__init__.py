@@ -379,6 +379,15 @@ class Reducer:
         return {"additions": per[:, :, 0].copy(), "fresh": per[:, :, 1].copy(), "naive": per[:, :, 2].copy(),
                 "mode": per[:, :, 3].copy(), "draws": counts[:, 12].copy(), "scale": scale, "vars": vars_}
 
+    def flip(self, max_flips):
+        """--max-flips pass (fg_reducer_flip): schemes 1.. become scheme 0 after up to max_flips ternary
+        flips from their reducers' streams.  Returns (ranks [schemes], coef [schemes][3][m][64])."""
+        schemes = self.cfg.schemes
+        ranks = np.zeros(schemes, np.int32)
+        coef = np.zeros((schemes, 3, self.m, 64), np.int8)
+        _check(self.lib.fg_reducer_flip(self.h, int(max_flips), _ptr(ranks), _ptr(coef)))
+        return ranks, coef
+
     def close(self):
         if self.h:
             self.lib.fg_reducer_destroy(self.h)

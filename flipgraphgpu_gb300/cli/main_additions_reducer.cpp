@@ -6,7 +6,9 @@
 // Additive flag: --z2-input 1 reads the scheme without the integer validity
 // check, so schemes that are valid only modulo 2 can be reduced (the
 // reference rejects them, scheme_additions_reducer.cu:48-51).
-// Not supported: --max-flips > 0 (scheme perturbation between iterations).
+// --max-flips > 0: before every iteration after the first, schemes 1.. are
+// flipped copies of the input (fg_reducer_flip) and the best reducer is chosen
+// by its total over U, V and W (scheme_additions_reducer.cu:172-182,296-339).
 #include <algorithm>
 #include <chrono>
 #include <cstdio>
@@ -113,8 +115,8 @@ std::string modeName(int mode, float scale) {  // additions_reducer.cuh:183-204
 
 class SchemeAdditionsReducer {
 public:
-    SchemeAdditionsReducer(int count, int schemesCount, int seed, const std::string &out, bool z2input)
-        : count_(count), schemesCount_(schemesCount), seed_(seed), out_(out), z2input_(z2input) {
+    SchemeAdditionsReducer(int count, int schemesCount, int maxFlips, int seed, const std::string &out, bool z2input)
+        : count_(count), schemesCount_(schemesCount), maxFlips_(maxFlips), seed_(seed), out_(out), z2input_(z2input) {
         topCount_ = std::min(10, count);
         for (int c = 0; c < 3; c++)
             for (int j = 0; j < count; j++) indices_[c].push_back(j);
@@ -187,7 +189,7 @@ public:
         int noImprovements = 0;
         for (int iteration = 1; noImprovements < maxNoImprovements; iteration++) {
             auto t1 = Clock::now();
-            runIteration();
+            runIteration(iteration);
             bool improved = updateBest(startAdditions);
             auto t2 = Clock::now();
             times.push_back(std::chrono::duration_cast<std::chrono::milliseconds>(t2 - t1).count() / 1000.0);
@@ -248,25 +250,30 @@ private:
         return total;
     }
 
-    Expressions naive(int c) const {  // copySchemeToReducers (scheme_additions_reducer.cu:463-492)
+    Expressions naive(int c) const { return naiveOf(coef0_.data(), m_, c); }
+
+    // copySchemeToReducers (scheme_additions_reducer.cu:463-492) of a scheme given as
+    // coefficient rows [3][m_][64] with rank `rank` (a flipped scheme may have dropped rank).
+    Expressions naiveOf(const int8_t *coef, int rank, int c) const {
         Expressions x;
         const int nn = scheme_.nn[c];
+        auto at = [&](int cc, int t, int i) { return (int)coef[((size_t)cc * m_ + t) * 64 + i]; };
         if (c < 2) {
             x.real = nn;
-            for (int t = 0; t < m_; t++) {
+            for (int t = 0; t < rank; t++) {
                 std::vector<int> e;
                 for (int i = 0; i < nn; i++) {
-                    int v = scheme_.coefficient(c, t, i);
+                    int v = at(c, t, i);
                     if (v) e.push_back(v > 0 ? i + 1 : -(i + 1));
                 }
                 x.e.push_back(e);
             }
         } else {
-            x.real = m_;
+            x.real = rank;
             for (int i = 0; i < nn; i++) {
                 std::vector<int> e;
-                for (int t = 0; t < m_; t++) {
-                    int v = scheme_.coefficient(2, t, i);
+                for (int t = 0; t < rank; t++) {
+                    int v = at(2, t, i);
                     if (v) e.push_back(v > 0 ? t + 1 : -(t + 1));
                 }
                 x.e.push_back(e);
@@ -282,12 +289,17 @@ private:
     }
 
     void initialize() {  // scheme_additions_reducer.cu:234-258
+        coef0_.assign((size_t)3 * m_ * 64, 0);
+        for (int c = 0; c < 3; c++)
+            for (int t = 0; t < m_; t++)
+                for (int i = 0; i < scheme_.nn[c]; i++)
+                    coef0_[((size_t)c * m_ + t) * 64 + i] = (int8_t)scheme_.coefficient(c, t, i);
         std::vector<int8_t> coef((size_t)schemesCount_ * 3 * m_ * 64, 0);
-        for (int s = 0; s < schemesCount_; s++)
-            for (int c = 0; c < 3; c++)
-                for (int t = 0; t < m_; t++)
-                    for (int i = 0; i < scheme_.nn[c]; i++)
-                        coef[(((size_t)s * 3 + c) * m_ + t) * 64 + i] = (int8_t)scheme_.coefficient(c, t, i);
+        for (int s = 0; s < schemesCount_; s++) std::copy(coef0_.begin(), coef0_.end(), coef.begin() + (size_t)s * coef0_.size());
+        schemeCoef_ = coef;
+        schemeRanks_.assign(schemesCount_, m_);
+        bestCoef_ = coef0_;
+        bestRank_ = m_;
         // One scheme and few reducers leave most SMs idle: wide blocks (results unchanged).
         fg_reducer_config cfg{count_, schemesCount_, (uint64_t)(long long)seed_, 0, 512};
         check(fg_reducer_create(&cfg, n1_, n2_, n3_, m_, coef.data(), &h_), "fg_reducer_create");
@@ -321,7 +333,9 @@ private:
         std::cout << std::endl;
     }
 
-    void runIteration() {  // scheme_additions_reducer.cu:260-270 (independent: --max-flips 0)
+    void runIteration(int iteration) {  // reduceIteration, scheme_additions_reducer.cu:172-182
+        if (maxFlips_ > 0 && iteration > 1)
+            check(fg_reducer_flip(h_, maxFlips_, schemeRanks_.data(), schemeCoef_.data()), "fg_reducer_flip");
         int32_t fresh[3];
         std::vector<int32_t> vars(3 * 1000, 0);
         for (int c = 0; c < 3; c++) {
@@ -331,7 +345,8 @@ private:
         counts_.assign((size_t)count_ * 13, 0);
         scales_.assign((size_t)count_ * 3, 0);
         vars_.assign((size_t)count_ * 3 * 1000, 0);
-        check(fg_reducer_run(h_, 1, fresh, vars.data(), counts_.data(), scales_.data(), vars_.data()), "fg_reducer_run");
+        check(fg_reducer_run(h_, maxFlips_ == 0 ? 1 : 0, fresh, vars.data(), counts_.data(), scales_.data(), vars_.data()),
+              "fg_reducer_run");
     }
 
     ReducerView view(int r, int c) const {
@@ -367,8 +382,33 @@ private:
         return updated;
     }
 
+    int total(int r, int field) const {  // U + V + W of one counts field (0 additions, 1 fresh)
+        return counts_[(size_t)r * 13 + field] + counts_[(size_t)r * 13 + 4 + field] + counts_[(size_t)r * 13 + 8 + field];
+    }
+
+    bool updateBestTogether() {  // scheme_additions_reducer.cu:296-339: one reducer's U, V and W
+        std::partial_sort(indices_[0].begin(), indices_[0].begin() + topCount_, indices_[0].end(), [&](int a, int b) {
+            if (total(a, 0) != total(b, 0)) return total(a, 0) < total(b, 0);
+            return total(a, 1) < total(b, 1);
+        });
+        const int top = indices_[0][0];
+        const int additions = total(top, 0), freshVars = total(top, 1);
+        if (additions < reducedAdditions_ || (additions == reducedAdditions_ && freshVars < reducedFresh_)) {
+            for (int c = 0; c < 3; c++) {
+                best_[c] = view(top, c);
+                bestAdditions_[c] = best_[c].additions;
+                bestFresh_[c] = best_[c].fresh;
+            }
+            const int s = top % schemesCount_;  // the scheme this reducer reduced
+            bestCoef_.assign(schemeCoef_.begin() + (size_t)s * 3 * m_ * 64, schemeCoef_.begin() + (size_t)(s + 1) * 3 * m_ * 64);
+            bestRank_ = schemeRanks_[s];
+            return true;
+        }
+        return false;
+    }
+
     bool updateBest(int startAdditions) {  // scheme_additions_reducer.cu:384-404
-        bool updated = updateBestIndependent();
+        bool updated = maxFlips_ == 0 ? updateBestIndependent() : updateBestTogether();
         int additions = bestAdditions_[0] + bestAdditions_[1] + bestAdditions_[2];
         int freshVars = bestFresh_[0] + bestFresh_[1] + bestFresh_[2];
         if (!updated) return false;
@@ -405,7 +445,9 @@ private:
         std::cout << "| mode | naive | reduced | fresh | mode | naive | reduced | fresh | mode | naive | reduced | fresh | naive | reduced | fresh |" << std::endl;
         std::cout << "+------+-------+---------+-------+------+-------+---------+-------+------+-------+---------+-------+-------+---------+-------+" << std::endl;
         for (int i = 0; i < topCount_ && i < count_; i++) {
-            ReducerView v[3] = {view(indices_[0][i], 0), view(indices_[1][i], 1), view(indices_[2][i], 2)};
+            // --max-flips: the rows are whole reducers (scheme_additions_reducer.cu:353-354)
+            const int k = maxFlips_ > 0 ? 0 : 1, l = maxFlips_ > 0 ? 0 : 2;
+            ReducerView v[3] = {view(indices_[0][i], 0), view(indices_[k][i], 1), view(indices_[l][i], 2)};
             std::cout << "| ";
             for (int c = 0; c < 3; c++)
                 std::cout << std::setw(4) << modeName(v[c].mode, v[c].scale) << "   " << std::setw(5) << v[c].naive
@@ -436,8 +478,8 @@ private:
         f << "    \"z2\": false," << std::endl;
         f << "    \"complexity\": {\"naive\": " << naiveTotal << ", \"reduced\": " << reducedAdditions_ << "}," << std::endl;
         const char *names[3] = {"u", "v", "w"};
-        for (int c = 0; c < 3; c++) {
-            Expressions x = naive(c);
+        for (int c = 0; c < 3; c++) {  // the best reducer's own scheme ("m" stays the input's, as the reference writes)
+            Expressions x = naiveOf(bestCoef_.data(), bestRank_, c);
             for (int q = 0; q < best_[c].fresh; q++) x.replace(best_[c].vars[2 * q], best_[c].vars[2 * q + 1]);
             x.write(f, names[c], "    ");
             f << (c < 2 ? "," : "") << std::endl;
@@ -447,7 +489,7 @@ private:
         std::cout << "Reduced scheme saved to \"" << p.str() << "\"" << std::endl;
     }
 
-    int count_, schemesCount_, seed_;
+    int count_, schemesCount_, maxFlips_, seed_;
     std::string out_;
     bool z2input_;
     int topCount_ = 10;
@@ -460,6 +502,9 @@ private:
     int reducedAdditions_ = 0, reducedFresh_ = 0;
     std::vector<int32_t> counts_, vars_;
     std::vector<float> scales_;
+    std::vector<int8_t> coef0_, schemeCoef_, bestCoef_;  // input, every scheme of this iteration, the best's
+    std::vector<int32_t> schemeRanks_;
+    int bestRank_ = 0;
 };
 
 }  // namespace
@@ -496,11 +541,6 @@ int main(int argc, char *argv[]) {
         std::cout << inputError << std::endl;
         return -1;
     }
-    if (maxFlips > 0) {
-        std::cout << "Error: --max-flips > 0 (scheme perturbation between iterations) is not available in this engine"
-                  << std::endl;
-        return -1;
-    }
     std::cout << "Compiled configuration:" << std::endl;
     std::cout << "- max expressions count (U / V / W): " << kMaxRank << " / " << kMaxRank << " / " << kMaxMatrixElements << std::endl;
     std::cout << "- max real variables (U / V / W): " << kMaxMatrixElements / 2 << " / " << kMaxMatrixElements / 2 << " / "
@@ -515,11 +555,16 @@ int main(int argc, char *argv[]) {
     std::cout << "- output path: " << outputPath << std::endl;
     std::cout << "- block size: " << blockSize << std::endl;
     if (startAdditions > 0) std::cout << "- start additions: " << startAdditions << std::endl;
+    if (maxFlips > 0) std::cout << "- max flips: " << maxFlips << std::endl;
     std::cout << "- max no improvements: " << maxNoImprovements << std::endl;
     std::cout << "- seed: " << seed << std::endl;
     std::cout << std::endl;
 
-    SchemeAdditionsReducer reducer(count, schemesCount, seed, outputPath, z2input);
+    if (maxFlips > 0 && schemesCount > count) {  // flipSchemesKernel reads states[s] of the reducers
+        std::cout << "Error: --schemes-count must not exceed --count when --max-flips > 0" << std::endl;
+        return -1;
+    }
+    SchemeAdditionsReducer reducer(count, schemesCount, maxFlips, seed, outputPath, z2input);
     bool correct = reducer.read(f);
     if (!correct) return -1;
     reducer.reduce(maxNoImprovements, startAdditions);

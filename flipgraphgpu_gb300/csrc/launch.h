@@ -46,5 +46,11 @@ cudaError_t launch_walk_group(const DevBatch &B, const WalkParams &P, int first,
 cudaError_t launch_walk_zb(const DevBatch &B, const WalkParams &P, int first, int count, int scap, int sms,
                            cudaStream_t s);
 cudaError_t launch_verify_zb(const DevBatch &B, int best, uint8_t *out, cudaStream_t s);
+// Additions reducer, --max-flips: schemes [1, schemes) of coef ([schemes][3][m][64], ternary)
+// become scheme 0 after up to maxFlips ZT flips drawn from states[s]; ranks, pairs (largest
+// pair-occurrence count of a component) and status are written for those schemes.
+cudaError_t launch_flip_schemes(int schemes, int n1, int n2, int n3, int m, int maxFlips, int8_t *coef,
+                                curandStateXORWOW_t *states, int32_t *ranks, int32_t *pairs, int32_t *status, int sms,
+                                cudaStream_t st);
 
 }  // namespace fg

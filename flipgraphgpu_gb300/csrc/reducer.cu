@@ -383,6 +383,7 @@ struct ReduceArgs {
     ReduceDims D;
     unsigned char *gscratch;         // non-null: per-block tables in global memory (slotBytes each)
     size_t slotBytes;
+    const int32_t *ranks = nullptr;  // [schemes] rank of each scheme (null: all m); rows past it are zero
 };
 
 // One reducer (runReducersKernel body for reducer idx); its pair tables start at `base`.
@@ -411,6 +412,9 @@ __device__ void reduce_one(const ReduceArgs &A, int idx, unsigned char *base, in
     r.P = nullptr;
     const int8_t *coef = A.coef + (size_t)(idx % A.schemes) * 3 * A.m * 64;
     const int nn[3] = {A.n1 * A.n2, A.n2 * A.n3, A.n3 * A.n1};
+    // A flipped scheme may have dropped rank (tryFlip reduces): it has fewer U and V
+    // expressions and W has fewer real variables (addExpression(w, scheme.m)).
+    const int ms = A.ranks ? A.ranks[idx % A.schemes] : A.m;
 
     // Modes (scheme_additions_reducer.cu:600-602): reducer 0 is plain greedy, no draws.
     int modes[3];
@@ -428,8 +432,8 @@ __device__ void reduce_one(const ReduceArgs &A, int idx, unsigned char *base, in
     for (int c = 0; c < 3; c++) {
         // copySchemeToReducers (scheme_additions_reducer.cu:463-492): naive expressions.
         RedState st;
-        st.E = D.E[c];
-        st.real = c < 2 ? nn[c] : A.m;
+        st.E = c < 2 ? ms : D.E[c];
+        st.real = c < 2 ? nn[c] : ms;
         st.fresh = 0;
         st.mode = modes[c];
         st.maxFresh = max_fresh(c);
@@ -548,6 +552,12 @@ struct fg_reducer {
     unsigned char *d_scratch = nullptr;  // global-memory tables when they exceed shared memory
     size_t slotBytes = 0;
     int slots = 0;
+    // --max-flips: the schemes 1.. are flipped copies of scheme 0 (fg_reducer_flip)
+    bool ternary0 = false;      // scheme 0's coefficients are all in {-1, 0, 1}
+    int32_t *d_ranks = nullptr; // [schemes] rank of each scheme after the last flip pass
+    int32_t *d_pairs = nullptr; // [schemes] largest pair-occurrence count of a component
+    int32_t *d_fstatus = nullptr;  // [schemes] walk status bits of the flip pass
+    bool flipped = false;       // d_ranks holds the ranks fg_reducer_run must use
 };
 
 namespace {
@@ -560,6 +570,41 @@ fg_status rfail(fg_status s, const char *msg) {
         cudaError_t e_ = (call);                                                \
         if (e_ != cudaSuccess) return rfail(FG_ERR_CUDA, cudaGetErrorString(e_)); \
     } while (0)
+
+// Pair tables for expressions holding at most `nocc` pair occurrences: in shared
+// memory when they fit (the kernel's attribute is set at every launch, since other
+// handles may have set it smaller), else one slot per resident block in global memory.
+fg_status plan_tables(fg_reducer *h, long nocc) {
+    ReduceDims &D = h->D;
+    const int m = h->m, nn[3] = {h->n1 * h->n2, h->n2 * h->n3, h->n3 * h->n1};
+    D.nocc = (int)nocc;
+    D.tbits = 4;
+    while ((1L << D.tbits) < 2 * nocc) D.tbits++;
+    const int T = 1 << D.tbits;
+    const int Lmax = nn[0] > nn[1] ? (nn[0] > m ? nn[0] : m) : (nn[1] > m ? nn[1] : m);
+    const int Emax = m > nn[2] ? m : nn[2];
+    const size_t bytes = (size_t)12 * T + (size_t)16 * D.nocc + 4 * (size_t)(Emax + 1) + 2000 +
+                         2 * (size_t)((Emax + 1 + 1) & ~1) + 2 * (size_t)Emax * Lmax + 64;
+    int optin = 0, sms = 0;
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->cfg.device);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->cfg.device);
+    if (h->d_scratch) cudaFree(h->d_scratch);
+    h->d_scratch = nullptr;
+    h->slotBytes = 0;
+    h->slots = 0;
+    h->smem = bytes;
+    if (bytes > (size_t)optin) {
+        // Tables in global memory (L2-resident per block), blocks loop over the reducers.
+        h->slotBytes = (bytes + 255) / 256 * 256;
+        h->slots = std::min(h->cfg.count, 4 * (sms > 0 ? sms : 1));
+        h->smem = 0;
+        if (cudaMalloc(&h->d_scratch, h->slotBytes * h->slots) != cudaSuccess) {
+            h->d_scratch = nullptr;
+            return rfail(FG_ERR_CAPACITY, "scheme too large for the reducer's global tables");
+        }
+    }
+    return FG_OK;
+}
 }  // namespace
 
 extern "C" {
@@ -595,29 +640,11 @@ fg_status fg_reducer_create(const fg_reducer_config *cfg, int n1, int n2, int n3
             if (tot > nocc) nocc = tot;
         }
     }
-    D.nocc = (int)nocc;
-    D.tbits = 4;
-    while ((1L << D.tbits) < 2 * nocc) D.tbits++;
-    const int T = 1 << D.tbits;
-    const int Lmax = nn[0] > nn[1] ? (nn[0] > m ? nn[0] : m) : (nn[1] > m ? nn[1] : m);
-    const int Emax = m > nn[2] ? m : nn[2];
-    h->smem = (size_t)12 * T + (size_t)16 * D.nocc + 4 * (size_t)(Emax + 1) + 2000 + 2 * (size_t)((Emax + 1 + 1) & ~1) +
-              2 * (size_t)Emax * Lmax + 64;
-    int dev = cfg->device, optin = 0;
-    if (cudaSetDevice(dev) != cudaSuccess) { delete h; return rfail(FG_ERR_CUDA, "cudaSetDevice failed"); }
-    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-    if (h->smem > (size_t)optin) {
-        // Tables in global memory (L2-resident per block), blocks loop over the reducers.
-        int sms = 0;
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        h->slotBytes = (h->smem + 255) / 256 * 256;
-        h->slots = std::min(cfg->count, 4 * (sms > 0 ? sms : 1));
-        h->smem = 0;
-        if (cudaMalloc(&h->d_scratch, h->slotBytes * h->slots) != cudaSuccess) {
-            delete h;
-            return rfail(FG_ERR_CAPACITY, "scheme too large for the reducer's global tables");
-        }
-    }
+    h->ternary0 = true;
+    for (size_t q = 0; q < (size_t)3 * m * 64; q++) h->ternary0 &= coef[q] >= -1 && coef[q] <= 1;
+    if (cudaSetDevice(cfg->device) != cudaSuccess) { delete h; return rfail(FG_ERR_CUDA, "cudaSetDevice failed"); }
+    fg_status ps = plan_tables(h, nocc);
+    if (ps != FG_OK) { delete h; return ps; }
     size_t ncoef = (size_t)cfg->schemes * 3 * m * 64;
     cudaError_t e = cudaMalloc(&h->d_coef, ncoef);
     if (e == cudaSuccess) e = cudaMemcpy(h->d_coef, coef, ncoef, cudaMemcpyHostToDevice);
@@ -626,12 +653,13 @@ fg_status fg_reducer_create(const fg_reducer_config *cfg, int n1, int n2, int n3
     if (e == cudaSuccess) e = cudaMalloc(&h->d_out, 4 * 13 * (size_t)cfg->count);
     if (e == cudaSuccess) e = cudaMalloc(&h->d_scale, 4 * 3 * (size_t)cfg->count);
     if (e == cudaSuccess) e = cudaMalloc(&h->d_vars, 2 * (size_t)cfg->count * 3 * 1000);
+    if (e == cudaSuccess) e = cudaMalloc(&h->d_ranks, 4 * (size_t)cfg->schemes);
+    if (e == cudaSuccess) e = cudaMalloc(&h->d_pairs, 4 * (size_t)cfg->schemes);
+    if (e == cudaSuccess) e = cudaMalloc(&h->d_fstatus, 4 * (size_t)cfg->schemes);
     if (e == cudaSuccess) {
         k_seed_reducers<<<(cfg->count + 127) / 128, 128>>>(h->d_states, cfg->count, (unsigned long long)cfg->seed);
         e = cudaGetLastError();
     }
-    if (e == cudaSuccess && h->smem)
-        e = cudaFuncSetAttribute(k_reduce, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)h->smem);
     if (e == cudaSuccess) e = cudaDeviceSynchronize();
     if (e != cudaSuccess) {
         fg_reducer_destroy(h);
@@ -667,6 +695,8 @@ fg_status fg_reducer_run(fg_reducer *h, int independent, const int32_t *best_fre
     A.D = h->D;
     A.gscratch = h->d_scratch;
     A.slotBytes = h->slotBytes;
+    A.ranks = h->flipped ? h->d_ranks : nullptr;
+    if (h->smem) RCUDA(cudaFuncSetAttribute(k_reduce, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)h->smem));
     k_reduce<<<h->d_scratch ? h->slots : A.count, reduce_threads(h->cfg.threads), h->smem>>>(A);
     RCUDA(cudaGetLastError());
     RCUDA(cudaMemcpy(out_counts, h->d_out, 4 * 13 * (size_t)A.count, cudaMemcpyDeviceToHost));
@@ -679,9 +709,44 @@ fg_status fg_reducer_run(fg_reducer *h, int independent, const int32_t *best_fre
     return FG_OK;
 }
 
+fg_status fg_reducer_flip(fg_reducer *h, int max_flips, int32_t *ranks_out, int8_t *coef_out) {
+    if (!h) return rfail(FG_ERR_ARG, "null handle");
+    if (max_flips < 0) return rfail(FG_ERR_ARG, "max_flips must be >= 0");
+    if (h->cfg.schemes > h->cfg.count)
+        return rfail(FG_ERR_ARG, "the flip pass draws from the reducers' streams: schemes must not exceed count");
+    if (!h->ternary0) return rfail(FG_ERR_ARG, "the flip pass needs scheme 0's coefficients in {-1, 0, 1}");
+    RCUDA(cudaSetDevice(h->cfg.device));
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->cfg.device);
+    const int S = h->cfg.schemes;
+    std::vector<int32_t> ranks(S, h->m), pairs(S, h->D.nocc), status(S, 0);
+    RCUDA(launch_flip_schemes(S, h->n1, h->n2, h->n3, h->m, max_flips, h->d_coef, h->d_states, h->d_ranks, h->d_pairs,
+                              h->d_fstatus, sms, 0));
+    RCUDA(cudaDeviceSynchronize());
+    if (S > 1) {
+        RCUDA(cudaMemcpy(ranks.data() + 1, h->d_ranks + 1, 4 * (size_t)(S - 1), cudaMemcpyDeviceToHost));
+        RCUDA(cudaMemcpy(pairs.data() + 1, h->d_pairs + 1, 4 * (size_t)(S - 1), cudaMemcpyDeviceToHost));
+        RCUDA(cudaMemcpy(status.data() + 1, h->d_fstatus + 1, 4 * (size_t)(S - 1), cudaMemcpyDeviceToHost));
+    }
+    RCUDA(cudaMemcpy(h->d_ranks, ranks.data(), 4, cudaMemcpyHostToDevice));  // scheme 0 is not flipped
+    h->flipped = true;
+    // Flips make expressions denser: grow the pair tables when a scheme needs more room.
+    const long need = *std::max_element(pairs.begin(), pairs.end());
+    if (need > h->D.nocc) {
+        fg_status ps = plan_tables(h, need);
+        if (ps != FG_OK) return ps;
+    }
+    if (ranks_out) std::copy(ranks.begin(), ranks.end(), ranks_out);
+    if (coef_out) RCUDA(cudaMemcpy(coef_out, h->d_coef, (size_t)S * 3 * h->m * 64, cudaMemcpyDeviceToHost));
+    for (int s = 1; s < S; s++)
+        if (status[s]) return rfail(FG_ERR_WALK, "a scheme's flips stopped at a retry bound");
+    return FG_OK;
+}
+
 fg_status fg_reducer_destroy(fg_reducer *h) {
     if (!h) return FG_OK;
-    void *ptrs[] = {h->d_coef, h->d_states, h->d_best, h->d_out, h->d_scale, h->d_vars, h->d_scratch};
+    void *ptrs[] = {h->d_coef, h->d_states, h->d_best,  h->d_out,   h->d_scale,
+                    h->d_vars, h->d_scratch, h->d_ranks, h->d_pairs, h->d_fstatus};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     delete h;

@@ -355,6 +355,19 @@ fg_status fg_reducer_create(const fg_reducer_config *cfg, int n1, int n2, int n3
  * may be NULL. */
 fg_status fg_reducer_run(fg_reducer *h, int independent, const int32_t *best_fresh, const int32_t *best_vars,
                          int32_t *out_counts, float *out_scale, int32_t *out_vars);
+
+/* The flip pass of --max-flips > 0 (flipSchemesKernel, scheme_additions_reducer.cu:
+ * 448-460, run before every reduction after the first, reduceIteration
+ * scheme_additions_reducer.cu:172-176): each scheme s in [1, schemes) becomes
+ * scheme 0 after curand() % (max_flips + 1) ternary flips (SchemeInteger::tryFlip
+ * with reductions, scheme_integer.cu:907-975; the first flip that finds no pair
+ * ends it), drawn from reducer s's stream, which the next fg_reducer_run
+ * continues.  A flip that reduces leaves scheme s with a lower rank; the
+ * reducers then use it (fewer U and V expressions, fewer W variables).  Needs
+ * schemes <= count and scheme 0 ternary.  ranks_out [schemes] and coef_out
+ * [schemes][3][m][64] (rows past a scheme's rank zero) may be NULL.  A scheme
+ * whose flips stopped at a retry bound returns FG_ERR_WALK after the pass. */
+fg_status fg_reducer_flip(fg_reducer *h, int max_flips, int32_t *ranks_out, int8_t *coef_out);
 fg_status fg_reducer_destroy(fg_reducer *h);
 
 /* One reducer pass without any device allocation: the same result as

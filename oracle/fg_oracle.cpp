@@ -2645,9 +2645,15 @@ int fgo_complexity(int ring, int S, int cap, const int32_t *n, const int32_t *m,
 
 // Reducer sizes per config.cuh:16-32 with AdditionsReducer's template order
 // <maxExpressions, maxFresh, maxExpressionLength, maxSubexpressions>.
-int fgo_reduce(int n1, int n2, int n3, int m, const int8_t *coef, int count, int independent,
-               const fgo_tape *tape, int rng, uint64_t seed, int32_t *out, int32_t *modes,
-               int64_t *consumed, const fgo_reducer_state *best, fgo_reducer_state **best_out) {
+}  // extern "C"
+
+// runReducersKernel (scheme_additions_reducer.cu:494-540) for reducers 0..count-1;
+// reducer idx reduces scheme idx % schemes (coef [schemes][3][m][64], rank ranks[s]
+// or m).  vars_out (may be NULL): [count][3][500][2] fresh variables.
+static int reduce_impl(int n1, int n2, int n3, int m, const int8_t *coef, const int32_t *ranks, int schemes,
+                       int count, int independent, const fgo_tape *tape, int rng, uint64_t seed, int32_t *out,
+                       int32_t *modes, int64_t *consumed, const fgo_reducer_state *best,
+                       fgo_reducer_state **best_out, int32_t *vars_out) {
     const int nn[3] = {n1 * n2, n2 * n3, n3 * n1};
     const int maxFresh[3] = {250, 250, 500};
     const int maxLen[3] = {32, 32, 175};
@@ -2675,19 +2681,21 @@ int fgo_reduce(int n1, int n2, int n3, int m, const int8_t *coef, int count, int
             R[p].maxLen = maxLen[p];
             R[p].sub.maxPairs = maxSub[p];
         }
-        // copySchemeToReducers (scheme_additions_reducer.cu:463-492)
+        // copySchemeToReducers (scheme_additions_reducer.cu:463-492) of schemes[idx % schemesCount]
+        const int8_t *cf = coef + (size_t)(idx % schemes) * 3 * m * 64;
+        const int ms = ranks ? ranks[idx % schemes] : m;
         std::vector<int> row(std::max(m, 64));
-        for (int t = 0; t < m; t++) {
-            for (int i = 0; i < nn[0]; i++) row[i] = coef[((size_t)0 * m + t) * 64 + i];
+        for (int t = 0; t < ms; t++) {
+            for (int i = 0; i < nn[0]; i++) row[i] = cf[((size_t)0 * m + t) * 64 + i];
             R[0].addExpression(row.data(), nn[0]);
         }
-        for (int t = 0; t < m; t++) {
-            for (int i = 0; i < nn[1]; i++) row[i] = coef[((size_t)1 * m + t) * 64 + i];
+        for (int t = 0; t < ms; t++) {
+            for (int i = 0; i < nn[1]; i++) row[i] = cf[((size_t)1 * m + t) * 64 + i];
             R[1].addExpression(row.data(), nn[1]);
         }
         for (int i = 0; i < nn[2]; i++) {
-            for (int t = 0; t < m; t++) row[t] = coef[((size_t)2 * m + t) * 64 + i];
-            R[2].addExpression(row.data(), m);
+            for (int t = 0; t < ms; t++) row[t] = cf[((size_t)2 * m + t) * 64 + i];
+            R[2].addExpression(row.data(), ms);
         }
         auto body = [&](auto &r) {
             for (int p = 0; p < 3; p++) R[p].setMode(idx == 0 ? GREEDY : kModes[r.raw() % 15]);
@@ -2711,6 +2719,11 @@ int fgo_reduce(int n1, int n2, int n3, int m, const int8_t *coef, int count, int
             out[idx * 9 + p * 3 + 1] = R[p].freshVariables;
             out[idx * 9 + p * 3 + 2] = R[p].naiveAdditions;
             if (modes) modes[idx * 3 + p] = R[p].mode;
+            if (vars_out)
+                for (size_t q = 0; q < R[p].vars.size() && q < 500; q++) {
+                    vars_out[(((size_t)idx * 3 + p) * 500 + q) * 2] = R[p].vars[q].first;
+                    vars_out[(((size_t)idx * 3 + p) * 500 + q) * 2 + 1] = R[p].vars[q].second;
+                }
         }
         bad += status != 0;
     }
@@ -2726,6 +2739,70 @@ int fgo_reduce(int n1, int n2, int n3, int m, const int8_t *coef, int count, int
             st->vars[p] = all[(size_t)bi * 3 + p].vars;
         }
         *best_out = st;
+    }
+    return bad;
+}
+
+extern "C" {
+
+int fgo_reduce(int n1, int n2, int n3, int m, const int8_t *coef, int count, int independent,
+               const fgo_tape *tape, int rng, uint64_t seed, int32_t *out, int32_t *modes,
+               int64_t *consumed, const fgo_reducer_state *best, fgo_reducer_state **best_out) {
+    return reduce_impl(n1, n2, n3, m, coef, nullptr, 1, count, independent, tape, rng, seed, out, modes, consumed,
+                       best, best_out, nullptr);
+}
+
+int fgo_reduce_schemes(int n1, int n2, int n3, int m, const int8_t *coef, const int32_t *ranks, int schemes,
+                       int count, int independent, const fgo_tape *tape, int32_t *out, int32_t *modes,
+                       int64_t *consumed, const fgo_reducer_state *best, int32_t *vars_out) {
+    return reduce_impl(n1, n2, n3, m, coef, ranks, schemes, count, independent, tape, FGO_RNG_TAPE, 0, out, modes,
+                       consumed, best, nullptr, vars_out);
+}
+
+// flipSchemesKernel (scheme_additions_reducer.cu:448-460).
+int fgo_flip_schemes(int n1, int n2, int n3, int m, const int8_t *coef0, int schemes, int max_flips,
+                     const fgo_tape *tape, int8_t *coef_out, int32_t *ranks_out, int64_t *consumed) {
+    const int nn[3] = {n1 * n2, n2 * n3, n3 * n1};
+    std::memcpy(coef_out, coef0, (size_t)3 * m * 64);
+    ranks_out[0] = m;
+    if (consumed) consumed[0] = 0;
+    int bad = 0;
+    std::vector<ZT> scratch(1);
+    ZT &z = scratch[0];
+    for (int idx = 1; idx < schemes; idx++) {
+        int32_t status = 0;
+        RefDraws rt;
+        rt.d = tape->draws + tape->offsets[idx];
+        rt.u = tape->uniforms + tape->offsets[idx];
+        rt.n = tape->offsets[idx + 1] - tape->offsets[idx];
+        rt.status = &status;
+        // schemes[0].copyTo(schemes[idx]) (scheme_integer.cu:66-79): terms, then initFlips
+        z.status = &status;
+        z.n[0] = n1; z.n[1] = n2; z.n[2] = n3;
+        for (int c = 0; c < 3; c++) z.nn[c] = nn[c];
+        z.m = m;
+        for (int c = 0; c < 3; c++)
+            for (int t = 0; t < m; t++) {
+                Tern a;
+                for (int e = 0; e < nn[c]; e++) {
+                    const int8_t x = coef0[((size_t)c * m + t) * 64 + e];
+                    if (x) a.v |= (uint64_t)1 << e;
+                    if (x < 0) a.s |= (uint64_t)1 << e;
+                }
+                z.x[c][t] = a;
+            }
+        z.rebuildLists();
+        const uint32_t flips = rt.raw() % (uint32_t)(max_flips + 1);
+        for (uint32_t i = 0; i < flips; i++)
+            if (!z.tryFlip(rt, true) || status) break;
+        int8_t *out = coef_out + (size_t)idx * 3 * m * 64;
+        for (int c = 0; c < 3; c++)
+            for (int t = 0; t < m; t++)
+                for (int e = 0; e < 64; e++)
+                    out[((size_t)c * m + t) * 64 + e] = (int8_t)(t < z.m && e < nn[c] ? z.x[c][t].at(e) : 0);
+        ranks_out[idx] = z.m;
+        if (consumed) consumed[idx] = rt.pos;
+        bad += status != 0;
     }
     return bad;
 }

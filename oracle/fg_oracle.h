@@ -132,6 +132,20 @@ int fgo_reduce(int n1, int n2, int n3, int m, const int8_t *coef, int count, int
                const fgo_tape *tape, int rng, uint64_t seed, int32_t *out, int32_t *modes,
                int64_t *consumed, const fgo_reducer_state *best, fgo_reducer_state **best_out);
 void fgo_reducer_state_free(fgo_reducer_state *s);
+/* runReducersKernel over several schemes (--max-flips): reducer r reduces scheme
+ * r % schemes of coef [schemes][3][m][64] at rank ranks[s] (NULL: m), draws from
+ * tape walk r.  vars_out (may be NULL): [count][3][500][2] fresh variables of
+ * every reducer (the "together" incumbent is one reducer's three lists). */
+int fgo_reduce_schemes(int n1, int n2, int n3, int m, const int8_t *coef, const int32_t *ranks, int schemes,
+                       int count, int independent, const fgo_tape *tape, int32_t *out, int32_t *modes,
+                       int64_t *consumed, const fgo_reducer_state *best, int32_t *vars_out);
+/* flipSchemesKernel (scheme_additions_reducer.cu:448-460): scheme s in [1, schemes)
+ * := scheme 0 (coef0 [3][m][64], lists by initFlips) after curand() % (max_flips + 1)
+ * SchemeInteger::tryFlip calls with reductions, stopping at the first without a
+ * flip; stream s is tape walk s.  coef_out [schemes][3][m][64] (scheme 0 copied,
+ * rows past a rank zero), ranks_out [schemes], consumed [schemes] draws. */
+int fgo_flip_schemes(int n1, int n2, int n3, int m, const int8_t *coef0, int schemes, int max_flips,
+                     const fgo_tape *tape, int8_t *coef_out, int32_t *ranks_out, int64_t *consumed);
 /* Incumbent from explicit fresh-variable lists: fresh [3], vars [3][500][2]. */
 fgo_reducer_state *fgo_reducer_state_make(const int32_t *fresh, const int32_t *vars);
 

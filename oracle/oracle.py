@@ -43,6 +43,8 @@ def lib():
         _lib.fgo_minimize.restype = ctypes.c_int
         _lib.fgo_validate.restype = ctypes.c_int
         _lib.fgo_reduce.restype = ctypes.c_int
+        _lib.fgo_reduce_schemes.restype = ctypes.c_int
+        _lib.fgo_flip_schemes.restype = ctypes.c_int
         _lib.fgo_reduce_gauss.restype = ctypes.c_int
         _lib.fgo_validate_zb.restype = ctypes.c_int
     return _lib
@@ -238,6 +240,44 @@ def reduce(n, m, coef, count, tape=None, independent=True, rng="tape", seed=0, b
                      _ptr(consumed), best, ctypes.byref(state))
     # out columns per component: additions, fresh, naive
     return out, modes, consumed, state
+
+
+def tape_tail(tape, used):
+    """The tape with the first used[w] draws of every walk consumed (a stream continued)."""
+    draws, unis, offs = tape
+    parts = [(draws[offs[w] + used[w]:offs[w + 1]], unis[offs[w] + used[w]:offs[w + 1]]) for w in range(len(offs) - 1)]
+    return make_tape(parts)
+
+
+def flip_schemes(n, m, coef0, schemes, max_flips, tape):
+    """flipSchemesKernel: schemes 1.. := scheme 0 after up to max_flips ZT flips (stream s = tape walk s).
+    Returns (coef [schemes,3,m,64], ranks [schemes], consumed [schemes], status count)."""
+    coef0 = np.ascontiguousarray(coef0, np.int8)
+    assert coef0.shape == (3, m, 64)
+    coef = np.zeros((schemes, 3, m, 64), np.int8)
+    ranks = np.zeros(schemes, np.int32)
+    consumed = np.zeros(schemes, np.int64)
+    t, _keep = _tape_c(tape)
+    bad = lib().fgo_flip_schemes(n[0], n[1], n[2], m, _ptr(coef0), schemes, max_flips, ctypes.byref(t), _ptr(coef),
+                                 _ptr(ranks), _ptr(consumed))
+    return coef, ranks, consumed, bad
+
+
+def reduce_schemes(n, m, coef, ranks, count, tape, independent=False, best=None):
+    """One reducer launch over several schemes (reducer r: scheme r % schemes at rank ranks[s]).
+    Returns (out[count,9], modes[count,3], consumed[count], vars[count,3,500,2])."""
+    coef = np.ascontiguousarray(coef, np.int8)
+    schemes = coef.shape[0]
+    assert coef.shape == (schemes, 3, m, 64)
+    ranks = np.ascontiguousarray(ranks, np.int32)
+    out = np.zeros((count, 9), np.int32)
+    modes = np.zeros((count, 3), np.int32)
+    consumed = np.zeros(count, np.int64)
+    vars_ = np.zeros((count, 3, 500, 2), np.int32)
+    t, _keep = _tape_c(tape)
+    lib().fgo_reduce_schemes(n[0], n[1], n[2], m, _ptr(coef), _ptr(ranks), schemes, count, int(independent),
+                             ctypes.byref(t), _ptr(out), _ptr(modes), _ptr(consumed), best, _ptr(vars_))
+    return out, modes, consumed, vars_
 
 
 def reducer_state_free(state):

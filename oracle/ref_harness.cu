@@ -15,11 +15,17 @@
 //       written, cut exactly at the number of draws the walk consumed (found
 //       by stepping a fresh curand_init(seed, idx, 0) state until it equals
 //       the walk's final state).
-//   reduce IN COUNT SCHEMES_COUNT SEED OUT
+//   reduce IN COUNT SCHEMES_COUNT SEED OUT [MAX_FLIPS ITERATIONS]
 //       Reads one scheme body (n1 n2 n3 m + U,V,W rows) with
 //       checkValidity=false, runs initializeKernel and one runReducersKernel
 //       (scheme_additions_reducer.cu:433-540) and writes per-reducer
 //       additions / fresh-variable counts / modes plus the reducer tapes.
+//       With MAX_FLIPS > 0, ITERATIONS iterations of reduceIteration
+//       (scheme_additions_reducer.cu:172-182: flipSchemesKernel from the
+//       second on, then runReducersKernel with independent=false), each
+//       followed by the host's updateBestTogether (:296-339, the index vector
+//       kept across iterations as the class keeps it); per iteration the
+//       schemes' ranks, every reducer's counts and the chosen top reducer.
 //
 //   gauss IN SEED OUT   (Z2 build)
 //       Reads schemes in flip_graph's text layout (a count, then per scheme
@@ -32,6 +38,7 @@
 // Binary output: little-endian int32 / uint32 / uint64 / float records; the
 // layout is documented in tests/golden/make_golden.py which parses it.
 
+#include <algorithm>
 #include <chrono>
 #include <cstdio>
 #include <cstdlib>
@@ -215,7 +222,10 @@ static int cmd_walk(int argc, char **argv) {
     return 0;
 }
 
+static int cmd_reduce_flips(int argc, char **argv);
+
 static int cmd_reduce(int argc, char **argv) {
+    if (argc == 9 && atoi(argv[7]) > 0) return cmd_reduce_flips(argc, argv);
     if (argc != 7) { fprintf(stderr, "reduce: bad arguments\n"); return 1; }
     const char *in = argv[2];
     int count = atoi(argv[3]), schemesCount = atoi(argv[4]), seed = atoi(argv[5]);
@@ -253,6 +263,81 @@ static int cmd_reduce(int argc, char **argv) {
     }
     int maxDraws = 1 << 18;
     write_tapes(f, states, count, seed, maxDraws);
+    fclose(f);
+    return 0;
+}
+
+static int cmd_reduce_flips(int argc, char **argv) {
+    const char *in = argv[2];
+    int count = atoi(argv[3]), schemesCount = atoi(argv[4]), seed = atoi(argv[5]);
+    const char *out = argv[6];
+    int maxFlips = atoi(argv[7]), iterations = atoi(argv[8]);
+    if (count < 10 || schemesCount > count || iterations < 1) { fprintf(stderr, "reduce: bad flip arguments\n"); return 1; }
+    typedef AdditionsReducer<MAX_U_EXPRESSIONS, MAX_U_FRESH_VARIABLES, MAX_U_REAL_VARIABLES, MAX_U_SUBEXPRESSIONS> RU;
+    typedef AdditionsReducer<MAX_V_EXPRESSIONS, MAX_V_FRESH_VARIABLES, MAX_V_REAL_VARIABLES, MAX_V_SUBEXPRESSIONS> RV;
+    typedef AdditionsReducer<MAX_W_EXPRESSIONS, MAX_W_FRESH_VARIABLES, MAX_W_REAL_VARIABLES, MAX_W_SUBEXPRESSIONS> RW;
+    RU *ru; RV *rv; RW *rw; SchemeInteger *schemes; curandState *states;
+    HCHECK(cudaMallocManaged(&ru, (count + 1) * sizeof(RU)));
+    HCHECK(cudaMallocManaged(&rv, (count + 1) * sizeof(RV)));
+    HCHECK(cudaMallocManaged(&rw, (count + 1) * sizeof(RW)));
+    HCHECK(cudaMallocManaged(&schemes, (count + 1) * sizeof(SchemeInteger)));
+    HCHECK(cudaMallocManaged(&states, count * sizeof(curandState)));
+    std::ifstream fin(in);
+    int n1, n2, n3, m;
+    fin >> n1 >> n2 >> n3 >> m;
+    if (!schemes[0].read(fin, n1, n2, n3, m, false)) { fprintf(stderr, "read failed\n"); return 1; }
+    int blockSize = 32, numBlocks = (count + blockSize - 1) / blockSize;
+    initializeKernel<<<numBlocks, blockSize>>>(ru, rv, rw, schemes, states, count, schemesCount, seed);
+    HCHECK(cudaGetLastError());
+    HCHECK(cudaDeviceSynchronize());
+    // SchemeAdditionsReducer::initialize (scheme_additions_reducer.cu:145-160)
+    int reducedAdditions = ru[count].getAdditions() + rv[count].getAdditions() + rw[count].getAdditions();
+    int reducedFresh = n1 * n2 * (n1 * n2 - 1) + n2 * n3 * (n2 * n3 - 1) + m * (m - 1);
+    std::vector<int> indices(count);
+    for (int i = 0; i < count; i++) indices[i] = i;
+    FILE *f = fopen(out, "wb");
+    put_i32(f, 0x46475232);  // magic "FGR2"
+    put_i32(f, count); put_i32(f, seed); put_i32(f, schemesCount); put_i32(f, maxFlips); put_i32(f, iterations);
+    for (int it = 1; it <= iterations; it++) {
+        if (it > 1) {
+            flipSchemesKernel<<<(schemesCount + blockSize - 1) / blockSize, blockSize>>>(schemes, states, schemesCount, maxFlips);
+            HCHECK(cudaGetLastError());
+            HCHECK(cudaDeviceSynchronize());
+        }
+        runReducersKernel<<<numBlocks, blockSize>>>(ru, rv, rw, schemes, states, count, schemesCount, false);
+        HCHECK(cudaGetLastError());
+        HCHECK(cudaDeviceSynchronize());
+        for (int s = 0; s < schemesCount; s++) put_i32(f, schemes[s].m);
+        for (int r = 0; r < count; r++) {
+            put_i32(f, ru[r].getAdditions()); put_i32(f, ru[r].getFreshVars()); put_i32(f, ru[r].getNaiveAdditions());
+            put_i32(f, rv[r].getAdditions()); put_i32(f, rv[r].getFreshVars()); put_i32(f, rv[r].getNaiveAdditions());
+            put_i32(f, rw[r].getAdditions()); put_i32(f, rw[r].getFreshVars()); put_i32(f, rw[r].getNaiveAdditions());
+            std::string modes = ru[r].getMode() + "," + rv[r].getMode() + "," + rw[r].getMode();
+            put_i32(f, (int)modes.size());
+            fwrite(modes.data(), 1, modes.size(), f);
+        }
+        // updateBestTogether: reducers ordered by total additions, then total fresh variables
+        auto total = [&](int r, bool fresh) {
+            return fresh ? ru[r].getFreshVars() + rv[r].getFreshVars() + rw[r].getFreshVars()
+                         : ru[r].getAdditions() + rv[r].getAdditions() + rw[r].getAdditions();
+        };
+        std::partial_sort(indices.begin(), indices.begin() + 10, indices.end(), [&](int a, int b) {
+            if (total(a, false) != total(b, false)) return total(a, false) < total(b, false);
+            return total(a, true) < total(b, true);
+        });
+        const int top = indices[0];
+        const int additions = total(top, false), fresh = total(top, true);
+        const int improved = additions < reducedAdditions || (additions == reducedAdditions && fresh < reducedFresh);
+        if (improved) {
+            reducedAdditions = additions;
+            reducedFresh = fresh;
+            ru[count].copyFrom(ru[top]);
+            rv[count].copyFrom(rv[top]);
+            rw[count].copyFrom(rw[top]);
+        }
+        put_i32(f, top); put_i32(f, improved);
+    }
+    write_tapes(f, states, count, seed, 1 << 18);
     fclose(f);
     return 0;
 }

@@ -156,6 +156,30 @@ def read_reduce(path):
     return d
 
 
+def read_reduce_flips(path):
+    """ref_harness reduce with MAX_FLIPS > 0: per iteration the schemes' ranks, every reducer's
+    counts and modes, and the top reducer of updateBestTogether; then the reducer tapes."""
+    r = _Reader(_open(path))
+    assert r.i32() == 0x46475232, "not a flip-reduce dump"
+    count, seed, schemes, max_flips, iterations = (r.i32() for _ in range(5))
+    d = {"count": count, "seed": seed, "schemes": schemes, "max_flips": max_flips, "iterations": []}
+    for _ in range(iterations):
+        it = {"ranks": [int(x) for x in r.i32(schemes)], "reducers": []}
+        for _ in range(count):
+            v = r.i32(9)
+            ln = r.i32()
+            modes = bytes(r.b[r.o:r.o + ln]).decode()
+            r.o += ln
+            it["reducers"].append({"u": tuple(int(x) for x in v[0:3]), "v": tuple(int(x) for x in v[3:6]),
+                                   "w": tuple(int(x) for x in v[6:9]), "modes": modes.split(",")})
+        it["top"] = r.i32()
+        it["improved"] = r.i32()
+        d["iterations"].append(it)
+    d["tapes"] = _tapes(r, count)
+    assert r.o == len(r.b), "trailing bytes in flip-reduce dump"
+    return d
+
+
 def read_gauss(path):
     r = _Reader(_open(path))
     assert r.i32() == 0x46474731, "not a Gauss dump"

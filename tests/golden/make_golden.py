@@ -162,9 +162,29 @@ def gauss(out_dir):
     os.remove(inp)
 
 
-def do_run(out_dir, resize_only=False, cli_only=False, gauss_only=False):
+# The reducer's --max-flips mode (flipSchemesKernel + runReducersKernel with
+# independent=false + updateBestTogether) on input_zt_333.txt:
+# (count, schemes, seed, max_flips, iterations).
+REDUCE_FLIP_CASES = [(12, 6, 43, 20, 3)]
+
+
+def reduce_flips(out_dir):
+    inp = os.path.join(out_dir, "input_zt_333.txt")
+    if not os.path.exists(inp):
+        with gzip.open(os.path.join(HERE, "input_zt_333.txt.gz"), "rb") as f, open(inp, "wb") as o:
+            o.write(f.read())
+    for count, schemes, seed, flips, iterations in REDUCE_FLIP_CASES:
+        run([harness("zt"), "reduce", inp, str(count), str(schemes), str(seed),
+             os.path.join(out_dir, f"flipreduce_zt_333_f{flips}.bin"), str(flips), str(iterations)])
+
+
+def do_run(out_dir, resize_only=False, cli_only=False, gauss_only=False, flips_only=False):
     os.makedirs(out_dir, exist_ok=True)
     run([os.path.join(ROOT, "oracle", "build_ref.sh")])
+    if flips_only:
+        reduce_flips(out_dir)
+        os.remove(os.path.join(out_dir, "input_zt_333.txt"))
+        return
     if gauss_only:
         gauss(out_dir)
         return
@@ -195,6 +215,8 @@ def do_run(out_dir, resize_only=False, cli_only=False, gauss_only=False):
     for ring in ("zt", "z2"):
         inp = os.path.join(out_dir, f"input_{ring}_333.txt")
         run([harness("zt"), "reduce", inp, "12", "1", "41", os.path.join(out_dir, f"reduce_{ring}_333.bin")])
+
+    reduce_flips(out_dir)
 
     # End-to-end executables (outputs compared file for file).
     ref_reduced = os.path.join(out_dir, "cli_additions_reducer")
@@ -285,8 +307,9 @@ if __name__ == "__main__":
     ap.add_argument("--resize-only", action="store_true", help="with --run: only the resize walks")
     ap.add_argument("--cli-only", action="store_true", help="with --run: only the flip_graph runs of CLI_CASES")
     ap.add_argument("--gauss-only", action="store_true", help="with --run: only the tryReduceGauss calls")
+    ap.add_argument("--flips-only", action="store_true", help="with --run: only the reducer's --max-flips iterations")
     a = ap.parse_args()
     if a.run:
-        do_run(a.run, a.resize_only, a.cli_only, a.gauss_only)
+        do_run(a.run, a.resize_only, a.cli_only, a.gauss_only, a.flips_only)
     if a.pack:
         do_pack(a.pack)
