@@ -702,9 +702,16 @@ fg_status fg_reducer_run(fg_reducer *h, int independent, const int32_t *best_fre
     RCUDA(cudaMemcpy(out_counts, h->d_out, 4 * 13 * (size_t)A.count, cudaMemcpyDeviceToHost));
     if (out_scale) RCUDA(cudaMemcpy(out_scale, h->d_scale, 4 * 3 * (size_t)A.count, cudaMemcpyDeviceToHost));
     if (out_vars) {
+        // The kernel writes each component's first 2 * fresh entries; the rest of the
+        // row is returned as zero (the device buffer keeps earlier runs' pairs there).
         std::vector<int16_t> v((size_t)A.count * 3 * 1000);
         RCUDA(cudaMemcpy(v.data(), h->d_vars, v.size() * 2, cudaMemcpyDeviceToHost));
-        for (size_t q = 0; q < v.size(); q++) out_vars[q] = v[q];
+        for (int r = 0; r < A.count; r++)
+            for (int c = 0; c < 3; c++) {
+                const int used = 2 * out_counts[(size_t)r * 13 + c * 4 + 1];
+                const size_t row = ((size_t)r * 3 + c) * 1000;
+                for (int q = 0; q < 1000; q++) out_vars[row + q] = q < used ? v[row + q] : 0;
+            }
     }
     return FG_OK;
 }

@@ -351,8 +351,8 @@ fg_status fg_reducer_create(const fg_reducer_config *cfg, int n1, int n2, int n3
  * out_counts [count][13] = per component (U, V, W) four ints: additions, fresh
  * variables, naive additions, selection mode; then the number of draws the
  * reducer consumed in this run.  out_scale [count][3]; out_vars [count][3][500][2]
- * the fresh variables (pairs of signed variable ids).  Either of the last two
- * may be NULL. */
+ * the fresh variables (pairs of signed variable ids; zero past each
+ * component's fresh count).  Either of the last two may be NULL. */
 fg_status fg_reducer_run(fg_reducer *h, int independent, const int32_t *best_fresh, const int32_t *best_vars,
                          int32_t *out_counts, float *out_scale, int32_t *out_vars);
 

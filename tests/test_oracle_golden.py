@@ -77,6 +77,55 @@ def test_reducer_matches_reference(ring):
         assert consumed[r] == d["tapes"][r]["used"], r
 
 
+MODE_PREFIX = {0: "g", 1: "ga", 2: "gr", 3: "gi", 4: "wr", 5: "mix", 6: "rnd"}
+
+
+def test_reducer_max_flips_matches_reference():
+    """The reducer's --max-flips iterations as the reference ran them (ref_harness reduce with
+    MAX_FLIPS: flipSchemesKernel from the second iteration, runReducersKernel with
+    independent=false, updateBestTogether): flipped ranks, every reducer's counts, modes and
+    draws, and the incumbent's improvement, replayed by the oracle from the same tapes."""
+    with gzip.open(golden("input_zt_333.txt.gz"), "rt") as f:
+        n, m, coef0 = read_scheme_text(f.read())
+    d = golden_io.read_reduce_flips(golden("flipreduce_zt_333_f20.bin.gz"))
+    count, schemes, flips = d["count"], d["schemes"], d["max_flips"]
+    tape = O.make_tape([(t["draws"], t["uniforms"]) for t in d["tapes"]])
+    used = np.zeros(count, np.int64)
+    coef, ranks = np.tile(coef0[None], (schemes, 1, 1, 1)), np.full(schemes, m, np.int32)
+    best_fresh, best_vars = np.zeros(3, np.int32), np.zeros((3, 500, 2), np.int32)
+    nn = [n[0] * n[1], n[1] * n[2], n[2] * n[0]]
+    reduced = None
+    for it, ref in enumerate(d["iterations"], start=1):
+        if it > 1:
+            coef, ranks, consumed, bad = O.flip_schemes(n, m, coef0, schemes, flips, O.tape_tail(tape, used))
+            assert bad == 0
+            used[:schemes] += consumed
+        assert list(ranks) == ref["ranks"], it
+        state = O.reducer_state(best_fresh, best_vars)
+        out, modes, consumed, vars_ = O.reduce_schemes(n, m, coef, ranks, count, O.tape_tail(tape, used),
+                                                      independent=False, best=state)
+        O.reducer_state_free(state)
+        used += consumed
+        for r in range(count):
+            rr = ref["reducers"][r]
+            assert (tuple(out[r, 0:3]), tuple(out[r, 3:6]), tuple(out[r, 6:9])) == (rr["u"], rr["v"], rr["w"]), (it, r)
+            assert [MODE_PREFIX[int(x)] for x in modes[r]] == [x.rstrip("0123456789") for x in rr["modes"]], (it, r)
+        if reduced is None:  # SchemeAdditionsReducer::initialize: naive additions, maximal fresh counts
+            reduced = (int(out[0, 2] + out[0, 5] + out[0, 8]),
+                       nn[0] * (nn[0] - 1) + nn[1] * (nn[1] - 1) + m * (m - 1))
+        # updateBestTogether: the reference's top reducer has the lowest (additions, fresh) total
+        tot = out[:, 0] + out[:, 3] + out[:, 6]
+        fresh = out[:, 1] + out[:, 4] + out[:, 7]
+        top = ref["top"]
+        assert (tot[top], fresh[top]) == min(zip(tot, fresh)), it
+        improved = (tot[top], fresh[top]) < reduced
+        assert int(improved) == ref["improved"], it
+        if improved:
+            reduced = (int(tot[top]), int(fresh[top]))
+            best_fresh, best_vars = out[top, 1::3].astype(np.int32), vars_[top].copy()
+    assert [int(x) for x in used] == [t["used"] for t in d["tapes"]]
+
+
 @pytest.mark.parametrize("shape", [(2, 2, 2), (2, 3, 4), (3, 3, 3), (4, 4, 4), (3, 4, 5), (4, 5, 8)])
 def test_naive_schemes_validate(shape):
     n1, n2, n3 = shape

@@ -1,4 +1,5 @@
-"""The additions reducer's --max-flips mode on the GPU through the C ABI.
+"""The additions reducer's --max-flips mode on the GPU through the C ABI
+(collected after the other GPU tests).
 
 Per iteration (reduceIteration, scheme_additions_reducer.cu:172-182): from the
 second on, fg_reducer_flip turns schemes 1.. into flipped copies of scheme 0
@@ -71,7 +72,7 @@ def test_flip_iterations_vs_oracle(count, schemes, seed, max_flips):
         assert np.array_equal(out[:, 2::3], g["naive"]), it
         assert np.array_equal(modes, g["mode"]), it
         assert np.array_equal(consumed, g["draws"]), it
-        assert np.array_equal(vars_, g["vars"]), it
+        assert np.array_equal(vars_, g["vars"]), it  # rows past 2 * fresh are zero on both sides
         used += consumed
         # updateBestTogether: one reducer's three components, lowest total additions then fresh
         tot, fresh = g["additions"].sum(1), g["fresh"].sum(1)
