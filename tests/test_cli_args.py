@@ -99,3 +99,16 @@ def test_ternary_input_flags_coefficients_outside_the_ring(tmp_path):
     rc, out, _ = run("flip_graph", "-n1", "3", "-n2", "3", "-n3", "3", "--input-path", str(src), "--ring", "ZT",
                      "--schemes", "32", "--max-iterations", "10", "--max-launches", "1", "--path", str(tmp_path / "o"))
     assert "invalid set (0, 2)" in out
+
+
+def test_max_flips_needs_a_stream_per_scheme(tmp_path):
+    """--max-flips flips scheme s with reducer s's stream (flipSchemesKernel), so the
+    executable refuses more schemes than reducers before any device work."""
+    import gzip
+    from helpers import GOLDEN
+    src = tmp_path / "in.txt"
+    src.write_text(gzip.open(os.path.join(GOLDEN, "input_zt_333.txt.gz"), "rt").read())
+    rc, out, _ = run("additions_reducer", "-i", str(src), "-o", str(tmp_path), "--count", "4", "--schemes-count", "8",
+                     "--max-flips", "5")
+    assert "- max flips: 5" in out
+    assert "--schemes-count must not exceed --count" in out and rc == 255
