@@ -1,5 +1,4 @@
-"""The additions reducer's --max-flips mode on the GPU through the C ABI
-(collected after the other GPU tests).
+"""The additions reducer's --max-flips mode on the GPU through the C ABI.
 
 Per iteration (reduceIteration, scheme_additions_reducer.cu:172-182): from the
 second on, fg_reducer_flip turns schemes 1.. into flipped copies of scheme 0
