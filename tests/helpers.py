@@ -4,8 +4,6 @@ import os
 
 import numpy as np
 
-import golden_io
-
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
 

@@ -9,7 +9,6 @@ files with the same names and byte-identical contents.
 import gzip
 import os
 import platform
-import shutil
 import subprocess
 
 import pytest
