@@ -115,7 +115,8 @@ private:
         if (zt_) { sgn_.assign(nf, 0); bsgn_.assign(nf, 0); val_.assign(nf, 0); bval_.assign(nf, 0); }
         rec_ = fg_records{n_.data(), m_.data(), fac_.data(), zt_ ? sgn_.data() : nullptr, zt_ ? val_.data() : nullptr,
                           ls_.data(), lists_.data(), fl_.data(), br_.data(), bm_.data(), bfac_.data(),
-                          zt_ ? bsgn_.data() : nullptr, zt_ ? bval_.data() : nullptr, pos_.data(), st_.data()};
+                          zt_ ? bsgn_.data() : nullptr, zt_ ? bval_.data() : nullptr, pos_.data(), st_.data(),
+                          /*best_n*/ nullptr, /*fac2*/ nullptr, /*best_fac2*/ nullptr};
     }
 
     std::string savePath(const HostScheme &s, int iteration, int runId) const {  // complexity_minimizer.cu:136-149

@@ -150,7 +150,8 @@ private:
             r = fg_records{n.data(), m.data(), fac.data(), sgn.empty() ? nullptr : sgn.data(),
                            valid.empty() ? nullptr : valid.data(), list_size.data(), lists.data(), flips.data(),
                            best_rank.data(), best_m.data(), best_fac.data(), best_sgn.empty() ? nullptr : best_sgn.data(),
-                           best_valid.empty() ? nullptr : best_valid.data(), rng_pos.data(), status.data()};
+                           best_valid.empty() ? nullptr : best_valid.data(), rng_pos.data(), status.data(),
+                           /*best_n*/ nullptr, /*fac2*/ nullptr, /*best_fac2*/ nullptr};
         }
     };
 
