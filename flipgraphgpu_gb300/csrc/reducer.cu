@@ -418,7 +418,6 @@ __device__ void reduce_one(const ReduceArgs &A, int idx, unsigned char *base, in
 
     // Modes (scheme_additions_reducer.cu:600-602): reducer 0 is plain greedy, no draws.
     int modes[3];
-    float scales[3];
     for (int c = 0; c < 3; c++) modes[c] = idx == 0 ? GREEDY : c_modes[r.raw() % 15];
     // Partial initialisation draws (scheme_additions_reducer.cu:604-623).
     int partial[3] = {0, 0, 0};
@@ -501,7 +500,6 @@ __device__ void reduce_one(const ReduceArgs &A, int idx, unsigned char *base, in
             A.out[idx * 13 + c * 4 + 1] = st.fresh;
             A.out[idx * 13 + c * 4 + 2] = st.naive;
             A.out[idx * 13 + c * 4 + 3] = st.mode;
-            scales[c] = st.scale;
             A.out_scale[idx * 3 + c] = st.scale;
         }
         if (A.out_vars)
@@ -513,7 +511,6 @@ __device__ void reduce_one(const ReduceArgs &A, int idx, unsigned char *base, in
         A.states[idx] = r.st;
         A.out[idx * 13 + 12] = (int32_t)r.count;
     }
-    (void)scales;
 }
 
 // Reducers blockIdx.x, blockIdx.x + gridDim.x, ...; tables in dynamic shared memory, or in
