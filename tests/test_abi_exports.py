@@ -77,3 +77,27 @@ def test_ctypes_structs_mirror_the_header(c_name, py_name):
     for (name, ctype), (_, pytype) in zip(c_fields, py_fields):
         want = ctypes.c_void_p if ctype == "pointer" else C_TYPES[ctype]
         assert pytype == want, (c_name, name, ctype, pytype)
+
+
+@pytest.mark.parametrize("ring", ["z2", "zt", "zb"])
+def test_engine_checks_record_layouts_before_the_library_sees_them(ring):
+    """Records are passed to fg_set_records / fg_get_records as raw pointers: the Python
+    mirror rejects arrays whose shape, type or contiguity differ from the handle's."""
+    import numpy as np
+    eng = fg.Engine.__new__(fg.Engine)  # sizes only; no device handle is created
+    eng.walks, eng.cap, eng.ring, eng.h = 6, 27, ring, None
+    eng._match(fg.Records(6, 27, ring))
+    eng._match(fg.Records(6, 27, ring, lists=False))
+    bad = [fg.Records(5, 27, ring), fg.Records(6, 28, ring), fg.Records(6, 27, "z2" if ring != "z2" else "zt")]
+    r = fg.Records(6, 27, ring)
+    r.fac = r.fac[:, :, :20]
+    bad.append(r)
+    r = fg.Records(6, 27, ring)
+    r.m = r.m.astype(np.int64)
+    bad.append(r)
+    r = fg.Records(6, 27, ring)
+    r.best_fac = np.asfortranarray(r.best_fac)
+    bad.append(r)
+    for rec in bad:
+        with pytest.raises(ValueError):
+            eng._match(rec)
