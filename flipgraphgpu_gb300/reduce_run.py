@@ -4,7 +4,10 @@
 
 Reads one scheme in the additions_reducer text layout ("n1 n2 n3 m" and its
 rows), runs --launches launches of --count reducers over it and prints runs/s
-and the best addition count.
+and the best addition count.  With --max-flips F each launch after the warm-up
+is preceded by the flip pass (schemes 1..--schemes-1 become copies of the
+scheme with up to F ternary flips) and reduces with independent=false, as the
+additions_reducer executable's --max-flips iterations do.
 """
 import argparse
 import json
@@ -22,7 +25,11 @@ def main():
     ap.add_argument("--launches", type=int, default=2)
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--threads", type=int, default=512, help="threads per reducer block (0: the library's 128)")
+    ap.add_argument("--schemes", type=int, default=1, help="schemes side by side (reducer r reduces scheme r %% schemes)")
+    ap.add_argument("--max-flips", type=int, default=0, help="flip pass before each timed launch (0: none)")
     a = ap.parse_args()
+    if a.max_flips > 0 and a.schemes > a.count:
+        ap.error("--schemes must not exceed --count with --max-flips (one stream per scheme)")
     tok = [int(x) for x in open(a.scheme).read().split()]
     n, m = tok[:3], tok[3]
     nn = [n[0] * n[1], n[1] * n[2], n[2] * n[0]]
@@ -32,18 +39,22 @@ def main():
         for t in range(m):
             coef[0, c, t, :nn[c]] = tok[p:p + nn[c]]
             p += nn[c]
-    red = Reducer(n, m, coef, count=a.count, schemes=1, seed=a.seed, threads=a.threads)
-    red.run()  # warm-up
+    coef = np.tile(coef, (a.schemes, 1, 1, 1))
+    independent = a.max_flips == 0
+    red = Reducer(n, m, coef, count=a.count, schemes=a.schemes, seed=a.seed, threads=a.threads)
+    red.run(independent=independent)  # warm-up
     t = time.perf_counter()
     best = None
     for _ in range(a.launches):
-        out = red.run()
+        if a.max_flips > 0:
+            red.flip(a.max_flips)
+        out = red.run(independent=independent)
         adds = out["additions"].sum(axis=1)
         best = int(adds.min()) if best is None else min(best, int(adds.min()))
     dt = time.perf_counter() - t
     red.close()
-    print(json.dumps({"scheme": a.scheme, "count": a.count, "launches": a.launches,
-                      "runs_per_s": a.count * a.launches / dt, "best_additions": best}))
+    print(json.dumps({"scheme": a.scheme, "count": a.count, "schemes": a.schemes, "max_flips": a.max_flips,
+                      "launches": a.launches, "runs_per_s": a.count * a.launches / dt, "best_additions": best}))
 
 
 if __name__ == "__main__":
