@@ -211,3 +211,31 @@ def test_reduce_gauss_matches_reference(path):
         for c in range(3):
             assert np.array_equal(b.fac[w, c, :s["m"]], np.asarray(s["uvw"][c], np.uint64)), (w, c)
     assert [int(x) for x in b.rng_pos] == [t["used"] for t in d["tapes"]]
+
+
+def test_flip_pass_properties():
+    """flipSchemesKernel's restatement on synthetic streams: max_flips 0 takes one draw per
+    stream and copies the scheme; with flips every scheme stays an exact ternary scheme."""
+    with gzip.open(golden("input_zt_333.txt.gz"), "rt") as f:
+        n, m, coef0 = read_scheme_text(f.read())
+    rng = np.random.default_rng(7)
+    S = 10
+    tapes = []
+    for _ in range(S):
+        d = rng.integers(0, 2 ** 32, 60000, dtype=np.uint64).astype(np.uint32)
+        tapes.append((d, ((d >> np.uint32(8)).astype(np.float32) + 1) / np.float32(16777216.0)))
+    tape = O.make_tape(tapes)
+    coef, ranks, consumed, bad = O.flip_schemes(n, m, coef0, S, 0, tape)
+    assert bad == 0 and (coef == coef0[None]).all() and (ranks == m).all()
+    assert list(consumed) == [0] + [1] * (S - 1)
+    coef, ranks, consumed, bad = O.flip_schemes(n, m, coef0, S, 40, tape)
+    assert bad == 0 and (coef[0] == coef0).all() and (ranks <= m).all() and (consumed[1:] >= 1).all()
+    bits = np.uint64(1) << np.arange(64, dtype=np.uint64)
+    fac = np.where(coef != 0, bits, np.uint64(0)).sum(axis=3, dtype=np.uint64)
+    sgn = np.where(coef < 0, bits, np.uint64(0)).sum(axis=3, dtype=np.uint64)
+    valid = np.zeros((S, 3, m), np.uint8)
+    for s in range(S):
+        valid[s, :, :ranks[s]] = 1
+        assert not coef[s, :, ranks[s]:].any()
+    assert O.validate_arrays("zt", np.tile(np.asarray(n, np.int32), (S, 1)), ranks, fac, sgn, valid).all()
+    assert (coef[1:] != coef0[None]).any()  # the flips changed schemes
