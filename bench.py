@@ -20,8 +20,20 @@ step uploads the records (fg_set_records), runs, and downloads them
 (fg_get_records); the copies are inside the timed region.
 
 `--impl reference` times the reference's algorithm on the host CPU cores (the
-CPU restatement in oracle/, all cores): the reference has no host walker of
-its own (its walk operators are __device__-only, scheme_z2.cuh:40-54).
+CPU restatement of its list-mode walk in oracle/, all cores): the reference has
+no host walker of its own (its walk operators are __device__-only,
+scheme_z2.cuh:40-54).
+
+Keys beside the headline, all measured after the timed region:
+  ref_cuda  the reference's own CUDA build (oracle/_ref, compiled from its
+            sources) on the same workload: its unmodified randomWalkKernel
+            timed with CUDA events, accepted flips counted by a twin kernel
+            checked state-for-state against it;
+  bitexact  this engine's reference mode (bit-exact trajectories) on the same
+            workload;
+  ttr       time to rank 23 on 3x3x3 (1,024 walks) for the fast, bit-exact and
+            learned-proposal modes and the reference's CUDA build, 3 seeds;
+  ttr_444   time to rank 47 on 4x4x4 (65,536 walks) within a 60 s budget.
 """
 import argparse
 import json
@@ -41,6 +53,7 @@ SHAPES = [(2, 2, 2), (2, 2, 3), (2, 3, 4), (3, 3, 4), (3, 4, 5), (4, 4, 4)]
 # factor word of the Z2 kernels: 32-bit in the fast mode (factors of <= 24 entries,
 # every shape here), 64-bit in the list modes
 WORD_BYTES = {"fast": 4, "philox": 8, "reference": 8}
+DTYPE = {"fast": "u32", "philox": "u64", "reference": "u64"}
 METRIC = "verified flips/s"
 CONFIG_NAME = "batched uneven Z2 search: 65,536 walks over (2,2,2),(2,2,3),(2,3,4),(3,3,4),(3,4,5),(4,4,4)"
 
@@ -142,7 +155,15 @@ def smem_peak_gbs():
 
 
 # ------------------------------------------------------------------ CPU side
-def cpu_walks(walks_per_shape, iterations, plus, seed, threads):
+# The oracle's two walks: "philox" is the reference's list algorithm (FlipSet lists, the
+# reference's candidate order and draw sites, scheme_z2.cu:531-641,982-1154) on the
+# Philox stream; "fast" is this engine's fast-mode walk (partner counts, canonical pair
+# order).  The reference itself has no host walker (its operators are __device__-only).
+CPU_WALKS = {"philox": "the reference's list-mode walk (FlipSet lists) on the Philox stream",
+             "fast": "the fast-mode walk (partner counts, canonical pair order) on the Philox stream"}
+
+
+def cpu_walks(walks_per_shape, iterations, plus, seed, threads, rng="philox"):
     """Oracle (CPU restatement) walks over every shape; returns (verified flips, seconds, walks)."""
     from oracle import oracle as O
     jobs = []
@@ -157,7 +178,7 @@ def cpu_walks(walks_per_shape, iterations, plus, seed, threads):
         n1, n2, n3, k, sd = job
         b = O.WalkBatch(k, 64, "z2")
         O.init_naive(b, n1, n2, n3)
-        cfg = b.cfg("fast", iterations=iterations, plus_iterations=plus, launches=1, expand_p=0.01, seed=sd)
+        cfg = b.cfg(rng, iterations=iterations, plus_iterations=plus, launches=1, expand_p=0.01, seed=sd)
         O.walk(b, cfg)
         ok = O.validate(b)
         results.append((int(b.accepted[ok].sum()), int(b.accepted.sum())))
@@ -170,28 +191,42 @@ def cpu_walks(walks_per_shape, iterations, plus, seed, threads):
     return sum(r[0] for r in results), dt, sum(j[3] for j in jobs)
 
 
-def cpu_baseline(args, seconds_target=15.0):
+def cpu_sample(rng, seconds_target, threads, wps):
+    """Grows the sample until it is about seconds_target of CPU work (at least a third of it)."""
+    iters = 200
+    while True:
+        v, dt, nw = cpu_walks(wps, iters, 100000, 8, threads, rng)
+        if dt >= seconds_target / 3 or iters >= 10_000_000:
+            return v, dt, nw, iters
+        iters = int(iters * min(50.0, max(2.0, seconds_target / max(dt, 1e-3))))
+
+
+def cpu_baseline(args, seconds_target=8.0):
+    """The oracle on all host cores: the reference's list algorithm (value) and the fast-mode
+    walk (fast_mode_port), each a bounded sample of the benchmark's six shapes."""
     threads = os.cpu_count() or 1
     wps = max(threads, 16)
     cpu_walks(wps, 10, 100000, 6, threads)  # loads the oracle library outside the timed samples
-    # Grow the sample until it is about seconds_target of CPU work (at least a third of it).
-    iters = 200
-    while True:
-        v, dt, nw = cpu_walks(wps, iters, 100000, 8, threads)
-        if dt >= seconds_target / 3 or iters >= 10_000_000:
-            break
-        iters = int(iters * min(50.0, max(2.0, seconds_target / max(dt, 1e-3))))
-    return {"value": v / dt, "unit": METRIC, "cores": threads, "kind": "port",
-            "sample": f"{nw} walks ({wps} per shape) x {iters} steps of the oracle's fast-stream walk, "
-                      f"{threads} host threads, {dt:.1f} s"}
+    out = {}
+    for rng in ("philox", "fast"):
+        v, dt, nw, iters = cpu_sample(rng, seconds_target, threads, wps)
+        out[rng] = {"value": v / dt, "unit": METRIC, "walk": CPU_WALKS[rng],
+                    "sample": f"{nw} walks ({wps} per shape) x {iters} steps, {threads} host threads, {dt:.1f} s"}
+    lst = out["philox"]
+    return {"value": lst["value"], "unit": METRIC, "cores": threads, "kind": "port",
+            "sample": f"{lst['walk']}: {lst['sample']}", "fast_mode_port": out["fast"]}
 
 
 def reference_arm(args):
+    """The reference's algorithm on the host cores: the oracle's restatement of its list-mode
+    walk (FlipSet lists, its candidate order and draw sites) on the Philox stream, all host
+    threads, over the benchmark's six shapes.  Each step is a bounded sample: --ref-walks-per-shape
+    walks of each shape (at least one per thread) x --ref-iterations steps."""
     ws, rank = dist_env()
     if rank != 0:
         return 0
     threads = os.cpu_count() or 1
-    wps = max(threads, 16)
+    wps = max(threads, args.ref_walks_per_shape)
     iters = args.ref_iterations
     for _ in range(args.warmup):
         cpu_walks(wps, max(10, iters // 10), 100000, 3, threads)
@@ -202,17 +237,102 @@ def reference_arm(args):
         tot_v += v
         tot_t += dt
     value = tot_v / tot_t
+    sample = (f"{nw} walks ({wps} per shape of the six) x {iters} steps per step, {CPU_WALKS['philox']}, "
+              f"{threads} host threads")
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * tot_t / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
             "data": "synthetic (naive starting schemes)",
-            "config": {"workload": CONFIG_NAME, "walks_sampled": nw, "iterations_per_step": iters,
-                       "plus_iterations": 100000, "expand_p": 0.01, "mode": "fast"},
-            "cpu_baseline": {"value": value, "unit": METRIC, "cores": threads, "kind": "port",
-                             "sample": f"{nw} walks x {iters} steps per step on {threads} threads"},
+            "config": {"workload": CONFIG_NAME, "walks_sampled": nw, "walks_per_shape": wps,
+                       "iterations_per_step": iters, "plus_iterations": 100000, "expand_p": 0.01,
+                       "walk": "reference list algorithm (oracle restatement), Philox stream",
+                       "note": "a bounded CPU sample of the GPU workload (65,536 walks x 10,000 steps does not fit "
+                               "a CPU step); flips/s is per walk-step independent of the walk count"},
+            "cpu_baseline": {"value": value, "unit": METRIC, "cores": threads, "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
     return 0
+
+
+# ------------------------------------------------------------------ reference CUDA build
+def ref_harness_path(ring):
+    import platform
+    p = os.path.join(ROOT, "oracle", "_ref", f"{ring}-{platform.machine()}", "ref_harness")
+    return p if os.path.exists(p) else None
+
+
+def run_ref_harness(ring, argv, timeout):
+    """One run of the reference's own CUDA build (oracle/_ref, compiled from its sources by
+    oracle/build_ref.sh) outside every timed region; returns its JSON line or a reason."""
+    exe = ref_harness_path(ring)
+    if exe is None:
+        return {"unavailable": f"no reference build for {ring} (oracle/_ref/{ring}-<machine>/ref_harness)"}
+    try:
+        r = subprocess.run([exe] + [str(a) for a in argv], stdout=subprocess.PIPE, stderr=subprocess.PIPE,
+                           text=True, timeout=timeout)
+    except subprocess.TimeoutExpired:
+        return {"unavailable": f"ref_harness {argv[0]} exceeded {timeout} s"}
+    lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
+    if r.returncode != 0 or not lines:
+        return {"unavailable": f"ref_harness {argv[0]} rc={r.returncode}: {r.stderr.strip()[-200:]}"}
+    return json.loads(lines[-1])
+
+
+def ref_cuda_baseline(args, walks, iterations, ours_value):
+    """The reference's unmodified randomWalkKernel (flip_graph.cu:520-573, Z2 build) on the
+    same six-shape workload, its accepted flips counted exactly by a counting twin run on a
+    copy of its state and checked equal state for state; plus its time to rank 23 on 3x3x3."""
+    shapes = [f"{a}x{b}x{c}" for a, b, c in SHAPES]
+    t = run_ref_harness("z2", ["time", walks, iterations, args.ref_cuda_launches, args.seed, args.plus_iterations]
+                        + shapes, timeout=600)
+    out = {"workload": f"{CONFIG_NAME}; {iterations} steps per launch, resize off, expand 0.01, plus after "
+                       f"{args.plus_iterations}", "kernel": "randomWalkKernel (unmodified, Z2 build, block 32)"}
+    if "unavailable" in t:
+        out["unavailable"] = t["unavailable"]
+        return out
+    out.update({"value": t["verified_flips_per_s"], "unit": METRIC, "ms_per_launch": t["ms_per_launch"],
+                "launches": t["launches"], "accepted_flips": t["accepted_flips"],
+                "verified_flips": t["verified_flips"], "twin_mismatches": t["twin_mismatches"],
+                "valid_walks": t["valid_walks"], "best_ranks": t["best_ranks"],
+                "ours_over_reference": ours_value / t["verified_flips_per_s"] if t["verified_flips_per_s"] else None})
+    return out
+
+
+# ------------------------------------------------------------------ time to target rank
+def ttr_one(fg, mode, shape, walks, target, plus, iters, seconds, seed, net=None, candidates=8, min_entropy=0.05):
+    """Wall time from engine creation until a verified best scheme reaches `target` (Z2, naive
+    start, plus after `plus` flips without a rank drop, flip limit 10^7 per walk, expand 0.01),
+    or the best rank after `seconds`."""
+    n1, n2, n3 = shape
+    cap = n1 * n2 * n3
+    t0 = time.perf_counter()
+    eng = fg.Engine(walks, cap, "z2", mode, seed, iters, plus, 0.01, 0.0, 0, 0)
+    if mode == "learned":
+        eng.set_proposal(net, candidates=candidates, temperature=1.0, min_entropy=min_entropy)
+    eng.init_naive(n1, n2, n3)
+    reached, launches, best, flips = False, 0, cap, 0
+    while launches * iters < 10_000_000 and time.perf_counter() - t0 < seconds:
+        st = eng.run(1)
+        launches += 1
+        flips += st["verified_flips"]
+        best = min(best, st["min_best_rank"])
+        if st["min_best_rank"] <= target:
+            c = eng.counters()
+            w = int(np.argmin(c["best_rank"]))
+            reached = bool(eng.validate(best=True)[w])
+            if reached:
+                break
+    dt = time.perf_counter() - t0
+    eng.close()
+    return {"mode": mode, "seed": seed, "reached": reached, "seconds": dt, "launches": launches,
+            "steps_per_walk": launches * iters, "best_rank": int(best), "verified_flips": int(flips)}
+
+
+def ttr_summary(runs):
+    ok = [r["seconds"] for r in runs if r["reached"]]
+    return {"reached": f"{len(ok)}/{len(runs)}", "median_seconds": statistics.median(ok) if ok else None,
+            "median_steps_per_walk": statistics.median([r["steps_per_walk"] for r in runs if r["reached"]]) if ok else None,
+            "runs": runs}
 
 
 def reduce_over_ranks(seconds, units, dist=None):
@@ -319,12 +439,13 @@ def gpu_arm(args):
                  "source": prof["issue_source"]}
     except (OSError, KeyError, ValueError):
         pass
+    eng.close()
     if rank == 0:
         cpu = cpu_baseline(args) if (ws == 1 and not args.no_cpu) else None
         line = {
             "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1000 * dev_s / args.steps, "wall_ms_per_step": 1000 * wall / args.steps,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": DTYPE[args.mode],
             "data": "synthetic (naive starting schemes)",
             "config": {"workload": CONFIG_NAME, "walks": walks, "iterations_per_step": iters,
                        "plus_iterations": args.plus_iterations, "expand_p": 0.01, "mode": args.mode,
@@ -346,46 +467,120 @@ def gpu_arm(args):
                     "steps": args.e2e_steps},
             "cpu_baseline": cpu,
         }
+        if ws == 1 and not args.no_extras:
+            line.update(extras(fg, args, value))
         print(json.dumps(line))
-    eng.close()
     if dist:
         dist.destroy_process_group()
     return 0
+
+
+def bitexact_leg(fg, args, walks, iterations):
+    """This engine's reference mode (bit-exact with the reference's kernel: its cuRAND XORWOW
+    stream, FlipSet lists and draw order) on the benchmark's six-shape workload."""
+    eng = fg.Engine(walks, 64, "z2", "reference", args.seed, iterations, args.plus_iterations, 0.01, 0.0, 0, 0)
+    eng.init_naive_shapes(shapes_for(walks))
+    eng.run(1)
+    v, ms = 0, 0.0
+    for _ in range(args.ref_cuda_launches):
+        st = eng.run(1)
+        v += st["verified_flips"]
+        ms += st["kernel_ms"] + st["verify_ms"]
+    eng.close()
+    return {"value": v / (ms / 1000.0), "unit": METRIC, "mode": "reference (bit-exact, XORWOW, FlipSet lists)",
+            "launches": args.ref_cuda_launches, "iterations_per_launch": iterations, "walks": walks}
+
+
+def extras(fg, args, value):
+    """Keys beside the headline, each outside the timed region: the reference's own CUDA build
+    on the same workload (ref_cuda), this engine's bit-exact mode there (bitexact), time to rank
+    23 on 3x3x3 per mode (ttr) and time to rank 47 on 4x4x4 (ttr_444)."""
+    log = lambda msg: print(f"[bench] {msg}", file=sys.stderr, flush=True)  # noqa: E731
+    out = {}
+    t = time.perf_counter()
+    ref = ref_cuda_baseline(args, args.walks, args.iterations, value)
+    be = bitexact_leg(fg, args, args.walks, args.iterations)
+    if "value" in ref:
+        be["over_reference_cuda"] = be["value"] / ref["value"]
+    out["ref_cuda"], out["bitexact"] = ref, be
+    log(f"ref_cuda and bitexact legs {time.perf_counter() - t:.1f} s")
+    # time to rank 23 on 3x3x3 (1,024 walks, plus after 50,000, flip limit 10^7)
+    t = time.perf_counter()
+    shape, target, walks = (3, 3, 3), 23, 1024
+    with fg.Engine(32, 27, "z2", "fast", 1, 10, 50000) as warm:  # CUDA context and module load
+        warm.init_naive(*shape)
+        warm.run(1)
+    ttr = {"workload": "time to rank 23, 3x3x3 Z2, 1,024 walks from the naive scheme, plus after 50,000 flips, "
+                       "flip limit 10^7 per walk, wall time from engine creation, every scheme verified exactly"}
+    for mode, iters in (("fast", 1000), ("reference", 1000)):
+        ttr[mode] = ttr_summary([ttr_one(fg, mode, shape, walks, target, 50000, iters, 60.0, sd)
+                                 for sd in args.ttr_seeds])
+    net, info = train_proposal(fg, args)
+    ttr["learned"] = ttr_summary([ttr_one(fg, "learned", shape, walks, target, 50000, 200, 60.0, sd, net=net,
+                                          candidates=args.learned_candidates) for sd in args.ttr_seeds])
+    ttr["learned"]["training"] = info
+    net.close()
+    refruns = []
+    for sd in args.ttr_seeds:
+        r = run_ref_harness("z2", ["ttr", 3, 3, 3, walks, 1000, 50000, sd, target, 60], timeout=120)
+        if "unavailable" not in r:
+            r = {"mode": "reference CUDA build", "seed": sd, **r, "reached": bool(r.get("reached"))}
+        refruns.append(r)
+    ttr["reference_cuda"] = (ttr_summary(refruns) if all("unavailable" not in r for r in refruns)
+                             else {"unavailable": refruns[0].get("unavailable")})
+    fast, lrn = ttr["fast"]["median_seconds"], ttr["learned"]["median_seconds"]
+    ttr["learned_over_uniform_time"] = lrn / fast if (fast and lrn) else None
+    out["ttr"] = ttr
+    log(f"ttr legs {time.perf_counter() - t:.1f} s")
+    # time to rank 47 on 4x4x4 (65,536 walks, plus after 10^5, within a 60 s budget)
+    t = time.perf_counter()
+    r = ttr_one(fg, "fast", (4, 4, 4), 65536, 47, 100000, 5000, args.ttr444_seconds, args.seed)
+    out["ttr_444"] = {"workload": f"time to rank 47, 4x4x4 Z2, 65,536 walks, plus after 100,000 flips, "
+                                  f"{args.ttr444_seconds:.0f} s budget", **r}
+    log(f"ttr_444 leg {time.perf_counter() - t:.1f} s")
+    return out
+
+
+def train_proposal(fg, args):
+    """Trains the flip-proposal network on records of plain walks of 3x3x3 (the time-to-rank
+    workload's shape); returns (net, summary)."""
+    t0 = time.perf_counter()
+    feats, labels, total, launches = [], [], 0, 0
+    with fg.Engine(16384, 27, "z2", "learned", args.seed, 2000, 50000, 0.01, 0.0) as eng:
+        eng.init_naive(3, 3, 3)
+        while total < args.ttr_learned_records and launches < 64:
+            f, y = eng.collect_records(every=args.learned_every, horizon=args.learned_horizon, launches=2,
+                                       capacity=1 << 22)
+            feats.append(f)
+            labels.append(y)
+            total += len(y)
+            launches += 2
+    f = np.concatenate(feats)[:args.ttr_learned_records]
+    y = np.concatenate(labels)[:args.ttr_learned_records]
+    t1 = time.perf_counter()
+    net = fg.Mlp(seed=args.seed)
+    loss = net.train(f, y, batch=8192, epochs=args.learned_epochs, lr=1e-3, seed=args.seed)
+    return net, {"records": int(len(y)), "positive_fraction": float(y.mean()) if len(y) else None,
+                 "collect_seconds": t1 - t0, "train_seconds": time.perf_counter() - t1, "final_loss": loss,
+                 "candidates": args.learned_candidates}
 
 
 def ttr_arm(args):
     """Time to target rank over Z2 from the naive scheme: --ttr-walks walks of --ttr-shape, plus
     transition after --ttr-plus flips without a rank drop, flip limit 10^7 per walk, stop when a
     verified best scheme reaches --ttr-target.  Launches of --ttr-iterations steps; wall time from
-    engine creation.  Prints one JSON line per mode."""
+    engine creation.  Prints one JSON line per mode and seed."""
     import flipgraphgpu_gb300 as fg
-    n1, n2, n3 = (int(x) for x in args.ttr_shape.split("x"))
-    cap = n1 * n2 * n3
-    with fg.Engine(32, cap, "z2", "fast", args.seed, 10, args.ttr_plus) as warm:  # CUDA context + module load
-        warm.init_naive(n1, n2, n3)
+    shape = tuple(int(x) for x in args.ttr_shape.split("x"))
+    with fg.Engine(32, shape[0] * shape[1] * shape[2], "z2", "fast", args.seed, 10, args.ttr_plus) as warm:
+        warm.init_naive(*shape)  # CUDA context and module load
         warm.run(1)
     for mode in args.ttr_modes.split(","):
-        iters = args.ttr_iterations
-        t0 = time.perf_counter()
-        eng = fg.Engine(args.ttr_walks, cap, "z2", mode, args.seed, iters, args.ttr_plus, 0.01, 0.0, 0, 0)
-        eng.init_naive(n1, n2, n3)
-        reached, launches, best, flips = False, 0, cap, 0
-        while launches * iters < 10_000_000 and time.perf_counter() - t0 < args.ttr_seconds:
-            st = eng.run(1)
-            launches += 1
-            flips += st["verified_flips"]
-            best = min(best, st["min_best_rank"])
-            if st["min_best_rank"] <= args.ttr_target:
-                c = eng.counters()
-                w = int(np.argmin(c["best_rank"]))
-                reached = bool(eng.validate(best=True)[w])
-                break
-        dt = time.perf_counter() - t0
-        eng.close()
-        print(json.dumps({"workload": f"time to rank {args.ttr_target}, {args.ttr_shape} Z2, {args.ttr_walks} walks",
-                          "mode": mode, "reached": reached, "seconds": dt, "launches": launches,
-                          "steps_per_walk": launches * iters, "best_rank": best, "verified_flips": flips,
-                          "plus_iterations": args.ttr_plus, "seed": args.seed}))
+        for sd in args.ttr_seeds:
+            r = ttr_one(fg, mode, shape, args.ttr_walks, args.ttr_target, args.ttr_plus, args.ttr_iterations,
+                        args.ttr_seconds, sd)
+            print(json.dumps({"workload": f"time to rank {args.ttr_target}, {args.ttr_shape} Z2, "
+                                          f"{args.ttr_walks} walks", "plus_iterations": args.ttr_plus, **r}))
     return 0
 
 
@@ -569,24 +764,40 @@ def post_arm(args):
 
 def zt_arm(args):
     """Integer-coefficient search: 16,384 walks per shape of (3,3,3) and (4,4,4) from the naive
-    schemes, exact integer verification; verified flips/s and ranks reached.  Ternary (ZT,
-    the reference's ring, reference stream) and bounded by |c| <= 2 (ZB, fast mode)."""
+    schemes, exact integer verification; verified flips/s and ranks reached.  Ternary (ZT, the
+    reference's default ring) and Z2 in this engine's bit-exact reference mode, each beside the
+    reference's own CUDA build on the same walks, steps and seed (ref_harness time, accepted flips
+    counted by its twin kernel); then bounded by |c| <= 2 (ZB, fast mode)."""
     import flipgraphgpu_gb300 as fg
-    for shape in ((3, 3, 3), (4, 4, 4)):
-        n1, n2, n3 = shape
-        eng = fg.Engine(args.zt_walks, n1 * n2 * n3, "zt", "reference", args.seed, args.zt_iterations, 100000, 0.01, 0.0, 0, 0)
-        eng.init_naive(n1, n2, n3)
-        eng.run(1)
-        tot_v, tot_ms = 0, 0.0
-        for _ in range(args.steps):
-            st = eng.run(1)
-            tot_v += st["verified_flips"]
-            tot_ms += st["kernel_ms"] + st["verify_ms"]
-        c = eng.counters()
-        print(json.dumps({"workload": f"ZT {n1}x{n2}x{n3}, {args.zt_walks} walks", "verified_flips_per_s": tot_v / (tot_ms / 1000),
-                          "steps": args.steps, "iterations_per_step": args.zt_iterations, "best_rank": int(c["best_rank"].min()),
-                          "walks_valid": int(c["valid"].sum())}))
-        eng.close()
+    for ring in ("zt", "z2"):
+        for shape in ((3, 3, 3), (4, 4, 4)):
+            n1, n2, n3 = shape
+            eng = fg.Engine(args.zt_walks, n1 * n2 * n3, ring, "reference", args.seed, args.zt_iterations, 100000,
+                            0.01, 0.0, 0, 0)
+            eng.init_naive(n1, n2, n3)
+            eng.run(1)
+            tot_v, tot_ms = 0, 0.0
+            for _ in range(args.steps):
+                st = eng.run(1)
+                tot_v += st["verified_flips"]
+                tot_ms += st["kernel_ms"] + st["verify_ms"]
+            c = eng.counters()
+            eng.close()
+            ours = tot_v / (tot_ms / 1000)
+            ref = run_ref_harness(ring, ["time", args.zt_walks, args.zt_iterations, args.steps, args.seed, 100000,
+                                         f"{n1}x{n2}x{n3}"], timeout=900)
+            line = {"workload": f"{ring.upper()} {n1}x{n2}x{n3}, {args.zt_walks} walks, bit-exact reference mode",
+                    "verified_flips_per_s": ours, "steps": args.steps, "iterations_per_step": args.zt_iterations,
+                    "best_rank": int(c["best_rank"].min()), "walks_valid": int(c["valid"].sum())}
+            if "unavailable" in ref:
+                line["ref_cuda"] = ref
+            else:
+                line["ref_cuda"] = {"verified_flips_per_s": ref["verified_flips_per_s"],
+                                    "ms_per_launch": ref["ms_per_launch"], "twin_mismatches": ref["twin_mismatches"],
+                                    "valid_walks": ref["valid_walks"], "best_ranks": ref["best_ranks"]}
+                line["ours_over_reference_cuda"] = ours / ref["verified_flips_per_s"]
+            print(json.dumps(line))
+            sys.stdout.flush()
     # Integer coefficients bounded by |c| <= 2 (fast mode; flips leaving the bound are rejected).
     for shape in ((3, 3, 3), (4, 4, 4)):
         n1, n2, n3 = shape
@@ -624,7 +835,13 @@ def main():
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--walks-per-block", type=int, default=0)
     ap.add_argument("--e2e-steps", type=int, default=3)
-    ap.add_argument("--ref-iterations", type=int, default=20000)
+    ap.add_argument("--ref-iterations", type=int, default=100000, help="reference arm: steps per walk per step")
+    ap.add_argument("--ref-walks-per-shape", type=int, default=64, help="reference arm: walks of each shape")
+    ap.add_argument("--ref-cuda-launches", type=int, default=2, help="timed launches of the reference CUDA build")
+    ap.add_argument("--no-extras", action="store_true", help="headline only: no ref_cuda, bitexact, ttr keys")
+    ap.add_argument("--ttr-seeds", type=lambda x: [int(v) for v in x.split(",")], default=[1, 2, 3])
+    ap.add_argument("--ttr444-seconds", type=float, default=60.0)
+    ap.add_argument("--ttr-learned-records", type=int, default=2_000_000)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-autotune", action="store_true", help="keep the static kernel choice")
     ap.add_argument("--fast-kernel", default=None, choices=["auto", "thread", "group", "warp"],

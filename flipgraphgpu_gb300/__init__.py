@@ -38,7 +38,7 @@ class Config(ctypes.Structure):
                 ("plus_iterations", ctypes.c_int32), ("expand_p", ctypes.c_double), ("reduce_p", ctypes.c_double),
                 ("device", ctypes.c_int32), ("walks_per_block", ctypes.c_int32), ("resize_p", ctypes.c_double),
                 ("sandwich_p", ctypes.c_double), ("basis_p", ctypes.c_double), ("gauss_p", ctypes.c_double),
-                ("zt_sandwich", ctypes.c_int32)]
+                ("zt_sandwich", ctypes.c_int32), ("retry_cap", ctypes.c_int32)]
 
 
 class _Records(ctypes.Structure):
@@ -198,13 +198,14 @@ class Engine:
 
     def __init__(self, walks, cap, ring="z2", mode="reference", seed=1, iterations=10000, plus_iterations=8000,
                  expand_p=0.01, reduce_p=0.0, device=0, walks_per_block=0, resize_p=0.0, sandwich_p=0.0,
-                 basis_p=0.0, gauss_p=0.0, zt_sandwich=False):
+                 basis_p=0.0, gauss_p=0.0, zt_sandwich=False, retry_cap=0):
         """mode: "reference" (XORWOW, reference lists, bit-exact), "philox" (Philox, lists) or
-        "fast" (Philox, implicit pair enumeration, thread-per-walk kernel)."""
+        "fast" (Philox, implicit pair enumeration, thread-per-walk kernel).  retry_cap bounds the
+        loops the reference leaves unbounded (0 = the library default, 2^20)."""
         self.lib = library()
         self.cfg = Config(RINGS[ring], MODES[mode], walks, cap, seed, iterations, plus_iterations, expand_p,
                           reduce_p, device, walks_per_block, resize_p, sandwich_p, basis_p, gauss_p,
-                          int(zt_sandwich))
+                          int(zt_sandwich), retry_cap)
         self.walks, self.cap, self.ring = walks, cap, ring
         self.h = ctypes.c_void_p()
         _check(self.lib.fg_create(ctypes.byref(self.cfg), ctypes.byref(self.h)))

@@ -14,6 +14,9 @@
 //                         modes; the reference defines SchemeZ2::tryReduceGauss but never calls it)
 //   --ternary-sandwiching 1  ZT: the sandwiching move conjugates by random signed permutations
 //                         (the reference's ternary sandwiching is empty)
+//   --retry-cap N         bound on the loops the reference leaves unbounded (tryPlus's pair
+//                         rejection, trySplitExisted, while (tryReduce())); a walk that exceeds it
+//                         stops and a warning is printed (0: the library default, 2^20)
 // Resize meta-operators (--resize-probability, default 0.2), sandwiching and
 // basis-change moves run on both rings in the reference and philox modes; in
 // the fast mode a positive probability is reported and treated as 0.
@@ -43,6 +46,7 @@ struct Options {
     std::string path, inputPath, ring, mode;
     double expand, reduce, sandwiching, basis, resize, gauss, timeBudget;
     bool ternarySandwiching;
+    int retryCap;
     long maxLaunches;
     int targetRank;
 };
@@ -101,10 +105,16 @@ public:
         auto startTime = Clock::now();
         auto t1 = Clock::now();
         std::vector<double> elapsedTimes;
+        int stopped = 0;
         for (long iteration = 0;; iteration++) {
             fg_stats st;
             fg_status s = resizeOn_ ? fg_run_walks(h_, 1, &st) : fg_run(h_, 1, &st);
             if (s != FG_OK && s != FG_ERR_WALK) check(s, "fg_run");
+            if (s == FG_ERR_WALK && st.walks_failed > stopped) {  // the reference would hang here
+                stopped = st.walks_failed;
+                std::cout << "Warning: " << stopped << " walk(s) stopped at a retry bound or a slot overflow "
+                          << "(their schemes are kept; the other walks go on)" << std::endl;
+            }
             auto t2 = Clock::now();
             elapsedTimes.push_back(std::chrono::duration_cast<std::chrono::milliseconds>(t2 - t1).count() / 1000.0);
             report(startTime, (int)iteration + 1, elapsedTimes);
@@ -174,6 +184,7 @@ private:
         c.basis_p = resizeHere(o_) ? o_.basis : 0.0;
         c.gauss_p = resizeHere(o_) && !zt_ ? o_.gauss : 0.0;
         c.zt_sandwich = o_.ternarySandwiching ? 1 : 0;
+        c.retry_cap = o_.retryCap;
         check(fg_create(&c, &h_), "fg_create");
     }
 
@@ -386,6 +397,8 @@ int main(int argc, char *argv[]) {
                "Gauss (XOR) reduction probability (divided by max iterations; Z2, list modes)", "0.0");
     parser.add("--ternary-sandwiching", ArgType::Natural, "0|1",
                "ZT: sandwiching conjugates by random signed permutations (the reference's move is empty)", "0");
+    parser.add("--retry-cap", ArgType::Natural, "INT",
+               "bound on the reference's unbounded retry loops (0: the library default)", "0");
     parser.add("--max-launches", ArgType::Natural, "INT", "stop after this many launches (0: never)", "0");
     parser.add("--target-rank", ArgType::Natural, "INT", "stop when a best rank reaches this (0: off)", "0");
     parser.add("--time-budget", ArgType::Real, "REAL", "stop after this many seconds (0: off)", "0");
@@ -409,6 +422,7 @@ int main(int argc, char *argv[]) {
     o.resize = std::stod(parser.get("--resize-probability"));
     o.gauss = std::stod(parser.get("--gauss-probability"));
     o.ternarySandwiching = parser.get("--ternary-sandwiching") == "1";
+    o.retryCap = std::stoi(parser.get("--retry-cap"));
     o.ring = parser.get("--ring");
     o.mode = parser.get("--mode");
     o.maxLaunches = std::stol(parser.get("--max-launches"));

@@ -263,6 +263,7 @@ void compute_params(fg_handle *h) {
     P.key0 = (uint32_t)c.seed;
     P.key1 = (uint32_t)(c.seed >> 32);
     P.random_iterations = c.resize_p > 0 ? 1 : 0;
+    P.retry_cap = c.retry_cap > 0 ? c.retry_cap : kRetryCap;
 }
 
 int verify_grid(fg_handle *h) { return (h->B.S + 3) / 4; }
@@ -514,6 +515,7 @@ fg_status fg_create(const fg_config *cfg, fg_handle **out) {
     if (cfg->resize_p > 0 && cfg->cap < FG_MAX_RANK)
         return fail(FG_ERR_CAPACITY, "resizing needs cap >= 350 (products reach the maximal rank)");
     if (cfg->iterations <= 0) return fail(FG_ERR_ARG, "iterations must be positive");
+    if (cfg->retry_cap < 0) return fail(FG_ERR_ARG, "retry_cap must be >= 0 (0 = the default bound)");
     fg_handle *h = new fg_handle;
     h->cfg = *cfg;
     h->dev = cfg->device;

@@ -65,7 +65,14 @@ struct WalkParams {
     int zt_sandwich;  // ZT: sandwiching by signed permutations (the reference's move is empty)
     uint32_t key0, key1;  // Philox key (seed)
     int random_iterations;  // resizing on: each launch runs randint(1, iterations) steps (flip_graph.cu:531)
+    int retry_cap;          // bound on the reference's unbounded retry loops (> 0)
 };
+
+// The retry bound of a walk's parameters; kRetryCap where a caller runs without them
+// (the additions reducer's flip pass).
+__device__ __forceinline__ int retry_cap_of(const WalkParams *P) {
+    return P && P->retry_cap > 0 ? P->retry_cap : kRetryCap;
+}
 
 __device__ __forceinline__ int lane_id() { return threadIdx.x & 31; }
 __device__ __forceinline__ unsigned lanemask_lt() { return (1u << lane_id()) - 1u; }

@@ -568,9 +568,22 @@ fg_status rfail(fg_status s, const char *msg) {
         if (e_ != cudaSuccess) return rfail(FG_ERR_CUDA, cudaGetErrorString(e_)); \
     } while (0)
 
+// k_reduce's dynamic shared-memory limit is one setting per process and device.
+// Every launcher only raises it, under one lock, to at least its launch's size:
+// a launch on another thread can then never find it lowered below its own size.
+std::mutex g_smem_limit_mu;
+
+cudaError_t raise_reduce_smem_limit(size_t bytes) {
+    std::lock_guard<std::mutex> lock(g_smem_limit_mu);
+    cudaFuncAttributes fa;
+    cudaError_t e = cudaFuncGetAttributes(&fa, k_reduce);
+    if (e != cudaSuccess) return e;
+    if ((size_t)fa.maxDynamicSharedSizeBytes >= bytes) return cudaSuccess;
+    return cudaFuncSetAttribute(k_reduce, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+}
+
 // Pair tables for expressions holding at most `nocc` pair occurrences: in shared
-// memory when they fit (the kernel's attribute is set at every launch, since other
-// handles may have set it smaller), else one slot per resident block in global memory.
+// memory when they fit, else one slot per resident block in global memory.
 fg_status plan_tables(fg_reducer *h, long nocc) {
     ReduceDims &D = h->D;
     const int m = h->m, nn[3] = {h->n1 * h->n2, h->n2 * h->n3, h->n3 * h->n1};
@@ -693,7 +706,7 @@ fg_status fg_reducer_run(fg_reducer *h, int independent, const int32_t *best_fre
     A.gscratch = h->d_scratch;
     A.slotBytes = h->slotBytes;
     A.ranks = h->flipped ? h->d_ranks : nullptr;
-    if (h->smem) RCUDA(cudaFuncSetAttribute(k_reduce, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)h->smem));
+    if (h->smem) RCUDA(raise_reduce_smem_limit(h->smem));
     k_reduce<<<h->d_scratch ? h->slots : A.count, reduce_threads(h->cfg.threads), h->smem>>>(A);
     RCUDA(cudaGetLastError());
     RCUDA(cudaMemcpy(out_counts, h->d_out, 4 * 13 * (size_t)A.count, cudaMemcpyDeviceToHost));
@@ -764,28 +777,23 @@ fg_status fg_reducer_destroy(fg_reducer *h) {
 // single file-scope scratch array, so a call makes no device allocation.  All
 // calls in the process share that array: calls that overlap in time (from two
 // host threads, or two devices' calls interleaved) race on it and must be
-// serialised by the caller.
+// serialised by the caller.  Its pair tables live in shared memory only (the
+// allocating path moves oversized tables to global memory; this one cannot).
 namespace {
 
 constexpr size_t kNoallocScratchBytes = (size_t)4 << 20;
 constexpr int kNoallocMaxCount = 1024;
-constexpr int kNoallocMaxDevices = 64;
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoallocScratchBytes];
 
-std::mutex g_noalloc_mu;
-unsigned char *g_noalloc_base[kNoallocMaxDevices] = {};
-
-// Device address of the scratch array on `dev`, looked up once per device.
-cudaError_t noalloc_base(int dev, unsigned char **base) {
-    std::lock_guard<std::mutex> lock(g_noalloc_mu);
-    if (!g_noalloc_base[dev]) {
-        void *p = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess) return e;
-        if (!p) return cudaErrorInvalidSymbol;
-        g_noalloc_base[dev] = static_cast<unsigned char *>(p);
-    }
-    *base = g_noalloc_base[dev];
+// Device address of the scratch array on the current device.  Resolved on every
+// call (a cheap runtime lookup), so a call after cudaDeviceReset, which ends the
+// context and with it the old address, gets the new context's address.
+cudaError_t noalloc_base(unsigned char **base) {
+    void *p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) return e;
+    if (!p) return cudaErrorInvalidSymbol;
+    *base = static_cast<unsigned char *>(p);
     return cudaSuccess;
 }
 
@@ -802,7 +810,7 @@ fg_status fg_reducer_run_noalloc(const fg_reducer_config *cfg, int n1, int n2, i
     if (cfg->count <= 0 || cfg->schemes <= 0) return rfail(FG_ERR_ARG, "count and schemes must be positive");
     if (n1 <= 0 || n2 <= 0 || n3 <= 0 || n1 * n2 > 64 || n2 * n3 > 64 || n3 * n1 > 64 || m <= 0 || m > FG_MAX_RANK)
         return rfail(FG_ERR_ARG, "scheme sizes out of range");
-    if (cfg->device < 0 || cfg->device >= kNoallocMaxDevices) return rfail(FG_ERR_ARG, "device out of range");
+    if (cfg->device < 0) return rfail(FG_ERR_ARG, "device out of range");
     if (cfg->count > kNoallocMaxCount) return rfail(FG_ERR_CAPACITY, "count above the no-allocation limit (1024)");
     int bf[3] = {0, 0, 0};
     for (int c = 0; c < 3; c++) {
@@ -853,7 +861,7 @@ fg_status fg_reducer_run_noalloc(const fg_reducer_config *cfg, int n1, int n2, i
     RCUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, cfg->device));
     if (smem > (size_t)optin) return rfail(FG_ERR_CAPACITY, "scheme too large for the shared-memory reducer");
     unsigned char *base = nullptr;
-    RCUDA(noalloc_base(cfg->device, &base));
+    RCUDA(noalloc_base(&base));
 
     std::vector<int16_t> bv(3 * 500 * 2, 0);
     for (int c = 0; c < 3; c++)
@@ -866,12 +874,7 @@ fg_status fg_reducer_run_noalloc(const fg_reducer_config *cfg, int n1, int n2, i
     auto *states = reinterpret_cast<curandStateXORWOW_t *>(base + oStates);
     k_seed_reducers<<<(cfg->count + 127) / 128, 128>>>(states, cfg->count, (unsigned long long)cfg->seed);
     RCUDA(cudaGetLastError());
-    // Raise (never lower) the kernel's dynamic shared-memory limit, so handles
-    // made by fg_reducer_create keep theirs.
-    cudaFuncAttributes fa;
-    RCUDA(cudaFuncGetAttributes(&fa, k_reduce));
-    if ((size_t)fa.maxDynamicSharedSizeBytes < smem)
-        RCUDA(cudaFuncSetAttribute(k_reduce, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    RCUDA(raise_reduce_smem_limit(smem));
 
     ReduceArgs A;
     A.count = cfg->count;

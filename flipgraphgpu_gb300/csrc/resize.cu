@@ -100,7 +100,7 @@ __device__ void swap_size(Z &z, int p1, int p2) {  // scheme_z2.cu:916-979, sche
 template <class Z>
 __device__ void reduce_all(Z &z) {  // while (tryReduce()) ; bounded
     for (int guard = 0; z.tryReduce(); guard++)
-        if (guard > kRetryCap) { z.status |= ST_RETRY; return; }
+        if (guard > retry_cap_of(z.r.P)) { z.status |= ST_RETRY; return; }
 }
 
 template <class Z>

@@ -48,7 +48,7 @@ template <class R, int S> struct RingOps<ZTWalk<R, S>> {
 template <class R>
 __device__ bool invertible_gf2(int n, uint32_t *m, uint32_t *inv, R &r, int &status) {
     const uint32_t low = n >= 32 ? 0xFFFFFFFFu : ((1u << n) - 1u);
-    for (int guard = 0; guard <= kRetryCap; guard++) {
+    for (int guard = 0, cap = retry_cap_of(r.P); guard <= cap; guard++) {
         uint64_t aug[16];
         for (int i = 0; i < n; i++) {
             m[i] = r.raw() & low;

@@ -330,7 +330,7 @@ struct SimtZ2 {
         int a = (int)r.below((uint32_t)m), b = (int)r.below((uint32_t)m);
         int guard = 0;
         while (a == b || F(0, a) == F(0, b) || F(1, a) == F(1, b) || F(2, a) == F(2, b)) {
-            if (++guard > kRetryCap) { status |= ST_RETRY; return false; }
+            if (++guard > retry_cap_of(r.P)) { status |= ST_RETRY; return false; }
             a = (int)r.below((uint32_t)m);
             b = (int)r.below((uint32_t)m);
         }

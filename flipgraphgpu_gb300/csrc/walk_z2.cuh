@@ -208,7 +208,7 @@ struct Z2Walk {
         int a = (int)r.below((uint32_t)m), b = (int)r.below((uint32_t)m);
         int guard = 0;
         while (a == b || X(0, a) == X(0, b) || X(1, a) == X(1, b) || X(2, a) == X(2, b)) {
-            if (++guard > kRetryCap) { status |= ST_RETRY; return false; }
+            if (++guard > retry_cap_of(r.P)) { status |= ST_RETRY; return false; }
             a = (int)r.below((uint32_t)m);
             b = (int)r.below((uint32_t)m);
         }

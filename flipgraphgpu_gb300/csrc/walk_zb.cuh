@@ -361,7 +361,7 @@ struct ZBWalk {
             return sim(get(c, a), B, v3neg(B, Lc[c]));
         };
         while (a == b || same(0) || same(1) || same(2)) {
-            if (++guard > kRetryCap) { status |= ST_RETRY; return false; }
+            if (++guard > retry_cap_of(r.P)) { status |= ST_RETRY; return false; }
             a = (int)r.below((uint32_t)m);
             b = (int)r.below((uint32_t)m);
         }

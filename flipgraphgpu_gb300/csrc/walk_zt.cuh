@@ -272,7 +272,7 @@ struct ZTWalk {
             rebuild();
             int guard = 0;
             while (tryReduce())
-                if (++guard > kRetryCap) { status |= ST_RETRY; break; }
+                if (++guard > retry_cap_of(r.P)) { status |= ST_RETRY; break; }
             return;
         }
         unsigned eqJ[S], eqK[S];
@@ -417,7 +417,7 @@ struct ZTWalk {
         int a = (int)r.below((uint32_t)m), b = (int)r.below((uint32_t)m);
         int guard = 0;
         while (a == b || teq(X(0, a), X(0, b)) || teq(X(1, a), X(1, b)) || teq(X(2, a), X(2, b))) {
-            if (++guard > kRetryCap) { status |= ST_RETRY; return false; }
+            if (++guard > retry_cap_of(r.P)) { status |= ST_RETRY; return false; }
             a = (int)r.below((uint32_t)m);
             b = (int)r.below((uint32_t)m);
         }
@@ -460,7 +460,7 @@ struct ZTWalk {
         int a, b, i;
         int guard = 0;
         do {
-            if (++guard > kRetryCap) { status |= ST_RETRY; return false; }
+            if (++guard > retry_cap_of(r.P)) { status |= ST_RETRY; return false; }
             a = (int)r.below((uint32_t)m);
             b = (int)r.below((uint32_t)m);
             i = (int)r.below(3);

@@ -86,6 +86,12 @@ typedef struct {
     int32_t zt_sandwich;      /* ZT: 1 = the sandwiching move conjugates by random signed permutation
                                  matrices (coefficients stay in {-1, 0, 1}); 0 (default) = the
                                  reference's empty ternary move (scheme_integer.cu:1215-1217) */
+    int32_t retry_cap;        /* bound on the loops the reference leaves unbounded (tryPlus's pair
+                                 rejection, scheme_z2.cu:1036-1039, scheme_integer.cu:984-987;
+                                 trySplitExisted, scheme_integer.cu:1029-1033; while (tryReduce()),
+                                 the invertible-matrix redraw): a walk that exceeds it stops with
+                                 FG_WALK_RETRY in its status and fg_run returns FG_ERR_WALK.
+                                 0 = the library default, 2^20 */
 } fg_config;
 
 /* Host-side walk records, structure of arrays over `walks` records with
@@ -376,10 +382,13 @@ fg_status fg_reducer_destroy(fg_reducer *h);
  * incumbent variables, outputs) placed in one static scratch array of 4 MiB
  * inside the library.  No counterpart in the reference, whose reducer always
  * allocates managed memory (scheme_additions_reducer.cu:4-29).  Inputs that
- * do not fit (count > 1024, or schemes * 3 * m * 64 coefficient bytes plus the
- * per-reducer buffers above 4 MiB) return FG_ERR_CAPACITY.  All calls share the
- * one scratch array: calls that overlap in time race on it, so the caller
- * serialises them. */
+ * do not fit return FG_ERR_CAPACITY: count > 1024; schemes * 3 * m * 64
+ * coefficient bytes plus the per-reducer buffers above 4 MiB; or pair tables
+ * larger than one block's shared memory (dense schemes, e.g. 4x4x4 at rank 51
+ * and up), which fg_reducer_create would move to allocated global memory.
+ * The scratch array's device address is looked up on every call, so calls
+ * may span a cudaDeviceReset.  All calls share the one scratch array: calls
+ * that overlap in time race on it, so the caller serialises them. */
 fg_status fg_reducer_run_noalloc(const fg_reducer_config *cfg, int n1, int n2, int n3, int m, const int8_t *coef,
                                  int independent, const int32_t *best_fresh, const int32_t *best_vars,
                                  int32_t *out_counts, float *out_scale);

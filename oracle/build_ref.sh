@@ -12,9 +12,12 @@
 #     (the reference's own flags plus -gencode for sm_103a and the
 #     `-include cstdint` shim its config.cuh needs) into
 #     oracle/_ref/{zt,z2}-<machine> (x86_64 here, aarch64 on the GPU machine).
+#     `build_ref.sh harness` builds only ref_harness (what the benchmark's
+#     reference-CUDA leg runs); no argument builds the three executables too.
 #
-# Nothing here modifies /root/reference, and nothing in the product links or
-# executes the result: it is used to generate and re-check tests/golden/.
+# Nothing here modifies the reference tree, and nothing in the product links or
+# executes the result: it is used to generate and re-check tests/golden/, and
+# bench.py runs ref_harness beside the product as the reference-CUDA baseline.
 set -e
 cd "$(dirname "$0")/.."
 REF="${FG_REFERENCE_DIR:-/root/reference}"
@@ -36,9 +39,11 @@ if ! command -v nvcc >/dev/null 2>&1; then
 fi
 JOBS="${FG_JOBS:-$(nproc)}"
 ARCHDIR="$(uname -m)"
-make -s -j"$JOBS" -f oracle/ref.mk SRC="$OUT/src_zt" OUT="$OUT/zt-$ARCHDIR" &
+TZT=""; TZ2=""
+if [ "${1:-}" = "harness" ]; then TZT="$OUT/zt-$ARCHDIR/ref_harness"; TZ2="$OUT/z2-$ARCHDIR/ref_harness"; fi
+make -s -j"$JOBS" -f oracle/ref.mk SRC="$OUT/src_zt" OUT="$OUT/zt-$ARCHDIR" $TZT &
 P1=$!
-make -s -j"$JOBS" -f oracle/ref.mk SRC="$OUT/src_z2" OUT="$OUT/z2-$ARCHDIR" &
+make -s -j"$JOBS" -f oracle/ref.mk SRC="$OUT/src_z2" OUT="$OUT/z2-$ARCHDIR" $TZ2 &
 P2=$!
 wait $P1; R1=$?
 wait $P2; R2=$?

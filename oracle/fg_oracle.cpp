@@ -40,6 +40,7 @@ namespace {
 constexpr int kMaxRank = 350;   // config.cuh:10
 constexpr int kMaxPairs = 500;  // config.cuh:14
 constexpr int kRetryCap = 1 << 20;
+inline int retry_cap(const fgo_walk_cfg *cfg) { return cfg->retry_cap > 0 ? cfg->retry_cap : kRetryCap; }
 constexpr int kMaxMatrix = 64;      // config.cuh:11 (64-bit factors)
 constexpr int kMaxExtensionN = 16;  // config.cuh:37
 enum { ST_TAPE = 1, ST_RETRY = 2, ST_OVERFLOW = 4 };
@@ -154,6 +155,8 @@ struct Z2 {
     uint64_t x[3][kMaxRank];
     FlipList lists[3];
     int32_t *status;
+    int retryCap = kRetryCap;  // fgo_walk_cfg::retry_cap (0 there = kRetryCap)
+    int slotCap = kMaxRank;    // the records' slots per walk (fgo_walk_cfg::cap)
     // Implicit pair enumeration (the library's fast mode): no FlipSet lists;
     // a flip samples an ordered equal-factor pair uniformly in the canonical
     // order (component c, term t ascending, partner t' ascending).
@@ -237,7 +240,7 @@ struct Z2 {
     }
 
     void addTriplet(int i, int j, int k, uint64_t a, uint64_t b, uint64_t c) {  // scheme_z2.cu:177-182
-        if (m >= kMaxRank) { *status |= ST_OVERFLOW; return; }
+        if (m >= kMaxRank || m >= slotCap) { *status |= ST_OVERFLOW; return; }
         x[i][m] = a; x[j][m] = b; x[k][m] = c;
         m++;
     }
@@ -319,7 +322,7 @@ struct Z2 {
         int a = (int)r.below(m), b = (int)r.below(m);
         int guard = 0;
         while (a == b || x[0][a] == x[0][b] || x[1][a] == x[1][b] || x[2][a] == x[2][b]) {
-            if (++guard > kRetryCap) { *status |= ST_RETRY; return false; }
+            if (++guard > retryCap) { *status |= ST_RETRY; return false; }
             a = (int)r.below(m);
             b = (int)r.below(m);
         }
@@ -498,7 +501,7 @@ struct Z2 {
     // elimination of [M | I] finds every pivot.  Rows are bit masks (entry (i, j) = bit j).
     template <class R> bool invertibleMatrix(int n_, uint32_t *mrow, uint32_t *inv, R &r) {
         const uint32_t low = n_ >= 32 ? 0xFFFFFFFFu : ((1u << n_) - 1u);
-        for (int guard = 0; guard <= kRetryCap; guard++) {
+        for (int guard = 0; guard <= retryCap; guard++) {
             for (int i = 0; i < n_; i++) mrow[i] = r.raw() & low;
             uint64_t aug[16];
             for (int i = 0; i < n_; i++) aug[i] = (uint64_t)mrow[i] | ((uint64_t)1 << (n_ + i));
@@ -784,7 +787,7 @@ struct Z2 {
 
     void reduceAll() {  // while (tryReduce()) ; (bounded)
         for (int guard = 0; tryReduce(); guard++)
-            if (guard > kRetryCap) { *status |= ST_RETRY; return; }
+            if (guard > retryCap) { *status |= ST_RETRY; return; }
     }
 
     template <class R> bool tryProject(R &r, int minN = 2) {  // scheme_z2.cu:1165-1185
@@ -929,6 +932,8 @@ struct ZT {
     Tern x[3][kMaxRank];
     FlipList lists[3];
     int32_t *status;
+    int retryCap = kRetryCap;  // fgo_walk_cfg::retry_cap (0 there = kRetryCap)
+    int slotCap = kMaxRank;    // the records' slots per walk (fgo_walk_cfg::cap)
 
     bool nonzero(int t) const { return x[0][t].v && x[1][t].v && x[2][t].v; }
 
@@ -974,7 +979,7 @@ struct ZT {
     }
 
     void addTriplet(int i, int j, int k, const Tern &a, const Tern &b, const Tern &c) {
-        if (m >= kMaxRank) { *status |= ST_OVERFLOW; return; }
+        if (m >= kMaxRank || m >= slotCap) { *status |= ST_OVERFLOW; return; }
         x[i][m] = a; x[j][m] = b; x[k][m] = c;
         m++;
     }
@@ -1035,7 +1040,7 @@ struct ZT {
             rebuildLists();
             int guard = 0;
             while (tryReduce())
-                if (++guard > kRetryCap) { *status |= ST_RETRY; break; }
+                if (++guard > retryCap) { *status |= ST_RETRY; break; }
             return;
         }
         for (int t = 0; t < m; t++) {
@@ -1124,7 +1129,7 @@ struct ZT {
         int a = (int)r.below(m), b = (int)r.below(m);
         int guard = 0;
         while (a == b || x[0][a] == x[0][b] || x[1][a] == x[1][b] || x[2][a] == x[2][b]) {
-            if (++guard > kRetryCap) { *status |= ST_RETRY; return false; }
+            if (++guard > retryCap) { *status |= ST_RETRY; return false; }
             a = (int)r.below(m);
             b = (int)r.below(m);
         }
@@ -1152,7 +1157,7 @@ struct ZT {
         int a, b, i;
         int guard = 0;
         do {
-            if (++guard > kRetryCap) { *status |= ST_RETRY; return false; }
+            if (++guard > retryCap) { *status |= ST_RETRY; return false; }
             a = (int)r.below(m);
             b = (int)r.below(m);
             i = (int)r.below(3);
@@ -1444,7 +1449,7 @@ struct ZT {
 
     void reduceAll() {
         for (int guard = 0; tryReduce(); guard++)
-            if (guard > kRetryCap) { *status |= ST_RETRY; return; }
+            if (guard > retryCap) { *status |= ST_RETRY; return; }
     }
     template <class R> bool tryProject(R &r, int minN = 2) {  // scheme_integer.cu:1103-1123
         int idx[3], size = 0;
@@ -1610,6 +1615,7 @@ void walkLaunch(Scheme &s, R &r, const fgo_walk_cfg *cfg, fgo_batch *b, int w) {
         int rank = s.m;
         if (!s.tryFlip(r, true)) {
             s.tryExpand(randint(1, 2, r), r);
+            if (b->status[w]) break;  // a retry bound or overflow stops the walk, as on the GPU
             continue;
         }
         if (b->accepted) b->accepted[w]++;
@@ -1651,6 +1657,8 @@ void runWalks(const fgo_walk_cfg *cfg, int S, fgo_batch *b, const fgo_tape *tape
         loadScheme(*s, b, w, cfg->cap);
         setImplicit(*s, cfg->rng == FGO_RNG_FAST);
         s->status = &b->status[w];
+        s->retryCap = retry_cap(cfg);
+        s->slotCap = cfg->cap;
         if (cfg->rng == FGO_RNG_TAPE) {
             RefDraws r;
             r.d = tape->draws + tape->offsets[w];
@@ -1698,6 +1706,8 @@ void runMinimize(const fgo_walk_cfg *cfg, int S, fgo_batch *b, const fgo_tape *t
         loadScheme(*s, b, w, cfg->cap);  // lists keep their persisted order
         setImplicit(*s, cfg->rng == FGO_RNG_FAST);
         s->status = &b->status[w];
+        s->retryCap = retry_cap(cfg);
+        s->slotCap = cfg->cap;
         if (cfg->rng == FGO_RNG_TAPE) {
             RefDraws r;
             r.d = tape->draws + tape->offsets[w];
@@ -1788,6 +1798,8 @@ struct ZB {
     int n[3], nn[3], m;
     ZBVec x[3][kMaxRank];
     int32_t *status;
+    int retryCap = kRetryCap;  // fgo_walk_cfg::retry_cap (0 there = kRetryCap)
+    int slotCap = kMaxRank;    // the records' slots per walk (fgo_walk_cfg::cap)
 
     int full() const { return n[0] * n[1] * n[2]; }
     bool zeroTerm(int t) const { return zbZero(x[0][t]) || zbZero(x[1][t]) || zbZero(x[2][t]); }
@@ -1821,7 +1833,7 @@ struct ZB {
             if (zeroTerm(t)) { removeAt(t); t--; }
     }
     void append(const ZBVec &a, const ZBVec &b, const ZBVec &c) {
-        if (m >= kMaxRank) { *status |= ST_OVERFLOW; return; }
+        if (m >= kMaxRank || m >= slotCap) { *status |= ST_OVERFLOW; return; }
         x[0][m] = a; x[1][m] = b; x[2][m] = c;
         m++;
     }
@@ -1918,7 +1930,7 @@ struct ZB {
         int a = (int)r.below((uint32_t)m), b = (int)r.below((uint32_t)m);
         int guard = 0;
         while (a == b || zbSim(x[0][a], x[0][b]) || zbSim(x[1][a], x[1][b]) || zbSim(x[2][a], x[2][b])) {
-            if (++guard > kRetryCap) { *status |= ST_RETRY; return false; }
+            if (++guard > retryCap) { *status |= ST_RETRY; return false; }
             a = (int)r.below((uint32_t)m);
             b = (int)r.below((uint32_t)m);
         }
@@ -2103,6 +2115,8 @@ void runWalksZB(const fgo_walk_cfg *cfg, int S, fgo_batch *b) {
         std::memset(s->x, 0, sizeof(s->x));
         loadZB(*s, b, w, cfg->cap);
         s->status = &b->status[w];
+        s->retryCap = retry_cap(cfg);
+        s->slotCap = cfg->cap;
         FastDraws r;
         r.key[0] = (uint32_t)cfg->seed;
         r.key[1] = (uint32_t)(cfg->seed >> 32);
@@ -2399,6 +2413,8 @@ void runResize(const fgo_walk_cfg *cfg, int S, fgo_batch *b, std::vector<R> &rs)
         loadScheme(cur[w], b, w, cap);
         loadBest(best[w], b, w, cap);
         cur[w].status = best[w].status = &b->status[w];
+        cur[w].retryCap = best[w].retryCap = retry_cap(cfg);
+        cur[w].slotCap = best[w].slotCap = cap;
     }
     std::map<std::string, int> table;
     table[sizeKey(cur[0].n)] = cur[0].n[0] * cur[0].n[1] * cur[0].n[2];

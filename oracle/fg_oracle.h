@@ -49,6 +49,7 @@ typedef struct {
                                  reference's walk, whose tryReduceGauss is never called) */
     int32_t zt_sandwich;      /* ZT: 1 = sandwiching by random signed permutations (the reference's
                                  ternary sandwiching is empty); 0 = as the reference */
+    int32_t retry_cap;        /* bound on the reference's unbounded retry loops; 0 = 2^20 */
 } fgo_walk_cfg;
 
 /* Structure-of-arrays batch of S walk records.  Factor arrays are [S][3][cap];

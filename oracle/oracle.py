@@ -56,7 +56,7 @@ class WalkCfg(ctypes.Structure):
                 ("launches", ctypes.c_int32), ("expand_p", ctypes.c_double),
                 ("reduce_p", ctypes.c_double), ("seed", ctypes.c_uint64), ("resize_p", ctypes.c_double),
                 ("sandwich_p", ctypes.c_double), ("basis_p", ctypes.c_double), ("gauss_p", ctypes.c_double),
-                ("zt_sandwich", ctypes.c_int32)]
+                ("zt_sandwich", ctypes.c_int32), ("retry_cap", ctypes.c_int32)]
 
 
 class _Batch(ctypes.Structure):
@@ -118,9 +118,10 @@ class WalkBatch:
         return _Batch(*[_ptr(getattr(self, f)) for f in self.FIELDS])
 
     def cfg(self, rng="tape", iterations=1000, plus_iterations=8000, launches=1, expand_p=0.01,
-            reduce_p=0.0, seed=0, resize_p=0.0, sandwich_p=0.0, basis_p=0.0, gauss_p=0.0, zt_sandwich=0):
+            reduce_p=0.0, seed=0, resize_p=0.0, sandwich_p=0.0, basis_p=0.0, gauss_p=0.0, zt_sandwich=0,
+            retry_cap=0):
         return WalkCfg(RING[self.ring], RNG[rng], self.cap, iterations, plus_iterations, launches,
-                       expand_p, reduce_p, seed, resize_p, sandwich_p, basis_p, gauss_p, zt_sandwich)
+                       expand_p, reduce_p, seed, resize_p, sandwich_p, basis_p, gauss_p, zt_sandwich, retry_cap)
 
 
 def make_tape(tapes):

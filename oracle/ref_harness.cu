@@ -384,70 +384,177 @@ static int cmd_gauss(int argc, char **argv) {
 }
 #endif
 
+// Counting twin of randomWalkKernel (flip_graph.cu:520-573, randomIterations
+// false): the same loop over the reference's own Scheme operators, taking the
+// same draws in the same order, plus one per-walk count of accepted flips
+// (tryFlip returned true).  cmd_time runs it on a copy of the state the
+// unmodified kernel starts from and checks on the device that both end in
+// byte-identical states, so the count is the unmodified kernel's.
+__global__ void countingWalkKernel(Scheme *schemes, Scheme *schemesBest, int *bestRanks, int *flips,
+                                   curandState *states, int schemesCount, int maxIterations, int plusIterations,
+                                   double reduceProbability, double expandProbability, double sandwichingProbability,
+                                   double basisProbability, unsigned long long *accepted) {
+    int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= schemesCount) return;
+    Scheme &scheme = schemes[idx];
+    curandState &state = states[idx];
+    int flipsCount = flips[idx];
+    int bestRank = bestRanks[idx];
+    unsigned long long count = 0;
+    for (int iteration = 0; iteration < maxIterations; iteration++) {
+        int rank = scheme.m;
+        if (!scheme.tryFlip(state)) {
+            scheme.tryExpand(randint(1, 2, state), state);
+            continue;
+        }
+        count++;
+        if (scheme.m < rank) flipsCount = 0;
+        flipsCount++;
+        if (scheme.m < bestRank || (scheme.m == bestRank && curand_uniform(&state) < 0.01)) {
+            bestRank = scheme.m;
+            scheme.copyTo(schemesBest[idx], false);
+        }
+        if (curand_uniform(&state) * maxIterations < reduceProbability) scheme.tryReduce();
+        if (curand_uniform(&state) * maxIterations < expandProbability && scheme.m <= schemesBest[idx].m + 2) {
+            if (scheme.tryExpand(randint(1, 2, state), state)) flipsCount = 0;
+        }
+        if (curand_uniform(&state) * maxIterations < sandwichingProbability) scheme.sandwiching(state);
+        if (curand_uniform(&state) * maxIterations < basisProbability) scheme.swapBasis(state);
+        if (flipsCount >= plusIterations && scheme.tryPlus(state)) flipsCount = 0;
+    }
+    flips[idx] = flipsCount;
+    bestRanks[idx] = bestRank;
+    accepted[idx] = count;
+}
+
+// Per walk: 1 when the two runs' schemes, best schemes, counters and cuRAND
+// states differ anywhere (whole structs, word by word); valid = validate().
+__global__ void compareWalksKernel(const Scheme *a, const Scheme *b, const Scheme *ab, const Scheme *bb,
+                                   const int *ar, const int *br, const int *af, const int *bf,
+                                   const curandState *as, const curandState *bs, int S, int *differs, int *valid) {
+    int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= S) return;
+    int d = ar[idx] != br[idx] || af[idx] != bf[idx];
+    const uint32_t *x = reinterpret_cast<const uint32_t *>(&a[idx]), *y = reinterpret_cast<const uint32_t *>(&b[idx]);
+    for (size_t q = 0; q < sizeof(Scheme) / 4 && !d; q++) d = x[q] != y[q];
+    x = reinterpret_cast<const uint32_t *>(&ab[idx]); y = reinterpret_cast<const uint32_t *>(&bb[idx]);
+    for (size_t q = 0; q < sizeof(Scheme) / 4 && !d; q++) d = x[q] != y[q];
+    x = reinterpret_cast<const uint32_t *>(&as[idx]); y = reinterpret_cast<const uint32_t *>(&bs[idx]);
+    for (size_t q = 0; q < sizeof(curandState) / 4 && !d; q++) d = x[q] != y[q];
+    differs[idx] = d;
+    valid[idx] = a[idx].validate() ? 1 : 0;
+}
+
+struct WalkArrays {
+    Scheme *schemes = nullptr, *best = nullptr;
+    int *bestRanks = nullptr, *flips = nullptr;
+    curandState *states = nullptr;
+    void alloc(int S) {
+        HCHECK(cudaMallocManaged(&schemes, S * sizeof(Scheme)));
+        HCHECK(cudaMallocManaged(&best, S * sizeof(Scheme)));
+        HCHECK(cudaMallocManaged(&bestRanks, S * sizeof(int)));
+        HCHECK(cudaMallocManaged(&flips, S * sizeof(int)));
+        HCHECK(cudaMallocManaged(&states, S * sizeof(curandState)));
+    }
+    void copyFrom(const WalkArrays &o, int S) {
+        HCHECK(cudaMemcpy(schemes, o.schemes, S * sizeof(Scheme), cudaMemcpyDefault));
+        HCHECK(cudaMemcpy(best, o.best, S * sizeof(Scheme), cudaMemcpyDefault));
+        HCHECK(cudaMemcpy(bestRanks, o.bestRanks, S * sizeof(int), cudaMemcpyDefault));
+        HCHECK(cudaMemcpy(flips, o.flips, S * sizeof(int), cudaMemcpyDefault));
+        HCHECK(cudaMemcpy(states, o.states, S * sizeof(curandState), cudaMemcpyDefault));
+    }
+    void release() { cudaFree(schemes); cudaFree(best); cudaFree(bestRanks); cudaFree(flips); cudaFree(states); }
+};
+
 // time S ITERS LAUNCHES SEED PLUS_ITERS shape... (e.g. 2x2x2 3x3x3)
 //   Throughput of the reference's own walk kernel on the batched uneven
 //   workload, set up the way the reference runs several shapes: one naive
 //   scheme per shape replicated idx % count by initializeCopyKernel
 //   (flip_graph.cu:459-470), best ranks per shape as updateRanks leaves them
-//   (flip_graph.cu:249-266), resize off.  Each launch is timed with CUDA
-//   events; flips are counted as S * ITERS per launch, an upper bound (every
-//   step of randomWalkKernel that finds no flip candidate is not a flip).
+//   (flip_graph.cu:249-266), resize off.  Each launch of the unmodified
+//   randomWalkKernel is timed with CUDA events.  Accepted flips come from the
+//   counting twin run on a copy of the same state; after every launch the two
+//   runs are compared on the device (twin_mismatches must be 0) and every
+//   scheme is validated: verified flips are the accepted flips of walks whose
+//   scheme passes validate() after the launch.
 static int cmd_time(int argc, char **argv) {
     if (argc < 8) { fprintf(stderr, "time: bad arguments\n"); return 1; }
     int S = atoi(argv[2]), iters = atoi(argv[3]), launches = atoi(argv[4]), seed = atoi(argv[5]);
     int plusIters = atoi(argv[6]);
     int count = argc - 7;
     int blockSize = 32, numBlocks = (S + blockSize - 1) / blockSize;
-    Scheme *schemes, *best; int *bestRanks, *flips; curandState *states;
-    HCHECK(cudaMallocManaged(&schemes, S * sizeof(Scheme)));
-    HCHECK(cudaMallocManaged(&best, S * sizeof(Scheme)));
-    HCHECK(cudaMallocManaged(&bestRanks, S * sizeof(int)));
-    HCHECK(cudaMallocManaged(&flips, S * sizeof(int)));
-    HCHECK(cudaMallocManaged(&states, S * sizeof(curandState)));
+    WalkArrays A, B;
+    A.alloc(S);
+    B.alloc(S);
+    unsigned long long *accepted; int *differs, *valid;
+    HCHECK(cudaMallocManaged(&accepted, S * sizeof(unsigned long long)));
+    HCHECK(cudaMallocManaged(&differs, S * sizeof(int)));
+    HCHECK(cudaMallocManaged(&valid, S * sizeof(int)));
     for (int i = 0; i < count; i++) {
         int a, b, c;
         if (sscanf(argv[7 + i], "%dx%dx%d", &a, &b, &c) != 3) { fprintf(stderr, "bad shape\n"); return 1; }
-        schemes[i].initializeNaive(a, b, c);
+        A.schemes[i].initializeNaive(a, b, c);
     }
-    initializeRandomStatesKernel<<<numBlocks, blockSize>>>(states, S, seed);
-    initializeCopyKernel<<<numBlocks, blockSize>>>(schemes, S, count);
+    initializeRandomStatesKernel<<<numBlocks, blockSize>>>(A.states, S, seed);
+    initializeCopyKernel<<<numBlocks, blockSize>>>(A.schemes, S, count);
     HCHECK(cudaDeviceSynchronize());
-    initializeSchemesKernel<<<numBlocks, blockSize>>>(schemes, best, bestRanks, flips, 1, 1, 1, S);
+    initializeSchemesKernel<<<numBlocks, blockSize>>>(A.schemes, A.best, A.bestRanks, A.flips, 1, 1, 1, S);
     HCHECK(cudaDeviceSynchronize());
-    for (int w = 0; w < S; w++) bestRanks[w] = schemes[w].m;
+    for (int w = 0; w < S; w++) A.bestRanks[w] = A.schemes[w].m;
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
     // One untimed launch brings managed memory to the device.
-    randomWalkKernel<<<numBlocks, blockSize>>>(schemes, best, bestRanks, flips, states, S, iters, plusIters,
+    randomWalkKernel<<<numBlocks, blockSize>>>(A.schemes, A.best, A.bestRanks, A.flips, A.states, S, iters, plusIters,
                                                0.0, 0.01, 0.0, 0.0, false);
     HCHECK(cudaDeviceSynchronize());
-    double total_ms = 0;
+    B.copyFrom(A, S);
+    double total_ms = 0, acceptedAll = 0, verifiedAll = 0;
+    long long mismatches = 0;
+    int validLast = 0;
     for (int L = 0; L < launches; L++) {
         cudaEventRecord(e0);
-        randomWalkKernel<<<numBlocks, blockSize>>>(schemes, best, bestRanks, flips, states, S, iters, plusIters,
-                                                   0.0, 0.01, 0.0, 0.0, false);
+        randomWalkKernel<<<numBlocks, blockSize>>>(A.schemes, A.best, A.bestRanks, A.flips, A.states, S, iters,
+                                                   plusIters, 0.0, 0.01, 0.0, 0.0, false);
         cudaEventRecord(e1);
         HCHECK(cudaEventSynchronize(e1));
         float ms = 0;
         cudaEventElapsedTime(&ms, e0, e1);
         total_ms += ms;
-        printf("launch %d: %.3f ms\n", L, ms);
+        countingWalkKernel<<<numBlocks, blockSize>>>(B.schemes, B.best, B.bestRanks, B.flips, B.states, S, iters,
+                                                     plusIters, 0.0, 0.01, 0.0, 0.0, accepted);
+        HCHECK(cudaGetLastError());
+        compareWalksKernel<<<numBlocks, blockSize>>>(A.schemes, B.schemes, A.best, B.best, A.bestRanks, B.bestRanks,
+                                                     A.flips, B.flips, A.states, B.states, S, differs, valid);
+        HCHECK(cudaGetLastError());
+        HCHECK(cudaDeviceSynchronize());
+        validLast = 0;
+        for (int w = 0; w < S; w++) {
+            mismatches += differs[w];
+            acceptedAll += (double)accepted[w];
+            if (valid[w]) verifiedAll += (double)accepted[w];
+            validLast += valid[w];
+        }
+        fprintf(stderr, "launch %d: %.3f ms\n", L, ms);
     }
     int minRank[64];
     for (int i = 0; i < count && i < 64; i++) minRank[i] = 1 << 30;
-    int valid = 0;
     for (int w = 0; w < S; w++) {
         int i = w % count;
-        if (i < 64 && bestRanks[w] < minRank[i]) minRank[i] = bestRanks[w];
-        valid += schemes[w].validate();
+        if (i < 64 && A.bestRanks[w] < minRank[i]) minRank[i] = A.bestRanks[w];
     }
     double flipsUpper = (double)S * iters * launches;
     printf("{\"walks\": %d, \"iterations\": %d, \"launches\": %d, \"ms_per_launch\": %.3f, "
-           "\"flips_per_s_upper_bound\": %.6e, \"valid_walks\": %d, \"best_ranks\": [",
-           S, iters, launches, total_ms / launches, flipsUpper / (total_ms / 1000.0), valid);
+           "\"accepted_flips\": %.0f, \"verified_flips\": %.0f, \"verified_flips_per_s\": %.6e, "
+           "\"flips_per_s_upper_bound\": %.6e, \"twin_mismatches\": %lld, \"valid_walks\": %d, \"ring\": \"%s\", "
+           "\"best_ranks\": [",
+           S, iters, launches, total_ms / launches, acceptedAll, verifiedAll, verifiedAll / (total_ms / 1000.0),
+           flipsUpper / (total_ms / 1000.0), mismatches, validLast, kRingIsZT ? "ZT" : "Z2");
     for (int i = 0; i < count && i < 64; i++) printf("%s%d", i ? ", " : "", minRank[i]);
     printf("]}\n");
+    A.release();
+    B.release();
+    cudaFree(accepted); cudaFree(differs); cudaFree(valid);
     return 0;
 }
 

@@ -59,3 +59,16 @@ def test_noalloc_rejects_oversize_inputs():
         fg.reducer_run_noalloc(n, m, coef[None], count=1025, schemes=1, seed=1)
     with pytest.raises(RuntimeError):
         fg.reducer_run_noalloc(n, m, np.repeat(coef[None], 1200, axis=0), count=8, schemes=1200, seed=1)
+
+
+def test_noalloc_rejects_pair_tables_beyond_shared_memory():
+    """A dense 4x4x4 scheme of rank 64: each of the 16 W expressions holds 64 variables,
+    2,016 pair occurrences each, far beyond one block's shared memory.  The allocating
+    path moves such tables to global memory; the no-allocation one reports capacity."""
+    n, m = (4, 4, 4), 64
+    coef = np.zeros((1, 3, m, 64), np.int8)
+    coef[0, :, :, :16] = 1
+    with pytest.raises(fg.FlipGraphError) as e:
+        fg.reducer_run_noalloc(n, m, coef, count=4, schemes=1, seed=1)
+    assert e.value.status == 3  # FG_ERR_CAPACITY
+    assert "shared-memory" in str(e.value)
