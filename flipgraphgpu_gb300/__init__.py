@@ -254,6 +254,13 @@ class Engine:
         self.lib.fg_rebuild_lists.restype = ctypes.c_int
         _check(self.lib.fg_rebuild_lists(self.h))
 
+    def set_list_kernel(self, kernel):
+        """List modes, Z2: 'thread' (one thread per walk; no resizing, sandwiching, basis changes
+        or Gauss reduction), 'warp' (one warp per walk) or 'auto'.  Results are identical."""
+        kinds = {"auto": -1, "warp": 0, "thread": 1}
+        self.lib.fg_set_list_kernel.restype = ctypes.c_int
+        _check(self.lib.fg_set_list_kernel(self.h, kinds[kernel]))
+
     def set_fast_kernel(self, kernel, lanes=0):
         """Fast mode kernel for every segment: 'thread', 'group' (lanes 4/8/16, 0 = auto),
         'warp', or 'auto'.  Results are identical; only speed changes."""

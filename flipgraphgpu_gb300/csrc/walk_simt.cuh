@@ -40,8 +40,12 @@ struct ThreadPhilox {
     }
     __device__ __forceinline__ uint32_t below(uint32_t k) { return __umulhi(raw(), k); }
     __device__ __forceinline__ bool coin() { return raw() >> 31; }
-    __device__ __forceinline__ bool gate_reduce() { return P->reduce_T != kGateOff && (uint64_t)raw() < P->reduce_T; }
-    __device__ __forceinline__ bool gate_expand() { return P->expand_T != kGateOff && (uint64_t)raw() < P->expand_T; }
+    __device__ __forceinline__ bool gate(uint64_t T) { return T != kGateOff && (uint64_t)raw() < T; }
+    __device__ __forceinline__ bool gate_reduce() { return gate(P->reduce_T); }
+    __device__ __forceinline__ bool gate_expand() { return gate(P->expand_T); }
+    __device__ __forceinline__ bool gate_sandwich() { return gate(P->sandwich_T); }
+    __device__ __forceinline__ bool gate_basis() { return gate(P->basis_T); }
+    __device__ __forceinline__ bool gate_gauss() { return gate(P->gauss_T); }
     __device__ __forceinline__ bool tie() { return raw() < 42949672u; }
     __device__ __forceinline__ uint64_t mask(int nn) { return nn >= 32 ? (uint64_t)raw() : (uint64_t)(raw() & ((1u << nn) - 1u)); }
 };

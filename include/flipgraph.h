@@ -256,6 +256,18 @@ fg_status fg_rebuild_lists(fg_handle *h);
 enum { FG_FAST_THREAD = 0, FG_FAST_GROUP = 1, FG_FAST_WARP = 2 };
 fg_status fg_set_fast_kernel(fg_handle *h, int kernel, int lanes);
 
+/* List modes (reference stream and philox lists) on the Z2 ring: the kernel that
+ * runs randomWalkKernel's loop (flip_graph.cu:520-573).  FG_LIST_WARP = one warp
+ * per walk (every option, including resizing, sandwiching, basis changes and the
+ * Gauss reduction); FG_LIST_THREAD = one thread per walk with the FlipSet lists
+ * in a device scratch of 6,000 bytes per walk, allocated on first use (only
+ * with resizing, sandwiching, basis changes and the Gauss reduction off);
+ * -1 = automatic (thread per walk where it applies and the batch has enough
+ * walks to fill the GPU).  Both give identical results.  FG_LIST_THREAD on a
+ * configuration it does not cover returns FG_ERR_ARG. */
+enum { FG_LIST_WARP = 0, FG_LIST_THREAD = 1 };
+fg_status fg_set_list_kernel(fg_handle *h, int kernel);
+
 /* Z2 fast mode: chooses each shape segment's kernel (thread per walk with 1, 2
  * or 4 warps per block; 8, 16 or 32 lanes per walk) by timing the step's
  * concurrent launches of all segments for `iterations` steps: from the static

@@ -47,16 +47,23 @@ def test_philox_device_matches_oracle():
         assert list(out[q]) == O.philox([int(x) for x in ctr[q]], list(key))
 
 
+@pytest.mark.parametrize("list_kernel", ["warp", "thread"])
 @pytest.mark.parametrize("path", walk_fixtures(), ids=lambda p: p.split("/")[-1].split(".")[0])
-def test_walk_matches_reference_kernel(path):
-    """Same seed, same flags: the library reproduces the reference's per-launch state."""
+def test_walk_matches_reference_kernel(path, list_kernel):
+    """Same seed, same flags: the library reproduces the reference's per-launch state, with one
+    warp per walk and (Z2 without the resize, sandwiching and basis moves) one thread per walk."""
     d = golden_io.read_walk(path)
     ring = d["ring"]
+    moves = d["resize_p"] > 0 or d["sandwich_p"] > 0 or d["basis_p"] > 0
+    if list_kernel == "thread" and (ring != "z2" or moves):
+        pytest.skip("the thread-per-walk list kernel covers Z2 without resize, sandwiching and basis moves")
     n1, n2, n3 = d["n"]
     cap = 352 if d["resize_p"] > 0 else n1 * n2 * n3
     with fg.Engine(d["walks"], cap, ring, "reference", d["seed"], d["iterations"], d["plus_iterations"],
                    d["expand_p"], d["reduce_p"], resize_p=d["resize_p"], sandwich_p=d["sandwich_p"],
                    basis_p=d["basis_p"]) as eng:
+        if ring == "z2" and not moves:
+            eng.set_list_kernel(list_kernel)
         eng.init_naive(n1, n2, n3)
         for L, block in enumerate(d["launches"]):
             eng.run(1)
@@ -226,12 +233,14 @@ def test_walk_fast_mode_vs_oracle(shapes, iters, plus, expand_p, reduce_p, kerne
     ((2, 5, 5), 16, 800, 200, 0.01, 0.0, 1),   # nn = 25 x 25 x 10, cap 50 -> two slots per lane
     ((4, 5, 8), 8, 400, 200, 0.01, 0.0, 1),    # nn = 20 x 40 x 32, cap 160, > 32-bit factors
 ])
-def test_walk_reference_stream_vs_oracle(shape, S, iters, plus, expand_p, reduce_p, launches):
+@pytest.mark.parametrize("list_kernel", ["warp", "thread"])
+def test_walk_reference_stream_vs_oracle(shape, S, iters, plus, expand_p, reduce_p, launches, list_kernel):
     n1, n2, n3 = shape
     cap = n1 * n2 * n3
     seed = 1000 + n1 * 100 + n2 * 10 + n3
     kw = dict(iterations=iters, plus_iterations=plus, expand_p=expand_p, reduce_p=reduce_p)
     with fg.Engine(S, cap, "z2", "xorwow", seed, iters, plus, expand_p, reduce_p) as eng:
+        eng.set_list_kernel(list_kernel)
         eng.init_naive(n1, n2, n3)
         rec0 = eng.records()
         eng.run(launches)
@@ -252,12 +261,14 @@ def test_walk_reference_stream_vs_oracle(shape, S, iters, plus, expand_p, reduce
     ((3, 4, 5), 32, 1500, 600, 4.0, 0.0),
     ((4, 5, 8), 8, 500, 200, 0.01, 0.0),
 ])
-def test_walk_fast_stream_vs_oracle(shape, S, iters, plus, expand_p, reduce_p):
+@pytest.mark.parametrize("list_kernel", ["warp", "thread"])
+def test_walk_fast_stream_vs_oracle(shape, S, iters, plus, expand_p, reduce_p, list_kernel):
     n1, n2, n3 = shape
     cap = n1 * n2 * n3
     seed = 77 + n1 + n2 + n3
     kw = dict(iterations=iters, plus_iterations=plus, expand_p=expand_p, reduce_p=reduce_p, seed=seed)
     with fg.Engine(S, cap, "z2", "philox", seed, iters, plus, expand_p, reduce_p) as eng:
+        eng.set_list_kernel(list_kernel)
         eng.init_naive(n1, n2, n3)
         rec0 = eng.records()
         eng.run(2)
@@ -457,3 +468,31 @@ def test_fast_minimize_vs_oracle(shape, S):
     for f in ("m", "fac", "best_m", "best_fac", "rng_pos", "status"):
         a, o = getattr(rec, f), getattr(b, f)
         assert np.array_equal(a, o), f
+
+
+@pytest.mark.parametrize("mode", ["reference", "philox"])
+def test_list_kernels_agree_on_a_large_mixed_batch(mode):
+    """20,480 walks over six shapes: the automatic choice takes the thread-per-walk list kernel
+    (enough walks to fill the GPU); it equals the warp-per-walk kernel field for field."""
+    shapes = [(2, 2, 2), (2, 2, 3), (2, 3, 4), (3, 3, 4), (3, 4, 5), (4, 4, 4)]
+    S = 20480
+    sh = np.array([shapes[w * len(shapes) // S] for w in range(S)], np.int32)
+    out = {}
+    for kernel in ("warp", "thread", "auto"):
+        with fg.Engine(S, 64, "z2", mode, 5, 600, 300, 2.0, 0.0) as eng:
+            eng.set_list_kernel(kernel)
+            eng.init_naive_shapes(sh)
+            eng.run(2)
+            out[kernel] = eng.records()
+            assert eng.validate().all() and eng.validate(best=True).all()
+    compare_records(out["thread"], out["warp"], f"{mode} thread vs warp")
+    compare_records(out["auto"], out["warp"], f"{mode} auto vs warp")
+
+
+def test_thread_list_kernel_is_refused_where_it_does_not_apply():
+    with fg.Engine(32, 27, "zt", "reference", 1, 10, 100) as eng:
+        with pytest.raises(fg.FlipGraphError):
+            eng.set_list_kernel("thread")
+    with fg.Engine(32, 352, "z2", "reference", 1, 10, 100, resize_p=0.2) as eng:
+        with pytest.raises(fg.FlipGraphError):
+            eng.set_list_kernel("thread")
