@@ -213,7 +213,7 @@ struct fg_handle {
     int simtMaxCap = -1;                  // fg_set_fast_split: thread per walk up to this slot count (-1: off)
     int fastKernel = -1, groupLanes = 0;  // fg_set_fast_kernel override (-1: per-segment choice)
     int listKernel = -1;                  // fg_set_list_kernel override (-1: automatic)
-    uint32_t *d_listScratch = nullptr;    // thread-per-walk list kernel: lists interleaved by walk
+    void *d_listScratch = nullptr;        // thread-per-walk list kernel: lists interleaved by walk
     // Fast mode: the walk launches of one step (all segments, forked and joined) as a CUDA
     // graph, captured on first use and dropped whenever the launch plan changes.
     cudaGraphExec_t walkGraph = nullptr;
@@ -439,49 +439,53 @@ cudaError_t launch_segments(fg_handle *h) {
     return cudaSuccess;
 }
 
-// List modes: the thread-per-walk list kernel covers the Z2 ring without resizing,
+// List modes: the thread-per-walk list kernel covers both rings without resizing,
 // sandwiching, basis changes or the Gauss reduction (their moves run in the warp kernel).
 bool list_thread_possible(const fg_config &c) {
-    return c.ring == FG_RING_Z2 && (c.mode == FG_MODE_REFERENCE || c.mode == FG_MODE_PHILOX_LISTS) &&
+    return (c.ring == FG_RING_Z2 || c.ring == FG_RING_ZT) &&
+           (c.mode == FG_MODE_REFERENCE || c.mode == FG_MODE_PHILOX_LISTS) &&
            !(c.resize_p > 0) && !(c.sandwich_p > 0) && !(c.basis_p > 0) && !(c.gauss_p > 0);
 }
 
 // Automatic choice: thread per walk when every segment's factors fit a block's shared
 // memory and the batch gives at least kListThreadWarpsPerSM warps of walks per SM (with
 // fewer walks one warp per walk fills the GPU better).  Measured on GB300, reference
-// stream, 3x3x3: 8,192 walks (1.7 warps per SM) 1.17 G flips/s with a thread per walk
-// against 0.75 G with a warp; 4,096 walks 0.59 G against 0.71 G.
-constexpr double kListThreadWarpsPerSM = 1.5;
+// stream, 3x3x3: Z2 with 8,192 walks (1.7 warps per SM) 1.14 G flips/s with a thread per
+// walk against 0.78 G with a warp, 4,096 walks 0.57 G against 0.70 G; ZT with 16,384 walks
+// (3.4 warps per SM) 285 M against 205 M, 8,192 walks 150 M against 198 M.
+constexpr double kListThreadWarpsPerSM[2] = {1.5, 3.0};  // Z2, ZT
 
 bool list_thread_chosen(const fg_handle *h) {
     if (h->listKernel == FG_LIST_WARP || !list_thread_possible(h->cfg)) return false;
     int optin = 0;
     cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->dev);
-    for (const Segment &g : h->segs)
-        if (simt_list_smem_per_warp(g.scap, g.nnmax > 32) > (size_t)optin) return false;
+    for (const Segment &g : h->segs) {
+        if (g.scap > 256 || simt_list_smem_per_warp(h->cfg.ring, g.scap, g.nnmax) > (size_t)optin) return false;
+        if (h->cfg.ring == FG_RING_ZT && g.nnmax > 16) return false;  // ternary words hold 16 entries
+    }
     if (h->listKernel == FG_LIST_THREAD) return true;
-    return (double)h->B.S / 32.0 / (h->sms > 0 ? h->sms : 1) >= kListThreadWarpsPerSM;
+    return (double)h->B.S / 32.0 / (h->sms > 0 ? h->sms : 1) >= kListThreadWarpsPerSM[h->cfg.ring == FG_RING_ZT];
 }
 
 // One thread-per-walk list launch per segment, forked from and joined into h->stream.
 cudaError_t launch_list_segments(fg_handle *h) {
     cudaError_t e;
     if (!h->d_listScratch) {
-        e = cudaMalloc((void **)&h->d_listScratch, simt_list_scratch_words(h->B.S) * sizeof(uint32_t));
+        e = cudaMalloc(&h->d_listScratch, simt_list_scratch_bytes(h->cfg.ring, h->B.S));
         if (e != cudaSuccess) { h->d_listScratch = nullptr; return e; }
     }
     const int rng = h->cfg.mode == FG_MODE_REFERENCE ? RNG_XORWOW : RNG_PHILOX;
     const int wpb = h->cfg.walks_per_block > 0 ? std::min(h->cfg.walks_per_block, 8) : 2;  // warps per block
     if (h->segs.size() == 1) {
         const Segment &g = h->segs[0];
-        return launch_walk_simt_list(h->B, h->P, rng, g.first, g.count, g.scap, g.nnmax > 32, wpb, h->sms,
+        return launch_walk_simt_list(h->cfg.ring, h->B, h->P, rng, g.first, g.count, g.scap, g.nnmax, wpb, h->sms,
                                      h->d_listScratch, h->stream);
     }
     if ((e = cudaEventRecord(h->fork, h->stream)) != cudaSuccess) return e;
     for (size_t i = 0; i < h->segs.size(); i++) {
         const Segment &g = h->segs[i];
         if ((e = cudaStreamWaitEvent(h->side[i], h->fork, 0)) != cudaSuccess) return e;
-        if ((e = launch_walk_simt_list(h->B, h->P, rng, g.first, g.count, g.scap, g.nnmax > 32, wpb, h->sms,
+        if ((e = launch_walk_simt_list(h->cfg.ring, h->B, h->P, rng, g.first, g.count, g.scap, g.nnmax, wpb, h->sms,
                                        h->d_listScratch, h->side[i])) != cudaSuccess)
             return e;
         if ((e = cudaEventRecord(h->join[i], h->side[i])) != cudaSuccess) return e;
@@ -768,7 +772,7 @@ fg_status fg_set_list_kernel(fg_handle *h, int kernel) {
     if (!h) return fail(FG_ERR_ARG, "null handle");
     if (kernel < -1 || kernel > FG_LIST_THREAD) return fail(FG_ERR_ARG, "kernel in -1..1");
     if (kernel == FG_LIST_THREAD && !list_thread_possible(h->cfg))
-        return fail(FG_ERR_ARG, "the thread-per-walk list kernel runs on Z2 in a list mode without resizing, "
+        return fail(FG_ERR_ARG, "the thread-per-walk list kernel runs in a list mode without resizing, "
                                 "sandwiching, basis changes or the Gauss reduction");
     h->listKernel = kernel;
     return FG_OK;

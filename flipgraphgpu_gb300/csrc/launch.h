@@ -27,14 +27,15 @@ int occupancy_walk(int ring, int cap, int rng, int wpb);
 // factor slots per walk in shared memory; wide = 64-bit words (nn > 24).
 cudaError_t launch_walk_simt(const DevBatch &B, const WalkParams &P, int first, int count, int scap, int wide,
                              int wpb, int sms, cudaStream_t s);
-// List modes (Z2; resize, sandwiching, basis and Gauss moves off): thread-per-walk walk over
-// walks [first, first + count) with the reference's FlipSet lists; rng RNG_XORWOW (bit-exact)
-// or RNG_PHILOX.  `lists` is a scratch of simt_list_scratch_words(S) words; wide = 64-bit
-// factor words (factors of more than 32 entries).
-cudaError_t launch_walk_simt_list(const DevBatch &B, const WalkParams &P, int rng, int first, int count, int scap,
-                                  int wide, int wpb, int sms, uint32_t *lists, cudaStream_t s);
-size_t simt_list_smem_per_warp(int scap, int wide);
-size_t simt_list_scratch_words(int walks);
+// List modes (resize, sandwiching, basis and Gauss moves off): thread-per-walk walk over
+// walks [first, first + count) with the reference's FlipSet lists; ring 0 = Z2, 1 = ZT
+// (factors of at most 16 entries); rng RNG_XORWOW (bit-exact) or RNG_PHILOX.  `scratch`
+// holds simt_list_scratch_bytes(ring, S) bytes (16-byte aligned); scap <= 256; nnmax = the
+// segment's largest factor size (Z2 factor words of 16, 32 or 64 bits follow from it).
+cudaError_t launch_walk_simt_list(int ring, const DevBatch &B, const WalkParams &P, int rng, int first, int count,
+                                  int scap, int nnmax, int wpb, int sms, void *scratch, cudaStream_t s);
+size_t simt_list_smem_per_warp(int ring, int scap, int nnmax);
+size_t simt_list_scratch_bytes(int ring, int walks);
 // Fast mode complexity minimizer (minimizeKernel), one thread per walk; bestC[w] is the
 // walk's best complexity so far, lowered in place.
 cudaError_t launch_minimize_simt(const DevBatch &B, const WalkParams &P, int first, int count, int scap, int wide,

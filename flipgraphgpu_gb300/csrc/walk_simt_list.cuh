@@ -8,10 +8,11 @@
 // Layout.  Factors live in shared memory, 32 walks interleaved by lane: word
 // (c, t) of the lane's walk at x[(c * ld + t) * 32], so every access a thread
 // makes to its own walk hits bank `lane`.  The three FlipSet lists live in a
-// global scratch buffer, interleaved the same way per group of 32 walks:
-// entry (c, q) at L[(c * kListCap + q) * 32]; a warp scanning entry q of its 32
-// walks reads one 128-byte line.  The lists' live part (a few hundred entries
-// per walk) stays in L2.
+// global scratch buffer as 16-bit pairs (a << 8 | b; slots <= 256), eight to a
+// 16-byte vector, the vectors of a group of 32 walks interleaved by lane:
+// vector (c, v) of the lane's walk at V[(c * kListVecs + v) * 32].  A list scan
+// loads 8 entries per thread per load (a warp reads 512 contiguous bytes) and
+// tests them with byte-wise SIMD compares.  The lists' live part stays in L2.
 #pragma once
 #include "fg_device.cuh"
 #include "walk_simt.cuh"
@@ -21,15 +22,75 @@ namespace fg {
 // Per-thread XORWOW (the reference's stream), one cuRAND state per walk.
 using ThreadXorwow = XorwowDraws;
 
+// 16-bit list entries: eight per 16-byte vector, ceil(500 / 8) vectors per component.
+constexpr int kListVecs = (kListCap + 7) / 8;
+
+__device__ __forceinline__ uint32_t pack16(int a, int b) { return ((uint32_t)a << 8) | (uint32_t)b; }
+
+// Bit e (0..7) set when entry e of the vector holds index idx (< 256) in either half.
+__device__ __forceinline__ unsigned vec_touch_mask(const uint4 &v, uint32_t idx) {
+    const uint32_t rep = idx * 0x01010101u;
+    const uint32_t w[4] = {__vcmpeq4(v.x, rep), __vcmpeq4(v.y, rep), __vcmpeq4(v.z, rep), __vcmpeq4(v.w, rep)};
+    unsigned m = 0;
+#pragma unroll
+    for (int q = 0; q < 4; q++) m |= (((w[q] & 0xFFFFu) ? 1u : 0u) | ((w[q] >> 16) ? 2u : 0u)) << (2 * q);
+    return m;
+}
+
+// The three FlipSet lists of one walk (flip_set.cu) in the scratch layout above, with
+// the reference's append and swap-with-last removal order.
+struct SimtLists {
+    uint4 *V;  // this walk's list column in the global scratch (16-bit entries)
+    int sz0, sz1, sz2;
+
+    __device__ __forceinline__ uint4 vec(int c, int v) const { return V[(size_t)(c * kListVecs + v) << 5]; }
+    __device__ __forceinline__ uint16_t *entry(int c, int q) const {
+        return reinterpret_cast<uint16_t *>(V + ((size_t)(c * kListVecs + (q >> 3)) << 5)) + (q & 7);
+    }
+    __device__ __forceinline__ uint32_t Lq(int c, int q) const { return *entry(c, q); }
+    __device__ __forceinline__ void setLq(int c, int q, uint32_t v) { *entry(c, q) = (uint16_t)v; }
+    __device__ __forceinline__ int sz(int c) const { return c == 0 ? sz0 : (c == 1 ? sz1 : sz2); }
+    __device__ __forceinline__ void setSz(int c, int v) { if (c == 0) sz0 = v; else if (c == 1) sz1 = v; else sz2 = v; }
+
+    // FlipSet::add (flip_set.cu:7-13): appended, silently dropped past the capacity.
+    __device__ __forceinline__ void listAdd(int c, int a, int b) {
+        const int s = sz(c);
+        if (s >= kListCap) return;
+        setLq(c, s, pack16(a, b));
+        setSz(c, s + 1);
+    }
+
+    // FlipSet::remove(index) (flip_set.cu:27-31): every pair touching idx is
+    // replaced by the last pair, which is then tested at the same position.  The
+    // scan reads two vectors (16 entries) per step and skips them whole when no
+    // live entry from position q on matches.
+    __device__ void listRemoveIndex(int c, uint32_t idx) {
+        int s = sz(c), q = 0;
+        while (q < s) {
+            const int v = q >> 3;
+            const uint4 a = vec(c, v);
+            const bool two = (v + 1) * 8 < s;
+            const uint4 b = two ? vec(c, v + 1) : make_uint4(0u, 0u, 0u, 0u);
+            unsigned hit = vec_touch_mask(a, idx) | (two ? vec_touch_mask(b, idx) << 8 : 0u);
+            hit &= ~0u << (q & 7);                                          // from position q on
+            const int live = s - v * 8;                                      // entries below s
+            if (live < 16) hit &= (1u << live) - 1u;
+            if (!hit) { q = (v + 2) * 8; continue; }
+            q = v * 8 + __ffs(hit) - 1;
+            s--;
+            setLq(c, q, Lq(c, s));  // position q is tested again
+        }
+        setSz(c, s);
+    }
+};
+
 template <class W, class R>
-struct SimtListZ2 {
-    W *x;         // this walk's factor column in shared memory
-    uint32_t *L;  // this walk's list column in the global scratch
-    int ld;       // slots per component in shared memory
-    int cap;      // slots a rank may reach (addTriplet beyond it overflows)
+struct SimtListZ2 : SimtLists {
+    W *x;      // this walk's factor column in shared memory
+    int ld;    // slots per component in shared memory (<= 256)
+    int cap;   // slots a rank may reach (addTriplet beyond it overflows)
     int n0, n1, n2, nn0, nn1, nn2, full;
     int m;
-    int sz0, sz1, sz2;
     int status;
     R &r;
 
@@ -37,40 +98,8 @@ struct SimtListZ2 {
 
     __device__ __forceinline__ W X(int c, int t) const { return x[(size_t)(c * ld + t) << 5]; }
     __device__ __forceinline__ void setX(int c, int t, W v) { x[(size_t)(c * ld + t) << 5] = v; }
-    __device__ __forceinline__ uint32_t Lq(int c, int q) const { return L[(size_t)(c * kListCap + q) << 5]; }
-    __device__ __forceinline__ void setLq(int c, int q, uint32_t v) { L[(size_t)(c * kListCap + q) << 5] = v; }
-    __device__ __forceinline__ int sz(int c) const { return c == 0 ? sz0 : (c == 1 ? sz1 : sz2); }
-    __device__ __forceinline__ void setSz(int c, int v) { if (c == 0) sz0 = v; else if (c == 1) sz1 = v; else sz2 = v; }
     __device__ __forceinline__ int nn(int c) const { return c == 0 ? nn0 : (c == 1 ? nn1 : nn2); }
     __device__ __forceinline__ bool nonzero(int t) const { return X(0, t) && X(1, t) && X(2, t); }
-
-    // FlipSet::add (flip_set.cu:7-13): appended, silently dropped past the capacity.
-    __device__ __forceinline__ void listAdd(int c, int a, int b) {
-        const int s = sz(c);
-        if (s >= kListCap) return;
-        setLq(c, s, ((uint32_t)a << 16) | (uint32_t)b);
-        setSz(c, s + 1);
-    }
-
-    // FlipSet::remove(index) (flip_set.cu:27-31): every pair touching idx is
-    // replaced by the last pair, which is then tested at the same position.  Four
-    // entries are loaded at a time; a group without a match is skipped whole.
-    __device__ void listRemoveIndex(int c, uint32_t idx) {
-        int s = sz(c), q = 0;
-        while (q + 4 <= s) {
-            const uint32_t v0 = Lq(c, q), v1 = Lq(c, q + 1), v2 = Lq(c, q + 2), v3 = Lq(c, q + 3);
-            const bool h0 = touches(v0, idx), h1 = touches(v1, idx), h2 = touches(v2, idx), h3 = touches(v3, idx);
-            if (!(h0 | h1 | h2 | h3)) { q += 4; continue; }
-            q += h0 ? 0 : (h1 ? 1 : (h2 ? 2 : 3));
-            s--;
-            setLq(c, q, Lq(c, s));  // position q is tested again
-        }
-        while (q < s) {
-            if (touches(Lq(c, q), idx)) { s--; setLq(c, q, Lq(c, s)); }
-            else q++;
-        }
-        setSz(c, s);
-    }
 
     // initFlips (scheme_z2.cu:141-150): all equal pairs, lexicographic, capped.
     __device__ void rebuild() {
@@ -80,7 +109,7 @@ struct SimtListZ2 {
                 const W v = X(c, a);
                 for (int b = a + 1; b < m; b++)
                     if (X(c, b) == v) {
-                        if (s < kListCap) setLq(c, s, ((uint32_t)a << 16) | (uint32_t)b);
+                        if (s < kListCap) setLq(c, s, pack16(a, b));
                         s++;
                     }
             }
@@ -162,7 +191,7 @@ struct SimtListZ2 {
         if (idx < sz0) { i = 0; j = 1; k = 2; pr = Lq(0, idx); }
         else if (idx < sz0 + sz1) { i = 1; j = 0; k = 2; pr = Lq(1, idx - sz0); }
         else { i = 2; j = 0; k = 1; pr = Lq(2, idx - sz0 - sz1); }
-        int a = (int)(pr >> 16), b = (int)(pr & 0xFFFFu);
+        int a = (int)(pr >> 8), b = (int)(pr & 0xFFu);
         if (r.coin()) { int tmp = j; j = k; k = tmp; }
         if (r.coin()) { int tmp = a; a = b; b = tmp; }
         flip(i, j, k, a, b, checkReduce);
@@ -254,13 +283,13 @@ struct SimtListZ2 {
     __device__ bool tryReduce() {
         for (int q = 0; q < sz0; q++) {
             const uint32_t pr = Lq(0, q);
-            const int a = (int)(pr >> 16), b = (int)(pr & 0xFFFFu);
+            const int a = (int)(pr >> 8), b = (int)(pr & 0xFFu);
             if (X(1, a) == X(1, b)) { reduce(2, a, b); return true; }
             if (X(2, a) == X(2, b)) { reduce(1, a, b); return true; }
         }
         for (int q = 0; q < sz1; q++) {
             const uint32_t pr = Lq(1, q);
-            const int a = (int)(pr >> 16), b = (int)(pr & 0xFFFFu);
+            const int a = (int)(pr >> 8), b = (int)(pr & 0xFFu);
             if (X(2, a) == X(2, b)) { reduce(0, a, b); return true; }
         }
         return false;

@@ -260,7 +260,7 @@ fg_status fg_set_fast_kernel(fg_handle *h, int kernel, int lanes);
  * runs randomWalkKernel's loop (flip_graph.cu:520-573).  FG_LIST_WARP = one warp
  * per walk (every option, including resizing, sandwiching, basis changes and the
  * Gauss reduction); FG_LIST_THREAD = one thread per walk with the FlipSet lists
- * in a device scratch of 6,000 bytes per walk, allocated on first use (only
+ * in a device scratch of 3,024 bytes per walk, allocated on first use (only
  * with resizing, sandwiching, basis changes and the Gauss reduction off);
  * -1 = automatic (thread per walk where it applies and the batch has enough
  * walks to fill the GPU).  Both give identical results.  FG_LIST_THREAD on a

@@ -51,18 +51,18 @@ def test_philox_device_matches_oracle():
 @pytest.mark.parametrize("path", walk_fixtures(), ids=lambda p: p.split("/")[-1].split(".")[0])
 def test_walk_matches_reference_kernel(path, list_kernel):
     """Same seed, same flags: the library reproduces the reference's per-launch state, with one
-    warp per walk and (Z2 without the resize, sandwiching and basis moves) one thread per walk."""
+    warp per walk and (without the resize, sandwiching and basis moves) one thread per walk."""
     d = golden_io.read_walk(path)
     ring = d["ring"]
     moves = d["resize_p"] > 0 or d["sandwich_p"] > 0 or d["basis_p"] > 0
-    if list_kernel == "thread" and (ring != "z2" or moves):
-        pytest.skip("the thread-per-walk list kernel covers Z2 without resize, sandwiching and basis moves")
+    if list_kernel == "thread" and moves:
+        pytest.skip("the thread-per-walk list kernel runs without resize, sandwiching and basis moves")
     n1, n2, n3 = d["n"]
     cap = 352 if d["resize_p"] > 0 else n1 * n2 * n3
     with fg.Engine(d["walks"], cap, ring, "reference", d["seed"], d["iterations"], d["plus_iterations"],
                    d["expand_p"], d["reduce_p"], resize_p=d["resize_p"], sandwich_p=d["sandwich_p"],
                    basis_p=d["basis_p"]) as eng:
-        if ring == "z2" and not moves:
+        if not moves:
             eng.set_list_kernel(list_kernel)
         eng.init_naive(n1, n2, n3)
         for L, block in enumerate(d["launches"]):
@@ -150,12 +150,16 @@ def xorwow_tape_for(rec, seed):
     ((4, 4, 4), 16, 150, 100, 0.01, 0.0),
     ((2, 4, 5), 16, 300, 100, 2.0, 0.0),   # nn = 8 x 20 x 10: sign-extended random splits
 ])
-def test_zt_walk_reference_stream_vs_oracle(shape, S, iters, plus, expand_p, reduce_p):
+@pytest.mark.parametrize("list_kernel", ["warp", "thread"])
+def test_zt_walk_reference_stream_vs_oracle(shape, S, iters, plus, expand_p, reduce_p, list_kernel):
     n1, n2, n3 = shape
+    if list_kernel == "thread" and max(n1 * n2, n2 * n3, n3 * n1) > 16:
+        pytest.skip("the thread-per-walk ternary kernel holds factors of at most 16 entries")
     cap = n1 * n2 * n3
     seed = 500 + n1 * 100 + n2 * 10 + n3
     kw = dict(iterations=iters, plus_iterations=plus, expand_p=expand_p, reduce_p=reduce_p)
     with fg.Engine(S, cap, "zt", "reference", seed, iters, plus, expand_p, reduce_p) as eng:
+        eng.set_list_kernel(list_kernel)
         eng.init_naive(n1, n2, n3)
         rec0 = eng.records()
         eng.run(2)
@@ -470,27 +474,29 @@ def test_fast_minimize_vs_oracle(shape, S):
         assert np.array_equal(a, o), f
 
 
-@pytest.mark.parametrize("mode", ["reference", "philox"])
-def test_list_kernels_agree_on_a_large_mixed_batch(mode):
-    """20,480 walks over six shapes: the automatic choice takes the thread-per-walk list kernel
-    (enough walks to fill the GPU); it equals the warp-per-walk kernel field for field."""
+@pytest.mark.parametrize("ring,mode", [("z2", "reference"), ("z2", "philox"), ("zt", "reference"), ("zt", "philox")])
+def test_list_kernels_agree_on_a_large_mixed_batch(ring, mode):
+    """20,480 walks over several shapes: the automatic choice takes the thread-per-walk list
+    kernel (enough walks to fill the GPU); it equals the warp-per-walk kernel field for field."""
     shapes = [(2, 2, 2), (2, 2, 3), (2, 3, 4), (3, 3, 4), (3, 4, 5), (4, 4, 4)]
+    if ring == "zt":  # ternary factors of at most 16 entries
+        shapes = [(2, 2, 2), (2, 2, 3), (2, 3, 4), (3, 3, 3), (2, 4, 4), (4, 4, 4)]
     S = 20480
     sh = np.array([shapes[w * len(shapes) // S] for w in range(S)], np.int32)
     out = {}
     for kernel in ("warp", "thread", "auto"):
-        with fg.Engine(S, 64, "z2", mode, 5, 600, 300, 2.0, 0.0) as eng:
+        with fg.Engine(S, 64, ring, mode, 5, 300 if ring == "zt" else 600, 300, 2.0, 0.0) as eng:
             eng.set_list_kernel(kernel)
             eng.init_naive_shapes(sh)
             eng.run(2)
             out[kernel] = eng.records()
             assert eng.validate().all() and eng.validate(best=True).all()
-    compare_records(out["thread"], out["warp"], f"{mode} thread vs warp")
-    compare_records(out["auto"], out["warp"], f"{mode} auto vs warp")
+    compare_records(out["thread"], out["warp"], f"{ring} {mode} thread vs warp")
+    compare_records(out["auto"], out["warp"], f"{ring} {mode} auto vs warp")
 
 
 def test_thread_list_kernel_is_refused_where_it_does_not_apply():
-    with fg.Engine(32, 27, "zt", "reference", 1, 10, 100) as eng:
+    with fg.Engine(32, 27, "zt", "reference", 1, 10, 100, sandwich_p=1.0) as eng:
         with pytest.raises(fg.FlipGraphError):
             eng.set_list_kernel("thread")
     with fg.Engine(32, 352, "z2", "reference", 1, 10, 100, resize_p=0.2) as eng:
