@@ -36,6 +36,8 @@ cudaError_t launch_walk_simt_list(int ring, const DevBatch &B, const WalkParams 
                                   int scap, int nnmax, int wpb, int sms, void *scratch, cudaStream_t s);
 size_t simt_list_smem_per_warp(int ring, int scap, int nnmax);
 size_t simt_list_scratch_bytes(int ring, int walks);
+// Fills the scratch's constant part (the remainder table the ZT draws use); once, after allocation.
+cudaError_t simt_list_init_scratch(int ring, int walks, void *scratch, cudaStream_t s);
 // Fast mode complexity minimizer (minimizeKernel), one thread per walk; bestC[w] is the
 // walk's best complexity so far, lowered in place.
 cudaError_t launch_minimize_simt(const DevBatch &B, const WalkParams &P, int first, int count, int scap, int wide,

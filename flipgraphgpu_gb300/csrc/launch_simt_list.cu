@@ -1,5 +1,7 @@
 // List-mode walk kernels, one thread per walk (Z2: walk_simt_list.cuh, ZT:
 // walk_simt_list_zt.cuh), and their launcher.
+#include <vector>
+
 #include "launch.h"
 #include "walk_simt_list.cuh"
 #include "walk_simt_list_zt.cuh"
@@ -37,7 +39,7 @@ template <class Z> struct ListRing;
 template <class W, class R> struct ListRing<SimtListZ2<W, R>> {
     static constexpr int kWords = 1;  // factor words per (component, slot)
     static constexpr int kScratchVecs = 3 * kListVecs;
-    static __device__ void bind(SimtListZ2<W, R> &z, unsigned char *col, uint4 *scr) {
+    static __device__ void bind(SimtListZ2<W, R> &z, unsigned char *col, uint4 *scr, const uint2 *) {
         z.x = reinterpret_cast<W *>(col);
         z.V = scr;
     }
@@ -56,11 +58,12 @@ template <class W, class R> struct ListRing<SimtListZ2<W, R>> {
 template <class R> struct ListRing<SimtListZT<R>> {
     static constexpr int kWords = 2;  // values and signs
     static constexpr int kScratchVecs = 3 * kListVecs + kPermVecs;
-    static __device__ void bind(SimtListZT<R> &z, unsigned char *col, uint4 *scr) {
+    static __device__ void bind(SimtListZT<R> &z, unsigned char *col, uint4 *scr, const uint2 *mg) {
         z.xv = reinterpret_cast<uint32_t *>(col);
         z.xs = z.xv + (size_t)3 * z.ld * 32;
         z.V = scr;
         z.J = scr + ((size_t)3 * kListVecs << 5);
+        z.mg = mg;
     }
     static __device__ void load(SimtListZT<R> &z, const DevBatch &B, int w, int m) {
         const size_t o = (size_t)w * 3 * B.cap;
@@ -93,12 +96,12 @@ template <class R> struct ListRing<SimtListZT<R>> {
 // are off for this kernel; their gates still take the reference's draws).
 template <class Z, class R>
 __device__ void simt_list_walk_one(const DevBatch &B, const WalkParams &P, int w, unsigned char *col, int ld,
-                                   uint4 *scr) {
+                                   uint4 *scr, const uint2 *mg) {
     const WalkHeader h = B.hdr[w];
     R r = ThreadDrawsIO<R>::load(B, P, w, h);
     Z z(r);
     z.ld = ld;
-    ListRing<Z>::bind(z, col, scr);
+    ListRing<Z>::bind(z, col, scr, mg);
     z.cap = ld < B.cap ? ld : B.cap;
     z.n0 = h.n[0]; z.n1 = h.n[1]; z.n2 = h.n[2];
     z.nn0 = z.n0 * z.n1; z.nn1 = z.n1 * z.n2; z.nn2 = z.n2 * z.n0;
@@ -170,7 +173,8 @@ __device__ void simt_list_walk_one(const DevBatch &B, const WalkParams &P, int w
 // of wb bytes per slot and component); walk w's scratch column of 16-byte vectors at
 // scratch + (w / 32) * kScratchVecs * 32 + w % 32.
 template <class Z, class R, int WB>
-__global__ void k_walk_simt_list(DevBatch B, WalkParams P, int first, int count, int ld, uint4 *scratch) {
+__global__ void k_walk_simt_list(DevBatch B, WalkParams P, int first, int count, int ld, uint4 *scratch,
+                                 const uint2 *mg) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, wpb = blockDim.x >> 5;
     unsigned char *col = smem + ((size_t)warp * ListRing<Z>::kWords * 3 * ld * 32 + lane) * WB;
@@ -179,14 +183,14 @@ __global__ void k_walk_simt_list(DevBatch B, WalkParams P, int first, int count,
         if (q < count) {
             const int w = first + q;
             uint4 *scr = scratch + (size_t)(w >> 5) * ListRing<Z>::kScratchVecs * 32 + (w & 31);
-            simt_list_walk_one<Z, R>(B, P, w, col, ld, scr);
+            simt_list_walk_one<Z, R>(B, P, w, col, ld, scr, mg);
         }
     }
 }
 
 template <class Z, class R, int WB>
 cudaError_t walk_simt_list_t(const DevBatch &B, const WalkParams &P, int first, int count, int ld, int wpb, int sms,
-                             uint4 *scratch, cudaStream_t s) {
+                             uint4 *scratch, const uint2 *mg, cudaStream_t s) {
     if (ld > 256) return cudaErrorInvalidValue;  // list entries hold slot indices in 8 bits
     auto smemFor = [&](int k) { return (size_t)k * ListRing<Z>::kWords * 3 * ld * 32 * WB; };
     int dev = 0, optin = 0;
@@ -204,7 +208,7 @@ cudaError_t walk_simt_list_t(const DevBatch &B, const WalkParams &P, int first, 
     if (blocks < 1) return cudaErrorInvalidConfiguration;
     const int need = (count + 32 * wpb - 1) / (32 * wpb);
     const int grid = need < blocks * sms ? need : blocks * sms;
-    k_walk_simt_list<Z, R, WB><<<grid, 32 * wpb, smem, s>>>(B, P, first, count, ld, scratch);
+    k_walk_simt_list<Z, R, WB><<<grid, 32 * wpb, smem, s>>>(B, P, first, count, ld, scratch, mg);
     return cudaGetLastError();
 }
 
@@ -219,26 +223,46 @@ size_t simt_list_smem_per_warp(int ring, int scap, int nnmax) {
     return ring == 1 ? (size_t)2 * 3 * scap * 32 * 4 : (size_t)3 * scap * 32 * simt_list_word_bytes(nnmax);
 }
 
-size_t simt_list_scratch_bytes(int ring, int walks) {
+// The lists (and for ZT the permutation draws) of every walk, then the remainder table.
+size_t simt_list_walk_bytes(int ring, int walks) {
     const int vecs = ring == 1 ? 3 * kListVecs + kPermVecs : 3 * kListVecs;
     return (size_t)((walks + 31) / 32) * 32 * vecs * sizeof(uint4);
+}
+
+size_t simt_list_scratch_bytes(int ring, int walks) {
+    return simt_list_walk_bytes(ring, walks) + (size_t)kRemTableSize * sizeof(uint2);
+}
+
+cudaError_t simt_list_init_scratch(int ring, int walks, void *scratch, cudaStream_t s) {
+    std::vector<uint2> t(kRemTableSize, make_uint2(0u, 1u));
+    for (uint32_t d = 2; d < (uint32_t)kRemTableSize; d++) {
+        uint32_t l = 0;
+        while ((1u << l) < d) l++;
+        t[d] = make_uint2((uint32_t)((((uint64_t)((1u << l) - d)) << 32) / d + 1), l);
+    }
+    unsigned char *dst = static_cast<unsigned char *>(scratch) + simt_list_walk_bytes(ring, walks);
+    cudaError_t e = cudaMemcpyAsync(dst, t.data(), t.size() * sizeof(uint2), cudaMemcpyHostToDevice, s);
+    if (e != cudaSuccess) return e;
+    return cudaStreamSynchronize(s);  // the host table goes out of scope
 }
 
 cudaError_t launch_walk_simt_list(int ring, const DevBatch &B, const WalkParams &P, int rng, int first, int count,
                                   int scap, int nnmax, int wpb, int sms, void *scratch, cudaStream_t s) {
     const int wb = simt_list_word_bytes(nnmax);
     uint4 *v = static_cast<uint4 *>(scratch);
+    const uint2 *mg = reinterpret_cast<const uint2 *>(static_cast<unsigned char *>(scratch) +
+                                                      simt_list_walk_bytes(ring, B.S));
     using U64 = unsigned long long;
     if (ring == 1) {
-        if (rng == RNG_XORWOW) return walk_simt_list_t<SimtListZT<ThreadXorwow>, ThreadXorwow, 4>(B, P, first, count, scap, wpb, sms, v, s);
-        return walk_simt_list_t<SimtListZT<ThreadPhilox>, ThreadPhilox, 4>(B, P, first, count, scap, wpb, sms, v, s);
+        if (rng == RNG_XORWOW) return walk_simt_list_t<SimtListZT<ThreadXorwow>, ThreadXorwow, 4>(B, P, first, count, scap, wpb, sms, v, mg, s);
+        return walk_simt_list_t<SimtListZT<ThreadPhilox>, ThreadPhilox, 4>(B, P, first, count, scap, wpb, sms, v, mg, s);
     }
     if (rng == RNG_XORWOW) {
-        if (wb == 8) return walk_simt_list_t<SimtListZ2<U64, ThreadXorwow>, ThreadXorwow, 8>(B, P, first, count, scap, wpb, sms, v, s);
-        return walk_simt_list_t<SimtListZ2<uint32_t, ThreadXorwow>, ThreadXorwow, 4>(B, P, first, count, scap, wpb, sms, v, s);
+        if (wb == 8) return walk_simt_list_t<SimtListZ2<U64, ThreadXorwow>, ThreadXorwow, 8>(B, P, first, count, scap, wpb, sms, v, mg, s);
+        return walk_simt_list_t<SimtListZ2<uint32_t, ThreadXorwow>, ThreadXorwow, 4>(B, P, first, count, scap, wpb, sms, v, mg, s);
     }
-    if (wb == 8) return walk_simt_list_t<SimtListZ2<U64, ThreadPhilox>, ThreadPhilox, 8>(B, P, first, count, scap, wpb, sms, v, s);
-    return walk_simt_list_t<SimtListZ2<uint32_t, ThreadPhilox>, ThreadPhilox, 4>(B, P, first, count, scap, wpb, sms, v, s);
+    if (wb == 8) return walk_simt_list_t<SimtListZ2<U64, ThreadPhilox>, ThreadPhilox, 8>(B, P, first, count, scap, wpb, sms, v, mg, s);
+    return walk_simt_list_t<SimtListZ2<uint32_t, ThreadPhilox>, ThreadPhilox, 4>(B, P, first, count, scap, wpb, sms, v, mg, s);
 }
 
 }  // namespace fg

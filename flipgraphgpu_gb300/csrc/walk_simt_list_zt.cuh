@@ -10,7 +10,7 @@
 // j_i = curand() % (i + 1), i = size-1 .. 1, are written eight to a 16-byte
 // vector into the walk's column of the global scratch; position p of the
 // permutation is then traced back through the swaps (pos = j_i when pos = i,
-// i when pos = j_i), four positions per pass over the draws.
+// i when pos = j_i), several positions per pass over the draws.
 //
 // Layout: values and signs of the factors in shared memory, 32 walks interleaved
 // by lane (word (c, t) at [(c * ld + t) * 32]); a factor that overflowed (the
@@ -19,6 +19,7 @@
 // 16 entries, so the reference's random splits (Addition::random, 16 bits per
 // draw) fit a 32-bit word below that mark.  Lists as in walk_simt_list.cuh.
 #pragma once
+#include <type_traits>
 #include "walk_simt_list.cuh"
 #include "walk_zt.cuh"
 
@@ -28,10 +29,23 @@ namespace fg {
 constexpr int kPermVecs = (3 * kListCap + 7) / 8;
 constexpr uint32_t kInvalidMark = 0x80000000u;
 
+// x % d for 2 <= d <= 3 * kListCap + 1 by multiplication with the divisor's magic number
+// (Granlund and Montgomery, "Division by invariant integers using multiplication", PLDI
+// 1994, unsigned N = 32): mg = (m, l) with l = ceil(log2 d), m = floor(2^32 (2^l - d) / d) + 1;
+// q = (t + ((x - t) >> 1)) >> (l - 1) with t = mulhi(m, x).  Exact for every 32-bit x.
+constexpr int kRemTableSize = 3 * kListCap + 2;
+
+__device__ __forceinline__ uint32_t rem_magic(uint32_t x, uint32_t d, uint2 mg) {
+    const uint32_t t = __umulhi(mg.x, x);
+    const uint32_t q = (t + ((x - t) >> 1)) >> (mg.y - 1);
+    return x - q * d;
+}
+
 template <class R>
 struct SimtListZT : SimtLists {
     uint32_t *xv, *xs;  // this walk's value and sign columns in shared memory
     uint4 *J;           // this walk's permutation-draw column in the global scratch
+    const uint2 *mg;    // remainder magic numbers, indexed by divisor
     int ld;             // slots per component in shared memory (<= 256)
     int cap;            // slots a rank may reach
     int n0, n1, n2, nn0, nn1, nn2, full;
@@ -208,7 +222,11 @@ struct SimtListZT : SimtLists {
     __device__ __forceinline__ void drawPermutation(int size) {
         uint64_t lo = 0, hi = 0;
         for (int i = size - 1; i >= 1; i--) {
-            const uint64_t x = r.below((uint32_t)(i + 1));
+            uint64_t x;
+            if constexpr (std::is_same<R, XorwowDraws>::value)  // curand() % (i + 1), exactly
+                x = rem_magic(r.raw(), (uint32_t)(i + 1), __ldg(mg + i + 1));
+            else
+                x = r.below((uint32_t)(i + 1));
             hi = (hi << 16) | (lo >> 48);
             lo = (lo << 16) | x;
             if ((i & 7) == 0 || i == 1) {
@@ -222,10 +240,11 @@ struct SimtListZT : SimtLists {
         }
     }
 
-    // Positions p .. p+3 of the permutation, traced back through the swaps.
-    __device__ __forceinline__ void tracePositions(int p, int size, int (&pos)[4]) const {
+    // Positions p .. p+N-1 of the permutation, traced back through the swaps.
+    template <int N>
+    __device__ __forceinline__ void tracePositions(int p, int size, int (&pos)[N]) const {
 #pragma unroll
-        for (int q = 0; q < 4; q++) pos[q] = p + q;
+        for (int q = 0; q < N; q++) pos[q] = p + q;
         for (int v = 0; v <= (size - 1) >> 3; v++) {
             const uint4 buf = J[(size_t)v << 5];
             const uint32_t wv[4] = {buf.x, buf.y, buf.z, buf.w};
@@ -235,43 +254,61 @@ struct SimtListZT : SimtLists {
                 if (i < 1 || i >= size) continue;
                 const int j = (int)((wv[u >> 1] >> (16 * (u & 1))) & 0xFFFFu);
 #pragma unroll
-                for (int q = 0; q < 4; q++) pos[q] = pos[q] == i ? j : (pos[q] == j ? i : pos[q]);
+                for (int q = 0; q < N; q++) pos[q] = pos[q] == i ? j : (pos[q] == j ? i : pos[q]);
             }
         }
     }
 
-    // tryFlip (scheme_integer.cu:907-975).
+    // Candidate `idx` of the listed pairs with its two orientation draws and the reference's
+    // bound tests; on success the flip's (j, k, a, b) in fj, fk, fa, fb and fi = i.
+    __device__ __forceinline__ bool tryCandidate(int idx, int &fi, int &fj, int &fk, int &fa, int &fb) {
+        int i, j, k;
+        uint32_t pr;
+        if (idx < sz0) { i = 0; j = 1; k = 2; pr = Lq(0, idx); }
+        else if (idx < sz0 + sz1) { i = 1; j = 0; k = 2; pr = Lq(1, idx - sz0); }
+        else { i = 2; j = 0; k = 1; pr = Lq(2, idx - sz0 - sz1); }
+        int a = (int)(pr >> 8), b = (int)(pr & 0xFFu);
+        if (r.coin()) { int tmp = j; j = k; k = tmp; }
+        if (r.coin()) { int tmp = a; a = b; b = tmp; }
+        const Tern ja = X(j, a), jb = X(j, b), ka = X(k, a), kb = X(k, b);
+        if (tlimitSum(ja, jb, j != 2) && tlimitSub(kb, ka, false)) {
+            const bool keep = k == 2 || tposSub(kb, ka);
+            fi = i; fj = j; fk = k; fa = keep ? a : b; fb = keep ? b : a;
+            return true;
+        }
+        if (tlimitSum(ka, kb, k != 2) && tlimitSub(jb, ja, false)) {
+            const bool keep = j == 2 || tposSub(jb, ja);
+            fi = i; fj = k; fk = j; fa = keep ? a : b; fb = keep ? b : a;
+            return true;
+        }
+        return false;
+    }
+
+    // tryFlip (scheme_integer.cu:907-975).  The candidates are searched first and the flip is
+    // applied once after the search, so the 32 walks of a warp apply their flips together
+    // whichever candidate each accepted.  Nearly every flip accepts its first candidate, so
+    // the first pass traces two positions, later passes eight.
     __device__ __forceinline__ bool tryFlip(bool checkReduce) {
         const int size = sz0 + sz1 + sz2;
         drawPermutation(size);
-        for (int p0 = 0; p0 < size; p0 += 4) {
-            int pos[4];
-            tracePositions(p0, size, pos);
-            const int lim = size - p0 < 4 ? size - p0 : 4;
-            for (int q = 0; q < lim; q++) {
-                const int idx = q == 0 ? pos[0] : (q == 1 ? pos[1] : (q == 2 ? pos[2] : pos[3]));
-                int i, j, k;
-                uint32_t pr;
-                if (idx < sz0) { i = 0; j = 1; k = 2; pr = Lq(0, idx); }
-                else if (idx < sz0 + sz1) { i = 1; j = 0; k = 2; pr = Lq(1, idx - sz0); }
-                else { i = 2; j = 0; k = 1; pr = Lq(2, idx - sz0 - sz1); }
-                int a = (int)(pr >> 8), b = (int)(pr & 0xFFu);
-                if (r.coin()) { int tmp = j; j = k; k = tmp; }
-                if (r.coin()) { int tmp = a; a = b; b = tmp; }
-                const Tern ja = X(j, a), jb = X(j, b), ka = X(k, a), kb = X(k, b);
-                if (tlimitSum(ja, jb, j != 2) && tlimitSub(kb, ka, false)) {
-                    if (k == 2 || tposSub(kb, ka)) flip(i, j, k, a, b, checkReduce);
-                    else flip(i, j, k, b, a, checkReduce);
-                    return true;
-                }
-                if (tlimitSum(ka, kb, k != 2) && tlimitSub(jb, ja, false)) {
-                    if (j == 2 || tposSub(jb, ja)) flip(i, k, j, a, b, checkReduce);
-                    else flip(i, k, j, b, a, checkReduce);
-                    return true;
-                }
-            }
+        int fi = -1, fj = 0, fk = 0, fa = 0, fb = 0;
+        {
+            int pos[2];
+            tracePositions<2>(0, size, pos);
+            if (size > 0 && tryCandidate(pos[0], fi, fj, fk, fa, fb)) {}
+            else if (size > 1 && tryCandidate(pos[1], fi, fj, fk, fa, fb)) {}
         }
-        return false;
+        for (int p0 = 2; fi < 0 && p0 < size; p0 += 8) {
+            int pos[8];
+            tracePositions<8>(p0, size, pos);
+            const int lim = size - p0 < 8 ? size - p0 : 8;
+#pragma unroll
+            for (int q = 0; q < 8; q++)
+                if (q < lim && fi < 0) tryCandidate(pos[q], fi, fj, fk, fa, fb);
+        }
+        if (fi < 0) return false;
+        flip(fi, fj, fk, fa, fb, checkReduce);
+        return true;
     }
 
     // plus (scheme_integer.cu:503-539).
