@@ -30,7 +30,8 @@ Keys beside the headline, all measured after the timed region:
             timed with CUDA events, accepted flips counted by a twin kernel
             checked state-for-state against it;
   bitexact  this engine's reference mode (bit-exact trajectories) on the same
-            workload;
+            workload; bitexact_by_shape the same for both rings at 16,384 walks
+            of 3x3x3 and 4x4x4 beside the reference's build;
   ttr       time to rank 23 on 3x3x3 (1,024 walks) for the fast, bit-exact and
             learned-proposal modes and the reference's CUDA build, 3 seeds;
   ttr_444   time to rank 47 on 4x4x4 (65,536 walks) within a 60 s budget.
@@ -491,6 +492,35 @@ def bitexact_leg(fg, args, walks, iterations):
             "launches": args.ref_cuda_launches, "iterations_per_launch": iterations, "walks": walks}
 
 
+def bitexact_by_shape(fg, args, walks=16384, iterations=200):
+    """This engine's bit-exact reference mode beside the reference's own CUDA build, both rings,
+    16,384 walks of one shape (3x3x3 and 4x4x4), 200 steps per launch, plus after 10^5."""
+    rows = []
+    for ring in ("zt", "z2"):
+        for n1, n2, n3 in ((3, 3, 3), (4, 4, 4)):
+            eng = fg.Engine(walks, n1 * n2 * n3, ring, "reference", args.seed, iterations, 100000, 0.01, 0.0, 0, 0)
+            eng.init_naive(n1, n2, n3)
+            eng.run(1)
+            v, ms = 0, 0.0
+            for _ in range(2):
+                st = eng.run(1)
+                v += st["verified_flips"]
+                ms += st["kernel_ms"] + st["verify_ms"]
+            eng.close()
+            ours = v / (ms / 1000)
+            ref = run_ref_harness(ring, ["time", walks, iterations, 2, args.seed, 100000, f"{n1}x{n2}x{n3}"],
+                                  timeout=600)
+            row = {"ring": ring.upper(), "shape": f"{n1}x{n2}x{n3}", "walks": walks, "iterations_per_launch": iterations,
+                   "ours": ours}
+            if "unavailable" in ref:
+                row["ref_cuda"] = ref
+            else:
+                row.update({"ref_cuda": ref["verified_flips_per_s"], "twin_mismatches": ref["twin_mismatches"],
+                            "ours_over_reference_cuda": ours / ref["verified_flips_per_s"]})
+            rows.append(row)
+    return {"unit": METRIC, "mode": "reference (bit-exact)", "rows": rows}
+
+
 def extras(fg, args, value):
     """Keys beside the headline, each outside the timed region: the reference's own CUDA build
     on the same workload (ref_cuda), this engine's bit-exact mode there (bitexact), time to rank
@@ -503,6 +533,7 @@ def extras(fg, args, value):
     if "value" in ref:
         be["over_reference_cuda"] = be["value"] / ref["value"]
     out["ref_cuda"], out["bitexact"] = ref, be
+    out["bitexact_by_shape"] = bitexact_by_shape(fg, args)
     log(f"ref_cuda and bitexact legs {time.perf_counter() - t:.1f} s")
     # time to rank 23 on 3x3x3 (1,024 walks, plus after 50,000, flip limit 10^7)
     t = time.perf_counter()

@@ -18,8 +18,9 @@
 //                         rejection, trySplitExisted, while (tryReduce())); a walk that exceeds it
 //                         stops and a warning is printed (0: the library default, 2^20)
 // Resize meta-operators (--resize-probability, default 0.2), sandwiching and
-// basis-change moves run on both rings in the reference and philox modes; in
-// the fast mode a positive probability is reported and treated as 0.
+// basis-change moves run on both rings in the reference and philox modes; the
+// fast mode resizes on the Z2 ring (grown factors of at most 56 entries) and
+// treats the other moves' probabilities as 0, with a note.
 #include <algorithm>
 #include <chrono>
 #include <cstdio>
@@ -51,8 +52,10 @@ struct Options {
     int targetRank;
 };
 
-// The meta-operators and basis moves run in the list modes only.
-bool resizeHere(const Options &o) { return o.mode != "fast"; }
+// Sandwiching, basis-change moves and the Gauss reduction run in the list modes; the resize
+// meta-operators also in the fast mode on the Z2 ring.
+bool movesHere(const Options &o) { return o.mode != "fast"; }
+bool resizeHere(const Options &o) { return o.mode != "fast" || o.ring == "Z2"; }
 
 class FlipGraph {
 public:
@@ -180,9 +183,9 @@ private:
         c.reduce_p = o_.reduce;
         c.device = 0;
         c.resize_p = resizeOn_ ? o_.resize : 0.0;
-        c.sandwich_p = resizeHere(o_) ? o_.sandwiching : 0.0;
-        c.basis_p = resizeHere(o_) ? o_.basis : 0.0;
-        c.gauss_p = resizeHere(o_) && !zt_ ? o_.gauss : 0.0;
+        c.sandwich_p = movesHere(o_) ? o_.sandwiching : 0.0;
+        c.basis_p = movesHere(o_) ? o_.basis : 0.0;
+        c.gauss_p = movesHere(o_) && !zt_ ? o_.gauss : 0.0;
         c.zt_sandwich = o_.ternarySandwiching ? 1 : 0;
         c.retry_cap = o_.retryCap;
         check(fg_create(&c, &h_), "fg_create");
@@ -479,10 +482,12 @@ int main(int argc, char *argv[]) {
     if (o.gauss > 0) std::cout << "  - gauss: " << o.gauss << std::endl;  // no reference counterpart
     std::cout << "- log period: " << o.logPeriod << std::endl;
     std::cout << "- seed: " << o.seed << std::endl;
-    if (!resizeHere(o) && (o.sandwiching > 0 || o.basis > 0 || o.resize > 0 || o.gauss > 0))
-        std::cout << "Note: resizing, sandwiching, basis-change moves and the Gauss reduction are not available in "
+    if (!movesHere(o) && (o.sandwiching > 0 || o.basis > 0 || o.gauss > 0))
+        std::cout << "Note: sandwiching, basis-change moves and the Gauss reduction are not available in "
                      "the fast mode; their probabilities are treated as 0"
                   << std::endl;
+    if (!resizeHere(o) && o.resize > 0)
+        std::cout << "Note: resizing is not available for the ZB ring; its probability is treated as 0" << std::endl;
     if (o.gauss > 0 && o.ring == "ZT")
         std::cout << "Note: the Gauss reduction is defined for the Z2 ring only; its probability is treated as 0"
                   << std::endl;

@@ -266,6 +266,8 @@ void compute_params(fg_handle *h) {
     P.key1 = (uint32_t)(c.seed >> 32);
     P.random_iterations = c.resize_p > 0 ? 1 : 0;
     P.retry_cap = c.retry_cap > 0 ? c.retry_cap : kRetryCap;
+    // the fast mode's words keep the partner count in their top byte: factors of at most 56 entries
+    P.max_matrix = c.mode == FG_MODE_FAST ? 56 : 64;
 }
 
 int verify_grid(fg_handle *h) { return (h->B.S + 3) / 4; }
@@ -572,8 +574,9 @@ fg_status fg_create(const fg_config *cfg, fg_handle **out) {
         return fail(FG_ERR_ARG, "unknown mode");
     if (cfg->cap <= 0 || slots_for_cap(cfg->cap) == 0 || cfg->cap > FG_MAX_RANK + 2)
         return fail(FG_ERR_CAPACITY, "cap must be in [1, 352]");
-    if (cfg->resize_p > 0 && cfg->mode != FG_MODE_REFERENCE && cfg->mode != FG_MODE_PHILOX_LISTS)
-        return fail(FG_ERR_ARG, "resizing runs in a list mode (reference or philox)");
+    if (cfg->resize_p > 0 && cfg->mode != FG_MODE_REFERENCE && cfg->mode != FG_MODE_PHILOX_LISTS &&
+        !(cfg->mode == FG_MODE_FAST && cfg->ring == FG_RING_Z2))
+        return fail(FG_ERR_ARG, "resizing runs in a list mode (reference or philox) or the Z2 fast mode");
     if ((cfg->sandwich_p > 0 || cfg->basis_p > 0) && cfg->mode != FG_MODE_REFERENCE && cfg->mode != FG_MODE_PHILOX_LISTS)
         return fail(FG_ERR_ARG, "sandwiching and basis-change moves run in a list mode (reference or philox)");
     if (cfg->gauss_p > 0 && (cfg->ring != FG_RING_Z2 || (cfg->mode != FG_MODE_REFERENCE && cfg->mode != FG_MODE_PHILOX_LISTS)))
@@ -1091,8 +1094,9 @@ fg_status fg_resize(fg_handle *h) {
     if (!h->ready) return fail(FG_ERR_STATE, "records not initialised");
     FG_CUDA(cudaSetDevice(h->dev));
     FG_CUDA(launch_resize(h->cfg.ring, h->B, h->P, h->cfg.mode == FG_MODE_REFERENCE ? RNG_XORWOW : RNG_PHILOX, h->cfg.resize_p,
-                          h->wpb, h->grid, h->stream));
+                          h->wpb, h->grid, uses_lists(h), h->stream));
     FG_CUDA(cudaStreamSynchronize(h->stream));
+    if (h->cfg.mode == FG_MODE_FAST) return refresh_plan(h);  // shape segments follow the new sizes
     return FG_OK;
 }
 
@@ -1153,9 +1157,10 @@ fg_status run_launches(fg_handle *h, int launches, fg_stats *stats, bool resizin
         if (ls) return ls;
         if (resizing) {
             FG_CUDA(launch_resize(h->cfg.ring, h->B, h->P, h->cfg.mode == FG_MODE_REFERENCE ? RNG_XORWOW : RNG_PHILOX,
-                                  h->cfg.resize_p, h->wpb, h->grid, h->stream));
+                                  h->cfg.resize_p, h->wpb, h->grid, uses_lists(h), h->stream));
             fg_status us = update_ranks(h);
             if (us) return us;
+            if (h->cfg.mode == FG_MODE_FAST && (us = refresh_plan(h))) return us;  // segments follow the sizes
         }
         FG_CUDA(cudaEventRecord(h->ev[1], h->stream));
         fg_status st = launch_verify(h, 0);

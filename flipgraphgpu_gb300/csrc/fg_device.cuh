@@ -66,6 +66,7 @@ struct WalkParams {
     uint32_t key0, key1;  // Philox key (seed)
     int random_iterations;  // resizing on: each launch runs randint(1, iterations) steps (flip_graph.cu:531)
     int retry_cap;          // bound on the reference's unbounded retry loops (> 0)
+    int max_matrix;         // resizing: most entries a grown factor may hold (64; 56 in the fast mode)
 };
 
 // The retry bound of a walk's parameters; kRetryCap where a caller runs without them

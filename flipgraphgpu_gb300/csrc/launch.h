@@ -46,8 +46,9 @@ cudaError_t launch_minimize_simt(const DevBatch &B, const WalkParams &P, int fir
 cudaError_t launch_minimize_group(const DevBatch &B, const WalkParams &P, int first, int count, int scap, int wide,
                                   int sms, int32_t *bestC, cudaStream_t s);
 // Resize meta-operators (one warp per walk, Z2, cap 352) and the best-rank table's copies.
+// keepLists = 0 (fast mode): the walks' list sizes are left at zero.
 cudaError_t launch_resize(int ring, const DevBatch &B, const WalkParams &P, int rng, double p, int wpb, int grid,
-                          cudaStream_t s);
+                          int keepLists, cudaStream_t s);
 cudaError_t launch_copy_best(const DevBatch &B, const int32_t *walks, int count, const int32_t *bestRank, cudaStream_t s);
 // Fast mode, `lanes` (4, 8, 16 or 32; 0 = by slot count) lanes per walk (same semantics as
 // launch_walk_simt); 32 lanes is the one-warp-per-walk kernel.

@@ -40,7 +40,9 @@ __device__ void group_walk_one(const DevBatch &B, const WalkParams &P, int w, W 
     uint64_t accepted = 0;
     bool copied = false;
     uint64_t *bdst = B.best_fac + (size_t)w * 3 * B.cap;
-    for (int it = 0; it < P.iterations; it++) {
+    // with resizing on, each launch runs randint(1, iterations) steps (flip_graph.cu:531)
+    const int iterations = P.random_iterations ? randint(1, P.iterations, r) : P.iterations;
+    for (int it = 0; it < iterations; it++) {
         const int rank = z.m;
         if (!z.tryFlip(true)) {
             if (z.status) break;
@@ -72,6 +74,8 @@ __device__ void group_walk_one(const DevBatch &B, const WalkParams &P, int w, W 
             for (int t = (bestM < 0 ? 0 : bestM) + g; t < B.cap; t += G) bdst[c * B.cap + t] = 0ull;
     __syncwarp(mask);
     if (g == 0) {
+        if (copied && B.best_n)  // resizing: the best scheme's sizes
+            for (int c = 0; c < 3; c++) B.best_n[w * 3 + c] = hw.n[c];
         hw.m = z.m;
         hw.flips = flipsCount;
         hw.best_rank = bestRank;

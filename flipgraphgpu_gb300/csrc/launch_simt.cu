@@ -47,7 +47,9 @@ __device__ void simt_walk_one(const DevBatch &B, const WalkParams &P, int w, W *
     int flipsCount = h.flips, bestRank = h.best_rank, bestM = h.best_m;
     uint64_t accepted = 0;
     bool copied = false;
-    for (int it = 0; it < P.iterations; it++) {
+    // with resizing on, each launch runs randint(1, iterations) steps (flip_graph.cu:531)
+    const int iterations = P.random_iterations ? randint(1, P.iterations, r) : P.iterations;
+    for (int it = 0; it < iterations; it++) {
         const int rank = z.m;
         if (!z.tryFlip(true)) {
             if (z.status) break;
@@ -75,6 +77,8 @@ __device__ void simt_walk_one(const DevBatch &B, const WalkParams &P, int w, W *
     for (int c = 0; c < 3; c++)
         for (int t = 0; t < B.cap; t++) dst[c * B.cap + t] = t < z.m ? (uint64_t)z.F(c, t) : 0ull;
     if (copied) simt_clear_best_tail(B, w, bestM);
+    if (copied && B.best_n)  // resizing: the best scheme's sizes
+        for (int c = 0; c < 3; c++) B.best_n[w * 3 + c] = h.n[c];
     WalkHeader o = h;
     o.m = z.m;
     o.flips = flipsCount;

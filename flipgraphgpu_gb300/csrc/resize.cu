@@ -18,7 +18,6 @@ namespace fg {
 
 namespace {
 
-constexpr int kMaxMatrix = 64;      // config.cuh:11 (64-bit factors)
 constexpr int kMaxExtensionN = 16;  // config.cuh:37
 constexpr int kMinProjectN = 2;     // config.cuh:34
 constexpr int kMaxRankRef = 350;    // config.cuh:10
@@ -262,10 +261,11 @@ __device__ void product_with(Z &z, const BestView &o, uint64_t *ownV, uint64_t *
     z.rebuild();
 }
 
-__device__ bool valid_grown(const int g[3], int rank, int maxN) {  // scheme_z2.cu:260-294
+// scheme_z2.cu:260-294; maxMatrix = the reference's 64 (config.cuh:11), 56 in the fast mode.
+__device__ bool valid_grown(const int g[3], int rank, int maxN, int maxMatrix) {
     if (rank > kMaxRankRef) return false;
     for (int q = 0; q < 3; q++)
-        if (g[q] * g[(q + 1) % 3] > kMaxMatrix || g[q] > maxN) return false;
+        if (g[q] * g[(q + 1) % 3] > maxMatrix || g[q] > maxN) return false;
     return true;
 }
 
@@ -289,7 +289,7 @@ __device__ bool try_extend(Z &z, R &r) {  // scheme_z2.cu:1187-1206, scheme_inte
     for (int i = 0; i < 3; i++) {
         int g[3] = {z.n0, z.n1, z.n2};
         g[i] += 1;
-        if (valid_grown(g, z.m + g[(i + 1) % 3] * g[(i + 2) % 3], kMaxExtensionN)) idx[size++] = i;
+        if (valid_grown(g, z.m + g[(i + 1) % 3] * g[(i + 2) % 3], kMaxExtensionN, r.P->max_matrix)) idx[size++] = i;
     }
     if (!size) return false;
     extend(z, idx[r.raw() % (uint32_t)size]);
@@ -303,7 +303,7 @@ __device__ bool try_product(Z &z, R &r) {  // scheme_z2.cu:1208-1223, scheme_int
     for (int i = 0; i < 3; i++) {
         int g[3] = {z.n0, z.n1, z.n2};
         g[i] *= 2;
-        if (valid_grown(g, z.m * 2, kMaxExtensionN)) idx[size++] = i;
+        if (valid_grown(g, z.m * 2, kMaxExtensionN, r.P->max_matrix)) idx[size++] = i;
     }
     if (!size) return false;
     product(z, idx[r.raw() % (uint32_t)size]);
@@ -316,30 +316,31 @@ __device__ bool try_merge(Z &z, const BestView &o, R &r) {  // scheme_z2.cu:1225
     const int n[3] = {z.n0, z.n1, z.n2};
     const bool eq0 = n[0] == o.n[0], eq1 = n[1] == o.n[1], eq2 = n[2] == o.n[2];
     const int s0 = n[0] + o.n[0], s1 = n[1] + o.n[1], s2 = n[2] + o.n[2];
+    const int mx = r.P->max_matrix;
     int p[3], size = 0;
-    if (s0 <= kMaxExtensionN && s0 * n[1] <= kMaxMatrix && s0 * n[2] <= kMaxMatrix && eq1 && eq2) p[size++] = 0;
-    if (eq0 && s1 <= kMaxExtensionN && n[0] * s1 <= kMaxMatrix && n[2] * s1 <= kMaxMatrix && eq2) p[size++] = 1;
-    if (eq0 && eq1 && s2 <= kMaxExtensionN && n[0] * s2 <= kMaxMatrix && n[1] * s2 <= kMaxMatrix) p[size++] = 2;
+    if (s0 <= kMaxExtensionN && s0 * n[1] <= mx && s0 * n[2] <= mx && eq1 && eq2) p[size++] = 0;
+    if (eq0 && s1 <= kMaxExtensionN && n[0] * s1 <= mx && n[2] * s1 <= mx && eq2) p[size++] = 1;
+    if (eq0 && eq1 && s2 <= kMaxExtensionN && n[0] * s2 <= mx && n[1] * s2 <= mx) p[size++] = 2;
     if (!size) return false;
     merge(z, o, p[r.raw() % (uint32_t)size]);
     return true;
 }
 
 template <class Z>
-__device__ bool try_product_with(Z &z, const BestView &o, uint64_t *ownV, uint64_t *ownS) {  // scheme_z2.cu:1256-1275
+__device__ bool try_product_with(Z &z, const BestView &o, uint64_t *ownV, uint64_t *ownS, int maxMatrix) {  // scheme_z2.cu:1256-1275
     if (z.m * o.m > kMaxRankRef) return false;
     const int n[3] = {z.n0, z.n1, z.n2};
     int g[3];
     for (int q = 0; q < 3; q++) g[q] = n[q] * o.n[q];
     for (int q = 0; q < 3; q++)
-        if (g[q] > kMaxExtensionN || g[q] * g[(q + 1) % 3] > kMaxMatrix) return false;
+        if (g[q] > kMaxExtensionN || g[q] * g[(q + 1) % 3] > maxMatrix) return false;
     product_with(z, o, ownV, ownS);
     return true;
 }
 
 // resizeKernel (flip_graph.cu:575-613) for walk w.
 template <class Walker, class R>
-__device__ void resize_one(const DevBatch &B, const WalkParams &P, int w, unsigned char *base, double p) {
+__device__ void resize_one(const DevBatch &B, const WalkParams &P, int w, unsigned char *base, double p, int keepLists) {
     const WalkHeader h = B.hdr[w];
     if (h.status) return;
     R r = DrawsIO<R>::load(B, P, w, h);
@@ -368,7 +369,7 @@ __device__ void resize_one(const DevBatch &B, const WalkParams &P, int w, unsign
         if (q < 0.05) try_project(z, r);
         else if (q < 0.55)
             try_product_with(z, best_view(B, (int)(r.raw() % (uint32_t)B.S)), B.fac + (size_t)w * 3 * B.cap,
-                             B.sgn ? B.sgn + (size_t)w * 3 * B.cap : nullptr);
+                             B.sgn ? B.sgn + (size_t)w * 3 * B.cap : nullptr, P.max_matrix);
         else if (q < 0.85) try_product(z, r);
         else try_extend(z, r);
     }
@@ -379,18 +380,21 @@ __device__ void resize_one(const DevBatch &B, const WalkParams &P, int w, unsign
         o.n[0] = z.n0; o.n[1] = z.n1; o.n[2] = z.n2;
         o.m = z.m;
         o.status = z.status;
-        o.list_size[0] = z.sz0; o.list_size[1] = z.sz1; o.list_size[2] = z.sz2;
+        // the fast mode keeps no lists: its walks count partners when they load
+        o.list_size[0] = keepLists ? z.sz0 : 0;
+        o.list_size[1] = keepLists ? z.sz1 : 0;
+        o.list_size[2] = keepLists ? z.sz2 : 0;
         o.draws = r.count;
         B.hdr[w] = o;
     }
 }
 
 template <class Walker, class R>
-__global__ void k_resize(DevBatch B, WalkParams P, double p) {
+__global__ void k_resize(DevBatch B, WalkParams P, double p, int keepLists) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int wpb = blockDim.x >> 5, warp = threadIdx.x >> 5;
     unsigned char *base = smem + RingIO<Walker>::smem(B.cap) * warp;
-    for (int w = blockIdx.x * wpb + warp; w < B.S; w += gridDim.x * wpb) resize_one<Walker, R>(B, P, w, base, p);
+    for (int w = blockIdx.x * wpb + warp; w < B.S; w += gridDim.x * wpb) resize_one<Walker, R>(B, P, w, base, p, keepLists);
 }
 
 // The per-size best-rank table's copies (FlipGraph::updateRanks, flip_graph.cu:257-261):
@@ -421,24 +425,24 @@ __global__ void k_copy_best(DevBatch B, const int32_t *walks, int count, const i
 }
 
 template <class Walker, class R>
-cudaError_t resize_t(const DevBatch &B, const WalkParams &P, double p, int wpb, int grid, cudaStream_t s) {
+cudaError_t resize_t(const DevBatch &B, const WalkParams &P, double p, int wpb, int grid, int keepLists, cudaStream_t s) {
     const size_t smem = RingIO<Walker>::smem(B.cap) * wpb;
     cudaError_t e = cudaFuncSetAttribute(k_resize<Walker, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e) return e;
-    k_resize<Walker, R><<<grid, 32 * wpb, smem, s>>>(B, P, p);
+    k_resize<Walker, R><<<grid, 32 * wpb, smem, s>>>(B, P, p, keepLists);
     return cudaGetLastError();
 }
 
 }  // namespace
 
 cudaError_t launch_resize(int ring, const DevBatch &B, const WalkParams &P, int rng, double p, int wpb, int grid,
-                          cudaStream_t s) {
+                          int keepLists, cudaStream_t s) {
     if (slots_for_cap(B.cap) != 11 || !B.best_n) return cudaErrorInvalidValue;
     if (ring == 0)
-        return rng == RNG_XORWOW ? resize_t<Z2Walk<XorwowDraws, 11>, XorwowDraws>(B, P, p, wpb, grid, s)
-                                 : resize_t<Z2Walk<PhiloxDraws, 11>, PhiloxDraws>(B, P, p, wpb, grid, s);
-    return rng == RNG_XORWOW ? resize_t<ZTWalk<XorwowDraws, 11>, XorwowDraws>(B, P, p, wpb, grid, s)
-                             : resize_t<ZTWalk<PhiloxDraws, 11>, PhiloxDraws>(B, P, p, wpb, grid, s);
+        return rng == RNG_XORWOW ? resize_t<Z2Walk<XorwowDraws, 11>, XorwowDraws>(B, P, p, wpb, grid, keepLists, s)
+                                 : resize_t<Z2Walk<PhiloxDraws, 11>, PhiloxDraws>(B, P, p, wpb, grid, keepLists, s);
+    return rng == RNG_XORWOW ? resize_t<ZTWalk<XorwowDraws, 11>, XorwowDraws>(B, P, p, wpb, grid, keepLists, s)
+                             : resize_t<ZTWalk<PhiloxDraws, 11>, PhiloxDraws>(B, P, p, wpb, grid, keepLists, s);
 }
 
 cudaError_t launch_copy_best(const DevBatch &B, const int32_t *walks, int count, const int32_t *bestRank, cudaStream_t s) {

@@ -69,9 +69,10 @@ typedef struct {
     int32_t device;           /* CUDA device ordinal */
     int32_t walks_per_block;  /* 0 = library default */
     double resize_p;          /* --resize-probability: > 0 turns on the resize meta-operators
-                                 (Z2, list modes, cap >= 350): each launch runs a random number
-                                 of steps, then resizes walks and updates the best rank per size
-                                 (flip_graph.cu:286-299,575-613,249-266) */
+                                 (list modes on both rings, the fast mode on Z2; cap >= 350): each
+                                 launch runs a random number of steps, then resizes walks and
+                                 updates the best rank per size (flip_graph.cu:286-299,575-613,
+                                 249-266); in the fast mode grown factors hold at most 56 entries */
     double sandwich_p;        /* --sandwiching-probability (list modes; per step: sandwich_p / iterations):
                                  conjugate every term by random invertible GF(2) matrices and rebuild
                                  the lists (scheme_z2.cu:1277-1300; a no-op that still takes its

@@ -157,6 +157,7 @@ struct Z2 {
     int32_t *status;
     int retryCap = kRetryCap;  // fgo_walk_cfg::retry_cap (0 there = kRetryCap)
     int slotCap = kMaxRank;    // the records' slots per walk (fgo_walk_cfg::cap)
+    int maxMatrix = kMaxMatrix;  // resizing: most entries of a grown factor (56 in the fast mode)
     // Implicit pair enumeration (the library's fast mode): no FlipSet lists;
     // a flip samples an ordered equal-factor pair uniformly in the canonical
     // order (component c, term t ascending, partner t' ascending).
@@ -643,7 +644,7 @@ struct Z2 {
     bool isValidGrown(const int g[3], int extraRank, int maxN) const {  // scheme_z2.cu:260-294
         if (extraRank > kMaxRank) return false;
         for (int q = 0; q < 3; q++)
-            if (g[q] * g[(q + 1) % 3] > kMaxMatrix || g[q] > maxN) return false;
+            if (g[q] * g[(q + 1) % 3] > maxMatrix || g[q] > maxN) return false;
         return true;
     }
     bool isValidExtension(int i, int maxN) const {
@@ -823,9 +824,9 @@ struct Z2 {
         const bool eq0 = n[0] == o.n[0], eq1 = n[1] == o.n[1], eq2 = n[2] == o.n[2];
         const int s0 = n[0] + o.n[0], s1 = n[1] + o.n[1], s2 = n[2] + o.n[2];
         int p[3], size = 0;
-        if (s0 <= kMaxExtensionN && s0 * n[1] <= kMaxMatrix && s0 * n[2] <= kMaxMatrix && eq1 && eq2) p[size++] = 0;
-        if (eq0 && s1 <= kMaxExtensionN && n[0] * s1 <= kMaxMatrix && n[2] * s1 <= kMaxMatrix && eq2) p[size++] = 1;
-        if (eq0 && eq1 && s2 <= kMaxExtensionN && n[0] * s2 <= kMaxMatrix && n[1] * s2 <= kMaxMatrix) p[size++] = 2;
+        if (s0 <= kMaxExtensionN && s0 * n[1] <= maxMatrix && s0 * n[2] <= maxMatrix && eq1 && eq2) p[size++] = 0;
+        if (eq0 && s1 <= kMaxExtensionN && n[0] * s1 <= maxMatrix && n[2] * s1 <= maxMatrix && eq2) p[size++] = 1;
+        if (eq0 && eq1 && s2 <= kMaxExtensionN && n[0] * s2 <= maxMatrix && n[1] * s2 <= maxMatrix) p[size++] = 2;
         if (!size) return false;
         merge(o, p[r.raw() % (uint32_t)size]);
         return true;
@@ -835,7 +836,7 @@ struct Z2 {
         int g[3];
         for (int q = 0; q < 3; q++) g[q] = n[q] * o.n[q];
         for (int q = 0; q < 3; q++)
-            if (g[q] > kMaxExtensionN || g[q] * g[(q + 1) % 3] > kMaxMatrix) return false;
+            if (g[q] > kMaxExtensionN || g[q] * g[(q + 1) % 3] > maxMatrix) return false;
         productWith(o);
         return true;
     }
@@ -1649,6 +1650,11 @@ inline void storeScheme(const ZT &s, fgo_batch *b, int w, int cap) { storeZT(s, 
 
 inline void setImplicit(Z2 &s, bool on) { s.implicit = on; }
 inline void setImplicit(ZT &, bool) {}
+// The fast mode's words keep the partner count in their top byte: grown factors of at most 56 entries.
+inline void setMaxMatrix(Z2 &s, int v) { s.maxMatrix = v; }
+inline void setMaxMatrix(ZT &, int) {}
+inline void rebuildIfList(Z2 &s) { s.rebuildLists(); }  // implicit: clears the lists
+inline void rebuildIfList(ZT &) {}
 
 template <class Scheme>
 void runWalks(const fgo_walk_cfg *cfg, int S, fgo_batch *b, const fgo_tape *tape) {
@@ -2415,6 +2421,9 @@ void runResize(const fgo_walk_cfg *cfg, int S, fgo_batch *b, std::vector<R> &rs)
         cur[w].status = best[w].status = &b->status[w];
         cur[w].retryCap = best[w].retryCap = retry_cap(cfg);
         cur[w].slotCap = best[w].slotCap = cap;
+        setImplicit(cur[w], cfg->rng == FGO_RNG_FAST);  // the fast mode: implicit pairs, no lists
+        setImplicit(best[w], cfg->rng == FGO_RNG_FAST);
+        setMaxMatrix(cur[w], cfg->rng == FGO_RNG_FAST ? 56 : kMaxMatrix);
     }
     std::map<std::string, int> table;
     table[sizeKey(cur[0].n)] = cur[0].n[0] * cur[0].n[1] * cur[0].n[2];
@@ -2425,8 +2434,15 @@ void runResize(const fgo_walk_cfg *cfg, int S, fgo_batch *b, std::vector<R> &rs)
             walkLaunch(cur[w], rs[w], cfg, b, w);
             loadBest(best[w], b, w, cap);
         }
-        for (int w = 0; w < S; w++)
-            if (!b->status[w]) resizeStep(cur[w], rs[w], best, S, cfg->resize_p);
+        for (int w = 0; w < S; w++) {
+            if (b->status[w]) continue;
+            // The fast mode's resize step keeps the reference's list order (each operator
+            // rebuilds the lists, and its reductions follow them); its walk then drops them.
+            const bool fast = cfg->rng == FGO_RNG_FAST;
+            if (fast) setImplicit(cur[w], false);
+            resizeStep(cur[w], rs[w], best, S, cfg->resize_p);
+            if (fast) { setImplicit(cur[w], true); rebuildIfList(cur[w]); }
+        }
         updateRanks(table, cur, best, b, S, cap);
     }
     for (int w = 0; w < S; w++) {
@@ -2526,7 +2542,7 @@ int fgo_walk(const fgo_walk_cfg *cfg, int S, fgo_batch *b, const fgo_tape *tape)
         return bad;
     }
     if (cfg->resize_p > 0) {
-        if (cfg->rng == FGO_RNG_FAST) return -1;
+        if (cfg->rng == FGO_RNG_FAST && cfg->ring != FGO_RING_Z2) return -1;
         if (cfg->ring == FGO_RING_Z2) runWalksResize<Z2>(cfg, S, b, tape);
         else runWalksResize<ZT>(cfg, S, b, tape);
         int bad = 0;

@@ -228,6 +228,36 @@ def test_walk_fast_mode_vs_oracle(shapes, iters, plus, expand_p, reduce_p, kerne
     compare_records(rec, b, f"{shapes}")
 
 
+@pytest.mark.parametrize("kernel", ["split", "warp", "group"])
+@pytest.mark.parametrize("shape,resize_p,launches", [((2, 3, 3), 0.5, 4), ((3, 3, 3), 0.2, 3), ((2, 2, 4), 1.0, 5)])
+def test_fast_mode_resize_vs_oracle(shape, resize_p, launches, kernel):
+    """The fast mode with the resize meta-operators (the reference's default --resize-probability
+    0.2): each launch runs a random number of fast steps, then the resize step (reference list order,
+    Philox stream) and the per-size best-rank table; field for field equal to the oracle's fast mode,
+    every scheme exact, grown factors of at most 56 entries."""
+    n1, n2, n3 = shape
+    S, cap, seed, iters, plus = 64, 352, 71 + n1 * n2 * n3, 400, 300
+    kw = dict(iterations=iters, plus_iterations=plus, expand_p=0.01, reduce_p=0.0, seed=seed, resize_p=resize_p)
+    with fg.Engine(S, cap, "z2", "fast", seed, iters, plus, 0.01, 0.0, resize_p=resize_p) as eng:
+        if kernel == "split":  # thread per walk up to 64 slots, a warp per walk for larger grown shapes
+            eng.set_fast_split(64)
+        else:
+            eng.set_fast_kernel(kernel, 16 if kernel == "group" else 0)
+        eng.init_naive(n1, n2, n3)
+        rec0 = eng.records()
+        eng.run(launches)
+        rec = eng.records()
+        assert eng.validate().all() and eng.validate(best=True).all()
+    b = batch_from(rec0)
+    b.best_n[:] = rec0.n
+    O.walk(b, b.cfg("fast", launches=launches, **kw))
+    compare_records(rec, b, f"fast resize {shape} {kernel}")
+    assert np.array_equal(rec.best_n, b.best_n)
+    assert len({tuple(x) for x in rec.n}) > 1  # the walks did resize
+    nn = np.maximum.reduce([rec.n[:, 0] * rec.n[:, 1], rec.n[:, 1] * rec.n[:, 2], rec.n[:, 2] * rec.n[:, 0]])
+    assert nn.max() <= 56
+
+
 @pytest.mark.parametrize("shape,S,iters,plus,expand_p,reduce_p,launches", [
     ((3, 3, 3), 96, 3000, 400, 0.01, 0.0, 2),
     ((2, 2, 3), 64, 2000, 100, 5.0, 0.0, 1),
