@@ -532,3 +532,33 @@ def test_thread_list_kernel_is_refused_where_it_does_not_apply():
     with fg.Engine(32, 352, "z2", "reference", 1, 10, 100, resize_p=0.2) as eng:
         with pytest.raises(fg.FlipGraphError):
             eng.set_list_kernel("thread")
+
+
+@pytest.mark.parametrize("kernel,lanes", [("thread", 0), ("group", 8), ("warp", 0)])
+@pytest.mark.parametrize("m", [5, 6, 7, 8])
+def test_fast_mode_flip_of_a_zero_factor_vs_oracle(kernel, lanes, m):
+    """A term with a zero factor (the reference's random split can leave one) flipped on its
+    equal partner: the flip's old factor is zero, which also matches the empty slots past the
+    rank.  Every fast kernel must leave those slots alone and follow the oracle."""
+    S, cap, seed = 64, 8, 321
+    terms = [(1, 1, 1), (1, 0, 2), (2, 4, 4), (4, 8, 8), (8, 2, 4), (3, 5, 6), (5, 6, 3), (6, 3, 5)][:m]
+    rec0 = fg.Records(S, cap, "z2")
+    rec0.n[:] = (2, 2, 2)
+    rec0.m[:] = m
+    rec0.fac[:] = 0
+    for t, uvw in enumerate(terms):
+        for c in range(3):
+            rec0.fac[:, c, t] = uvw[c]
+    rec0.best_fac[:] = rec0.fac
+    rec0.best_rank[:] = m
+    rec0.best_m[:] = m
+    kw = dict(iterations=60, plus_iterations=10**6, expand_p=0.0, reduce_p=0.0, seed=seed)
+    with fg.Engine(S, cap, "z2", "fast", seed, 60, 10**6, 0.0, 0.0) as eng:
+        eng.set_fast_kernel(kernel, lanes)
+        eng.set_records(rec0)
+        rec0 = eng.records()
+        eng.run(1)
+        rec = eng.records()
+    assert not rec.status.any()
+    b = run_oracle_like(rec0, kw, 1, "fast")
+    compare_records(rec, b, f"zero factor {kernel} m={m}")
