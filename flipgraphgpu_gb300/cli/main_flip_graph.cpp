@@ -18,9 +18,9 @@
 //                         rejection, trySplitExisted, while (tryReduce())); a walk that exceeds it
 //                         stops and a warning is printed (0: the library default, 2^20)
 // Resize meta-operators (--resize-probability, default 0.2), sandwiching and
-// basis-change moves run on both rings in the reference and philox modes; the
-// fast mode resizes on the Z2 ring (grown factors of at most 56 entries) and
-// treats the other moves' probabilities as 0, with a note.
+// basis-change moves run on both rings in the reference and philox modes and on
+// the Z2 ring in the fast mode (grown factors of at most 56 entries there); the
+// fast mode treats the Gauss reduction's probability as 0, with a note.
 #include <algorithm>
 #include <chrono>
 #include <cstdio>
@@ -52,9 +52,10 @@ struct Options {
     int targetRank;
 };
 
-// Sandwiching, basis-change moves and the Gauss reduction run in the list modes; the resize
-// meta-operators also in the fast mode on the Z2 ring.
-bool movesHere(const Options &o) { return o.mode != "fast"; }
+// Resizing, sandwiching and basis-change moves run in the list modes and in the fast mode on
+// the Z2 ring; the Gauss reduction in the list modes.
+bool movesHere(const Options &o) { return o.mode != "fast" || o.ring == "Z2"; }  // sandwiching, basis changes
+bool gaussHere(const Options &o) { return o.mode != "fast"; }
 bool resizeHere(const Options &o) { return o.mode != "fast" || o.ring == "Z2"; }
 
 class FlipGraph {
@@ -185,7 +186,7 @@ private:
         c.resize_p = resizeOn_ ? o_.resize : 0.0;
         c.sandwich_p = movesHere(o_) ? o_.sandwiching : 0.0;
         c.basis_p = movesHere(o_) ? o_.basis : 0.0;
-        c.gauss_p = movesHere(o_) && !zt_ ? o_.gauss : 0.0;
+        c.gauss_p = gaussHere(o_) && !zt_ ? o_.gauss : 0.0;
         c.zt_sandwich = o_.ternarySandwiching ? 1 : 0;
         c.retry_cap = o_.retryCap;
         check(fg_create(&c, &h_), "fg_create");
@@ -482,9 +483,12 @@ int main(int argc, char *argv[]) {
     if (o.gauss > 0) std::cout << "  - gauss: " << o.gauss << std::endl;  // no reference counterpart
     std::cout << "- log period: " << o.logPeriod << std::endl;
     std::cout << "- seed: " << o.seed << std::endl;
-    if (!movesHere(o) && (o.sandwiching > 0 || o.basis > 0 || o.gauss > 0))
-        std::cout << "Note: sandwiching, basis-change moves and the Gauss reduction are not available in "
-                     "the fast mode; their probabilities are treated as 0"
+    if (!movesHere(o) && (o.sandwiching > 0 || o.basis > 0))
+        std::cout << "Note: sandwiching and basis-change moves are not available for the ZB ring; their "
+                     "probabilities are treated as 0"
+                  << std::endl;
+    if (!gaussHere(o) && o.gauss > 0)
+        std::cout << "Note: the Gauss reduction is not available in the fast mode; its probability is treated as 0"
                   << std::endl;
     if (!resizeHere(o) && o.resize > 0)
         std::cout << "Note: resizing is not available for the ZB ring; its probability is treated as 0" << std::endl;

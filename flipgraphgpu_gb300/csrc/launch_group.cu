@@ -64,6 +64,8 @@ __device__ void group_walk_one(const DevBatch &B, const WalkParams &P, int w, W 
         if (r.gate_expand() && z.m <= bestM + 2) {
             if (z.tryExpand(randint(1, 2, r))) flipsCount = 0;
         }
+        if (r.gate_sandwich()) z.sandwich();  // flip_graph.cu:560-561
+        if (r.gate_basis()) z.swapBasis();    // flip_graph.cu:563-564
         if (flipsCount >= P.plus_iterations && z.tryPlus()) flipsCount = 0;
         if (z.status) break;
     }

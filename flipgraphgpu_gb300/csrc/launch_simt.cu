@@ -25,8 +25,10 @@ __device__ __forceinline__ void simt_clear_best_tail(const DevBatch &B, int w, i
         for (int t = bestM < 0 ? 0 : bestM; t < B.cap; t++) dst[c * B.cap + t] = 0ull;
 }
 
-// randomWalkKernel (flip_graph.cu:520-573) for one walk, one thread.
-template <class W>
+// randomWalkKernel (flip_graph.cu:520-573) for one walk, one thread.  MV: the sandwiching
+// and basis-change gates are compiled in (a run with both probabilities 0 takes the kernel
+// without them: their calls alone cost the walk loop a quarter of its speed).
+template <class W, bool MV>
 __device__ void simt_walk_one(const DevBatch &B, const WalkParams &P, int w, W *s, int scap) {
     const WalkHeader h = B.hdr[w];
     ThreadPhilox r;
@@ -69,6 +71,10 @@ __device__ void simt_walk_one(const DevBatch &B, const WalkParams &P, int w, W *
         if (r.gate_reduce()) z.tryReduce();
         if (r.gate_expand() && z.m <= bestM + 2) {
             if (z.tryExpand(randint(1, 2, r))) flipsCount = 0;
+        }
+        if constexpr (MV) {
+            if (r.gate_sandwich()) z.sandwich();  // flip_graph.cu:560-561
+            if (r.gate_basis()) z.swapBasis();    // flip_graph.cu:563-564
         }
         if (flipsCount >= P.plus_iterations && z.tryPlus()) flipsCount = 0;
         if (z.status) break;
@@ -159,14 +165,14 @@ __global__ void k_minimize_simt(DevBatch B, WalkParams P, int first, int count, 
 }
 
 // Walks [first, first + count) of the batch; scap = slots per walk in shared memory.
-template <class W>
+template <class W, bool MV>
 __global__ void k_walk_simt(DevBatch B, WalkParams P, int first, int count, int scap) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, wpb = blockDim.x >> 5;
     W *s = reinterpret_cast<W *>(smem) + (size_t)warp * 3 * simt_ld(scap) * 32 + lane;
     for (int base = (blockIdx.x * wpb + warp) * 32; base < count; base += gridDim.x * wpb * 32) {
         const int q = base + lane;
-        if (q < count) simt_walk_one<W>(B, P, first + q, s, scap);
+        if (q < count) simt_walk_one<W, MV>(B, P, first + q, s, scap);
     }
 }
 
@@ -193,7 +199,7 @@ cudaError_t minimize_simt_t(const DevBatch &B, const WalkParams &P, int first, i
     return cudaGetLastError();
 }
 
-template <class W>
+template <class W, bool MV>
 cudaError_t walk_simt_t(const DevBatch &B, const WalkParams &P, int first, int count, int scap, int wpb, int sms,
                         cudaStream_t s) {
     int dev = 0, optin = 0;
@@ -203,15 +209,15 @@ cudaError_t walk_simt_t(const DevBatch &B, const WalkParams &P, int first, int c
     if (perWarp > (size_t)optin) return cudaErrorInvalidConfiguration;  // rank too large for this mode
     while (wpb > 1 && simt_smem<W>(scap, wpb) > (size_t)optin) wpb--;
     size_t smem = simt_smem<W>(scap, wpb);
-    cudaError_t e = cudaFuncSetAttribute(k_walk_simt<W>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = cudaFuncSetAttribute(k_walk_simt<W, MV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     int blocks = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, k_walk_simt<W>, 32 * wpb, smem);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, k_walk_simt<W, MV>, 32 * wpb, smem);
     if (e != cudaSuccess) return e;
     if (blocks < 1) return cudaErrorInvalidConfiguration;
     int need = (count + 32 * wpb - 1) / (32 * wpb);
     int grid = need < blocks * sms ? need : blocks * sms;
-    k_walk_simt<W><<<grid, 32 * wpb, smem, s>>>(B, P, first, count, scap);
+    k_walk_simt<W, MV><<<grid, 32 * wpb, smem, s>>>(B, P, first, count, scap);
     return cudaGetLastError();
 }
 
@@ -219,8 +225,11 @@ cudaError_t walk_simt_t(const DevBatch &B, const WalkParams &P, int first, int c
 
 cudaError_t launch_walk_simt(const DevBatch &B, const WalkParams &P, int first, int count, int scap, int wide,
                              int wpb, int sms, cudaStream_t s) {
-    if (wide) return walk_simt_t<unsigned long long>(B, P, first, count, scap, wpb, sms, s);
-    return walk_simt_t<uint32_t>(B, P, first, count, scap, wpb, sms, s);
+    const bool moves = P.sandwich_T != kGateOff || P.basis_T != kGateOff;
+    if (wide) return moves ? walk_simt_t<unsigned long long, true>(B, P, first, count, scap, wpb, sms, s)
+                           : walk_simt_t<unsigned long long, false>(B, P, first, count, scap, wpb, sms, s);
+    return moves ? walk_simt_t<uint32_t, true>(B, P, first, count, scap, wpb, sms, s)
+                 : walk_simt_t<uint32_t, false>(B, P, first, count, scap, wpb, sms, s);
 }
 
 cudaError_t launch_minimize_simt(const DevBatch &B, const WalkParams &P, int first, int count, int scap, int wide,

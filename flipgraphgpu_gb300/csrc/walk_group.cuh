@@ -52,6 +52,8 @@ struct GroupDraws {
     __device__ __forceinline__ bool coin() { return raw() >> 31; }
     __device__ __forceinline__ bool gate_reduce() { return P->reduce_T != kGateOff && (uint64_t)raw() < P->reduce_T; }
     __device__ __forceinline__ bool gate_expand() { return P->expand_T != kGateOff && (uint64_t)raw() < P->expand_T; }
+    __device__ __forceinline__ bool gate_sandwich() { return P->sandwich_T != kGateOff && (uint64_t)raw() < P->sandwich_T; }
+    __device__ __forceinline__ bool gate_basis() { return P->basis_T != kGateOff && (uint64_t)raw() < P->basis_T; }
     __device__ __forceinline__ bool tie() { return raw() < 42949672u; }
 };
 
@@ -66,7 +68,7 @@ struct GroupFast {
     static constexpr int HS = Serial::HS;
     static constexpr W FM = Serial::FM;
     static constexpr W ONE = Serial::ONE;
-    enum { OP_ZEROFLIP, OP_REDUCE, OP_EXPAND, OP_PLUS, OP_TRYREDUCE };
+    enum { OP_ZEROFLIP, OP_REDUCE, OP_EXPAND, OP_PLUS, OP_TRYREDUCE, OP_SANDWICH, OP_BASIS };
 
     W *s;  // [3][cap] compact, this group's walk
     int cap;
@@ -102,7 +104,10 @@ struct GroupFast {
         x.n0 = n0; x.n1 = n1; x.n2 = n2; x.cap = cap;
         x.m = m; x.P0 = P0; x.P1 = P1; x.P2 = P2; x.status = status; x.result = 0;
         x.k0 = r.k0; x.k1 = r.k1; x.walk = r.walk; x.count = r.count; x.P = r.P;
-        if (g == 0) serial_op<W>(s, x, op, a0, a1, a2, a3);
+        if (g == 0) {
+            if (op >= OP_SANDWICH) serial_move<W>(s, x, op == OP_SANDWICH);
+            else serial_op<W>(s, x, op, a0, a1, a2, a3);
+        }
         __syncwarp(mask);
         m = __shfl_sync(mask, x.m, 0, G);
         P0 = __shfl_sync(mask, x.P0, 0, G);
@@ -249,6 +254,8 @@ struct GroupFast {
     __device__ bool tryExpand(int count) { return serial(OP_EXPAND, count) != 0; }
     __device__ bool tryPlus() { return serial(OP_PLUS) != 0; }
     __device__ bool tryReduce() { return serial(OP_TRYREDUCE) != 0; }
+    __device__ void sandwich() { serial(OP_SANDWICH); }
+    __device__ void swapBasis() { serial(OP_BASIS); }
 };
 
 }  // namespace fg

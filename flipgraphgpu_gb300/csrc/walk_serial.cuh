@@ -46,4 +46,21 @@ __device__ __noinline__ void serial_op(W *s, SerialCtx &x, int op, int a0, int a
     x.count = tp.count; x.result = res;
 }
 
+// Sandwiching (sandwich != 0) or a basis change of a compact walk, as serial_op; kept apart
+// so that the matrices of the sandwiching move do not enlarge serial_op's frame.
+template <class W>
+__device__ __noinline__ void serial_move(W *s, SerialCtx &x, int sandwich) {
+    ThreadPhilox tp;
+    tp.k0 = x.k0; tp.k1 = x.k1; tp.walk = x.walk; tp.count = x.count; tp.blk = -1; tp.P = x.P;
+    SimtZ2<W, 0> z(tp);
+    z.s = s; z.cap = x.cap; z.ld = x.cap;
+    z.n0 = x.n0; z.n1 = x.n1; z.n2 = x.n2;
+    z.nn0 = x.n0 * x.n1; z.nn1 = x.n1 * x.n2; z.nn2 = x.n2 * x.n0; z.full = x.n0 * x.n1 * x.n2;
+    z.m = x.m; z.P0 = x.P0; z.P1 = x.P1; z.P2 = x.P2; z.status = x.status;
+    if (sandwich) z.sandwich();
+    else z.swapBasis();
+    x.status = z.status;
+    x.count = tp.count;
+}
+
 }  // namespace fg

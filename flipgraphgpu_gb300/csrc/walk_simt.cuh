@@ -17,6 +17,7 @@
 // compaction orders follow the reference.
 #pragma once
 #include "fg_device.cuh"
+#include "gf2.cuh"
 
 namespace fg {
 
@@ -394,6 +395,58 @@ struct SimtZ2 {
             for (int b = a + 1; b < m; b++)
                 if (F(1, a) == F(1, b) && F(2, a) == F(2, b)) { reduce(0, a, b); return true; }
         return false;
+    }
+
+    // sandwiching (scheme_z2.cu:1277-1300): every term conjugated by random invertible
+    // matrices.  Conjugation is a bijection on each component, so equal factors stay equal
+    // and the partner counts in the top bytes stand.
+    __device__ __noinline__ void sandwich() {
+        if (n0 > 16 || n1 > 16 || n2 > 16) return;  // MAX_SANDWICHING_N, config.cuh:40
+        uint32_t u[16], u1[16], v[16], v1[16], w[16], w1[16];
+        if (!invertible_gf2(n0, u, u1, r, status) || !invertible_gf2(n1, v, v1, r, status) ||
+            !invertible_gf2(n2, w, w1, r, status))
+            return;
+        for (int t = 0; t < m; t++) {
+            W &x0 = A(0, t), &x1 = A(1, t), &x2 = A(2, t);
+            x0 = (x0 & ~FM) | (W)conj_gf2((uint64_t)(x0 & FM), u, v1, n0, n1);
+            x1 = (x1 & ~FM) | (W)conj_gf2((uint64_t)(x1 & FM), v, w1, n1, n2);
+            x2 = (x2 & ~FM) | (W)conj_gf2((uint64_t)(x2 & FM), w, u1, n2, n0);
+        }
+    }
+
+    // swapBasis (scheme_z2.cu:1302-1313, swapBasisRows / swapBasisColumns 864-914): two
+    // basis vectors trade places in U and W (rows) or V and W (columns).  A permutation of
+    // entries keeps equal factors equal, so the partner counts stand.
+    __device__ __noinline__ void swapBasis() {
+        const bool rows = r.raw() % 2;
+        const int nb = rows ? n0 : n2;
+        const int a = (int)(r.raw() % (uint32_t)nb), b = (int)(r.raw() % (uint32_t)nb);
+        if (a == b) return;
+        // entries (i, j) of an n x k matrix sit at bit i * k + j; swapping index a and b of
+        // the rows (or columns) swaps the bits of two rows (or two columns)
+        auto swapRows = [](uint64_t x, int k, int p, int q) {
+            const uint64_t mk = k >= 64 ? ~0ull : ((1ull << k) - 1);
+            const uint64_t rp = (x >> (p * k)) & mk, rq = (x >> (q * k)) & mk;
+            return (x & ~((mk << (p * k)) | (mk << (q * k)))) | (rp << (q * k)) | (rq << (p * k));
+        };
+        auto swapCols = [](uint64_t x, int n, int k, int p, int q) {
+            for (int i = 0; i < n; i++) {
+                const uint64_t bp = (x >> (i * k + p)) & 1ull, bq = (x >> (i * k + q)) & 1ull;
+                x ^= (bp ^ bq) * ((1ull << (i * k + p)) | (1ull << (i * k + q)));
+            }
+            return x;
+        };
+        for (int t = 0; t < m; t++) {
+            if (rows) {  // rows of U (n0 x n1) and columns of W (n2 x n0)
+                W &x0 = A(0, t), &x2 = A(2, t);
+                x0 = (x0 & ~FM) | (W)swapRows((uint64_t)(x0 & FM), n1, a, b);
+                x2 = (x2 & ~FM) | (W)swapCols((uint64_t)(x2 & FM), n2, n0, a, b);
+            } else {  // columns of V (n1 x n2) and rows of W (n2 x n0)
+                W &x1 = A(1, t), &x2 = A(2, t);
+                x1 = (x1 & ~FM) | (W)swapCols((uint64_t)(x1 & FM), n1, n2, a, b);
+                x2 = (x2 & ~FM) | (W)swapRows((uint64_t)(x2 & FM), n0, a, b);
+            }
+        }
     }
 
     __device__ int complexity() const {

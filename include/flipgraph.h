@@ -73,11 +73,11 @@ typedef struct {
                                  launch runs a random number of steps, then resizes walks and
                                  updates the best rank per size (flip_graph.cu:286-299,575-613,
                                  249-266); in the fast mode grown factors hold at most 56 entries */
-    double sandwich_p;        /* --sandwiching-probability (list modes; per step: sandwich_p / iterations):
-                                 conjugate every term by random invertible GF(2) matrices and rebuild
-                                 the lists (scheme_z2.cu:1277-1300; a no-op that still takes its
-                                 gate draw on ZT, scheme_integer.cu:1215-1217) */
-    double basis_p;           /* --basis-probability (list modes; per step: basis_p / iterations):
+    double sandwich_p;        /* --sandwiching-probability (list modes, Z2 fast mode; per step:
+                                 sandwich_p / iterations): conjugate every term by random invertible
+                                 GF(2) matrices and rebuild the lists (scheme_z2.cu:1277-1300; a no-op
+                                 that still takes its gate draw on ZT, scheme_integer.cu:1215-1217) */
+    double basis_p;           /* --basis-probability (list modes, Z2 fast mode; per step: basis_p / iterations):
                                  swap two basis vectors (scheme_z2.cu:1302-1313,
                                  scheme_integer.cu:1219-1233) */
     double gauss_p;           /* Z2, list modes: per step with probability gauss_p / iterations, the
@@ -176,7 +176,7 @@ fg_status fg_set_records(fg_handle *h, const fg_records *rec);
 fg_status fg_get_records(fg_handle *h, fg_records *rec);
 
 /* Runs `launches` launches of the walk (randomWalkKernel, flip_graph.cu:520-573,
- * with resize, sandwiching and basis probabilities 0) on every walk, then
+ * each move gated by its probability in the config) on every walk, then
  * verifies every walk's scheme exactly (flip_graph.cu:571-572).  Stats
  * cover this call. */
 fg_status fg_run(fg_handle *h, int launches, fg_stats *stats);

@@ -258,6 +258,62 @@ def test_fast_mode_resize_vs_oracle(shape, resize_p, launches, kernel):
     assert nn.max() <= 56
 
 
+@pytest.mark.parametrize("kernel,lanes", [("thread", 0), ("group", 4), ("group", 16), ("warp", 0)],
+                         ids=["thread", "group4", "group16", "warp"])
+@pytest.mark.parametrize("shape,S,iters,plus,sandwich_p,basis_p", [
+    ((3, 3, 3), 64, 600, 300, 24.0, 48.0),
+    ((2, 3, 4), 64, 600, 200, 60.0, 0.0),
+    ((4, 4, 4), 32, 400, 500, 0.0, 40.0),
+    ((2, 4, 8), 32, 300, 200, 15.0, 30.0),   # nn = 8 x 32 x 16: 64-bit words
+    ((2, 2, 17), 16, 200, 100, 20.0, 20.0),  # n > 16: sandwiching skipped (MAX_SANDWICHING_N), basis moves run
+])
+def test_fast_mode_sandwich_and_basis_vs_oracle(shape, S, iters, plus, sandwich_p, basis_p, kernel, lanes):
+    """Sandwiching and basis-change moves in the fast mode (flip_graph.cu:560-564): gated per step on
+    the walk's Philox stream after the expansion, on every fast kernel; field for field equal to the
+    oracle's fast mode, every scheme exact."""
+    n1, n2, n3 = shape
+    cap, seed = n1 * n2 * n3, 313 + n1 * n2 * n3
+    kw = dict(iterations=iters, plus_iterations=plus, expand_p=0.01, reduce_p=0.0, seed=seed,
+              sandwich_p=sandwich_p, basis_p=basis_p)
+    with fg.Engine(S, cap, "z2", "fast", seed, iters, plus, 0.01, 0.0, sandwich_p=sandwich_p,
+                   basis_p=basis_p) as eng:
+        eng.set_fast_kernel(kernel, lanes)
+        eng.init_naive(n1, n2, n3)
+        rec0 = eng.records()
+        st = eng.run(2)
+        rec = eng.records()
+        assert eng.validate().all() and eng.validate(best=True).all()
+    assert st["walks_valid"] == S and st["flips"] > 0
+    b = run_oracle_like(rec0, kw, 2, "fast")
+    compare_records(rec, b, f"fast moves {shape} {kernel}{lanes}")
+
+
+@pytest.mark.parametrize("kernel", ["split", "group"])
+def test_fast_mode_all_moves_with_resizing_vs_oracle(kernel):
+    """The fast mode with resizing, sandwiching and basis changes together: the moves run on the
+    resized shapes too; equal to the oracle's fast mode."""
+    S, cap, seed, iters, plus = 64, 352, 4242, 400, 300
+    kw = dict(iterations=iters, plus_iterations=plus, expand_p=0.01, reduce_p=0.0, seed=seed, resize_p=0.5,
+              sandwich_p=20.0, basis_p=20.0)
+    with fg.Engine(S, cap, "z2", "fast", seed, iters, plus, 0.01, 0.0, resize_p=0.5, sandwich_p=20.0,
+                   basis_p=20.0) as eng:
+        if kernel == "split":
+            eng.set_fast_split(64)
+        else:
+            eng.set_fast_kernel("group", 8)
+        eng.init_naive(2, 3, 3)
+        rec0 = eng.records()
+        eng.run(4)
+        rec = eng.records()
+        assert eng.validate().all() and eng.validate(best=True).all()
+    b = batch_from(rec0)
+    b.best_n[:] = rec0.n
+    O.walk(b, b.cfg("fast", launches=4, **kw))
+    compare_records(rec, b, f"fast resize + moves {kernel}")
+    assert np.array_equal(rec.best_n, b.best_n)
+    assert len({tuple(x) for x in rec.n}) > 1
+
+
 @pytest.mark.parametrize("shape,S,iters,plus,expand_p,reduce_p,launches", [
     ((3, 3, 3), 96, 3000, 400, 0.01, 0.0, 2),
     ((2, 2, 3), 64, 2000, 100, 5.0, 0.0, 1),

@@ -176,6 +176,27 @@ def test_fast_mode_walk_is_deterministic_and_valid():
     assert (b1.best_m < 27).any()
 
 
+@pytest.mark.parametrize("shape", [(3, 3, 3), (2, 4, 8), (2, 2, 17)])
+def test_fast_mode_moves_keep_schemes_exact(shape):
+    """Fast mode (implicit pairs) with sandwiching and basis changes at a high rate: deterministic,
+    every scheme exact, and the moves change the trajectory (their gate draws alone would not
+    change the factor multiset of a walk whose gates never fire)."""
+    n1, n2, n3 = shape
+    b1 = O.WalkBatch(8, n1 * n2 * n3, "z2")
+    O.init_naive(b1, n1, n2, n3)
+    b2, b0 = b1.copy(), b1.copy()
+    kw = dict(iterations=600, plus_iterations=200, launches=2, seed=11)
+    cfg = b1.cfg("fast", sandwich_p=60.0, basis_p=60.0, **kw)
+    O.walk(b1, cfg)
+    O.walk(b2, cfg)
+    O.walk(b0, b0.cfg("fast", **kw))
+    for f in ("m", "fac", "rng_pos", "best_m", "best_fac"):
+        assert np.array_equal(getattr(b1, f), getattr(b2, f))
+    assert O.validate(b1).all() and O.validate(b1, best=True).all()
+    assert (b1.rng_pos > b0.rng_pos).all()
+    assert not np.array_equal(b1.fac, b0.fac)
+
+
 def gauss_fixtures():
     return sorted(glob.glob(golden("gauss_z2_s*.bin.gz")))
 
