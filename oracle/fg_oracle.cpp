@@ -2556,6 +2556,91 @@ int fgo_walk(const fgo_walk_cfg *cfg, int S, fgo_batch *b, const fgo_tape *tape)
     return bad;
 }
 
+// ============================================================ proposal bound
+// How many steps a better flip proposal can save the fast-mode walk (no reference
+// counterpart; bounds what a learned proposal can gain).  greedy = 0: the uniform
+// proposal (tryFlipImplicit).  greedy = 1: an exact one-step lookahead: every ordered
+// equal pair and orientation is applied to a copy of the scheme (with the reduction
+// test), and when some of them lower the rank one of those is taken uniformly, else
+// the uniform proposal runs.  The rest of a step is the fast walk's (flip_graph.cu:
+// 533-569): expansion when no pair exists or by its gate while m <= best + 2, plus
+// after plus_iterations flips without a drop.  steps[w] = the steps walk w (Philox
+// stream w of seed) took from the naive scheme until its rank first reached target,
+// or -1 when it did not within max_steps.
+namespace {
+bool greedyFlip(Z2 &s, Z2 &tmp, std::vector<uint32_t> &cand, FastDraws &r) {
+    cand.clear();
+    for (int c = 0; c < 3; c++)
+        for (int a = 0; a < s.m; a++)
+            for (int b = 0; b < s.m; b++) {
+                if (a == b || s.x[c][a] != s.x[c][b]) continue;
+                for (int o = 0; o < 2; o++) {
+                    tmp.m = s.m;
+                    for (int q = 0; q < 3; q++) std::memcpy(tmp.x[q], s.x[q], sizeof(uint64_t) * s.m);
+                    int i = c, j = c == 0 ? 1 : 0, k = c == 2 ? 1 : 2;
+                    if (o) std::swap(j, k);
+                    tmp.flip(i, j, k, a, b, true);
+                    if (tmp.m < s.m) cand.push_back((uint32_t)(c << 24 | a << 14 | b << 4 | o));
+                }
+            }
+    if (cand.empty()) return false;
+    const uint32_t p = cand[r.below((uint32_t)cand.size())];
+    const int c = (int)(p >> 24), a = (int)((p >> 14) & 1023), b = (int)((p >> 4) & 1023);
+    int i = c, j = c == 0 ? 1 : 0, k = c == 2 ? 1 : 2;
+    if (p & 1) std::swap(j, k);
+    s.flip(i, j, k, a, b, true);
+    return true;
+}
+}  // namespace
+
+int fgo_lookahead_ttr(int n1, int n2, int n3, int walks, int target, int64_t max_steps, int plus_iterations,
+                      double expand_p, int iterations, uint64_t seed, int greedy, int64_t *steps) {
+    if (n1 < 1 || n2 < 1 || n3 < 1 || n1 * n2 * n3 > kMaxRank - 2 || n1 * n2 > 64 || n2 * n3 > 64 || n3 * n1 > 64)
+        return -1;
+    Z2 *s = new Z2, *tmp = new Z2;
+    std::vector<uint32_t> cand;
+    int32_t st = 0, tst = 0;
+    int failed = 0;
+    for (int w = 0; w < walks; w++) {
+        st = 0;
+        s->implicit = true;
+        s->status = &st;
+        s->initNaive(n1, n2, n3);
+        *tmp = *s;
+        tmp->status = &tst;
+        FastDraws r;
+        r.key[0] = (uint32_t)seed;
+        r.key[1] = (uint32_t)(seed >> 32);
+        r.walk = (uint32_t)w;
+        r.pos = 0;
+        r.status = &st;
+        steps[w] = -1;
+        int flipsCount = 0, best = s->m;
+        for (int64_t it = 0; it < max_steps; it++) {
+            const int rank = s->m;
+            const bool flipped = (greedy && greedyFlip(*s, *tmp, cand, r)) || s->tryFlip(r, true);
+            if (!flipped) {
+                s->tryExpand(randint(1, 2, r), r);
+                if (st) break;
+                continue;
+            }
+            if (s->m < rank) flipsCount = 0;
+            flipsCount++;
+            if (s->m <= target) { steps[w] = it + 1; break; }
+            if (s->m < best) best = s->m;
+            if (r.gate(expand_p, iterations) && s->m <= best + 2) {
+                if (s->tryExpand(randint(1, 2, r), r)) flipsCount = 0;
+            }
+            if (flipsCount >= plus_iterations && s->tryPlus(r)) flipsCount = 0;
+            if (st) break;
+        }
+        failed += steps[w] < 0;
+    }
+    delete s;
+    delete tmp;
+    return failed;
+}
+
 int fgo_reduce_gauss(const fgo_walk_cfg *cfg, int S, fgo_batch *b, const fgo_tape *tape, int32_t *found) {
     if (cfg->ring != FGO_RING_Z2) return -1;
     Z2 *s = new Z2;

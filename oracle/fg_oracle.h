@@ -154,6 +154,13 @@ fgo_reducer_state *fgo_reducer_state_make(const int32_t *fresh, const int32_t *v
  * evaluated fused (as nvcc contracts them by default) or unfused. */
 void fgo_set_fma(int fuse_float, int fuse_double);
 
+/* Steps from the naive scheme to rank `target` of fast-mode Z2 walks under the uniform
+ * proposal (greedy = 0) or an exact one-step lookahead that takes a rank-lowering flip
+ * whenever one exists (greedy = 1); steps[w] = -1 when walk w did not get there within
+ * max_steps.  Returns the number of such walks, -1 for an unsupported shape. */
+int fgo_lookahead_ttr(int n1, int n2, int n3, int walks, int target, int64_t max_steps, int plus_iterations,
+                      double expand_p, int iterations, uint64_t seed, int greedy, int64_t *steps);
+
 /* Philox4x32-10 block function (Salmon et al., SC'11) for known-answer tests. */
 void fgo_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
 

@@ -47,6 +47,7 @@ def lib():
         _lib.fgo_flip_schemes.restype = ctypes.c_int
         _lib.fgo_reduce_gauss.restype = ctypes.c_int
         _lib.fgo_validate_zb.restype = ctypes.c_int
+        _lib.fgo_lookahead_ttr.restype = ctypes.c_int
     return _lib
 
 
@@ -153,6 +154,21 @@ def walk(batch, cfg, tape=None):
     cb = batch._c()
     t, _keep = _tape_c(tape)
     return lib().fgo_walk(ctypes.byref(cfg), batch.S, ctypes.byref(cb), ctypes.byref(t) if t else None)
+
+
+def lookahead_ttr(shape, walks, target, max_steps, plus_iterations=50000, expand_p=0.01, iterations=1000,
+                  seed=1, greedy=False):
+    """Steps from the naive scheme to rank `target` per fast-mode Z2 walk under the uniform
+    proposal or (greedy) an exact one-step lookahead that takes a rank-lowering flip
+    whenever one exists; -1 for a walk that did not get there within max_steps."""
+    n1, n2, n3 = shape
+    steps = np.zeros(walks, np.int64)
+    rc = lib().fgo_lookahead_ttr(n1, n2, n3, walks, target, ctypes.c_int64(max_steps), plus_iterations,
+                                 ctypes.c_double(expand_p), iterations, ctypes.c_uint64(seed), int(greedy),
+                                 steps.ctypes.data_as(ctypes.c_void_p))
+    if rc < 0:
+        raise ValueError("unsupported shape")
+    return steps
 
 
 def reduce_gauss(batch, cfg, tape=None):
