@@ -369,10 +369,10 @@ def gpu_arm(args):
     shapes = shapes_for(walks)
     eng.init_naive_shapes(shapes)
     kernels = None
-    if args.mode == "fast" and not args.no_autotune:  # per-segment kernel choice, trajectories unchanged
+    if args.autotune > 0:  # per-segment kernel choice, trajectories unchanged
         names = {0: "thread", 1: "group", 2: "warp"}
         kernels = [f"{names.get(k, 'auto')}{l if k == 1 else ''}{f'/{w}w' if k == 0 else ''}"
-                   for k, l, w in eng.autotune(200)]
+                   for k, l, w in eng.autotune(args.autotune)]
     for _ in range(args.warmup):
         eng.run(1)
 
@@ -489,7 +489,8 @@ def bitexact_leg(fg, args, walks, iterations):
         ms += st["kernel_ms"] + st["verify_ms"]
     eng.close()
     return {"value": v / (ms / 1000.0), "unit": METRIC, "mode": "reference (bit-exact, XORWOW, FlipSet lists)",
-            "launches": args.ref_cuda_launches, "iterations_per_launch": iterations, "walks": walks}
+            "launches": args.ref_cuda_launches, "iterations_per_launch": iterations, "walks": walks,
+            "kernel": "thread per walk, static choice (6 warps per block: several Z2 segments)"}
 
 
 def bitexact_by_shape(fg, args, walks=16384, iterations=200):
@@ -874,7 +875,9 @@ def main():
     ap.add_argument("--ttr444-seconds", type=float, default=60.0)
     ap.add_argument("--ttr-learned-records", type=int, default=2_000_000)
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--no-autotune", action="store_true", help="keep the static kernel choice")
+    ap.add_argument("--autotune", type=int, default=0, metavar="STEPS",
+                    help="run fg_autotune with trials of STEPS steps before timing (0: the static kernel "
+                         "choice, measured as fast as any tuned one on this workload)")
     ap.add_argument("--fast-kernel", default=None, choices=["auto", "thread", "group", "warp"],
                     help="fast mode: one kernel for every shape instead of the automatic choice")
     ap.add_argument("--lanes", type=int, default=0, help="group kernel: lanes per walk (4, 8, 16; 0 = by slots)")

@@ -269,7 +269,8 @@ class Engine:
         _check(self.lib.fg_set_fast_kernel(self.h, kinds[kernel], int(lanes)))
 
     def autotune(self, iterations=200):
-        """Z2 fast mode: per shape segment, the fastest kernel over `iterations` steps (trajectories
+        """Z2 fast mode: per shape segment, the fastest kernel over `iterations` steps; list modes on
+        the thread-per-walk list kernel: per segment, the fastest warps per block (trajectories
         unchanged).  Returns [(kind, lanes, warps_per_block)] per segment, kind 0 thread, 1 group,
         2 warp per walk."""
         n = self.lib.fg_segment_count(self.h)

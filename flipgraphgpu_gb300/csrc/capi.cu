@@ -207,6 +207,7 @@ struct fg_handle {
     cudaEvent_t fork = nullptr, join[kSideStreams] = {};
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
     std::vector<Segment> segs;
+    std::vector<int> launchOrder;  // segments by ascending work (slots x walks), launched in this order
     LearnedBuffers learned;
     LearnedConfig lcfg;
     fg_mlp *mlp = nullptr;
@@ -328,6 +329,15 @@ void plan_segments(fg_handle *h, const std::vector<WalkHeader> &hdr) {
     }
     if ((int)segs.size() > kSideStreams) segs.assign(1, Segment{0, S, maxScap, anyWide, maxNN});
     h->segs = segs;
+    // Segments launch in ascending order of work, whatever the order of the shapes in the
+    // batch.  Measured on GB300 with the six-shape batch (65,536 walks, 2x2x2 .. 4x4x4):
+    // smallest first 3.35 G (bit-exact lists) and 5.3 G (fast) verified flips/s, largest
+    // first 2.76 G and 4.25 G.
+    h->launchOrder.resize(segs.size());
+    for (size_t i = 0; i < segs.size(); i++) h->launchOrder[i] = (int)i;
+    std::stable_sort(h->launchOrder.begin(), h->launchOrder.end(), [&](int a, int b) {
+        return (long long)segs[a].scap * segs[a].count < (long long)segs[b].scap * segs[b].count;
+    });
     drop_graph(h);
 }
 
@@ -401,7 +411,9 @@ fg_status update_ranks(fg_handle *h) {
 // choice, else fg_set_fast_split's split, else the measured crossover.
 void segment_kernel(const fg_handle *h, const Segment &g, int &kind, int &lanes, int &wpb) {
     lanes = 32;
-    wpb = h->cfg.walks_per_block > 0 ? h->cfg.walks_per_block : 2;
+    // static warps per block of the thread kernel: 4 (six-shape batch on GB300: 5.42 G flips/s
+    // against 5.28 G with 2 and 5.30 G with 8)
+    wpb = h->cfg.walks_per_block > 0 ? h->cfg.walks_per_block : 4;
     if (h->fastKernel >= 0) { kind = h->fastKernel; lanes = kind == FG_FAST_GROUP ? h->groupLanes : 32; return; }
     if (g.kind >= 0) {
         kind = g.kind;
@@ -429,7 +441,7 @@ cudaError_t launch_segments(fg_handle *h) {
         return launch_segment(h, h->segs[0], kind, lanes, wpb, h->stream);
     }
     if ((e = cudaEventRecord(h->fork, h->stream)) != cudaSuccess) return e;
-    for (size_t i = 0; i < h->segs.size(); i++) {
+    for (const int i : h->launchOrder) {
         const Segment &g = h->segs[i];
         int kind, lanes, wpb;
         segment_kernel(h, g, kind, lanes, wpb);
@@ -469,6 +481,18 @@ bool list_thread_chosen(const fg_handle *h) {
     return (double)h->B.S / 32.0 / (h->sms > 0 ? h->sms : 1) >= kListThreadWarpsPerSM[h->cfg.ring == FG_RING_ZT];
 }
 
+// Static warps per block of the thread-per-walk list kernel: walks_per_block when given
+// (at most 8), else 6 for Z2 batches of several shape segments and 4 otherwise.  Measured on
+// GB300 (reference stream, verified flips/s, 4 against 6): Z2 six shapes 2x2x2..4x4x4,
+// 65,536 walks 3.35 G against 3.65 G, 16,384 walks 1.09 G against 1.35 G; Z2 3x3x3, 3x3x4,
+// 4x4x4, 65,536 walks 2.53 G against 2.84 G; ZT six shapes of at most 16 entries, 65,536
+// walks 2.04 G against 1.92 G; ZT 3x3x3 + 2x4x4 1.62 G against 0.95 G; one shape (16,384
+// walks of 3x3x3 or 4x4x4, both rings) 4 best by 1-8 %.
+int list_wpb(const fg_handle *h) {
+    if (h->cfg.walks_per_block > 0) return std::min(h->cfg.walks_per_block, 8);
+    return h->cfg.ring == FG_RING_Z2 && h->segs.size() > 1 ? 6 : 4;
+}
+
 // One thread-per-walk list launch per segment, forked from and joined into h->stream.
 cudaError_t launch_list_segments(fg_handle *h) {
     cudaError_t e;
@@ -479,19 +503,19 @@ cudaError_t launch_list_segments(fg_handle *h) {
         if (e != cudaSuccess) return e;
     }
     const int rng = h->cfg.mode == FG_MODE_REFERENCE ? RNG_XORWOW : RNG_PHILOX;
-    // warps per block: 4 measured best on GB300 (six-shape batch 3.35 G flips/s against 3.25 G with 2)
-    const int wpb = h->cfg.walks_per_block > 0 ? std::min(h->cfg.walks_per_block, 8) : 4;
+    // warps per block: the autotuner's choice for the segment, else the static one
+    auto wpbOf = [&](const Segment &g) { return g.wpb > 0 ? g.wpb : list_wpb(h); };
     if (h->segs.size() == 1) {
         const Segment &g = h->segs[0];
-        return launch_walk_simt_list(h->cfg.ring, h->B, h->P, rng, g.first, g.count, g.scap, g.nnmax, wpb, h->sms,
-                                     h->d_listScratch, h->stream);
+        return launch_walk_simt_list(h->cfg.ring, h->B, h->P, rng, g.first, g.count, g.scap, g.nnmax, wpbOf(g),
+                                     h->sms, h->d_listScratch, h->stream);
     }
     if ((e = cudaEventRecord(h->fork, h->stream)) != cudaSuccess) return e;
-    for (size_t i = 0; i < h->segs.size(); i++) {
+    for (const int i : h->launchOrder) {
         const Segment &g = h->segs[i];
         if ((e = cudaStreamWaitEvent(h->side[i], h->fork, 0)) != cudaSuccess) return e;
-        if ((e = launch_walk_simt_list(h->cfg.ring, h->B, h->P, rng, g.first, g.count, g.scap, g.nnmax, wpb, h->sms,
-                                       h->d_listScratch, h->side[i])) != cudaSuccess)
+        if ((e = launch_walk_simt_list(h->cfg.ring, h->B, h->P, rng, g.first, g.count, g.scap, g.nnmax, wpbOf(g),
+                                       h->sms, h->d_listScratch, h->side[i])) != cudaSuccess)
             return e;
         if ((e = cudaEventRecord(h->join[i], h->side[i])) != cudaSuccess) return e;
         if ((e = cudaStreamWaitEvent(h->stream, h->join[i], 0)) != cudaSuccess) return e;
@@ -798,81 +822,143 @@ fg_status fg_set_fast_kernel(fg_handle *h, int kernel, int lanes) {
 fg_status fg_autotune(fg_handle *h, int iterations, int32_t *kinds, int32_t *lanes, int32_t *warps) {
     if (!h || iterations <= 0) return fail(FG_ERR_ARG, "bad argument");
     if (!h->ready) return fail(FG_ERR_STATE, "records not initialised");
-    if (h->cfg.mode != FG_MODE_FAST || h->cfg.ring != FG_RING_Z2)
-        return fail(FG_ERR_ARG, "the autotuner chooses among the Z2 fast-mode kernels");
+    const bool fast = h->cfg.mode == FG_MODE_FAST && h->cfg.ring == FG_RING_Z2;
+    const bool lists = !fast && uses_lists(h) && list_thread_chosen(h);
+    if (!fast && !lists)
+        return fail(FG_ERR_ARG, "the autotuner chooses among the Z2 fast-mode kernels and the warps per block "
+                                "of the thread-per-walk list kernel");
     FG_CUDA(cudaSetDevice(h->dev));
     FG_CUDA(cudaStreamSynchronize(h->stream));
     const size_t S = (size_t)h->B.S, nf = S * 3 * h->B.cap;
-    // Snapshot of everything a fast-mode launch changes; every trial starts from it and it
-    // is put back at the end, so tuning leaves trajectories and stream positions untouched.
-    WalkHeader *hdr0 = nullptr;
-    uint64_t *fac0 = nullptr, *best0 = nullptr;
-    auto release = [&]() { cudaFree(hdr0); cudaFree(fac0); cudaFree(best0); };
-    if (cudaMalloc(&hdr0, S * sizeof(WalkHeader)) != cudaSuccess || cudaMalloc(&fac0, nf * 8) != cudaSuccess ||
-        cudaMalloc(&best0, nf * 8) != cudaSuccess) {
-        release();
-        return fail(FG_ERR_CUDA, "autotune snapshot allocation failed");
+    // Snapshot of everything a launch changes (records, best schemes, lists, cuRAND states);
+    // every trial starts from it and it is put back at the end, so tuning leaves
+    // trajectories and stream positions untouched.
+    struct Region {
+        void *p;
+        size_t bytes;
+    };
+    std::vector<Region> regs = {{h->B.hdr, S * sizeof(WalkHeader)}, {h->B.fac, nf * 8}, {h->B.best_fac, nf * 8}};
+    if (lists) {
+        regs.push_back({h->B.lists, S * 3 * kListCap * sizeof(uint32_t)});
+        if (h->B.xorwow) regs.push_back({h->B.xorwow, S * sizeof(curandStateXORWOW_t)});
+        if (h->cfg.ring == FG_RING_ZT)
+            for (Region r : {Region{h->B.sgn, nf * 8}, Region{h->B.best_sgn, nf * 8}, Region{h->B.valid, nf},
+                             Region{h->B.best_valid, nf}})
+                regs.push_back(r);
     }
+    size_t total = 0;
+    for (const Region &r : regs) total += (r.bytes + 255) / 256 * 256;
+    unsigned char *snap = nullptr;
+    if (cudaMalloc(&snap, total) != cudaSuccess) return fail(FG_ERR_CUDA, "autotune snapshot allocation failed");
     auto restore = [&](bool save) -> cudaError_t {
-        cudaError_t e;
-        WalkHeader *hs = save ? h->B.hdr : hdr0, *hd = save ? hdr0 : h->B.hdr;
-        uint64_t *fs = save ? h->B.fac : fac0, *fd = save ? fac0 : h->B.fac;
-        uint64_t *bs = save ? h->B.best_fac : best0, *bd = save ? best0 : h->B.best_fac;
-        if ((e = cudaMemcpyAsync(hd, hs, S * sizeof(WalkHeader), cudaMemcpyDeviceToDevice, h->stream)) != cudaSuccess) return e;
-        if ((e = cudaMemcpyAsync(fd, fs, nf * 8, cudaMemcpyDeviceToDevice, h->stream)) != cudaSuccess) return e;
-        return cudaMemcpyAsync(bd, bs, nf * 8, cudaMemcpyDeviceToDevice, h->stream);
+        size_t off = 0;
+        for (const Region &r : regs) {
+            void *dst = save ? (void *)(snap + off) : r.p;
+            const void *src = save ? r.p : (const void *)(snap + off);
+            cudaError_t e = cudaMemcpyAsync(dst, src, r.bytes, cudaMemcpyDeviceToDevice, h->stream);
+            if (e != cudaSuccess) return e;
+            off += (r.bytes + 255) / 256 * 256;
+        }
+        return cudaSuccess;
     };
     cudaError_t e = restore(true);
     const int savedIterations = h->P.iterations;
     h->P.iterations = iterations;
     drop_graph(h);
-    // (kind, lanes, warps per block): thread per walk with 1, 2, 4 warps per block; 8, 16, 32 lanes per walk
-    const int cand[6][3] = {{FG_FAST_THREAD, 0, 1}, {FG_FAST_THREAD, 0, 2}, {FG_FAST_THREAD, 0, 4},
-                            {FG_FAST_GROUP, 8, 0},  {FG_FAST_GROUP, 16, 0}, {FG_FAST_WARP, 32, 0}};
-    // The segments run concurrently, so a choice is judged by the whole step: starting from
-    // the static choice, each segment in turn takes the candidate that minimises the time of
-    // all segments' launches with the others fixed (one sweep of coordinate descent).
-    auto trial = [&](float &ms) -> cudaError_t {
+    // Fast mode (kind, lanes, warps per block): thread per walk with 2, 4, 8 warps per block;
+    // 8, 16, 32 lanes per walk.  List modes: the thread-per-walk list kernel with 2, 4, 6, 8
+    // warps per block.  Warps per block change how the concurrently launched segments share
+    // the SMs.  Measured on GB300, six-shape batch, every segment alike: the bit-exact list
+    // kernel 3.35 G flips/s with 4, 3.65 G with 6; the fast kernel 5.42 G with 4, 4.36 G with 6.
+    const int fastCand[6][3] = {{FG_FAST_THREAD, 0, 2}, {FG_FAST_THREAD, 0, 4}, {FG_FAST_THREAD, 0, 8},
+                                {FG_FAST_GROUP, 8, 0},  {FG_FAST_GROUP, 16, 0}, {FG_FAST_WARP, 32, 0}};
+    const int listCand[4][3] = {{FG_FAST_THREAD, 0, 2}, {FG_FAST_THREAD, 0, 4}, {FG_FAST_THREAD, 0, 6},
+                                {FG_FAST_THREAD, 0, 8}};
+    const int (*cand)[3] = fast ? fastCand : listCand;
+    const int nCand = fast ? 6 : 4;
+    auto launchAll = [&]() { return fast ? launch_segments(h) : launch_list_segments(h); };
+    // The segments run concurrently, so a choice is judged by the whole step.  One timing: from
+    // the snapshot an untimed launch (kernel attributes), then from the snapshot a timed one.
+    auto timeOnce = [&](float &ms) -> cudaError_t {
         cudaError_t te;
         if ((te = restore(false)) != cudaSuccess) return te;
-        launch_segments(h);  // warm (kernel attributes); not timed
+        launchAll();
         if ((te = restore(false)) != cudaSuccess) return te;
         cudaEventRecord(h->ev[0], h->stream);
-        cudaError_t le = launch_segments(h);
+        cudaError_t le = launchAll();
         cudaEventRecord(h->ev[1], h->stream);
         if ((te = cudaStreamSynchronize(h->stream)) != cudaSuccess) return te;
-        if (le != cudaSuccess) {  // a candidate this segment cannot run (e.g. shared memory)
+        ms = 1e30f;
+        if (le != cudaSuccess) {  // a candidate a segment cannot run (e.g. shared memory)
             cudaGetLastError();
-            ms = 1e30f;
             return cudaSuccess;
         }
         cudaEventElapsedTime(&ms, h->ev[0], h->ev[1]);
         return cudaSuccess;
     };
-    for (Segment &g : h->segs) {  // explicit static choice as the starting point
-        int k, l, w;
-        g.kind = -1;
-        segment_kernel(h, g, k, l, w);
-        g.kind = k; g.lanes = l; g.wpb = k == FG_FAST_THREAD ? w : 0;
-    }
-    for (size_t i = 0; e == cudaSuccess && i < h->segs.size(); i++) {
-        Segment &g = h->segs[i];
-        const Segment keep = g;
-        float best = 1e30f;
-        Segment choice = keep;
-        for (const auto &c : cand) {
-            g.kind = c[0]; g.lanes = c[1]; g.wpb = c[2];
-            float ms = 0;
-            if ((e = trial(ms)) != cudaSuccess) break;
-            if (ms < best) { best = ms; choice = g; }
+    // A candidate replaces the configuration in place only when, timed in the order in place,
+    // candidate, candidate, in place (so that a drift of the clocks over the tuning cancels),
+    // its two steps take less than kMargin of the other two: launches of segments on side
+    // streams share the SMs in an order that varies from run to run, and the clocks fall as
+    // the tuning heats the GPU, so small differences do not carry over.
+    constexpr float kMargin = 0.97f;
+    auto better = [&](const std::vector<Segment> &inPlace, const std::vector<Segment> &candidate,
+                      bool &yes) -> cudaError_t {
+        float t[4];
+        const std::vector<Segment> *order[4] = {&inPlace, &candidate, &candidate, &inPlace};
+        for (int q = 0; q < 4; q++) {
+            h->segs = *order[q];
+            cudaError_t te = timeOnce(t[q]);
+            if (te != cudaSuccess) return te;
         }
-        g = best < 1e30f ? choice : keep;
+        h->segs = inPlace;
+        yes = t[1] + t[2] < kMargin * (t[0] + t[3]);
+        return cudaSuccess;
+    };
+    for (Segment &g : h->segs) {  // explicit static choice as the starting point
+        if (fast) {
+            int k, l, w;
+            g.kind = -1;
+            segment_kernel(h, g, k, l, w);
+            g.kind = k; g.lanes = l; g.wpb = k == FG_FAST_THREAD ? w : 0;
+        } else {
+            g.kind = FG_FAST_THREAD; g.lanes = 0; g.wpb = list_wpb(h);
+        }
+    }
+    // First one warps-per-block value for every thread-per-walk segment at once (the segments
+    // share the SMs, so a common value can beat every single-segment change).
+    for (int w : {2, 4, 6, 8}) {
+        if (e != cudaSuccess) break;
+        if (fast && w == 6) continue;
+        std::vector<Segment> cand = h->segs;
+        bool differs = false;
+        for (Segment &g : cand)
+            if (g.kind == FG_FAST_THREAD && g.wpb != w) { g.wpb = w; differs = true; }
+        if (!differs) continue;
+        const std::vector<Segment> inPlace = h->segs;
+        bool yes = false;
+        if ((e = better(inPlace, cand, yes)) != cudaSuccess) break;
+        h->segs = yes ? cand : inPlace;
+    }
+    // Then each segment in turn, the others fixed (one sweep of coordinate descent).
+    for (size_t i = 0; e == cudaSuccess && i < h->segs.size(); i++) {
+        for (int c = 0; c < nCand && e == cudaSuccess; c++) {
+            const Segment &g = h->segs[i];
+            if (cand[c][0] == g.kind && cand[c][2] == g.wpb && (g.kind == FG_FAST_THREAD || cand[c][1] == g.lanes))
+                continue;  // the configuration in place
+            const std::vector<Segment> inPlace = h->segs;
+            std::vector<Segment> next = inPlace;
+            next[i].kind = cand[c][0]; next[i].lanes = cand[c][1]; next[i].wpb = cand[c][2];
+            bool yes = false;
+            if ((e = better(inPlace, next, yes)) != cudaSuccess) break;
+            h->segs = yes ? next : inPlace;
+        }
     }
     h->P.iterations = savedIterations;
     cudaError_t re = restore(false);
     if (e == cudaSuccess) e = re;
     if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
-    release();
+    cudaFree(snap);
     drop_graph(h);
     if (e != cudaSuccess) return fail(FG_ERR_CUDA, cudaGetErrorString(e));
     for (size_t i = 0; i < h->segs.size(); i++) {

@@ -269,10 +269,14 @@ fg_status fg_set_fast_kernel(fg_handle *h, int kernel, int lanes);
 enum { FG_LIST_WARP = 0, FG_LIST_THREAD = 1 };
 fg_status fg_set_list_kernel(fg_handle *h, int kernel);
 
-/* Z2 fast mode: chooses each shape segment's kernel (thread per walk with 1, 2
- * or 4 warps per block; 8, 16 or 32 lanes per walk) by timing the step's
- * concurrent launches of all segments for `iterations` steps: from the static
- * choice, each segment in turn takes the candidate with the shortest step.
+/* Z2 fast mode: chooses each shape segment's kernel (thread per walk with 2, 4
+ * or 8 warps per block; 8, 16 or 32 lanes per walk); list modes on the
+ * thread-per-walk list kernel: each segment's warps per block (2, 4, 6 or 8,
+ * kinds 0, lanes 0).  Both by timing the step's concurrent launches of all
+ * segments for `iterations` steps: from the static choice, first one warps-per-
+ * block value for every thread-per-walk segment, then each segment in turn; a
+ * candidate replaces the configuration in place only when, timed in the order
+ * in place, candidate, candidate, in place, it is more than 3 % faster.
  * Each trial starts from a snapshot of the records, which is put back
  * afterwards, so tuning changes no trajectory and no stream position.  The
  * choice holds until the records are replaced (fg_set_records, fg_init_naive*)

@@ -526,13 +526,42 @@ def test_autotune_and_graph_replay_keep_trajectories():
             if tune:
                 choice = eng.autotune(100)
                 assert len(choice) == len(shapes)
-                assert all(k in (0, 1, 2) and (w in (1, 2, 4) if k == 0 else w == 0) for k, _, w in choice)
+                assert all(k in (0, 1, 2) and (w in (1, 2, 4, 6, 8) if k == 0 else w == 0) for k, _, w in choice)
             for _ in range(4):
                 eng.run(1)
             out.append(eng.records())
             assert eng.validate().all()
     for f in ("n", "m", "fac", "flips", "best_rank", "best_m", "best_fac", "rng_pos", "status"):
         assert np.array_equal(getattr(out[0], f), getattr(out[1], f)), f
+
+
+@pytest.mark.parametrize("ring", ["z2", "zt"])
+def test_list_autotune_keeps_bit_exact_trajectories(ring):
+    """In the reference mode fg_autotune picks each segment's warps per block for the thread-per-walk
+    list kernel on a snapshot of records, lists and cuRAND states that it puts back: the tuned run
+    equals the untuned one field for field, lists and stream positions included."""
+    shapes = [(2, 2, 2), (2, 3, 3), (3, 3, 3), (2, 4, 4)]
+    per = 1536
+    S = per * len(shapes)
+    sh = np.array([shapes[w // per] for w in range(S)], np.int32)
+    out = []
+    for tune in (False, True):
+        with fg.Engine(S, 32, ring, "reference", 17, 300, 2000, 0.5, 0.0) as eng:
+            eng.set_list_kernel("thread")
+            eng.init_naive_shapes(sh)
+            if tune:
+                choice = eng.autotune(50)
+                assert len(choice) == len(shapes)
+                assert all(k == 0 and l == 0 and w in (2, 4, 6, 8) for k, l, w in choice)
+            for _ in range(3):
+                eng.run(1)
+            out.append(eng.records())
+            assert eng.validate().all()
+    for f in ("n", "m", "fac", "sgn", "flips", "best_rank", "best_m", "best_fac", "rng_pos", "status",
+              "list_size", "list_pairs"):
+        a, o = getattr(out[0], f, None), getattr(out[1], f, None)
+        if a is not None:
+            assert np.array_equal(a, o), f
 
 
 @pytest.mark.parametrize("shape,S", [((3, 3, 3), 256), ((4, 4, 4), 256), ((2, 4, 8), 256), ((3, 3, 3), 10240)])
