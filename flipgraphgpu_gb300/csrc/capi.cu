@@ -228,6 +228,9 @@ struct fg_handle {
     int32_t *d_copyList = nullptr, *d_bestRanks = nullptr;
     uint8_t *d_valid = nullptr;
     bool ready = false;
+    // ZT: every live factor of the records valid, with bits 32-63 copying bit 31 (what the
+    // thread-per-walk list kernel's 32-bit words hold for factors of 17-31 entries)
+    bool ternaryWordsOk = true;
 };
 
 namespace {
@@ -475,7 +478,9 @@ bool list_thread_chosen(const fg_handle *h) {
     cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->dev);
     for (const Segment &g : h->segs) {
         if (g.scap > 256 || simt_list_smem_per_warp(h->cfg.ring, g.scap, g.nnmax) > (size_t)optin) return false;
-        if (h->cfg.ring == FG_RING_ZT && g.nnmax > 16) return false;  // ternary words hold 16 entries
+        // ternary words: 31 entries (a naive factor of 32 entries sets bit 31 without copying it
+        // upwards); above 16 the records must suit them (no overflow mark)
+        if (h->cfg.ring == FG_RING_ZT && (g.nnmax > 31 || (g.nnmax > 16 && !h->ternaryWordsOk))) return false;
     }
     if (h->listKernel == FG_LIST_THREAD) return true;
     return (double)h->B.S / 32.0 / (h->sms > 0 ? h->sms : 1) >= kListThreadWarpsPerSM[h->cfg.ring == FG_RING_ZT];
@@ -716,6 +721,7 @@ fg_status fg_init_naive(fg_handle *h, int n1, int n2, int n3) {
     fg_status st = refresh_plan(h);
     if (st) return st;
     h->ready = true;
+    h->ternaryWordsOk = true;
     h->tableReady = false;
     return FG_OK;
 }
@@ -744,6 +750,7 @@ fg_status fg_init_naive_shapes(fg_handle *h, const int32_t *shapes) {
     fg_status st = refresh_plan(h);
     if (st) return st;
     h->ready = true;
+    h->ternaryWordsOk = true;
     h->tableReady = false;
     return FG_OK;
 }
@@ -1100,6 +1107,15 @@ fg_status fg_set_records(fg_handle *h, const fg_records *rec) {
     FG_CUDA(cudaMemcpy(h->B.best_fac, rec->best_fac ? rec->best_fac : rec->fac, nf * sizeof(uint64_t),
                        cudaMemcpyHostToDevice));
     if (h->cfg.ring == FG_RING_ZT) {
+        h->ternaryWordsOk = true;
+        auto sext32 = [](uint64_t x) { return (uint64_t)(int64_t)(int32_t)(uint32_t)x; };
+        for (int w = 0; w < S && h->ternaryWordsOk; w++)
+            for (int c = 0; c < 3; c++)
+                for (int t = 0; t < rec->m[w]; t++) {
+                    const size_t q = ((size_t)w * 3 + c) * cap + t;
+                    if (!rec->valid[q] || sext32(rec->fac[q]) != rec->fac[q] || sext32(rec->sgn[q]) != rec->sgn[q])
+                        h->ternaryWordsOk = false;
+                }
         FG_CUDA(cudaMemcpy(h->B.sgn, rec->sgn, nf * 8, cudaMemcpyHostToDevice));
         FG_CUDA(cudaMemcpy(h->B.valid, rec->valid, nf, cudaMemcpyHostToDevice));
         FG_CUDA(cudaMemcpy(h->B.best_sgn, rec->best_sgn ? rec->best_sgn : rec->sgn, nf * 8, cudaMemcpyHostToDevice));

@@ -65,14 +65,24 @@ template <class R> struct ListRing<SimtListZT<R>> {
         z.J = scr + ((size_t)3 * kListVecs << 5);
         z.mg = mg;
     }
+    // 64-bit record words in, 32-bit words out: every factor's bits 32-63 must copy bit 31
+    // and, above 16 entries, every factor must be valid (the host routes other batches to
+    // the warp kernel; a word that breaks this stops the walk with ST_INTERNAL, its record
+    // untouched, rather than being cut).
     static __device__ void load(SimtListZT<R> &z, const DevBatch &B, int w, int m) {
         const size_t o = (size_t)w * 3 * B.cap;
+        const int nnmax = max(z.nn0, max(z.nn1, z.nn2));
+        z.mk = nnmax > 16 ? 0u : kInvalidMark;
         for (int c = 0; c < 3; c++)
             for (int t = 0; t < z.ld; t++) {
                 const bool in = t < m;
                 const size_t q = o + c * B.cap + t;
-                z.xv[z.at(c, t)] = in ? (uint32_t)B.fac[q] : 0u;
-                z.xs[z.at(c, t)] = in ? ((uint32_t)B.sgn[q] | (B.valid[q] ? 0u : kInvalidMark)) : 0u;
+                const uint64_t v = in ? B.fac[q] : 0ull, sg = in ? B.sgn[q] : 0ull;
+                const bool ok = !in || B.valid[q];
+                if ((uint64_t)(int64_t)(int32_t)v != v || (uint64_t)(int64_t)(int32_t)sg != sg || (!ok && !z.mk))
+                    z.status |= ST_INTERNAL;
+                z.xv[z.at(c, t)] = (uint32_t)v;
+                z.xs[z.at(c, t)] = (uint32_t)sg | (ok ? 0u : z.mk);
             }
     }
     static __device__ void store(const SimtListZT<R> &z, const DevBatch &B, int w, bool best) {
@@ -83,10 +93,10 @@ template <class R> struct ListRing<SimtListZT<R>> {
         for (int c = 0; c < 3; c++)
             for (int t = 0; t < B.cap; t++) {
                 const bool in = t < z.m;
-                const uint32_t sg = in ? z.xs[z.at(c, t)] : 0u;
-                dv[o + c * B.cap + t] = in ? (uint64_t)z.xv[z.at(c, t)] : 0ull;
-                ds[o + c * B.cap + t] = (uint64_t)(sg & ~kInvalidMark);
-                dk[o + c * B.cap + t] = in && !(sg & kInvalidMark) ? 1 : 0;
+                const uint32_t sg = in ? z.xs[z.at(c, t)] : 0u, v = in ? z.xv[z.at(c, t)] : 0u;
+                dv[o + c * B.cap + t] = (uint64_t)(int64_t)(int32_t)v;
+                ds[o + c * B.cap + t] = (uint64_t)(int64_t)(int32_t)(sg & ~z.mk);
+                dk[o + c * B.cap + t] = in && !(sg & z.mk) ? 1 : 0;
             }
     }
 };
@@ -110,6 +120,10 @@ __device__ void simt_list_walk_one(const DevBatch &B, const WalkParams &P, int w
     z.sz0 = h.list_size[0]; z.sz1 = h.list_size[1]; z.sz2 = h.list_size[2];
     z.status = h.status;
     ListRing<Z>::load(z, B, w, h.m);
+    if (z.status & ~h.status) {  // a record the ring's words cannot hold: the walk stops, its record untouched
+        B.hdr[w].status = z.status;
+        return;
+    }
     for (int c = 0; c < 3; c++) {
         const uint32_t *ls = B.lists + ((size_t)w * 3 + c) * kListCap;
         for (int q = 0; q < h.list_size[c]; q++) z.setLq(c, q, pack16((int)(ls[q] >> 16), (int)(ls[q] & 0xFFFFu)));

@@ -13,11 +13,18 @@
 // i when pos = j_i), several positions per pass over the draws.
 //
 // Layout: values and signs of the factors in shared memory, 32 walks interleaved
-// by lane (word (c, t) at [(c * ld + t) * 32]); a factor that overflowed (the
-// reference's Addition::valid false, only possible for input coefficients
-// outside {-1, 0, 1}) is marked by bit 31 of its sign word.  Factors of at most
-// 16 entries, so the reference's random splits (Addition::random, 16 bits per
-// draw) fit a 32-bit word below that mark.  Lists as in walk_simt_list.cuh.
+// by lane (word (c, t) at [(c * ld + t) * 32]), as 32-bit words: factors of at
+// most 31 entries.  The reference's random split (Addition::random, 16 bits per
+// chunk) shifts its second chunk as an int, so bits 32-63 of such a factor copy
+// bit 31, and the naive factors of at most 31 entries leave bits 31-63 clear; a
+// 32-bit word w stands for the 64-bit factor sext(w), and every operation of the
+// walk (xor, and, equality, lowest set bit) commutes with that extension.  (A
+// naive factor of 32 entries sets bit 31 alone: such shapes take the warp kernel.)  A factor that overflowed (the reference's Addition::valid false,
+// only possible for input coefficients outside {-1, 0, 1}; the walk's own moves
+// test their limits first) is marked by bit 31 of its sign word in walks whose
+// factors hold at most 16 entries (mk = that bit); walks with wider factors need
+// every input factor valid (the host checks) and use all 32 bits (mk = 0).
+// Lists as in walk_simt_list.cuh.
 #pragma once
 #include <type_traits>
 #include "walk_simt_list.cuh"
@@ -46,6 +53,7 @@ struct SimtListZT : SimtLists {
     uint32_t *xv, *xs;  // this walk's value and sign columns in shared memory
     uint4 *J;           // this walk's permutation-draw column in the global scratch
     const uint2 *mg;    // remainder magic numbers, indexed by divisor
+    uint32_t mk;        // the invalid mark of a sign word: kInvalidMark, or 0 for factors of > 16 entries
     int ld;             // slots per component in shared memory (<= 256)
     int cap;            // slots a rank may reach
     int n0, n1, n2, nn0, nn1, nn2, full;
@@ -58,14 +66,15 @@ struct SimtListZT : SimtLists {
     __device__ __forceinline__ size_t at(int c, int t) const { return (size_t)(c * ld + t) << 5; }
     __device__ __forceinline__ Tern X(int c, int t) const {
         const uint32_t s = xs[at(c, t)];
-        return Tern{(uint64_t)xv[at(c, t)], (uint64_t)(s & ~kInvalidMark), !(s & kInvalidMark)};
+        return Tern{(uint64_t)xv[at(c, t)], (uint64_t)(s & ~mk), !(s & mk)};
     }
     __device__ __forceinline__ void setX(int c, int t, const Tern &a) {
         xv[at(c, t)] = (uint32_t)a.v;
-        xs[at(c, t)] = (uint32_t)a.s | (a.ok ? 0u : kInvalidMark);
+        if (!a.ok && !mk) status |= ST_INTERNAL;  // no mark for factors of > 16 entries
+        xs[at(c, t)] = (uint32_t)a.s | (a.ok ? 0u : mk);
     }
     __device__ __forceinline__ bool sameX(int c, int t, const Tern &a) const {  // values and signs
-        return xv[at(c, t)] == (uint32_t)a.v && (xs[at(c, t)] & ~kInvalidMark) == (uint32_t)a.s;
+        return xv[at(c, t)] == (uint32_t)a.v && (xs[at(c, t)] & ~mk) == (uint32_t)a.s;
     }
     __device__ __forceinline__ int nn(int c) const { return c == 0 ? nn0 : (c == 1 ? nn1 : nn2); }
     __device__ __forceinline__ bool nonzero(int t) const { return xv[at(0, t)] && xv[at(1, t)] && xv[at(2, t)]; }
@@ -115,13 +124,13 @@ struct SimtListZT : SimtLists {
     __device__ __forceinline__ void fixSigns() {
         for (int t = 0; t < m; t++) {
             const uint32_t v0 = xv[at(0, t)], v1 = xv[at(1, t)];
-            const uint32_t s0 = xs[at(0, t)] & ~kInvalidMark, s1 = xs[at(1, t)] & ~kInvalidMark;
+            const uint32_t s0 = xs[at(0, t)] & ~mk, s1 = xs[at(1, t)] & ~mk;
             const bool pi = firstPositive(v0, s0), pj = firstPositive(v1, s1);
             if (pi && pj) continue;
             const int c0 = (!pi && !pj) ? 0 : (!pi ? 0 : 1);
             const int c1 = (!pi && !pj) ? 1 : 2;
-            xs[at(c0, t)] = (~xs[at(c0, t)] & xv[at(c0, t)]) | (xs[at(c0, t)] & kInvalidMark);
-            xs[at(c1, t)] = (~xs[at(c1, t)] & xv[at(c1, t)]) | (xs[at(c1, t)] & kInvalidMark);
+            xs[at(c0, t)] = (~xs[at(c0, t)] & xv[at(c0, t)] & ~mk) | (xs[at(c0, t)] & mk);
+            xs[at(c1, t)] = (~xs[at(c1, t)] & xv[at(c1, t)] & ~mk) | (xs[at(c1, t)] & mk);
         }
     }
 
@@ -365,10 +374,15 @@ struct SimtListZT : SimtLists {
         return true;
     }
 
-    // Addition::random (addition.cu:66-80) for factors of at most 16 entries: one chunk.
-    __device__ __forceinline__ Tern randomTern() {
-        const uint32_t sb = r.raw() & 0xFFFFu;
-        const uint32_t vb = r.raw() & 0xFFFFu;
+    // Addition::random (addition.cu:66-80): a sign chunk then a value chunk of 16 bits per 16
+    // entries; the second chunk lands in bits 16-31 (its sign extension is implicit).
+    __device__ __forceinline__ Tern randomTern(int n) {
+        uint32_t sb = r.raw() & 0xFFFFu;
+        uint32_t vb = r.raw() & 0xFFFFu;
+        if (n > 16) {
+            sb |= (r.raw() & 0xFFFFu) << 16;
+            vb |= (r.raw() & 0xFFFFu) << 16;
+        }
         return Tern{(uint64_t)vb, (uint64_t)(sb & vb), true};
     }
 
@@ -377,7 +391,7 @@ struct SimtListZT : SimtLists {
         const int t = (int)r.below((uint32_t)m);
         int i, j, k;
         perm3(i, j, k);
-        const Tern a = randomTern();
+        const Tern a = randomTern(nn(i));
         if (!tlimitSub(X(i, t), a, i != 2)) return false;
         split(i, j, k, t, a);
         return true;

@@ -262,7 +262,8 @@ fg_status fg_set_fast_kernel(fg_handle *h, int kernel, int lanes);
  * per walk (every option, including resizing, sandwiching, basis changes and the
  * Gauss reduction); FG_LIST_THREAD = one thread per walk with the FlipSet lists
  * in a device scratch of 3,024 bytes per walk, allocated on first use (only
- * with resizing, sandwiching, basis changes and the Gauss reduction off);
+ * with resizing, sandwiching, basis changes and the Gauss reduction off, and
+ * on ZT for factors of at most 31 entries, every input factor valid above 16);
  * -1 = automatic (thread per walk where it applies and the batch has enough
  * walks to fill the GPU).  Both give identical results.  FG_LIST_THREAD on a
  * configuration it does not cover returns FG_ERR_ARG. */

@@ -153,8 +153,8 @@ def xorwow_tape_for(rec, seed):
 @pytest.mark.parametrize("list_kernel", ["warp", "thread"])
 def test_zt_walk_reference_stream_vs_oracle(shape, S, iters, plus, expand_p, reduce_p, list_kernel):
     n1, n2, n3 = shape
-    if list_kernel == "thread" and max(n1 * n2, n2 * n3, n3 * n1) > 16:
-        pytest.skip("the thread-per-walk ternary kernel holds factors of at most 16 entries")
+    if list_kernel == "thread" and max(n1 * n2, n2 * n3, n3 * n1) > 31:
+        pytest.skip("the thread-per-walk ternary kernel holds factors of at most 31 entries")
     cap = n1 * n2 * n3
     seed = 500 + n1 * 100 + n2 * 10 + n3
     kw = dict(iterations=iters, plus_iterations=plus, expand_p=expand_p, reduce_p=reduce_p)
@@ -594,8 +594,6 @@ def test_list_kernels_agree_on_a_large_mixed_batch(ring, mode):
     """20,480 walks over several shapes: the automatic choice takes the thread-per-walk list
     kernel (enough walks to fill the GPU); it equals the warp-per-walk kernel field for field."""
     shapes = [(2, 2, 2), (2, 2, 3), (2, 3, 4), (3, 3, 4), (3, 4, 5), (4, 4, 4)]
-    if ring == "zt":  # ternary factors of at most 16 entries
-        shapes = [(2, 2, 2), (2, 2, 3), (2, 3, 4), (3, 3, 3), (2, 4, 4), (4, 4, 4)]
     S = 20480
     sh = np.array([shapes[w * len(shapes) // S] for w in range(S)], np.int32)
     out = {}
@@ -608,6 +606,68 @@ def test_list_kernels_agree_on_a_large_mixed_batch(ring, mode):
             assert eng.validate().all() and eng.validate(best=True).all()
     compare_records(out["thread"], out["warp"], f"{ring} {mode} thread vs warp")
     compare_records(out["auto"], out["warp"], f"{ring} {mode} auto vs warp")
+
+
+@pytest.mark.parametrize("shape", [(3, 4, 5), (4, 4, 5), (5, 5, 5), (2, 3, 10)])
+def test_zt_thread_list_kernel_on_wide_factors_vs_oracle(shape):
+    """Ternary factors of 17-31 entries in the thread-per-walk list kernel (32-bit words standing
+    for the reference's sign-extended 64-bit factors): random splits draw two chunks, the records
+    come back sign-extended; field for field equal to the oracle replaying the cuRAND stream."""
+    n1, n2, n3 = shape
+    S, iters, plus, expand_p = 64, 300, 60, 3.0
+    cap = n1 * n2 * n3 + 8
+    seed = 900 + n1 * 100 + n2 * 10 + n3
+    kw = dict(iterations=iters, plus_iterations=plus, expand_p=expand_p, reduce_p=0.0)
+    with fg.Engine(S, cap, "zt", "reference", seed, iters, plus, expand_p, 0.0) as eng:
+        eng.set_list_kernel("thread")
+        eng.init_naive(n1, n2, n3)
+        rec0 = eng.records()
+        eng.run(2)
+        rec = eng.records()
+        assert eng.validate().all() and eng.validate(best=True).all()
+    b = run_oracle_like(rec0, kw, 2, "tape", xorwow_tape_for(rec, seed))
+    compare_records(rec, b, f"zt wide {shape}")
+    hi = rec.fac >> np.uint64(31)  # bits 31-63: all zero or all one
+    assert np.isin(hi, [0, (1 << 33) - 1]).all()
+
+
+def test_zt_factors_of_32_entries_take_the_warp_kernel():
+    """A naive factor of 32 entries sets bit 31 without copying it into bits 32-63, which the
+    thread kernel's 32-bit words cannot stand for: the thread kernel is refused, the automatic
+    choice runs the warp kernel."""
+    with fg.Engine(64, 72, "zt", "reference", 5, 100, 60, 0.01, 0.0) as eng:
+        eng.set_list_kernel("thread")
+        eng.init_naive(2, 4, 8)
+        with pytest.raises(fg.FlipGraphError):
+            eng.run(1)
+    with fg.Engine(64, 72, "zt", "reference", 5, 100, 60, 0.01, 0.0) as eng:
+        eng.init_naive(2, 4, 8)
+        st = eng.run(1)
+        assert st["walks_valid"] == 64
+
+
+def test_zt_wide_records_with_an_invalid_factor_take_the_warp_kernel():
+    """An input factor marked invalid (valid = 0) has no place in the 32-bit words of factors of
+    > 16 entries: the thread kernel is refused for such records, the automatic choice takes the
+    warp kernel, and the walk still follows the oracle."""
+    S, n, seed, iters = 64, (3, 4, 5), 77, 200
+    with fg.Engine(S, 68, "zt", "reference", seed, iters, 60, 0.01, 0.0) as eng:
+        eng.init_naive(*n)
+        rec0 = eng.records()
+    rec0.valid[5, 0, 3] = 0
+    rec0.best_valid[5, 0, 3] = 0
+    with fg.Engine(S, 68, "zt", "reference", seed, iters, 60, 0.01, 0.0) as eng:
+        eng.set_records(rec0)
+        eng.set_list_kernel("thread")
+        with pytest.raises(fg.FlipGraphError):
+            eng.run(1)
+    with fg.Engine(S, 68, "zt", "reference", seed, iters, 60, 0.01, 0.0) as eng:
+        eng.set_records(rec0)
+        eng.run(1)
+        rec = eng.records()
+    b = run_oracle_like(rec0, dict(iterations=iters, plus_iterations=60, expand_p=0.01, reduce_p=0.0), 1, "tape",
+                        xorwow_tape_for(rec, seed))
+    compare_records(rec, b, "zt wide, one invalid factor")
 
 
 def test_thread_list_kernel_is_refused_where_it_does_not_apply():
