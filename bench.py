@@ -42,6 +42,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import threading
 import time
 
@@ -525,7 +526,8 @@ def bitexact_by_shape(fg, args, walks=16384, iterations=200):
 def extras(fg, args, value):
     """Keys beside the headline, each outside the timed region: the reference's own CUDA build
     on the same workload (ref_cuda), this engine's bit-exact mode there (bitexact), time to rank
-    23 on 3x3x3 per mode (ttr) and time to rank 47 on 4x4x4 (ttr_444)."""
+    23 on 3x3x3 per mode (ttr), time to rank 47 on 4x4x4 (ttr_444) and the additions reducer
+    beside the reference's (reducer)."""
     log = lambda msg: print(f"[bench] {msg}", file=sys.stderr, flush=True)  # noqa: E731
     out = {}
     t = time.perf_counter()
@@ -570,6 +572,153 @@ def extras(fg, args, value):
     out["ttr_444"] = {"workload": f"time to rank 47, 4x4x4 Z2, 65,536 walks, plus after 100,000 flips, "
                                   f"{args.ttr444_seconds:.0f} s budget", **r}
     log(f"ttr_444 leg {time.perf_counter() - t:.1f} s")
+    t = time.perf_counter()
+    out["reducer"] = reducer_leg(fg, args)
+    out["minimizer"] = minimizer_leg(fg, args)
+    log(f"reducer and minimizer legs {time.perf_counter() - t:.1f} s")
+    return out
+
+
+REDUCER_SCHEME = os.path.join(ROOT, "tests", "golden", "scheme_444_z2_r47.txt")
+
+
+def read_reducer_scheme():
+    """The committed 4x4x4 Z2 scheme of rank 47 as (n, m, coef [1][3][m][64] int8)."""
+    tok = [int(x) for x in open(REDUCER_SCHEME).read().split()]
+    n, m = tok[:3], tok[3]
+    nn = [n[0] * n[1], n[1] * n[2], n[2] * n[0]]
+    coef = np.zeros((1, 3, m, 64), np.int8)
+    p = 4
+    for c in range(3):
+        for t in range(m):
+            coef[0, c, t, :nn[c]] = tok[p:p + nn[c]]
+            p += nn[c]
+    return n, m, coef
+
+
+def searched_scheme_444(fg, path, seed=3):
+    """A 4x4x4 Z2 scheme as the minimizer meets them: the current scheme of the lowest-rank walk
+    (with at least one equal-factor pair, so that flips exist) after four launches of 5,000
+    fast-mode steps over 4,096 walks; written to PATH in the reference's text layout.
+    Returns (n, m, factor bitmasks [3][m])."""
+    with fg.Engine(4096, 64, "z2", "fast", seed, 5000, 100000, 0.01, 0.0) as eng:
+        eng.init_naive(4, 4, 4)
+        eng.run(4)
+        rec = eng.records()
+    n = [4, 4, 4]
+    order = np.argsort(rec.m, kind="stable")
+    for w in order:
+        m = int(rec.m[w])
+        fac = rec.fac[w, :, :m]
+        if any(len(set(fac[c].tolist())) < m for c in range(3)):
+            break
+    nn = [16, 16, 16]
+    with open(path, "w") as f:
+        f.write(f"{n[0]} {n[1]} {n[2]} {m}\n")
+        for c in range(3):
+            for t in range(m):
+                f.write(" ".join(str((int(fac[c, t]) >> j) & 1) for j in range(nn[c])) + "\n")
+    return n, m, fac.copy()
+
+
+def minimizer_leg(fg, args, count=4096, iterations=2000, launches=2, seed=3):
+    """The complexity minimizer (minimizeKernel, complexity_minimizer.cu:173-214) on COUNT copies
+    of one searched 4x4x4 Z2 scheme: this engine's bit-exact minimizer (the reference's cuRAND
+    stream and FlipSet lists) beside the reference's own CUDA build, LAUNCHES launches of
+    ITERATIONS flips from the same start; every walk's best complexity is compared."""
+    with tempfile.TemporaryDirectory() as tmp:
+        path = os.path.join(tmp, "scheme_444.txt")
+        n, m, fac = searched_scheme_444(fg, path, seed)
+        nn = [n[0] * n[1], n[1] * n[2], n[2] * n[0]]
+        rec = fg.Records(count, m, "z2")
+        rec.n[:] = n
+        rec.m[:] = m
+        rec.fac[:] = fac[None]
+        rec.best_fac[:] = rec.fac
+        rec.best_rank[:] = m
+        rec.best_m[:] = m
+        c0 = int(sum(bin(int(x)).count("1") for x in fac.ravel())) - 2 * m - nn[2]
+        with fg.Engine(32, m, "z2", "reference", seed, 10, 10**9, 0.0, 0.0) as warm:  # module load, attributes
+            warm.set_records(_first_walks(fg, rec, 32))
+            warm.rebuild_lists()
+            warm.minimize(np.full(32, c0, np.int32))
+        eng = fg.Engine(count, m, "z2", "reference", seed, iterations, 10**9, 0.0, 0.0)
+        eng.set_records(rec)
+        eng.rebuild_lists()
+        bc = np.full(count, c0, np.int32)
+        flips, t = 0, time.perf_counter()
+        for _ in range(launches):
+            bc = eng.minimize(bc)
+            flips += int(eng.counters()["flips"].sum())
+        dt = time.perf_counter() - t
+        ok = eng.validate(best=True)
+        eng.close()
+        out = {"workload": f"complexity minimizer, {count} copies of one searched 4x4x4 Z2 scheme of rank {m} "
+                           f"(complexity {c0}), {launches} launches of {iterations} flips, seed {seed}",
+               "unit": "verified flips/s", "ours": flips / dt if dt > 0 else None, "ours_seconds": dt,
+               "flips": flips, "best_complexity": int(bc.min()), "best_schemes_exact": bool(ok.all()),
+               "kernel": "bit-exact list-mode minimizer (the reference's stream and pair order), one warp per walk"}
+        per = os.path.join(tmp, "ref_minimizer.txt")
+        ref = run_ref_harness("z2", ["minimize_time", path, count, iterations, seed, launches, per], timeout=600)
+        if "unavailable" in ref:
+            out["ref_cuda"] = ref
+            return out
+        ref_bc = np.array([int(x) for x in open(per).read().split()], np.int64)
+    same = len(ref_bc) == count and bool(np.array_equal(ref_bc, bc))
+    ref_s = ref["ms_per_launch"] * launches / 1000.0
+    # identical best complexities: the reference's build made the same flips
+    out.update({"ref_cuda": flips / ref_s if same and ref_s > 0 else None, "ref_cuda_seconds": ref_s,
+                "ref_kernel": "minimizeKernel (unmodified, Z2 build, block 32)",
+                "ours_over_reference_cuda": ref_s / dt if same and dt > 0 else None,
+                "identical_to_reference": same})
+    return out
+
+
+def _first_walks(fg, rec, k):
+    """Records of the first k walks of rec."""
+    sub = fg.Records(k, rec.cap, rec.ring)
+    for name, _ in fg.Records.FIELDS:
+        a, b = getattr(rec, name, None), getattr(sub, name, None)
+        if a is not None and b is not None:
+            b[...] = a[:k]
+    return sub
+
+
+def reducer_leg(fg, args, count=4096, seed=3):
+    """The additions reducer (runReducersKernel, scheme_additions_reducer.cu:494-540) on a 4x4x4
+    Z2 scheme of rank 47 (found by this engine's search, a committed fixture): COUNT reducers,
+    one launch each side, this engine beside the reference's own CUDA build with the same
+    seed; both are bit-exact, so every reducer's U, V and W addition counts and modes are
+    compared too."""
+    n, m, coef = read_reducer_scheme()
+    warm = fg.Reducer(n, m, coef, count=32, schemes=1, seed=seed, threads=512)  # module load, attributes
+    warm.run(want_vars=False)
+    warm.close()
+    red = fg.Reducer(n, m, coef, count=count, schemes=1, seed=seed, threads=512)
+    t = time.perf_counter()
+    got = red.run(want_vars=False)  # synchronous: launch, then the counts copied back
+    dt = time.perf_counter() - t
+    red.close()
+    out = {"workload": f"additions reducer, {count} reducers on one 4x4x4 Z2 scheme of rank 47, seed {seed}, "
+                       "independent (no flips)",
+           "unit": "reducer runs/s", "ours": count / dt, "ours_seconds": dt,
+           "best_additions": int(got["additions"].sum(axis=1).min()),
+           "kernel": "one block of 512 threads per reducer (pair tables in shared memory)"}
+    with tempfile.TemporaryDirectory() as tmp:
+        per = os.path.join(tmp, "ref_reducers.txt")
+        ref = run_ref_harness("zt", ["reduce_time", REDUCER_SCHEME, count, seed, 1, per], timeout=600)
+        if "unavailable" in ref:
+            out["ref_cuda"] = ref
+            return out
+        rows = [ln.split() for ln in open(per)]
+    same = len(rows) == count and all(
+        [int(x) for x in rows[r][:3]] == [int(got["additions"][r, c]) for c in range(3)] and
+        rows[r][3:] == [fg.mode_name(got["mode"][r, c], got["scale"][r, c]) for c in range(3)]
+        for r in range(count))
+    out.update({"ref_cuda": ref["runs_per_s"], "ref_cuda_seconds": ref["ms_per_launch"] / 1000.0,
+                "ref_kernel": "runReducersKernel (unmodified, one thread per reducer, block 32)",
+                "ours_over_reference_cuda": out["ours"] / ref["runs_per_s"],
+                "identical_to_reference": bool(same)})
     return out
 
 

@@ -376,14 +376,16 @@ class Reducer:
         _check(self.lib.fg_reducer_create(ctypes.byref(self.cfg), n[0], n[1], n[2], m, _ptr(self.coef),
                                           ctypes.byref(self.h)))
 
-    def run(self, independent=True, best_fresh=None, best_vars=None):
+    def run(self, independent=True, best_fresh=None, best_vars=None, want_vars=True):
+        """One runReducersKernel launch; want_vars=False skips copying the fresh variables back
+        (out["vars"] is then None)."""
         counts = np.zeros((self.count, 13), np.int32)
         scale = np.zeros((self.count, 3), np.float32)
-        vars_ = np.zeros((self.count, 3, 500, 2), np.int32)
+        vars_ = np.zeros((self.count, 3, 500, 2), np.int32) if want_vars else None
         bf = np.ascontiguousarray(best_fresh if best_fresh is not None else np.zeros(3), np.int32)
         bv = np.ascontiguousarray(best_vars if best_vars is not None else np.zeros((3, 500, 2)), np.int32)
         _check(self.lib.fg_reducer_run(self.h, int(independent), _ptr(bf), _ptr(bv), _ptr(counts), _ptr(scale),
-                                       _ptr(vars_)))
+                                       _ptr(vars_) if vars_ is not None else None))
         per = counts[:, :12].reshape(self.count, 3, 4)
         return {"additions": per[:, :, 0].copy(), "fresh": per[:, :, 1].copy(), "naive": per[:, :, 2].copy(),
                 "mode": per[:, :, 3].copy(), "draws": counts[:, 12].copy(), "scale": scale, "vars": vars_}

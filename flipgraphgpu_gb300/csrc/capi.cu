@@ -487,14 +487,14 @@ bool list_thread_chosen(const fg_handle *h) {
 }
 
 // Static warps per block of the thread-per-walk list kernel: walks_per_block when given
-// (at most 8), else 6 for Z2 batches of several shape segments and 4 otherwise.  Measured on
+// (at most 16), else 6 for Z2 batches of several shape segments and 4 otherwise.  Measured on
 // GB300 (reference stream, verified flips/s, 4 against 6): Z2 six shapes 2x2x2..4x4x4,
 // 65,536 walks 3.35 G against 3.65 G, 16,384 walks 1.09 G against 1.35 G; Z2 3x3x3, 3x3x4,
 // 4x4x4, 65,536 walks 2.53 G against 2.84 G; ZT six shapes of at most 16 entries, 65,536
 // walks 2.04 G against 1.92 G; ZT 3x3x3 + 2x4x4 1.62 G against 0.95 G; one shape (16,384
 // walks of 3x3x3 or 4x4x4, both rings) 4 best by 1-8 %.
 int list_wpb(const fg_handle *h) {
-    if (h->cfg.walks_per_block > 0) return std::min(h->cfg.walks_per_block, 8);
+    if (h->cfg.walks_per_block > 0) return std::min(h->cfg.walks_per_block, 16);
     return h->cfg.ring == FG_RING_Z2 && h->segs.size() > 1 ? 6 : 4;
 }
 

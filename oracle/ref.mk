@@ -26,5 +26,5 @@ $(OUT)/complexity_minimizer: $(OBJ) $(CM) $(OUT)/obj/main_complexity_minimizer.o
 	$(NVCC) $(FLAGS) $^ -o $@
 $(OUT)/additions_reducer: $(OBJ) $(AR) $(OUT)/obj/main_additions_reducer.o
 	$(NVCC) $(FLAGS) $^ -o $@
-$(OUT)/ref_harness: $(OBJ) $(FG) $(AR) $(OUT)/obj/harness.o
+$(OUT)/ref_harness: $(OBJ) $(FG) $(CM) $(AR) $(OUT)/obj/harness.o
 	$(NVCC) $(FLAGS) $^ -o $@

@@ -27,6 +27,19 @@
 //       kept across iterations as the class keeps it); per iteration the
 //       schemes' ranks, every reducer's counts and the chosen top reducer.
 //
+//   reduce_time IN COUNT SEED LAUNCHES [OUT]
+//       Times runReducersKernel (independent, after initializeKernel) on COUNT
+//       reducers over the scheme of IN with CUDA events; prints JSON with the
+//       reducer runs per second and the addition totals' minimum and sum (the
+//       benchmark's reference leg for the additions reducer).
+//
+//   minimize_time IN COUNT ITERATIONS SEED LAUNCHES [OUT]
+//       The complexity minimizer's initializeKernel and LAUNCHES timed
+//       minimizeKernel launches (complexity_minimizer.cu:173-214) on COUNT copies
+//       of the scheme of IN; prints the mean launch time and the best complexity,
+//       and writes every walk's best complexity to OUT (the benchmark's
+//       reference leg for the minimizer).
+//
 //   gauss IN SEED OUT   (Z2 build)
 //       Reads schemes in flip_graph's text layout (a count, then per scheme
 //       "n1 n2 n3 m" and its rows; checkValidity=false), gives scheme k the
@@ -47,6 +60,7 @@
 #include <string>
 #include <vector>
 
+#include "entities/complexity_minimizer.cuh"
 #include "entities/flip_graph.cuh"
 #include "entities/scheme_additions_reducer.cuh"
 
@@ -267,6 +281,70 @@ static int cmd_reduce(int argc, char **argv) {
     return 0;
 }
 
+// reduce_time IN COUNT SEED LAUNCHES [OUT]: LAUNCHES times initializeKernel + one timed
+// runReducersKernel (independent) of COUNT reducers over the one scheme of IN (read with
+// checkValidity=false); prints the mean kernel time, reducer runs per second and the
+// per-reducer addition totals' minimum and sum (the same seed every launch).  OUT, when
+// given, receives one text line per reducer: U, V, W additions and the three modes.
+static int cmd_reduce_time(int argc, char **argv) {
+    if (argc != 6 && argc != 7) { fprintf(stderr, "reduce_time: bad arguments\n"); return 1; }
+    const char *in = argv[2];
+    int count = atoi(argv[3]), seed = atoi(argv[4]), launches = atoi(argv[5]);
+    if (count < 1 || launches < 1) { fprintf(stderr, "reduce_time: bad arguments\n"); return 1; }
+    typedef AdditionsReducer<MAX_U_EXPRESSIONS, MAX_U_FRESH_VARIABLES, MAX_U_REAL_VARIABLES, MAX_U_SUBEXPRESSIONS> RU;
+    typedef AdditionsReducer<MAX_V_EXPRESSIONS, MAX_V_FRESH_VARIABLES, MAX_V_REAL_VARIABLES, MAX_V_SUBEXPRESSIONS> RV;
+    typedef AdditionsReducer<MAX_W_EXPRESSIONS, MAX_W_FRESH_VARIABLES, MAX_W_REAL_VARIABLES, MAX_W_SUBEXPRESSIONS> RW;
+    RU *ru; RV *rv; RW *rw; SchemeInteger *schemes; curandState *states;
+    HCHECK(cudaMallocManaged(&ru, (count + 1) * sizeof(RU)));
+    HCHECK(cudaMallocManaged(&rv, (count + 1) * sizeof(RV)));
+    HCHECK(cudaMallocManaged(&rw, (count + 1) * sizeof(RW)));
+    HCHECK(cudaMallocManaged(&schemes, (count + 1) * sizeof(SchemeInteger)));
+    HCHECK(cudaMallocManaged(&states, count * sizeof(curandState)));
+    std::ifstream fin(in);
+    int n1, n2, n3, m;
+    fin >> n1 >> n2 >> n3 >> m;
+    if (!schemes[0].read(fin, n1, n2, n3, m, false)) { fprintf(stderr, "read failed\n"); return 1; }
+    int blockSize = 32, numBlocks = (count + blockSize - 1) / blockSize;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    double total_ms = 0;
+    for (int L = 0; L < launches; L++) {
+        initializeKernel<<<numBlocks, blockSize>>>(ru, rv, rw, schemes, states, count, 1, seed);
+        HCHECK(cudaGetLastError());
+        HCHECK(cudaDeviceSynchronize());
+        cudaEventRecord(e0);
+        runReducersKernel<<<numBlocks, blockSize>>>(ru, rv, rw, schemes, states, count, 1, true);
+        cudaEventRecord(e1);
+        HCHECK(cudaGetLastError());
+        HCHECK(cudaEventSynchronize(e1));
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        total_ms += ms;
+        fprintf(stderr, "launch %d: %.3f ms\n", L, ms);
+    }
+    if (argc == 7) {
+        FILE *f = fopen(argv[6], "w");
+        if (!f) { fprintf(stderr, "reduce_time: cannot write %s\n", argv[6]); return 1; }
+        for (int r = 0; r < count; r++)
+            fprintf(f, "%d %d %d %s %s %s\n", ru[r].getAdditions(), rv[r].getAdditions(), rw[r].getAdditions(),
+                    ru[r].getMode().c_str(), rv[r].getMode().c_str(), rw[r].getMode().c_str());
+        fclose(f);
+    }
+    long long sum = 0;
+    int best = 1 << 30;
+    for (int r = 0; r < count; r++) {
+        const int a = ru[r].getAdditions() + rv[r].getAdditions() + rw[r].getAdditions();
+        sum += a;
+        if (a < best) best = a;
+    }
+    printf("{\"reducers\": %d, \"launches\": %d, \"ms_per_launch\": %.3f, \"runs_per_s\": %.6e, "
+           "\"best_additions\": %d, \"sum_additions\": %lld, \"seed\": %d}\n",
+           count, launches, total_ms / launches, count / (total_ms / launches / 1000.0), best, sum, seed);
+    cudaFree(ru); cudaFree(rv); cudaFree(rw); cudaFree(schemes); cudaFree(states);
+    return 0;
+}
+
 static int cmd_reduce_flips(int argc, char **argv) {
     const char *in = argv[2];
     int count = atoi(argv[3]), schemesCount = atoi(argv[4]), seed = atoi(argv[5]);
@@ -339,6 +417,62 @@ static int cmd_reduce_flips(int argc, char **argv) {
     }
     write_tapes(f, states, count, seed, 1 << 18);
     fclose(f);
+    return 0;
+}
+
+// minimize_time IN COUNT ITERATIONS SEED LAUNCHES [OUT]: the complexity minimizer's own
+// kernels (complexity_minimizer.cu:173-214): initializeKernel replicates the one scheme of IN
+// (read with checkValidity=false) to COUNT walks with streams curand_init(SEED, idx, 0), then
+// LAUNCHES timed minimizeKernel launches of ITERATIONS flips each.  Prints the mean launch
+// time; OUT, when given, receives each walk's best complexity, one per line.
+static int cmd_minimize_time(int argc, char **argv) {
+    if (argc != 7 && argc != 8) { fprintf(stderr, "minimize_time: bad arguments\n"); return 1; }
+    const char *in = argv[2];
+    int count = atoi(argv[3]), iterations = atoi(argv[4]), seed = atoi(argv[5]), launches = atoi(argv[6]);
+    if (count < 1 || iterations < 1 || launches < 1) { fprintf(stderr, "minimize_time: bad arguments\n"); return 1; }
+    Scheme *schemes, *best;
+    int *bestComplexities;
+    curandState *states;
+    HCHECK(cudaMallocManaged(&schemes, count * sizeof(Scheme)));
+    HCHECK(cudaMallocManaged(&best, count * sizeof(Scheme)));
+    HCHECK(cudaMallocManaged(&bestComplexities, count * sizeof(int)));
+    HCHECK(cudaMallocManaged(&states, count * sizeof(curandState)));
+    std::ifstream fin(in);
+    int n1, n2, n3, m;
+    fin >> n1 >> n2 >> n3 >> m;
+    if (!schemes[0].read(fin, n1, n2, n3, m, false)) { fprintf(stderr, "read failed\n"); return 1; }
+    const int complexity = schemes[0].getComplexity();
+    int blockSize = 32, numBlocks = (count + blockSize - 1) / blockSize;
+    initializeKernel<<<numBlocks, blockSize>>>(schemes, best, bestComplexities, states, count, 1, complexity, seed);
+    HCHECK(cudaGetLastError());
+    HCHECK(cudaDeviceSynchronize());
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    double total_ms = 0;
+    for (int L = 0; L < launches; L++) {
+        cudaEventRecord(e0);
+        minimizeKernel<<<numBlocks, blockSize>>>(schemes, best, bestComplexities, states, count, iterations);
+        cudaEventRecord(e1);
+        HCHECK(cudaGetLastError());
+        HCHECK(cudaEventSynchronize(e1));
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        total_ms += ms;
+        fprintf(stderr, "launch %d: %.3f ms\n", L, ms);
+    }
+    int bestAll = 1 << 30;
+    for (int w = 0; w < count; w++) bestAll = std::min(bestAll, bestComplexities[w]);
+    if (argc == 8) {
+        FILE *f = fopen(argv[7], "w");
+        if (!f) { fprintf(stderr, "minimize_time: cannot write %s\n", argv[7]); return 1; }
+        for (int w = 0; w < count; w++) fprintf(f, "%d\n", bestComplexities[w]);
+        fclose(f);
+    }
+    printf("{\"walks\": %d, \"iterations\": %d, \"launches\": %d, \"ms_per_launch\": %.3f, "
+           "\"initial_complexity\": %d, \"best_complexity\": %d, \"seed\": %d}\n",
+           count, iterations, launches, total_ms / launches, complexity, bestAll, seed);
+    cudaFree(schemes); cudaFree(best); cudaFree(bestComplexities); cudaFree(states);
     return 0;
 }
 
@@ -598,11 +732,13 @@ static int cmd_ttr(int argc, char **argv) {
 }
 
 int main(int argc, char **argv) {
-    if (argc < 2) { fprintf(stderr, "usage: ref_harness walk|reduce|time|ttr ...\n"); return 1; }
+    if (argc < 2) { fprintf(stderr, "usage: ref_harness walk|reduce|reduce_time|minimize_time|time|ttr ...\n"); return 1; }
     if (std::string(argv[1]) == "ttr") return cmd_ttr(argc, argv);
     std::string cmd = argv[1];
     if (cmd == "walk") return cmd_walk(argc, argv);
     if (cmd == "reduce") return cmd_reduce(argc, argv);
+    if (cmd == "reduce_time") return cmd_reduce_time(argc, argv);
+    if (cmd == "minimize_time") return cmd_minimize_time(argc, argv);
     if (cmd == "time") return cmd_time(argc, argv);
 #ifndef SCHEME_INTEGER
     if (cmd == "gauss") return cmd_gauss(argc, argv);
