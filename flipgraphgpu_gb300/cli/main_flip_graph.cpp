@@ -10,8 +10,8 @@
 //   --max-launches N      stop after N launches (0: run forever, as the reference does)
 //   --target-rank R       stop once a walk's best rank reaches R (0: off)
 //   --time-budget S       stop after S seconds (0: off)
-//   --gauss-probability P Gauss (XOR) reduction per step with probability P / max iterations (Z2, list
-//                         modes; the reference defines SchemeZ2::tryReduceGauss but never calls it)
+//   --gauss-probability P Gauss (XOR) reduction per step with probability P / max iterations (Z2;
+//                         the reference defines SchemeZ2::tryReduceGauss but never calls it)
 //   --ternary-sandwiching 1  ZT: the sandwiching move conjugates by random signed permutations
 //                         (the reference's ternary sandwiching is empty)
 //   --retry-cap N         bound on the loops the reference leaves unbounded (tryPlus's pair
@@ -19,8 +19,7 @@
 //                         stops and a warning is printed (0: the library default, 2^20)
 // Resize meta-operators (--resize-probability, default 0.2), sandwiching and
 // basis-change moves run on both rings in the reference and philox modes and on
-// the Z2 ring in the fast mode (grown factors of at most 56 entries there); the
-// fast mode treats the Gauss reduction's probability as 0, with a note.
+// the Z2 ring in the fast mode (grown factors of at most 56 entries there).
 #include <algorithm>
 #include <chrono>
 #include <cstdio>
@@ -53,9 +52,9 @@ struct Options {
 };
 
 // Resizing, sandwiching and basis-change moves run in the list modes and in the fast mode on
-// the Z2 ring; the Gauss reduction in the list modes.
+// the Z2 ring; the Gauss reduction on the Z2 ring in every mode.
 bool movesHere(const Options &o) { return o.mode != "fast" || o.ring == "Z2"; }  // sandwiching, basis changes
-bool gaussHere(const Options &o) { return o.mode != "fast"; }
+bool gaussHere(const Options &o) { return o.ring == "Z2"; }
 bool resizeHere(const Options &o) { return o.mode != "fast" || o.ring == "Z2"; }
 
 class FlipGraph {
@@ -398,7 +397,7 @@ int main(int argc, char *argv[]) {
     parser.add("--ring", ArgType::String, "ZT|Z2|ZB", "coefficient ring (ZB: integers with |c| <= 2, fast mode)", "ZT");
     parser.add("--mode", ArgType::String, "MODE", "reference (bit-exact stream) | fast | philox", "reference");
     parser.add("--gauss-probability", ArgType::Real, "REAL",
-               "Gauss (XOR) reduction probability (divided by max iterations; Z2, list modes)", "0.0");
+               "Gauss (XOR) reduction probability (divided by max iterations; Z2)", "0.0");
     parser.add("--ternary-sandwiching", ArgType::Natural, "0|1",
                "ZT: sandwiching conjugates by random signed permutations (the reference's move is empty)", "0");
     parser.add("--retry-cap", ArgType::Natural, "INT",
@@ -487,12 +486,9 @@ int main(int argc, char *argv[]) {
         std::cout << "Note: sandwiching and basis-change moves are not available for the ZB ring; their "
                      "probabilities are treated as 0"
                   << std::endl;
-    if (!gaussHere(o) && o.gauss > 0)
-        std::cout << "Note: the Gauss reduction is not available in the fast mode; its probability is treated as 0"
-                  << std::endl;
     if (!resizeHere(o) && o.resize > 0)
         std::cout << "Note: resizing is not available for the ZB ring; its probability is treated as 0" << std::endl;
-    if (o.gauss > 0 && o.ring == "ZT")
+    if (o.gauss > 0 && o.ring != "Z2")
         std::cout << "Note: the Gauss reduction is defined for the Z2 ring only; its probability is treated as 0"
                   << std::endl;
 

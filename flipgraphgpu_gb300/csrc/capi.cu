@@ -609,8 +609,8 @@ fg_status fg_create(const fg_config *cfg, fg_handle **out) {
     if ((cfg->sandwich_p > 0 || cfg->basis_p > 0) && cfg->mode != FG_MODE_REFERENCE && cfg->mode != FG_MODE_PHILOX_LISTS &&
         !(cfg->mode == FG_MODE_FAST && cfg->ring == FG_RING_Z2))
         return fail(FG_ERR_ARG, "sandwiching and basis-change moves run in a list mode (reference or philox) or the Z2 fast mode");
-    if (cfg->gauss_p > 0 && (cfg->ring != FG_RING_Z2 || (cfg->mode != FG_MODE_REFERENCE && cfg->mode != FG_MODE_PHILOX_LISTS)))
-        return fail(FG_ERR_ARG, "the Gauss reduction runs on the Z2 ring in a list mode (reference or philox)");
+    if (cfg->gauss_p > 0 && (cfg->ring != FG_RING_Z2 || cfg->mode == FG_MODE_LEARNED))
+        return fail(FG_ERR_ARG, "the Gauss reduction runs on the Z2 ring in a list mode (reference or philox) or the fast mode");
     if (cfg->resize_p > 0 && cfg->cap < FG_MAX_RANK)
         return fail(FG_ERR_CAPACITY, "resizing needs cap >= 350 (products reach the maximal rank)");
     if (cfg->iterations <= 0) return fail(FG_ERR_ARG, "iterations must be positive");

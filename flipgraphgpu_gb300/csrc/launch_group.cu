@@ -61,6 +61,7 @@ __device__ void group_walk_one(const DevBatch &B, const WalkParams &P, int w, W 
             copied = true;
         }
         if (r.gate_reduce()) z.tryReduce();
+        if (r.gate_gauss()) z.tryReduceGauss();  // not in the reference's walk
         if (r.gate_expand() && z.m <= bestM + 2) {
             if (z.tryExpand(randint(1, 2, r))) flipsCount = 0;
         }

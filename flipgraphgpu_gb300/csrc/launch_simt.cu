@@ -25,9 +25,10 @@ __device__ __forceinline__ void simt_clear_best_tail(const DevBatch &B, int w, i
         for (int t = bestM < 0 ? 0 : bestM; t < B.cap; t++) dst[c * B.cap + t] = 0ull;
 }
 
-// randomWalkKernel (flip_graph.cu:520-573) for one walk, one thread.  MV: the sandwiching
-// and basis-change gates are compiled in (a run with both probabilities 0 takes the kernel
-// without them: their calls alone cost the walk loop a quarter of its speed).
+// randomWalkKernel (flip_graph.cu:520-573) for one walk, one thread.  MV: the gates of the
+// rare moves (Gauss reduction, sandwiching, basis changes) are compiled in (a run with their
+// probabilities 0 takes the kernel without them: their calls alone cost the walk loop a
+// quarter of its speed).
 template <class W, bool MV>
 __device__ void simt_walk_one(const DevBatch &B, const WalkParams &P, int w, W *s, int scap) {
     const WalkHeader h = B.hdr[w];
@@ -69,6 +70,9 @@ __device__ void simt_walk_one(const DevBatch &B, const WalkParams &P, int w, W *
             copied = true;
         }
         if (r.gate_reduce()) z.tryReduce();
+        if constexpr (MV) {
+            if (r.gate_gauss()) z.tryReduceGauss();  // not in the reference's walk
+        }
         if (r.gate_expand() && z.m <= bestM + 2) {
             if (z.tryExpand(randint(1, 2, r))) flipsCount = 0;
         }
@@ -225,7 +229,7 @@ cudaError_t walk_simt_t(const DevBatch &B, const WalkParams &P, int first, int c
 
 cudaError_t launch_walk_simt(const DevBatch &B, const WalkParams &P, int first, int count, int scap, int wide,
                              int wpb, int sms, cudaStream_t s) {
-    const bool moves = P.sandwich_T != kGateOff || P.basis_T != kGateOff;
+    const bool moves = P.sandwich_T != kGateOff || P.basis_T != kGateOff || P.gauss_T != kGateOff;
     if (wide) return moves ? walk_simt_t<unsigned long long, true>(B, P, first, count, scap, wpb, sms, s)
                            : walk_simt_t<unsigned long long, false>(B, P, first, count, scap, wpb, sms, s);
     return moves ? walk_simt_t<uint32_t, true>(B, P, first, count, scap, wpb, sms, s)

@@ -54,6 +54,7 @@ struct GroupDraws {
     __device__ __forceinline__ bool gate_expand() { return P->expand_T != kGateOff && (uint64_t)raw() < P->expand_T; }
     __device__ __forceinline__ bool gate_sandwich() { return P->sandwich_T != kGateOff && (uint64_t)raw() < P->sandwich_T; }
     __device__ __forceinline__ bool gate_basis() { return P->basis_T != kGateOff && (uint64_t)raw() < P->basis_T; }
+    __device__ __forceinline__ bool gate_gauss() { return P->gauss_T != kGateOff && (uint64_t)raw() < P->gauss_T; }
     __device__ __forceinline__ bool tie() { return raw() < 42949672u; }
 };
 
@@ -68,7 +69,7 @@ struct GroupFast {
     static constexpr int HS = Serial::HS;
     static constexpr W FM = Serial::FM;
     static constexpr W ONE = Serial::ONE;
-    enum { OP_ZEROFLIP, OP_REDUCE, OP_EXPAND, OP_PLUS, OP_TRYREDUCE, OP_SANDWICH, OP_BASIS };
+    enum { OP_ZEROFLIP, OP_REDUCE, OP_EXPAND, OP_PLUS, OP_TRYREDUCE, OP_SANDWICH, OP_BASIS, OP_GAUSS };
 
     W *s;  // [3][cap] compact, this group's walk
     int cap;
@@ -105,7 +106,7 @@ struct GroupFast {
         x.m = m; x.P0 = P0; x.P1 = P1; x.P2 = P2; x.status = status; x.result = 0;
         x.k0 = r.k0; x.k1 = r.k1; x.walk = r.walk; x.count = r.count; x.P = r.P;
         if (g == 0) {
-            if (op >= OP_SANDWICH) serial_move<W>(s, x, op == OP_SANDWICH);
+            if (op >= OP_SANDWICH) serial_move<W>(s, x, op - OP_SANDWICH);
             else serial_op<W>(s, x, op, a0, a1, a2, a3);
         }
         __syncwarp(mask);
@@ -256,6 +257,7 @@ struct GroupFast {
     __device__ bool tryReduce() { return serial(OP_TRYREDUCE) != 0; }
     __device__ void sandwich() { serial(OP_SANDWICH); }
     __device__ void swapBasis() { serial(OP_BASIS); }
+    __device__ bool tryReduceGauss() { return serial(OP_GAUSS) != 0; }
 };
 
 }  // namespace fg

@@ -46,10 +46,11 @@ __device__ __noinline__ void serial_op(W *s, SerialCtx &x, int op, int a0, int a
     x.count = tp.count; x.result = res;
 }
 
-// Sandwiching (sandwich != 0) or a basis change of a compact walk, as serial_op; kept apart
-// so that the matrices of the sandwiching move do not enlarge serial_op's frame.
+// A rare move of a compact walk, as serial_op: move 0 sandwiching, 1 a basis change, 2 the
+// Gauss reduction (x.result: it reduced); kept apart so that their matrices and index
+// arrays do not enlarge serial_op's frame.
 template <class W>
-__device__ __noinline__ void serial_move(W *s, SerialCtx &x, int sandwich) {
+__device__ __noinline__ void serial_move(W *s, SerialCtx &x, int move) {
     ThreadPhilox tp;
     tp.k0 = x.k0; tp.k1 = x.k1; tp.walk = x.walk; tp.count = x.count; tp.blk = -1; tp.P = x.P;
     SimtZ2<W, 0> z(tp);
@@ -57,10 +58,12 @@ __device__ __noinline__ void serial_move(W *s, SerialCtx &x, int sandwich) {
     z.n0 = x.n0; z.n1 = x.n1; z.n2 = x.n2;
     z.nn0 = x.n0 * x.n1; z.nn1 = x.n1 * x.n2; z.nn2 = x.n2 * x.n0; z.full = x.n0 * x.n1 * x.n2;
     z.m = x.m; z.P0 = x.P0; z.P1 = x.P1; z.P2 = x.P2; z.status = x.status;
-    if (sandwich) z.sandwich();
-    else z.swapBasis();
-    x.status = z.status;
-    x.count = tp.count;
+    int res = 0;
+    if (move == 0) z.sandwich();
+    else if (move == 1) z.swapBasis();
+    else res = z.tryReduceGauss();
+    x.m = z.m; x.P0 = z.P0; x.P1 = z.P1; x.P2 = z.P2; x.status = z.status;
+    x.count = tp.count; x.result = res;
 }
 
 }  // namespace fg

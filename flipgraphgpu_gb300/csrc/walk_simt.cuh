@@ -449,6 +449,94 @@ struct SimtZ2 {
         }
     }
 
+    // First XOR combination inside a run of terms (findXorCombination's search order): target
+    // member t, then members a < b < c < d of the run skipping t; a 4-term sum is tested before
+    // the 3-term sum of its prefix, which is tested before the 2-term sum.  comb receives the
+    // members then the target; returns their number (0: none).
+    __device__ int gaussXor(int j, const uint16_t *run, int size, int *comb) const {
+        if (size < 3) return 0;
+        for (int t = 0; t < size; t++) {
+            const W target = F(j, run[t]);
+            for (int a = 0; a < size; a++) {
+                if (a == t) continue;
+                const W va = F(j, run[a]);
+                for (int b = a + 1; b < size; b++) {
+                    if (b == t) continue;
+                    const W vb = F(j, run[b]);
+                    for (int c = b + 1; c < size; c++) {
+                        if (c == t) continue;
+                        const W vc = F(j, run[c]);
+                        for (int d = c + 1; d < size; d++) {
+                            if (d == t) continue;
+                            if ((va ^ vb ^ vc ^ F(j, run[d])) == target) {
+                                comb[0] = run[a]; comb[1] = run[b]; comb[2] = run[c]; comb[3] = run[d]; comb[4] = run[t];
+                                return 5;
+                            }
+                        }
+                        if ((va ^ vb ^ vc) == target) {
+                            comb[0] = run[a]; comb[1] = run[b]; comb[2] = run[c]; comb[3] = run[t];
+                            return 4;
+                        }
+                    }
+                    if ((va ^ vb) == target) {
+                        comb[0] = run[a]; comb[1] = run[b]; comb[2] = run[t];
+                        return 3;
+                    }
+                }
+            }
+        }
+        return 0;
+    }
+
+    // tryReduceGauss (scheme_z2.cu:312-442,621-629,1156-1163; defined by the reference, not
+    // called by its walk): for the components p in a random order (randomPermutation of 3),
+    // the terms sorted by their p-factor with the reference's Shell sort (gaps 701, 301, 132,
+    // 57, 23, 10, 4, 1; each sort starts from the previous order), and in each run of equal
+    // p-factors a member whose factor in component p+1 (then p+2) is the XOR of 2-4 other
+    // members' factors there is folded into them: its third factor is added to theirs and
+    // the term removed, then zero terms are compacted.  Partner counts follow every edit.
+    __device__ __noinline__ bool tryReduceGauss() {
+        int perm[3] = {0, 1, 2};
+        for (int q = 2; q > 0; q--) {
+            const int j = (int)r.below((uint32_t)(q + 1));
+            const int t = perm[q]; perm[q] = perm[j]; perm[j] = t;
+        }
+        uint16_t idx[kMaxRank + 2];
+        for (int t = 0; t < m; t++) idx[t] = (uint16_t)t;
+        int comb[5], size = 0, i = -1;
+        for (int q = 0; q < 3 && i < 0; q++) {
+            const int p = perm[q];
+            constexpr int gaps[8] = {701, 301, 132, 57, 23, 10, 4, 1};
+            for (int g = 0; g < 8; g++) {
+                const int gap = gaps[g];
+                if (gap > m) continue;
+                for (int a = gap; a < m; a++) {
+                    const uint16_t tmp = idx[a];
+                    const W key = F(p, tmp);
+                    int b = a;
+                    while (b >= gap && F(p, idx[b - gap]) > key) {
+                        idx[b] = idx[b - gap];
+                        b -= gap;
+                    }
+                    idx[b] = tmp;
+                }
+            }
+            int start = 0;
+            for (int e = 1; e <= m && i < 0; e++) {
+                if (e != m && F(p, idx[e]) == F(p, idx[start])) continue;
+                if ((size = gaussXor((p + 1) % 3, idx + start, e - start, comb)) > 0) i = (p + 2) % 3;
+                else if ((size = gaussXor((p + 2) % 3, idx + start, e - start, comb)) > 0) i = (p + 1) % 3;
+                start = e;
+            }
+        }
+        if (i < 0) return false;
+        const int last = comb[size - 1];
+        for (int q = 0; q < size - 1; q++) setWord(i, comb[q], F(i, comb[q]) ^ F(i, last));  // reduceGauss
+        removeAt(last);
+        removeZeroes();
+        return true;
+    }
+
     __device__ int complexity() const {
         int c = 0;
         for (int t = 0; t < m; t++) c += __popcll((uint64_t)F(0, t)) + __popcll((uint64_t)F(1, t)) + __popcll((uint64_t)F(2, t));

@@ -80,7 +80,7 @@ typedef struct {
     double basis_p;           /* --basis-probability (list modes, Z2 fast mode; per step: basis_p / iterations):
                                  swap two basis vectors (scheme_z2.cu:1302-1313,
                                  scheme_integer.cu:1219-1233) */
-    double gauss_p;           /* Z2, list modes: per step with probability gauss_p / iterations, the
+    double gauss_p;           /* Z2, list and fast modes: per step with probability gauss_p / iterations, the
                                  Gauss (XOR) reduction SchemeZ2::tryReduceGauss (scheme_z2.cu:312-442,
                                  1156-1163), which the reference defines but its walk never calls;
                                  0 (default) takes no draw, keeping the reference's trajectories */

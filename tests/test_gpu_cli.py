@@ -215,3 +215,33 @@ def test_flip_graph_zb_ring_saves_exact_schemes(work):
     back = os.path.join(work, "zb_back")
     run([os.path.join(BIN, "scheme_converter"), "-i", txt, "-o", back, "--ring", "ZB"], work)
     assert (len(os.listdir(back)) if os.path.isdir(back) else 1) == len(files)
+
+
+def test_flip_graph_fast_mode_runs_every_move(work):
+    """flip_graph --mode fast on Z2 with the reference's default resizing (0.2) and sandwiching and
+    basis-change moves: no note that a move is off, the walks resize, and every saved scheme is an
+    exact Z2 scheme of its sizes."""
+    import json
+    import numpy as np
+    from oracle import oracle as O
+    out = os.path.join(work, "fast_moves")
+    os.makedirs(out)
+    log = run([os.path.join(BIN, "flip_graph"), "-n1", "2", "-n2", "3", "-n3", "3", "--ring", "Z2", "--mode", "fast",
+               "--schemes", "256", "--max-iterations", "2000", "--plus-iterations", "500", "--sandwiching-probability",
+               "20", "--basis-probability", "20", "--seed", "9", "--max-launches", "6", "--path", out], work)
+    assert "not available" not in log and "treated as 0" not in log, log[-2000:]
+    files = sorted(os.listdir(out))
+    assert files and all(f.endswith("_Z2.json") for f in files)
+    sizes = set()
+    for name in files:
+        d = json.load(open(os.path.join(out, name)))
+        n, m = d["n"], d["m"]
+        sizes.add(tuple(n))
+        b = O.WalkBatch(1, max(m, 1), "z2")
+        b.n[0] = n
+        b.m[0] = m
+        for c, key_ in enumerate("uvw"):
+            for t, row in enumerate(d[key_]):
+                b.fac[0, c, t] = sum(1 << e for e, x in enumerate(row) if x % 2)
+        assert O.validate(b).all(), name
+    assert len(sizes) > 1  # resized schemes were saved too

@@ -483,6 +483,38 @@ def test_gauss_reduction_vs_oracle(mode, shape):
     assert (rec.m < m0).mean() > 0.5
 
 
+@pytest.mark.parametrize("kernel,lanes", [("thread", 0), ("group", 8), ("warp", 0)], ids=["thread", "group8", "warp"])
+@pytest.mark.parametrize("shape", [(3, 3, 3), (2, 3, 4), (4, 4, 4)])
+def test_fast_mode_gauss_reduction_vs_oracle(shape, kernel, lanes):
+    """The Gauss (XOR) reduction in the fast mode (gated after the reduction gate, Philox stream,
+    partner counts kept through the fold and the compaction) on schemes with planted
+    combinations, on every fast kernel: field for field equal to the oracle's fast mode."""
+    n1, n2, n3 = shape
+    S, cap, seed = 64, n1 * n2 * n3 + 8, 900 + n1 * n2 * n3
+    iters, plus = 60, 100000
+    with fg.Engine(S, cap, "z2", "philox", seed, iters, plus, 0.01, 0.0) as src:
+        src.init_naive(n1, n2, n3)
+        rec = src.records()
+    planted_gauss(rec, np.random.default_rng(seed))
+    fast = fg.Records(S, cap, "z2", lists=False)
+    for f in ("n", "m", "fac", "best_fac", "best_rank", "best_m"):
+        getattr(fast, f)[...] = getattr(rec, f)
+    with fg.Engine(S, cap, "z2", "fast", seed, iters, plus, 0.01, 0.0, gauss_p=60.0, sandwich_p=10.0) as eng:
+        eng.set_fast_kernel(kernel, lanes)
+        eng.set_records(fast)
+        rec0 = eng.records()
+        m0 = rec0.m.copy()
+        assert eng.validate().all()
+        eng.run(2)
+        out = eng.records()
+        assert eng.validate().all() and eng.validate(best=True).all()
+    kw = dict(iterations=iters, plus_iterations=plus, expand_p=0.01, reduce_p=0.0, gauss_p=60.0, sandwich_p=10.0,
+              seed=seed)
+    b = run_oracle_like(rec0, kw, 2, "fast")
+    compare_records(out, b, f"fast gauss {shape} {kernel}")
+    assert (out.m < m0).mean() > 0.5
+
+
 @pytest.mark.parametrize("mode,shape,resize_p", [("reference", (3, 3, 3), 0.0), ("philox", (2, 3, 3), 0.0),
                                                  ("reference", (2, 2, 3), 0.6)])
 def test_ternary_sandwiching_vs_oracle(mode, shape, resize_p):
