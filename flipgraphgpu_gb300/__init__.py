@@ -255,8 +255,8 @@ class Engine:
         _check(self.lib.fg_rebuild_lists(self.h))
 
     def set_list_kernel(self, kernel):
-        """List modes, Z2: 'thread' (one thread per walk; no resizing, sandwiching, basis changes
-        or Gauss reduction), 'warp' (one warp per walk) or 'auto'.  Results are identical."""
+        """List modes: 'thread' (one thread per walk; no sandwiching, basis changes or Gauss
+        reduction), 'warp' (one warp per walk) or 'auto'.  Results are identical."""
         kinds = {"auto": -1, "warp": 0, "thread": 1}
         self.lib.fg_set_list_kernel.restype = ctypes.c_int
         _check(self.lib.fg_set_list_kernel(self.h, kinds[kernel]))

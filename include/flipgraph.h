@@ -262,10 +262,12 @@ fg_status fg_set_fast_kernel(fg_handle *h, int kernel, int lanes);
  * per walk (every option, including resizing, sandwiching, basis changes and the
  * Gauss reduction); FG_LIST_THREAD = one thread per walk with the FlipSet lists
  * in a device scratch of 3,024 bytes per walk, allocated on first use (only
- * with resizing, sandwiching, basis changes and the Gauss reduction off, and
- * on ZT for factors of at most 31 entries, every input factor valid above 16);
- * -1 = automatic (thread per walk where it applies and the batch has enough
- * walks to fill the GPU).  Both give identical results.  FG_LIST_THREAD on a
+ * with sandwiching, basis changes and the Gauss reduction off, for slots up to
+ * 256, and on ZT for factors of at most 31 entries, every input factor valid
+ * above 16; with resizing the segments follow the sizes after every resize,
+ * and a launch whose sizes do not fit takes the warp kernel);
+ * -1 = automatic (thread per walk where it applies, resizing is off and the
+ * batch has enough walks to fill the GPU).  Both give identical results.  FG_LIST_THREAD on a
  * configuration it does not cover returns FG_ERR_ARG. */
 enum { FG_LIST_WARP = 0, FG_LIST_THREAD = 1 };
 fg_status fg_set_list_kernel(fg_handle *h, int kernel);

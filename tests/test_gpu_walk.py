@@ -51,12 +51,12 @@ def test_philox_device_matches_oracle():
 @pytest.mark.parametrize("path", walk_fixtures(), ids=lambda p: p.split("/")[-1].split(".")[0])
 def test_walk_matches_reference_kernel(path, list_kernel):
     """Same seed, same flags: the library reproduces the reference's per-launch state, with one
-    warp per walk and (without the resize, sandwiching and basis moves) one thread per walk."""
+    warp per walk and (without the sandwiching and basis moves) one thread per walk."""
     d = golden_io.read_walk(path)
     ring = d["ring"]
-    moves = d["resize_p"] > 0 or d["sandwich_p"] > 0 or d["basis_p"] > 0
+    moves = d["sandwich_p"] > 0 or d["basis_p"] > 0
     if list_kernel == "thread" and moves:
-        pytest.skip("the thread-per-walk list kernel runs without resize, sandwiching and basis moves")
+        pytest.skip("the thread-per-walk list kernel runs without sandwiching and basis moves")
     n1, n2, n3 = d["n"]
     cap = 352 if d["resize_p"] > 0 else n1 * n2 * n3
     with fg.Engine(d["walks"], cap, ring, "reference", d["seed"], d["iterations"], d["plus_iterations"],
@@ -88,14 +88,19 @@ def test_walk_matches_reference_kernel(path, list_kernel):
     ("zt", "reference", (3, 3, 3), 12, 60, 40, 0.0, 10.0, 20.0, 3),
     ("zt", "philox", (2, 3, 3), 12, 60, 40, 0.5, 5.0, 20.0, 3),
 ])
-def test_meta_moves_vs_oracle(ring, mode, shape, S, iters, plus, resize_p, sandwich_p, basis_p, launches):
-    """Resize meta-operators, sandwiching and basis changes on the GPU (one warp per walk) against
-    the oracle: sizes, factors, lists, best schemes and sizes, best ranks and stream positions."""
+@pytest.mark.parametrize("list_kernel", ["warp", "thread"])
+def test_meta_moves_vs_oracle(ring, mode, shape, S, iters, plus, resize_p, sandwich_p, basis_p, launches, list_kernel):
+    """Resize meta-operators, sandwiching and basis changes on the GPU (one warp per walk; one
+    thread per walk with resizing alone) against the oracle: sizes, factors, lists, best schemes
+    and sizes, best ranks and stream positions."""
+    if list_kernel == "thread" and (sandwich_p > 0 or basis_p > 0):
+        pytest.skip("the thread-per-walk list kernel runs without sandwiching and basis moves")
     n1, n2, n3 = shape
     seed = 500 + n1 + n2 + n3
     cap = 352 if resize_p > 0 else n1 * n2 * n3
     with fg.Engine(S, cap, ring, mode, seed, iters, plus, 0.01, 0.0, resize_p=resize_p, sandwich_p=sandwich_p,
                    basis_p=basis_p) as eng:
+        eng.set_list_kernel(list_kernel)
         eng.init_naive(n1, n2, n3)
         rec0 = eng.records()
         eng.run(launches)
@@ -706,7 +711,7 @@ def test_thread_list_kernel_is_refused_where_it_does_not_apply():
     with fg.Engine(32, 27, "zt", "reference", 1, 10, 100, sandwich_p=1.0) as eng:
         with pytest.raises(fg.FlipGraphError):
             eng.set_list_kernel("thread")
-    with fg.Engine(32, 352, "z2", "reference", 1, 10, 100, resize_p=0.2) as eng:
+    with fg.Engine(32, 27, "z2", "reference", 1, 10, 100, gauss_p=1.0) as eng:
         with pytest.raises(fg.FlipGraphError):
             eng.set_list_kernel("thread")
 
