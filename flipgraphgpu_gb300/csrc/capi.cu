@@ -209,6 +209,7 @@ struct fg_handle {
     std::vector<Segment> segs;
     std::vector<int> launchOrder;  // segments by ascending work (slots x walks), launched in this order
     LearnedBuffers learned;
+    LearnedGraph learnedGraph;  // the learned step loop, captured once per set of arguments
     LearnedConfig lcfg;
     fg_mlp *mlp = nullptr;
     int simtMaxCap = -1;                  // fg_set_fast_split: thread per walk up to this slot count (-1: off)
@@ -546,7 +547,7 @@ fg_status launch_walks(fg_handle *h) {
     if (h->cfg.mode == FG_MODE_LEARNED) {
         for (const Segment &g : h->segs)
             if (g.nnmax > 21) return fail(FG_ERR_CAPACITY, "the learned mode takes factors of at most 21 entries");
-        FG_CUDA(learned_launch(h->learned, h->B, h->P, h->lcfg, h->mlp, h->stream));
+        FG_CUDA(learned_launch(h->learned, h->B, h->P, h->lcfg, h->mlp, h->stream, &h->learnedGraph));
         return FG_OK;
     }
     if (h->cfg.mode != FG_MODE_FAST) {
@@ -703,6 +704,7 @@ fg_status fg_destroy(fg_handle *h) {
     if (!h) return FG_OK;
     cudaSetDevice(h->dev);
     if (h->stream) cudaStreamSynchronize(h->stream);
+    h->learnedGraph.reset();
     learned_free(h->learned);
     drop_graph(h);
     void *ptrs[] = {h->B.hdr, h->B.fac, h->B.sgn, h->B.valid, h->B.lists, h->B.best_fac, h->B.best_sgn,
@@ -776,6 +778,7 @@ fg_status fg_set_proposal(fg_handle *h, fg_mlp *mlp, int candidates, float tempe
         return fail(FG_ERR_ARG, "candidates in [1, 16], temperature > 0, min_entropy >= 0");
     FG_CUDA(cudaSetDevice(h->dev));
     FG_CUDA(cudaStreamSynchronize(h->stream));
+    h->learnedGraph.reset();  // the captured step loop names the old network's and buffers' addresses
     if (candidates != h->learned.K) FG_CUDA(learned_alloc(h->learned, h->B.S, h->B.cap, candidates));
     h->mlp = mlp;
     h->lcfg.K = candidates;

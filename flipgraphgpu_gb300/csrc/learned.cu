@@ -280,17 +280,71 @@ void learned_free(LearnedBuffers &L) {
     L = LearnedBuffers{};
 }
 
-cudaError_t learned_launch(LearnedBuffers &L, const DevBatch &B, const WalkParams &P, const LearnedConfig &C,
-                           fg_mlp *mlp, cudaStream_t s) {
+namespace {
+
+cudaError_t learned_steps(LearnedBuffers &L, const DevBatch &B, const WalkParams &P, const LearnedConfig &C,
+                          fg_mlp *mlp, int useScores, cudaStream_t s) {
     const int threads = 128, blocks = (L.S + threads - 1) / threads;
-    k_learned_load<<<blocks, threads, 0, s>>>(B, P, L);
-    cudaError_t e = cudaGetLastError();
-    const int useScores = (L.K > 1 && mlp) ? 1 : 0;
+    cudaError_t e = cudaSuccess;
     for (int step = 0; step <= P.iterations && !e; step++) {
         k_learned_step<<<blocks, threads, 0, s>>>(B, P, L, C, useScores);
         e = cudaGetLastError();
         if (!e && useScores && step < P.iterations) e = mlp_score_device(mlp, L.feat, L.S * L.K, L.scores, s);
     }
+    return e;
+}
+
+template <class T> void append_bytes(std::vector<unsigned char> &k, const T &v) {
+    const unsigned char *p = reinterpret_cast<const unsigned char *>(&v);
+    k.insert(k.end(), p, p + sizeof(T));
+}
+
+// The step loop, through G's graph when G is given (see LearnedGraph).
+cudaError_t learned_steps_graph(LearnedBuffers &L, const DevBatch &B, const WalkParams &P, const LearnedConfig &C,
+                                fg_mlp *mlp, int useScores, cudaStream_t s, LearnedGraph *G) {
+    if (!G) return learned_steps(L, B, P, C, mlp, useScores, s);
+    std::vector<unsigned char> key;
+    append_bytes(key, B);
+    append_bytes(key, P);
+    append_bytes(key, C);
+    append_bytes(key, L);
+    append_bytes(key, mlp);
+    append_bytes(key, mlp_workspace_epoch(mlp));
+    append_bytes(key, useScores);
+    if (key != G->key) {  // new arguments: run directly once
+        G->reset();
+        G->key = key;
+        G->primed = true;
+        return learned_steps(L, B, P, C, mlp, useScores, s);
+    }
+    if (G->exec) return cudaGraphLaunch(G->exec, s);
+    if (G->failed) return learned_steps(L, B, P, C, mlp, useScores, s);
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed);
+    if (e) return e;
+    const cudaError_t le = learned_steps(L, B, P, C, mlp, useScores, s);
+    const cudaError_t ce = cudaStreamEndCapture(s, &g);
+    if (le == cudaSuccess && ce == cudaSuccess) e = cudaGraphInstantiate(&G->exec, g, 0);
+    else e = le != cudaSuccess ? le : ce;
+    if (g) cudaGraphDestroy(g);
+    if (e != cudaSuccess) {  // not capturable here: direct launches from now on
+        cudaGetLastError();
+        G->exec = nullptr;
+        G->failed = true;
+        return learned_steps(L, B, P, C, mlp, useScores, s);
+    }
+    return cudaGraphLaunch(G->exec, s);
+}
+
+}  // namespace
+
+cudaError_t learned_launch(LearnedBuffers &L, const DevBatch &B, const WalkParams &P, const LearnedConfig &C,
+                           fg_mlp *mlp, cudaStream_t s, LearnedGraph *G) {
+    const int threads = 128, blocks = (L.S + threads - 1) / threads;
+    k_learned_load<<<blocks, threads, 0, s>>>(B, P, L);
+    cudaError_t e = cudaGetLastError();
+    const int useScores = (L.K > 1 && mlp) ? 1 : 0;
+    if (!e) e = learned_steps_graph(L, B, P, C, mlp, useScores, s, G);
     if (!e) {
         k_learned_store<<<blocks, threads, 0, s>>>(B, L);
         e = cudaGetLastError();

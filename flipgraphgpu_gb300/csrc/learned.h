@@ -43,12 +43,27 @@ struct LearnedBuffers {
     uint32_t *drops = nullptr;   // [S][dropCap] accepted-flip indices at which the rank dropped
 };
 
+// The step loop of a launch (step kernels and the network's scoring between them) as a CUDA
+// graph: captured on the second launch with the same arguments (the first one runs directly
+// and sets the kernels' attributes and the network's workspace), then replayed.
+struct LearnedGraph {
+    cudaGraphExec_t exec = nullptr;
+    std::vector<unsigned char> key;  // the launch arguments the graph was captured with
+    bool primed = false, failed = false;
+    void reset() {
+        if (exec) cudaGraphExecDestroy(exec);
+        exec = nullptr;
+        key.clear();
+        primed = failed = false;
+    }
+};
+
 cudaError_t learned_alloc(LearnedBuffers &L, int S, int scap, int K);
 cudaError_t learned_alloc_records(LearnedBuffers &L, long long recCap, int dropCap);
 void learned_free(LearnedBuffers &L);
 // One launch (P.iterations steps per walk) over the batch records in B.
 cudaError_t learned_launch(LearnedBuffers &L, const DevBatch &B, const WalkParams &P, const LearnedConfig &C,
-                           fg_mlp *mlp, cudaStream_t s);
+                           fg_mlp *mlp, cudaStream_t s, LearnedGraph *G = nullptr);
 // Labels of the logged records: 1 if the walk's rank dropped at or within
 // `horizon` accepted flips after the record's flip, 0 if it did not; records
 // whose outcome is unknown (walk ended or drop log full) are dropped.

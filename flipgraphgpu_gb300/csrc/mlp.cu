@@ -35,6 +35,7 @@ struct fg_mlp {
     float *scores = nullptr, *ds = nullptr, *lab = nullptr, *loss = nullptr;
     int *err = nullptr;
     int adamStep = 0;
+    unsigned long long epoch = 0;  // bumped whenever the workspace is reallocated (captured graphs name its buffers)
 };
 
 namespace fg {
@@ -179,6 +180,7 @@ cudaError_t ensure_workspace(fg_mlp *m, int rowsPad) {
         return e;
     }
     m->cap = rowsPad;
+    m->epoch++;
     return cudaSuccess;
 }
 
@@ -270,6 +272,8 @@ fg_status check_err(fg_mlp *m) {
 }
 
 }  // namespace
+
+unsigned long long mlp_workspace_epoch(const fg_mlp *m) { return m ? m->epoch : 0ull; }
 
 cudaError_t mlp_score_device(fg_mlp *m, const uint64_t *features, int rows, float *scores, cudaStream_t s) {
     const int rowsPad = (rows + 127) / 128 * 128;

@@ -26,5 +26,8 @@ constexpr int kMlpParams = kOffB3 + 1;
 // Scores `rows` rows of feature words ([rows][3] uint64, device) into
 // scores[rows] (device) on stream s; the network's device must be current.
 cudaError_t mlp_score_device(fg_mlp *m, const uint64_t *features, int rows, float *scores, cudaStream_t s);
+// Counts the reallocations of the network's workspace (0 for no network): a graph that
+// captured the scoring is valid only while this is unchanged.
+unsigned long long mlp_workspace_epoch(const fg_mlp *m);
 
 }  // namespace fg
