@@ -178,15 +178,14 @@ def test_fast_mode_walk_is_deterministic_and_valid():
 
 @pytest.mark.parametrize("shape", [(3, 3, 3), (2, 4, 8), (2, 2, 17)])
 def test_fast_mode_moves_keep_schemes_exact(shape):
-    """Fast mode (implicit pairs) with sandwiching and basis changes at a high rate: deterministic,
-    every scheme exact, and the moves change the trajectory (their gate draws alone would not
-    change the factor multiset of a walk whose gates never fire)."""
+    """Fast mode (implicit pairs) with sandwiching, basis changes and the Gauss reduction at a
+    high rate: deterministic, every scheme exact, and the moves change the trajectory."""
     n1, n2, n3 = shape
     b1 = O.WalkBatch(8, n1 * n2 * n3, "z2")
     O.init_naive(b1, n1, n2, n3)
     b2, b0 = b1.copy(), b1.copy()
     kw = dict(iterations=600, plus_iterations=200, launches=2, seed=11)
-    cfg = b1.cfg("fast", sandwich_p=60.0, basis_p=60.0, **kw)
+    cfg = b1.cfg("fast", sandwich_p=60.0, basis_p=60.0, gauss_p=30.0, **kw)
     O.walk(b1, cfg)
     O.walk(b2, cfg)
     O.walk(b0, b0.cfg("fast", **kw))
