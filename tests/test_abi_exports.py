@@ -101,3 +101,13 @@ def test_engine_checks_record_layouts_before_the_library_sees_them(ring):
     for rec in bad:
         with pytest.raises(ValueError):
             eng._match(rec)
+
+
+def test_integration_stub_lists_every_config_field():
+    """The ctypes binding a maintainer copies from INTEGRATION.md names every field of fg_config,
+    in order, with the types the package's own mirror uses."""
+    doc = open(os.path.join(os.path.dirname(HEADER), "..", "INTEGRATION.md")).read()
+    block = doc[doc.index("class Config(ctypes.Structure)"):]
+    block = block[:block.index("]") + 1]
+    stub = [(name, getattr(ctypes, t)) for name, t in re.findall(r'\("([a-z_0-9]+)", ctypes\.(c_[a-z0-9]+)\)', block)]
+    assert stub == list(fg.Config._fields_)
