@@ -863,6 +863,7 @@ fg_status fg_autotune(fg_handle *h, int iterations, int32_t *kinds, int32_t *lan
         size_t bytes;
     };
     std::vector<Region> regs = {{h->B.hdr, S * sizeof(WalkHeader)}, {h->B.fac, nf * 8}, {h->B.best_fac, nf * 8}};
+    if (h->B.best_n) regs.push_back({h->B.best_n, S * 3 * sizeof(int32_t)});  // resizing: best sizes
     if (lists) {
         regs.push_back({h->B.lists, S * 3 * kListCap * sizeof(uint32_t)});
         if (h->B.xorwow) regs.push_back({h->B.xorwow, S * sizeof(curandStateXORWOW_t)});
