@@ -668,6 +668,76 @@ def test_zt_thread_list_kernel_on_wide_factors_vs_oracle(shape):
     assert np.isin(hi, [0, (1 << 33) - 1]).all()
 
 
+def strassen_blocks(k):
+    """A ternary scheme for 2 x 2 x 2k of rank 7k (Strassen's seven products on each 2 x 2 block
+    of B's and C's columns), signs canonical (first nonzero of u and v positive): the walks start
+    below the naive rank, so random splits (two 16-bit chunks for factors of 20 entries) occur."""
+    n1, n2, n3 = 2, 2, 2 * k
+    A = lambda i, c: i * n2 + c  # noqa: E731
+    terms = []
+    for blk in range(k):
+        B = lambda r, jj: r * n3 + 2 * blk + jj  # noqa: E731
+        C = lambda i, jj: (2 * blk + jj) * n1 + i  # noqa: E731
+        terms += [({A(0, 0): 1, A(1, 1): 1}, {B(0, 0): 1, B(1, 1): 1}, {C(0, 0): 1, C(1, 1): 1}),
+                  ({A(1, 0): 1, A(1, 1): 1}, {B(0, 0): 1}, {C(1, 0): 1, C(1, 1): -1}),
+                  ({A(0, 0): 1}, {B(0, 1): 1, B(1, 1): -1}, {C(0, 1): 1, C(1, 1): 1}),
+                  ({A(1, 1): 1}, {B(1, 0): 1, B(0, 0): -1}, {C(0, 0): 1, C(1, 0): 1}),
+                  ({A(0, 0): 1, A(0, 1): 1}, {B(1, 1): 1}, {C(0, 0): -1, C(0, 1): 1}),
+                  ({A(1, 0): 1, A(0, 0): -1}, {B(0, 0): 1, B(0, 1): 1}, {C(1, 1): 1}),
+                  ({A(0, 1): 1, A(1, 1): -1}, {B(1, 0): 1, B(1, 1): 1}, {C(0, 0): 1})]
+    neg = lambda d: {e: -x for e, x in d.items()}  # noqa: E731
+    out = []
+    for u, v, w in terms:
+        pu, pv = u[min(u)] > 0, v[min(v)] > 0
+        if not pu and not pv:
+            u, v = neg(u), neg(v)
+        elif not pu:
+            u, w = neg(u), neg(w)
+        elif not pv:
+            v, w = neg(v), neg(w)
+        out.append((u, v, w))
+    return (n1, n2, n3), out
+
+
+@pytest.mark.parametrize("mode", ["philox", "reference"])
+def test_zt_thread_list_kernel_splits_wide_factors_vs_oracle(mode):
+    """From a scheme below the naive rank the ternary walks split factors of 20 entries (two
+    16-bit chunks, the second sign-extended in the reference); the thread-per-walk kernel's
+    32-bit words follow the oracle field for field, records written back sign-extended."""
+    (n1, n2, n3), terms = strassen_blocks(5)
+    S, cap, seed, iters, plus = 64, 48, 97, 1500, 60
+    m = len(terms)
+    rec = fg.Records(S, cap, "zt")
+    rec.n[:] = (n1, n2, n3)
+    rec.m[:] = m
+    for t, tri in enumerate(terms):
+        for c, d in enumerate(tri):
+            for e, x in d.items():
+                rec.fac[:, c, t] |= np.uint64(1 << e)
+                if x < 0:
+                    rec.sgn[:, c, t] |= np.uint64(1 << e)
+    rec.valid[:, :, :m] = 1
+    rec.best_fac[:] = rec.fac
+    rec.best_sgn[:] = rec.sgn
+    rec.best_valid[:] = rec.valid
+    rec.best_rank[:] = m
+    rec.best_m[:] = m
+    kw = dict(iterations=iters, plus_iterations=plus, expand_p=200.0, reduce_p=0.0, seed=seed)
+    with fg.Engine(S, cap, "zt", mode, seed, iters, plus, 200.0, 0.0) as eng:
+        eng.set_list_kernel("thread")
+        eng.set_records(rec)
+        eng.rebuild_lists()
+        rec0 = eng.records()
+        assert eng.validate().all()
+        eng.run(2)
+        out = eng.records()
+        assert eng.validate().all() and eng.validate(best=True).all()
+    tape = xorwow_tape_for(out, seed) if mode == "reference" else None
+    b = run_oracle_like(rec0, kw, 2, "tape" if mode == "reference" else "philox", tape)
+    compare_records(out, b, f"zt splits {mode}")
+    assert (out.m != m).any()
+
+
 def test_zt_factors_of_32_entries_take_the_warp_kernel():
     """A naive factor of 32 entries sets bit 31 without copying it into bits 32-63, which the
     thread kernel's 32-bit words cannot stand for: the thread kernel is refused, the automatic

@@ -259,3 +259,25 @@ def test_flip_pass_properties():
         assert not coef[s, :, ranks[s]:].any()
     assert O.validate_arrays("zt", np.tile(np.asarray(n, np.int32), (S, 1)), ranks, fac, sgn, valid).all()
     assert (coef[1:] != coef0[None]).any()  # the flips changed schemes
+
+
+@pytest.mark.parametrize("shape", [(3, 4, 5), (2, 3, 10), (5, 5, 5)])
+def test_ternary_factors_up_to_31_entries_stay_sign_extended(shape):
+    """The thread-per-walk ternary kernel keeps factors of 17-31 entries as 32-bit words standing
+    for sext(word): the reference's random split sign-extends its second 16-bit chunk, naive
+    factors leave bits 31-63 clear, and xor / and keep the property.  Walks with many splits
+    (philox lists, the oracle) must keep bits 32-63 of every value and sign equal to bit 31."""
+    n1, n2, n3 = shape
+    b = O.WalkBatch(16, n1 * n2 * n3 + 8, "zt")
+    O.init_naive(b, n1, n2, n3)
+    O.walk(b, b.cfg("philox", iterations=400, plus_iterations=60, launches=3, expand_p=40.0, seed=5))
+    assert O.validate(b).all()
+    for w in range(b.S):
+        m = int(b.m[w])
+        for arr in (b.fac[w, :, :m], b.sgn[w, :, :m]):
+            hi = arr >> np.uint64(31)
+            assert np.isin(hi, [0, (1 << 33) - 1]).all()
+    nn = [n1 * n2, n2 * n3, n3 * n1]
+    wide = [c for c in range(3) if nn[c] > 16]
+    # some split drew a second chunk: entries at or above the factor's size are set
+    assert any((b.fac[:, c, :] >> np.uint64(nn[c]) != 0).any() for c in wide)
