@@ -9,7 +9,7 @@ import numpy as np
 import pytest
 
 import golden_io
-from helpers import diff_walk, walk_fixtures
+from helpers import diff_walk, strassen_blocks, walk_fixtures
 from oracle import oracle as O
 
 pytestmark = pytest.mark.gpu
@@ -666,37 +666,6 @@ def test_zt_thread_list_kernel_on_wide_factors_vs_oracle(shape):
     compare_records(rec, b, f"zt wide {shape}")
     hi = rec.fac >> np.uint64(31)  # bits 31-63: all zero or all one
     assert np.isin(hi, [0, (1 << 33) - 1]).all()
-
-
-def strassen_blocks(k):
-    """A ternary scheme for 2 x 2 x 2k of rank 7k (Strassen's seven products on each 2 x 2 block
-    of B's and C's columns), signs canonical (first nonzero of u and v positive): the walks start
-    below the naive rank, so random splits (two 16-bit chunks for factors of 20 entries) occur."""
-    n1, n2, n3 = 2, 2, 2 * k
-    A = lambda i, c: i * n2 + c  # noqa: E731
-    terms = []
-    for blk in range(k):
-        B = lambda r, jj: r * n3 + 2 * blk + jj  # noqa: E731
-        C = lambda i, jj: (2 * blk + jj) * n1 + i  # noqa: E731
-        terms += [({A(0, 0): 1, A(1, 1): 1}, {B(0, 0): 1, B(1, 1): 1}, {C(0, 0): 1, C(1, 1): 1}),
-                  ({A(1, 0): 1, A(1, 1): 1}, {B(0, 0): 1}, {C(1, 0): 1, C(1, 1): -1}),
-                  ({A(0, 0): 1}, {B(0, 1): 1, B(1, 1): -1}, {C(0, 1): 1, C(1, 1): 1}),
-                  ({A(1, 1): 1}, {B(1, 0): 1, B(0, 0): -1}, {C(0, 0): 1, C(1, 0): 1}),
-                  ({A(0, 0): 1, A(0, 1): 1}, {B(1, 1): 1}, {C(0, 0): -1, C(0, 1): 1}),
-                  ({A(1, 0): 1, A(0, 0): -1}, {B(0, 0): 1, B(0, 1): 1}, {C(1, 1): 1}),
-                  ({A(0, 1): 1, A(1, 1): -1}, {B(1, 0): 1, B(1, 1): 1}, {C(0, 0): 1})]
-    neg = lambda d: {e: -x for e, x in d.items()}  # noqa: E731
-    out = []
-    for u, v, w in terms:
-        pu, pv = u[min(u)] > 0, v[min(v)] > 0
-        if not pu and not pv:
-            u, v = neg(u), neg(v)
-        elif not pu:
-            u, w = neg(u), neg(w)
-        elif not pv:
-            v, w = neg(v), neg(w)
-        out.append((u, v, w))
-    return (n1, n2, n3), out
 
 
 @pytest.mark.parametrize("mode", ["philox", "reference"])

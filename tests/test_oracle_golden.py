@@ -14,7 +14,7 @@ import numpy as np
 import pytest
 
 import golden_io
-from helpers import diff_walk, golden, read_scheme_text, walk_fixtures
+from helpers import diff_walk, golden, read_scheme_text, strassen_blocks, walk_fixtures
 from oracle import oracle as O
 
 
@@ -261,23 +261,35 @@ def test_flip_pass_properties():
     assert (coef[1:] != coef0[None]).any()  # the flips changed schemes
 
 
-@pytest.mark.parametrize("shape", [(3, 4, 5), (2, 3, 10), (5, 5, 5)])
-def test_ternary_factors_up_to_31_entries_stay_sign_extended(shape):
+def test_ternary_factors_up_to_31_entries_stay_sign_extended():
     """The thread-per-walk ternary kernel keeps factors of 17-31 entries as 32-bit words standing
     for sext(word): the reference's random split sign-extends its second 16-bit chunk, naive
-    factors leave bits 31-63 clear, and xor / and keep the property.  Walks with many splits
-    (philox lists, the oracle) must keep bits 32-63 of every value and sign equal to bit 31."""
-    n1, n2, n3 = shape
-    b = O.WalkBatch(16, n1 * n2 * n3 + 8, "zt")
-    O.init_naive(b, n1, n2, n3)
-    O.walk(b, b.cfg("philox", iterations=400, plus_iterations=60, launches=3, expand_p=40.0, seed=5))
+    factors leave bits 31-63 clear, and xor / and keep the property.  From a 2x2x10 scheme below
+    the naive rank (so that factors of 20 entries are split), the oracle's walk keeps bits 32-63
+    of every value and sign equal to bit 31 after every launch, and every scheme exact."""
+    (n1, n2, n3), terms = strassen_blocks(5)
+    S, cap, m = 16, 48, len(terms)
+    b = O.WalkBatch(S, cap, "zt")
+    b.n[:] = (n1, n2, n3)
+    b.m[:] = m
+    for t, tri in enumerate(terms):
+        for c, d in enumerate(tri):
+            for e, x in d.items():
+                b.fac[:, c, t] |= np.uint64(1 << e)
+                if x < 0:
+                    b.sgn[:, c, t] |= np.uint64(1 << e)
+    b.valid[:, :, :m] = 1
+    b.best_fac[:] = b.fac
+    b.best_sgn[:] = b.sgn
+    b.best_valid[:] = b.valid
+    b.best_rank[:] = m
+    b.best_m[:] = m
     assert O.validate(b).all()
-    for w in range(b.S):
-        m = int(b.m[w])
-        for arr in (b.fac[w, :, :m], b.sgn[w, :, :m]):
-            hi = arr >> np.uint64(31)
-            assert np.isin(hi, [0, (1 << 33) - 1]).all()
-    nn = [n1 * n2, n2 * n3, n3 * n1]
-    wide = [c for c in range(3) if nn[c] > 16]
-    # some split drew a second chunk: entries at or above the factor's size are set
-    assert any((b.fac[:, c, :] >> np.uint64(nn[c]) != 0).any() for c in wide)
+    ranks = set()
+    for launch in range(4):
+        O.walk(b, b.cfg("philox", iterations=500, plus_iterations=60, launches=1, expand_p=200.0, seed=5 + launch))
+        assert O.validate(b).all() and not b.status.any()
+        for arr in (b.fac, b.sgn, b.best_fac, b.best_sgn):
+            assert np.isin(arr >> np.uint64(31), [0, (1 << 33) - 1]).all()
+        ranks.update(int(x) for x in b.m)
+    assert len(ranks) > 1  # the walks left the starting rank: splits and merges ran
