@@ -153,7 +153,7 @@ def xorwow_tape_for(rec, seed):
     ((2, 2, 3), 64, 600, 50, 10.0, 0.0),
     ((2, 3, 3), 32, 600, 100, 0.01, 20.0),
     ((4, 4, 4), 16, 150, 100, 0.01, 0.0),
-    ((2, 4, 5), 16, 300, 100, 2.0, 0.0),   # nn = 8 x 20 x 10: sign-extended random splits
+    ((2, 4, 5), 16, 300, 100, 2.0, 0.0),   # nn = 8 x 20 x 10: factors of more than 16 entries
 ])
 @pytest.mark.parametrize("list_kernel", ["warp", "thread"])
 def test_zt_walk_reference_stream_vs_oracle(shape, S, iters, plus, expand_p, reduce_p, list_kernel):
